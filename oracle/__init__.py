@@ -1,0 +1,200 @@
+"""CPU oracle for the TreeSPH force path (test infrastructure only).
+
+Loads oracle/_build/liboracle.so (the C restatement of the reference's
+algorithm in tsph_oracle.c) and, where it has been built in this checkout,
+oracle/_ref/libgasref.so (the reference's own sources compiled by
+build_ref.sh).  Only tests/, __graft_entry__.smoke() and bench.py's CPU
+baseline leg use this package, as the checker; the product never does.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = os.path.join(HERE, "_build", "liboracle.so")
+_REF = os.path.join(HERE, "_ref", "libgasref.so")
+
+_P = ctypes.POINTER(ctypes.c_double)
+_IP = ctypes.POINTER(ctypes.c_int)
+_UP = ctypes.POINTER(ctypes.c_ulonglong)
+
+
+class GravParams(ctypes.Structure):
+    """Same field order as orc_grav_params / the reference harness."""
+    _fields_ = [("nBucket", ctypes.c_int), ("iOrder", ctypes.c_int),
+                ("bPeriodic", ctypes.c_int), ("bEwald", ctypes.c_int),
+                ("iEwOrder", ctypes.c_int), ("nReps", ctypes.c_int),
+                ("dTheta", ctypes.c_double), ("dPeriod", ctypes.c_double),
+                ("fEwCut", ctypes.c_double), ("fEwhCut", ctypes.c_double)]
+
+
+class SphParams(ctypes.Structure):
+    _fields_ = [("nSmooth", ctypes.c_int), ("bPeriodic", ctypes.c_int),
+                ("dPeriod", ctypes.c_double), ("alpha", ctypes.c_double),
+                ("beta", ctypes.c_double), ("gamma", ctypes.c_double),
+                ("dEtaCourant", ctypes.c_double), ("nBucket", ctypes.c_int),
+                ("iViscosityLimiter", ctypes.c_int)]
+
+
+def grav_params(nBucket=8, iOrder=2, periodic=False, ewald=True, iEwOrder=4,
+                nReps=1, theta=0.7, L=1.0, fEwCut=2.6, fEwhCut=2.8):
+    return GravParams(nBucket, iOrder, int(periodic), int(ewald), iEwOrder,
+                      nReps, theta, L, fEwCut, fEwhCut)
+
+
+def sph_params(nSmooth=32, periodic=False, L=1.0, alpha=1.0, beta=2.0,
+               gamma=5.0 / 3.0, dEtaCourant=0.4, nBucket=8, limiter=1):
+    return SphParams(nSmooth, int(periodic), L, alpha, beta, gamma,
+                     dEtaCourant, nBucket, limiter)
+
+
+SPH_FIELDS = ["fBall2", "fDensity", "divv", "curlv_x", "curlv_y", "curlv_z",
+              "dvds", "BalsaraSwitch", "diff", "PoverRho2", "c", "ax", "ay",
+              "az", "uDotPdV", "uDotAV"]
+
+
+def build():
+    subprocess.check_call(["sh", os.path.join(HERE, "build_oracle.sh")])
+
+
+def reference_available():
+    return os.path.exists(_REF)
+
+
+def build_reference(refdir="/root/reference"):
+    subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh"), refdir])
+
+
+def _d(a):
+    return a.ctypes.data_as(_P)
+
+
+def _c64(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a if shape is None else a.reshape(shape)
+
+
+class _Impl:
+    def __init__(self, path, prefix):
+        self.lib = ctypes.CDLL(path)
+        self.prefix = prefix
+        self.lib[prefix + "grav"].restype = ctypes.c_int
+        self.lib[prefix + "tree"].restype = ctypes.c_int
+        self.lib[prefix + "lists"].restype = ctypes.c_int
+        self.lib[prefix + "sph"].restype = ctypes.c_int
+
+    def grav(self, pos, mass, soft, gp, nthreads=1):
+        pos = _c64(pos, (-1, 3)); mass = _c64(mass); soft = _c64(soft)
+        n = len(mass)
+        acc = np.zeros((n, 3)); pot = np.zeros(n); dtg = np.zeros(n)
+        cnt = np.zeros(5)
+        f = self.lib[self.prefix + "grav"]
+        if self.prefix == "orc_":
+            f(n, _d(pos), _d(mass), _d(soft), ctypes.byref(gp), _d(acc), _d(pot),
+              _d(dtg), _d(cnt), ctypes.c_int(nthreads))
+        else:
+            f(n, _d(pos), _d(mass), _d(soft), ctypes.byref(gp), _d(acc), _d(pot),
+              _d(dtg), _d(cnt))
+        return dict(acc=acc, pot=pot, dtGrav=dtg, counters=cnt)
+
+    def tree(self, pos, mass, soft, gp):
+        pos = _c64(pos, (-1, 3)); mass = _c64(mass); soft = _c64(soft)
+        n = len(mass)
+        f = self.lib[self.prefix + "tree"]
+        nn = f(n, _d(pos), _d(mass), _d(soft), ctypes.byref(gp), None, None, None)
+        inode = np.zeros((nn, 6), dtype=np.int32)
+        dnode = np.zeros((nn, 16))
+        perm = np.zeros(n, dtype=np.int32)
+        f(n, _d(pos), _d(mass), _d(soft), ctypes.byref(gp),
+          inode.ctypes.data_as(_IP), _d(dnode), perm.ctypes.data_as(_IP))
+        return inode, dnode, perm
+
+    def lists(self, pos, mass, soft, gp):
+        pos = _c64(pos, (-1, 3)); mass = _c64(mass); soft = _c64(soft)
+        n = len(mass)
+        f = self.lib[self.prefix + "lists"]
+        nb = f(n, _d(pos), _d(mass), _d(soft), ctypes.byref(gp), None)
+        bl = np.zeros((nb, 4), dtype=np.int32)
+        f(n, _d(pos), _d(mass), _d(soft), ctypes.byref(gp), bl.ctypes.data_as(_IP))
+        return bl
+
+    def sph(self, pos, vel, mass, soft, u, sp, nthreads=1):
+        pos = _c64(pos, (-1, 3)); vel = _c64(vel, (-1, 3)); mass = _c64(mass)
+        soft = _c64(soft); u = _c64(u)
+        n = len(mass)
+        out = np.zeros((n, 16)); dtn = np.zeros(n); mum = np.zeros(n)
+        f = self.lib[self.prefix + "sph"]
+        res = dict()
+        if self.prefix == "orc_":
+            cnt = np.zeros(n, dtype=np.int32)
+            hsh = np.zeros(n, dtype=np.uint64)
+            f(n, _d(pos), _d(vel), _d(mass), _d(soft), _d(u), ctypes.byref(sp),
+              _d(out), _d(dtn), _d(mum), cnt.ctypes.data_as(_IP),
+              hsh.ctypes.data_as(_UP), ctypes.c_int(nthreads))
+            res["nbr_count"] = cnt
+            res["nbr_hash"] = hsh
+        else:
+            f(n, _d(pos), _d(vel), _d(mass), _d(soft), _d(u), ctypes.byref(sp),
+              _d(out), _d(dtn), _d(mum))
+        for k, name in enumerate(SPH_FIELDS):
+            res[name] = out[:, k].copy()
+        res["dtNew"] = dtn
+        res["mumax"] = mum
+        return res
+
+
+_oracle = None
+_ref = None
+
+
+def oracle():
+    """The C restatement (always available once built)."""
+    global _oracle
+    if _oracle is None:
+        if not os.path.exists(_LIB):
+            build()
+        _oracle = _Impl(_LIB, "orc_")
+        _oracle.lib.orc_knn.restype = ctypes.c_int
+    return _oracle
+
+
+def reference():
+    """The reference's own code, or None where it was not built."""
+    global _ref
+    if _ref is None and os.path.exists(_REF):
+        _ref = _Impl(_REF, "ref_")
+    return _ref
+
+
+def knn_fball2(pos, nsmooth, periodic=False, L=1.0, nthreads=1):
+    pos = _c64(pos, (-1, 3))
+    n = pos.shape[0]
+    out = np.zeros(n)
+    oracle().lib.orc_knn(n, _d(pos), nsmooth, int(periodic), ctypes.c_double(L),
+                         _d(out), nthreads)
+    return out
+
+
+def v_sqrt1(r2):
+    r2 = _c64(r2)
+    out = np.zeros_like(r2)
+    oracle().lib.orc_v_sqrt1(len(r2), _d(r2), _d(out))
+    return out
+
+
+def kdk(which, dt, pos, vel, acc, ngas=0, u=None, udot=None, periodic=False,
+        L=1.0):
+    """In-place KDK half step on float64 arrays (see orc_kdk)."""
+    n = pos.shape[0]
+    vpred = np.zeros_like(vel)
+    upred = np.zeros(n) if u is not None else None
+    lib = oracle().lib
+    nul = ctypes.cast(None, _P)
+    lib.orc_kdk(n, which, ctypes.c_double(dt), int(periodic), ctypes.c_double(L),
+                _d(pos), _d(vel), _d(acc), ngas,
+                _d(u) if u is not None else nul,
+                _d(udot) if udot is not None else nul,
+                _d(vpred), _d(upred) if upred is not None else nul)
+    return vpred, upred

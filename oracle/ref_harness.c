@@ -1,0 +1,352 @@
+/*
+ * Harness around the UNMODIFIED reference sources (gasoline pkd.c, walk.c,
+ * grav.c, ewald.c, v_sqrt1.c, smooth.c, smoothfcn.c), compiled from where
+ * they lie by oracle/build_ref.sh into oracle/_ref/libgasref.so.
+ *
+ * TEST INFRASTRUCTURE ONLY.  It is used in this container to pin the C
+ * restatement in oracle/tsph_oracle.c and to write golden fixtures under
+ * tests/golden/.  Nothing in the product links or calls it.
+ *
+ * It reproduces, for a single rank, what the reference's master/PST layers
+ * do around the per-rank kernels:
+ *   msrBuildTree (master.c:4249-4308): pkdBuildBinary, a one-cell top tree
+ *     (pstColCells pst.c:3924-3929 with pLower = rank id 0), pkdCalcRoot +
+ *     pkdDistribRoot for Ewald;
+ *   msrGravity -> pstGravity -> pkdGravAll (pst.c:3310-3315);
+ *   msrSph (master.c:9258-9362): pkdBuildLocal, smSmooth(SMX_DENDVDX),
+ *     pkdGasPressure, smReSmooth(SMX_SPHPRESSURETERMS).
+ * Inputs and outputs are SoA arrays indexed by iOrder (input order).
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <math.h>
+#include <float.h>
+#include "pkd.h"
+#include "walk.h"
+#include "grav.h"
+#include "ewald.h"
+#include "smooth.h"
+#include "smoothfcn.h"
+#include "opentype.h"
+
+typedef struct {
+    int nBucket;
+    int iOrder;        /* multipole order of cell interactions (2 = quadrupole) */
+    int bPeriodic;
+    int bEwald;
+    int iEwOrder;
+    int nReps;
+    double dTheta;
+    double dPeriod;
+    double fEwCut;
+    double fEwhCut;
+} ref_grav_params;
+
+static struct mdlContext g_mdl;
+
+static PKD make_pkd(int n, const double *pos, const double *mass,
+                    const double *soft, int bPeriodic, double dPeriod,
+                    int iOrder, int bGas)
+{
+    PKD pkd;
+    FLOAT fPeriod[3];
+    int i, j;
+    memset(&g_mdl, 0, sizeof(g_mdl));
+    g_mdl.idSelf = 0;
+    g_mdl.nThreads = 1;
+    for (j = 0; j < 3; ++j) fPeriod[j] = bPeriodic ? dPeriod : FLOAT_MAXVAL;
+    pkdInitialize(&pkd, &g_mdl, iOrder, n, 0, fPeriod, 0.0, 0.0,
+                  bGas ? 0 : n, bGas ? n : 0, 0);
+    pkd->nLocal = n;
+    pkd->nActive = n;
+    pkd->nTreeActive = n;
+    pkd->nSmoothActive = n;
+    for (i = 0; i < n; ++i) {
+        PARTICLE *p = &pkd->pStore[i];
+        memset(p, 0, sizeof(*p));
+        p->iOrder = i;
+        p->iActive = TYPE_ACTIVE | TYPE_TREEACTIVE | TYPE_SMOOTHACTIVE |
+                     (bGas ? TYPE_GAS : TYPE_DARK);
+        p->fMass = mass[i];
+        p->fSoft = soft[i];
+        p->fSoft0 = soft[i];
+        for (j = 0; j < 3; ++j) p->r[j] = pos[3 * i + j];
+        p->fBall2 = 0.0;
+        p->fBallMax = 0.0;
+        p->dt = FLT_MAX;
+        p->dtGrav = 0.0;
+    }
+    return pkd;
+}
+
+/* One-rank top tree: kdTop[ROOT] is the local root with pLower = rank 0. */
+static void make_top(PKD pkd, KDN *pRoot)
+{
+    pkd->kdTop = malloc(2 * sizeof(KDN));
+    pkd->piLeaf = malloc(sizeof(int));
+    memset(pkd->kdTop, 0, 2 * sizeof(KDN));
+    pkd->kdTop[ROOT] = *pRoot;
+    pkd->kdTop[ROOT].pLower = 0;
+    if (pkd->kdTop[ROOT].pUpper < 0) pkd->kdTop[ROOT].pUpper = -1;
+    pkd->kdTop[ROOT].iLower = -1;
+    pkd->kdTop[ROOT].iUpper = -1;
+    pkd->piLeaf[0] = ROOT;
+}
+
+static void build_grav_tree(PKD pkd, const ref_grav_params *gp)
+{
+    KDN root;
+    struct ilCellNewt rootmom;
+    int iOrderTree = gp->iOrder;
+    if (gp->bPeriodic && gp->bEwald && gp->iEwOrder > iOrderTree)
+        iOrderTree = gp->iEwOrder;
+    pkdBuildBinary(pkd, gp->nBucket, OPEN_JOSH, gp->dTheta, iOrderTree,
+                   0, 1, &root);
+    make_top(pkd, &root);
+    pkdCalcRoot(pkd, &rootmom);
+    pkdDistribRoot(pkd, &rootmom);
+}
+
+/*
+ * Gravity: one pkdGravAll over all particles.  Outputs a[3n], pot[n],
+ * dtGrav[n] (by iOrder), counters[5] = nActive, dPartSum, dCellSum,
+ * dSoftSum, dFlop.  Returns the number of tree nodes.
+ */
+int ref_grav(int n, const double *pos, const double *mass, const double *soft,
+             const ref_grav_params *gp, double *acc, double *pot,
+             double *dtGrav, double *counters)
+{
+    PKD pkd = make_pkd(n, pos, mass, soft, gp->bPeriodic, gp->dPeriod,
+                       gp->iOrder, 0);
+    int nActive = 0, i, j, nNodes;
+    double dPartSum, dCellSum, dSoftSum, dFlop;
+    CASTAT cs;
+    double aSun[3] = {0, 0, 0};
+    build_grav_tree(pkd, gp);
+    for (i = 0; i < n; ++i) {
+        PARTICLE *p = &pkd->pStore[i];
+        for (j = 0; j < 3; ++j) p->a[j] = 0.0;
+        p->fPot = 0.0;
+        p->dtGrav = 0.0;
+    }
+    pkdGravAll(pkd, gp->bPeriodic ? gp->nReps : 0, gp->bPeriodic, gp->iOrder,
+               gp->bEwald, gp->iEwOrder, gp->fEwCut, gp->fEwhCut, 0, 0.0, 0,
+               0.0, aSun, &nActive, &dPartSum, &dCellSum, &dSoftSum, &cs,
+               &dFlop);
+    for (i = 0; i < n; ++i) {
+        PARTICLE *p = &pkd->pStore[i];
+        int k = p->iOrder;
+        for (j = 0; j < 3; ++j) acc[3 * k + j] = p->a[j];
+        pot[k] = p->fPot;
+        dtGrav[k] = p->dtGrav;
+    }
+    counters[0] = nActive;
+    counters[1] = dPartSum;
+    counters[2] = dCellSum;
+    counters[3] = dSoftSum;
+    counters[4] = dFlop;
+    nNodes = pkd->nNodes;
+    pkdFinish(pkd);
+    return nNodes;
+}
+
+/*
+ * Tree export for cell-membership parity.  Writes, for every node in the
+ * reference's own node order (depth-first, pkd.c:2452-2453):
+ *   inode[6*i+..] = pLower, pUpper, iDim, iLower, iUpper (threaded), 0
+ *   dnode[16*i+..] = fSplit, bnd.fMin[3], bnd.fMax[3], fMass, fSoft, r[3],
+ *                    fOpen2, Bmax, Qxx, Qyy
+ * and perm[pos] = iOrder of the particle at storage position pos.
+ * Returns the node count (call with inode == NULL to size buffers).
+ */
+int ref_tree(int n, const double *pos, const double *mass, const double *soft,
+             const ref_grav_params *gp, int *inode, double *dnode, int *perm)
+{
+    PKD pkd = make_pkd(n, pos, mass, soft, gp->bPeriodic, gp->dPeriod,
+                       gp->iOrder, 0);
+    int i, j, nNodes;
+    build_grav_tree(pkd, gp);
+    nNodes = pkd->nNodes;
+    if (inode) {
+        for (i = 0; i < nNodes; ++i) {
+            KDN *c = &pkd->kdNodes[i];
+            inode[6 * i + 0] = c->pLower;
+            inode[6 * i + 1] = c->pUpper;
+            inode[6 * i + 2] = c->iDim;
+            inode[6 * i + 3] = c->iLower;
+            inode[6 * i + 4] = c->iUpper;
+            inode[6 * i + 5] = 0;
+            dnode[16 * i + 0] = c->fSplit;
+            for (j = 0; j < 3; ++j) {
+                dnode[16 * i + 1 + j] = c->bnd.fMin[j];
+                dnode[16 * i + 4 + j] = c->bnd.fMax[j];
+                dnode[16 * i + 9 + j] = c->r[j];
+            }
+            dnode[16 * i + 7] = c->fMass;
+            dnode[16 * i + 8] = c->fSoft;
+            dnode[16 * i + 12] = c->fOpen2;
+            dnode[16 * i + 13] = c->mom.Bmax;
+            dnode[16 * i + 14] = c->mom.Qxx;
+            dnode[16 * i + 15] = c->mom.Qyy;
+        }
+        for (i = 0; i < n; ++i) perm[i] = pkd->pStore[i].iOrder;
+    }
+    pkdFinish(pkd);
+    return nNodes;
+}
+
+/*
+ * Interaction-list lengths per bucket, walked exactly as pkdGravAll does
+ * (active-bound swap pkd.c:2917-2944, then pkdBucketWalk).  For each
+ * bucket b in threaded-walk order: blist[4*b+..] = node index, nPart,
+ * nCellSoft, nCellNewt.  Returns the number of buckets.
+ */
+int ref_lists(int n, const double *pos, const double *mass, const double *soft,
+              const ref_grav_params *gp, int *blist)
+{
+    PKD pkd = make_pkd(n, pos, mass, soft, gp->bPeriodic, gp->dPeriod,
+                       gp->iOrder, 0);
+    KDN *c;
+    int iCell, nb = 0, i, j;
+    build_grav_tree(pkd, gp);
+    c = pkd->kdNodes;
+    iCell = pkd->iRoot;
+    while (iCell != -1) {
+        BND bndActive, bndTmp;
+        if (c[iCell].iLower != -1) { iCell = c[iCell].iLower; continue; }
+        for (j = 0; j < 3; ++j) {
+            bndActive.fMin[j] = FLOAT_MAXVAL;
+            bndActive.fMax[j] = -FLOAT_MAXVAL;
+        }
+        for (i = c[iCell].pLower; i <= c[iCell].pUpper; ++i)
+            for (j = 0; j < 3; ++j) {
+                if (pkd->pStore[i].r[j] < bndActive.fMin[j]) bndActive.fMin[j] = pkd->pStore[i].r[j];
+                if (pkd->pStore[i].r[j] > bndActive.fMax[j]) bndActive.fMax[j] = pkd->pStore[i].r[j];
+            }
+        bndTmp = c[iCell].bnd;
+        c[iCell].bnd = bndActive;
+        pkdBucketWalk(pkd, iCell, gp->bPeriodic ? gp->nReps : 0, gp->iOrder);
+        c[iCell].bnd = bndTmp;
+        if (blist) {
+            blist[4 * nb + 0] = iCell;
+            blist[4 * nb + 1] = pkd->nPart;
+            blist[4 * nb + 2] = pkd->nCellSoft;
+            blist[4 * nb + 3] = pkd->nCellNewt;
+        }
+        ++nb;
+        iCell = c[iCell].iUpper;
+    }
+    pkdFinish(pkd);
+    return nb;
+}
+
+typedef struct {
+    int nSmooth;
+    int bPeriodic;
+    double dPeriod;
+    double alpha;
+    double beta;
+    double gamma;
+    double dEtaCourant;
+    int nBucket;
+    int iViscosityLimiter;
+} ref_sph_params;
+
+/*
+ * SPH force pass as in msrSph for the all-active case (master.c:9308-9353):
+ * density tree, smSmooth(SMX_DENDVDX, symmetric), pkdGasPressure,
+ * smReSmooth(SMX_SPHPRESSURETERMS, symmetric).  Inputs: pos, vel (=vPred),
+ * mass, soft, u (=uPred).  Outputs (by iOrder):
+ *   out[16*i+..] = fBall2, fDensity, divv, curlv[3], dvds, BalsaraSwitch,
+ *                  diff, PoverRho2, c, a_hydro[3], uDotPdV, uDotAV
+ *   dtNew[i], mumax[i].
+ */
+int ref_sph(int n, const double *pos, const double *vel, const double *mass,
+            const double *soft, const double *u, const ref_sph_params *sp,
+            double *out, double *dtNew, double *mumax)
+{
+    PKD pkd = make_pkd(n, pos, mass, soft, sp->bPeriodic, sp->dPeriod, 2, 1);
+    KDN root;
+    SMX smx;
+    SMF smf;
+    CASTAT cs;
+    struct GasPressureContext gpc;
+    int i, j;
+    for (i = 0; i < n; ++i) {
+        PARTICLE *p = &pkd->pStore[i];
+        for (j = 0; j < 3; ++j) {
+            p->v[j] = vel[3 * i + j];
+            p->vPred[j] = vel[3 * i + j];
+        }
+        p->u = u[i];
+        p->uPred = u[i];
+    }
+    memset(&smf, 0, sizeof(smf));
+    smf.H = 0.0;
+    smf.a = 1.0;
+    smf.alpha = sp->alpha;
+    smf.beta = sp->beta;
+    smf.gamma = sp->gamma;
+    smf.algam = smf.alpha * sqrt(smf.gamma * (smf.gamma - 1));
+    smf.iViscosityLimiter = sp->iViscosityLimiter;
+    smf.dtFacCourant = pkdDtFacCourant(sp->dEtaCourant, smf.a);
+    smf.dtFacDiffusion = 2 * 0.1;
+    smf.bCannonical = 1;
+    smf.dtMin = FLOAT_MAXVAL;
+    smf.bStepZero = 1;
+
+    /* density tree: msrBuildTree(bTreeActiveOnly=1, bSmooth=1) */
+    pkdBuildLocal(pkd, sp->nBucket, OPEN_JOSH, 0.7, 2, 1, 0, &root);
+    make_top(pkd, &root);
+    smInitialize(&smx, pkd, &smf, sp->nSmooth, sp->bPeriodic, 1, SMX_DENDVDX, 1, 0.0);
+    smSmooth(smx, &smf);
+    smFinish(smx, &smf, &cs);
+
+    memset(&gpc, 0, sizeof(gpc));
+    gpc.iGasModel = GASMODEL_ADIABATIC;
+    gpc.gamma = sp->gamma;
+    gpc.gammam1 = sp->gamma - 1;
+    gpc.dResolveJeans = 0.0;
+    gpc.dCosmoFac = 1.0;
+    gpc.dtFacCourant = smf.dtFacCourant;
+    pkdGasPressure(pkd, &gpc);
+
+    for (i = 0; i < n; ++i) {
+        PARTICLE *p = &pkd->pStore[i];
+        for (j = 0; j < 3; ++j) p->a[j] = 0.0;
+    }
+    smInitialize(&smx, pkd, &smf, sp->nSmooth, sp->bPeriodic, 1, SMX_SPHPRESSURETERMS, 0, 0.0);
+    smReSmooth(smx, &smf);
+    smFinish(smx, &smf, &cs);
+
+    for (i = 0; i < n; ++i) {
+        PARTICLE *p = &pkd->pStore[i];
+        int k = p->iOrder;
+        double *o = &out[16 * k];
+        o[0] = p->fBall2;
+        o[1] = p->fDensity;
+        o[2] = p->divv;
+        o[3] = p->curlv[0];
+        o[4] = p->curlv[1];
+        o[5] = p->curlv[2];
+        o[6] = p->dvds;
+        o[7] = p->BalsaraSwitch;
+        o[8] = p->diff;
+        o[9] = p->PoverRho2;
+        o[10] = p->c;
+        o[11] = p->a[0];
+        o[12] = p->a[1];
+        o[13] = p->a[2];
+        o[14] = p->uDotPdV;
+        o[15] = p->uDotAV;
+        dtNew[k] = p->dtNew;
+        mumax[k] = p->mumax;
+    }
+    pkdFinish(pkd);
+    return 0;
+}
+
+/* The reference's approximate 1/sqrt (v_sqrt1.c:11), exported for tests. */
+void v_sqrt1(int, double *, double *);
+void ref_v_sqrt1(int n, double *r2, double *a) { v_sqrt1(n, r2, a); }
