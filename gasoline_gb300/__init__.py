@@ -1,0 +1,266 @@
+"""gasoline_gb300: GB300-native TreeSPH force path (gravity tree walk with
+Ewald, SPH density and pressure gathers, kick-drift-kick) behind the C ABI
+declared in include/tsph.h.
+
+This module is a thin ctypes binding of libtsph for tests, the benchmark
+and Python callers.  It mirrors the reference's per-rank entry points:
+``Context.grav_all`` is pkdGravAll (pkd.c:2869) including the tree build it
+needs, ``Context.smooth`` is smInitialize+smSmooth/smReSmooth+smFinish
+(smooth.c:54-1749) for SMX_DENDVDX and SMX_SPHPRESSURETERMS.
+
+There is no CPU fallback: if libtsph is missing or no GPU is present the
+calls raise.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import ics  # noqa: F401  (re-exported workload generators)
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIBPATH = os.path.join(HERE, "_lib", "libtsph.so")
+
+FP64 = 0
+FP32 = 1
+SMX_DENSITY = 1
+SMX_SPHPRESSURETERMS = 22
+SMX_DENDVDX = 23
+
+_P = ctypes.POINTER(ctypes.c_double)
+_IP = ctypes.POINTER(ctypes.c_int)
+_UP = ctypes.POINTER(ctypes.c_ulonglong)
+
+
+class GravParams(ctypes.Structure):
+    """tsph_grav_params (include/tsph.h)."""
+    _fields_ = [("nBucket", ctypes.c_int), ("iOrder", ctypes.c_int),
+                ("bPeriodic", ctypes.c_int), ("bEwald", ctypes.c_int),
+                ("iEwOrder", ctypes.c_int), ("nReps", ctypes.c_int),
+                ("dTheta", ctypes.c_double), ("dPeriod", ctypes.c_double),
+                ("fEwCut", ctypes.c_double), ("fEwhCut", ctypes.c_double),
+                ("precision", ctypes.c_int), ("reserved", ctypes.c_int)]
+
+
+class GravOut(ctypes.Structure):
+    _fields_ = [("nActive", ctypes.c_int), ("nBuckets", ctypes.c_int),
+                ("dPartSum", ctypes.c_double), ("dCellSum", ctypes.c_double),
+                ("dSoftSum", ctypes.c_double), ("dFlop", ctypes.c_double),
+                ("dFlopEwald", ctypes.c_double), ("dExactFrac", ctypes.c_double)]
+
+
+class SphParams(ctypes.Structure):
+    _fields_ = [("nSmooth", ctypes.c_int), ("bPeriodic", ctypes.c_int),
+                ("dPeriod", ctypes.c_double), ("alpha", ctypes.c_double),
+                ("beta", ctypes.c_double), ("gamma", ctypes.c_double),
+                ("dEtaCourant", ctypes.c_double),
+                ("iViscosityLimiter", ctypes.c_int), ("precision", ctypes.c_int),
+                ("bLearnedH", ctypes.c_int), ("reserved", ctypes.c_int)]
+
+
+class SmoothOut(ctypes.Structure):
+    _fields_ = [("nSmoothed", ctypes.c_int), ("nFallback", ctypes.c_int),
+                ("dPairs", ctypes.c_double)]
+
+
+def grav_params(nBucket=8, iOrder=2, periodic=False, ewald=True, iEwOrder=4,
+                nReps=1, theta=0.7, L=1.0, fEwCut=2.6, fEwhCut=2.8,
+                precision=FP64):
+    return GravParams(nBucket, iOrder, int(periodic), int(ewald), iEwOrder,
+                      nReps, theta, L, fEwCut, fEwhCut, precision, 0)
+
+
+def sph_params(nSmooth=32, periodic=False, L=1.0, alpha=1.0, beta=2.0,
+               gamma=5.0 / 3.0, dEtaCourant=0.4, limiter=1, precision=FP64,
+               learned_h=False):
+    return SphParams(nSmooth, int(periodic), L, alpha, beta, gamma,
+                     dEtaCourant, limiter, precision, int(learned_h), 0)
+
+
+class TsphError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"libtsph error {code}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def load():
+    """Load libtsph; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIBPATH):
+        raise RuntimeError(
+            f"{LIBPATH} not built: run `python -m gasoline_gb300.build`")
+    lib = ctypes.CDLL(LIBPATH)
+    lib.tsph_error_string.restype = ctypes.c_char_p
+    lib.tsph_last_cuda_error.restype = ctypes.c_char_p
+    lib.tsph_launch_count.restype = ctypes.c_longlong
+    for name in ("tsph_create", "tsph_set_particles", "tsph_set_velocities",
+                 "tsph_grav_all", "tsph_get_gravity", "tsph_get_tree",
+                 "tsph_get_lists", "tsph_smooth", "tsph_get_sph",
+                 "tsph_get_neighbour_hash", "tsph_kick", "tsph_drift",
+                 "tsph_get_state", "tsph_get_timings"):
+        getattr(lib, name).restype = ctypes.c_int
+    lib.tsph_destroy.restype = None
+    _lib = lib
+    return lib
+
+
+def _d(a):
+    return a.ctypes.data_as(_P)
+
+
+def _c64(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a if shape is None else a.reshape(shape)
+
+
+class Context:
+    """One libtsph context (one GPU, one stream)."""
+
+    def __init__(self, device=0, stream=None):
+        self.lib = load()
+        self._ctx = ctypes.c_void_p()
+        s = ctypes.c_void_p(stream) if stream else None
+        self._check(self.lib.tsph_create(ctypes.byref(self._ctx), device, s))
+        self.n = 0
+        self.ngas = 0
+
+    def close(self):
+        if self._ctx:
+            self.lib.tsph_destroy(self._ctx)
+            self._ctx = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != 0:
+            msg = self.lib.tsph_error_string(rc).decode()
+            if self._ctx:
+                cu = self.lib.tsph_last_cuda_error(self._ctx).decode()
+                if cu:
+                    msg += f" ({cu})"
+            raise TsphError(rc, msg)
+
+    # ---- particles ------------------------------------------------------
+    def set_particles(self, pos, mass, soft):
+        pos = _c64(pos, (-1, 3))
+        mass = _c64(mass)
+        soft = _c64(soft)
+        self.n = len(mass)
+        self._check(self.lib.tsph_set_particles(
+            self._ctx, self.n, _d(pos), _d(mass), _d(soft)))
+
+    def set_particles_ptr(self, n, pos_ptr, mass_ptr, soft_ptr):
+        """Same as set_particles from raw host pointers (e.g. pinned)."""
+        self.n = n
+        self._check(self.lib.tsph_set_particles(
+            self._ctx, n, ctypes.cast(pos_ptr, _P), ctypes.cast(mass_ptr, _P),
+            ctypes.cast(soft_ptr, _P)))
+
+    def set_velocities(self, vel, ngas=0, u=None):
+        vel = _c64(vel, (-1, 3))
+        self.ngas = ngas
+        up = _d(_c64(u)) if u is not None else None
+        if u is not None:
+            self._u_keep = _c64(u)
+            up = _d(self._u_keep)
+        self._check(self.lib.tsph_set_velocities(self._ctx, _d(vel), ngas, up))
+
+    # ---- gravity ----------------------------------------------------------
+    def grav_all(self, gp):
+        out = GravOut()
+        self._check(self.lib.tsph_grav_all(self._ctx, ctypes.byref(gp),
+                                           ctypes.byref(out)))
+        return {f: getattr(out, f) for f, _ in GravOut._fields_}
+
+    def get_gravity(self):
+        acc = np.zeros((self.n, 3))
+        pot = np.zeros(self.n)
+        dtg = np.zeros(self.n)
+        self._check(self.lib.tsph_get_gravity(self._ctx, _d(acc), _d(pot),
+                                              _d(dtg)))
+        return dict(acc=acc, pot=pot, dtGrav=dtg)
+
+    def get_gravity_ptr(self, acc_ptr):
+        self._check(self.lib.tsph_get_gravity(
+            self._ctx, ctypes.cast(acc_ptr, _P), None, None))
+
+    def get_tree(self):
+        nn = ctypes.c_int()
+        self._check(self.lib.tsph_get_tree(self._ctx, ctypes.byref(nn), None,
+                                           None, None))
+        inode = np.zeros((nn.value, 6), dtype=np.int32)
+        dnode = np.zeros((nn.value, 16))
+        perm = np.zeros(self.n, dtype=np.int32)
+        self._check(self.lib.tsph_get_tree(
+            self._ctx, ctypes.byref(nn), inode.ctypes.data_as(_IP), _d(dnode),
+            perm.ctypes.data_as(_IP)))
+        return inode, dnode, perm
+
+    def get_lists(self):
+        nb = ctypes.c_int()
+        self._check(self.lib.tsph_get_lists(self._ctx, ctypes.byref(nb), None))
+        bl = np.zeros((nb.value, 4), dtype=np.int32)
+        self._check(self.lib.tsph_get_lists(self._ctx, ctypes.byref(nb),
+                                            bl.ctypes.data_as(_IP)))
+        return bl
+
+    # ---- SPH ----------------------------------------------------------------
+    def smooth(self, smx_type, sp):
+        out = SmoothOut()
+        self._check(self.lib.tsph_smooth(self._ctx, smx_type, ctypes.byref(sp),
+                                         ctypes.byref(out)))
+        return {f: getattr(out, f) for f, _ in SmoothOut._fields_}
+
+    def get_sph(self):
+        out = np.zeros((self.ngas, 16))
+        dtn = np.zeros(self.ngas)
+        mum = np.zeros(self.ngas)
+        self._check(self.lib.tsph_get_sph(self._ctx, _d(out), _d(dtn), _d(mum)))
+        names = ["fBall2", "fDensity", "divv", "curlv_x", "curlv_y",
+                 "curlv_z", "dvds", "BalsaraSwitch", "diff", "PoverRho2", "c",
+                 "ax", "ay", "az", "uDotPdV", "uDotAV"]
+        res = {k: out[:, i].copy() for i, k in enumerate(names)}
+        res["dtNew"] = dtn
+        res["mumax"] = mum
+        return res
+
+    def get_neighbour_hash(self):
+        cnt = np.zeros(self.ngas, dtype=np.int32)
+        hsh = np.zeros(self.ngas, dtype=np.uint64)
+        self._check(self.lib.tsph_get_neighbour_hash(
+            self._ctx, cnt.ctypes.data_as(_IP), hsh.ctypes.data_as(_UP)))
+        return cnt, hsh
+
+    # ---- KDK ----------------------------------------------------------------
+    def kick(self, dt):
+        self._check(self.lib.tsph_kick(self._ctx, ctypes.c_double(dt)))
+
+    def drift(self, dt, periodic=False, L=1.0):
+        self._check(self.lib.tsph_drift(self._ctx, ctypes.c_double(dt),
+                                        int(periodic), ctypes.c_double(L)))
+
+    def get_state(self):
+        pos = np.zeros((self.n, 3))
+        vel = np.zeros((self.n, 3))
+        u = np.zeros(max(self.ngas, 1))
+        self._check(self.lib.tsph_get_state(self._ctx, _d(pos), _d(vel), _d(u)))
+        return pos, vel, u[:self.ngas]
+
+    def timings(self):
+        t = (ctypes.c_float * 8)()
+        self._check(self.lib.tsph_get_timings(self._ctx, t))
+        keys = ["build", "moments", "walk", "ewald", "knn", "density",
+                "pressure", "total"]
+        return {k: float(t[i]) for i, k in enumerate(keys)}
+
+    def launches(self):
+        return int(self.lib.tsph_launch_count(self._ctx))

@@ -1,0 +1,452 @@
+// C ABI of libtsph: context management, host<->device transfer in the
+// caller's particle order, and the pkdGravAll-equivalent driver.
+#include <float.h>
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "tsph_ctx.cuh"
+
+int tsph_cuda_fail(tsph_ctx *ctx, cudaError_t e, const char *where) {
+    if (ctx) snprintf(ctx->cudaErr, sizeof(ctx->cudaErr), "%s: %s", where, cudaGetErrorString(e));
+    if (e == cudaErrorMemoryAllocation) return TSPH_ERR_NOMEM;
+    return TSPH_ERR_CUDA;
+}
+
+extern "C" const char *tsph_error_string(int s) {
+    switch (s) {
+    case TSPH_OK: return "ok";
+    case TSPH_ERR_ARG: return "invalid argument";
+    case TSPH_ERR_CUDA: return "CUDA runtime error";
+    case TSPH_ERR_STACK_OVERFLOW: return "tree-walk stack overflow";
+    case TSPH_ERR_LIST_OVERFLOW: return "neighbour list overflow";
+    case TSPH_ERR_KNN_NO_CONVERGE: return "kNN search did not converge";
+    case TSPH_ERR_NONFINITE: return "non-finite particle data";
+    case TSPH_ERR_UNSUPPORTED: return "unsupported option or smooth type";
+    case TSPH_ERR_STATE: return "call out of order";
+    case TSPH_ERR_TREE_DEPTH: return "tree deeper than the level cap";
+    case TSPH_ERR_NOMEM: return "device allocation failed";
+    default: return "unknown status";
+    }
+}
+
+extern "C" const char *tsph_last_cuda_error(tsph_ctx *ctx) { return ctx ? ctx->cudaErr : ""; }
+
+extern "C" int tsph_create(tsph_ctx **pctx, int device, void *stream) {
+    if (!pctx) return TSPH_ERR_ARG;
+    *pctx = nullptr;
+    tsph_ctx *ctx = (tsph_ctx *)calloc(1, sizeof(tsph_ctx));
+    if (!ctx) return TSPH_ERR_NOMEM;
+    ctx->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) { int rc = tsph_cuda_fail(ctx, e, "cudaSetDevice"); free(ctx); return rc; }
+    if (stream) {
+        ctx->stream = (cudaStream_t)stream;
+        ctx->ownStream = false;
+    } else {
+        e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) { int rc = tsph_cuda_fail(ctx, e, "cudaStreamCreate"); free(ctx); return rc; }
+        ctx->ownStream = true;
+    }
+    cudaDeviceGetAttribute(&ctx->smCount, cudaDevAttrMultiProcessorCount, device);
+    if (cudaMalloc((void **)&ctx->dCnt, sizeof(TsphDevCounters)) != cudaSuccess ||
+        cudaMallocHost((void **)&ctx->hCnt, sizeof(TsphDevCounters)) != cudaSuccess ||
+        cudaMallocHost((void **)&ctx->B.hostCount, sizeof(int) * (TSPH_MAX_LEVELS + 16)) != cudaSuccess ||
+        cudaMalloc((void **)&ctx->dRoot, sizeof(double) * (64 + 256 * 32)) != cudaSuccess) {
+        tsph_destroy(ctx);
+        return TSPH_ERR_NOMEM;
+    }
+    for (int k = 0; k < 10; ++k) cudaEventCreate(&ctx->ev[k]);
+    *pctx = ctx;
+    return TSPH_OK;
+}
+
+#define FREE(p) do { if (p) cudaFree(p); (p) = nullptr; } while (0)
+
+extern "C" void tsph_destroy(tsph_ctx *ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    TsphDevState &C = ctx->C;
+    FREE(C.x); FREE(C.y); FREE(C.z); FREE(C.vx); FREE(C.vy); FREE(C.vz); FREE(C.m); FREE(C.h);
+    FREE(C.u); FREE(C.vpx); FREE(C.vpy); FREE(C.vpz); FREE(C.upred); FREE(C.ax); FREE(C.ay);
+    FREE(C.az); FREE(C.pot); FREE(C.dtGrav); FREE(C.hax); FREE(C.hay); FREE(C.haz); FREE(C.udot);
+    TsphDevParts *PP[2] = {&ctx->P, &ctx->G};
+    for (int k = 0; k < 2; ++k) {
+        TsphDevParts &P = *PP[k];
+        FREE(P.x); FREE(P.y); FREE(P.z); FREE(P.m); FREE(P.h); FREE(P.iord);
+        FREE(P.ph); FREE(P.pl); FREE(P.ax); FREE(P.ay); FREE(P.az); FREE(P.pot); FREE(P.dtGrav);
+    }
+    tsph_free_tree(ctx->T);
+    tsph_free_tree(ctx->TG);
+    TsphBuildBufs &B = ctx->B;
+    FREE(B.seg); FREE(B.lt); FREE(B.scan); FREE(B.scanTmp);
+    for (int k = 0; k < 2; ++k) { FREE(B.f_lo[k]); FREE(B.f_hi[k]); FREE(B.f_node[k]); }
+    FREE(B.f_split); FREE(B.f_rank); FREE(B.f_dim); FREE(B.f_m); FREE(B.f_fs); FREE(B.f_bnd);
+    FREE(B.t_lo); FREE(B.t_hi); FREE(B.t_dim); FREE(B.t_child); FREE(B.t_size); FREE(B.t_pre);
+    FREE(B.t_level); FREE(B.t_split); FREE(B.t_bnd); FREE(B.maxd2); FREE(B.leafFlag); FREE(B.leafScan);
+    TsphSphBufs &S = ctx->S;
+    FREE(S.vx); FREE(S.vy); FREE(S.vz); FREE(S.u); FREE(S.fBall2); FREE(S.rho); FREE(S.divv);
+    FREE(S.curl); FREE(S.dvds); FREE(S.bal); FREE(S.diff); FREE(S.pr2); FREE(S.cs); FREE(S.dtp);
+    FREE(S.hax); FREE(S.hay); FREE(S.haz); FREE(S.uPdV); FREE(S.uAV); FREE(S.dtNew); FREE(S.mumax);
+    FREE(S.seed); FREE(S.nnCount); FREE(S.nnHash); FREE(S.nodeBall2);
+    FREE(ctx->dCnt); FREE(ctx->dBucketLists); FREE(ctx->dRoot); FREE(ctx->dEwt); FREE(ctx->dStage);
+    if (ctx->hCnt) cudaFreeHost(ctx->hCnt);
+    if (ctx->B.hostCount) cudaFreeHost(ctx->B.hostCount);
+    for (int k = 0; k < 10; ++k) if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
+    if (ctx->ownStream && ctx->stream) cudaStreamDestroy(ctx->stream);
+    free(ctx);
+}
+
+int tsph_ensure_particles(tsph_ctx *ctx, int n) {
+    if (n <= ctx->cap && ctx->P.x) return TSPH_OK;
+    int cap = n + n / 8 + 1024;
+    int rc = 0;
+    TsphDevParts &P = ctx->P;
+    rc |= tsph_grow(ctx, &P.x, cap); rc |= tsph_grow(ctx, &P.y, cap); rc |= tsph_grow(ctx, &P.z, cap);
+    rc |= tsph_grow(ctx, &P.m, cap); rc |= tsph_grow(ctx, &P.h, cap); rc |= tsph_grow(ctx, &P.iord, cap);
+    rc |= tsph_grow(ctx, &P.ph, cap); rc |= tsph_grow(ctx, &P.pl, cap);
+    rc |= tsph_grow(ctx, &P.ax, cap); rc |= tsph_grow(ctx, &P.ay, cap); rc |= tsph_grow(ctx, &P.az, cap);
+    rc |= tsph_grow(ctx, &P.pot, cap); rc |= tsph_grow(ctx, &P.dtGrav, cap);
+    TsphDevParts &G = ctx->G;
+    rc |= tsph_grow(ctx, &G.x, cap); rc |= tsph_grow(ctx, &G.y, cap); rc |= tsph_grow(ctx, &G.z, cap);
+    rc |= tsph_grow(ctx, &G.m, cap); rc |= tsph_grow(ctx, &G.h, cap); rc |= tsph_grow(ctx, &G.iord, cap);
+    TsphDevState &C = ctx->C;
+    double **cs[] = {&C.x, &C.y, &C.z, &C.vx, &C.vy, &C.vz, &C.m, &C.h, &C.u, &C.vpx, &C.vpy,
+                     &C.vpz, &C.upred, &C.ax, &C.ay, &C.az, &C.pot, &C.dtGrav, &C.hax, &C.hay,
+                     &C.haz, &C.udot};
+    for (auto pp : cs) rc |= tsph_grow(ctx, pp, cap);
+    TsphSphBufs &S = ctx->S;
+    double **ss[] = {&S.vx, &S.vy, &S.vz, &S.u, &S.fBall2, &S.rho, &S.divv, &S.dvds, &S.bal,
+                     &S.diff, &S.pr2, &S.cs, &S.dtp, &S.hax, &S.hay, &S.haz, &S.uPdV, &S.uAV,
+                     &S.dtNew, &S.mumax, &S.seed};
+    for (auto pp : ss) rc |= tsph_grow(ctx, pp, cap);
+    rc |= tsph_grow(ctx, &S.curl, (size_t)3 * cap);
+    rc |= tsph_grow(ctx, &S.nnCount, cap);
+    rc |= tsph_grow(ctx, &S.nnHash, cap);
+    rc |= tsph_grow(ctx, &S.nodeBall2, (size_t)2 * cap + 64);
+    S.cap = cap;
+    TsphBuildBufs &B = ctx->B;
+    rc |= tsph_grow(ctx, &B.seg, cap); rc |= tsph_grow(ctx, &B.lt, cap); rc |= tsph_grow(ctx, &B.scan, cap);
+    rc |= tsph_grow(ctx, &B.scanTmp, cap / 1024 + 4096);
+    for (int k = 0; k < 2; ++k) {
+        rc |= tsph_grow(ctx, &B.f_lo[k], cap); rc |= tsph_grow(ctx, &B.f_hi[k], cap);
+        rc |= tsph_grow(ctx, &B.f_node[k], cap);
+    }
+    rc |= tsph_grow(ctx, &B.f_split, cap); rc |= tsph_grow(ctx, &B.f_rank, cap);
+    rc |= tsph_grow(ctx, &B.f_dim, cap); rc |= tsph_grow(ctx, &B.f_m, cap);
+    rc |= tsph_grow(ctx, &B.f_fs, cap); rc |= tsph_grow(ctx, &B.f_bnd, (size_t)6 * cap);
+    int tcap = 2 * cap + 2;
+    rc |= tsph_grow(ctx, &B.t_lo, tcap); rc |= tsph_grow(ctx, &B.t_hi, tcap);
+    rc |= tsph_grow(ctx, &B.t_dim, tcap); rc |= tsph_grow(ctx, &B.t_child, tcap);
+    rc |= tsph_grow(ctx, &B.t_size, tcap); rc |= tsph_grow(ctx, &B.t_pre, tcap);
+    rc |= tsph_grow(ctx, &B.t_level, tcap); rc |= tsph_grow(ctx, &B.t_split, tcap);
+    rc |= tsph_grow(ctx, &B.t_bnd, (size_t)6 * tcap);
+    rc |= tsph_grow(ctx, &ctx->dStage, (size_t)3 * cap);
+    if (rc) return TSPH_ERR_NOMEM;
+    B.cap = cap;
+    B.nodeCap = tcap;
+    ctx->cap = cap;
+    return TSPH_OK;
+}
+
+__global__ void k_load_state(int n, const double *__restrict__ pos3, TsphDevState C, int *piord,
+                             int *giord) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    C.x[i] = pos3[3 * i];
+    C.y[i] = pos3[3 * i + 1];
+    C.z[i] = pos3[3 * i + 2];
+    C.vx[i] = C.vy[i] = C.vz[i] = 0.0;
+    C.vpx[i] = C.vpy[i] = C.vpz[i] = 0.0;
+    C.u[i] = C.upred[i] = C.udot[i] = 0.0;
+    C.hax[i] = C.hay[i] = C.haz[i] = 0.0;
+    C.ax[i] = C.ay[i] = C.az[i] = C.pot[i] = C.dtGrav[i] = 0.0;
+    piord[i] = i;
+    giord[i] = i;
+}
+
+// tree-order copy of the state, keeping the previous tree permutation
+__global__ void k_gather_tree(int n, TsphDevState C, TsphDevParts P) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int o = P.iord[i];
+    P.x[i] = C.x[o];
+    P.y[i] = C.y[o];
+    P.z[i] = C.z[o];
+    P.m[i] = C.m[o];
+    P.h[i] = C.h[o];
+}
+
+__global__ void k_scatter_grav(int n, TsphDevParts P, TsphDevState C) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int o = P.iord[i];
+    C.ax[o] = P.ax[i];
+    C.ay[o] = P.ay[i];
+    C.az[o] = P.az[i];
+    C.pot[o] = P.pot[i];
+    C.dtGrav[o] = P.dtGrav[i];
+}
+
+__global__ void k_copy_by_order(int n, const double *__restrict__ src, const int *__restrict__ iord,
+                                double *dst) {
+    // dst[tree pos] = src[caller index]
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = src[iord[i]];
+}
+
+__global__ void k_check_finite(int n, TsphDevParts P, unsigned int *status) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double v = P.x[i] + P.y[i] + P.z[i] + P.m[i] + P.h[i];
+    if (!isfinite(v)) atomicOr(status, 1u << TSPH_ERR_NONFINITE);
+}
+
+extern "C" int tsph_set_particles(tsph_ctx *ctx, int n, const double *pos, const double *mass,
+                                  const double *soft) {
+    if (!ctx || n < 0 || (n > 0 && (!pos || !mass || !soft))) return TSPH_ERR_ARG;
+    if (n >= (1 << 27)) return TSPH_ERR_ARG;   // 27-bit particle indices in the walk entries
+    cudaSetDevice(ctx->device);
+    int rc = tsph_ensure_particles(ctx, n > 0 ? n : 1);
+    if (rc) return rc;
+    ctx->n = n;
+    ctx->ngas = 0;
+    ctx->haveTree = ctx->haveGrav = ctx->haveVel = false;
+    ctx->S.haveDensity = false;
+    ctx->P.n = n;
+    ctx->G.n = 0;
+    if (n == 0) { ctx->haveParts = true; return TSPH_OK; }
+    TSPH_CK(cudaMemcpyAsync(ctx->dStage, pos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
+    k_load_state<<<tsph_blocks(n, 256), 256, 0, ctx->stream>>>(n, ctx->dStage, ctx->C, ctx->P.iord,
+                                                               ctx->G.iord);
+    TSPH_LAUNCH_CK("k_load_state");
+    TSPH_CK(cudaMemcpyAsync(ctx->C.m, mass, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    TSPH_CK(cudaMemcpyAsync(ctx->C.h, soft, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    ctx->haveParts = true;
+    return TSPH_OK;
+}
+
+static int read_status(tsph_ctx *ctx) {
+    TSPH_CK(cudaMemcpyAsync(ctx->hCnt, ctx->dCnt, sizeof(TsphDevCounters), cudaMemcpyDeviceToHost,
+                            ctx->stream));
+    TSPH_CK(cudaStreamSynchronize(ctx->stream));
+    unsigned st = ctx->hCnt->status;
+    if (st) {
+        for (int k = 1; k < 32; ++k)
+            if (st & (1u << k)) return k;
+    }
+    return TSPH_OK;
+}
+
+extern "C" int tsph_grav_all(tsph_ctx *ctx, const tsph_grav_params *gp, tsph_grav_out *out) {
+    if (!ctx || !gp) return TSPH_ERR_ARG;
+    if (!ctx->haveParts) return TSPH_ERR_STATE;
+    if (gp->nBucket < 1 || gp->dTheta <= 0 || gp->iOrder < 1 || gp->iOrder > 4) return TSPH_ERR_ARG;
+    if (gp->bPeriodic && !(gp->dPeriod > 0)) return TSPH_ERR_ARG;
+    if (gp->precision != TSPH_FP32 && gp->precision != TSPH_FP64) return TSPH_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    const int n = ctx->n;
+    TSPH_CK(cudaMemsetAsync(ctx->dCnt, 0, sizeof(TsphDevCounters), ctx->stream));
+    cudaEventRecord(ctx->ev[0], ctx->stream);
+    if (n > 0) {
+        k_gather_tree<<<tsph_blocks(n, 256), 256, 0, ctx->stream>>>(n, ctx->C, ctx->P);
+        TSPH_LAUNCH_CK("k_gather_tree");
+        k_check_finite<<<tsph_blocks(n, 256), 256, 0, ctx->stream>>>(n, ctx->P, &ctx->dCnt->status);
+        TSPH_LAUNCH_CK("k_check_finite");
+    }
+    int rc = read_status(ctx);
+    if (rc) return rc;
+    // largest absolute coordinate, for the walk's rounding bound
+    ctx->dPeriodTree = gp->bPeriodic ? gp->dPeriod : 0.0;
+    rc = tsph_build_tree(ctx, ctx->P, ctx->T, n, gp->nBucket);
+    if (rc) return rc;
+    cudaEventRecord(ctx->ev[1], ctx->stream);
+    rc = tsph_tree_moments(ctx, ctx->P, ctx->T, n, gp->dTheta);
+    if (rc) return rc;
+    cudaEventRecord(ctx->ev[2], ctx->stream);
+    ctx->haveTree = true;
+    if (!gp->bPeriodic) {
+        // coordinate scale for the rounding floor: bounds of the root
+        double bnd[6];
+        TSPH_CK(cudaMemcpyAsync(bnd, ctx->T.bnd, sizeof(bnd), cudaMemcpyDeviceToHost, ctx->stream));
+        TSPH_CK(cudaStreamSynchronize(ctx->stream));
+        double r = 0;
+        for (int k = 0; k < 6; ++k) r = fmax(r, fabs(bnd[k]));
+        ctx->dPeriodTree = 2.0 * r;
+    } else {
+        ctx->dPeriodTree = 2.0 * gp->dPeriod;
+    }
+    if (n > 0 && ctx->T.nLeaves > 0) {
+        rc = tsph_walk_interact(ctx, gp);
+        if (rc) return rc;
+    }
+    cudaEventRecord(ctx->ev[3], ctx->stream);
+    if (n > 0) {
+        rc = tsph_ewald(ctx, gp);
+        if (rc) return rc;
+    }
+    if (n > 0) {
+        k_scatter_grav<<<tsph_blocks(n, 256), 256, 0, ctx->stream>>>(n, ctx->P, ctx->C);
+        TSPH_LAUNCH_CK("k_scatter_grav");
+    }
+    cudaEventRecord(ctx->ev[4], ctx->stream);
+    rc = read_status(ctx);
+    if (rc) return rc;
+    cudaEventElapsedTime(&ctx->timings[0], ctx->ev[0], ctx->ev[1]);
+    cudaEventElapsedTime(&ctx->timings[1], ctx->ev[1], ctx->ev[2]);
+    cudaEventElapsedTime(&ctx->timings[2], ctx->ev[2], ctx->ev[3]);
+    cudaEventElapsedTime(&ctx->timings[3], ctx->ev[3], ctx->ev[4]);
+    cudaEventElapsedTime(&ctx->timings[7], ctx->ev[0], ctx->ev[4]);
+    ctx->lastGrav = *gp;
+    ctx->haveGrav = true;
+    if (out) {
+        static const int qflop[5] = {10, 10, 41, 120, 277};
+        static const int mflop[5] = {10, 10, 48, 151, 343};
+        const TsphDevCounters &c = *ctx->hCnt;
+        memset(out, 0, sizeof(*out));
+        out->nActive = (int)c.nActive;
+        out->nBuckets = ctx->T.nLeaves;
+        out->dPartSum = (double)c.nPartPP + (double)c.nIntra;
+        out->dCellSum = (double)c.nCellNewt;
+        out->dSoftSum = (double)c.nCellSoft;
+        double fg = 38.0 * ((double)c.nPartPP + (double)c.nBucketSq) + 82.0 * (double)c.nCellSoft +
+                    (35.0 + qflop[gp->iOrder]) * (double)c.nCellNewt;
+        double fe = 0.0;
+        if (gp->bPeriodic && gp->bEwald && gp->iEwOrder >= 1)
+            fe = (double)c.nEwLoop * (104.0 + mflop[gp->iEwOrder]) + (double)n * ctx->nEwt * 58.0;
+        out->dFlop = fg + fe;
+        out->dFlopEwald = fe;
+        out->dExactFrac = c.nTests ? (double)c.nExactTests / (double)c.nTests : 0.0;
+    }
+    return TSPH_OK;
+}
+
+// interleave up to three caller-order arrays for one host copy
+__global__ void k_interleave(int n, const double *__restrict__ a0, const double *__restrict__ a1,
+                             const double *__restrict__ a2, int comp, double *dst) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    dst[comp * i] = a0[i];
+    if (comp > 1) dst[comp * i + 1] = a1[i];
+    if (comp > 2) dst[comp * i + 2] = a2[i];
+}
+
+// caller-order device arrays (n entries) -> host, interleaved by comp
+int tsph_copy_out_n(tsph_ctx *ctx, int n, const double *a0, const double *a1, const double *a2,
+                    int comp, double *host) {
+    if (n == 0 || !host) return TSPH_OK;
+    if (comp == 1) {
+        TSPH_CK(cudaMemcpyAsync(host, a0, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+        TSPH_CK(cudaStreamSynchronize(ctx->stream));
+        return TSPH_OK;
+    }
+    k_interleave<<<tsph_blocks(n, 256), 256, 0, ctx->stream>>>(n, a0, a1, a2, comp, ctx->dStage);
+    TSPH_LAUNCH_CK("k_interleave");
+    TSPH_CK(cudaMemcpyAsync(host, ctx->dStage, sizeof(double) * comp * n, cudaMemcpyDeviceToHost,
+                            ctx->stream));
+    TSPH_CK(cudaStreamSynchronize(ctx->stream));
+    return TSPH_OK;
+}
+
+int tsph_copy_out(tsph_ctx *ctx, const double *a0, const double *a1, const double *a2, int comp,
+                  double *host) {
+    return tsph_copy_out_n(ctx, ctx->n, a0, a1, a2, comp, host);
+}
+
+extern "C" int tsph_get_gravity(tsph_ctx *ctx, double *acc, double *pot, double *dtGrav) {
+    if (!ctx) return TSPH_ERR_ARG;
+    if (!ctx->haveGrav) return TSPH_ERR_STATE;
+    cudaSetDevice(ctx->device);
+    int rc = tsph_copy_out(ctx, ctx->C.ax, ctx->C.ay, ctx->C.az, 3, acc);
+    if (!rc) rc = tsph_copy_out(ctx, ctx->C.pot, nullptr, nullptr, 1, pot);
+    if (!rc) rc = tsph_copy_out(ctx, ctx->C.dtGrav, nullptr, nullptr, 1, dtGrav);
+    return rc;
+}
+
+extern "C" int tsph_get_tree(tsph_ctx *ctx, int *nNodes, int *inode, double *dnode, int *perm) {
+    if (!ctx || !nNodes) return TSPH_ERR_ARG;
+    if (!ctx->haveTree) return TSPH_ERR_STATE;
+    cudaSetDevice(ctx->device);
+    TSPH_CK(cudaStreamSynchronize(ctx->stream));
+    const TsphDevTree &T = ctx->T;
+    int nn = T.nNodes;
+    *nNodes = nn;
+    if (!inode) return TSPH_OK;
+    size_t N = (size_t)nn;
+    int *hi = (int *)malloc(sizeof(int) * N * 5);
+    double *hd = (double *)malloc(sizeof(double) * N * 19);
+    if (!hi || !hd) { free(hi); free(hd); return TSPH_ERR_NOMEM; }
+    int *pLo = hi, *pUp = hi + N, *dim = hi + 2 * N, *up = hi + 3 * N, *skip = hi + 4 * N;
+    double *fs = hd, *bnd = hd + N, *fm = hd + 7 * N, *so = hd + 8 * N, *r = hd + 9 * N;
+    double *fo = hd + 12 * N, *bm = hd + 13 * N, *q = hd + 14 * N;   // q needs 6N: ends at 20N
+    double *qbuf = (double *)malloc(sizeof(double) * N * 6);
+    if (!qbuf) { free(hi); free(hd); return TSPH_ERR_NOMEM; }
+    q = qbuf;
+    int rc = TSPH_OK;
+#define CPY(dst, src, cnt) \
+    if (!rc && cudaMemcpy(dst, src, cnt, cudaMemcpyDeviceToHost) != cudaSuccess) rc = TSPH_ERR_CUDA
+    CPY(pLo, T.pLower, sizeof(int) * N);
+    CPY(pUp, T.pUpper, sizeof(int) * N);
+    CPY(dim, T.iDim, sizeof(int) * N);
+    CPY(up, T.upper, sizeof(int) * N);
+    CPY(skip, T.skip, sizeof(int) * N);
+    CPY(fs, T.fSplit, sizeof(double) * N);
+    CPY(bnd, T.bnd, sizeof(double) * 6 * N);
+    CPY(fm, T.fMass, sizeof(double) * N);
+    CPY(so, T.fSoft, sizeof(double) * N);
+    CPY(r, T.r, sizeof(double) * 3 * N);
+    CPY(fo, T.fOpen2, sizeof(double) * N);
+    CPY(bm, T.Bmax, sizeof(double) * N);
+    CPY(q, T.Q, sizeof(double) * 6 * N);
+    if (perm && ctx->n > 0) CPY(perm, ctx->P.iord, sizeof(int) * ctx->n);
+#undef CPY
+    if (!rc) {
+        for (size_t i = 0; i < N; ++i) {
+            bool leaf = up[i] < 0;
+            inode[6 * i + 0] = pLo[i];
+            inode[6 * i + 1] = pUp[i];
+            inode[6 * i + 2] = dim[i];
+            inode[6 * i + 3] = leaf ? -1 : (int)i + 1;   // threaded: first child
+            inode[6 * i + 4] = skip[i];                  // threaded: next
+            inode[6 * i + 5] = 0;
+            dnode[16 * i + 0] = fs[i];
+            for (int k = 0; k < 3; ++k) {
+                dnode[16 * i + 1 + k] = bnd[6 * i + k];
+                dnode[16 * i + 4 + k] = bnd[6 * i + 3 + k];
+                dnode[16 * i + 9 + k] = r[3 * i + k];
+            }
+            dnode[16 * i + 7] = fm[i];
+            dnode[16 * i + 8] = so[i];
+            dnode[16 * i + 12] = fo[i];
+            dnode[16 * i + 13] = bm[i];
+            dnode[16 * i + 14] = q[6 * i + 0];
+            dnode[16 * i + 15] = q[6 * i + 1];
+        }
+    }
+    free(hi);
+    free(hd);
+    free(qbuf);
+    return rc;
+}
+
+extern "C" int tsph_get_lists(tsph_ctx *ctx, int *nBuckets, int *blist) {
+    if (!ctx || !nBuckets) return TSPH_ERR_ARG;
+    if (!ctx->haveGrav) return TSPH_ERR_STATE;
+    *nBuckets = ctx->T.nLeaves;
+    if (!blist || ctx->T.nLeaves == 0) return TSPH_OK;
+    cudaSetDevice(ctx->device);
+    TSPH_CK(cudaStreamSynchronize(ctx->stream));
+    TSPH_CK(cudaMemcpy(blist, ctx->dBucketLists, sizeof(int) * 4 * ctx->T.nLeaves,
+                       cudaMemcpyDeviceToHost));
+    return TSPH_OK;
+}
+
+extern "C" int tsph_get_timings(tsph_ctx *ctx, float *t8) {
+    if (!ctx || !t8) return TSPH_ERR_ARG;
+    memcpy(t8, ctx->timings, sizeof(float) * 8);
+    return TSPH_OK;
+}
+
+extern "C" long long tsph_launch_count(tsph_ctx *ctx) { return ctx ? ctx->launches : 0; }

@@ -1,0 +1,428 @@
+// K5: Ewald periodic correction.
+//
+// Follows pkdBucketEwald (ewald.c:15-178): for every particle a real-space
+// sum over the images (ix,iy,iz) in [-ceil(fEwCut), ceil(fEwCut)]^3 kept when
+// r <= fEwCut*L or inside the replica "hole" (the -erf branch, ewald.c:85-125),
+// with the small-r series below r^2 < 3e-3 L^2, then a k-space sum over the
+// table built by pkdEwaldInit (ewald.c:182-248), all with the complete root
+// multipoles of pkdCalcRoot/pkdDistribRoot (pkd.c:4395-4493) evaluated by
+// MEVAL (meval.h:21-81).  The table is built on the host in FP64 from root
+// moments reduced on the device in a fixed order (deterministic).
+// erf/erfc/exp/sin/cos are CUDA's own functions.
+#include <math.h>
+#include <stdlib.h>
+
+#include "tsph_ctx.cuh"
+
+#define EW_MAXH 512
+
+// complete root multipoles in the reference's ILCN member order
+struct EwMom {
+    double m, x, y, z;
+    double xx, yy, xy, xz, yz, zz;
+    double xxx, xyy, xxy, yyy, xxz, yyz, xyz, xzz, yzz, zzz;
+    double xxxx, xyyy, xxxy, yyyy, xxxz, yyyz, xxyy, xxyz, xyyz;
+    double xxzz, xyzz, xzzz, yyzz, yzzz, zzzz;
+};
+
+struct EwConst {
+    EwMom mom;
+    float momf[35];
+    double L, alpha, alpha2, k1, ka, fEwCut2, smallR2;
+    int nEwReps, nReps, nEwh, iOrder;
+    double hx[EW_MAXH], hy[EW_MAXH], hz[EW_MAXH], hC[EW_MAXH], hS[EW_MAXH];
+};
+__constant__ EwConst cE;
+
+// --------------------------------------------------------------------------
+// root moments: block partial sums in a fixed order, then a fixed-order sum
+// --------------------------------------------------------------------------
+#define RM_BS 256
+#define RM_NV 25
+
+__global__ void k_root_partial(int n, const double *__restrict__ x, const double *__restrict__ y,
+                               const double *__restrict__ z, const double *__restrict__ m,
+                               const double *__restrict__ rc, double *partial) {
+    __shared__ double sh[RM_NV][RM_BS / 32];
+    double acc[RM_NV];
+#pragma unroll
+    for (int k = 0; k < RM_NV; ++k) acc[k] = 0.0;
+    double cx = rc[0], cy = rc[1], cz = rc[2];
+    for (int p = blockIdx.x * RM_BS + threadIdx.x; p < n; p += gridDim.x * RM_BS) {
+        double mm = m[p], dx = x[p] - cx, dy = y[p] - cy, dz = z[p] - cz;
+        double dx2 = dx * dx, dy2 = dy * dy, dz2 = dz * dz;
+        // hexadecapole (complete): xxxx xyyy xxxy yyyy xxxz yyyz xxyy xxyz xyyz xxzz xyzz xzzz yyzz yzzz zzzz
+        acc[0] += mm * dx2 * dx2;
+        acc[1] += mm * dx * dy2 * dy;
+        acc[2] += mm * dx2 * dx * dy;
+        acc[3] += mm * dy2 * dy2;
+        acc[4] += mm * dx2 * dx * dz;
+        acc[5] += mm * dy2 * dy * dz;
+        acc[6] += mm * dx2 * dy2;
+        acc[7] += mm * dx2 * dy * dz;
+        acc[8] += mm * dx * dy2 * dz;
+        acc[9] += mm * dx2 * dz2;
+        acc[10] += mm * dx * dy * dz2;
+        acc[11] += mm * dx * dz2 * dz;
+        acc[12] += mm * dy2 * dz2;
+        acc[13] += mm * dy * dz2 * dz;
+        acc[14] += mm * dz2 * dz2;
+        // octopole (complete): xxx xyy xxy yyy xxz yyz xyz xzz yzz zzz
+        acc[15] += mm * dx2 * dx;
+        acc[16] += mm * dx * dy2;
+        acc[17] += mm * dx2 * dy;
+        acc[18] += mm * dy2 * dy;
+        acc[19] += mm * dx2 * dz;
+        acc[20] += mm * dy2 * dz;
+        acc[21] += mm * dx * dy * dz;
+        acc[22] += mm * dx * dz2;
+        acc[23] += mm * dy * dz2;
+        acc[24] += mm * dz2 * dz;
+    }
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < RM_NV; ++k) {
+        double v = acc[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) sh[k][w] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < RM_NV) {
+        double v = 0.0;
+        for (int j = 0; j < RM_BS / 32; ++j) v += sh[threadIdx.x][j];
+        partial[blockIdx.x * RM_NV + threadIdx.x] = v;
+    }
+}
+
+__global__ void k_root_final(int nb, const double *__restrict__ partial, double *out) {
+    int k = threadIdx.x;
+    if (k >= RM_NV) return;
+    double v = 0.0;
+    for (int b = 0; b < nb; ++b) v += partial[b * RM_NV + k];
+    out[k] = v;
+}
+
+// --------------------------------------------------------------------------
+// MEVAL and the per-particle Ewald kernel
+// --------------------------------------------------------------------------
+template <typename Real>
+struct MomR {
+    Real m, xx, yy, xy, xz, yz, zz;
+    Real xxx, xyy, xxy, yyy, xxz, yyz, xyz, xzz, yzz, zzz;
+    Real xxxx, xyyy, xxxy, yyyy, xxxz, yyyz, xxyy, xxyz, xyyz, xxzz, xyzz, xzzz, yyzz, yzzz, zzzz;
+};
+
+template <typename Real>
+__device__ __forceinline__ void load_mom(MomR<Real> &M) {
+    if (sizeof(Real) == 8) {
+        const EwMom &e = cE.mom;
+        M.m = e.m; M.xx = e.xx; M.yy = e.yy; M.xy = e.xy; M.xz = e.xz; M.yz = e.yz; M.zz = e.zz;
+        M.xxx = e.xxx; M.xyy = e.xyy; M.xxy = e.xxy; M.yyy = e.yyy; M.xxz = e.xxz; M.yyz = e.yyz;
+        M.xyz = e.xyz; M.xzz = e.xzz; M.yzz = e.yzz; M.zzz = e.zzz;
+        M.xxxx = e.xxxx; M.xyyy = e.xyyy; M.xxxy = e.xxxy; M.yyyy = e.yyyy; M.xxxz = e.xxxz;
+        M.yyyz = e.yyyz; M.xxyy = e.xxyy; M.xxyz = e.xxyz; M.xyyz = e.xyyz; M.xxzz = e.xxzz;
+        M.xyzz = e.xyzz; M.xzzz = e.xzzz; M.yyzz = e.yyzz; M.yzzz = e.yzzz; M.zzzz = e.zzzz;
+    } else {
+        const float *f = cE.momf;
+        M.m = f[0]; M.xx = f[4]; M.yy = f[5]; M.xy = f[6]; M.xz = f[7]; M.yz = f[8]; M.zz = f[9];
+        M.xxx = f[10]; M.xyy = f[11]; M.xxy = f[12]; M.yyy = f[13]; M.xxz = f[14]; M.yyz = f[15];
+        M.xyz = f[16]; M.xzz = f[17]; M.yzz = f[18]; M.zzz = f[19];
+        M.xxxx = f[20]; M.xyyy = f[21]; M.xxxy = f[22]; M.yyyy = f[23]; M.xxxz = f[24];
+        M.yyyz = f[25]; M.xxyy = f[26]; M.xxyz = f[27]; M.xyyz = f[28]; M.xxzz = f[29];
+        M.xyzz = f[30]; M.xzzz = f[31]; M.yyzz = f[32]; M.yzzz = f[33]; M.zzzz = f[34];
+    }
+}
+
+template <typename Real>
+__device__ __forceinline__ void meval(int iOrder, const MomR<Real> &mom, const Real *gam, Real dx,
+                                      Real dy, Real dz, Real &ax, Real &ay, Real &az, Real &fPot) {
+    Real Qmirx, Qmiry, Qmirz, Qmir, Qta = 0;
+    if (iOrder >= 4) {
+        Qmirx = Real(1.0 / 6.0) * (mom.xzzz * dz * dz * dz + 3 * mom.xyzz * dy * dz * dz + 3 * mom.xyyz * dy * dy * dz + mom.xyyy * dy * dy * dy + 3 * mom.xxzz * dx * dz * dz + 6 * mom.xxyz * dx * dy * dz + 3 * mom.xxyy * dx * dy * dy + 3 * mom.xxxz * dx * dx * dz + 3 * mom.xxxy * dx * dx * dy + mom.xxxx * dx * dx * dx);
+        Qmiry = Real(1.0 / 6.0) * (mom.yzzz * dz * dz * dz + 3 * mom.xyzz * dx * dz * dz + 3 * mom.xxyz * dx * dx * dz + mom.xxxy * dx * dx * dx + 3 * mom.yyzz * dy * dz * dz + 6 * mom.xyyz * dx * dy * dz + 3 * mom.xxyy * dx * dx * dy + 3 * mom.yyyz * dy * dy * dz + 3 * mom.xyyy * dx * dy * dy + mom.yyyy * dy * dy * dy);
+        Qmirz = Real(1.0 / 6.0) * (mom.yyyz * dy * dy * dy + 3 * mom.xyyz * dx * dy * dy + 3 * mom.xxyz * dx * dx * dy + mom.xxxz * dx * dx * dx + 3 * mom.yyzz * dy * dy * dz + 6 * mom.xyzz * dx * dy * dz + 3 * mom.xxzz * dx * dx * dz + 3 * mom.yzzz * dy * dz * dz + 3 * mom.xzzz * dx * dz * dz + mom.zzzz * dz * dz * dz);
+        Qmir = Real(0.25) * (Qmirx * dx + Qmiry * dy + Qmirz * dz);
+        Real Qxx = mom.xxxx + mom.xxyy + mom.xxzz;
+        Real Qxy = mom.xxxy + mom.xyyy + mom.xyzz;
+        Real Qxz = mom.xxxz + mom.xyyz + mom.xzzz;
+        Real Qyy = mom.xxyy + mom.yyyy + mom.yyzz;
+        Real Qyz = mom.xxyz + mom.yyyz + mom.yzzz;
+        Real Qzz = mom.xxzz + mom.yyzz + mom.zzzz;
+        Real Qtr = Real(0.125) * (Qxx + Qyy + Qzz);
+        Real Qhx = Real(0.5) * (Qxx * dx + Qxy * dy + Qxz * dz);
+        Real Qhy = Real(0.5) * (Qxy * dx + Qyy * dy + Qyz * dz);
+        Real Qhz = Real(0.5) * (Qxz * dx + Qyz * dy + Qzz * dz);
+        Real Qh = Real(0.5) * (Qhx * dx + Qhy * dy + Qhz * dz);
+        fPot -= gam[4] * Qmir - gam[3] * Qh + gam[2] * Qtr;
+        Qta += gam[5] * Qmir - gam[4] * Qh + gam[3] * Qtr;
+        ax += gam[4] * Qmirx - gam[3] * Qhx;
+        ay += gam[4] * Qmiry - gam[3] * Qhy;
+        az += gam[4] * Qmirz - gam[3] * Qhz;
+    }
+    if (iOrder >= 3) {
+        Qmirx = Real(0.5) * (mom.xzz * dz * dz + 2 * mom.xyz * dy * dz + mom.xyy * dy * dy + 2 * mom.xxz * dx * dz + 2 * mom.xxy * dx * dy + mom.xxx * dx * dx);
+        Qmiry = Real(0.5) * (mom.yzz * dz * dz + 2 * mom.xyz * dx * dz + mom.xxy * dx * dx + 2 * mom.yyz * dy * dz + 2 * mom.xyy * dx * dy + mom.yyy * dy * dy);
+        Qmirz = Real(0.5) * (mom.yyz * dy * dy + 2 * mom.xyz * dx * dy + mom.xxz * dx * dx + 2 * mom.yzz * dy * dz + 2 * mom.xzz * dx * dz + mom.zzz * dz * dz);
+        Qmir = Real(1.0 / 3.0) * (Qmirx * dx + Qmiry * dy + Qmirz * dz);
+        Real Qx = Real(0.5) * (mom.xxx + mom.xyy + mom.xzz);
+        Real Qy = Real(0.5) * (mom.xxy + mom.yyy + mom.yzz);
+        Real Qz = Real(0.5) * (mom.xxz + mom.yyz + mom.zzz);
+        Real Qtr = Qx * dx + Qy * dy + Qz * dz;
+        fPot -= gam[3] * Qmir - gam[2] * Qtr;
+        Qta += gam[4] * Qmir - gam[3] * Qtr;
+        ax += gam[3] * Qmirx - gam[2] * Qx;
+        ay += gam[3] * Qmiry - gam[2] * Qy;
+        az += gam[3] * Qmirz - gam[2] * Qz;
+    }
+    if (iOrder >= 2) {
+        Qmirx = mom.xz * dz + mom.xy * dy + mom.xx * dx;
+        Qmiry = mom.yz * dz + mom.xy * dx + mom.yy * dy;
+        Qmirz = mom.yz * dy + mom.xz * dx + mom.zz * dz;
+        Qmir = Real(0.5) * (Qmirx * dx + Qmiry * dy + Qmirz * dz);
+        Real Qtr = Real(0.5) * (mom.xx + mom.yy + mom.zz);
+        fPot -= gam[2] * Qmir - gam[1] * Qtr;
+        Qta += gam[3] * Qmir - gam[2] * Qtr;
+        ax += gam[2] * Qmirx;
+        ay += gam[2] * Qmiry;
+        az += gam[2] * Qmirz;
+    }
+    fPot -= gam[0] * mom.m;
+    Qta += gam[1] * mom.m;
+    ax -= dx * Qta;
+    ay -= dy * Qta;
+    az -= dz * Qta;
+}
+
+__device__ __forceinline__ float erf_r(float x) { return erff(x); }
+__device__ __forceinline__ double erf_r(double x) { return erf(x); }
+__device__ __forceinline__ float erfc_r(float x) { return erfcf(x); }
+__device__ __forceinline__ double erfc_r(double x) { return erfc(x); }
+__device__ __forceinline__ float exp_r(float x) { return expf(x); }
+__device__ __forceinline__ double exp_r(double x) { return exp(x); }
+__device__ __forceinline__ float sqrt_r(float x) { return sqrtf(x); }
+__device__ __forceinline__ double sqrt_r(double x) { return sqrt(x); }
+__device__ __forceinline__ void sincos_r(float x, float *s, float *c) { sincosf(x, s, c); }
+__device__ __forceinline__ void sincos_r(double x, double *s, double *c) { sincos(x, s, c); }
+
+template <typename Real>
+__global__ void __launch_bounds__(128) k_ewald(TsphDevParts P, TsphDevCounters *cnt) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long nLoop = 0;
+    if (p < P.n) {
+        MomR<Real> mom;
+        load_mom<Real>(mom);
+        const Real L = (Real)cE.L;
+        const Real alpha2 = (Real)cE.alpha2, alpha = (Real)cE.alpha, ka = (Real)cE.ka;
+        const Real fEwCut2 = (Real)cE.fEwCut2, smallR2 = (Real)cE.smallR2;
+        const int nEw = cE.nEwReps, nR = cE.nReps, iOrder = cE.iOrder;
+        Real fPot = (Real)(cE.mom.m * cE.k1), ax = 0, ay = 0, az = 0;
+        Real dx = (Real)(P.x[p] - cE.mom.x);
+        Real dy = (Real)(P.y[p] - cE.mom.y);
+        Real dz = (Real)(P.z[p] - cE.mom.z);
+        for (int ix = -nEw; ix <= nEw; ++ix) {
+            bool hx = (ix >= -nR && ix <= nR);
+            Real dxo = dx + ix * L;
+            for (int iy = -nEw; iy <= nEw; ++iy) {
+                bool hxy = hx && iy >= -nR && iy <= nR;
+                Real dyo = dy + iy * L;
+                for (int iz = -nEw; iz <= nEw; ++iz) {
+                    bool hole = hxy && iz >= -nR && iz <= nR;
+                    Real dzo = dz + iz * L;
+                    Real r2 = dxo * dxo + dyo * dyo + dzo * dzo;
+                    if (r2 > fEwCut2 && !hole) continue;
+                    Real gam[6];
+                    if (r2 < smallR2) {
+                        Real alphan = ka;
+                        Real s = r2 * alpha2;
+                        gam[0] = alphan * (s / 3 - 1);
+                        alphan *= 2 * alpha2;
+                        gam[1] = alphan * (s / 5 - Real(1.0 / 3.0));
+                        alphan *= 2 * alpha2;
+                        gam[2] = alphan * (s / 7 - Real(1.0 / 5.0));
+                        alphan *= 2 * alpha2;
+                        gam[3] = alphan * (s / 9 - Real(1.0 / 7.0));
+                        alphan *= 2 * alpha2;
+                        gam[4] = alphan * (s / 11 - Real(1.0 / 9.0));
+                        alphan *= 2 * alpha2;
+                        gam[5] = alphan * (s / 13 - Real(1.0 / 11.0));
+                    } else {
+                        Real r = sqrt_r(r2);
+                        Real dir = Real(1) / r;
+                        Real dir2 = dir * dir;
+                        Real a = exp_r(-r2 * alpha2);
+                        a *= ka * dir2;
+                        gam[0] = hole ? -erf_r(alpha * r) : erfc_r(alpha * r);
+                        gam[0] *= dir;
+                        gam[1] = gam[0] * dir2 + a;
+                        Real alphan = 2 * alpha2;
+                        gam[2] = 3 * gam[1] * dir2 + alphan * a;
+                        alphan *= 2 * alpha2;
+                        gam[3] = 5 * gam[2] * dir2 + alphan * a;
+                        alphan *= 2 * alpha2;
+                        gam[4] = 7 * gam[3] * dir2 + alphan * a;
+                        alphan *= 2 * alpha2;
+                        gam[5] = 9 * gam[4] * dir2 + alphan * a;
+                    }
+                    meval<Real>(iOrder, mom, gam, dxo, dyo, dzo, ax, ay, az, fPot);
+                    ++nLoop;
+                }
+            }
+        }
+        for (int i = 0; i < cE.nEwh; ++i) {
+            Real hx = (Real)cE.hx[i], hy = (Real)cE.hy[i], hz = (Real)cE.hz[i];
+            Real hC = (Real)cE.hC[i], hS = (Real)cE.hS[i];
+            Real hdotx = hx * dx + hy * dy + hz * dz;
+            Real s, c;
+            sincos_r(hdotx, &s, &c);
+            fPot += hC * c + hS * s;
+            Real t = hC * s - hS * c;
+            ax += hx * t;
+            ay += hy * t;
+            az += hz * t;
+        }
+        P.pot[p] += (double)fPot;
+        P.ax[p] += (double)ax;
+        P.ay[p] += (double)ay;
+        P.az[p] += (double)az;
+    }
+    // count real-space terms
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) nLoop += __shfl_xor_sync(0xffffffffu, nLoop, o);
+    if ((threadIdx.x & 31) == 0 && nLoop) atomicAdd(&cnt->nEwLoop, nLoop);
+}
+
+// --------------------------------------------------------------------------
+// host: QEVAL for the k-space table (qeval.h:21-64), same arithmetic as the
+// reference's pkdEwaldInit
+// --------------------------------------------------------------------------
+static void qeval_h(int iOrder, const EwMom &mom, const double *gam, double dx, double dy,
+                    double dz, double *fPot) {
+    double Qmirx, Qmiry, Qmirz, Qmir, Qta = 0.0, ax = 0, ay = 0, az = 0;
+    if (iOrder >= 4) {
+        Qmirx = (1.0 / 6.0) * (mom.xzzz * dz * dz * dz + 3 * mom.xyzz * dy * dz * dz + 3 * mom.xyyz * dy * dy * dz + mom.xyyy * dy * dy * dy + 3 * mom.xxzz * dx * dz * dz + 6 * mom.xxyz * dx * dy * dz + 3 * mom.xxyy * dx * dy * dy + 3 * mom.xxxz * dx * dx * dz + 3 * mom.xxxy * dx * dx * dy + mom.xxxx * dx * dx * dx);
+        Qmiry = (1.0 / 6.0) * (mom.yzzz * dz * dz * dz + 3 * mom.xyzz * dx * dz * dz + 3 * mom.xxyz * dx * dx * dz + mom.xxxy * dx * dx * dx + 3 * mom.yyzz * dy * dz * dz + 6 * mom.xyyz * dx * dy * dz + 3 * mom.xxyy * dx * dx * dy + 3 * mom.yyyz * dy * dy * dz + 3 * mom.xyyy * dx * dy * dy + mom.yyyy * dy * dy * dy);
+        Qmirz = (1.0 / 6.0) * (mom.yyyz * dy * dy * dy + 3 * mom.xyyz * dx * dy * dy + 3 * mom.xxyz * dx * dx * dy + mom.xxxz * dx * dx * dx + 3 * mom.yyzz * dy * dy * dz + 6 * mom.xyzz * dx * dy * dz + 3 * mom.xxzz * dx * dx * dz + 3 * mom.yzzz * dy * dz * dz + 3 * mom.xzzz * dx * dz * dz + mom.zzzz * dz * dz * dz);
+        Qmir = (1.0 / 4.0) * (Qmirx * dx + Qmiry * dy + Qmirz * dz);
+        *fPot -= gam[4] * Qmir;
+        Qta += gam[5] * Qmir;
+        ax += gam[4] * Qmirx; ay += gam[4] * Qmiry; az += gam[4] * Qmirz;
+    }
+    if (iOrder >= 3) {
+        Qmirx = (1.0 / 2.0) * (mom.xzz * dz * dz + 2 * mom.xyz * dy * dz + mom.xyy * dy * dy + 2 * mom.xxz * dx * dz + 2 * mom.xxy * dx * dy + mom.xxx * dx * dx);
+        Qmiry = (1.0 / 2.0) * (mom.yzz * dz * dz + 2 * mom.xyz * dx * dz + mom.xxy * dx * dx + 2 * mom.yyz * dy * dz + 2 * mom.xyy * dx * dy + mom.yyy * dy * dy);
+        Qmirz = (1.0 / 2.0) * (mom.yyz * dy * dy + 2 * mom.xyz * dx * dy + mom.xxz * dx * dx + 2 * mom.yzz * dy * dz + 2 * mom.xzz * dx * dz + mom.zzz * dz * dz);
+        Qmir = (1.0 / 3.0) * (Qmirx * dx + Qmiry * dy + Qmirz * dz);
+        *fPot -= gam[3] * Qmir;
+        Qta += gam[4] * Qmir;
+        ax += gam[3] * Qmirx; ay += gam[3] * Qmiry; az += gam[3] * Qmirz;
+    }
+    if (iOrder >= 2) {
+        Qmirx = (1.0 / 1.0) * (mom.xz * dz + mom.xy * dy + mom.xx * dx);
+        Qmiry = (1.0 / 1.0) * (mom.yz * dz + mom.xy * dx + mom.yy * dy);
+        Qmirz = (1.0 / 1.0) * (mom.yz * dy + mom.xz * dx + mom.zz * dz);
+        Qmir = (1.0 / 2.0) * (Qmirx * dx + Qmiry * dy + Qmirz * dz);
+        *fPot -= gam[2] * Qmir;
+        Qta += gam[3] * Qmir;
+        ax += gam[2] * Qmirx; ay += gam[2] * Qmiry; az += gam[2] * Qmirz;
+    }
+    *fPot -= gam[0] * mom.m;
+    (void)Qta; (void)ax; (void)ay; (void)az;
+}
+
+int tsph_ewald(tsph_ctx *ctx, const tsph_grav_params *gp) {
+    if (!(gp->bPeriodic && gp->bEwald) || gp->iEwOrder < 1) return TSPH_OK;
+    if (gp->iEwOrder > 4) return TSPH_ERR_ARG;
+    const int n = ctx->n;
+    if (n == 0) return TSPH_OK;
+    // root moments on the device
+    int nb = 256;
+    double *partial = ctx->dRoot + 64;
+    k_root_partial<<<nb, RM_BS, 0, ctx->stream>>>(n, ctx->P.x, ctx->P.y, ctx->P.z, ctx->P.m,
+                                                  ctx->T.r, partial);
+    TSPH_LAUNCH_CK("k_root_partial");
+    k_root_final<<<1, 32, 0, ctx->stream>>>(nb, partial, ctx->dRoot);
+    TSPH_LAUNCH_CK("k_root_final");
+    double h[25 + 11];
+    TSPH_CK(cudaMemcpyAsync(h, ctx->dRoot, sizeof(double) * 25, cudaMemcpyDeviceToHost, ctx->stream));
+    double node0[11];   // fMass, r[3], Q[6]
+    TSPH_CK(cudaMemcpyAsync(&node0[0], ctx->T.fMass, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    TSPH_CK(cudaMemcpyAsync(&node0[1], ctx->T.r, 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    TSPH_CK(cudaMemcpyAsync(&node0[4], ctx->T.Q, 6 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    TSPH_CK(cudaStreamSynchronize(ctx->stream));
+    static EwConst E;   // large; built on the host then copied
+    memset(&E, 0, sizeof(E));
+    EwMom &M = E.mom;
+    M.xxxx = h[0]; M.xyyy = h[1]; M.xxxy = h[2]; M.yyyy = h[3]; M.xxxz = h[4]; M.yyyz = h[5];
+    M.xxyy = h[6]; M.xxyz = h[7]; M.xyyz = h[8]; M.xxzz = h[9]; M.xyzz = h[10]; M.xzzz = h[11];
+    M.yyzz = h[12]; M.yzzz = h[13]; M.zzzz = h[14];
+    M.xxx = h[15]; M.xyy = h[16]; M.xxy = h[17]; M.yyy = h[18]; M.xxz = h[19]; M.yyz = h[20];
+    M.xyz = h[21]; M.xzz = h[22]; M.yzz = h[23]; M.zzz = h[24];
+    // pkdDistribRoot (pkd.c:4472-4493): mass, COM and complete quadrupole
+    M.m = node0[0];
+    M.x = node0[1]; M.y = node0[2]; M.z = node0[3];
+    M.xx = node0[4]; M.yy = node0[5]; M.zz = node0[6];
+    M.xy = node0[7]; M.xz = node0[8]; M.yz = node0[9];
+    const double *mv = &M.m;
+    for (int k = 0; k < 35; ++k) E.momf[k] = (float)mv[k];
+    double L = gp->dPeriod;
+    E.L = L;
+    E.alpha = 2.0 / L;
+    E.alpha2 = E.alpha * E.alpha;
+    E.k1 = M_PI / (E.alpha2 * L * L * L);
+    E.ka = 2.0 * E.alpha / sqrt(M_PI);
+    E.fEwCut2 = gp->fEwCut * gp->fEwCut * L * L;
+    E.smallR2 = 3.0e-3 * L * L;
+    int nEwReps = (int)ceil(gp->fEwCut);
+    E.nReps = gp->nReps;
+    E.nEwReps = nEwReps > gp->nReps ? nEwReps : gp->nReps;
+    E.iOrder = gp->iEwOrder;
+    // k-space table, pkdEwaldInit (ewald.c:182-248)
+    int hReps = (int)ceil(gp->fEwhCut), ih = 0;
+    double k4 = M_PI * M_PI / (E.alpha * E.alpha * L * L);
+    for (int hx = -hReps; hx <= hReps; ++hx)
+        for (int hy = -hReps; hy <= hReps; ++hy)
+            for (int hz = -hReps; hz <= hReps; ++hz) {
+                int h2 = hx * hx + hy * hy + hz * hz;
+                if (h2 == 0) continue;
+                if (h2 > gp->fEwhCut * gp->fEwhCut) continue;
+                if (ih == EW_MAXH) return TSPH_ERR_UNSUPPORTED;
+                double gam[6], mfacc = 0.0, mfacs = 0.0;
+                gam[0] = exp(-k4 * h2) / (M_PI * h2 * L);
+                gam[1] = 2 * M_PI / L * gam[0];
+                gam[2] = -2 * M_PI / L * gam[1];
+                gam[3] = 2 * M_PI / L * gam[2];
+                gam[4] = -2 * M_PI / L * gam[3];
+                gam[5] = 2 * M_PI / L * gam[4];
+                gam[1] = 0.0; gam[3] = 0.0; gam[5] = 0.0;
+                qeval_h(gp->iEwOrder, M, gam, hx, hy, hz, &mfacc);
+                gam[0] = exp(-k4 * h2) / (M_PI * h2 * L);
+                gam[1] = 2 * M_PI / L * gam[0];
+                gam[2] = -2 * M_PI / L * gam[1];
+                gam[3] = 2 * M_PI / L * gam[2];
+                gam[4] = -2 * M_PI / L * gam[3];
+                gam[5] = 2 * M_PI / L * gam[4];
+                gam[0] = 0.0; gam[2] = 0.0; gam[4] = 0.0;
+                qeval_h(gp->iEwOrder, M, gam, hx, hy, hz, &mfacs);
+                E.hx[ih] = 2 * M_PI / L * hx;
+                E.hy[ih] = 2 * M_PI / L * hy;
+                E.hz[ih] = 2 * M_PI / L * hz;
+                E.hC[ih] = mfacc;
+                E.hS[ih] = mfacs;
+                ++ih;
+            }
+    E.nEwh = ih;
+    ctx->nEwt = ih;
+    TSPH_CK(cudaMemcpyToSymbolAsync(cE, &E, sizeof(E), 0, cudaMemcpyHostToDevice, ctx->stream));
+    const int BS = 128;
+    if (gp->precision == TSPH_FP32) {
+        k_ewald<float><<<tsph_blocks(n, BS), BS, 0, ctx->stream>>>(ctx->P, ctx->dCnt);
+        TSPH_LAUNCH_CK("k_ewald<float>");
+    } else {
+        k_ewald<double><<<tsph_blocks(n, BS), BS, 0, ctx->stream>>>(ctx->P, ctx->dCnt);
+        TSPH_LAUNCH_CK("k_ewald<double>");
+    }
+    // (a pageable-source async copy returns once the source is staged, so
+    // the static host block may be reused by the next call)
+    return TSPH_OK;
+}

@@ -1,0 +1,735 @@
+// K3+K4: bucket walk fused with the particle-particle and particle-cell
+// interactions.
+//
+// Semantics follow the reference's pkdGravAll bucket loop (pkd.c:2911-3001),
+// pkdBucketWalk / pkdLocalWalk (walk.c:58-178, 306-439) and
+// pkdBucketInteract (grav.c:23-249):
+//   * a cell is opened when the bucket box lies within sqrt(fOpen2) of the
+//     cell's centre of mass (INTERSECTNP, walk.h:12-31) or it holds fewer
+//     than 4 particles (walk.c:81); an opened leaf contributes its particles
+//     (P-P), except the bucket itself in the unshifted replica (walk.c:93);
+//   * an accepted cell is "softened" when twoh2 = (cellSoft + maxSoft)^2 is
+//     not below fOpen2 and the bucket box lies within twoh (walk.c:122-127),
+//     otherwise Newtonian with the trace-free quadrupole (SETILIST);
+//   * P-P uses spline softening with twoh = h_i + h_j (SPLINEM), softened
+//     cells SPLINEQ, Newtonian cells QEVAL; intra-bucket pairs SPLINE.
+//
+// GB300 mapping: one warp per bucket.  The walk is a warp-cooperative
+// depth-first traversal with an explicit stack in shared memory: each step
+// pops up to 32 (cell, replica) entries, one per lane.  Opening tests run in
+// FP32 on hi/lo split coordinates relative to the bucket centre with a
+// rigorous rounding bound; only tests inside that bound are redone in FP64
+// with the reference's own operation order, so every decision equals the
+// reference's FP64 decision while FP64 work (1/64 rate on this part) stays
+// rare.  Accepted interactions are staged in shared-memory tiles and
+// evaluated with lanes = (bucket particle, entry slot), FP32 with tile
+// partial sums merged by compensated (Kahan) addition, or FP64.
+#include <float.h>
+#include <math.h>
+
+#include "tsph_ctx.cuh"
+
+#define NB 8                    // particles per bucket handled per warp
+#define SLOTS (32 / NB)         // entry slots per particle
+#define WPB 4                   // warps per block
+#define STK 2048                // walk stack entries per warp
+#define PPF 128                 // P-P tile size
+#define PPB (PPF + 32 * NB + NB)
+#define CNF 64                  // cell tile size
+#define CNB (CNF + 32)
+
+#define ACT_NONE 0
+#define ACT_OPEN 1
+#define ACT_LEAF 2
+#define ACT_NEWT 3
+#define ACT_SOFT 4
+
+struct WalkConst {
+    int nRep;
+    int selfRep;
+    double off[27][3];
+    float offh[27][3];
+    float offl[27][3];
+    float offmax;      // max |offset| component
+    float E0;          // absolute error floor of the hi/lo relative coordinates
+};
+__constant__ WalkConst cW;
+
+template <typename Real>
+struct WalkSmem {
+    int stack[STK];
+    int pp[PPB];
+    int cn[CNB];
+    int cs[CNB];
+    // staged entry data: P-P uses x,y,z,m,h ; cells use x,y,z,m,q0..q5,h
+    Real ex[PPF], ey[PPF], ez[PPF], em[PPF], eh[PPF];
+    Real q[6][CNF];
+    Real px[NB], py[NB], pz[NB], pm[NB], ph[NB];
+};
+
+struct WalkArgs {
+    TsphDevTree T;
+    TsphDevParts P;
+    TsphDevCounters *cnt;
+    int *bucketLists;      // optional, 4 ints per bucket
+    int nBuckets;
+    int *workCounter;
+    int iOrder;
+};
+
+__device__ __forceinline__ unsigned lane_lt() {
+    unsigned r;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(r));
+    return r;
+}
+
+// INTERSECTNP (walk.h:12-31) in FP64 with the reference's rounding.
+__device__ __forceinline__ bool intersect_exact(const double *bmin, const double *bmax,
+                                                double fBall2, double x, double y, double z) {
+    double dx = xsub(bmin[0], x), dx1 = xsub(x, bmax[0]);
+    double dy = xsub(bmin[1], y), dy1 = xsub(y, bmax[1]);
+    double dz = xsub(bmin[2], z), dz1 = xsub(z, bmax[2]);
+    double d2;
+    if (dx > 0.0) d2 = xmul(dx, dx);
+    else if (dx1 > 0.0) d2 = xmul(dx1, dx1);
+    else d2 = 0.0;
+    if (dy > 0.0) d2 = xadd(d2, xmul(dy, dy));
+    else if (dy1 > 0.0) d2 = xadd(d2, xmul(dy1, dy1));
+    if (dz > 0.0) d2 = xadd(d2, xmul(dz, dz));
+    else if (dz1 > 0.0) d2 = xadd(d2, xmul(dz1, dz1));
+    return d2 <= fBall2;
+}
+
+// Three-way FP32 filter: +1 certainly D2 > F, -1 certainly D2 <= F, 0 unsure.
+__device__ __forceinline__ int filt(float D2, float M, float F, float relF) {
+    if (D2 - M > F * (1.0f + relF)) return 1;
+    if (D2 + M < F * (1.0f - relF)) return -1;
+    return 0;
+}
+
+__device__ __forceinline__ void kahan_add(float &s, float &c, float v) {
+    float y = v - c;
+    float t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+__device__ __forceinline__ void kahan_add(double &s, double &c, double v) { s += v; (void)c; }
+
+// Error-free sum of two compensated pairs (used in the warp reduction).
+__device__ __forceinline__ void two_sum_merge(float &s, float &c, float s2, float c2) {
+    float t = s + s2;
+    float bp = t - s;
+    float err = (s - (t - bp)) + (s2 - bp);
+    s = t;
+    c = c + c2 - err;   // c holds the negated low part (Kahan convention)
+}
+__device__ __forceinline__ void two_sum_merge(double &s, double &c, double s2, double c2) {
+    s += s2;
+    c += c2;
+}
+
+template <typename Real>
+__device__ __forceinline__ Real rsq(Real x);
+template <>
+__device__ __forceinline__ float rsq<float>(float x) { return rsqrtf(x); }
+template <>
+__device__ __forceinline__ double rsq<double>(double x) { return rsqrt(x); }
+
+// SPLINEM (grav.h:53-72) given dir = 1/r.
+template <typename Real>
+__device__ __forceinline__ void spline_m(Real dir, Real r2, Real twoh, Real &a, Real &b) {
+    if (r2 < twoh * twoh) {
+        Real dih = Real(2.0) / twoh;
+        Real u = dih / dir;
+        if (u < Real(1.0)) {
+            a = dih * (Real(7.0 / 5.0) - Real(2.0 / 3.0) * u * u + Real(3.0 / 10.0) * u * u * u * u -
+                       Real(1.0 / 10.0) * u * u * u * u * u);
+            b = dih * dih * dih * (Real(4.0 / 3.0) - Real(6.0 / 5.0) * u * u + Real(0.5) * u * u * u);
+        } else {
+            a = Real(-1.0 / 15.0) * dir +
+                dih * (Real(8.0 / 5.0) - Real(4.0 / 3.0) * u * u + u * u * u -
+                       Real(3.0 / 10.0) * u * u * u * u + Real(1.0 / 30.0) * u * u * u * u * u);
+            b = Real(-1.0 / 15.0) * dir * dir * dir +
+                dih * dih * dih * (Real(8.0 / 3.0) - Real(3.0) * u + Real(6.0 / 5.0) * u * u -
+                                   Real(1.0 / 6.0) * u * u * u);
+        }
+    } else {
+        a = dir;
+        b = a * a * a;
+    }
+}
+
+// SPLINEQ (grav.h:17-51) given dir = 1/r.
+template <typename Real>
+__device__ __forceinline__ void spline_q(Real dir, Real r2, Real twoh, Real &a, Real &b, Real &c,
+                                         Real &d) {
+    if (r2 < twoh * twoh) {
+        Real dih = Real(2.0) / twoh;
+        Real u = dih / dir;
+        Real dih2 = dih * dih, dih3 = dih2 * dih, dih4 = dih2 * dih2, dih5 = dih4 * dih;
+        if (u < Real(1.0)) {
+            a = dih * (Real(7.0 / 5.0) - Real(2.0 / 3.0) * u * u + Real(3.0 / 10.0) * u * u * u * u -
+                       Real(1.0 / 10.0) * u * u * u * u * u);
+            b = dih3 * (Real(4.0 / 3.0) - Real(6.0 / 5.0) * u * u + Real(0.5) * u * u * u);
+            c = dih5 * (Real(12.0 / 5.0) - Real(1.5) * u);
+            d = Real(1.5) * dih5 * dih * dir;
+        } else {
+            Real dir2 = dir * dir, dir3 = dir2 * dir;
+            a = Real(-1.0 / 15.0) * dir +
+                dih * (Real(8.0 / 5.0) - Real(4.0 / 3.0) * u * u + u * u * u -
+                       Real(3.0 / 10.0) * u * u * u * u + Real(1.0 / 30.0) * u * u * u * u * u);
+            b = Real(-1.0 / 15.0) * dir3 +
+                dih3 * (Real(8.0 / 3.0) - Real(3.0) * u + Real(6.0 / 5.0) * u * u -
+                        Real(1.0 / 6.0) * u * u * u);
+            c = Real(-1.0 / 5.0) * dir3 * dir2 + Real(3.0) * dih4 * dir +
+                dih5 * (Real(-12.0 / 5.0) + Real(0.5) * u);
+            d = -dir3 * dir3 * dir + Real(3.0) * dih4 * dir3 - Real(0.5) * dih5 * dih * dir;
+        }
+    } else {
+        a = dir;
+        b = a * a * a;
+        c = Real(3.0) * b * a * a;
+        d = Real(5.0) * c * a * a;
+    }
+}
+
+template <typename Real>
+struct Acc {
+    Real s[4], c[4];     // ax, ay, az, pot (sum and compensation)
+    Real t[4];           // current tile partial
+    Real dt;             // max (m_i + m_j) * b
+};
+
+// Stage P-P entries [0, cnt) of the warp's buffer into shared memory.
+template <typename Real>
+__device__ __forceinline__ void stage_pp(WalkSmem<Real> &S, const TsphDevParts &P, int cnt,
+                                         int lane, float bchx, float bchy, float bchz,
+                                         float bclx, float bcly, float bclz) {
+    for (int e = lane; e < cnt; e += 32) {
+        int ent = S.pp[e];
+        int idx = ent >> 5, rep = ent & 31;
+        if (sizeof(Real) == 4) {
+            float4 a = P.ph[idx], b = P.pl[idx];
+            int r = rep == 31 ? cW.selfRep : rep;
+            S.ex[e] = (Real)(((a.x - bchx) + cW.offh[r][0]) + ((b.x - bclx) + cW.offl[r][0]));
+            S.ey[e] = (Real)(((a.y - bchy) + cW.offh[r][1]) + ((b.y - bcly) + cW.offl[r][1]));
+            S.ez[e] = (Real)(((a.z - bchz) + cW.offh[r][2]) + ((b.z - bclz) + cW.offl[r][2]));
+            S.em[e] = (Real)a.w;
+            S.eh[e] = (Real)b.w;
+        } else {
+            int r = rep == 31 ? cW.selfRep : rep;
+            S.ex[e] = (Real)(P.x[idx] + cW.off[r][0]);
+            S.ey[e] = (Real)(P.y[idx] + cW.off[r][1]);
+            S.ez[e] = (Real)(P.z[idx] + cW.off[r][2]);
+            S.em[e] = (Real)P.m[idx];
+            S.eh[e] = (Real)P.h[idx];
+        }
+    }
+}
+
+// Evaluate staged P-P entries for this lane's particle.
+template <typename Real>
+__device__ __forceinline__ void eval_pp(WalkSmem<Real> &S, int cnt, int i, int slot, int pidx,
+                                        int bucketLo, Acc<Real> &A) {
+    Real xi = S.px[i], yi = S.py[i], zi = S.pz[i], hi = S.ph[i], mi = S.pm[i];
+    for (int e = slot; e < cnt; e += SLOTS) {
+        int ent = S.pp[e];
+        if ((ent & 31) == 31 && (ent >> 5) == bucketLo + i) continue;   // self
+        Real dx = xi - S.ex[e], dy = yi - S.ey[e], dz = zi - S.ez[e];
+        Real d2 = dx * dx + dy * dy + dz * dz;
+        Real me = S.em[e], twoh = hi + S.eh[e];
+        Real dir = rsq<Real>(d2);
+        Real a, b;
+        spline_m<Real>(dir, d2, twoh, a, b);
+        Real idt2 = (mi + me) * b;
+        A.dt = idt2 > A.dt ? idt2 : A.dt;
+        a *= me;
+        b *= me;
+        A.t[3] -= a;
+        A.t[0] -= dx * b;
+        A.t[1] -= dy * b;
+        A.t[2] -= dz * b;
+    }
+    (void)pidx;
+}
+
+// Stage cell entries (Newtonian when soft == 0, else softened).
+template <typename Real>
+__device__ __forceinline__ void stage_cells(WalkSmem<Real> &S, const int *buf, const TsphDevTree &T,
+                                            int cnt, int lane, bool soft, float bchx, float bchy,
+                                            float bchz, float bclx, float bcly, float bclz) {
+    for (int e = lane; e < cnt; e += 32) {
+        int ent = buf[e];
+        int c = ent >> 5, r = ent & 31;
+        Real m, q[6], hc;
+        if (sizeof(Real) == 4) {
+            float4 h4 = T.wcomh[c], l4 = T.wcoml[c];
+            float4 m0 = T.wmom0[c], m1 = T.wmom1[c];
+            S.ex[e] = (Real)(((h4.x - bchx) + cW.offh[r][0]) + ((l4.x - bclx) + cW.offl[r][0]));
+            S.ey[e] = (Real)(((h4.y - bchy) + cW.offh[r][1]) + ((l4.y - bcly) + cW.offl[r][1]));
+            S.ez[e] = (Real)(((h4.z - bchz) + cW.offh[r][2]) + ((l4.z - bclz) + cW.offl[r][2]));
+            m = m0.x; q[0] = m0.y; q[1] = m0.z; q[2] = m0.w; q[3] = m1.x; q[4] = m1.y; q[5] = m1.z;
+            hc = m1.w;
+        } else {
+            S.ex[e] = (Real)(T.r[3 * c] + cW.off[r][0]);
+            S.ey[e] = (Real)(T.r[3 * c + 1] + cW.off[r][1]);
+            S.ez[e] = (Real)(T.r[3 * c + 2] + cW.off[r][2]);
+            m = (Real)T.fMass[c];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) q[k] = (Real)T.Q[6 * c + k];
+            hc = (Real)T.fSoft[c];
+        }
+        if (!soft) {   // reduced (trace-free) quadrupole, SETILIST walk.c:41-48
+            Real tr = q[0] + q[1] + q[2];
+            q[0] -= tr / Real(3.0);
+            q[1] -= tr / Real(3.0);
+            q[2] -= tr / Real(3.0);
+        }
+        S.em[e] = m;
+        S.eh[e] = hc;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) S.q[k][e] = q[k];
+    }
+}
+
+// Newtonian cells, QEVAL at order <= 2 (qeval.h:53-64).
+template <typename Real>
+__device__ __forceinline__ void eval_newt(WalkSmem<Real> &S, int cnt, int i, int slot, int iOrder,
+                                          Acc<Real> &A) {
+    Real xi = S.px[i], yi = S.py[i], zi = S.pz[i], mi = S.pm[i];
+    for (int e = slot; e < cnt; e += SLOTS) {
+        Real dx = xi - S.ex[e], dy = yi - S.ey[e], dz = zi - S.ez[e];
+        Real d2 = dx * dx + dy * dy + dz * dz;
+        Real g0 = rsq<Real>(d2);
+        Real dir2 = g0 * g0;
+        Real g1 = g0 * dir2;
+        Real g2 = Real(3) * g1 * dir2;
+        Real g3 = Real(5) * g2 * dir2;
+        Real m = S.em[e];
+        Real Qta = 0, pot = 0, ax = 0, ay = 0, az = 0;
+        if (iOrder >= 2) {
+            Real xx = S.q[0][e], yy = S.q[1][e], zz = S.q[2][e];
+            Real xy = S.q[3][e], xz = S.q[4][e], yz = S.q[5][e];
+            Real Qmirx = xz * dz + xy * dy + xx * dx;
+            Real Qmiry = yz * dz + xy * dx + yy * dy;
+            Real Qmirz = yz * dy + xz * dx + zz * dz;
+            Real Qmir = Real(0.5) * (Qmirx * dx + Qmiry * dy + Qmirz * dz);
+            pot -= g2 * Qmir;
+            Qta += g3 * Qmir;
+            ax += g2 * Qmirx;
+            ay += g2 * Qmiry;
+            az += g2 * Qmirz;
+        }
+        pot -= g0 * m;
+        Qta += g1 * m;
+        ax -= dx * Qta;
+        ay -= dy * Qta;
+        az -= dz * Qta;
+        A.t[0] += ax;
+        A.t[1] += ay;
+        A.t[2] += az;
+        A.t[3] += pot;
+        Real idt2 = (mi + m) * g1;
+        A.dt = idt2 > A.dt ? idt2 : A.dt;
+    }
+}
+
+// Softened cells with the full quadrupole (grav.c:126-150).
+template <typename Real>
+__device__ __forceinline__ void eval_soft(WalkSmem<Real> &S, int cnt, int i, int slot, Acc<Real> &A) {
+    Real xi = S.px[i], yi = S.py[i], zi = S.pz[i], hi = S.ph[i], mi = S.pm[i];
+    for (int e = slot; e < cnt; e += SLOTS) {
+        Real dx = xi - S.ex[e], dy = yi - S.ey[e], dz = zi - S.ez[e];
+        Real d2 = dx * dx + dy * dy + dz * dz;
+        Real twoh = hi + S.eh[e];
+        Real dir = rsq<Real>(d2);
+        Real a, b, c, d;
+        spline_q<Real>(dir, d2, twoh, a, b, c, d);
+        Real xx = S.q[0][e], yy = S.q[1][e], zz = S.q[2][e];
+        Real xy = S.q[3][e], xz = S.q[4][e], yz = S.q[5][e];
+        Real m = S.em[e];
+        Real qirx = xx * dx + xy * dy + xz * dz;
+        Real qiry = xy * dx + yy * dy + yz * dz;
+        Real qirz = xz * dx + yz * dy + zz * dz;
+        Real qir = Real(0.5) * (qirx * dx + qiry * dy + qirz * dz);
+        Real tr = Real(0.5) * (xx + yy + zz);
+        Real qir3 = b * m + d * qir - c * tr;
+        A.t[3] -= a * m + c * qir - b * tr;
+        A.t[0] -= qir3 * dx - c * qirx;
+        A.t[1] -= qir3 * dy - c * qiry;
+        A.t[2] -= qir3 * dz - c * qirz;
+        Real idt2 = (mi + m) * b;
+        A.dt = idt2 > A.dt ? idt2 : A.dt;
+    }
+}
+
+template <typename Real>
+__device__ __forceinline__ void flush_tile(Acc<Real> &A) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        kahan_add(A.s[k], A.c[k], A.t[k]);
+        A.t[k] = 0;
+    }
+}
+
+template <typename Real>
+__global__ void __launch_bounds__(WPB * 32) k_walk(WalkArgs W) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    WalkSmem<Real> &S = reinterpret_cast<WalkSmem<Real> *>(smraw)[wib];
+    const TsphDevTree &T = W.T;
+    const TsphDevParts &P = W.P;
+    const unsigned FULL = 0xffffffffu;
+    const float u32 = 5.9604645e-08f;   // 2^-24
+    const float relF = 4.0f * u32;
+
+    unsigned long long cPP = 0, cN = 0, cS = 0, cExact = 0, cTests = 0, cBsq = 0, cIntra = 0, cAct = 0;
+
+    for (;;) {
+        int b = 0;
+        if (lane == 0) b = atomicAdd(W.workCounter, 1);
+        b = __shfl_sync(FULL, b, 0);
+        if (b >= W.nBuckets) break;
+        const int node = T.leaves[b];
+        const int lo = T.pLower[node];
+        const int n = T.pUpper[node] - lo + 1;
+        if (n > NB) {
+            // a zero-extent leaf holding more than NB coincident particles
+            if (lane == 0) atomicOr(&W.cnt->status, 1u << TSPH_ERR_UNSUPPORTED);
+            continue;
+        }
+        // bucket geometry (FP64 once per bucket)
+        double bmn[3], bmx[3], bc[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            bmn[k] = T.bnd[6 * node + k];
+            bmx[k] = T.bnd[6 * node + 3 + k];
+            bc[k] = 0.5 * (bmn[k] + bmx[k]);
+        }
+        float bch[3], bcl[3], fbmn[3], fbmx[3];
+        float bext = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            split2f(bc[k], bch[k], bcl[k]);
+            fbmn[k] = (float)(bmn[k] - bc[k]);
+            fbmx[k] = (float)(bmx[k] - bc[k]);
+            bext = fmaxf(bext, fmaxf(fabsf(fbmn[k]), fabsf(fbmx[k])));
+        }
+        double fSoftMax = 0.0;
+        for (int p = lo; p <= lo + n - 1; ++p) fSoftMax = fmax(fSoftMax, P.h[p]);
+        const float fSoftMaxF = (float)fSoftMax;
+        // bucket particles
+        if (lane < NB) {
+            int p = lo + (lane < n ? lane : 0);
+            if (sizeof(Real) == 4) {
+                S.px[lane] = (Real)(float)(P.x[p] - bc[0]);
+                S.py[lane] = (Real)(float)(P.y[p] - bc[1]);
+                S.pz[lane] = (Real)(float)(P.z[p] - bc[2]);
+            } else {
+                S.px[lane] = (Real)P.x[p];
+                S.py[lane] = (Real)P.y[p];
+                S.pz[lane] = (Real)P.z[p];
+            }
+            S.pm[lane] = (Real)P.m[p];
+            S.ph[lane] = (Real)P.h[p];
+        }
+        // initial stack: the root in every replica; P-P buffer: the bucket's
+        // own particles for the intra-bucket pairs (replica tag 31)
+        int sp = 0, ppn = 0, cnn = 0, csn = 0, nPart = 0, nNewt = 0, nSoft = 0;
+        for (int r = lane; r < cW.nRep; r += 32) S.stack[r] = r;   // (0 << 5) | r
+        sp = cW.nRep;
+        if (lane < n) S.pp[lane] = ((lo + lane) << 5) | 31;
+        ppn = n;
+        bool overflow = false;
+        // accumulators: lane = (particle i, slot)
+        const int i = lane % NB, slot = lane / NB;
+        Acc<Real> A;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) { A.s[k] = 0; A.c[k] = 0; A.t[k] = 0; }
+        A.dt = 0;
+        __syncwarp();
+
+        while (sp > 0) {
+            const int take = sp < 32 ? sp : 32;
+            int ent = lane < take ? S.stack[sp - take + lane] : -1;
+            __syncwarp();
+            sp -= take;
+            int act = ACT_NONE, cell = 0, rep = 0, up = -1, cnt = 0, plo = 0;
+            if (ent >= 0) {
+                cell = ent >> 5;
+                rep = ent & 31;
+                int4 lk = T.wlink[cell];
+                plo = lk.x;
+                cnt = lk.y;
+                up = lk.z;
+                float4 ch = T.wcomh[cell], cl = T.wcoml[cell];
+                float rx = ((ch.x - bch[0]) + cW.offh[rep][0]) + ((cl.x - bcl[0]) + cW.offl[rep][0]);
+                float ry = ((ch.y - bch[1]) + cW.offh[rep][1]) + ((cl.y - bcl[1]) + cW.offl[rep][1]);
+                float rz = ((ch.z - bch[2]) + cW.offh[rep][2]) + ((cl.z - bcl[2]) + cW.offl[rep][2]);
+                float dx = fmaxf(fmaxf(fbmn[0] - rx, rx - fbmx[0]), 0.0f);
+                float dy = fmaxf(fmaxf(fbmn[1] - ry, ry - fbmx[1]), 0.0f);
+                float dz = fmaxf(fmaxf(fbmn[2] - rz, rz - fbmx[2]), 0.0f);
+                float D2 = dx * dx + dy * dy + dz * dz;
+                float Sx = fmaxf(fmaxf(fabsf(rx), fabsf(ry)), fabsf(rz)) + bext + cW.offmax;
+                float e = 6.0f * u32 * Sx + cW.E0;
+                float M = 2.0f * e * (dx + dy + dz + 2.0f * e) + 3.0f * e * e + 4.0f * u32 * D2;
+                bool open;
+                int fo = 0;
+                if (cnt < 4) {
+                    open = true;
+                } else {
+                    ++cTests;
+                    fo = filt(D2, M, ch.w, relF);
+                    if (fo == 0) {
+                        ++cExact;
+                        double x = xadd(T.r[3 * cell], cW.off[rep][0]);
+                        double y = xadd(T.r[3 * cell + 1], cW.off[rep][1]);
+                        double z = xadd(T.r[3 * cell + 2], cW.off[rep][2]);
+                        open = intersect_exact(bmn, bmx, T.fOpen2[cell], x, y, z);
+                    } else {
+                        open = fo < 0;
+                    }
+                }
+                if (open) {
+                    if (up >= 0) act = ACT_OPEN;
+                    else if (!(cell == node && rep == cW.selfRep)) act = ACT_LEAF;
+                } else {
+                    // softened or Newtonian (walk.c:122-127)
+                    float a32 = cl.w + fSoftMaxF;
+                    float t2 = a32 * a32;
+                    int fs = filt(t2, 8.0f * u32 * t2, ch.w, relF);   // t2 vs fOpen2
+                    bool newt;
+                    bool exactNeeded = (fs == 0);
+                    if (!exactNeeded) {
+                        if (fs < 0) newt = true;   // twoh2 < fOpen2 (certain)
+                        else {
+                            int fi = filt(D2, M + 8.0f * u32 * t2, t2, relF);
+                            if (fi == 0) exactNeeded = true;
+                            else newt = fi > 0;
+                        }
+                    }
+                    if (exactNeeded) {
+                        ++cExact;
+                        double twoh2 = xadd(T.fSoft[cell], fSoftMax);
+                        twoh2 = xmul(twoh2, twoh2);
+                        if (twoh2 < T.fOpen2[cell]) newt = true;
+                        else {
+                            double x = xadd(T.r[3 * cell], cW.off[rep][0]);
+                            double y = xadd(T.r[3 * cell + 1], cW.off[rep][1]);
+                            double z = xadd(T.r[3 * cell + 2], cW.off[rep][2]);
+                            newt = !intersect_exact(bmn, bmx, twoh2, x, y, z);
+                        }
+                    }
+                    act = newt ? ACT_NEWT : ACT_SOFT;
+                }
+            }
+            // children (upper first so the lower child is popped first)
+            unsigned bo = __ballot_sync(FULL, act == ACT_OPEN);
+            if (sp + 2 * __popc(bo) > STK) { overflow = true; break; }
+            if (act == ACT_OPEN) {
+                int pos = sp + 2 * __popc(bo & lane_lt());
+                S.stack[pos] = (up << 5) | rep;
+                S.stack[pos + 1] = ((cell + 1) << 5) | rep;
+            }
+            sp += 2 * __popc(bo);
+            // leaf particles
+            if (act == ACT_LEAF && cnt > NB) {
+                atomicOr(&W.cnt->status, 1u << TSPH_ERR_UNSUPPORTED);
+                act = ACT_NONE;
+            }
+            int c0 = act == ACT_LEAF ? cnt : 0;
+            int incl = c0;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                int y = __shfl_up_sync(FULL, incl, o);
+                if (lane >= o) incl += y;
+            }
+            int tot = __shfl_sync(FULL, incl, 31);
+            for (int k = 0; k < c0; ++k) S.pp[ppn + incl - c0 + k] = ((plo + k) << 5) | rep;
+            ppn += tot;
+            nPart += tot;
+            unsigned bn = __ballot_sync(FULL, act == ACT_NEWT);
+            if (act == ACT_NEWT) S.cn[cnn + __popc(bn & lane_lt())] = (cell << 5) | rep;
+            cnn += __popc(bn);
+            nNewt += __popc(bn);
+            unsigned bs = __ballot_sync(FULL, act == ACT_SOFT);
+            if (act == ACT_SOFT) S.cs[csn + __popc(bs & lane_lt())] = (cell << 5) | rep;
+            csn += __popc(bs);
+            nSoft += __popc(bs);
+            __syncwarp();
+            // evaluate full tiles
+            while (ppn >= PPF) {
+                stage_pp<Real>(S, P, PPF, lane, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
+                __syncwarp();
+                if (i < n) eval_pp<Real>(S, PPF, i, slot, lo + i, lo, A);
+                flush_tile(A);
+                __syncwarp();
+                for (int e = lane; e < ppn - PPF; e += 32) S.pp[e] = S.pp[PPF + e];
+                ppn -= PPF;
+                __syncwarp();
+            }
+            while (cnn >= CNF) {
+                stage_cells<Real>(S, S.cn, T, CNF, lane, false, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
+                __syncwarp();
+                if (i < n) eval_newt<Real>(S, CNF, i, slot, W.iOrder, A);
+                flush_tile(A);
+                __syncwarp();
+                for (int e = lane; e < cnn - CNF; e += 32) S.cn[e] = S.cn[CNF + e];
+                cnn -= CNF;
+                __syncwarp();
+            }
+            while (csn >= CNF) {
+                stage_cells<Real>(S, S.cs, T, CNF, lane, true, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
+                __syncwarp();
+                if (i < n) eval_soft<Real>(S, CNF, i, slot, A);
+                flush_tile(A);
+                __syncwarp();
+                for (int e = lane; e < csn - CNF; e += 32) S.cs[e] = S.cs[CNF + e];
+                csn -= CNF;
+                __syncwarp();
+            }
+        }
+        if (overflow) {
+            if (lane == 0) atomicOr(&W.cnt->status, 1u << TSPH_ERR_STACK_OVERFLOW);
+            __syncwarp();
+            continue;
+        }
+        // remaining partial tiles
+        if (ppn > 0) {
+            stage_pp<Real>(S, P, ppn, lane, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
+            __syncwarp();
+            if (i < n) eval_pp<Real>(S, ppn, i, slot, lo + i, lo, A);
+            flush_tile(A);
+            __syncwarp();
+        }
+        if (cnn > 0) {
+            stage_cells<Real>(S, S.cn, T, cnn, lane, false, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
+            __syncwarp();
+            if (i < n) eval_newt<Real>(S, cnn, i, slot, W.iOrder, A);
+            flush_tile(A);
+            __syncwarp();
+        }
+        if (csn > 0) {
+            stage_cells<Real>(S, S.cs, T, csn, lane, true, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
+            __syncwarp();
+            if (i < n) eval_soft<Real>(S, csn, i, slot, A);
+            flush_tile(A);
+            __syncwarp();
+        }
+        // reduce the SLOTS partial accumulators of each particle
+#pragma unroll
+        for (int o = NB; o < 32; o <<= 1) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                Real s2 = __shfl_xor_sync(FULL, A.s[k], o);
+                Real c2 = __shfl_xor_sync(FULL, A.c[k], o);
+                two_sum_merge(A.s[k], A.c[k], s2, c2);
+            }
+            Real d2 = __shfl_xor_sync(FULL, A.dt, o);
+            A.dt = d2 > A.dt ? d2 : A.dt;
+        }
+        if (lane < n) {
+            int p = lo + lane;
+            P.ax[p] = (double)A.s[0] - (double)A.c[0];
+            P.ay[p] = (double)A.s[1] - (double)A.c[1];
+            P.az[p] = (double)A.s[2] - (double)A.c[2];
+            P.pot[p] = (double)A.s[3] - (double)A.c[3];
+            P.dtGrav[p] = (double)A.dt;
+        }
+        if (lane == 0) {
+            cAct += n;
+            cPP += (unsigned long long)n * nPart;
+            cN += (unsigned long long)n * nNewt;
+            cS += (unsigned long long)n * nSoft;
+            cBsq += (unsigned long long)n * n;
+            cIntra += (unsigned long long)n * (n - 1) / 2;
+            if (W.bucketLists) {
+                W.bucketLists[4 * b + 0] = node;
+                W.bucketLists[4 * b + 1] = nPart;
+                W.bucketLists[4 * b + 2] = nSoft;
+                W.bucketLists[4 * b + 3] = nNewt;
+            }
+        }
+        __syncwarp();
+    }
+    // counters: tests per lane, the rest on lane 0
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        cTests += __shfl_xor_sync(FULL, cTests, o);
+        cExact += __shfl_xor_sync(FULL, cExact, o);
+    }
+    if (lane == 0) {
+        atomicAdd(&W.cnt->nActive, cAct);
+        atomicAdd(&W.cnt->nPartPP, cPP);
+        atomicAdd(&W.cnt->nCellNewt, cN);
+        atomicAdd(&W.cnt->nCellSoft, cS);
+        atomicAdd(&W.cnt->nBucketSq, cBsq);
+        atomicAdd(&W.cnt->nIntra, cIntra);
+        atomicAdd(&W.cnt->nTests, cTests);
+        atomicAdd(&W.cnt->nExactTests, cExact);
+    }
+}
+
+int tsph_walk_interact(tsph_ctx *ctx, const tsph_grav_params *gp) {
+    if (gp->iOrder < 1 || gp->iOrder > 2) return TSPH_ERR_UNSUPPORTED;
+    if (gp->bPeriodic && gp->nReps > 1) return TSPH_ERR_UNSUPPORTED;
+    if (gp->nBucket > NB) return TSPH_ERR_UNSUPPORTED;
+    WalkConst wc;
+    memset(&wc, 0, sizeof(wc));
+    int nR = gp->bPeriodic ? gp->nReps : 0;
+    int side = 2 * nR + 1;
+    wc.nRep = side * side * side;
+    wc.selfRep = wc.nRep / 2;
+    double L = gp->bPeriodic ? gp->dPeriod : 0.0;
+    float offmax = 0.0f;
+    double rabs = 0.0;
+    for (int ix = -nR, r = 0; ix <= nR; ++ix)
+        for (int iy = -nR; iy <= nR; ++iy)
+            for (int iz = -nR; iz <= nR; ++iz, ++r) {
+                int id[3] = {ix, iy, iz};
+                for (int k = 0; k < 3; ++k) {
+                    wc.off[r][k] = id[k] * L;
+                    wc.offh[r][k] = (float)wc.off[r][k];
+                    wc.offl[r][k] = (float)(wc.off[r][k] - (double)wc.offh[r][k]);
+                    offmax = fmaxf(offmax, fabsf(wc.offh[r][k]));
+                }
+            }
+    wc.offmax = offmax;
+    // absolute error floor of hi/lo coordinates: a few ulp^2 of the largest
+    // absolute coordinate (positions + offsets)
+    rabs = ctx->dPeriodTree + offmax;
+    wc.E0 = (float)(16.0 * 3.552713678800501e-15 * rabs) + 1e-30f;
+    cudaMemcpyToSymbolAsync(cW, &wc, sizeof(wc), 0, cudaMemcpyHostToDevice, ctx->stream);
+    TSPH_LAUNCH_CK("cW");
+
+    WalkArgs A;
+    A.T = ctx->T;
+    A.P = ctx->P;
+    A.cnt = ctx->dCnt;
+    A.nBuckets = ctx->T.nLeaves;
+    A.iOrder = gp->iOrder;
+    int rc = TSPH_OK;
+    if (ctx->bucketListCap < A.nBuckets) {
+        rc = tsph_grow(ctx, &ctx->dBucketLists, (size_t)4 * A.nBuckets + 64);
+        if (rc) return rc;
+        ctx->bucketListCap = A.nBuckets;
+    }
+    A.bucketLists = ctx->dBucketLists;
+    // work counter lives in the counters block's pad area
+    A.workCounter = (int *)&ctx->dCnt->pad;
+    TSPH_CK(cudaMemsetAsync(A.workCounter, 0, sizeof(int), ctx->stream));
+    int blocks = ctx->smCount * 4;
+    if (gp->precision == TSPH_FP32) {
+        size_t sm = sizeof(WalkSmem<float>) * WPB;
+        TSPH_CK(cudaFuncSetAttribute(k_walk<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        k_walk<float><<<blocks, WPB * 32, sm, ctx->stream>>>(A);
+        TSPH_LAUNCH_CK("k_walk<float>");
+    } else {
+        size_t sm = sizeof(WalkSmem<double>) * WPB;
+        TSPH_CK(cudaFuncSetAttribute(k_walk<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        k_walk<double><<<blocks, WPB * 32, sm, ctx->stream>>>(A);
+        TSPH_LAUNCH_CK("k_walk<double>");
+    }
+    return TSPH_OK;
+}

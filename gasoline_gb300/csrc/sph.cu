@@ -1,0 +1,887 @@
+// K6-K10: SPH smoothing lengths, density/velocity-gradient gather, gas
+// pressure, symmetric pressure/viscosity gather, kick and drift.
+//
+// Reference semantics:
+//   smSmooth (smooth.c:1439-1713): fBall2 = the nSmooth-th smallest squared
+//     distance, self included, distances dx = x - q.r, d2 = dx*dx+dy*dy+dz*dz
+//     (smooth.c:639-642), periodic images chosen per axis (smooth.h:291-390);
+//   DenDVDX (smoothfcn.c:3390-3627) with the M4 kernel (smoothfcn.c:200-214);
+//   pkdGasPressure (pkd.c:5750-5785), adiabatic, no Jeans floor;
+//   SphPressureTermsSym (smoothfcn.c:2276-2385, SphPressureTerms.h) over
+//     every pair with d2 <= fBall2 of either particle, summed from both sides.
+//
+// GB300 mapping: a gas-only kd-tree (the same device builder as gravity) and
+// one warp per gas particle.  The kNN is a ball gather around a seed radius
+// (the learned-h prediction when present, else the box of the deepest tree
+// cell holding >= nSmooth particles) followed by an exact radix select of
+// the nSmooth-th squared distance over the candidates' FP64 bit patterns;
+// a ball holding fewer than nSmooth grows and retries (the fallback), so
+// the neighbour set and fBall2 equal the exact kNN's.  Squared distances
+// are FP64 without FMA contraction, exactly as the reference rounds them.
+// The pressure pass gathers both roles of every pair (i in N(j) found via
+// a per-node max fBall2 bound), so no scatter-adds and no atomics: results
+// are deterministic run to run.
+#include <float.h>
+#include <math.h>
+
+#include "tsph_ctx.cuh"
+
+#define SW 4          // warps per block
+#define SSTK 1024     // walk stack per warp
+#define SCAP 1024     // kNN candidate capacity per warp
+#define SMAXIT 48     // radius iterations before giving up
+
+struct SphConst {
+    int ngas, k;
+    int bPeriodic;
+    double L;
+    double alpha, beta, gamma, gammam1, dtFacCourant;
+    int limiter;
+    float margin;     // absolute slack for FP32 box-distance pruning
+};
+__constant__ SphConst cS;
+
+__device__ __forceinline__ unsigned lane_lt_s() {
+    unsigned r;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(r));
+    return r;
+}
+
+// query coordinate shifted to the image of q nearest to it (x, x+L or x-L)
+__device__ __forceinline__ double img_q(double x, double q) {
+    if (!cS.bPeriodic) return x;
+    double d0 = fabs(x - q), dp = fabs((x + cS.L) - q), dm = fabs((x - cS.L) - q);
+    if (dp < d0 && dp <= dm) return x + cS.L;
+    if (dm < d0 && dm < dp) return x - cS.L;
+    return x;
+}
+
+// exact squared distance as the reference computes it, with dx = sx - q
+__device__ __forceinline__ double dist2_exact(double x, double y, double z, double qx, double qy,
+                                              double qz, double &dx, double &dy, double &dz) {
+    double sx = img_q(x, qx), sy = img_q(y, qy), sz = img_q(z, qz);
+    dx = xsub(sx, qx);
+    dy = xsub(sy, qy);
+    dz = xsub(sz, qz);
+    return xadd(xadd(xmul(dx, dx), xmul(dy, dy)), xmul(dz, dz));
+}
+
+// conservative FP32 squared distance from a point to a node box
+__device__ __forceinline__ float box_d2f(float x, float y, float z, float4 lo, float4 hi) {
+    float p[3] = {x, y, z}, a[3] = {lo.x, lo.y, lo.z}, b[3] = {hi.x, hi.y, hi.z};
+    float d2 = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        float d = fmaxf(fmaxf(a[k] - p[k], p[k] - b[k]), 0.0f);
+        if (cS.bPeriodic) {
+            float L = (float)cS.L;
+            float d1 = fmaxf(fmaxf(a[k] - (p[k] + L), (p[k] + L) - b[k]), 0.0f);
+            float d2b = fmaxf(fmaxf(a[k] - (p[k] - L), (p[k] - L) - b[k]), 0.0f);
+            d = fminf(d, fminf(d1, d2b));
+        }
+        d = fmaxf(d - cS.margin, 0.0f);
+        d2 += d * d;
+    }
+    return d2;
+}
+
+__device__ __forceinline__ double kern_m4(double ar2) {
+    double ak = 2.0 - sqrt(ar2);
+    if (ar2 < 1.0) ak = (1.0 - 0.75 * ak * ar2);
+    else ak = 0.25 * ak * ak * ak;
+    return ak;
+}
+__device__ __forceinline__ double dkern_m4(double ar2) {
+    double adk = sqrt(ar2);
+    if (ar2 < 1.0) adk = -3 + 2.25 * adk;
+    else adk = -0.75 * (2.0 - adk) * (2.0 - adk) / adk;
+    return adk;
+}
+
+__device__ __forceinline__ double wsum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+struct SphArgs {
+    TsphDevTree T;          // gas tree: wcomh = box min, wcoml = box max (float)
+    TsphDevParts G;
+    TsphSphBufs S;
+    TsphDevCounters *cnt;
+    int *work;
+    const double *seed;     // optional fBall2 seeds (tree order) or null
+};
+
+struct KnnSmem {
+    int stack[SSTK];
+    double d2[SCAP];
+    int idx[SCAP];
+};
+
+// Ball gather of all gas particles with d2 <= r2 around particle i.
+// Returns the count, or -1 when it exceeds SCAP or the stack overflows.
+__device__ int ball_gather(KnnSmem &W, const SphArgs &A, int lane, double xi, double yi, double zi,
+                           float xf, float yf, float zf, double r2) {
+    const unsigned FULL = 0xffffffffu;
+    int sp = 1, nc = 0;
+    if (lane == 0) W.stack[0] = 0;
+    __syncwarp();
+    float r2f = (float)r2 * 1.00001f;
+    bool bad = false;
+    while (sp > 0) {
+        int take = sp < 32 ? sp : 32;
+        int node = lane < take ? W.stack[sp - take + lane] : -1;
+        __syncwarp();
+        sp -= take;
+        bool open = false, leaf = false;
+        int4 lk = make_int4(0, 0, -1, 0);
+        if (node >= 0) {
+            lk = A.T.wlink[node];
+            float d2 = box_d2f(xf, yf, zf, A.T.wcomh[node], A.T.wcoml[node]);
+            if (d2 <= r2f) {
+                if (lk.z >= 0) open = true;
+                else leaf = true;
+            }
+        }
+        unsigned bo = __ballot_sync(FULL, open);
+        if (sp + 2 * __popc(bo) > SSTK) { bad = true; break; }
+        if (open) {
+            int pos = sp + 2 * __popc(bo & lane_lt_s());
+            W.stack[pos] = lk.z;
+            W.stack[pos + 1] = node + 1;
+        }
+        sp += 2 * __popc(bo);
+        // leaf particles, in a fixed order (leaf-lane major, particle minor)
+        int cnt = leaf ? lk.y : 0;
+        int maxc = __reduce_max_sync(FULL, (unsigned)cnt);
+        for (int k = 0; k < maxc; ++k) {
+            bool in = false;
+            double d2 = 0.0;
+            int j = lk.x + k;
+            if (k < cnt) {
+                double dx, dy, dz;
+                d2 = dist2_exact(xi, yi, zi, A.G.x[j], A.G.y[j], A.G.z[j], dx, dy, dz);
+                in = d2 <= r2;
+            }
+            unsigned bi = __ballot_sync(FULL, in);
+            if (nc + __popc(bi) > SCAP) { bad = true; }
+            else if (in) {
+                int pos = nc + __popc(bi & lane_lt_s());
+                W.d2[pos] = d2;
+                W.idx[pos] = j;
+            }
+            nc += __popc(bi);
+        }
+        __syncwarp();
+        if (bad) break;
+    }
+    __syncwarp();
+    return bad ? -1 : nc;
+}
+
+// k-th smallest of the candidates' squared distances: an MSB-first search
+// on the bit patterns (non-negative doubles order like their bits).
+__device__ double select_kth(const KnnSmem &W, int nc, int k, int lane) {
+    unsigned long long prefix = 0ULL;
+    for (int bit = 62; bit >= 0; --bit) {
+        unsigned long long cand = prefix | (1ULL << bit);
+        int c = 0;
+        for (int e = lane; e < nc; e += 32)
+            c += ((unsigned long long)__double_as_longlong(W.d2[e]) < cand) ? 1 : 0;
+        c = __reduce_add_sync(0xffffffffu, (unsigned)c);
+        if (c < k) prefix = cand;
+    }
+    return __longlong_as_double((long long)prefix);
+}
+
+__global__ void __launch_bounds__(SW * 32) k_knn_density(SphArgs A) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    KnnSmem &W = reinterpret_cast<KnnSmem *>(smraw)[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    const unsigned FULL = 0xffffffffu;
+    const int ng = cS.ngas, k = cS.k;
+    unsigned long long nFall = 0, nPairs = 0;
+    for (;;) {
+        int i = 0;
+        if (lane == 0) i = atomicAdd(A.work, 1);
+        i = __shfl_sync(FULL, i, 0);
+        if (i >= ng) break;
+        const double xi = A.G.x[i], yi = A.G.y[i], zi = A.G.z[i];
+        const float xf = (float)xi, yf = (float)yi, zf = (float)zi;
+        // seed radius
+        double r2;
+        if (A.seed && A.seed[i] > 0.0) {
+            r2 = A.seed[i];
+        } else {
+            int node = 0;
+            for (;;) {
+                int up = A.T.upper[node];
+                if (up < 0) break;
+                int child = (i >= A.T.pLower[up]) ? up : node + 1;
+                if (A.T.pUpper[child] - A.T.pLower[child] + 1 < k) break;
+                node = child;
+            }
+            r2 = 0.0;
+            const double *b = &A.T.bnd[6 * node];
+            double p[3] = {xi, yi, zi};
+            for (int a = 0; a < 3; ++a) {
+                double d = fmax(fabs(p[a] - b[a]), fabs(p[a] - b[3 + a]));
+                r2 += d * d;
+            }
+            r2 = r2 * (1.0 + 1e-9) + 1e-300;
+        }
+        double lo2 = 0.0, hi2 = 0.0;   // radii known too small / too large
+        int nc = -1, it = 0;
+        for (; it < SMAXIT; ++it) {
+            nc = ball_gather(W, A, lane, xi, yi, zi, xf, yf, zf, r2);
+            if (nc < 0) {                       // too many candidates: shrink
+                hi2 = r2;
+                r2 = lo2 > 0.0 ? sqrt(lo2 * hi2) : 0.5 * r2;
+            } else if (nc < k) {                // too few: grow (the fallback)
+                lo2 = r2;
+                r2 = hi2 > 0.0 ? sqrt(lo2 * hi2) : 2.25 * r2;
+                ++nFall;
+            } else {
+                break;
+            }
+        }
+        if (it == SMAXIT) {
+            if (lane == 0) atomicOr(&A.cnt->status, 1u << TSPH_ERR_KNN_NO_CONVERGE);
+            continue;
+        }
+        double fBall2 = select_kth(W, nc, k, lane);
+        // DenDVDX over N(i) = {j : d2 <= fBall2} (smoothfcn.c:3390-3627)
+        const double vxi = A.S.vx[i], vyi = A.S.vy[i], vzi = A.S.vz[i];
+        double ih2 = 4.0 / fBall2, ih = sqrt(ih2);
+        double fNorm = M_1_PI * ih2 * ih;
+        double s[14];
+#pragma unroll
+        for (int q = 0; q < 14; ++q) s[q] = 0.0;
+        int nn = 0;
+        unsigned long long hsh = 0ULL;
+        for (int e = lane; e < nc; e += 32) {
+            double d2 = W.d2[e];
+            if (d2 > fBall2) continue;
+            int j = W.idx[e];
+            ++nn;
+            unsigned long long hx = (unsigned long long)(A.G.iord[j] + 1);
+            hx *= 0x9E3779B97F4A7C15ULL;
+            hx ^= hx >> 29;
+            hx *= 0xBF58476D1CE4E5B9ULL;
+            hx ^= hx >> 32;
+            hsh += hx;
+            double dx, dy, dz;
+            dist2_exact(xi, yi, zi, A.G.x[j], A.G.y[j], A.G.z[j], dx, dy, dz);
+            double r2k = d2 * ih2;
+            double mj = A.G.m[j];
+            double rs = kern_m4(r2k);
+            s[0] += rs * mj;
+            double rs1 = dkern_m4(r2k) * mj;
+            double dvx = (-vxi + A.S.vx[j]), dvy = (-vyi + A.S.vy[j]), dvz = (-vzi + A.S.vz[j]);
+            s[1] += dvx * dx * rs1; s[2] += dvx * dy * rs1; s[3] += dvx * dz * rs1;
+            s[4] += dvy * dx * rs1; s[5] += dvy * dy * rs1; s[6] += dvy * dz * rs1;
+            s[7] += dvz * dx * rs1; s[8] += dvz * dy * rs1; s[9] += dvz * dz * rs1;
+            s[10] += (dx * dx + dy * dy + dz * dz) * rs1;
+            double uj = A.S.u[j];
+            s[11] += uj * dx * rs1;
+            s[12] += uj * dy * rs1;
+            s[13] += uj * dz * rs1;
+        }
+#pragma unroll
+        for (int q = 0; q < 14; ++q) s[q] = wsum(s[q]);
+        nn = __reduce_add_sync(FULL, (unsigned)nn);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) hsh += __shfl_xor_sync(FULL, hsh, o);
+        if (lane == 0) {
+            const double H = 0.0;
+            double fDensity = s[0] * fNorm;
+            double dvxdx = s[1], dvxdy = s[2], dvxdz = s[3], dvydx = s[4], dvydy = s[5],
+                   dvydz = s[6], dvzdx = s[7], dvzdy = s[8], dvzdz = s[9];
+            double divvnorm = s[10], grx = s[11], gry = s[12], grz = s[13];
+            double trace = dvxdx + dvydy + dvzdz;
+            double fNorm1 = (divvnorm != 0 ? 3 / fabs(divvnorm) : 0);
+            double divv = fNorm1 * trace + 3 * H;
+            double cx = fNorm1 * (dvzdy - dvydz), cy = fNorm1 * (dvxdz - dvzdx),
+                   cz = fNorm1 * (dvydx - dvxdy);
+            double Hcorr = (fNorm1 != 0 ? H / fNorm1 : 0);
+            double gnorm = grx * grx + gry * gry + grz * grz;
+            if (gnorm > 0) gnorm = 1 / sqrt(gnorm);
+            grx *= gnorm; gry *= gnorm; grz *= gnorm;
+            double dvdr = (((dvxdx + Hcorr) * grx + dvxdy * gry + dvxdz * grz) * grx +
+                           (dvydx * grx + (dvydy + Hcorr) * gry + dvydz * grz) * gry +
+                           (dvzdx * grx + dvzdy * gry + (dvzdz + Hcorr) * grz) * grz) * fNorm1;
+            double dvds = (divv < 0 ? 1.5 * (dvdr - (1. / 3.) * divv) : dvdr);
+            double bal;
+            if (cS.limiter == 1) {
+                bal = divv != 0.0 ? fabs(divv) / (fabs(divv) + sqrt(cx * cx + cy * cy + cz * cz)) : 0.0;
+            } else {
+                bal = 1.0;
+            }
+            double ot = (1. / 3.) * trace;
+            double sxx = dvxdx - ot, syy = dvydy - ot, szz = dvzdz - ot;
+            double sxy = 0.5 * (dvxdy + dvydx), sxz = 0.5 * (dvxdz + dvzdx), syz = 0.5 * (dvydz + dvzdy);
+            double S2 = fNorm1 * fNorm1 * (sxx * sxx + syy * syy + szz * szz +
+                                           2 * (sxy * sxy + sxz * sxz + syz * syz));
+            A.S.fBall2[i] = fBall2;
+            A.S.rho[i] = fDensity;
+            A.S.divv[i] = divv;
+            A.S.curl[3 * i] = cx;
+            A.S.curl[3 * i + 1] = cy;
+            A.S.curl[3 * i + 2] = cz;
+            A.S.dvds[i] = dvds;
+            A.S.bal[i] = bal;
+            A.S.diff[i] = 0.25 * fBall2 * sqrt(2 * S2);
+            A.S.nnCount[i] = nn;
+            A.S.nnHash[i] = hsh;
+            nPairs += nn;
+        }
+        __syncwarp();
+    }
+    if (lane == 0) {
+        if (nFall) atomicAdd(&A.cnt->nExactTests, nFall);
+        if (nPairs) atomicAdd(&A.cnt->nPartPP, nPairs);
+    }
+}
+
+// pkdGasPressure (pkd.c:5750-5785) for the adiabatic gas model.
+__global__ void k_gas_pressure(int ng, TsphSphBufs S) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ng) return;
+    double PoverRhoGas = cS.gammam1 * S.u[i];
+    double cGas = sqrt(cS.gamma * PoverRhoGas);
+    double PoverRho = PoverRhoGas + 0.0;
+    S.pr2[i] = PoverRho / S.rho[i];
+    double c = sqrt(cGas * cGas + (5. / 3.) * 0.0 + 2.0 * 0.0);
+    S.cs[i] = c;
+    double dt = cS.dtFacCourant * sqrt(S.fBall2[i] * 0.25) / (2 * c);
+    double dtp = FLT_MAX;
+    if (dt < dtp) dtp = dt;
+    S.dtp[i] = dtp;
+}
+
+// per gas-tree node: max fBall2 of its particles (atomicMax on the bits)
+__global__ void k_node_ball(int ng, TsphDevTree T, const double *__restrict__ fBall2,
+                            unsigned long long *nodeBall2) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    bool live = p < ng;
+    unsigned long long key = live ? (unsigned long long)__double_as_longlong(fBall2[p]) : 0ULL;
+    int i = 0;
+    unsigned mask = __ballot_sync(0xffffffffu, live);
+    while (mask) {
+        if (live) {
+            unsigned grp = __match_any_sync(mask, i);
+            unsigned hiw = (unsigned)(key >> 32), low = (unsigned)key;
+            unsigned mh = __reduce_max_sync(grp, hiw);
+            unsigned ml = __reduce_max_sync(grp, hiw == mh ? low : 0u);
+            if ((int)(threadIdx.x & 31) == __ffs(grp) - 1)
+                atomicMax(&nodeBall2[i], ((unsigned long long)mh << 32) | ml);
+            int up = T.upper[i];
+            if (up < 0) live = false;
+            else i = (p >= T.pLower[up]) ? up : i + 1;
+        }
+        mask = __ballot_sync(0xffffffffu, live);
+    }
+}
+
+// SphPressureTermsSym as a gather over both roles of every pair.
+__global__ void __launch_bounds__(SW * 32) k_pressure(SphArgs A) {
+    __shared__ int stackAll[SW][SSTK];
+    int *stack = stackAll[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    const unsigned FULL = 0xffffffffu;
+    const int ng = cS.ngas;
+    const double aFac = 1.0, vFac = 1.0, H = 0.0;
+    for (;;) {
+        int i = 0;
+        if (lane == 0) i = atomicAdd(A.work, 1);
+        i = __shfl_sync(FULL, i, 0);
+        if (i >= ng) break;
+        const double xi = A.G.x[i], yi = A.G.y[i], zi = A.G.z[i];
+        const float xf = (float)xi, yf = (float)yi, zf = (float)zi;
+        const double fbi = A.S.fBall2[i];
+        const TsphSphBufs &S = A.S;
+        double ax = 0, ay = 0, az = 0, uPdV = 0, uAV = 0, mu = 0.0, dtN = FLT_MAX;
+        int sp = 1;
+        if (lane == 0) stack[0] = 0;
+        __syncwarp();
+        bool bad = false;
+        while (sp > 0) {
+            int take = sp < 32 ? sp : 32;
+            int node = lane < take ? stack[sp - take + lane] : -1;
+            __syncwarp();
+            sp -= take;
+            bool open = false, leaf = false;
+            int4 lk = make_int4(0, 0, -1, 0);
+            if (node >= 0) {
+                lk = A.T.wlink[node];
+                double nb = __longlong_as_double((long long)S.nodeBall2[node]);
+                float bound = (float)(nb > fbi ? nb : fbi) * 1.00001f;
+                float d2 = box_d2f(xf, yf, zf, A.T.wcomh[node], A.T.wcoml[node]);
+                if (d2 <= bound) {
+                    if (lk.z >= 0) open = true;
+                    else leaf = true;
+                }
+            }
+            unsigned bo = __ballot_sync(FULL, open);
+            if (sp + 2 * __popc(bo) > SSTK) { bad = true; break; }
+            if (open) {
+                int pos = sp + 2 * __popc(bo & lane_lt_s());
+                stack[pos] = lk.z;
+                stack[pos + 1] = node + 1;
+            }
+            sp += 2 * __popc(bo);
+            int cnt = leaf ? lk.y : 0;
+            for (int kk = 0; kk < cnt; ++kk) {
+                int j = lk.x + kk;
+                double xj = A.G.x[j], yj = A.G.y[j], zj = A.G.z[j];
+                double dxi, dyi, dzi, dxj, dyj, dzj;
+                double d2i = dist2_exact(xi, yi, zi, xj, yj, zj, dxi, dyi, dzi);
+                double d2j = dist2_exact(xj, yj, zj, xi, yi, zi, dxj, dyj, dzj);
+                double fbj = S.fBall2[j];
+                bool inI = d2i <= fbi, inJ = d2j <= fbj;
+                if (!inI && !inJ) continue;
+                for (int role = 0; role < 2; ++role) {
+                    if (role == 0 && !inI) continue;
+                    if (role == 1 && !inJ) continue;
+                    // p = owner of the ball, q = the other particle
+                    int p = role == 0 ? i : j, q = role == 0 ? j : i;
+                    double dx = role == 0 ? dxi : dxj, dy = role == 0 ? dyi : dyj,
+                           dz = role == 0 ? dzi : dzj;
+                    double fDist2 = role == 0 ? d2i : d2j;
+                    double fbp = S.fBall2[p];
+                    double pc = S.cs[p], pMass = A.G.m[p], pDensity = S.rho[p];
+                    double pPoverRho2 = S.pr2[p], pd2 = pDensity * pDensity;
+                    double pPoverRho2f = (pPoverRho2 * pd2 + 0) / pd2;
+                    double ph = sqrt(0.25 * fbp);
+                    double ih2 = 4.0 / fbp;
+                    double fNorm = 0.5 * M_1_PI * ih2 / ph;
+                    double fNorm1 = fNorm * ih2;
+                    double r2 = fDist2 * ih2;
+                    double rs1 = dkern_m4(r2) * fNorm1;
+                    double rp = rs1 * pMass, rq = rs1 * A.G.m[q];
+                    double dvx = S.vx[p] - S.vx[q], dvy = S.vy[p] - S.vy[q], dvz = S.vz[p] - S.vz[q];
+                    double dvdotdr = vFac * (dvx * dx + dvy * dy + dvz * dz) + fDist2 * H;
+                    double qPoverRho2 = S.pr2[q], qd2 = S.rho[q] * S.rho[q];
+                    double qPoverRho2f = (qPoverRho2 * qd2 + 0) / qd2;
+                    double qc = S.cs[q];
+                    double Acc, dt;
+                    if (role == 0) {
+                        uPdV += rq * pPoverRho2 * dvdotdr;
+                        Acc = pPoverRho2f + qPoverRho2f;
+                    } else {
+                        uPdV += rp * qPoverRho2 * dvdotdr;
+                        Acc = qPoverRho2f + pPoverRho2f;
+                    }
+                    if (dvdotdr >= 0.0) {
+                        dt = cS.dtFacCourant * ph / (2 * (pc > qc ? pc : qc));
+                    } else {
+                        double absmu = -dvdotdr * aFac / sqrt(fDist2);
+                        if (absmu > mu) mu = absmu;
+                        double visc = (cS.alpha * (pc + qc) + cS.beta * 1.5 * absmu);
+                        dt = cS.dtFacCourant * ph / (0.625 * (pc + qc) + 0.375 * visc);
+                        visc = (0.5 * (S.bal[p] + S.bal[q])) * visc * absmu / (pDensity + S.rho[q]);
+                        if (role == 0) uAV += rq * (0.5 * visc) * dvdotdr;
+                        else uAV += rp * (0.5 * visc) * dvdotdr;
+                        Acc += visc;
+                    }
+                    if (role == 0) {
+                        Acc *= rq * aFac;
+                        ax -= Acc * dx; ay -= Acc * dy; az -= Acc * dz;
+                        if (dt < dtN) dtN = dt;
+                        if (4 * S.dtp[q] < dtN) dtN = 4 * S.dtp[q];
+                    } else {
+                        Acc *= rp * aFac;
+                        ax += Acc * dx; ay += Acc * dy; az += Acc * dz;
+                        if (dt < dtN) dtN = dt;
+                        if (4 * S.dtp[p] < dtN) dtN = 4 * S.dtp[p];
+                    }
+                }
+            }
+            __syncwarp();
+        }
+        if (bad) {
+            if (lane == 0) atomicOr(&A.cnt->status, 1u << TSPH_ERR_STACK_OVERFLOW);
+            continue;
+        }
+        ax = wsum(ax); ay = wsum(ay); az = wsum(az); uPdV = wsum(uPdV); uAV = wsum(uAV);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            double a = __shfl_xor_sync(FULL, mu, o);
+            double b = __shfl_xor_sync(FULL, dtN, o);
+            mu = a > mu ? a : mu;
+            dtN = b < dtN ? b : dtN;
+        }
+        if (lane == 0) {
+            S.hax[i] = ax; S.hay[i] = ay; S.haz[i] = az;
+            S.uPdV[i] = uPdV; S.uAV[i] = uAV; S.mumax[i] = mu; S.dtNew[i] = dtN;
+        }
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// gathers/scatters between caller order and gas-tree order
+// ---------------------------------------------------------------------------
+__global__ void k_gas_identity(int ng, int *iord) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < ng) iord[i] = i;
+}
+
+__global__ void k_gas_gather_pos(int ng, TsphDevState C, TsphDevParts G) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ng) return;
+    int o = G.iord[i];
+    G.x[i] = C.x[o]; G.y[i] = C.y[o]; G.z[i] = C.z[o];
+    G.m[i] = C.m[o]; G.h[i] = C.h[o];
+}
+
+__global__ void k_gas_gather_vel(int ng, TsphDevState C, const int *__restrict__ iord, TsphSphBufs S) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ng) return;
+    int o = iord[i];
+    S.vx[i] = C.vpx[o]; S.vy[i] = C.vpy[o]; S.vz[i] = C.vpz[o];
+    S.u[i] = C.upred[o];
+}
+
+// FP32 node boxes for the gas walks (stored in wcomh/wcoml of the gas tree)
+__global__ void k_gas_nodes(int nNodes, TsphDevTree T) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nNodes) return;
+    const double *b = &T.bnd[6 * i];
+    T.wcomh[i] = make_float4((float)b[0], (float)b[1], (float)b[2], 0.0f);
+    T.wcoml[i] = make_float4((float)b[3], (float)b[4], (float)b[5], 0.0f);
+    T.wlink[i] = make_int4(T.pLower[i], T.pUpper[i] - T.pLower[i] + 1, T.upper[i], 0);
+}
+
+__global__ void k_scatter_hydro(int ng, const int *__restrict__ iord, TsphSphBufs S, TsphDevState C) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ng) return;
+    int o = iord[i];
+    C.hax[o] = S.hax[i]; C.hay[o] = S.hay[i]; C.haz[o] = S.haz[i];
+    C.udot[o] = S.uPdV[i] + S.uAV[i];
+}
+
+__global__ void k_to_caller1(int ng, const int *__restrict__ iord, const double *__restrict__ a,
+                             int stride, int off, double *dst, int dstride, int doff) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ng) return;
+    dst[dstride * iord[i] + doff] = a[stride * i + off];
+}
+
+__global__ void k_load_vel(int n, const double *__restrict__ v3, TsphDevState C) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    C.vx[i] = C.vpx[i] = v3[3 * i];
+    C.vy[i] = C.vpy[i] = v3[3 * i + 1];
+    C.vz[i] = C.vpz[i] = v3[3 * i + 2];
+}
+
+__global__ void k_load_u(int ng, TsphDevState C) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ng) return;
+    C.upred[i] = C.u[i];
+    C.udot[i] = 0.0;
+}
+
+static void set_sph_const(tsph_ctx *ctx, const tsph_sph_params *sp) {
+    SphConst c;
+    memset(&c, 0, sizeof(c));
+    c.ngas = ctx->ngas;
+    c.k = sp->nSmooth < ctx->ngas ? sp->nSmooth : ctx->ngas;
+    c.bPeriodic = sp->bPeriodic;
+    c.L = sp->dPeriod;
+    c.alpha = sp->alpha;
+    c.beta = sp->beta;
+    c.gamma = sp->gamma;
+    c.gammam1 = sp->gamma - 1;
+    c.dtFacCourant = sp->dEtaCourant * 1.0 * 2 / 1.6;   // pkdDtFacCourant, a = 1
+    c.limiter = sp->iViscosityLimiter;
+    // FP32 box tests: pad by a few ulps of the largest coordinate
+    double bnd[6];
+    cudaMemcpy(bnd, ctx->TG.bnd, sizeof(bnd), cudaMemcpyDeviceToHost);
+    double r = 0;
+    for (int k = 0; k < 6; ++k) r = fmax(r, fabs(bnd[k]));
+    if (sp->bPeriodic) r += sp->dPeriod;
+    c.margin = (float)(8.0 * 5.960464477539063e-08 * r) + 1e-30f;
+    cudaMemcpyToSymbolAsync(cS, &c, sizeof(c), 0, cudaMemcpyHostToDevice, ctx->stream);
+}
+
+extern "C" int tsph_set_velocities(tsph_ctx *ctx, const double *vel, int ngas, const double *u) {
+    if (!ctx || !vel || ngas < 0) return TSPH_ERR_ARG;
+    if (!ctx->haveParts) return TSPH_ERR_STATE;
+    if (ngas > ctx->n || (ngas > 0 && !u)) return TSPH_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    const int n = ctx->n;
+    ctx->ngas = ngas;
+    ctx->G.n = ngas;
+    ctx->S.haveDensity = ctx->S.havePressure = false;
+    if (n == 0) { ctx->haveVel = true; return TSPH_OK; }
+    TSPH_CK(cudaMemcpyAsync(ctx->dStage, vel, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
+    k_load_vel<<<tsph_blocks(n, 256), 256, 0, ctx->stream>>>(n, ctx->dStage, ctx->C);
+    TSPH_LAUNCH_CK("k_load_vel");
+    if (ngas > 0) {
+        TSPH_CK(cudaMemcpyAsync(ctx->C.u, u, sizeof(double) * ngas, cudaMemcpyHostToDevice, ctx->stream));
+        k_load_u<<<tsph_blocks(ngas, 256), 256, 0, ctx->stream>>>(ngas, ctx->C);
+        TSPH_LAUNCH_CK("k_load_u");
+        k_gas_identity<<<tsph_blocks(ngas, 256), 256, 0, ctx->stream>>>(ngas, ctx->G.iord);
+        TSPH_LAUNCH_CK("k_gas_identity");
+    }
+    ctx->haveVel = true;
+    return TSPH_OK;
+}
+
+static int run_density(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_out *out) {
+    const int ng = ctx->ngas;
+    TsphSphBufs &S = ctx->S;
+    cudaEventRecord(ctx->ev[5], ctx->stream);
+    k_gas_gather_pos<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, ctx->C, ctx->G);
+    TSPH_LAUNCH_CK("k_gas_gather_pos");
+    int rc = tsph_build_tree(ctx, ctx->G, ctx->TG, ng, 16);
+    if (rc) return rc;
+    k_gas_nodes<<<tsph_blocks(ctx->TG.nNodes, 256), 256, 0, ctx->stream>>>(ctx->TG.nNodes, ctx->TG);
+    TSPH_LAUNCH_CK("k_gas_nodes");
+    k_gas_gather_vel<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, ctx->C, ctx->G.iord, S);
+    TSPH_LAUNCH_CK("k_gas_gather_vel");
+    set_sph_const(ctx, sp);
+    SphArgs A;
+    A.T = ctx->TG;
+    A.G = ctx->G;
+    A.S = S;
+    A.cnt = ctx->dCnt;
+    A.work = (int *)&ctx->dCnt->pad;
+    A.seed = (sp->bLearnedH && S.haveSeed) ? S.seed : nullptr;
+    TSPH_CK(cudaMemsetAsync(ctx->dCnt, 0, sizeof(TsphDevCounters), ctx->stream));
+    cudaEventRecord(ctx->ev[6], ctx->stream);
+    size_t sm = sizeof(KnnSmem) * SW;
+    TSPH_CK(cudaFuncSetAttribute(k_knn_density, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_knn_density<<<ctx->smCount * 3, SW * 32, sm, ctx->stream>>>(A);
+    TSPH_LAUNCH_CK("k_knn_density");
+    cudaEventRecord(ctx->ev[7], ctx->stream);
+    TSPH_CK(cudaMemcpyAsync(ctx->hCnt, ctx->dCnt, sizeof(TsphDevCounters), cudaMemcpyDeviceToHost,
+                            ctx->stream));
+    TSPH_CK(cudaStreamSynchronize(ctx->stream));
+    cudaEventElapsedTime(&ctx->timings[4], ctx->ev[5], ctx->ev[6]);
+    cudaEventElapsedTime(&ctx->timings[5], ctx->ev[6], ctx->ev[7]);
+    unsigned st = ctx->hCnt->status;
+    if (st) for (int k = 1; k < 32; ++k) if (st & (1u << k)) return k;
+    S.nFallback = (int)ctx->hCnt->nExactTests;
+    S.haveDensity = true;
+    S.havePressure = false;
+    S.last = *sp;
+    if (out) {
+        out->nSmoothed = ng;
+        out->nFallback = S.nFallback;
+        out->dPairs = (double)ctx->hCnt->nPartPP;
+    }
+    return TSPH_OK;
+}
+
+static int run_pressure(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_out *out) {
+    const int ng = ctx->ngas;
+    TsphSphBufs &S = ctx->S;
+    set_sph_const(ctx, sp);
+    cudaEventRecord(ctx->ev[8], ctx->stream);
+    k_gas_pressure<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, S);
+    TSPH_LAUNCH_CK("k_gas_pressure");
+    TSPH_CK(cudaMemsetAsync(S.nodeBall2, 0, sizeof(unsigned long long) * ctx->TG.nNodes, ctx->stream));
+    k_node_ball<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, ctx->TG, S.fBall2, S.nodeBall2);
+    TSPH_LAUNCH_CK("k_node_ball");
+    SphArgs A;
+    A.T = ctx->TG;
+    A.G = ctx->G;
+    A.S = S;
+    A.cnt = ctx->dCnt;
+    A.work = (int *)&ctx->dCnt->pad;
+    A.seed = nullptr;
+    TSPH_CK(cudaMemsetAsync(ctx->dCnt, 0, sizeof(TsphDevCounters), ctx->stream));
+    k_pressure<<<ctx->smCount * 4, SW * 32, 0, ctx->stream>>>(A);
+    TSPH_LAUNCH_CK("k_pressure");
+    k_scatter_hydro<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, ctx->G.iord, S, ctx->C);
+    TSPH_LAUNCH_CK("k_scatter_hydro");
+    cudaEventRecord(ctx->ev[9], ctx->stream);
+    TSPH_CK(cudaMemcpyAsync(ctx->hCnt, ctx->dCnt, sizeof(TsphDevCounters), cudaMemcpyDeviceToHost,
+                            ctx->stream));
+    TSPH_CK(cudaStreamSynchronize(ctx->stream));
+    cudaEventElapsedTime(&ctx->timings[6], ctx->ev[8], ctx->ev[9]);
+    unsigned st = ctx->hCnt->status;
+    if (st) for (int k = 1; k < 32; ++k) if (st & (1u << k)) return k;
+    S.havePressure = true;
+    if (out) {
+        out->nSmoothed = ng;
+        out->nFallback = 0;
+        out->dPairs = 0;
+    }
+    return TSPH_OK;
+}
+
+extern "C" int tsph_smooth(tsph_ctx *ctx, int smx_type, const tsph_sph_params *sp,
+                           tsph_smooth_out *out) {
+    if (!ctx || !sp) return TSPH_ERR_ARG;
+    if (smx_type != TSPH_SMX_DENDVDX && smx_type != TSPH_SMX_SPHPRESSURETERMS)
+        return TSPH_ERR_UNSUPPORTED;
+    if (!ctx->haveParts || !ctx->haveVel) return TSPH_ERR_STATE;
+    if (sp->nSmooth < 1 || sp->gamma <= 1.0) return TSPH_ERR_ARG;
+    if (sp->bPeriodic && !(sp->dPeriod > 0)) return TSPH_ERR_ARG;
+    if (sp->precision != TSPH_FP64 && sp->precision != TSPH_FP32) return TSPH_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (ctx->ngas == 0) {
+        if (out) memset(out, 0, sizeof(*out));
+        return TSPH_OK;
+    }
+    if (smx_type == TSPH_SMX_DENDVDX) return run_density(ctx, sp, out);
+    if (!ctx->S.haveDensity) return TSPH_ERR_STATE;
+    return run_pressure(ctx, sp, out);
+}
+
+extern "C" int tsph_get_sph(tsph_ctx *ctx, double *out16, double *dtNew, double *mumax) {
+    if (!ctx) return TSPH_ERR_ARG;
+    if (!ctx->S.haveDensity) return TSPH_ERR_STATE;
+    cudaSetDevice(ctx->device);
+    const int ng = ctx->ngas;
+    TsphSphBufs &S = ctx->S;
+    const int *iord = ctx->G.iord;
+    if (out16 && ng > 0) {
+        const double *src[16] = {S.fBall2, S.rho, S.divv, S.curl, S.curl, S.curl, S.dvds, S.bal,
+                                 S.diff, S.pr2, S.cs, S.hax, S.hay, S.haz, S.uPdV, S.uAV};
+        int strd[16] = {1, 1, 1, 3, 3, 3, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1};
+        int off[16] = {0, 0, 0, 0, 1, 2, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+        TSPH_CK(cudaMemsetAsync(ctx->dStage, 0, sizeof(double) * 3 * ng, ctx->stream));
+        // 16 fields interleaved: stage holds 3*cap doubles, so copy in groups of 3
+        for (int f0 = 0; f0 < 16; f0 += 3) {
+            int nf = 16 - f0 < 3 ? 16 - f0 : 3;
+            for (int f = 0; f < nf; ++f) {
+                bool ready = (f0 + f) < 9 || S.havePressure;
+                if (!ready) continue;
+                k_to_caller1<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(
+                    ng, iord, src[f0 + f], strd[f0 + f], off[f0 + f], ctx->dStage, 3, f);
+                TSPH_LAUNCH_CK("k_to_caller1");
+            }
+            static double *tmp = nullptr;
+            static size_t tmpN = 0;
+            if (tmpN < (size_t)3 * ng) {
+                free(tmp);
+                tmp = (double *)malloc(sizeof(double) * 3 * ng);
+                tmpN = (size_t)3 * ng;
+            }
+            TSPH_CK(cudaMemcpyAsync(tmp, ctx->dStage, sizeof(double) * 3 * ng, cudaMemcpyDeviceToHost,
+                                    ctx->stream));
+            TSPH_CK(cudaStreamSynchronize(ctx->stream));
+            for (int i = 0; i < ng; ++i)
+                for (int f = 0; f < nf; ++f) out16[16 * i + f0 + f] = tmp[3 * i + f];
+        }
+    }
+    double *arr[2] = {dtNew, mumax};
+    const double *srcs[2] = {S.dtNew, S.mumax};
+    for (int k = 0; k < 2; ++k) {
+        if (!arr[k] || ng == 0) continue;
+        if (!S.havePressure) return TSPH_ERR_STATE;
+        k_to_caller1<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, iord, srcs[k], 1, 0,
+                                                                    ctx->dStage, 1, 0);
+        TSPH_LAUNCH_CK("k_to_caller1");
+        TSPH_CK(cudaMemcpyAsync(arr[k], ctx->dStage, sizeof(double) * ng, cudaMemcpyDeviceToHost,
+                                ctx->stream));
+        TSPH_CK(cudaStreamSynchronize(ctx->stream));
+    }
+    return TSPH_OK;
+}
+
+__global__ void k_hash_to_caller(int ng, const int *__restrict__ iord, const int *__restrict__ cnt,
+                                 const unsigned long long *__restrict__ hsh, int *ocnt,
+                                 unsigned long long *ohsh) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ng) return;
+    ocnt[iord[i]] = cnt[i];
+    ohsh[iord[i]] = hsh[i];
+}
+
+extern "C" int tsph_get_neighbour_hash(tsph_ctx *ctx, int *count, unsigned long long *hash) {
+    if (!ctx || !count || !hash) return TSPH_ERR_ARG;
+    if (!ctx->S.haveDensity) return TSPH_ERR_STATE;
+    cudaSetDevice(ctx->device);
+    const int ng = ctx->ngas;
+    if (ng == 0) return TSPH_OK;
+    int *dc = (int *)ctx->dStage;
+    unsigned long long *dh = (unsigned long long *)(ctx->dStage + ng);
+    k_hash_to_caller<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, ctx->G.iord, ctx->S.nnCount,
+                                                                   ctx->S.nnHash, dc, dh);
+    TSPH_LAUNCH_CK("k_hash_to_caller");
+    TSPH_CK(cudaMemcpyAsync(count, dc, sizeof(int) * ng, cudaMemcpyDeviceToHost, ctx->stream));
+    TSPH_CK(cudaMemcpyAsync(hash, dh, sizeof(unsigned long long) * ng, cudaMemcpyDeviceToHost,
+                            ctx->stream));
+    TSPH_CK(cudaStreamSynchronize(ctx->stream));
+    return TSPH_OK;
+}
+
+// ---------------------------------------------------------------------------
+// kick and drift (pkdKick pkd.c:3780-3969, pkdDrift pkd.c:3686-3778)
+// ---------------------------------------------------------------------------
+__global__ void k_kick(int n, int ngas, double dt, TsphDevState C) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    bool gas = i < ngas;
+    double ax = C.ax[i], ay = C.ay[i], az = C.az[i];
+    if (gas) { ax += C.hax[i]; ay += C.hay[i]; az += C.haz[i]; }
+    double vx = C.vx[i] + ax * dt, vy = C.vy[i] + ay * dt, vz = C.vz[i] + az * dt;
+    if (gas) {
+        C.vpx[i] = vx; C.vpy[i] = vy; C.vpz[i] = vz;
+        double up = C.u[i] + C.udot[i] * dt;
+        if (up < 0) up = 0;
+        C.upred[i] = up;
+        C.u[i] = up;
+    } else {
+        C.vpx[i] = vx; C.vpy[i] = vy; C.vpz[i] = vz;
+    }
+    C.vx[i] = vx; C.vy[i] = vy; C.vz[i] = vz;
+}
+
+__global__ void k_drift(int n, double dt, int bPeriodic, double L, TsphDevState C) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double *r[3] = {C.x, C.y, C.z};
+    const double *v[3] = {C.vx, C.vy, C.vz};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        double x = r[k][i] + dt * v[k][i];
+        if (bPeriodic) {
+            if (x >= 0.5 * L) x -= L;
+            if (x < -0.5 * L) x += L;
+        }
+        r[k][i] = x;
+    }
+}
+
+extern "C" int tsph_kick(tsph_ctx *ctx, double dt) {
+    if (!ctx) return TSPH_ERR_ARG;
+    if (!ctx->haveParts || !ctx->haveVel) return TSPH_ERR_STATE;
+    cudaSetDevice(ctx->device);
+    if (ctx->n == 0) return TSPH_OK;
+    k_kick<<<tsph_blocks(ctx->n, 256), 256, 0, ctx->stream>>>(ctx->n, ctx->ngas, dt, ctx->C);
+    TSPH_LAUNCH_CK("k_kick");
+    TSPH_CK(cudaStreamSynchronize(ctx->stream));
+    return TSPH_OK;
+}
+
+extern "C" int tsph_drift(tsph_ctx *ctx, double dt, int bPeriodic, double dPeriod) {
+    if (!ctx) return TSPH_ERR_ARG;
+    if (!ctx->haveParts || !ctx->haveVel) return TSPH_ERR_STATE;
+    if (bPeriodic && !(dPeriod > 0)) return TSPH_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (ctx->n == 0) return TSPH_OK;
+    k_drift<<<tsph_blocks(ctx->n, 256), 256, 0, ctx->stream>>>(ctx->n, dt, bPeriodic, dPeriod, ctx->C);
+    TSPH_LAUNCH_CK("k_drift");
+    TSPH_CK(cudaStreamSynchronize(ctx->stream));
+    ctx->S.haveDensity = ctx->S.havePressure = false;
+    ctx->haveGrav = false;
+    return TSPH_OK;
+}
+
+extern "C" int tsph_get_state(tsph_ctx *ctx, double *pos, double *vel, double *u) {
+    if (!ctx) return TSPH_ERR_ARG;
+    if (!ctx->haveParts) return TSPH_ERR_STATE;
+    cudaSetDevice(ctx->device);
+    int rc = tsph_copy_out(ctx, ctx->C.x, ctx->C.y, ctx->C.z, 3, pos);
+    if (!rc) rc = tsph_copy_out(ctx, ctx->C.vx, ctx->C.vy, ctx->C.vz, 3, vel);
+    if (!rc && u && ctx->ngas > 0) rc = tsph_copy_out_n(ctx, ctx->ngas, ctx->C.u, nullptr, nullptr, 1, u);
+    return rc;
+}

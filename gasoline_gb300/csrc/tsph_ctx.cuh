@@ -1,0 +1,128 @@
+// Host-side context of libtsph: device buffers, stream, error state.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include "tsph_internal.cuh"
+
+struct TsphBuildBufs {
+    int cap;          // particle capacity
+    int nodeCap;      // temp node capacity
+    int *seg;         // frontier index per particle (-1 = in a finished leaf)
+    int *lt;          // r[d] < fSplit flag
+    int *scan;        // inclusive scan of lt
+    int *scanTmp;     // block sums for the scan
+    // frontier, double-buffered
+    int *f_lo[2], *f_hi[2], *f_node[2];
+    int *f_split, *f_rank, *f_dim, *f_m;
+    double *f_fs;
+    unsigned long long *f_bnd;   // 6 keys per frontier entry
+    // temporary nodes, numbered breadth first
+    int *t_lo, *t_hi, *t_dim, *t_child, *t_size, *t_pre, *t_level;
+    double *t_split, *t_bnd;
+    unsigned long long *maxd2;   // per final node: max squared distance to COM
+    int maxd2Cap;
+    int *leafFlag, *leafScan;
+    int *hostCount;              // pinned
+};
+
+// SPH arrays, in gas-tree order (G.iord maps to the caller index)
+struct TsphSphBufs {
+    int cap;
+    double *vx, *vy, *vz, *u;    // vPred, uPred gathered from the state
+    double *fBall2, *rho, *divv, *curl, *dvds, *bal, *diff, *pr2, *cs, *dtp;
+    double *hax, *hay, *haz, *uPdV, *uAV, *dtNew, *mumax;
+    double *seed;                // optional fBall2 seed per particle (learned h)
+    int *nnCount;
+    unsigned long long *nnHash;
+    unsigned long long *nodeBall2;   // per gas-tree node: max fBall2 (bits)
+    int nFallback;
+    bool haveDensity, havePressure, haveSeed;
+    tsph_sph_params last;
+};
+
+struct tsph_ctx {
+    int device;
+    cudaStream_t stream;
+    bool ownStream;
+    int smCount;
+    char cudaErr[256];
+    long long launches;
+
+    int n, ngas;
+    int cap;
+    TsphDevState C;              // caller order
+    TsphDevParts P;              // gravity tree order
+    TsphDevTree T;               // gravity tree
+    TsphDevParts G;              // gas tree order
+    TsphDevTree TG;              // gas tree
+    TsphBuildBufs B;
+    TsphSphBufs S;
+    TsphDevCounters *dCnt;       // device counters
+    TsphDevCounters *hCnt;       // pinned mirror
+    int *dBucketLists;           // 4 ints per bucket
+    int bucketListCap;
+
+    // Ewald
+    double *dRoot;               // 35 doubles: root complete moments
+    double *dEwt;                // 5 doubles per k-vector
+    int nEwt;
+    int ewtCap;
+
+    // input staging (caller order) and pinned host mirror
+    double *dStage;
+    size_t stageBytes;
+    void *hPin;
+    size_t hPinBytes;
+
+    bool haveParts, haveVel, haveTree, haveGrav;
+    tsph_grav_params lastGrav;
+    double dPeriodTree;
+
+    cudaEvent_t ev[10];
+    float timings[8];
+};
+
+// error helpers -----------------------------------------------------------
+int tsph_cuda_fail(tsph_ctx *ctx, cudaError_t e, const char *where);
+#define TSPH_CK(call)                                                  \
+    do {                                                               \
+        cudaError_t e_ = (call);                                       \
+        if (e_ != cudaSuccess) return tsph_cuda_fail(ctx, e_, #call);  \
+    } while (0)
+#define TSPH_LAUNCH_CK(where)                                          \
+    do {                                                               \
+        ctx->launches++;                                               \
+        cudaError_t e_ = cudaGetLastError();                           \
+        if (e_ != cudaSuccess) return tsph_cuda_fail(ctx, e_, where);  \
+    } while (0)
+
+template <typename T>
+static int tsph_grow(tsph_ctx *ctx, T **p, size_t count) {
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    cudaError_t e = cudaMalloc((void **)p, sizeof(T) * (count > 0 ? count : 1));
+    if (e != cudaSuccess) { *p = nullptr; return tsph_cuda_fail(ctx, e, "cudaMalloc"); }
+    return TSPH_OK;
+}
+
+static inline int tsph_blocks(long long n, int bs) {
+    long long b = (n + bs - 1) / bs;
+    return (int)(b > 0 ? b : 1);
+}
+
+// internal entry points implemented across the .cu files
+int tsph_scan_inclusive(tsph_ctx *ctx, const int *in, int *out, int n);
+int tsph_build_tree(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, int nBucket);
+int tsph_tree_moments(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, double dTheta);
+int tsph_copy_out(tsph_ctx *ctx, const double *a0, const double *a1, const double *a2, int comp,
+                  double *host);
+int tsph_copy_out_n(tsph_ctx *ctx, int n, const double *a0, const double *a1, const double *a2,
+                    int comp, double *host);
+void tsph_free_tree(TsphDevTree &T);
+int tsph_walk_interact(tsph_ctx *ctx, const tsph_grav_params *gp);
+int tsph_ewald(tsph_ctx *ctx, const tsph_grav_params *gp);
+int tsph_ensure_particles(tsph_ctx *ctx, int n);
+int tsph_sph_density(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_out *out);
+int tsph_sph_pressure(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_out *out);

@@ -1,0 +1,98 @@
+// Internal device-side data layout and helpers for libtsph.
+//
+// Particles live in HBM as structure-of-arrays in *tree order* (the order the
+// reference's pkdBuildBinary leaves pStore in, pkd.c:2627-2723), with the
+// caller's index kept in `iord`.  Tree nodes are stored in the reference's
+// own depth-first numbering (BuildBinary allocates a node, then its lower
+// subtree, then its upper subtree: pkd.c:2452-2453), so node i's lower child
+// is i+1 and the node after its subtree is i + size(i).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/tsph.h"
+
+#define TSPH_WARP 32
+#define TSPH_MAX_LEVELS 128
+
+// FP64 helpers that never contract into FMA: the reference's tree and walk
+// decisions are reproduced bit for bit, so every rounding step must match
+// the C source's separate multiply and add.
+__device__ __forceinline__ double xmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double xadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double xsub(double a, double b) { return __dsub_rn(a, b); }
+
+// Monotone 64-bit key of a double: key order == numeric order (no NaN).
+__device__ __forceinline__ unsigned long long dkey(double x) {
+    unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    return (b & 0x8000000000000000ULL) ? ~b : (b | 0x8000000000000000ULL);
+}
+__device__ __forceinline__ double dunkey(unsigned long long k) {
+    unsigned long long b = (k & 0x8000000000000000ULL) ? (k & 0x7FFFFFFFFFFFFFFFULL) : ~k;
+    return __longlong_as_double((long long)b);
+}
+
+// Split a double into float hi + float lo with hi + lo == x to ~2^-48.
+__host__ __device__ __forceinline__ void split2f(double x, float &hi, float &lo) {
+    hi = (float)x;
+    lo = (float)(x - (double)hi);
+}
+
+struct TsphDevTree {
+    int nNodes;
+    int nLeaves;
+    int cap;          // allocated node capacity
+    // node arrays, depth-first (reference) order
+    int *pLower, *pUpper, *iDim;
+    int *upper;       // upper child index, -1 for a leaf
+    int *skip;        // node after this subtree, -1 at the end (threaded "next")
+    double *fSplit;
+    double *bnd;      // 6 per node: min xyz, max xyz
+    double *fMass, *fSoft;
+    double *r;        // 3 per node, centre of mass
+    double *fOpen2, *Bmax;
+    double *Q;        // 6 per node: xx yy zz xy xz yz (complete, about the COM)
+    // walk copies in FP32
+    float4 *wcomh;    // com hi xyz + fOpen2 (float)
+    float4 *wcoml;    // com lo xyz + fSoft (float)
+    int4 *wlink;      // pLower, count, upper (-1 leaf), 0
+    float4 *wmom0;    // m, Qxx, Qyy, Qzz
+    float4 *wmom1;    // Qxy, Qxz, Qyz, fSoft
+    int *leaves;      // leaf node ids in depth-first order (the buckets)
+};
+
+struct TsphDevParts {
+    int n;
+    int ngas;
+    double *x, *y, *z, *m, *h;   // tree order
+    int *iord;                   // caller index of each tree-order slot
+    float4 *ph;                  // hi xyz + mass (float)
+    float4 *pl;                  // lo xyz + soft (float)
+    // outputs in tree order
+    double *ax, *ay, *az, *pot, *dtGrav;
+};
+
+// Particle state in the caller's order (the reference's iOrder): what the
+// kick/drift update and the host see.  The gravity tree and the gas tree
+// each keep their own tree-ordered copies (TsphDevParts) mapped back by iord.
+struct TsphDevState {
+    double *x, *y, *z, *vx, *vy, *vz, *m, *h, *u;
+    double *vpx, *vpy, *vpz, *upred;     // predicted (time-centred) v and u
+    double *ax, *ay, *az, *pot, *dtGrav; // gravity
+    double *hax, *hay, *haz, *udot;      // SPH (gas only): hydro accel, uDotPdV+uDotAV
+};
+
+// Counters accumulated by the walk (integers: deterministic).
+struct TsphDevCounters {
+    unsigned long long nActive;
+    unsigned long long nPartPP;      // sum over buckets of n * nPart
+    unsigned long long nIntra;       // sum over buckets of n*(n-1)/2
+    unsigned long long nBucketSq;    // sum over buckets of n*n
+    unsigned long long nCellNewt;    // sum of n * nCellNewt
+    unsigned long long nCellSoft;    // sum of n * nCellSoft
+    unsigned long long nEwLoop;      // Ewald real-space terms evaluated
+    unsigned long long nExactTests;  // opening tests settled in FP64
+    unsigned long long nTests;       // opening tests in total
+    unsigned int status;             // TSPH_ERR_* raised on device
+    unsigned int pad;
+};

@@ -87,7 +87,7 @@ def _grf_displacement(ng, index, rms, seed, box=1.0):
     out = np.empty((ng, ng, ng, 3))
     for d, kd in enumerate((kx, ky, kz)):
         psi_k = 1j * kd / k2 * delta_k
-        out[..., d] = np.fft.irfftn(psi_k, s=(ng, ng, ng))
+        out[..., d] = np.fft.irfftn(psi_k, s=(ng, ng, ng), axes=(0, 1, 2))
     out = out.reshape(-1, 3)
     cur = math.sqrt(float(np.mean(np.sum(out * out, axis=1))))
     return out * (rms / cur)

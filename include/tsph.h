@@ -1,0 +1,214 @@
+/*
+ * libtsph -- GB300-native TreeSPH force path behind a C ABI.
+ *
+ * The entry points replace the per-rank kernels of the reference (gasoline)
+ * that its processor-set tree calls on every rank:
+ *   tsph_grav_all   <- pkdGravAll           (pkd.h:797-801, pkd.c:2868-3060)
+ *                      with the tree build it needs, pkdBuildBinary
+ *                      (pkd.c:2627-2723), pkdCalcRoot/pkdDistribRoot
+ *                      (pkd.c:4395-4493) and pkdEwaldInit (ewald.c:182-248)
+ *   tsph_smooth     <- smInitialize + smSmooth / smReSmooth + smFinish
+ *                      (smooth.h:616-638, smooth.c:54-542,1439-1749) for the
+ *                      smooth types SMX_DENDVDX and SMX_SPHPRESSURETERMS
+ *                      (smoothfcn.h:147-199), with pkdGasPressure
+ *                      (pkd.c:5750-5785) run between the two
+ *   tsph_kick/drift <- pkdKick (pkd.c:3780-3969), pkdDrift (pkd.c:3686-3778)
+ *
+ * Arguments are plain pointers and sizes.  Arrays are in the caller's
+ * particle order (the reference's iOrder); positions, velocities and
+ * accelerations are interleaved xyz (3 doubles per particle), like the
+ * r[3]/v[3]/a[3] members of the reference's PARTICLE (pkd.h:90-225).
+ * Gas particles are the first ngas particles.
+ *
+ * Every call returns TSPH_OK (0) or a positive TSPH_ERR_* code; device-side
+ * failures (list overflow, kNN not converging, non-finite input) come back
+ * as codes rather than traps, and the context stays usable.  The reference
+ * aborts through assert() in the same situations.
+ *
+ * A context owns one GPU's device buffers and a CUDA stream; it is not
+ * thread-safe (like the reference's PKD, one context per host thread).
+ */
+#ifndef TSPH_H
+#define TSPH_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct tsph_ctx tsph_ctx;
+
+enum tsph_status {
+    TSPH_OK = 0,
+    TSPH_ERR_ARG = 1,             /* bad argument (NULL, n < 0, ...) */
+    TSPH_ERR_CUDA = 2,            /* CUDA runtime error; see tsph_last_cuda_error */
+    TSPH_ERR_STACK_OVERFLOW = 3,  /* walk stack exceeded its capacity */
+    TSPH_ERR_LIST_OVERFLOW = 4,   /* neighbour list exceeded its capacity */
+    TSPH_ERR_KNN_NO_CONVERGE = 5, /* kNN radius search hit its iteration cap */
+    TSPH_ERR_NONFINITE = 6,       /* NaN or Inf in the particle data */
+    TSPH_ERR_UNSUPPORTED = 7,     /* smooth type or option not implemented */
+    TSPH_ERR_STATE = 8,           /* call order (e.g. no particles loaded) */
+    TSPH_ERR_TREE_DEPTH = 9,      /* tree deeper than the build's level cap */
+    TSPH_ERR_NOMEM = 10           /* device allocation failed */
+};
+
+enum tsph_precision {
+    TSPH_FP64 = 0,   /* all pairwise and multipole arithmetic in FP64 */
+    TSPH_FP32 = 1    /* FP32 on bucket-relative offsets, compensated sums */
+};
+
+/* Smooth types, numbered as the reference's enum smx_smoothtype
+ * (smoothfcn.h:147-199). */
+enum tsph_smx {
+    TSPH_SMX_DENSITY = 1,
+    TSPH_SMX_SPHPRESSURETERMS = 22,
+    TSPH_SMX_DENDVDX = 23
+};
+
+/*
+ * Gravity parameters: the arguments of pkdGravAll (nReps, bPeriodic,
+ * iOrder, bEwald, iEwOrder, fEwCut, fEwhCut; pkd.h:797) plus those of the
+ * tree build it depends on (nBucket, dTheta with OPEN_JOSH opening,
+ * master.c:1897-1934; the period fPeriod of pkdInitialize) and the
+ * arithmetic precision.  Comoving and Sun-indirect terms (bComove,
+ * bDoSun) are not part of this path.
+ */
+typedef struct {
+    int nBucket;      /* max particles per leaf (reference default 8) */
+    int iOrder;       /* cell multipole order, 1..4 (2 = quadrupole) */
+    int bPeriodic;
+    int bEwald;
+    int iEwOrder;     /* Ewald multipole order, 1..4 */
+    int nReps;        /* periodic replicas per side (1 when periodic) */
+    double dTheta;    /* opening angle */
+    double dPeriod;   /* box length L (cube) */
+    double fEwCut;    /* real-space cut in units of L (2.6) */
+    double fEwhCut;   /* k-space cut (2.8) */
+    int precision;    /* enum tsph_precision */
+    int reserved;
+} tsph_grav_params;
+
+/* pkdGravAll's out-parameters (nActive, pdPartSum, pdCellSum, pdSoftSum,
+ * pdFlop), same definitions (pkd.c:2946-2962, grav.c:246-247,
+ * ewald.c:175-176), plus the fraction of opening tests settled in FP64. */
+typedef struct {
+    int nActive;
+    int nBuckets;
+    double dPartSum;
+    double dCellSum;
+    double dSoftSum;
+    double dFlop;
+    double dFlopEwald;
+    double dExactFrac;
+} tsph_grav_out;
+
+/* SPH parameters: the SMF fields the two passes read (smoothfcn.h:22-130,
+ * filled by msrSmoothFcnParam master.c:5548-5669) for a non-comoving run
+ * (a = 1, H = 0), adiabatic gas without cooling. */
+typedef struct {
+    int nSmooth;
+    int bPeriodic;
+    double dPeriod;
+    double alpha;         /* dConstAlpha */
+    double beta;          /* dConstBeta */
+    double gamma;         /* dConstGamma */
+    double dEtaCourant;   /* dtFacCourant = dEtaCourant*2/1.6 (pkd.c:5893) */
+    int iViscosityLimiter;/* 0 none, 1 Balsara (reference default) */
+    int precision;        /* enum tsph_precision for the gathers */
+    int bLearnedH;        /* seed the kNN with the h-network's prediction */
+    int reserved;
+} tsph_sph_params;
+
+typedef struct {
+    int nSmoothed;        /* SMF.nSmoothed */
+    int nFallback;        /* particles whose seeded ball held < nSmooth */
+    double dPairs;        /* neighbour pairs gathered */
+} tsph_smooth_out;
+
+/* --- context --------------------------------------------------------- */
+
+/* Create a context on `device`.  `stream` is a cudaStream_t to run on, or
+ * NULL for a stream the context creates and owns. */
+int tsph_create(tsph_ctx **pctx, int device, void *stream);
+void tsph_destroy(tsph_ctx *ctx);
+const char *tsph_error_string(int status);
+/* The last CUDA error message seen by this context ("" if none). */
+const char *tsph_last_cuda_error(tsph_ctx *ctx);
+
+/* Load particles (host arrays, caller order): pos[3n], mass[n], soft[n]
+ * (spline softening length, the reference's fSoft).  Replaces the previous
+ * set.  Device memory grows as needed and is kept between calls. */
+int tsph_set_particles(tsph_ctx *ctx, int n, const double *pos,
+                       const double *mass, const double *soft);
+/* Velocities vel[3n] (all particles) and, for the first ngas particles,
+ * specific thermal energy u[ngas] (the reference's u; uPred = u, vPred = v
+ * at load).  ngas may be 0. */
+int tsph_set_velocities(tsph_ctx *ctx, const double *vel, int ngas,
+                        const double *u);
+
+/* --- gravity (pkdGravAll) -------------------------------------------- */
+
+/* Build the gravity tree over the loaded particles and compute every
+ * particle's acceleration, potential and dtGrav (the reference's
+ * 1/dt^2 estimate), overwriting them (the reference accumulates into
+ * a[] after msrInitAccel zeroes it).  Results stay on the device. */
+int tsph_grav_all(tsph_ctx *ctx, const tsph_grav_params *gp,
+                  tsph_grav_out *out);
+/* Copy gravity results to the host in caller order; NULL skips a field. */
+int tsph_get_gravity(tsph_ctx *ctx, double *acc, double *pot, double *dtGrav);
+
+/* Tree export for parity checks, in the reference's node order.  Writes
+ * inode[6*i] = pLower, pUpper, iDim, iLower, iUpper (threaded), 0 and
+ * dnode[16*i] = fSplit, bnd.fMin[3], bnd.fMax[3], fMass, fSoft, r[3],
+ * fOpen2, Bmax, Qxx, Qyy; perm[pos] = caller index at tree position pos.
+ * With inode == NULL only returns the node count in *nNodes. */
+int tsph_get_tree(tsph_ctx *ctx, int *nNodes, int *inode, double *dnode,
+                  int *perm);
+/* Per-bucket interaction-list lengths of the last tsph_grav_all (in
+ * depth-first bucket order): blist[4*b] = node, nPart, nCellSoft,
+ * nCellNewt.  With blist == NULL returns the bucket count. */
+int tsph_get_lists(tsph_ctx *ctx, int *nBuckets, int *blist);
+
+/* --- SPH (smSmooth / smReSmooth) -------------------------------------- */
+
+/* Run one smooth pass over the gas particles:
+ *   TSPH_SMX_DENDVDX: exact kNN smoothing lengths (fBall2 = nSmooth-th
+ *     smallest squared distance, self included) and the DenDVDX gather;
+ *   TSPH_SMX_SPHPRESSURETERMS: gas pressure (pkdGasPressure) and the
+ *     symmetric pressure / artificial-viscosity terms over every pair with
+ *     d^2 <= fBall2 of either particle.
+ * Other types return TSPH_ERR_UNSUPPORTED. */
+int tsph_smooth(tsph_ctx *ctx, int smx_type, const tsph_sph_params *sp,
+                tsph_smooth_out *out);
+/* SPH results in caller order for the gas particles: out[16*i] = fBall2,
+ * fDensity, divv, curlv[3], dvds, BalsaraSwitch, diff, PoverRho2, c,
+ * a_hydro[3], uDotPdV, uDotAV; dtNew[i]; mumax[i]. NULL skips. */
+int tsph_get_sph(tsph_ctx *ctx, double *out16, double *dtNew, double *mumax);
+/* Neighbour-set fingerprint per gas particle: |N(i)| and an
+ * order-independent hash of the caller indices in N(i). */
+int tsph_get_neighbour_hash(tsph_ctx *ctx, int *count,
+                            unsigned long long *hash);
+
+/* --- kick-drift-kick (pkdKick / pkdDrift) ------------------------------ */
+
+/* v += a*dt (a = gravity + hydro); gas: vPred = v_old + a*dt,
+ * u += uDot*dt with uDot = uDotPdV + uDotAV, clamped at 0 (NOCOOLING,
+ * pkd.c:3936-3939). */
+int tsph_kick(tsph_ctx *ctx, double dt);
+/* r += v*dt, wrapped into [-L/2, L/2) when periodic (pkd.c:3726-3756). */
+int tsph_drift(tsph_ctx *ctx, double dt, int bPeriodic, double dPeriod);
+/* Copy state to the host in caller order; NULL skips a field. */
+int tsph_get_state(tsph_ctx *ctx, double *pos, double *vel, double *u);
+
+/* Timing of the last call's kernels on the context stream (ms), by phase:
+ * t[0] tree build, t[1] moments, t[2] walk+interactions, t[3] Ewald,
+ * t[4] kNN, t[5] density, t[6] pressure, t[7] total. */
+int tsph_get_timings(tsph_ctx *ctx, float *t8);
+/* Number of libtsph kernel launches issued since context creation. */
+long long tsph_launch_count(tsph_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

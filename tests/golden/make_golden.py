@@ -1,0 +1,71 @@
+"""Writes the golden fixtures in tests/golden/ from the reference's own code.
+
+Run in a checkout where the reference sources are available:
+    sh oracle/build_ref.sh /path/to/gasoline && python tests/golden/make_golden.py
+It calls the reference's pkdBuildBinary/pkdGravAll and smSmooth/smReSmooth
+through oracle/_ref/libgasref.so on small seeded inputs and stores inputs
+and outputs as compressed .npz files.  The tests compare the CPU oracle and
+the CUDA path against these files, so they need no reference at run time.
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.abspath(os.path.join(HERE, "..", "..")))
+
+import oracle  # noqa: E402
+from gasoline_gb300 import ics  # noqa: E402
+
+
+def grav_case(name, pos, mass, soft, gp):
+    R = oracle.reference()
+    g = R.grav(pos, mass, soft, gp)
+    inode, dnode, perm = R.tree(pos, mass, soft, gp)
+    bl = R.lists(pos, mass, soft, gp)
+    np.savez_compressed(
+        os.path.join(HERE, name + ".npz"), pos=pos, mass=mass, soft=soft,
+        params=np.array([gp.nBucket, gp.iOrder, gp.bPeriodic, gp.bEwald,
+                         gp.iEwOrder, gp.nReps, gp.dTheta, gp.dPeriod,
+                         gp.fEwCut, gp.fEwhCut]),
+        acc=g["acc"], pot=g["pot"], dtGrav=g["dtGrav"], counters=g["counters"],
+        inode=inode, dnode=dnode, perm=perm, blist=bl)
+    print(name, len(mass), "nodes", len(inode), "buckets", len(bl))
+
+
+def sph_case(name, pos, vel, mass, soft, u, sp):
+    R = oracle.reference()
+    r = R.sph(pos, vel, mass, soft, u, sp)
+    out = np.stack([r[k] for k in oracle.SPH_FIELDS], axis=1)
+    np.savez_compressed(
+        os.path.join(HERE, name + ".npz"), pos=pos, vel=vel, mass=mass,
+        soft=soft, u=u,
+        params=np.array([sp.nSmooth, sp.bPeriodic, sp.dPeriod, sp.alpha,
+                         sp.beta, sp.gamma, sp.dEtaCourant, sp.nBucket,
+                         sp.iViscosityLimiter]),
+        out=out, dtNew=r["dtNew"], mumax=r["mumax"])
+    print(name, len(mass))
+
+
+def main():
+    if not oracle.reference_available():
+        oracle.build_reference()
+    pos, vel, m = ics.plummer(2048, seed=11)
+    grav_case("grav_plummer_2k", pos, m, np.full(len(m), 0.01),
+              oracle.grav_params(periodic=False))
+    pos, vel, m = ics.lattice_box(8, seed=12)
+    grav_case("grav_box_8", pos, m, np.full(len(m), 1.0 / (50 * 8)),
+              oracle.grav_params(periodic=True, ewald=True))
+    pos, vel, m = ics.uniform_cube(1500, seed=13)
+    grav_case("grav_cube_soft", pos, m, np.full(len(m), 0.15),
+              oracle.grav_params(periodic=False, nBucket=8, theta=0.7))
+    pos, vel, m, u = ics.gas_sphere(2048, seed=14)
+    rng = np.random.Generator(np.random.PCG64(15))
+    vel = rng.normal(0.0, 0.1, (len(m), 3))
+    sph_case("sph_sphere_2k", pos, vel, m, np.full(len(m), 0.01), u,
+             oracle.sph_params(nSmooth=32))
+
+
+if __name__ == "__main__":
+    main()

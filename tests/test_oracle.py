@@ -1,0 +1,111 @@
+"""CPU tests: the oracle against the reference's golden vectors.
+
+The gravity oracle restates the reference operation by operation, so on
+the machine where the fixtures were written it matches them bit for bit;
+elsewhere (another libm, another ISA) trees, lists and counters must still
+match exactly and forces to a few ulps.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from golden_io import GRAV_CASES, grav_params_of, load, rel_err, sph_params_of
+
+
+@pytest.mark.parametrize("name", GRAV_CASES)
+def test_oracle_tree_matches_reference(orc, name):
+    d = load(name)
+    gp = grav_params_of(d, oracle)
+    inode, dnode, perm = orc.tree(d["pos"], d["mass"], d["soft"], gp)
+    assert np.array_equal(inode, d["inode"])
+    assert np.array_equal(perm, d["perm"])
+    # bounds, split, mass, softening, centre of mass, fOpen2, Bmax: bit-exact
+    assert np.array_equal(dnode[:, :14], d["dnode"][:, :14])
+    np.testing.assert_allclose(dnode[:, 14:], d["dnode"][:, 14:], rtol=1e-13, atol=1e-300)
+
+
+@pytest.mark.parametrize("name", GRAV_CASES)
+def test_oracle_lists_match_reference(orc, name):
+    d = load(name)
+    gp = grav_params_of(d, oracle)
+    bl = orc.lists(d["pos"], d["mass"], d["soft"], gp)
+    assert np.array_equal(bl, d["blist"])
+
+
+@pytest.mark.parametrize("name", GRAV_CASES)
+def test_oracle_forces_match_reference(orc, name):
+    d = load(name)
+    gp = grav_params_of(d, oracle)
+    g = orc.grav(d["pos"], d["mass"], d["soft"], gp)
+    assert np.array_equal(g["counters"][:4], d["counters"][:4])
+    assert g["counters"][4] == pytest.approx(d["counters"][4], rel=1e-12)
+    # ewald uses libm erf/exp/sin/cos, which may differ by an ulp across machines
+    assert rel_err(g["acc"], d["acc"]).max() < 1e-12
+    assert rel_err(g["pot"], d["pot"]).max() < 1e-12
+    assert rel_err(g["dtGrav"], d["dtGrav"]).max() < 1e-12
+
+
+def test_oracle_sph_matches_reference(orc):
+    d = load("sph_sphere_2k")
+    sp = sph_params_of(d, oracle)
+    r = orc.sph(d["pos"], d["vel"], d["mass"], d["soft"], d["u"], sp)
+    for k, name in enumerate(oracle.SPH_FIELDS):
+        ref = d["out"][:, k]
+        scale = np.max(np.abs(ref))
+        if name in ("fBall2", "c"):
+            assert np.array_equal(r[name], ref), name
+        else:
+            assert np.max(np.abs(r[name] - ref)) <= 1e-12 * scale, name
+    assert np.array_equal(r["dtNew"], d["dtNew"])
+    assert np.array_equal(r["mumax"], d["mumax"])
+    # the kNN neighbour count: exactly nSmooth for tie-free input
+    assert (r["nbr_count"] == 32).all()
+
+
+def test_oracle_v_sqrt1_accuracy():
+    x = np.exp(np.random.default_rng(3).uniform(-30, 30, 20000))
+    a = oracle.v_sqrt1(x)
+    rel = np.abs(a * np.sqrt(x) - 1.0)
+    assert rel.max() < 5e-10
+
+
+def test_oracle_knn_brute_force():
+    rng = np.random.default_rng(5)
+    pos = rng.uniform(-0.5, 0.5, (600, 3))
+    fb = oracle.knn_fball2(pos, 16)
+    d2 = ((pos[:, None, :] - pos[None, :, :]) ** 2).sum(-1)
+    ref = np.sort(d2, axis=1)[:, 15]
+    assert np.array_equal(fb, ref)
+
+
+def test_oracle_knn_periodic_brute_force():
+    rng = np.random.default_rng(6)
+    pos = rng.uniform(-0.5, 0.5, (500, 3))
+    fb = oracle.knn_fball2(pos, 16, periodic=True, L=1.0)
+    dx = pos[:, None, :] - pos[None, :, :]
+    dx = dx - np.round(dx)
+    ref = np.sort((dx ** 2).sum(-1), axis=1)[:, 15]
+    np.testing.assert_allclose(fb, ref, rtol=1e-12)
+
+
+def test_oracle_parallel_equals_serial(orc):
+    d = load("grav_plummer_2k")
+    gp = grav_params_of(d, oracle)
+    a = orc.grav(d["pos"], d["mass"], d["soft"], gp, nthreads=1)
+    b = orc.grav(d["pos"], d["mass"], d["soft"], gp, nthreads=4)
+    assert np.array_equal(a["acc"], b["acc"])
+    assert np.array_equal(a["counters"], b["counters"])
+
+
+@pytest.mark.skipif(not oracle.reference_available(), reason="reference not built here")
+@pytest.mark.parametrize("seed", [21, 22])
+def test_oracle_live_reference(orc, seed):
+    from gasoline_gb300 import ics
+    R = oracle.reference()
+    pos, vel, m = ics.lattice_box(12, seed=seed)
+    soft = np.full(len(m), 1.0 / 600)
+    gp = oracle.grav_params(periodic=True, ewald=True)
+    a = R.grav(pos, m, soft, gp)
+    b = orc.grav(pos, m, soft, gp)
+    assert np.array_equal(a["acc"], b["acc"])
+    assert np.array_equal(a["counters"], b["counters"])
