@@ -60,7 +60,8 @@ class SphParams(ctypes.Structure):
 
 class SmoothOut(ctypes.Structure):
     _fields_ = [("nSmoothed", ctypes.c_int), ("nFallback", ctypes.c_int),
-                ("dPairs", ctypes.c_double)]
+                ("dPairs", ctypes.c_double), ("dCandidates", ctypes.c_double),
+                ("bSeeded", ctypes.c_int), ("reserved", ctypes.c_int)]
 
 
 def grav_params(nBucket=8, iOrder=2, periodic=False, ewald=True, iEwOrder=4,
@@ -102,7 +103,10 @@ def load():
                  "tsph_grav_all", "tsph_get_gravity", "tsph_get_tree",
                  "tsph_get_lists", "tsph_smooth", "tsph_get_sph",
                  "tsph_get_neighbour_hash", "tsph_kick", "tsph_drift",
-                 "tsph_get_state", "tsph_get_timings"):
+                 "tsph_get_state", "tsph_get_timings", "tsph_fma_peak",
+                 "tsph_hnet_init", "tsph_hnet_set_params", "tsph_hnet_get_params",
+                 "tsph_hnet_loss_grad", "tsph_hnet_mode", "tsph_hnet_train",
+                 "tsph_hnet_info", "tsph_hnet_num_params"):
         getattr(lib, name).restype = ctypes.c_int
     lib.tsph_destroy.restype = None
     _lib = lib
@@ -254,6 +258,50 @@ class Context:
         u = np.zeros(max(self.ngas, 1))
         self._check(self.lib.tsph_get_state(self._ctx, _d(pos), _d(vel), _d(u)))
         return pos, vel, u[:self.ngas]
+
+    # ---- learned smoothing length ---------------------------------------------
+    def hnet_init(self, seed=1):
+        self._check(self.lib.tsph_hnet_init(self._ctx, ctypes.c_ulonglong(seed)))
+
+    def hnet_params(self):
+        n = self.lib.tsph_hnet_num_params()
+        w = np.zeros(n, dtype=np.float32)
+        self._check(self.lib.tsph_hnet_get_params(
+            self._ctx, w.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), n))
+        return w
+
+    def hnet_set_params(self, w):
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        self._check(self.lib.tsph_hnet_set_params(
+            self._ctx, w.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), len(w)))
+
+    def hnet_loss_grad(self, x, y):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.ascontiguousarray(y, dtype=np.float32)
+        n = self.lib.tsph_hnet_num_params()
+        g = np.zeros(n, dtype=np.float32)
+        loss = ctypes.c_double()
+        fp = ctypes.POINTER(ctypes.c_float)
+        self._check(self.lib.tsph_hnet_loss_grad(
+            self._ctx, len(y), x.ctypes.data_as(fp), y.ctypes.data_as(fp),
+            g.ctypes.data_as(fp), ctypes.byref(loss)))
+        return loss.value, g
+
+    def hnet_mode(self, collect=False, predict=False, margin=0.05):
+        self._check(self.lib.tsph_hnet_mode(self._ctx, int(collect), int(predict),
+                                            ctypes.c_double(margin)))
+
+    def hnet_train(self, steps=2000, batch=8192, lr=3e-3):
+        loss = ctypes.c_double()
+        self._check(self.lib.tsph_hnet_train(self._ctx, steps, batch,
+                                             ctypes.c_double(lr), ctypes.byref(loss)))
+        return loss.value
+
+    def hnet_info(self):
+        n = ctypes.c_longlong()
+        st = (ctypes.c_float * 8)()
+        self._check(self.lib.tsph_hnet_info(self._ctx, ctypes.byref(n), st))
+        return int(n.value), list(st)
 
     def timings(self):
         t = (ctypes.c_float * 8)()

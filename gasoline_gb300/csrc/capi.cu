@@ -72,11 +72,14 @@ extern "C" void tsph_destroy(tsph_ctx *ctx) {
     FREE(C.x); FREE(C.y); FREE(C.z); FREE(C.vx); FREE(C.vy); FREE(C.vz); FREE(C.m); FREE(C.h);
     FREE(C.u); FREE(C.vpx); FREE(C.vpy); FREE(C.vpz); FREE(C.upred); FREE(C.ax); FREE(C.ay);
     FREE(C.az); FREE(C.pot); FREE(C.dtGrav); FREE(C.hax); FREE(C.hay); FREE(C.haz); FREE(C.udot);
+    FREE(C.fb2prev); FREE(C.divvprev);
+    tsph_hnet_free(ctx);
     TsphDevParts *PP[2] = {&ctx->P, &ctx->G};
     for (int k = 0; k < 2; ++k) {
         TsphDevParts &P = *PP[k];
         FREE(P.x); FREE(P.y); FREE(P.z); FREE(P.m); FREE(P.h); FREE(P.iord);
         FREE(P.ph); FREE(P.pl); FREE(P.ax); FREE(P.ay); FREE(P.az); FREE(P.pot); FREE(P.dtGrav);
+        FREE(P.wsum); FREE(P.wcmp); FREE(P.wdt);
     }
     tsph_free_tree(ctx->T);
     tsph_free_tree(ctx->TG);
@@ -109,13 +112,15 @@ int tsph_ensure_particles(tsph_ctx *ctx, int n) {
     rc |= tsph_grow(ctx, &P.ph, cap); rc |= tsph_grow(ctx, &P.pl, cap);
     rc |= tsph_grow(ctx, &P.ax, cap); rc |= tsph_grow(ctx, &P.ay, cap); rc |= tsph_grow(ctx, &P.az, cap);
     rc |= tsph_grow(ctx, &P.pot, cap); rc |= tsph_grow(ctx, &P.dtGrav, cap);
+    rc |= tsph_grow(ctx, &P.wsum, cap); rc |= tsph_grow(ctx, &P.wcmp, cap);
+    rc |= tsph_grow(ctx, &P.wdt, cap);
     TsphDevParts &G = ctx->G;
     rc |= tsph_grow(ctx, &G.x, cap); rc |= tsph_grow(ctx, &G.y, cap); rc |= tsph_grow(ctx, &G.z, cap);
     rc |= tsph_grow(ctx, &G.m, cap); rc |= tsph_grow(ctx, &G.h, cap); rc |= tsph_grow(ctx, &G.iord, cap);
     TsphDevState &C = ctx->C;
     double **cs[] = {&C.x, &C.y, &C.z, &C.vx, &C.vy, &C.vz, &C.m, &C.h, &C.u, &C.vpx, &C.vpy,
                      &C.vpz, &C.upred, &C.ax, &C.ay, &C.az, &C.pot, &C.dtGrav, &C.hax, &C.hay,
-                     &C.haz, &C.udot};
+                     &C.haz, &C.udot, &C.fb2prev, &C.divvprev};
     for (auto pp : cs) rc |= tsph_grow(ctx, pp, cap);
     TsphSphBufs &S = ctx->S;
     double **ss[] = {&S.vx, &S.vy, &S.vz, &S.u, &S.fBall2, &S.rho, &S.divv, &S.dvds, &S.bal,
@@ -163,6 +168,7 @@ __global__ void k_load_state(int n, const double *__restrict__ pos3, TsphDevStat
     C.u[i] = C.upred[i] = C.udot[i] = 0.0;
     C.hax[i] = C.hay[i] = C.haz[i] = 0.0;
     C.ax[i] = C.ay[i] = C.az[i] = C.pot[i] = C.dtGrav[i] = 0.0;
+    C.fb2prev[i] = C.divvprev[i] = 0.0;
     piord[i] = i;
     giord[i] = i;
 }
@@ -284,7 +290,9 @@ extern "C" int tsph_grav_all(tsph_ctx *ctx, const tsph_grav_params *gp, tsph_gra
     }
     cudaEventRecord(ctx->ev[3], ctx->stream);
     if (n > 0) {
-        rc = tsph_ewald(ctx, gp);
+        bool ewald = gp->bPeriodic && gp->bEwald && gp->iEwOrder >= 1;
+        if (ewald) rc = tsph_ewald(ctx, gp);
+        else if (gp->precision == TSPH_FP32 && ctx->T.nLeaves > 0) rc = tsph_walk_finish_f32(ctx);
         if (rc) return rc;
     }
     if (n > 0) {

@@ -205,6 +205,16 @@ __device__ __forceinline__ double sqrt_r(double x) { return sqrt(x); }
 __device__ __forceinline__ void sincos_r(float x, float *s, float *c) { sincosf(x, s, c); }
 __device__ __forceinline__ void sincos_r(double x, double *s, double *c) { sincos(x, s, c); }
 
+// Kahan addition in FP32 (the Ewald terms are O(1) and cancel against the
+// replica part of the tree walk); plain addition in FP64.
+__device__ __forceinline__ void kadd(float &s, float &c, float v) {
+    float y = v - c;
+    float t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+__device__ __forceinline__ void kadd(double &s, double &c, double v) { s += v; (void)c; }
+
 template <typename Real>
 __global__ void __launch_bounds__(128) k_ewald(TsphDevParts P, TsphDevCounters *cnt) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -217,6 +227,7 @@ __global__ void __launch_bounds__(128) k_ewald(TsphDevParts P, TsphDevCounters *
         const Real fEwCut2 = (Real)cE.fEwCut2, smallR2 = (Real)cE.smallR2;
         const int nEw = cE.nEwReps, nR = cE.nReps, iOrder = cE.iOrder;
         Real fPot = (Real)(cE.mom.m * cE.k1), ax = 0, ay = 0, az = 0;
+        Real cpot = 0, cax = 0, cay = 0, caz = 0;   // compensations (FP32 only)
         Real dx = (Real)(P.x[p] - cE.mom.x);
         Real dy = (Real)(P.y[p] - cE.mom.y);
         Real dz = (Real)(P.z[p] - cE.mom.z);
@@ -232,7 +243,34 @@ __global__ void __launch_bounds__(128) k_ewald(TsphDevParts P, TsphDevCounters *
                     Real r2 = dxo * dxo + dyo * dyo + dzo * dzo;
                     if (r2 > fEwCut2 && !hole) continue;
                     Real gam[6];
-                    if (r2 < smallR2) {
+                    if (sizeof(Real) == 4 && hole && r2 * alpha2 < Real(4.0)) {
+                        // FP32: the recurrence below cancels catastrophically for a
+                        // hole image at small alpha*r.  With u = alpha^2 r^2,
+                        //   gam_n = -ka (2 alpha^2)^n S_n(u),
+                        //   S_n(u) = sum_j (-u)^j/(j!(2j+2n+1)) = int_0^1 t^2n e^(-u t^2) dt
+                        //          = e^-u T_n(u),  T_n = sum_j (2u)^j / prod_{i<=j}(2n+2i+1),
+                        // a series of positive terms; T_5 is summed directly and the
+                        // stable downward recurrence T_n = (2u T_{n+1} + 1)/(2n+1)
+                        // gives the rest (max rel. error ~2e-7 for u < 4).
+                        // The reference's small-r branch is the first two terms of S_n.
+                        Real u = r2 * alpha2, tu = 2 * u;
+                        Real t = Real(1.0 / 11.0), T5 = t;
+#pragma unroll
+                        for (int j = 1; j < 14; ++j) {
+                            t *= tu / Real(11 + 2 * j);
+                            T5 += t;
+                        }
+                        Real T[6];
+                        T[5] = T5;
+#pragma unroll
+                        for (int q = 4; q >= 0; --q) T[q] = (tu * T[q + 1] + 1) / Real(2 * q + 1);
+                        Real pre = -ka * exp_r(-u);
+#pragma unroll
+                        for (int q = 0; q < 6; ++q) {
+                            gam[q] = pre * T[q];
+                            pre *= 2 * alpha2;
+                        }
+                    } else if (r2 < smallR2) {
                         Real alphan = ka;
                         Real s = r2 * alpha2;
                         gam[0] = alphan * (s / 3 - 1);
@@ -264,7 +302,12 @@ __global__ void __launch_bounds__(128) k_ewald(TsphDevParts P, TsphDevCounters *
                         alphan *= 2 * alpha2;
                         gam[5] = 9 * gam[4] * dir2 + alphan * a;
                     }
-                    meval<Real>(iOrder, mom, gam, dxo, dyo, dzo, ax, ay, az, fPot);
+                    Real tx = 0, ty = 0, tz = 0, tp = 0;
+                    meval<Real>(iOrder, mom, gam, dxo, dyo, dzo, tx, ty, tz, tp);
+                    kadd(ax, cax, tx);
+                    kadd(ay, cay, ty);
+                    kadd(az, caz, tz);
+                    kadd(fPot, cpot, tp);
                     ++nLoop;
                 }
             }
@@ -275,16 +318,26 @@ __global__ void __launch_bounds__(128) k_ewald(TsphDevParts P, TsphDevCounters *
             Real hdotx = hx * dx + hy * dy + hz * dz;
             Real s, c;
             sincos_r(hdotx, &s, &c);
-            fPot += hC * c + hS * s;
+            kadd(fPot, cpot, hC * c + hS * s);
             Real t = hC * s - hS * c;
-            ax += hx * t;
-            ay += hy * t;
-            az += hz * t;
+            kadd(ax, cax, hx * t);
+            kadd(ay, cay, hy * t);
+            kadd(az, caz, hz * t);
         }
-        P.pot[p] += (double)fPot;
-        P.ax[p] += (double)ax;
-        P.ay[p] += (double)ay;
-        P.az[p] += (double)az;
+        if constexpr (sizeof(Real) == 4) {
+            // walk (compensated FP32 pair) + Ewald (compensated FP32 pair), in FP64
+            float4 ws = P.wsum[p], wc = P.wcmp[p];
+            P.ax[p] = ((double)ws.x - (double)wc.x) + ((double)ax - (double)cax);
+            P.ay[p] = ((double)ws.y - (double)wc.y) + ((double)ay - (double)cay);
+            P.az[p] = ((double)ws.z - (double)wc.z) + ((double)az - (double)caz);
+            P.pot[p] = ((double)ws.w - (double)wc.w) + ((double)fPot - (double)cpot);
+            P.dtGrav[p] = (double)P.wdt[p];
+        } else {
+            P.pot[p] += (double)fPot;
+            P.ax[p] += (double)ax;
+            P.ay[p] += (double)ay;
+            P.az[p] += (double)az;
+        }
     }
     // count real-space terms
 #pragma unroll

@@ -32,7 +32,7 @@
 #define NB 8                    // particles per bucket handled per warp
 #define SLOTS (32 / NB)         // entry slots per particle
 #define WPB 4                   // warps per block
-#define STK 2048                // walk stack entries per warp
+#define STK 1536                // walk stack entries per warp (~32 x tree depth)
 #define PPF 128                 // P-P tile size
 #define PPB (PPF + 32 * NB + NB)
 #define CNF 64                  // cell tile size
@@ -98,6 +98,30 @@ __device__ __forceinline__ bool intersect_exact(const double *bmin, const double
     if (dz > 0.0) d2 = xadd(d2, xmul(dz, dz));
     else if (dz1 > 0.0) d2 = xadd(d2, xmul(dz1, dz1));
     return d2 <= fBall2;
+}
+
+// The reference's FP64 decisions for one (bucket, cell, replica), used only
+// when the FP32 filter cannot settle them.  Returns 0 = not opened
+// (Newtonian), 1 = opened, 2 = not opened (softened) when !openTestOnly.
+__device__ __noinline__ int exact_decision(const TsphDevTree &T, const TsphDevParts &P, int node,
+                                           int lo, int n, int cell, const double *off,
+                                           bool openTestOnly) {
+    double bmn[3], bmx[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        bmn[k] = T.bnd[6 * node + k];
+        bmx[k] = T.bnd[6 * node + 3 + k];
+    }
+    double x = xadd(T.r[3 * cell], off[0]);
+    double y = xadd(T.r[3 * cell + 1], off[1]);
+    double z = xadd(T.r[3 * cell + 2], off[2]);
+    if (openTestOnly) return intersect_exact(bmn, bmx, T.fOpen2[cell], x, y, z) ? 1 : 0;
+    double fSoftMax = 0.0;
+    for (int p = lo; p < lo + n; ++p) fSoftMax = fmax(fSoftMax, P.h[p]);
+    double twoh2 = xadd(T.fSoft[cell], fSoftMax);
+    twoh2 = xmul(twoh2, twoh2);
+    if (twoh2 < T.fOpen2[cell]) return 0;
+    return intersect_exact(bmn, bmx, twoh2, x, y, z) ? 2 : 0;
 }
 
 // Three-way FP32 filter: +1 certainly D2 > F, -1 certainly D2 <= F, 0 unsure.
@@ -325,9 +349,11 @@ __device__ __forceinline__ void eval_newt(WalkSmem<Real> &S, int cnt, int i, int
         ax -= dx * Qta;
         ay -= dy * Qta;
         az -= dz * Qta;
-        A.t[0] += ax;
-        A.t[1] += ay;
-        A.t[2] += az;
+        // far cells give O(1) terms that cancel to a small net force in a
+        // periodic box: compensate each term, not only each tile
+        kahan_add(A.s[0], A.c[0], ax);
+        kahan_add(A.s[1], A.c[1], ay);
+        kahan_add(A.s[2], A.c[2], az);
         A.t[3] += pot;
         Real idt2 = (mi + m) * g1;
         A.dt = idt2 > A.dt ? idt2 : A.dt;
@@ -355,9 +381,9 @@ __device__ __forceinline__ void eval_soft(WalkSmem<Real> &S, int cnt, int i, int
         Real tr = Real(0.5) * (xx + yy + zz);
         Real qir3 = b * m + d * qir - c * tr;
         A.t[3] -= a * m + c * qir - b * tr;
-        A.t[0] -= qir3 * dx - c * qirx;
-        A.t[1] -= qir3 * dy - c * qiry;
-        A.t[2] -= qir3 * dz - c * qirz;
+        kahan_add(A.s[0], A.c[0], -(qir3 * dx - c * qirx));
+        kahan_add(A.s[1], A.c[1], -(qir3 * dy - c * qiry));
+        kahan_add(A.s[2], A.c[2], -(qir3 * dz - c * qirz));
         Real idt2 = (mi + m) * b;
         A.dt = idt2 > A.dt ? idt2 : A.dt;
     }
@@ -399,41 +425,41 @@ __global__ void __launch_bounds__(WPB * 32) k_walk(WalkArgs W) {
             if (lane == 0) atomicOr(&W.cnt->status, 1u << TSPH_ERR_UNSUPPORTED);
             continue;
         }
-        // bucket geometry (FP64 once per bucket)
-        double bmn[3], bmx[3], bc[3];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            bmn[k] = T.bnd[6 * node + k];
-            bmx[k] = T.bnd[6 * node + 3 + k];
-            bc[k] = 0.5 * (bmn[k] + bmx[k]);
+        // bucket geometry: FP32 records prepared once per bucket (k_bucket_prep)
+        // for the FP32 path; the FP64 twin reads the FP64 bounds directly
+        float bch[3], bcl[3], fbmn[3], fbmx[3], bext, fSoftMaxF;
+        double bc64[3];
+        {
+            float4 r0 = T.brec[4 * b], r1 = T.brec[4 * b + 1];
+            float4 r2 = T.brec[4 * b + 2], r3 = T.brec[4 * b + 3];
+            bch[0] = r0.x; bch[1] = r0.y; bch[2] = r0.z; fSoftMaxF = r0.w;
+            bcl[0] = r1.x; bcl[1] = r1.y; bcl[2] = r1.z; bext = r1.w;
+            fbmn[0] = r2.x; fbmn[1] = r2.y; fbmn[2] = r2.z;
+            fbmx[0] = r3.x; fbmx[1] = r3.y; fbmx[2] = r3.z;
         }
-        float bch[3], bcl[3], fbmn[3], fbmx[3];
-        float bext = 0.0f;
+        if constexpr (sizeof(Real) == 8) {
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            split2f(bc[k], bch[k], bcl[k]);
-            fbmn[k] = (float)(bmn[k] - bc[k]);
-            fbmx[k] = (float)(bmx[k] - bc[k]);
-            bext = fmaxf(bext, fmaxf(fabsf(fbmn[k]), fabsf(fbmx[k])));
+            for (int k = 0; k < 3; ++k) bc64[k] = 0.0;
         }
-        double fSoftMax = 0.0;
-        for (int p = lo; p <= lo + n - 1; ++p) fSoftMax = fmax(fSoftMax, P.h[p]);
-        const float fSoftMaxF = (float)fSoftMax;
         // bucket particles
         if (lane < NB) {
             int p = lo + (lane < n ? lane : 0);
-            if (sizeof(Real) == 4) {
-                S.px[lane] = (Real)(float)(P.x[p] - bc[0]);
-                S.py[lane] = (Real)(float)(P.y[p] - bc[1]);
-                S.pz[lane] = (Real)(float)(P.z[p] - bc[2]);
+            if constexpr (sizeof(Real) == 4) {
+                float4 a = P.ph[p], c = P.pl[p];
+                S.px[lane] = ((a.x - bch[0]) + (c.x - bcl[0]));
+                S.py[lane] = ((a.y - bch[1]) + (c.y - bcl[1]));
+                S.pz[lane] = ((a.z - bch[2]) + (c.z - bcl[2]));
+                S.pm[lane] = a.w;
+                S.ph[lane] = c.w;
             } else {
                 S.px[lane] = (Real)P.x[p];
                 S.py[lane] = (Real)P.y[p];
                 S.pz[lane] = (Real)P.z[p];
+                S.pm[lane] = (Real)P.m[p];
+                S.ph[lane] = (Real)P.h[p];
             }
-            S.pm[lane] = (Real)P.m[p];
-            S.ph[lane] = (Real)P.h[p];
         }
+        (void)bc64;
         // initial stack: the root in every replica; P-P buffer: the bucket's
         // own particles for the intra-bucket pairs (replica tag 31)
         int sp = 0, ppn = 0, cnn = 0, csn = 0, nPart = 0, nNewt = 0, nSoft = 0;
@@ -483,10 +509,7 @@ __global__ void __launch_bounds__(WPB * 32) k_walk(WalkArgs W) {
                     fo = filt(D2, M, ch.w, relF);
                     if (fo == 0) {
                         ++cExact;
-                        double x = xadd(T.r[3 * cell], cW.off[rep][0]);
-                        double y = xadd(T.r[3 * cell + 1], cW.off[rep][1]);
-                        double z = xadd(T.r[3 * cell + 2], cW.off[rep][2]);
-                        open = intersect_exact(bmn, bmx, T.fOpen2[cell], x, y, z);
+                        open = exact_decision(T, P, node, lo, n, cell, cW.off[rep], true) == 1;
                     } else {
                         open = fo < 0;
                     }
@@ -511,15 +534,7 @@ __global__ void __launch_bounds__(WPB * 32) k_walk(WalkArgs W) {
                     }
                     if (exactNeeded) {
                         ++cExact;
-                        double twoh2 = xadd(T.fSoft[cell], fSoftMax);
-                        twoh2 = xmul(twoh2, twoh2);
-                        if (twoh2 < T.fOpen2[cell]) newt = true;
-                        else {
-                            double x = xadd(T.r[3 * cell], cW.off[rep][0]);
-                            double y = xadd(T.r[3 * cell + 1], cW.off[rep][1]);
-                            double z = xadd(T.r[3 * cell + 2], cW.off[rep][2]);
-                            newt = !intersect_exact(bmn, bmx, twoh2, x, y, z);
-                        }
+                        newt = exact_decision(T, P, node, lo, n, cell, cW.off[rep], false) == 0;
                     }
                     act = newt ? ACT_NEWT : ACT_SOFT;
                 }
@@ -631,11 +646,17 @@ __global__ void __launch_bounds__(WPB * 32) k_walk(WalkArgs W) {
         }
         if (lane < n) {
             int p = lo + lane;
-            P.ax[p] = (double)A.s[0] - (double)A.c[0];
-            P.ay[p] = (double)A.s[1] - (double)A.c[1];
-            P.az[p] = (double)A.s[2] - (double)A.c[2];
-            P.pot[p] = (double)A.s[3] - (double)A.c[3];
-            P.dtGrav[p] = (double)A.dt;
+            if constexpr (sizeof(Real) == 4) {
+                P.wsum[p] = make_float4(A.s[0], A.s[1], A.s[2], A.s[3]);
+                P.wcmp[p] = make_float4(A.c[0], A.c[1], A.c[2], A.c[3]);
+                P.wdt[p] = A.dt;
+            } else {
+                P.ax[p] = (double)A.s[0];
+                P.ay[p] = (double)A.s[1];
+                P.az[p] = (double)A.s[2];
+                P.pot[p] = (double)A.s[3];
+                P.dtGrav[p] = (double)A.dt;
+            }
         }
         if (lane == 0) {
             cAct += n;
@@ -671,6 +692,53 @@ __global__ void __launch_bounds__(WPB * 32) k_walk(WalkArgs W) {
     }
 }
 
+// FP32 geometry of every bucket: centre (hi/lo), max softening, box
+// extent, box corners relative to the centre.  The FP64 work happens here
+// once per bucket, by one thread, instead of redundantly on every lane of
+// the walk (FP64 issues at 1/64 of the FP32 rate on this part).
+__global__ void k_bucket_prep(int nBuckets, TsphDevTree T, TsphDevParts P) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nBuckets) return;
+    int node = T.leaves[b];
+    int lo = T.pLower[node], hi = T.pUpper[node];
+    double bc[3];
+    float bh[3], bl[3], mn[3], mx[3];
+    float ext = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        double a = T.bnd[6 * node + k], c = T.bnd[6 * node + 3 + k];
+        bc[k] = 0.5 * (a + c);
+        split2f(bc[k], bh[k], bl[k]);
+        mn[k] = (float)(a - bc[k]);
+        mx[k] = (float)(c - bc[k]);
+        ext = fmaxf(ext, fmaxf(fabsf(mn[k]), fabsf(mx[k])));
+    }
+    double sm = 0.0;
+    for (int p = lo; p <= hi; ++p) sm = fmax(sm, P.h[p]);
+    T.brec[4 * b] = make_float4(bh[0], bh[1], bh[2], (float)sm);
+    T.brec[4 * b + 1] = make_float4(bl[0], bl[1], bl[2], ext);
+    T.brec[4 * b + 2] = make_float4(mn[0], mn[1], mn[2], 0.0f);
+    T.brec[4 * b + 3] = make_float4(mx[0], mx[1], mx[2], 0.0f);
+}
+
+// FP32 walk without an Ewald pass: fold the compensated pairs into FP64
+__global__ void k_finish_f32(int n, TsphDevParts P) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    float4 s = P.wsum[p], c = P.wcmp[p];
+    P.ax[p] = (double)s.x - (double)c.x;
+    P.ay[p] = (double)s.y - (double)c.y;
+    P.az[p] = (double)s.z - (double)c.z;
+    P.pot[p] = (double)s.w - (double)c.w;
+    P.dtGrav[p] = (double)P.wdt[p];
+}
+
+int tsph_walk_finish_f32(tsph_ctx *ctx) {
+    k_finish_f32<<<tsph_blocks(ctx->n, 256), 256, 0, ctx->stream>>>(ctx->n, ctx->P);
+    TSPH_LAUNCH_CK("k_finish_f32");
+    return TSPH_OK;
+}
+
 int tsph_walk_interact(tsph_ctx *ctx, const tsph_grav_params *gp) {
     if (gp->iOrder < 1 || gp->iOrder > 2) return TSPH_ERR_UNSUPPORTED;
     if (gp->bPeriodic && gp->nReps > 1) return TSPH_ERR_UNSUPPORTED;
@@ -700,8 +768,7 @@ int tsph_walk_interact(tsph_ctx *ctx, const tsph_grav_params *gp) {
     // absolute coordinate (positions + offsets)
     rabs = ctx->dPeriodTree + offmax;
     wc.E0 = (float)(16.0 * 3.552713678800501e-15 * rabs) + 1e-30f;
-    cudaMemcpyToSymbolAsync(cW, &wc, sizeof(wc), 0, cudaMemcpyHostToDevice, ctx->stream);
-    TSPH_LAUNCH_CK("cW");
+    TSPH_CK(cudaMemcpyToSymbolAsync(cW, &wc, sizeof(wc), 0, cudaMemcpyHostToDevice, ctx->stream));
 
     WalkArgs A;
     A.T = ctx->T;
@@ -719,6 +786,8 @@ int tsph_walk_interact(tsph_ctx *ctx, const tsph_grav_params *gp) {
     // work counter lives in the counters block's pad area
     A.workCounter = (int *)&ctx->dCnt->pad;
     TSPH_CK(cudaMemsetAsync(A.workCounter, 0, sizeof(int), ctx->stream));
+    k_bucket_prep<<<tsph_blocks(A.nBuckets, 128), 128, 0, ctx->stream>>>(A.nBuckets, ctx->T, ctx->P);
+    TSPH_LAUNCH_CK("k_bucket_prep");
     int blocks = ctx->smCount * 4;
     if (gp->precision == TSPH_FP32) {
         size_t sm = sizeof(WalkSmem<float>) * WPB;

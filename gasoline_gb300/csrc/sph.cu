@@ -201,7 +201,7 @@ __global__ void __launch_bounds__(SW * 32) k_knn_density(SphArgs A) {
     const int lane = threadIdx.x & 31;
     const unsigned FULL = 0xffffffffu;
     const int ng = cS.ngas, k = cS.k;
-    unsigned long long nFall = 0, nPairs = 0;
+    unsigned long long nFall = 0, nPairs = 0, nCand = 0;
     for (;;) {
         int i = 0;
         if (lane == 0) i = atomicAdd(A.work, 1);
@@ -250,6 +250,7 @@ __global__ void __launch_bounds__(SW * 32) k_knn_density(SphArgs A) {
             if (lane == 0) atomicOr(&A.cnt->status, 1u << TSPH_ERR_KNN_NO_CONVERGE);
             continue;
         }
+        nCand += nc;
         double fBall2 = select_kth(W, nc, k, lane);
         // DenDVDX over N(i) = {j : d2 <= fBall2} (smoothfcn.c:3390-3627)
         const double vxi = A.S.vx[i], vyi = A.S.vy[i], vzi = A.S.vz[i];
@@ -341,6 +342,7 @@ __global__ void __launch_bounds__(SW * 32) k_knn_density(SphArgs A) {
     if (lane == 0) {
         if (nFall) atomicAdd(&A.cnt->nExactTests, nFall);
         if (nPairs) atomicAdd(&A.cnt->nPartPP, nPairs);
+        if (nCand) atomicAdd(&A.cnt->nCellNewt, nCand);
     }
 }
 
@@ -569,6 +571,14 @@ __global__ void k_to_caller1(int ng, const int *__restrict__ iord, const double 
     dst[dstride * iord[i] + doff] = a[stride * i + off];
 }
 
+__global__ void k_save_prev(int ng, const int *__restrict__ iord, const double *__restrict__ fb2,
+                            const double *__restrict__ divv, double *fb2prev, double *divvprev) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ng) return;
+    fb2prev[iord[i]] = fb2[i];
+    divvprev[iord[i]] = divv[i];
+}
+
 __global__ void k_load_vel(int n, const double *__restrict__ v3, TsphDevState C) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -616,6 +626,7 @@ extern "C" int tsph_set_velocities(tsph_ctx *ctx, const double *vel, int ngas, c
     ctx->ngas = ngas;
     ctx->G.n = ngas;
     ctx->S.haveDensity = ctx->S.havePressure = false;
+    ctx->hnet.havePrev = false;
     if (n == 0) { ctx->haveVel = true; return TSPH_OK; }
     TSPH_CK(cudaMemcpyAsync(ctx->dStage, vel, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
     k_load_vel<<<tsph_blocks(n, 256), 256, 0, ctx->stream>>>(n, ctx->dStage, ctx->C);
@@ -644,6 +655,15 @@ static int run_density(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_out
     k_gas_gather_vel<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, ctx->C, ctx->G.iord, S);
     TSPH_LAUNCH_CK("k_gas_gather_vel");
     set_sph_const(ctx, sp);
+    const int kk = sp->nSmooth < ng ? sp->nSmooth : ng;
+    rc = tsph_hnet_features(ctx, kk);
+    if (rc) return rc;
+    if (sp->bLearnedH) {
+        rc = tsph_hnet_seed(ctx);
+        if (rc) return rc;
+    } else {
+        S.haveSeed = false;
+    }
     SphArgs A;
     A.T = ctx->TG;
     A.G = ctx->G;
@@ -665,6 +685,13 @@ static int run_density(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_out
     cudaEventElapsedTime(&ctx->timings[5], ctx->ev[6], ctx->ev[7]);
     unsigned st = ctx->hCnt->status;
     if (st) for (int k = 1; k < 32; ++k) if (st & (1u << k)) return k;
+    // h-network: samples of this pass, then this pass becomes "previous"
+    rc = tsph_hnet_append(ctx);
+    if (rc) return rc;
+    k_save_prev<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, ctx->G.iord, S.fBall2, S.divv,
+                                                              ctx->C.fb2prev, ctx->C.divvprev);
+    TSPH_LAUNCH_CK("k_save_prev");
+    ctx->hnet.havePrev = true;
     S.nFallback = (int)ctx->hCnt->nExactTests;
     S.haveDensity = true;
     S.havePressure = false;
@@ -673,6 +700,8 @@ static int run_density(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_out
         out->nSmoothed = ng;
         out->nFallback = S.nFallback;
         out->dPairs = (double)ctx->hCnt->nPartPP;
+        out->dCandidates = (double)ctx->hCnt->nCellNewt;
+        out->bSeeded = S.haveSeed ? 1 : 0;
     }
     return TSPH_OK;
 }
@@ -708,9 +737,8 @@ static int run_pressure(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_ou
     if (st) for (int k = 1; k < 32; ++k) if (st & (1u << k)) return k;
     S.havePressure = true;
     if (out) {
+        memset(out, 0, sizeof(*out));
         out->nSmoothed = ng;
-        out->nFallback = 0;
-        out->dPairs = 0;
     }
     return TSPH_OK;
 }

@@ -516,6 +516,8 @@ void tsph_free_tree(TsphDevTree &T) {
     TFREE(T.fSplit); TFREE(T.bnd); TFREE(T.fMass); TFREE(T.fSoft); TFREE(T.r);
     TFREE(T.fOpen2); TFREE(T.Bmax); TFREE(T.Q); TFREE(T.wcomh); TFREE(T.wcoml);
     TFREE(T.wlink); TFREE(T.wmom0); TFREE(T.wmom1); TFREE(T.leaves);
+    if (T.brec) cudaFree(T.brec);
+    T.brec = nullptr;
     T.cap = 0;
 }
 
@@ -543,6 +545,7 @@ static int ensure_nodes(tsph_ctx *ctx, TsphDevTree &T, int nNodes) {
     rc |= tsph_grow(ctx, &T.wmom0, cap);
     rc |= tsph_grow(ctx, &T.wmom1, cap);
     rc |= tsph_grow(ctx, &T.leaves, cap);
+    rc |= tsph_grow(ctx, &T.brec, (size_t)4 * cap);
     if (rc) return TSPH_ERR_NOMEM;
     T.cap = cap;
     // per-node scratch shared by both trees (sized to the larger)

@@ -42,6 +42,24 @@ struct TsphSphBufs {
     tsph_sph_params last;
 };
 
+// Learned smoothing-length network (3 -> 32 -> 32 -> 1, tanh, FP32).
+#define HNET_H 32
+#define HNET_NP (HNET_H * 3 + HNET_H + HNET_H * HNET_H + HNET_H + HNET_H + 1)
+struct TsphHnet {
+    float *W;            // parameters, layout W1[32x3] b1[32] W2[32x32] b2[32] W3[32] b3
+    float *grad;         // full gradient
+    float *m1, *m2;      // Adam moments
+    float *partial;      // per-warp partial gradients
+    float *loss;         // per-warp partial losses
+    float *feat;         // features of the current density pass (gas-tree order), 3 per particle
+    float *samples;      // training samples: 4 floats (x0,x1,x2,target) each
+    long long nSamples, capSamples;
+    float stats[8];      // mean/std of the three features and the target
+    bool init, statsReady, trained, collect, predict, havePrev;
+    double margin;       // log-radius safety margin of the seed
+    long long adamStep;
+};
+
 struct tsph_ctx {
     int device;
     cudaStream_t stream;
@@ -79,6 +97,8 @@ struct tsph_ctx {
     bool haveParts, haveVel, haveTree, haveGrav;
     tsph_grav_params lastGrav;
     double dPeriodTree;
+
+    TsphHnet hnet;
 
     cudaEvent_t ev[10];
     float timings[8];
@@ -122,7 +142,13 @@ int tsph_copy_out_n(tsph_ctx *ctx, int n, const double *a0, const double *a1, co
                     int comp, double *host);
 void tsph_free_tree(TsphDevTree &T);
 int tsph_walk_interact(tsph_ctx *ctx, const tsph_grav_params *gp);
+int tsph_walk_finish_f32(tsph_ctx *ctx);
 int tsph_ewald(tsph_ctx *ctx, const tsph_grav_params *gp);
 int tsph_ensure_particles(tsph_ctx *ctx, int n);
 int tsph_sph_density(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_out *out);
+// h-network hooks used by the density pass (mlp.cu)
+int tsph_hnet_features(tsph_ctx *ctx, int k);
+int tsph_hnet_seed(tsph_ctx *ctx);
+int tsph_hnet_append(tsph_ctx *ctx);
+void tsph_hnet_free(tsph_ctx *ctx);
 int tsph_sph_pressure(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_out *out);

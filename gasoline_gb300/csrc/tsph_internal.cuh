@@ -59,6 +59,8 @@ struct TsphDevTree {
     float4 *wmom0;    // m, Qxx, Qyy, Qzz
     float4 *wmom1;    // Qxy, Qxz, Qyz, fSoft
     int *leaves;      // leaf node ids in depth-first order (the buckets)
+    float4 *brec;     // per bucket: centre hi + soft max, centre lo + extent,
+                      // box min - centre (+ n), box max - centre (FP32)
 };
 
 struct TsphDevParts {
@@ -70,6 +72,10 @@ struct TsphDevParts {
     float4 *pl;                  // lo xyz + soft (float)
     // outputs in tree order
     double *ax, *ay, *az, *pot, *dtGrav;
+    // FP32 walk results as compensated pairs (sum, negated low part) of
+    // (ax, ay, az, pot), combined in FP64 with the Ewald term
+    float4 *wsum, *wcmp;
+    float *wdt;
 };
 
 // Particle state in the caller's order (the reference's iOrder): what the
@@ -80,6 +86,7 @@ struct TsphDevState {
     double *vpx, *vpy, *vpz, *upred;     // predicted (time-centred) v and u
     double *ax, *ay, *az, *pot, *dtGrav; // gravity
     double *hax, *hay, *haz, *udot;      // SPH (gas only): hydro accel, uDotPdV+uDotAV
+    double *fb2prev, *divvprev;          // last density pass: fBall2, divv (h-network inputs)
 };
 
 // Counters accumulated by the walk (integers: deterministic).

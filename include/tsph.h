@@ -122,8 +122,11 @@ typedef struct {
 
 typedef struct {
     int nSmoothed;        /* SMF.nSmoothed */
-    int nFallback;        /* particles whose seeded ball held < nSmooth */
+    int nFallback;        /* ball radii grown because a ball held < nSmooth */
     double dPairs;        /* neighbour pairs gathered */
+    double dCandidates;   /* particles inside the gathered balls (kNN cost) */
+    int bSeeded;          /* 1 when the learned-h prediction seeded the balls */
+    int reserved;
 } tsph_smooth_out;
 
 /* --- context --------------------------------------------------------- */
@@ -190,6 +193,30 @@ int tsph_get_sph(tsph_ctx *ctx, double *out16, double *dtNew, double *mumax);
 int tsph_get_neighbour_hash(tsph_ctx *ctx, int *count,
                             unsigned long long *hash);
 
+/* --- learned smoothing length (no counterpart in the reference) --------
+ * A 3 -> 32 -> 32 -> 1 tanh network (FP32) predicts each gas particle's
+ * log(fBall2_now / fBall2_prev) from the last pass's fBall2 and divv and the
+ * density of the deepest gas-tree cell holding >= nSmooth particles.  With
+ * sph.bLearnedH the prediction (widened by `margin` in log radius) seeds the
+ * DENDVDX ball gather; balls holding < nSmooth grow and retry, so fBall2
+ * and the neighbour sets are those of the exact kNN.  Training runs on the
+ * GPU (Adam) over samples collected from earlier passes. */
+int tsph_hnet_num_params(void);
+int tsph_hnet_init(tsph_ctx *ctx, unsigned long long seed);
+int tsph_hnet_set_params(tsph_ctx *ctx, const float *params, int n);
+int tsph_hnet_get_params(tsph_ctx *ctx, float *params, int n);
+/* 0.5*mean((net(x)-y)^2) and its gradient over given normalised samples
+ * x[3n], y[n] (for gradient checks). */
+int tsph_hnet_loss_grad(tsph_ctx *ctx, int n, const float *x3, const float *y,
+                        float *grad, double *loss);
+/* collect: append each DENDVDX pass's (features, target) samples;
+ * predict: allow seeding (needs a trained network). */
+int tsph_hnet_mode(tsph_ctx *ctx, int collect, int predict, double margin);
+/* `steps` Adam steps on random batches of the collected samples; *loss is
+ * the final loss over all samples (normalised units). */
+int tsph_hnet_train(tsph_ctx *ctx, int steps, int batch, double lr, double *loss);
+int tsph_hnet_info(tsph_ctx *ctx, long long *nSamples, float *stats8);
+
 /* --- kick-drift-kick (pkdKick / pkdDrift) ------------------------------ */
 
 /* v += a*dt (a = gravity + hydro); gas: vPred = v_old + a*dt,
@@ -207,6 +234,9 @@ int tsph_get_state(tsph_ctx *ctx, double *pos, double *vel, double *u);
 int tsph_get_timings(tsph_ctx *ctx, float *t8);
 /* Number of libtsph kernel launches issued since context creation. */
 long long tsph_launch_count(tsph_ctx *ctx);
+/* Measured FMA throughput of this GPU in TFLOP/s (precision FP32 or FP64),
+ * the denominator of the force kernels' roofline fraction. */
+int tsph_fma_peak(tsph_ctx *ctx, int precision, double *tflops);
 
 #ifdef __cplusplus
 }

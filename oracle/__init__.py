@@ -177,6 +177,17 @@ def knn_fball2(pos, nsmooth, periodic=False, L=1.0, nthreads=1):
     return out
 
 
+class exact_rsqrt:
+    """Context manager: the oracle takes 1/r as 1.0/sqrt(r2) instead of the
+    reference's v_sqrt1 approximation while active."""
+
+    def __enter__(self):
+        oracle().lib.orc_set_exact_rsqrt(1)
+
+    def __exit__(self, *a):
+        oracle().lib.orc_set_exact_rsqrt(0)
+
+
 def v_sqrt1(r2):
     r2 = _c64(r2)
     out = np.zeros_like(r2)

@@ -361,7 +361,14 @@ static void vs_init(void) {
     g_vs_init = 1;
 }
 
+/* When set, 1/sqrt is taken as 1.0/sqrt(r2) instead of the reference's
+ * v_sqrt1 approximation (used to separate the reference's own 2e-10 1/sqrt
+ * error from other differences). */
+static int g_exact_rsqrt = 0;
+void orc_set_exact_rsqrt(int on) { g_exact_rsqrt = on; }
+
 static inline double vs_one(double r2) {
+    if (g_exact_rsqrt) return 1.0 / sqrt(r2);
     uint64_t bits;
     int it;
     double x, s;

@@ -76,6 +76,10 @@ void orc_kdk(int n, int which, double dt, int bPeriodic, double dPeriod,
              double *pos, double *vel, const double *acc, int ngas,
              double *u, const double *udot, double *vpred, double *upred);
 
+/* Use 1.0/sqrt(r2) in place of v_sqrt1 for the interaction 1/r (off by
+ * default, which restates the reference exactly). */
+void orc_set_exact_rsqrt(int on);
+
 /* v_sqrt1 restated (reference v_sqrt1.c:11-113). */
 void orc_v_sqrt1(int n, const double *r2, double *a);
 
