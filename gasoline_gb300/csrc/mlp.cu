@@ -1,7 +1,7 @@
 // K11: learned smoothing length (no counterpart in the reference).
 //
 // A 3 -> 32 -> 32 -> 1 tanh network, FP32, predicts for every gas particle
-// t = log(fBall2_now) - log(fBall2_prev) from
+// t = log(fBall2_now) from
 //   f0 = log(fBall2_prev)                       (last density pass)
 //   f1 = (2/3) log(V_A / n_A)                   (deepest gas-tree cell A
 //                                                holding >= nSmooth particles)
@@ -170,7 +170,7 @@ __global__ void k_hnet_features(int ng, int k, TsphDevTree T, const int *__restr
     feat[3 * i + 2] = (float)divvprev[o];
 }
 
-// seed fBall2 = exp(f0 + t_pred + 2*margin) for the kNN ball gather
+// seed fBall2 = exp(t_pred + 2*margin) for the kNN ball gather
 __global__ void k_hnet_predict(int ng, const float *__restrict__ W, const float *__restrict__ feat,
                                const float *__restrict__ st, double margin, double *seed) {
     __shared__ float Ws[HNET_NP];
@@ -189,7 +189,7 @@ __global__ void k_hnet_predict(int ng, const float *__restrict__ W, const float 
         float o = sample_fwd_bwd(Ws, x, 0.0f, lane, g, false);
         if (lane == 0) {
             double t = (double)o * st[7] + st[6];
-            seed[i] = exp((double)f[0] + t + 2.0 * margin);
+            seed[i] = exp(t + 2.0 * margin);
         }
     }
 }
@@ -203,7 +203,7 @@ __global__ void k_hnet_append(int ng, const float *__restrict__ feat, const doub
     s[0] = feat[3 * i];
     s[1] = feat[3 * i + 1];
     s[2] = feat[3 * i + 2];
-    s[3] = (float)(log(fBall2[i]) - (double)feat[3 * i]);
+    s[3] = (float)log(fBall2[i]);
 }
 
 // mean and std of the 4 sample columns (fixed-order reduction, one block)

@@ -195,7 +195,7 @@ int tsph_get_neighbour_hash(tsph_ctx *ctx, int *count,
 
 /* --- learned smoothing length (no counterpart in the reference) --------
  * A 3 -> 32 -> 32 -> 1 tanh network (FP32) predicts each gas particle's
- * log(fBall2_now / fBall2_prev) from the last pass's fBall2 and divv and the
+ * log(fBall2) from the last pass's fBall2 and divv and the
  * density of the deepest gas-tree cell holding >= nSmooth particles.  With
  * sph.bLearnedH the prediction (widened by `margin` in log radius) seeds the
  * DENDVDX ball gather; balls holding < nSmooth grow and retry, so fBall2
