@@ -217,6 +217,26 @@ int tsph_hnet_mode(tsph_ctx *ctx, int collect, int predict, double margin);
 int tsph_hnet_train(tsph_ctx *ctx, int steps, int batch, double lr, double *loss);
 int tsph_hnet_info(tsph_ctx *ctx, long long *nSamples, float *stats8);
 
+/* Loss and gradient of the h-network without allocating device memory.  No
+ * counterpart in the reference.  For callers that cannot allocate where they
+ * need the gradient: a host code that reserves all its device memory up
+ * front and updates the network inside its step loop, where a cudaMalloc
+ * would synchronise the device and stall its other streams, or exceed a
+ * fixed memory budget.  Every argument is a device pointer: params[
+ * tsph_hnet_num_params()], normalised samples x3[3n] and y[n]; outputs
+ * grad[tsph_hnet_num_params()] and loss[1] (0.5*mean((net(x)-y)^2)).  Runs
+ * on `stream` (a cudaStream_t, NULL = default) of the current device and
+ * returns without synchronising.  Scratch lives in one fixed device array
+ * of ~2.5 MB that the library holds on every GPU that loads it until exit;
+ * n above TSPH_HNET_NOALLOC_MAX_SAMPLES returns TSPH_ERR_ARG.  The first
+ * call on each device looks up that array's address (make it before any
+ * stream capture).  Calls share the array: calls that overlap on the GPU
+ * race and must be serialised by the caller. */
+#define TSPH_HNET_NOALLOC_MAX_SAMPLES 16384
+int tsph_hnet_loss_grad_noalloc(const float *params, int n, const float *x3,
+                                const float *y, float *grad, float *loss,
+                                void *stream);
+
 /* --- kick-drift-kick (pkdKick / pkdDrift) ------------------------------ */
 
 /* v += a*dt (a = gravity + hydro); gas: vPred = v_old + a*dt,
