@@ -113,11 +113,36 @@ struct SphArgs {
     const double *seed;     // optional fBall2 seeds (tree order) or null
 };
 
+#define SNBR 256      // neighbours summed in canonical (index) order
+
 struct KnnSmem {
     int stack[SSTK];
     double d2[SCAP];
     int idx[SCAP];
+    int nbr[SNBR];
 };
+
+// Sort nbr[0, cnt) ascending (bitonic network over the next power of two,
+// padded with INT_MAX), one warp.
+__device__ void warp_sort_idx(int *nbr, int cnt, int lane) {
+    int P = 1;
+    while (P < cnt) P <<= 1;
+    for (int e = cnt + lane; e < P; e += 32) nbr[e] = 0x7fffffff;
+    __syncwarp();
+    for (int k = 2; k <= P; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = lane; i < P; i += 32) {
+                int l = i ^ j;
+                if (l > i) {
+                    int a = nbr[i], b = nbr[l];
+                    bool up = (i & k) == 0;
+                    if ((a > b) == up) { nbr[i] = b; nbr[l] = a; }
+                }
+            }
+            __syncwarp();
+        }
+    }
+}
 
 // Ball gather of all gas particles with d2 <= r2 around particle i.
 // Returns the count, or -1 when it exceeds SCAP or the stack overflows.
@@ -259,12 +284,31 @@ __global__ void __launch_bounds__(SW * 32) k_knn_density(SphArgs A) {
         double s[14];
 #pragma unroll
         for (int q = 0; q < 14; ++q) s[q] = 0.0;
+        // N(i) in ascending particle order, so the sums below depend only on
+        // the neighbour set, not on the order the ball gather found them
+        int nsel = 0;
+        for (int e0 = 0; e0 < nc; e0 += 32) {
+            int e = e0 + lane;
+            bool in = e < nc && W.d2[e] <= fBall2;
+            unsigned bi = __ballot_sync(FULL, in);
+            if (in && nsel + __popc(bi & lane_lt_s()) < SNBR)
+                W.nbr[nsel + __popc(bi & lane_lt_s())] = W.idx[e];
+            nsel += __popc(bi);
+        }
+        __syncwarp();
+        const bool sorted = nsel <= SNBR;
+        if (sorted) warp_sort_idx(W.nbr, nsel, lane);
         int nn = 0;
         unsigned long long hsh = 0ULL;
-        for (int e = lane; e < nc; e += 32) {
-            double d2 = W.d2[e];
-            if (d2 > fBall2) continue;
-            int j = W.idx[e];
+        const int nloop = sorted ? nsel : nc;
+        for (int e = lane; e < nloop; e += 32) {
+            int j;
+            if (sorted) {
+                j = W.nbr[e];
+            } else {                             // more than SNBR ties: gather order
+                if (W.d2[e] > fBall2) continue;
+                j = W.idx[e];
+            }
             ++nn;
             unsigned long long hx = (unsigned long long)(A.G.iord[j] + 1);
             hx *= 0x9E3779B97F4A7C15ULL;
@@ -273,7 +317,7 @@ __global__ void __launch_bounds__(SW * 32) k_knn_density(SphArgs A) {
             hx ^= hx >> 32;
             hsh += hx;
             double dx, dy, dz;
-            dist2_exact(xi, yi, zi, A.G.x[j], A.G.y[j], A.G.z[j], dx, dy, dz);
+            const double d2 = dist2_exact(xi, yi, zi, A.G.x[j], A.G.y[j], A.G.z[j], dx, dy, dz);
             double r2k = d2 * ih2;
             double mj = A.G.m[j];
             double rs = kern_m4(r2k);

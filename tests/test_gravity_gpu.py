@@ -25,6 +25,10 @@ FP32_RMS = 3e-5
 # a net force ~50x smaller than either, which amplifies the reference's own
 # v_sqrt1 error (2e-10 per term) to ~1e-8 and FP32 rounding to ~1e-4.
 PER_FP64_VS_REF_RMS = 3e-8
+# The periodic potential crosses zero, so its per-particle relative error is
+# unbounded; it is measured against max |pot| instead (the exact-rsqrt oracle
+# itself sits at 2e-8 of max |pot| from the reference's potential).
+PER_POT_VS_REF_SCALED = 1e-7
 PER_FP64_VS_EXACT_RMS = 1e-12
 PER_FP32_P99 = 3e-4
 
@@ -81,8 +85,12 @@ def test_fp64_forces_vs_reference(ctx, name):
     e = rel_err(r["acc"], d["acc"])
     bar = PER_FP64_VS_REF_RMS if gp.bPeriodic else FP64_RMS
     assert rms(e) < bar, (rms(e), e.max())
-    ep = rel_err(r["pot"], d["pot"])
-    assert rms(ep) < bar
+    if gp.bPeriodic:
+        ep = np.abs(r["pot"] - d["pot"]) / np.abs(d["pot"]).max()
+        assert rms(ep) < PER_POT_VS_REF_SCALED, (rms(ep), ep.max())
+    else:
+        ep = rel_err(r["pot"], d["pot"])
+        assert rms(ep) < bar
     edt = rel_err(r["dtGrav"], d["dtGrav"])
     assert edt.max() < 1e-8
 
@@ -131,6 +139,8 @@ def test_periodic_box_16_vs_oracle(ctx, orc, prec):
     if prec == g.FP64:
         assert rms(e) < PER_FP64_VS_EXACT_RMS, (rms(e), e.max())
         assert rms(rel_err(r["acc"], ref0["acc"])) < PER_FP64_VS_REF_RMS
+        ep = np.abs(r["pot"] - ref["pot"]) / np.abs(ref["pot"]).max()
+        assert rms(ep) < PER_FP64_VS_EXACT_RMS, (rms(ep), ep.max())
     else:
         assert np.percentile(e, 99) < PER_FP32_P99, np.percentile(e, 99)
     assert r["out"]["dCellSum"] == ref["counters"][2]
