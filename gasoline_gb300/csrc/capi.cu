@@ -77,7 +77,7 @@ extern "C" void tsph_destroy(tsph_ctx *ctx) {
     TsphDevParts *PP[2] = {&ctx->P, &ctx->G};
     for (int k = 0; k < 2; ++k) {
         TsphDevParts &P = *PP[k];
-        FREE(P.x); FREE(P.y); FREE(P.z); FREE(P.m); FREE(P.h); FREE(P.iord);
+        FREE(P.x); FREE(P.y); FREE(P.z); FREE(P.m); FREE(P.h); FREE(P.iord); FREE(P.rid);
         FREE(P.ph); FREE(P.pl); FREE(P.ax); FREE(P.ay); FREE(P.az); FREE(P.pot); FREE(P.dtGrav);
         FREE(P.wsum); FREE(P.wcmp); FREE(P.wdt);
     }
@@ -85,10 +85,7 @@ extern "C" void tsph_destroy(tsph_ctx *ctx) {
     tsph_free_tree(ctx->TG);
     TsphBuildBufs &B = ctx->B;
     FREE(B.seg); FREE(B.lt); FREE(B.scan); FREE(B.scanTmp);
-    for (int k = 0; k < 2; ++k) { FREE(B.f_lo[k]); FREE(B.f_hi[k]); FREE(B.f_node[k]); }
-    FREE(B.f_split); FREE(B.f_rank); FREE(B.f_dim); FREE(B.f_m); FREE(B.f_fs); FREE(B.f_bnd);
-    FREE(B.t_lo); FREE(B.t_hi); FREE(B.t_dim); FREE(B.t_child); FREE(B.t_size); FREE(B.t_pre);
-    FREE(B.t_level); FREE(B.t_split); FREE(B.t_bnd); FREE(B.maxd2); FREE(B.leafFlag); FREE(B.leafScan);
+    tsph_free_build(B);
     TsphSphBufs &S = ctx->S;
     FREE(S.vx); FREE(S.vy); FREE(S.vz); FREE(S.u); FREE(S.fBall2); FREE(S.rho); FREE(S.divv);
     FREE(S.curl); FREE(S.dvds); FREE(S.bal); FREE(S.diff); FREE(S.pr2); FREE(S.cs); FREE(S.dtp);
@@ -135,23 +132,11 @@ int tsph_ensure_particles(tsph_ctx *ctx, int n) {
     TsphBuildBufs &B = ctx->B;
     rc |= tsph_grow(ctx, &B.seg, cap); rc |= tsph_grow(ctx, &B.lt, cap); rc |= tsph_grow(ctx, &B.scan, cap);
     rc |= tsph_grow(ctx, &B.scanTmp, cap / 1024 + 4096);
-    for (int k = 0; k < 2; ++k) {
-        rc |= tsph_grow(ctx, &B.f_lo[k], cap); rc |= tsph_grow(ctx, &B.f_hi[k], cap);
-        rc |= tsph_grow(ctx, &B.f_node[k], cap);
-    }
-    rc |= tsph_grow(ctx, &B.f_split, cap); rc |= tsph_grow(ctx, &B.f_rank, cap);
-    rc |= tsph_grow(ctx, &B.f_dim, cap); rc |= tsph_grow(ctx, &B.f_m, cap);
-    rc |= tsph_grow(ctx, &B.f_fs, cap); rc |= tsph_grow(ctx, &B.f_bnd, (size_t)6 * cap);
-    int tcap = 2 * cap + 2;
-    rc |= tsph_grow(ctx, &B.t_lo, tcap); rc |= tsph_grow(ctx, &B.t_hi, tcap);
-    rc |= tsph_grow(ctx, &B.t_dim, tcap); rc |= tsph_grow(ctx, &B.t_child, tcap);
-    rc |= tsph_grow(ctx, &B.t_size, tcap); rc |= tsph_grow(ctx, &B.t_pre, tcap);
-    rc |= tsph_grow(ctx, &B.t_level, tcap); rc |= tsph_grow(ctx, &B.t_split, tcap);
-    rc |= tsph_grow(ctx, &B.t_bnd, (size_t)6 * tcap);
+    rc |= tsph_grow(ctx, &P.rid, cap);
+    rc |= tsph_grow(ctx, &G.rid, cap);
     rc |= tsph_grow(ctx, &ctx->dStage, (size_t)3 * cap);
     if (rc) return TSPH_ERR_NOMEM;
     B.cap = cap;
-    B.nodeCap = tcap;
     ctx->cap = cap;
     return TSPH_OK;
 }
@@ -224,6 +209,8 @@ extern "C" int tsph_set_particles(tsph_ctx *ctx, int n, const double *pos, const
     ctx->P.n = n;
     ctx->G.n = 0;
     if (n == 0) { ctx->haveParts = true; return TSPH_OK; }
+    rc = tsph_set_ranges(ctx, ctx->P, ctx->T, n, 1, &n);
+    if (rc) return rc;
     TSPH_CK(cudaMemcpyAsync(ctx->dStage, pos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
     k_load_state<<<tsph_blocks(n, 256), 256, 0, ctx->stream>>>(n, ctx->dStage, ctx->C, ctx->P.iord,
                                                                ctx->G.iord);

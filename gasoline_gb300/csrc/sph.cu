@@ -681,6 +681,8 @@ extern "C" int tsph_set_velocities(tsph_ctx *ctx, const double *vel, int ngas, c
         TSPH_LAUNCH_CK("k_load_u");
         k_gas_identity<<<tsph_blocks(ngas, 256), 256, 0, ctx->stream>>>(ngas, ctx->G.iord);
         TSPH_LAUNCH_CK("k_gas_identity");
+        int rc = tsph_set_ranges(ctx, ctx->G, ctx->TG, ngas, 1, &ngas);
+        if (rc) return rc;
     }
     ctx->haveVel = true;
     return TSPH_OK;

@@ -94,30 +94,84 @@ int tsph_scan_inclusive(tsph_ctx *ctx, const int *in, int *out, int n) {
 }
 
 // ---------------------------------------------------------------------------
-// level kernels
+// top phase: level-wise over all nodes larger than the task size
 // ---------------------------------------------------------------------------
-__global__ void k_init_build(int *seg, int n, int *f_lo, int *f_hi, int *f_node) {
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p < n) seg[p] = 0;
-    if (p == 0) { f_lo[0] = 0; f_hi[0] = n - 1; f_node[0] = 0; }
+__device__ __forceinline__ void key_init(double *t_bnd, int v) {
+    unsigned long long *k = reinterpret_cast<unsigned long long *>(t_bnd + 6 * v);
+    k[0] = k[1] = k[2] = ~0ULL;
+    k[3] = k[4] = k[5] = 0ULL;
 }
 
-__global__ void k_fbnd_init(unsigned long long *f_bnd, int F) {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= F) return;
+__device__ __forceinline__ void key_atomics(double *t_bnd, int s, const unsigned long long *mn,
+                                            const unsigned long long *mx) {
+    unsigned long long *k = reinterpret_cast<unsigned long long *>(t_bnd + 6 * s);
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        f_bnd[6 * s + k] = ~0ULL;      // min
-        f_bnd[6 * s + 3 + k] = 0ULL;   // max
+    for (int d = 0; d < 3; ++d) {
+        atomicMin(&k[d], mn[d]);
+        atomicMax(&k[3 + d], mx[d]);
     }
+}
+
+// Roots of the forest: temp ids 0..nR-1.  Roots larger than S start the top
+// phase's frontier; the others are subtree tasks straight away.
+__global__ void k_roots(int nR, const int *__restrict__ rLo, const int *__restrict__ rHi, int S,
+                        int *t_lo, int *t_hi, double *t_bnd, int *front, int *tasks,
+                        TsphBuildCtl *ctl) {
+    __shared__ int ws[2][32];
+    __shared__ int carry[2];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (threadIdx.x < 2) carry[threadIdx.x] = 0;
+    __syncthreads();
+    for (int base = 0; base < nR; base += blockDim.x) {
+        int r = base + threadIdx.x;
+        bool live = r < nR;
+        int lo = live ? rLo[r] : 0, hi = live ? rHi[r] : -1;
+        bool big = live && (hi - lo + 1 > S);
+        bool small = live && !big;
+        unsigned bb = __ballot_sync(0xffffffffu, big), bs = __ballot_sync(0xffffffffu, small);
+        if (lane == 0) { ws[0][w] = __popc(bb); ws[1][w] = __popc(bs); }
+        __syncthreads();
+        int ob = carry[0], os = carry[1], tb = 0, ts = 0;
+        for (int k = 0; k < nw; ++k) {
+            if (k < w) { ob += ws[0][k]; os += ws[1][k]; }
+            tb += ws[0][k];
+            ts += ws[1][k];
+        }
+        unsigned lt = (1u << lane) - 1u;
+        if (live) {
+            t_lo[r] = lo;
+            t_hi[r] = hi;
+            key_init(t_bnd, r);
+            if (big) front[ob + __popc(bb & lt)] = r;
+            else tasks[os + __popc(bs & lt)] = r;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) { carry[0] += tb; carry[1] += ts; }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        ctl->taskCount = carry[1];
+        ctl->taskNext = 0;
+        ctl->nTop = nR;
+        ctl->status = 0;
+        ctl->nNodes = 0;
+    }
+}
+
+__global__ void k_seg_init(int n, int *seg, const int *__restrict__ rid, const int *__restrict__ rHi,
+                           const int *__restrict__ rLo, int S) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    int r = rid[p];
+    seg[p] = (rHi[r] - rLo[r] + 1 > S) ? r : -1;
 }
 
 // Segmented min/max of positions per frontier node.  Particles of one node
 // are contiguous, so runs inside a warp are reduced with shuffles and the
 // run head issues the atomics.
 __global__ void k_bounds(const double *__restrict__ x, const double *__restrict__ y,
-                         const double *__restrict__ z, const int *__restrict__ seg,
-                         unsigned long long *f_bnd, int n) {
+                         const double *__restrict__ z, const int *__restrict__ seg, double *t_bnd,
+                         int n) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     int lane = threadIdx.x & 31;
     int s = (p < n) ? seg[p] : -1;
@@ -146,103 +200,94 @@ __global__ void k_bounds(const double *__restrict__ x, const double *__restrict_
     }
     int sp = __shfl_up_sync(0xffffffffu, s, 1);
     bool head = (lane == 0) || (sp != s);
-    if (s >= 0 && head) {
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            atomicMin(&f_bnd[6 * s + k], mn[k]);
-            atomicMax(&f_bnd[6 * s + 3 + k], mx[k]);
-        }
-    }
+    if (s >= 0 && head) key_atomics(t_bnd, s, mn, mx);
 }
 
-// Decide leaf/split for every frontier node (BuildBinary pkd.c:2460-2506).
-__global__ void k_split(int F, const int *__restrict__ f_lo, const int *__restrict__ f_hi,
-                        const int *__restrict__ f_node, const unsigned long long *__restrict__ f_bnd,
-                        int nBucket, int *f_split, int *f_dim, double *f_fs,
-                        int *t_lo, int *t_hi, int *t_dim, int *t_child, double *t_split,
-                        double *t_bnd, int *t_level, int level) {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= F) return;
+// Bounds keys -> doubles, and the split decision of a node
+// (BuildBinary pkd.c:2460-2506): split at the midpoint of the longest axis
+// unless the node holds at most nBucket particles or has zero extent.
+__device__ __forceinline__ bool decide_node(int v, int nBucket, int *t_lo, int *t_hi, int *t_dim,
+                                            int *t_child, double *t_split, double *t_bnd) {
+    // the keys were accumulated by atomics in L2: read them past L1
+    const unsigned long long *k = reinterpret_cast<const unsigned long long *>(t_bnd + 6 * v);
     double bmin[3], bmax[3];
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        bmin[k] = dunkey(f_bnd[6 * s + k]);
-        bmax[k] = dunkey(f_bnd[6 * s + 3 + k]);
+    for (int d = 0; d < 3; ++d) {
+        bmin[d] = dunkey(__ldcg(k + d));
+        bmax[d] = dunkey(__ldcg(k + 3 + d));
     }
-    int lo = f_lo[s], hi = f_hi[s], node = f_node[s];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        t_bnd[6 * v + d] = bmin[d];
+        t_bnd[6 * v + 3 + d] = bmax[d];
+    }
     int good = 0;
 #pragma unroll
-    for (int k = 0; k < 3; ++k)
-        if (bmax[k] > bmin[k]) good = 1;
-    t_lo[node] = lo;
-    t_hi[node] = hi;
-    t_level[node] = level;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        t_bnd[6 * node + k] = bmin[k];
-        t_bnd[6 * node + 3 + k] = bmax[k];
-    }
-    t_child[node] = -1;
-    if ((hi - lo + 1 > nBucket) && good) {
+    for (int d = 0; d < 3; ++d)
+        if (bmax[d] > bmin[d]) good = 1;
+    if ((t_hi[v] - t_lo[v] + 1 > nBucket) && good) {
         int d = 0;
         for (int j = 1; j < 3; ++j)
             if (xsub(bmax[j], bmin[j]) > xsub(bmax[d], bmin[d])) d = j;
-        double fs = xmul(0.5, xadd(bmin[d], bmax[d]));
-        f_split[s] = 1;
-        f_dim[s] = d;
-        f_fs[s] = fs;
-        t_dim[node] = d;
-        t_split[node] = fs;
-    } else {
-        f_split[s] = 0;
-        f_dim[s] = -1;
-        f_fs[s] = 0.0;
-        t_dim[node] = -1;
-        t_split[node] = 0.0;
+        t_dim[v] = d;
+        t_split[v] = xmul(0.5, xadd(bmin[d], bmax[d]));
+        return true;
     }
+    t_dim[v] = -1;
+    t_split[v] = 0.0;
+    t_child[v] = -1;
+    return false;
+}
+
+// Top-phase frontier: nodes of at most S particles become subtree tasks,
+// the others split here (or end as zero-extent leaves).
+__global__ void k_top_split(int F, const int *__restrict__ f_node, int S, int nBucket, int *t_lo,
+                            int *t_hi, int *t_dim, int *t_child, int *t_size, double *t_split,
+                            double *t_bnd, int *f_split, int *tasks, TsphBuildCtl *ctl) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= F) return;
+    int v = f_node[k];
+    if (t_hi[v] - t_lo[v] + 1 <= S) {
+        t_dim[v] = -2;                       // handed to a subtree task
+        f_split[k] = 0;
+        key_init(t_bnd, v);
+        tasks[atomicAdd(&ctl->taskCount, 1)] = v;
+        return;
+    }
+    bool sp = decide_node(v, nBucket, t_lo, t_hi, t_dim, t_child, t_split, t_bnd);
+    if (!sp) t_size[v] = 1;
+    f_split[k] = sp ? 1 : 0;
 }
 
 __global__ void k_flag(const double *__restrict__ x, const double *__restrict__ y,
                        const double *__restrict__ z, const int *__restrict__ seg,
-                       const int *__restrict__ f_split, const int *__restrict__ f_dim,
-                       const double *__restrict__ f_fs, int *lt, int n) {
+                       const int *__restrict__ t_dim, const double *__restrict__ t_split, int *lt,
+                       int n) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
     int s = seg[p];
     int v = 0;
-    if (s >= 0 && f_split[s]) {
-        int d = f_dim[s];
-        double r = d == 0 ? x[p] : (d == 1 ? y[p] : z[p]);
-        v = r < f_fs[s] ? 1 : 0;
+    if (s >= 0) {
+        int d = t_dim[s];
+        if (d >= 0) {
+            double r = d == 0 ? x[p] : (d == 1 ? y[p] : z[p]);
+            v = r < t_split[s] ? 1 : 0;
+        }
     }
     lt[p] = v;
 }
 
-// Swap each misplaced pair of the Hoare partition: the left element of rank
-// t (t-th element >= fSplit in [lo, m)) with the right element of rank t
-// (t-th element < fSplit counted from hi downwards in [m, hi]).
-__global__ void k_swap(double *x, double *y, double *z, double *m, double *h, int *iord,
-                       const int *__restrict__ seg, const int *__restrict__ f_split,
-                       const int *__restrict__ f_lo, const int *__restrict__ f_hi,
-                       const int *__restrict__ lt, const int *__restrict__ S, int n) {
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n) return;
-    int s = seg[p];
-    if (s < 0 || !f_split[s] || lt[p]) return;
-    int lo = f_lo[s], hi = f_hi[s];
-    int Slo = lo > 0 ? S[lo - 1] : 0;
-    int mid = lo + (S[hi] - Slo);          // first index of the upper part
-    if (p >= mid) return;                  // already in place
-    int ltBefore = (p > 0 ? S[p - 1] : 0) - Slo;
-    int t = (p - lo) - ltBefore;           // rank among misplaced-left
-    int target = S[hi] - t;                // S[q] value at the partner
-    // smallest q in [mid, hi] with S[q] >= target
-    int a = mid, b = hi;
+// Smallest q in [a, b] with S[q] >= target (S non-decreasing).
+__device__ __forceinline__ int lower_bound_scan(const int *__restrict__ S, int a, int b, int target) {
     while (a < b) {
         int c = (a + b) >> 1;
         if (S[c] >= target) b = c; else a = c + 1;
     }
-    int q = a;
+    return a;
+}
+
+__device__ __forceinline__ void swap_particles(double *x, double *y, double *z, double *m, double *h,
+                                               int *iord, int p, int q) {
     double t0;
     t0 = x[p]; x[p] = x[q]; x[q] = t0;
     t0 = y[p]; y[p] = y[q]; y[q] = t0;
@@ -252,38 +297,353 @@ __global__ void k_swap(double *x, double *y, double *z, double *m, double *h, in
     int ti = iord[p]; iord[p] = iord[q]; iord[q] = ti;
 }
 
-__global__ void k_children(int F, const int *__restrict__ f_lo, const int *__restrict__ f_hi,
-                           const int *__restrict__ f_node, const int *__restrict__ f_split,
-                           const int *__restrict__ f_rank, const int *__restrict__ S,
-                           int nTemp, int *f_m, int *t_child, int *nf_lo, int *nf_hi, int *nf_node) {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= F || !f_split[s]) return;
-    int lo = f_lo[s], hi = f_hi[s];
+// Swap each misplaced pair of the Hoare partition: the left element of rank
+// t (t-th element >= fSplit in [lo, m)) with the right element of rank t
+// (t-th element < fSplit counted from hi downwards in [m, hi]).  S is an
+// inclusive scan of the flags that starts at particle `base`.
+__global__ void k_swap(double *x, double *y, double *z, double *m, double *h, int *iord,
+                       const int *__restrict__ seg, const int *__restrict__ t_dim,
+                       const int *__restrict__ t_lo, const int *__restrict__ t_hi,
+                       const int *__restrict__ lt, const int *__restrict__ S, int n) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    int s = seg[p];
+    if (s < 0 || t_dim[s] < 0 || lt[p]) return;
+    int lo = t_lo[s], hi = t_hi[s];
+    int Slo = lo > 0 ? S[lo - 1] : 0;
+    int mid = lo + (S[hi] - Slo);          // first index of the upper part
+    if (p >= mid) return;                  // already in place
+    int ltBefore = (p > 0 ? S[p - 1] : 0) - Slo;
+    int t = (p - lo) - ltBefore;           // rank among misplaced-left
+    int q = lower_bound_scan(S, mid, hi, S[hi] - t);
+    swap_particles(x, y, z, m, h, iord, p, q);
+}
+
+__global__ void k_top_children(int F, const int *__restrict__ f_node, const int *__restrict__ f_split,
+                               const int *__restrict__ f_rank, const int *__restrict__ S, int nTop,
+                               int *t_lo, int *t_hi, int *t_child, double *t_bnd, int *nf_node,
+                               TsphBuildCtl *ctl) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k == 0) ctl->nTop = nTop + 2 * f_rank[F - 1];
+    if (k >= F || !f_split[k]) return;
+    int v = f_node[k];
+    int lo = t_lo[v], hi = t_hi[v];
     int Slo = lo > 0 ? S[lo - 1] : 0;
     int mid = lo + (S[hi] - Slo);
-    int r = f_rank[s] - 1;
-    int c = nTemp + 2 * r;
-    f_m[s] = mid;
-    t_child[f_node[s]] = c;
-    nf_lo[2 * r] = lo;
-    nf_hi[2 * r] = mid - 1;
+    int r = f_rank[k] - 1;
+    int c = nTop + 2 * r;
+    t_child[v] = c;
+    t_lo[c] = lo;
+    t_hi[c] = mid - 1;
+    t_lo[c + 1] = mid;
+    t_hi[c + 1] = hi;
+    key_init(t_bnd, c);
+    key_init(t_bnd, c + 1);
     nf_node[2 * r] = c;
-    nf_lo[2 * r + 1] = mid;
-    nf_hi[2 * r + 1] = hi;
     nf_node[2 * r + 1] = c + 1;
 }
 
-__global__ void k_seg(int *seg, const int *__restrict__ f_split, const int *__restrict__ f_rank,
-                      const int *__restrict__ f_m, int n) {
+__global__ void k_top_seg(int *seg, const int *__restrict__ t_dim, const int *__restrict__ t_child,
+                          const int *__restrict__ t_lo, int n) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
     int s = seg[p];
     if (s < 0) return;
-    if (f_split[s]) seg[p] = 2 * (f_rank[s] - 1) + (p >= f_m[s] ? 1 : 0);
-    else seg[p] = -1;
+    if (t_dim[s] >= 0) {
+        int c = t_child[s];
+        seg[p] = p < t_lo[c + 1] ? c : c + 1;
+    } else {
+        seg[p] = -1;
+    }
 }
 
-// subtree sizes, bottom-up over one BFS level [a, b)
+// ---------------------------------------------------------------------------
+// subtree phase: one CTA builds the whole subtree of a task, level by level
+// ---------------------------------------------------------------------------
+#define ST_BS 512
+#define ST_W (ST_BS / 32)
+#define ST_MAXLEV 96
+
+struct BuildArgs {
+    double *x, *y, *z, *m, *h;
+    int *iord;
+    int *seg, *lt, *scan;
+    int *t_lo, *t_hi, *t_dim, *t_child, *t_size, *t_root, *t_loc;
+    double *t_split, *t_bnd;
+    const int *tasks;
+    TsphBuildCtl *ctl;
+    int topCap, nBucket;
+};
+
+__device__ __forceinline__ unsigned lanemask_lt_b() {
+    unsigned r;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(r));
+    return r;
+}
+
+// Exclusive offset of this warp's total within the block, and the block
+// total.  Two barriers.
+__device__ __forceinline__ int st_warp_offset(int wtot, int *ws, int &total) {
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) ws[w] = wtot;
+    __syncthreads();
+    int off = 0, tot = 0;
+#pragma unroll
+    for (int k = 0; k < ST_W; ++k) {
+        int v = ws[k];
+        if (k < w) off += v;
+        tot += v;
+    }
+    __syncthreads();
+    total = tot;
+    return off;
+}
+
+// Bounds of every node of the current level: each warp reduces a
+// contiguous chunk of the task's particles, carrying the open run of one
+// node from step to step so a node costs about one atomic per warp.
+__device__ void st_bounds(const BuildArgs &A, int lo, int hi) {
+    const unsigned FULL = 0xffffffffu;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m = hi - lo + 1;
+    const int C = ((m + ST_BS - 1) / ST_BS) * 32;
+    const int b0 = lo + w * C;
+    const int b1 = min(b0 + C, hi + 1);
+    int cs = -1;
+    unsigned long long cmn[3] = {~0ULL, ~0ULL, ~0ULL}, cmx[3] = {0ULL, 0ULL, 0ULL};
+    for (int base = b0; base < b1; base += 32) {
+        int p = base + lane;
+        int s = p < b1 ? A.seg[p] : -1;
+        unsigned long long mn[3], mx[3];
+        if (s >= 0) {
+            mn[0] = mx[0] = dkey(A.x[p]);
+            mn[1] = mx[1] = dkey(A.y[p]);
+            mn[2] = mx[2] = dkey(A.z[p]);
+            if (lane == 0 && s == cs) {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    mn[k] = cmn[k] < mn[k] ? cmn[k] : mn[k];
+                    mx[k] = cmx[k] > mx[k] ? cmx[k] : mx[k];
+                }
+            }
+        } else {
+            mn[0] = mn[1] = mn[2] = ~0ULL;
+            mx[0] = mx[1] = mx[2] = 0ULL;
+        }
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int so = __shfl_down_sync(FULL, s, o);
+            bool same = (lane + o < 32) && (so == s);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                unsigned long long a = __shfl_down_sync(FULL, mn[k], o);
+                unsigned long long b = __shfl_down_sync(FULL, mx[k], o);
+                if (same) {
+                    mn[k] = a < mn[k] ? a : mn[k];
+                    mx[k] = b > mx[k] ? b : mx[k];
+                }
+            }
+        }
+        const int s0 = __shfl_sync(FULL, s, 0);
+        const int s31 = __shfl_sync(FULL, s, 31);
+        if (cs >= 0 && s0 != cs && lane == 0) key_atomics(A.t_bnd, cs, cmn, cmx);
+        unsigned lastMask = __ballot_sync(FULL, s31 >= 0 && s == s31);
+        int hl = lastMask ? __ffs(lastMask) - 1 : -1;
+        int sp = __shfl_up_sync(FULL, s, 1);
+        bool head = lane == 0 || sp != s;
+        if (s >= 0 && head && lane != hl) key_atomics(A.t_bnd, s, mn, mx);
+        if (hl >= 0) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                cmn[k] = __shfl_sync(FULL, mn[k], hl);
+                cmx[k] = __shfl_sync(FULL, mx[k], hl);
+            }
+            cs = s31;
+        } else {
+            cs = -1;
+        }
+    }
+    if (cs >= 0 && lane == 0) key_atomics(A.t_bnd, cs, cmn, cmx);
+}
+
+__global__ void __launch_bounds__(ST_BS) k_subtree(BuildArgs A) {
+    __shared__ int ws[ST_W];
+    __shared__ int lvStart[ST_MAXLEV], lvCnt[ST_MAXLEV];
+    __shared__ int sTask;
+    const unsigned FULL = 0xffffffffu;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            int t = atomicAdd(&A.ctl->taskNext, 1);
+            sTask = t < A.ctl->taskCount ? A.tasks[t] : -1;
+        }
+        __syncthreads();
+        const int root = sTask;
+        if (root < 0) break;
+        const int lo = A.t_lo[root], hi = A.t_hi[root];
+        const int m = hi - lo + 1;
+        const int slot0 = A.topCap + 2 * lo, slotEnd = slot0 + 2 * m;
+        const int C = ((m + ST_BS - 1) / ST_BS) * 32;
+        const int b0 = lo + w * C, b1 = min(b0 + C, hi + 1);
+        for (int p = lo + threadIdx.x; p <= hi; p += ST_BS) A.seg[p] = root;
+        if (threadIdx.x == 0) {
+            key_init(A.t_bnd, root);
+            lvStart[0] = root;
+            lvCnt[0] = 1;
+        }
+        __syncthreads();
+        int L = 0;
+        bool failed = false;
+        for (;;) {
+            const int start = lvStart[L], cnt = lvCnt[L];
+            // 1. bounds of this level's nodes
+            st_bounds(A, lo, hi);
+            __syncthreads();
+            // 2. split decisions
+            for (int k = threadIdx.x; k < cnt; k += ST_BS)
+                decide_node(start + k, A.nBucket, A.t_lo, A.t_hi, A.t_dim, A.t_child, A.t_split,
+                            A.t_bnd);
+            __syncthreads();
+            // 3. partition flags and their scan over the task's particles
+            int wtot = 0;
+            for (int base = b0; base < b1; base += 32) {
+                int p = base + lane;
+                int f = 0;
+                if (p < b1) {
+                    int s = A.seg[p];
+                    if (s >= 0) {
+                        int d = A.t_dim[s];
+                        if (d >= 0) {
+                            double r = d == 0 ? A.x[p] : (d == 1 ? A.y[p] : A.z[p]);
+                            f = r < A.t_split[s] ? 1 : 0;
+                        }
+                    }
+                    A.lt[p] = f;
+                }
+                wtot += __popc(__ballot_sync(FULL, f));
+            }
+            int tot;
+            int run = st_warp_offset(wtot, ws, tot);
+            for (int base = b0; base < b1; base += 32) {
+                int p = base + lane;
+                int f = p < b1 ? A.lt[p] : 0;
+                unsigned bal = __ballot_sync(FULL, f);
+                if (p < b1) A.scan[p] = run + __popc(bal & (lanemask_lt_b() | (1u << lane)));
+                run += __popc(bal);
+            }
+            __syncthreads();
+            // 4. Hoare-partition swaps (scan is task-local: S(lo - 1) = 0)
+            for (int p = lo + threadIdx.x; p <= hi; p += ST_BS) {
+                int s = A.seg[p];
+                if (s < 0 || A.t_dim[s] < 0 || A.lt[p]) continue;
+                int vlo = A.t_lo[s], vhi = A.t_hi[s];
+                int Slo = vlo > lo ? A.scan[vlo - 1] : 0;
+                int Shi = A.scan[vhi];
+                int mid = vlo + (Shi - Slo);
+                if (p >= mid) continue;
+                int t = (p - vlo) - ((p > lo ? A.scan[p - 1] : 0) - Slo);
+                int q = lower_bound_scan(A.scan, mid, vhi, Shi - t);
+                swap_particles(A.x, A.y, A.z, A.m, A.h, A.iord, p, q);
+            }
+            __syncthreads();
+            // 5. children of the split nodes, numbered by split rank
+            const int next = (L == 0) ? slot0 : start + cnt;
+            const int NC = ((cnt + ST_BS - 1) / ST_BS) * 32;
+            const int k0 = w * NC, k1 = min(k0 + NC, cnt);
+            int ntot = 0;
+            for (int kb = k0; kb < k1; kb += 32) {
+                int k = kb + lane;
+                bool f = k < k1 && A.t_dim[start + k] >= 0;
+                ntot += __popc(__ballot_sync(FULL, f));
+            }
+            int nsplit;
+            int rank = st_warp_offset(ntot, ws, nsplit);
+            for (int kb = k0; kb < k1; kb += 32) {
+                int k = kb + lane;
+                bool f = k < k1 && A.t_dim[start + k] >= 0;
+                unsigned bal = __ballot_sync(FULL, f);
+                if (f) {
+                    int v = start + k;
+                    int c = next + 2 * (rank + __popc(bal & lanemask_lt_b()));
+                    if (c + 1 >= slotEnd) {
+                        atomicOr(&A.ctl->status, 1 << TSPH_ERR_ARG);
+                    } else {
+                        int vlo = A.t_lo[v], vhi = A.t_hi[v];
+                        int Slo = vlo > lo ? A.scan[vlo - 1] : 0;
+                        int mid = vlo + (A.scan[vhi] - Slo);
+                        A.t_child[v] = c;
+                        A.t_lo[c] = vlo;
+                        A.t_hi[c] = mid - 1;
+                        A.t_lo[c + 1] = mid;
+                        A.t_hi[c + 1] = vhi;
+                        key_init(A.t_bnd, c);
+                        key_init(A.t_bnd, c + 1);
+                        A.t_root[c] = root;
+                        A.t_root[c + 1] = root;
+                    }
+                }
+                rank += __popc(bal);
+            }
+            __syncthreads();
+            // 6. particles follow their node into a child, or finish in a leaf
+            for (int p = lo + threadIdx.x; p <= hi; p += ST_BS) {
+                int s = A.seg[p];
+                if (s < 0) continue;
+                if (A.t_dim[s] >= 0) {
+                    int c = A.t_child[s];
+                    A.seg[p] = p < A.t_lo[c + 1] ? c : c + 1;
+                } else {
+                    A.seg[p] = -1;
+                }
+            }
+            if (nsplit == 0) break;
+            if (L + 1 >= ST_MAXLEV) {
+                if (threadIdx.x == 0) atomicOr(&A.ctl->status, 1 << TSPH_ERR_TREE_DEPTH);
+                failed = true;
+                break;
+            }
+            if (threadIdx.x == 0) {
+                lvStart[L + 1] = next;
+                lvCnt[L + 1] = 2 * nsplit;
+            }
+            __syncthreads();
+            ++L;
+        }
+        __syncthreads();
+        if (!failed) {
+            // subtree sizes bottom-up, then depth-first offsets from the root
+            for (int l = L; l >= 0; --l) {
+                const int start = lvStart[l], cnt = lvCnt[l];
+                for (int k = threadIdx.x; k < cnt; k += ST_BS) {
+                    int v = start + k;
+                    int c = A.t_child[v];
+                    A.t_size[v] = 1 + (c >= 0 ? A.t_size[c] + A.t_size[c + 1] : 0);
+                }
+                __syncthreads();
+            }
+            if (threadIdx.x == 0) A.t_loc[root] = 0;
+            __syncthreads();
+            for (int l = 0; l < L; ++l) {
+                const int start = lvStart[l], cnt = lvCnt[l];
+                for (int k = threadIdx.x; k < cnt; k += ST_BS) {
+                    int v = start + k;
+                    int c = A.t_child[v];
+                    if (c < 0) continue;
+                    int lv = A.t_loc[v];
+                    A.t_loc[c] = lv + 1;
+                    A.t_loc[c + 1] = lv + 1 + A.t_size[c];
+                }
+                __syncthreads();
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// depth-first numbering and the final node arrays
+// ---------------------------------------------------------------------------
+// subtree sizes, bottom-up over one top level [a, b)
 __global__ void k_size(int a, int b, const int *__restrict__ t_child, int *t_size) {
     int v = a + blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= b) return;
@@ -291,7 +651,44 @@ __global__ void k_size(int a, int b, const int *__restrict__ t_child, int *t_siz
     t_size[v] = 1 + (c >= 0 ? t_size[c] + t_size[c + 1] : 0);
 }
 
-// depth-first (reference) index, top-down over one BFS level [a, b)
+// roots: trees are stored one after another in range order
+__global__ void k_root_pre(int nR, const int *__restrict__ t_size, int *t_pre, int *sysRoot,
+                           int *rEnd, TsphBuildCtl *ctl) {
+    __shared__ int ws[32];
+    __shared__ int carry;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < nR; base += blockDim.x) {
+        int r = base + threadIdx.x;
+        int v = r < nR ? t_size[r] : 0;
+        int t = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t += y;
+        }
+        if (lane == 31) ws[w] = t;
+        __syncthreads();
+        int off = carry, tot = 0;
+        for (int k = 0; k < nw; ++k) {
+            if (k < w) off += ws[k];
+            tot += ws[k];
+        }
+        if (r < nR) {
+            int e = off + t - v;
+            t_pre[r] = e;
+            sysRoot[r] = e;
+            rEnd[r] = e + v;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) carry += tot;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) ctl->nNodes = carry;
+}
+
+// depth-first (reference) index, top-down over one top level [a, b)
 __global__ void k_pre(int a, int b, const int *__restrict__ t_child,
                       const int *__restrict__ t_size, int *t_pre) {
     int v = a + blockIdx.x * blockDim.x + threadIdx.x;
@@ -303,30 +700,51 @@ __global__ void k_pre(int a, int b, const int *__restrict__ t_child,
     t_pre[c + 1] = pv + 1 + t_size[c];
 }
 
-__global__ void k_scatter_nodes(int nTemp, const int *__restrict__ t_lo, const int *__restrict__ t_hi,
+__global__ void k_slot_pre(int topCap, int nSlots, const int *__restrict__ t_root,
+                           const int *__restrict__ t_loc, int *t_pre) {
+    int w = topCap + blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= topCap + nSlots) return;
+    int r = t_root[w];
+    if (r >= 0) t_pre[w] = t_pre[r] + t_loc[w];
+}
+
+__global__ void k_scatter_nodes(int topCap, int tcap, const TsphBuildCtl *__restrict__ ctl,
+                                const int *__restrict__ t_lo, const int *__restrict__ t_hi,
                                 const int *__restrict__ t_dim, const int *__restrict__ t_child,
                                 const int *__restrict__ t_size, const int *__restrict__ t_pre,
-                                const double *__restrict__ t_split, const double *__restrict__ t_bnd,
-                                TsphDevTree T, int *leafFlag) {
+                                const int *__restrict__ t_root, const double *__restrict__ t_split,
+                                const double *__restrict__ t_bnd, const int *__restrict__ rid,
+                                int nR, TsphDevTree T, int *leafFlag) {
     int v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= nTemp) return;
+    if (v >= tcap) return;
+    if (v < topCap ? v >= ctl->nTop : t_root[v] < 0) return;
     int i = t_pre[v];
     int c = t_child[v];
     T.pLower[i] = t_lo[v];
     T.pUpper[i] = t_hi[v];
-    T.iDim[i] = t_dim[v];
+    T.iDim[i] = t_dim[v] >= 0 ? t_dim[v] : -1;
     T.fSplit[i] = t_split[v];
 #pragma unroll
     for (int k = 0; k < 6; ++k) T.bnd[6 * i + k] = t_bnd[6 * v + k];
     T.upper[i] = c >= 0 ? t_pre[c + 1] : -1;
     int nx = i + t_size[v];
-    T.skip[i] = nx < nTemp ? nx : -1;
+    T.skip[i] = nx < T.rEnd[rid[t_lo[v]]] ? nx : -1;
     leafFlag[i] = c < 0 ? 1 : 0;
+    if (c >= 0) {
+        T.parent[t_pre[c]] = i;
+        T.parent[t_pre[c + 1]] = i;
+    }
+    if (v < nR) T.parent[i] = -1;
 }
 
-__global__ void k_leaf_list(int nNodes, const int *__restrict__ leafFlag,
-                            const int *__restrict__ leafScan, int *leaves) {
+__global__ void k_leaf_list(const TsphBuildCtl *__restrict__ ctl, const int *__restrict__ leafFlag,
+                            const int *__restrict__ leafScan, int *leaves, int *dcnt) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int nNodes = ctl->nNodes;
+    if (i == 0) {
+        dcnt[0] = nNodes;
+        dcnt[1] = nNodes > 0 ? leafScan[nNodes - 1] : 0;
+    }
     if (i >= nNodes || !leafFlag[i]) return;
     leaves[leafScan[i] - 1] = i;
 }
@@ -334,16 +752,64 @@ __global__ void k_leaf_list(int nNodes, const int *__restrict__ leafFlag,
 // ---------------------------------------------------------------------------
 // moments
 // ---------------------------------------------------------------------------
+// Mass, softening and centre of mass of an interior node from its two
+// children in the reference's order (pkd.c:2522-2547); the quadrupole by the
+// parallel-axis theorem (equal to the reference's direct sum up to
+// rounding).  Children may have been written by other SMs: read past L1.
+__device__ void combine_node(TsphDevTree &T, int i) {
+    const int l = i + 1, u = T.upper[i];
+    double fMass = 0.0, fSoft = 0.0, r[3] = {0.0, 0.0, 0.0};
+    double fm = __ldcg(&T.fMass[l]);
+    fMass = xadd(fMass, fm);
+    fSoft = xadd(fSoft, xmul(fm, __ldcg(&T.fSoft[l])));
+#pragma unroll
+    for (int j = 0; j < 3; ++j) r[j] = xadd(r[j], xmul(fm, __ldcg(&T.r[3 * l + j])));
+    fm = __ldcg(&T.fMass[u]);
+    fMass = xadd(fMass, fm);
+    fSoft = xadd(fSoft, xmul(fm, __ldcg(&T.fSoft[u])));
+#pragma unroll
+    for (int j = 0; j < 3; ++j) r[j] = xadd(r[j], xmul(fm, __ldcg(&T.r[3 * u + j])));
+    if (fMass > 0) {
+        fSoft = __ddiv_rn(fSoft, fMass);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) r[j] = __ddiv_rn(r[j], fMass);
+    }
+    T.fMass[i] = fMass;
+    T.fSoft[i] = fSoft;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) T.r[3 * i + j] = r[j];
+    double q[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) q[k] = __ldcg(&T.Q[6 * l + k]) + __ldcg(&T.Q[6 * u + k]);
+    int cc[2] = {l, u};
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+        int ch = cc[s];
+        double mc = __ldcg(&T.fMass[ch]);
+        double dx = __ldcg(&T.r[3 * ch]) - r[0], dy = __ldcg(&T.r[3 * ch + 1]) - r[1],
+               dz = __ldcg(&T.r[3 * ch + 2]) - r[2];
+        q[0] += mc * dx * dx;
+        q[1] += mc * dy * dy;
+        q[2] += mc * dz * dz;
+        q[3] += mc * dx * dy;
+        q[4] += mc * dx * dz;
+        q[5] += mc * dy * dz;
+    }
+#pragma unroll
+    for (int k = 0; k < 6; ++k) T.Q[6 * i + k] = q[k];
+}
+
 // Leaf mass, softening and centre of mass summed in tree order exactly as
 // BuildBinary (pkd.c:2559-2574); quadrupole summed as pkdCalcCell
-// (pkd.c:2094-2130).
-__global__ void k_leaf_moments(int nLeaves, const int *__restrict__ leaves, TsphDevTree T,
-                               const double *__restrict__ x, const double *__restrict__ y,
-                               const double *__restrict__ z, const double *__restrict__ m,
-                               const double *__restrict__ h) {
+// (pkd.c:2094-2130).  Then the thread climbs: at each parent the second
+// child to finish (counted by an atomic) combines it, so every interior
+// node is formed once, after both children, with no per-level launches.
+__global__ void k_moments(TsphDevTree T, const double *__restrict__ x, const double *__restrict__ y,
+                          const double *__restrict__ z, const double *__restrict__ m,
+                          const double *__restrict__ h, int *visit) {
     int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= nLeaves) return;
-    int i = leaves[b];
+    if (b >= T.dcnt[1]) return;
+    int i = T.leaves[b];
     int lo = T.pLower[i], hi = T.pUpper[i];
     double fMass = 0.0, fSoft = 0.0, r0 = 0.0, r1 = 0.0, r2 = 0.0;
     for (int p = lo; p <= hi; ++p) {
@@ -378,56 +844,15 @@ __global__ void k_leaf_moments(int nLeaves, const int *__restrict__ leaves, Tsph
     }
 #pragma unroll
     for (int k = 0; k < 6; ++k) T.Q[6 * i + k] = q[k];
-}
-
-// Interior nodes of one BFS level: combine the two children in the
-// reference's order (pkd.c:2522-2547); the quadrupole by the parallel-axis
-// theorem (equal to the reference's direct sum up to rounding).
-__global__ void k_combine(int a, int b, const int *__restrict__ t_child,
-                          const int *__restrict__ t_pre, TsphDevTree T) {
-    int v = a + blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= b) return;
-    int c = t_child[v];
-    if (c < 0) return;
-    int i = t_pre[v], l = t_pre[c], u = t_pre[c + 1];
-    double fMass = 0.0, fSoft = 0.0, r[3] = {0.0, 0.0, 0.0};
-    double fm = T.fMass[l];
-    fMass = xadd(fMass, fm);
-    fSoft = xadd(fSoft, xmul(fm, T.fSoft[l]));
-#pragma unroll
-    for (int j = 0; j < 3; ++j) r[j] = xadd(r[j], xmul(fm, T.r[3 * l + j]));
-    fm = T.fMass[u];
-    fMass = xadd(fMass, fm);
-    fSoft = xadd(fSoft, xmul(fm, T.fSoft[u]));
-#pragma unroll
-    for (int j = 0; j < 3; ++j) r[j] = xadd(r[j], xmul(fm, T.r[3 * u + j]));
-    if (fMass > 0) {
-        fSoft = __ddiv_rn(fSoft, fMass);
-#pragma unroll
-        for (int j = 0; j < 3; ++j) r[j] = __ddiv_rn(r[j], fMass);
+    for (;;) {
+        __threadfence();
+        int par = T.parent[i];
+        if (par < 0) break;
+        if (atomicAdd(&visit[par], 1) == 0) break;   // the sibling is not done yet
+        __threadfence();
+        combine_node(T, par);
+        i = par;
     }
-    T.fMass[i] = fMass;
-    T.fSoft[i] = fSoft;
-#pragma unroll
-    for (int j = 0; j < 3; ++j) T.r[3 * i + j] = r[j];
-    double q[6];
-#pragma unroll
-    for (int k = 0; k < 6; ++k) q[k] = T.Q[6 * l + k] + T.Q[6 * u + k];
-    int cc[2] = {l, u};
-#pragma unroll
-    for (int s = 0; s < 2; ++s) {
-        int ch = cc[s];
-        double mc = T.fMass[ch];
-        double dx = T.r[3 * ch] - r[0], dy = T.r[3 * ch + 1] - r[1], dz = T.r[3 * ch + 2] - r[2];
-        q[0] += mc * dx * dx;
-        q[1] += mc * dy * dy;
-        q[2] += mc * dz * dz;
-        q[3] += mc * dx * dy;
-        q[4] += mc * dx * dz;
-        q[5] += mc * dy * dz;
-    }
-#pragma unroll
-    for (int k = 0; k < 6; ++k) T.Q[6 * i + k] = q[k];
 }
 
 __global__ void k_zero_u64(unsigned long long *a, int n) {
@@ -436,16 +861,16 @@ __global__ void k_zero_u64(unsigned long long *a, int n) {
 }
 
 // Bmax of every node = max over its particles of |r - COM| (pkd.c:2086-2092).
-// Each particle descends from the root to its leaf; max of d^2 is taken on
-// the raw bits (non-negative doubles order like their bit patterns) and the
-// square root taken once: sqrt is monotone, so this equals the max of the
-// per-particle square roots the reference takes.
+// Each particle descends from its tree's root to its leaf; max of d^2 is
+// taken on the raw bits (non-negative doubles order like their bit
+// patterns) and the square root taken once: sqrt is monotone, so this
+// equals the max of the per-particle square roots the reference takes.
 __global__ void k_bmax(int n, TsphDevTree T, const double *__restrict__ x,
                        const double *__restrict__ y, const double *__restrict__ z,
-                       unsigned long long *maxd2) {
+                       const int *__restrict__ rid, unsigned long long *maxd2) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     bool live = p < n;
-    int i = 0;
+    int i = live ? T.sysRoot[rid[p]] : 0;
     double px = live ? x[p] : 0.0, py = live ? y[p] : 0.0, pz = live ? z[p] : 0.0;
     unsigned mask = __ballot_sync(0xffffffffu, live);
     while (mask) {
@@ -471,10 +896,10 @@ __global__ void k_bmax(int n, TsphDevTree T, const double *__restrict__ x,
 }
 
 // Opening radius, OPEN_JOSH (pkd.c:2245-2253); walk copies in FP32.
-__global__ void k_open(int nNodes, TsphDevTree T, const unsigned long long *__restrict__ maxd2,
+__global__ void k_open(TsphDevTree T, const unsigned long long *__restrict__ maxd2,
                        double twoOverSqrt3, double dCrit) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nNodes) return;
+    if (i >= T.dcnt[0]) return;
     double Bmax = sqrt(__longlong_as_double((long long)maxd2[i]));
     double dOpen = __ddiv_rn(xmul(twoOverSqrt3, Bmax), dCrit);
     if (dOpen < Bmax) dOpen = Bmax;
@@ -515,48 +940,149 @@ void tsph_free_tree(TsphDevTree &T) {
     TFREE(T.pLower); TFREE(T.pUpper); TFREE(T.iDim); TFREE(T.upper); TFREE(T.skip);
     TFREE(T.fSplit); TFREE(T.bnd); TFREE(T.fMass); TFREE(T.fSoft); TFREE(T.r);
     TFREE(T.fOpen2); TFREE(T.Bmax); TFREE(T.Q); TFREE(T.wcomh); TFREE(T.wcoml);
-    TFREE(T.wlink); TFREE(T.wmom0); TFREE(T.wmom1); TFREE(T.leaves);
+    TFREE(T.wlink); TFREE(T.wmom0); TFREE(T.wmom1); TFREE(T.leaves); TFREE(T.parent);
+    TFREE(T.rLo); TFREE(T.rHi); TFREE(T.sysRoot); TFREE(T.rEnd); TFREE(T.dcnt);
     if (T.brec) cudaFree(T.brec);
     T.brec = nullptr;
+    free(T.hLo);
+    free(T.hHi);
+    T.hLo = T.hHi = nullptr;
     T.cap = 0;
+    T.rCap = 0;
 }
 
+void tsph_free_build(TsphBuildBufs &B) {
+    TFREE(B.f_node[0]); TFREE(B.f_node[1]); TFREE(B.f_split); TFREE(B.f_rank); TFREE(B.tasks);
+    TFREE(B.t_lo); TFREE(B.t_hi); TFREE(B.t_dim); TFREE(B.t_child); TFREE(B.t_size);
+    TFREE(B.t_pre); TFREE(B.t_root); TFREE(B.t_loc); TFREE(B.t_split); TFREE(B.t_bnd);
+    TFREE(B.maxd2); TFREE(B.visit); TFREE(B.leafFlag); TFREE(B.leafScan); TFREE(B.ctl);
+    B.tcap = B.topCap = B.nodeScratchCap = 0;
+}
+
+// Final node arrays: a forest over n particles in nR trees has at most
+// 2n - nR nodes.
 static int ensure_nodes(tsph_ctx *ctx, TsphDevTree &T, int nNodes) {
     TsphBuildBufs &B = ctx->B;
-    if (nNodes <= T.cap && T.pLower && nNodes <= B.nodeCap) return TSPH_OK;
-    int cap = nNodes + nNodes / 4 + 64;
     int rc = 0;
-    rc |= tsph_grow(ctx, &T.pLower, cap);
-    rc |= tsph_grow(ctx, &T.pUpper, cap);
-    rc |= tsph_grow(ctx, &T.iDim, cap);
-    rc |= tsph_grow(ctx, &T.upper, cap);
-    rc |= tsph_grow(ctx, &T.skip, cap);
-    rc |= tsph_grow(ctx, &T.fSplit, cap);
-    rc |= tsph_grow(ctx, &T.bnd, (size_t)6 * cap);
-    rc |= tsph_grow(ctx, &T.fMass, cap);
-    rc |= tsph_grow(ctx, &T.fSoft, cap);
-    rc |= tsph_grow(ctx, &T.r, (size_t)3 * cap);
-    rc |= tsph_grow(ctx, &T.fOpen2, cap);
-    rc |= tsph_grow(ctx, &T.Bmax, cap);
-    rc |= tsph_grow(ctx, &T.Q, (size_t)6 * cap);
-    rc |= tsph_grow(ctx, &T.wcomh, cap);
-    rc |= tsph_grow(ctx, &T.wcoml, cap);
-    rc |= tsph_grow(ctx, &T.wlink, cap);
-    rc |= tsph_grow(ctx, &T.wmom0, cap);
-    rc |= tsph_grow(ctx, &T.wmom1, cap);
-    rc |= tsph_grow(ctx, &T.leaves, cap);
-    rc |= tsph_grow(ctx, &T.brec, (size_t)4 * cap);
-    if (rc) return TSPH_ERR_NOMEM;
-    T.cap = cap;
-    // per-node scratch shared by both trees (sized to the larger)
-    if (B.maxd2Cap < cap) {
-        rc |= tsph_grow(ctx, &B.maxd2, cap);
-        rc |= tsph_grow(ctx, &B.leafFlag, cap);
-        rc |= tsph_grow(ctx, &B.leafScan, cap);
+    if (nNodes > T.cap || !T.pLower) {
+        int cap = nNodes + 64;
+        rc |= tsph_grow(ctx, &T.pLower, cap);
+        rc |= tsph_grow(ctx, &T.pUpper, cap);
+        rc |= tsph_grow(ctx, &T.iDim, cap);
+        rc |= tsph_grow(ctx, &T.upper, cap);
+        rc |= tsph_grow(ctx, &T.skip, cap);
+        rc |= tsph_grow(ctx, &T.parent, cap);
+        rc |= tsph_grow(ctx, &T.fSplit, cap);
+        rc |= tsph_grow(ctx, &T.bnd, (size_t)6 * cap);
+        rc |= tsph_grow(ctx, &T.fMass, cap);
+        rc |= tsph_grow(ctx, &T.fSoft, cap);
+        rc |= tsph_grow(ctx, &T.r, (size_t)3 * cap);
+        rc |= tsph_grow(ctx, &T.fOpen2, cap);
+        rc |= tsph_grow(ctx, &T.Bmax, cap);
+        rc |= tsph_grow(ctx, &T.Q, (size_t)6 * cap);
+        rc |= tsph_grow(ctx, &T.wcomh, cap);
+        rc |= tsph_grow(ctx, &T.wcoml, cap);
+        rc |= tsph_grow(ctx, &T.wlink, cap);
+        rc |= tsph_grow(ctx, &T.wmom0, cap);
+        rc |= tsph_grow(ctx, &T.wmom1, cap);
+        rc |= tsph_grow(ctx, &T.leaves, cap);
+        rc |= tsph_grow(ctx, &T.brec, (size_t)4 * cap);
         if (rc) return TSPH_ERR_NOMEM;
-        B.maxd2Cap = cap;
+        T.cap = cap;
+    }
+    // per-node scratch shared by both trees (sized to the larger)
+    if (B.nodeScratchCap < T.cap) {
+        rc |= tsph_grow(ctx, &B.maxd2, T.cap);
+        rc |= tsph_grow(ctx, &B.visit, T.cap);
+        rc |= tsph_grow(ctx, &B.leafFlag, T.cap);
+        rc |= tsph_grow(ctx, &B.leafScan, T.cap);
+        if (rc) return TSPH_ERR_NOMEM;
+        B.nodeScratchCap = T.cap;
     }
     return TSPH_OK;
+}
+
+// Temporary nodes: top-phase nodes all hold more than the task size (at
+// least 1024 particles), so a level has at most n/1024 of them.
+static int ensure_temp(tsph_ctx *ctx, int n, int nR) {
+    TsphBuildBufs &B = ctx->B;
+    int topCap = nR + 2 * (n / 1024 + 1) * TSPH_MAX_LEVELS + 512;
+    int tcap = topCap + 2 * n;
+    if (B.ctl && topCap <= B.topCap && tcap <= B.tcap) return TSPH_OK;
+    topCap += topCap / 8;
+    tcap = topCap + 2 * (n + n / 8 + 64);
+    int rc = 0;
+    rc |= tsph_grow(ctx, &B.f_node[0], topCap);
+    rc |= tsph_grow(ctx, &B.f_node[1], topCap);
+    rc |= tsph_grow(ctx, &B.f_split, topCap);
+    rc |= tsph_grow(ctx, &B.f_rank, topCap);
+    rc |= tsph_grow(ctx, &B.tasks, topCap);
+    rc |= tsph_grow(ctx, &B.t_lo, tcap);
+    rc |= tsph_grow(ctx, &B.t_hi, tcap);
+    rc |= tsph_grow(ctx, &B.t_dim, tcap);
+    rc |= tsph_grow(ctx, &B.t_child, tcap);
+    rc |= tsph_grow(ctx, &B.t_size, tcap);
+    rc |= tsph_grow(ctx, &B.t_pre, tcap);
+    rc |= tsph_grow(ctx, &B.t_root, tcap);
+    rc |= tsph_grow(ctx, &B.t_loc, tcap);
+    rc |= tsph_grow(ctx, &B.t_split, tcap);
+    rc |= tsph_grow(ctx, &B.t_bnd, (size_t)6 * tcap);
+    if (!B.ctl) rc |= tsph_grow(ctx, &B.ctl, 1);
+    if (rc) return TSPH_ERR_NOMEM;
+    B.topCap = topCap;
+    B.tcap = tcap;
+    return TSPH_OK;
+}
+
+// The forest's trees: nR consecutive particle ranges of the given sizes
+// (each at least 1), in tree order.  A single system is one range.
+int tsph_set_ranges(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, int nR,
+                    const int *counts) {
+    if (nR < 1) return TSPH_ERR_ARG;
+    int rc = 0;
+    if (T.rCap < nR || !T.rLo) {
+        rc |= tsph_grow(ctx, &T.rLo, nR);
+        rc |= tsph_grow(ctx, &T.rHi, nR);
+        rc |= tsph_grow(ctx, &T.sysRoot, nR);
+        rc |= tsph_grow(ctx, &T.rEnd, nR);
+        if (!T.dcnt) rc |= tsph_grow(ctx, &T.dcnt, 2);
+        if (rc) return TSPH_ERR_NOMEM;
+        free(T.hLo);
+        free(T.hHi);
+        T.hLo = (int *)malloc(sizeof(int) * nR);
+        T.hHi = (int *)malloc(sizeof(int) * nR);
+        if (!T.hLo || !T.hHi) return TSPH_ERR_NOMEM;
+        T.rCap = nR;
+    }
+    if (!P.rid || ctx->B.cap < n) return TSPH_ERR_STATE;
+    int *hrid = (int *)malloc(sizeof(int) * (n > 0 ? n : 1));
+    if (!hrid) return TSPH_ERR_NOMEM;
+    int lo = 0, mx = 0;
+    for (int r = 0; r < nR; ++r) {
+        if (counts[r] < 1 || lo + counts[r] > n) { free(hrid); return TSPH_ERR_ARG; }
+        T.hLo[r] = lo;
+        T.hHi[r] = lo + counts[r] - 1;
+        for (int p = lo; p < lo + counts[r]; ++p) hrid[p] = r;
+        mx = counts[r] > mx ? counts[r] : mx;
+        lo += counts[r];
+    }
+    if (lo != n) { free(hrid); return TSPH_ERR_ARG; }
+    T.nR = nR;
+    T.maxRange = mx;
+    cudaError_t e = cudaMemcpy(T.rLo, T.hLo, sizeof(int) * nR, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(T.rHi, T.hHi, sizeof(int) * nR, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && n > 0) e = cudaMemcpy(P.rid, hrid, sizeof(int) * n, cudaMemcpyHostToDevice);
+    free(hrid);
+    if (e != cudaSuccess) return tsph_cuda_fail(ctx, e, "tsph_set_ranges");
+    return TSPH_OK;
+}
+
+// Task size: the largest node handed whole to one CTA.
+static int task_size(tsph_ctx *ctx, int n) {
+    int S = ctx->taskSize > 0 ? ctx->taskSize : n / (ctx->smCount * 2);
+    if (S < 1024) S = 1024;
+    if (S > 65536) S = 65536;
+    return S;
 }
 
 int tsph_build_tree(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, int nBucket) {
@@ -567,91 +1093,136 @@ int tsph_build_tree(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, int n
         // an empty bucket (pkdBuildBinary's bEmpty branch, pkd.c:2686-2714)
         int rc = ensure_nodes(ctx, T, 1);
         if (rc) return rc;
-        int h6[6] = {0, -1, -1, -1, -1, 0};
+        static const int h6[4] = {0, -1, 1, 0};
         TSPH_CK(cudaMemcpyAsync(T.pLower, &h6[0], sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
         TSPH_CK(cudaMemcpyAsync(T.pUpper, &h6[1], sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+        if (T.dcnt)
+            TSPH_CK(cudaMemcpyAsync(T.dcnt, &h6[2], 2 * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
         TSPH_CK(cudaStreamSynchronize(ctx->stream));
         T.nNodes = 1;
         T.nLeaves = 0;
         return TSPH_OK;
     }
-    k_init_build<<<tsph_blocks(n, BS), BS, 0, ctx->stream>>>(B.seg, n, B.f_lo[0], B.f_hi[0], B.f_node[0]);
-    TSPH_LAUNCH_CK("k_init_build");
-    int F = 1, cur = 0, nTemp = 1, level = 0;
+    if (T.nR < 1 || T.hHi[T.nR - 1] != n - 1) return TSPH_ERR_STATE;
+    const int nR = T.nR;
+    int rc = ensure_temp(ctx, n, nR);
+    if (rc) return rc;
+    const int nodeNeed = 2 * n;
+    rc = ensure_nodes(ctx, T, nodeNeed);
+    if (rc) return rc;
+    const int S = task_size(ctx, n);
+    int F = 0;
+    for (int r = 0; r < nR; ++r)
+        if (T.hHi[r] - T.hLo[r] + 1 > S) ++F;
+    k_roots<<<1, 1024, 0, ctx->stream>>>(nR, T.rLo, T.rHi, S, B.t_lo, B.t_hi, B.t_bnd, B.f_node[0],
+                                         B.tasks, B.ctl);
+    TSPH_LAUNCH_CK("k_roots");
+    TSPH_CK(cudaMemsetAsync(B.t_root + B.topCap, 0xff, sizeof(int) * 2 * (size_t)n, ctx->stream));
+    // top phase
     int levelStart[TSPH_MAX_LEVELS + 2];
+    int nTop = nR, cur = 0, level = 0;
     levelStart[0] = 0;
+    levelStart[1] = nR;
+    if (F > 0) {
+        k_seg_init<<<tsph_blocks(n, BS), BS, 0, ctx->stream>>>(n, B.seg, P.rid, T.rHi, T.rLo, S);
+        TSPH_LAUNCH_CK("k_seg_init");
+    }
     while (F > 0) {
-        if (level >= TSPH_MAX_LEVELS) return TSPH_ERR_TREE_DEPTH;
-        levelStart[level + 1] = nTemp;   // provisional; fixed below
-        k_fbnd_init<<<tsph_blocks(F, BS), BS, 0, ctx->stream>>>(B.f_bnd, F);
-        TSPH_LAUNCH_CK("k_fbnd_init");
-        k_bounds<<<tsph_blocks(n, BS), BS, 0, ctx->stream>>>(P.x, P.y, P.z, B.seg, B.f_bnd, n);
+        if (level + 1 >= TSPH_MAX_LEVELS) return TSPH_ERR_TREE_DEPTH;
+        k_bounds<<<tsph_blocks(n, BS), BS, 0, ctx->stream>>>(P.x, P.y, P.z, B.seg, B.t_bnd, n);
         TSPH_LAUNCH_CK("k_bounds");
-        k_split<<<tsph_blocks(F, BS), BS, 0, ctx->stream>>>(
-            F, B.f_lo[cur], B.f_hi[cur], B.f_node[cur], B.f_bnd, nBucket, B.f_split, B.f_dim,
-            B.f_fs, B.t_lo, B.t_hi, B.t_dim, B.t_child, B.t_split, B.t_bnd, B.t_level, level);
-        TSPH_LAUNCH_CK("k_split");
-        k_flag<<<tsph_blocks(n, BS), BS, 0, ctx->stream>>>(P.x, P.y, P.z, B.seg, B.f_split, B.f_dim,
-                                                           B.f_fs, B.lt, n);
+        k_top_split<<<tsph_blocks(F, BS), BS, 0, ctx->stream>>>(
+            F, B.f_node[cur], S, nBucket, B.t_lo, B.t_hi, B.t_dim, B.t_child, B.t_size, B.t_split,
+            B.t_bnd, B.f_split, B.tasks, B.ctl);
+        TSPH_LAUNCH_CK("k_top_split");
+        k_flag<<<tsph_blocks(n, BS), BS, 0, ctx->stream>>>(P.x, P.y, P.z, B.seg, B.t_dim, B.t_split,
+                                                           B.lt, n);
         TSPH_LAUNCH_CK("k_flag");
-        int rc = tsph_scan_inclusive(ctx, B.lt, B.scan, n);
+        rc = tsph_scan_inclusive(ctx, B.lt, B.scan, n);
         if (rc) return rc;
         k_swap<<<tsph_blocks(n, BS), BS, 0, ctx->stream>>>(P.x, P.y, P.z, P.m, P.h, P.iord, B.seg,
-                                                           B.f_split, B.f_lo[cur], B.f_hi[cur],
-                                                           B.lt, B.scan, n);
+                                                           B.t_dim, B.t_lo, B.t_hi, B.lt, B.scan, n);
         TSPH_LAUNCH_CK("k_swap");
         rc = tsph_scan_inclusive(ctx, B.f_split, B.f_rank, F);
         if (rc) return rc;
-        k_children<<<tsph_blocks(F, BS), BS, 0, ctx->stream>>>(
-            F, B.f_lo[cur], B.f_hi[cur], B.f_node[cur], B.f_split, B.f_rank, B.scan, nTemp, B.f_m,
-            B.t_child, B.f_lo[1 - cur], B.f_hi[1 - cur], B.f_node[1 - cur]);
-        TSPH_LAUNCH_CK("k_children");
-        k_seg<<<tsph_blocks(n, BS), BS, 0, ctx->stream>>>(B.seg, B.f_split, B.f_rank, B.f_m, n);
-        TSPH_LAUNCH_CK("k_seg");
+        if (nTop + 2 * F > B.topCap) return TSPH_ERR_TREE_DEPTH;
+        k_top_children<<<tsph_blocks(F, BS), BS, 0, ctx->stream>>>(
+            F, B.f_node[cur], B.f_split, B.f_rank, B.scan, nTop, B.t_lo, B.t_hi, B.t_child, B.t_bnd,
+            B.f_node[1 - cur], B.ctl);
+        TSPH_LAUNCH_CK("k_top_children");
+        k_top_seg<<<tsph_blocks(n, BS), BS, 0, ctx->stream>>>(B.seg, B.t_dim, B.t_child, B.t_lo, n);
+        TSPH_LAUNCH_CK("k_top_seg");
         TSPH_CK(cudaMemcpyAsync(B.hostCount, B.f_rank + (F - 1), sizeof(int), cudaMemcpyDeviceToHost,
                                 ctx->stream));
         TSPH_CK(cudaStreamSynchronize(ctx->stream));
         int nSplit = B.hostCount[0];
-        levelStart[level + 1] = nTemp;
-        nTemp += 2 * nSplit;
+        nTop += 2 * nSplit;
+        if (nTop > B.topCap) return TSPH_ERR_TREE_DEPTH;
         F = 2 * nSplit;
-        if (nTemp > B.nodeCap - 2 && F > 0) return TSPH_ERR_ARG;   // cannot happen: nodes <= 2n-1
         cur = 1 - cur;
-        level++;
+        ++level;
+        levelStart[level + 1] = nTop;
     }
-    int nLevels = level;
-    levelStart[nLevels] = nTemp;
-    int rc = ensure_nodes(ctx, T, nTemp);
-    if (rc) return rc;
-    // subtree sizes bottom-up, depth-first numbering top-down
-    for (int l = nLevels - 1; l >= 0; --l) {
+    const int topLevels = level + 1;     // level 0 = the roots
+    B.topLevels = topLevels;
+    // subtree phase
+    BuildArgs A;
+    A.x = P.x; A.y = P.y; A.z = P.z; A.m = P.m; A.h = P.h; A.iord = P.iord;
+    A.seg = B.seg; A.lt = B.lt; A.scan = B.scan;
+    A.t_lo = B.t_lo; A.t_hi = B.t_hi; A.t_dim = B.t_dim; A.t_child = B.t_child;
+    A.t_size = B.t_size; A.t_root = B.t_root; A.t_loc = B.t_loc;
+    A.t_split = B.t_split; A.t_bnd = B.t_bnd;
+    A.tasks = B.tasks; A.ctl = B.ctl;
+    A.topCap = B.topCap; A.nBucket = nBucket;
+    if (ctx->subtreeBlocks == 0) {
+        int per = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_subtree, ST_BS, 0);
+        ctx->subtreeBlocks = (per > 0 ? per : 1) * ctx->smCount;
+    }
+    k_subtree<<<ctx->subtreeBlocks, ST_BS, 0, ctx->stream>>>(A);
+    TSPH_LAUNCH_CK("k_subtree");
+    // numbering
+    for (int l = topLevels - 1; l >= 0; --l) {
         int a = levelStart[l], b = levelStart[l + 1];
         k_size<<<tsph_blocks(b - a, BS), BS, 0, ctx->stream>>>(a, b, B.t_child, B.t_size);
         TSPH_LAUNCH_CK("k_size");
     }
-    TSPH_CK(cudaMemsetAsync(B.t_pre, 0, sizeof(int), ctx->stream));
-    for (int l = 0; l < nLevels; ++l) {
+    k_root_pre<<<1, 1024, 0, ctx->stream>>>(nR, B.t_size, B.t_pre, T.sysRoot, T.rEnd, B.ctl);
+    TSPH_LAUNCH_CK("k_root_pre");
+    for (int l = 0; l < topLevels; ++l) {
         int a = levelStart[l], b = levelStart[l + 1];
         k_pre<<<tsph_blocks(b - a, BS), BS, 0, ctx->stream>>>(a, b, B.t_child, B.t_size, B.t_pre);
         TSPH_LAUNCH_CK("k_pre");
     }
-    k_scatter_nodes<<<tsph_blocks(nTemp, BS), BS, 0, ctx->stream>>>(
-        nTemp, B.t_lo, B.t_hi, B.t_dim, B.t_child, B.t_size, B.t_pre, B.t_split, B.t_bnd, T,
-        B.leafFlag);
+    k_slot_pre<<<tsph_blocks(2 * (long long)n, BS), BS, 0, ctx->stream>>>(B.topCap, 2 * n, B.t_root,
+                                                                          B.t_loc, B.t_pre);
+    TSPH_LAUNCH_CK("k_slot_pre");
+    TSPH_CK(cudaMemsetAsync(B.leafFlag, 0, sizeof(int) * (size_t)nodeNeed, ctx->stream));
+    const int scatN = B.topCap + 2 * n;
+    k_scatter_nodes<<<tsph_blocks(scatN, BS), BS, 0, ctx->stream>>>(
+        B.topCap, scatN, B.ctl, B.t_lo, B.t_hi, B.t_dim, B.t_child, B.t_size, B.t_pre, B.t_root,
+        B.t_split, B.t_bnd, P.rid, nR, T, B.leafFlag);
     TSPH_LAUNCH_CK("k_scatter_nodes");
-    rc = tsph_scan_inclusive(ctx, B.leafFlag, B.leafScan, nTemp);
+    rc = tsph_scan_inclusive(ctx, B.leafFlag, B.leafScan, nodeNeed);
     if (rc) return rc;
-    k_leaf_list<<<tsph_blocks(nTemp, BS), BS, 0, ctx->stream>>>(nTemp, B.leafFlag, B.leafScan,
-                                                                T.leaves);
+    k_leaf_list<<<tsph_blocks(nodeNeed, BS), BS, 0, ctx->stream>>>(B.ctl, B.leafFlag, B.leafScan,
+                                                                   T.leaves, T.dcnt);
     TSPH_LAUNCH_CK("k_leaf_list");
-    TSPH_CK(cudaMemcpyAsync(B.hostCount, B.leafScan + (nTemp - 1), sizeof(int),
-                            cudaMemcpyDeviceToHost, ctx->stream));
-    TSPH_CK(cudaStreamSynchronize(ctx->stream));
-    T.nNodes = nTemp;
-    T.nLeaves = B.hostCount[0];
-    // keep the level table for the moment pass
-    memcpy(ctx->B.hostCount + 1, levelStart, sizeof(int) * (nLevels + 1));
-    ctx->B.hostCount[TSPH_MAX_LEVELS + 4] = nLevels;
+    if (!ctx->capturing) {
+        TSPH_CK(cudaMemcpyAsync(B.hostCount, T.dcnt, 2 * sizeof(int), cudaMemcpyDeviceToHost,
+                                ctx->stream));
+        TSPH_CK(cudaMemcpyAsync(B.hostCount + 2, &B.ctl->status, sizeof(int), cudaMemcpyDeviceToHost,
+                                ctx->stream));
+        TSPH_CK(cudaStreamSynchronize(ctx->stream));
+        int st = B.hostCount[2];
+        for (int k = 1; k < 32; ++k)
+            if (st & (1 << k)) return k;
+        T.nNodes = B.hostCount[0];
+        T.nLeaves = B.hostCount[1];
+    } else {
+        T.nNodes = nodeNeed;     // upper bounds; the device holds the counts
+        T.nLeaves = n;
+    }
     return TSPH_OK;
 }
 
@@ -659,23 +1230,16 @@ int tsph_tree_moments(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, dou
     TsphBuildBufs &B = ctx->B;
     const int BS = 256;
     if (n == 0) return TSPH_OK;
-    int nLevels = B.hostCount[TSPH_MAX_LEVELS + 4];
-    const int *levelStart = B.hostCount + 1;
-    k_leaf_moments<<<tsph_blocks(T.nLeaves, BS), BS, 0, ctx->stream>>>(T.nLeaves, T.leaves, T, P.x,
-                                                                      P.y, P.z, P.m, P.h);
-    TSPH_LAUNCH_CK("k_leaf_moments");
-    for (int l = nLevels - 1; l >= 0; --l) {
-        int a = levelStart[l], b = levelStart[l + 1];
-        k_combine<<<tsph_blocks(b - a, BS), BS, 0, ctx->stream>>>(a, b, B.t_child, B.t_pre, T);
-        TSPH_LAUNCH_CK("k_combine");
-    }
-    k_zero_u64<<<tsph_blocks(T.nNodes, BS), BS, 0, ctx->stream>>>(B.maxd2, T.nNodes);
+    const int nodeNeed = 2 * n;
+    TSPH_CK(cudaMemsetAsync(B.visit, 0, sizeof(int) * (size_t)nodeNeed, ctx->stream));
+    k_moments<<<tsph_blocks(n, 128), 128, 0, ctx->stream>>>(T, P.x, P.y, P.z, P.m, P.h, B.visit);
+    TSPH_LAUNCH_CK("k_moments");
+    k_zero_u64<<<tsph_blocks(nodeNeed, BS), BS, 0, ctx->stream>>>(B.maxd2, nodeNeed);
     TSPH_LAUNCH_CK("k_zero_u64");
-    k_bmax<<<tsph_blocks(n, BS), BS, 0, ctx->stream>>>(n, T, P.x, P.y, P.z, B.maxd2);
+    k_bmax<<<tsph_blocks(n, BS), BS, 0, ctx->stream>>>(n, T, P.x, P.y, P.z, P.rid, B.maxd2);
     TSPH_LAUNCH_CK("k_bmax");
     const double twoOverSqrt3 = 2 / sqrt(3.0);
-    k_open<<<tsph_blocks(T.nNodes, BS), BS, 0, ctx->stream>>>(T.nNodes, T, B.maxd2, twoOverSqrt3,
-                                                              dTheta);
+    k_open<<<tsph_blocks(nodeNeed, BS), BS, 0, ctx->stream>>>(T, B.maxd2, twoOverSqrt3, dTheta);
     TSPH_LAUNCH_CK("k_open");
     k_parts32<<<tsph_blocks(n, BS), BS, 0, ctx->stream>>>(n, P.x, P.y, P.z, P.m, P.h, P.ph, P.pl);
     TSPH_LAUNCH_CK("k_parts32");

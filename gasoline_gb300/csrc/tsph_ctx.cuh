@@ -6,25 +6,40 @@
 
 #include "tsph_internal.cuh"
 
+// Device-side control block of one tree build.
+struct TsphBuildCtl {
+    int taskCount;    // subtree tasks queued
+    int taskNext;     // next task to claim
+    int nTop;         // temp nodes made by the level-wise top phase
+    int status;       // TSPH_ERR_* bits raised on the device
+    int nNodes;       // nodes of the finished forest
+    int pad[3];
+};
+
 struct TsphBuildBufs {
     int cap;          // particle capacity
-    int nodeCap;      // temp node capacity
-    int *seg;         // frontier index per particle (-1 = in a finished leaf)
+    int topCap;       // temp ids [0, topCap): roots and top-phase nodes
+    int tcap;         // topCap + 2*cap: task slots follow, 2 per particle
+    int *seg;         // temp id of the frontier node of each particle (-1 = done)
     int *lt;          // r[d] < fSplit flag
     int *scan;        // inclusive scan of lt
     int *scanTmp;     // block sums for the scan
-    // frontier, double-buffered
-    int *f_lo[2], *f_hi[2], *f_node[2];
-    int *f_split, *f_rank, *f_dim, *f_m;
-    double *f_fs;
-    unsigned long long *f_bnd;   // 6 keys per frontier entry
-    // temporary nodes, numbered breadth first
-    int *t_lo, *t_hi, *t_dim, *t_child, *t_size, *t_pre, *t_level;
-    double *t_split, *t_bnd;
+    int *f_node[2];   // top-phase frontier (temp ids), double-buffered
+    int *f_split, *f_rank;
+    int *tasks;       // subtree task roots (temp ids)
+    // temporary nodes: roots, then the top phase breadth first, then the
+    // subtree slots of every task (a task over particles [lo, hi] owns
+    // slots topCap + 2*lo ... topCap + 2*hi + 1)
+    int *t_lo, *t_hi, *t_dim, *t_child, *t_size, *t_pre, *t_root, *t_loc;
+    double *t_split;
+    double *t_bnd;    // 6 per node; holds order-preserving keys while bounds accumulate
     unsigned long long *maxd2;   // per final node: max squared distance to COM
-    int maxd2Cap;
+    int *visit;                  // per final node: children finished (bottom-up moments)
+    int nodeScratchCap;
     int *leafFlag, *leafScan;
+    TsphBuildCtl *ctl;           // device
     int *hostCount;              // pinned
+    int topLevels;               // top-phase levels of the last build
 };
 
 // SPH arrays, in gas-tree order (G.iord maps to the caller index)
@@ -100,6 +115,11 @@ struct tsph_ctx {
 
     TsphHnet hnet;
 
+    // tree build tuning and mode
+    int taskSize;                // largest node one CTA builds whole (0 = automatic)
+    int subtreeBlocks;           // resident CTAs of the subtree kernel
+    bool capturing;              // inside a CUDA graph capture: no host reads
+
     cudaEvent_t ev[10];
     float timings[8];
 };
@@ -135,7 +155,9 @@ static inline int tsph_blocks(long long n, int bs) {
 // internal entry points implemented across the .cu files
 int tsph_scan_inclusive(tsph_ctx *ctx, const int *in, int *out, int n);
 int tsph_build_tree(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, int nBucket);
+int tsph_set_ranges(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, int nR, const int *counts);
 int tsph_tree_moments(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, double dTheta);
+void tsph_free_build(TsphBuildBufs &B);
 int tsph_copy_out(tsph_ctx *ctx, const double *a0, const double *a1, const double *a2, int comp,
                   double *host);
 int tsph_copy_out_n(tsph_ctx *ctx, int n, const double *a0, const double *a1, const double *a2,

@@ -59,6 +59,17 @@ struct TsphDevTree {
     float4 *wmom0;    // m, Qxx, Qyy, Qzz
     float4 *wmom1;    // Qxy, Qxz, Qyz, fSoft
     int *leaves;      // leaf node ids in depth-first order (the buckets)
+    int *parent;      // parent node, -1 at a root
+    // forest of independent trees over contiguous particle ranges (one
+    // range = one system; a single system is a forest of one)
+    int nR;           // trees
+    int maxRange;     // particles in the largest tree (host)
+    int *rLo, *rHi;   // device: particle range of each tree
+    int *hLo, *hHi;   // host copies
+    int *sysRoot;     // device: root node of each tree
+    int *rEnd;        // device: one past the last node of each tree
+    int *dcnt;        // device: nNodes, nLeaves
+    int rCap;
     float4 *brec;     // per bucket: centre hi + soft max, centre lo + extent,
                       // box min - centre (+ n), box max - centre (FP32)
 };
@@ -68,6 +79,7 @@ struct TsphDevParts {
     int ngas;
     double *x, *y, *z, *m, *h;   // tree order
     int *iord;                   // caller index of each tree-order slot
+    int *rid;                    // tree (range) of each tree-order slot
     float4 *ph;                  // hi xyz + mass (float)
     float4 *pl;                  // lo xyz + soft (float)
     // outputs in tree order
