@@ -78,6 +78,12 @@ def sph_params(nSmooth=32, periodic=False, L=1.0, alpha=1.0, beta=2.0,
                      dEtaCourant, limiter, precision, int(learned_h), 0)
 
 
+class Tuning(ctypes.Structure):
+    """tsph_tuning (include/tsph.h): launch-shape knobs, result-neutral."""
+    _fields_ = [("taskSize", ctypes.c_int), ("walkBlocksPerSM", ctypes.c_int),
+                ("reserved", ctypes.c_int * 6)]
+
+
 class TsphError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__(f"libtsph error {code}: {msg}")
@@ -106,7 +112,9 @@ def load():
                  "tsph_get_state", "tsph_get_timings", "tsph_fma_peak",
                  "tsph_hnet_init", "tsph_hnet_set_params", "tsph_hnet_get_params",
                  "tsph_hnet_loss_grad", "tsph_hnet_mode", "tsph_hnet_train",
-                 "tsph_hnet_info", "tsph_hnet_num_params"):
+                 "tsph_hnet_info", "tsph_hnet_num_params", "tsph_set_tuning",
+                 "tsph_get_tuning", "tsph_set_systems", "tsph_step",
+                 "tsph_step_status"):
         getattr(lib, name).restype = ctypes.c_int
     lib.tsph_destroy.restype = None
     _lib = lib
@@ -312,3 +320,32 @@ class Context:
 
     def launches(self):
         return int(self.lib.tsph_launch_count(self._ctx))
+
+    def set_systems(self, sys_of, nsys=None):
+        """Independent systems (tsph_set_systems): sys_of[i] is the system
+        of caller particle i."""
+        so = np.ascontiguousarray(sys_of, dtype=np.int32)
+        if nsys is None:
+            nsys = int(so.max()) + 1 if len(so) else 1
+        self._check(self.lib.tsph_set_systems(self._ctx, int(nsys), so.ctypes.data_as(_IP)))
+
+    def step(self, dt, gp, sp=None, graph=False):
+        """One kick-drift-kick step (tsph_step); with graph=True the step is
+        captured once as a CUDA graph and replayed.  Queued only: call
+        step_status() to wait and collect errors."""
+        self._check(self.lib.tsph_step(self._ctx, ctypes.c_double(dt), ctypes.byref(gp),
+                                       ctypes.byref(sp) if sp is not None else None,
+                                       1 if graph else 0))
+
+    def step_status(self):
+        """Wait for queued steps; raise on the first error they raised."""
+        self._check(self.lib.tsph_step_status(self._ctx))
+
+    def set_tuning(self, taskSize=0, walkBlocksPerSM=0):
+        t = Tuning(taskSize, walkBlocksPerSM)
+        self._check(self.lib.tsph_set_tuning(self._ctx, ctypes.byref(t)))
+
+    def get_tuning(self):
+        t = Tuning()
+        self._check(self.lib.tsph_get_tuning(self._ctx, ctypes.byref(t)))
+        return {"taskSize": t.taskSize, "walkBlocksPerSM": t.walkBlocksPerSM}

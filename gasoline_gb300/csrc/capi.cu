@@ -27,6 +27,7 @@ extern "C" const char *tsph_error_string(int s) {
     case TSPH_ERR_STATE: return "call out of order";
     case TSPH_ERR_TREE_DEPTH: return "tree deeper than the level cap";
     case TSPH_ERR_NOMEM: return "device allocation failed";
+    case TSPH_ERR_BOUNDS: return "particle outside the captured coordinate bound";
     default: return "unknown status";
     }
 }
@@ -53,7 +54,10 @@ extern "C" int tsph_create(tsph_ctx **pctx, int device, void *stream) {
     if (cudaMalloc((void **)&ctx->dCnt, sizeof(TsphDevCounters)) != cudaSuccess ||
         cudaMallocHost((void **)&ctx->hCnt, sizeof(TsphDevCounters)) != cudaSuccess ||
         cudaMallocHost((void **)&ctx->B.hostCount, sizeof(int) * (TSPH_MAX_LEVELS + 16)) != cudaSuccess ||
-        cudaMalloc((void **)&ctx->dRoot, sizeof(double) * (64 + 256 * 32)) != cudaSuccess) {
+        cudaMalloc((void **)&ctx->dRoot, sizeof(double) * (64 + 256 * 32)) != cudaSuccess ||
+        cudaMalloc((void **)&ctx->dAux, sizeof(unsigned long long) * 4) != cudaSuccess ||
+        cudaMalloc((void **)&ctx->dStepStatus, sizeof(unsigned int)) != cudaSuccess ||
+        cudaMemset(ctx->dStepStatus, 0, sizeof(unsigned int)) != cudaSuccess) {
         tsph_destroy(ctx);
         return TSPH_ERR_NOMEM;
     }
@@ -92,6 +96,9 @@ extern "C" void tsph_destroy(tsph_ctx *ctx) {
     FREE(S.hax); FREE(S.hay); FREE(S.haz); FREE(S.uPdV); FREE(S.uAV); FREE(S.dtNew); FREE(S.mumax);
     FREE(S.seed); FREE(S.nnCount); FREE(S.nnHash); FREE(S.nodeBall2);
     FREE(ctx->dCnt); FREE(ctx->dBucketLists); FREE(ctx->dRoot); FREE(ctx->dEwt); FREE(ctx->dStage);
+    FREE(ctx->dAux); FREE(ctx->dStepStatus);
+    free(ctx->hSys);
+    if (ctx->graphExec) cudaGraphExecDestroy(ctx->graphExec);
     if (ctx->hCnt) cudaFreeHost(ctx->hCnt);
     if (ctx->B.hostCount) cudaFreeHost(ctx->B.hostCount);
     for (int k = 0; k < 10; ++k) if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
@@ -188,11 +195,18 @@ __global__ void k_copy_by_order(int n, const double *__restrict__ src, const int
     if (i < n) dst[i] = src[iord[i]];
 }
 
-__global__ void k_check_finite(int n, TsphDevParts P, unsigned int *status) {
+// Non-finite input, the coordinate scale of the walk's rounding bound, and
+// (for a captured step) particles beyond the bound the graph was built for.
+__global__ void k_check_finite(int n, TsphDevParts P, TsphDevCounters *cnt, double limit) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    double v = P.x[i] + P.y[i] + P.z[i] + P.m[i] + P.h[i];
-    if (!isfinite(v)) atomicOr(status, 1u << TSPH_ERR_NONFINITE);
+    double a = 0.0;
+    if (i < n) {
+        double v = P.x[i] + P.y[i] + P.z[i] + P.m[i] + P.h[i];
+        if (!isfinite(v)) atomicOr(&cnt->status, 1u << TSPH_ERR_NONFINITE);
+        a = fmax(fabs(P.x[i]), fmax(fabs(P.y[i]), fabs(P.z[i])));
+        if (a > limit) atomicOr(&cnt->status, 1u << TSPH_ERR_BOUNDS);
+    }
+    warp_max_abs(a, &cnt->maxAbs);
 }
 
 extern "C" int tsph_set_particles(tsph_ctx *ctx, int n, const double *pos, const double *mass,
@@ -208,9 +222,11 @@ extern "C" int tsph_set_particles(tsph_ctx *ctx, int n, const double *pos, const
     ctx->S.haveDensity = false;
     ctx->P.n = n;
     ctx->G.n = 0;
+    ctx->sysVersion++;
     if (n == 0) { ctx->haveParts = true; return TSPH_OK; }
     rc = tsph_set_ranges(ctx, ctx->P, ctx->T, n, 1, &n);
     if (rc) return rc;
+    ctx->nSys = 1;
     TSPH_CK(cudaMemcpyAsync(ctx->dStage, pos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
     k_load_state<<<tsph_blocks(n, 256), 256, 0, ctx->stream>>>(n, ctx->dStage, ctx->C, ctx->P.iord,
                                                                ctx->G.iord);
@@ -218,6 +234,84 @@ extern "C" int tsph_set_particles(tsph_ctx *ctx, int n, const double *pos, const
     TSPH_CK(cudaMemcpyAsync(ctx->C.m, mass, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
     TSPH_CK(cudaMemcpyAsync(ctx->C.h, soft, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
     ctx->haveParts = true;
+    return TSPH_OK;
+}
+
+// Tree order grouped by system: a stable counting sort of the caller
+// indices [0, n) by sys[], the sizes of the non-empty systems in order.
+static int order_by_system(const int *sys, int n, int nSys, int *order, int *counts, int *nR) {
+    int *start = (int *)calloc((size_t)nSys + 1, sizeof(int));
+    if (!start) return TSPH_ERR_NOMEM;
+    for (int i = 0; i < n; ++i) start[sys[i] + 1]++;
+    int r = 0;
+    for (int s = 0; s < nSys; ++s) {
+        if (start[s + 1] > 0) counts[r++] = start[s + 1];
+        start[s + 1] += start[s];
+    }
+    for (int i = 0; i < n; ++i) order[start[sys[i]]++] = i;
+    free(start);
+    *nR = r;
+    return TSPH_OK;
+}
+
+static int apply_systems_one(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n) {
+    if (n == 0) return TSPH_OK;
+    int *order = (int *)malloc(sizeof(int) * (size_t)n);
+    int *counts = (int *)malloc(sizeof(int) * (size_t)(ctx->nSys > n ? n : ctx->nSys));
+    if (!order || !counts) { free(order); free(counts); return TSPH_ERR_NOMEM; }
+    int nR = 0;
+    int rc = order_by_system(ctx->hSys, n, ctx->nSys, order, counts, &nR);
+    if (!rc) {
+        cudaError_t e = cudaMemcpy(P.iord, order, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice);
+        rc = e == cudaSuccess ? tsph_set_ranges(ctx, P, T, n, nR, counts) : tsph_cuda_fail(ctx, e, "iord");
+    }
+    free(order);
+    free(counts);
+    return rc;
+}
+
+// Gas tree order grouped by system (the gas particles are the first ngas).
+int tsph_apply_gas_systems(tsph_ctx *ctx) {
+    if (ctx->nSys <= 1 || !ctx->hSys) {
+        int ng = ctx->ngas;
+        return ng > 0 ? tsph_set_ranges(ctx, ctx->G, ctx->TG, ng, 1, &ng) : TSPH_OK;
+    }
+    return apply_systems_one(ctx, ctx->G, ctx->TG, ctx->ngas);
+}
+
+extern "C" int tsph_set_systems(tsph_ctx *ctx, int nSys, const int *sysOf) {
+    if (!ctx || nSys < 1) return TSPH_ERR_ARG;
+    if (!ctx->haveParts) return TSPH_ERR_STATE;
+    const int n = ctx->n;
+    if (n > 0 && !sysOf) return TSPH_ERR_ARG;
+    for (int i = 0; i < n; ++i)
+        if (sysOf[i] < 0 || sysOf[i] >= nSys) return TSPH_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    TSPH_CK(cudaStreamSynchronize(ctx->stream));
+    free(ctx->hSys);
+    ctx->hSys = (int *)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    if (!ctx->hSys) return TSPH_ERR_NOMEM;
+    if (n > 0) memcpy(ctx->hSys, sysOf, sizeof(int) * (size_t)n);
+    ctx->nSys = nSys;
+    int rc = apply_systems_one(ctx, ctx->P, ctx->T, n);
+    if (rc) return rc;
+    rc = tsph_apply_gas_systems(ctx);
+    if (rc) return rc;
+    ctx->haveTree = ctx->haveGrav = false;
+    ctx->S.haveDensity = ctx->S.havePressure = false;
+    ctx->sysVersion++;
+    return TSPH_OK;
+}
+
+__global__ void k_fold_status(const TsphDevCounters *cnt, unsigned int *acc) {
+    if (threadIdx.x == 0 && cnt->status) atomicOr(acc, cnt->status);
+}
+
+// Keep a pass's device status bits in the step's status word before the
+// next pass clears the counters.
+int tsph_fold_status(tsph_ctx *ctx) {
+    k_fold_status<<<1, 32, 0, ctx->stream>>>(ctx->dCnt, ctx->dStepStatus);
+    TSPH_LAUNCH_CK("k_fold_status");
     return TSPH_OK;
 }
 
@@ -238,35 +332,41 @@ extern "C" int tsph_grav_all(tsph_ctx *ctx, const tsph_grav_params *gp, tsph_gra
     if (!ctx->haveParts) return TSPH_ERR_STATE;
     if (gp->nBucket < 1 || gp->dTheta <= 0 || gp->iOrder < 1 || gp->iOrder > 4) return TSPH_ERR_ARG;
     if (gp->bPeriodic && !(gp->dPeriod > 0)) return TSPH_ERR_ARG;
+    if (gp->bPeriodic && ctx->T.nR > 1) return TSPH_ERR_UNSUPPORTED;   // isolated systems only
     if (gp->precision != TSPH_FP32 && gp->precision != TSPH_FP64) return TSPH_ERR_ARG;
     cudaSetDevice(ctx->device);
     const int n = ctx->n;
+    // Inside a graph capture (tsph_step) nothing here may wait for the
+    // device: no status reads, no timing events, scales fixed beforehand.
+    const bool cap = ctx->capturing;
+    if (cap && gp->bPeriodic) return TSPH_ERR_UNSUPPORTED;
+    // a direct call re-uploads constants a captured step relies on
+    if (!cap) ctx->sysVersion++;
     TSPH_CK(cudaMemsetAsync(ctx->dCnt, 0, sizeof(TsphDevCounters), ctx->stream));
-    cudaEventRecord(ctx->ev[0], ctx->stream);
+    if (!cap) cudaEventRecord(ctx->ev[0], ctx->stream);
     if (n > 0) {
         k_gather_tree<<<tsph_blocks(n, 256), 256, 0, ctx->stream>>>(n, ctx->C, ctx->P);
         TSPH_LAUNCH_CK("k_gather_tree");
-        k_check_finite<<<tsph_blocks(n, 256), 256, 0, ctx->stream>>>(n, ctx->P, &ctx->dCnt->status);
+        k_check_finite<<<tsph_blocks(n, 256), 256, 0, ctx->stream>>>(
+            n, ctx->P, ctx->dCnt, ctx->capLimit > 0 ? ctx->capLimit : INFINITY);
         TSPH_LAUNCH_CK("k_check_finite");
     }
-    int rc = read_status(ctx);
+    int rc = cap ? TSPH_OK : read_status(ctx);
     if (rc) return rc;
-    // largest absolute coordinate, for the walk's rounding bound
     ctx->dPeriodTree = gp->bPeriodic ? gp->dPeriod : 0.0;
     rc = tsph_build_tree(ctx, ctx->P, ctx->T, n, gp->nBucket);
     if (rc) return rc;
-    cudaEventRecord(ctx->ev[1], ctx->stream);
+    if (!cap) cudaEventRecord(ctx->ev[1], ctx->stream);
     rc = tsph_tree_moments(ctx, ctx->P, ctx->T, n, gp->dTheta);
     if (rc) return rc;
-    cudaEventRecord(ctx->ev[2], ctx->stream);
+    if (!cap) cudaEventRecord(ctx->ev[2], ctx->stream);
     ctx->haveTree = true;
     if (!gp->bPeriodic) {
-        // coordinate scale for the rounding floor: bounds of the root
-        double bnd[6];
-        TSPH_CK(cudaMemcpyAsync(bnd, ctx->T.bnd, sizeof(bnd), cudaMemcpyDeviceToHost, ctx->stream));
-        TSPH_CK(cudaStreamSynchronize(ctx->stream));
-        double r = 0;
-        for (int k = 0; k < 6; ++k) r = fmax(r, fabs(bnd[k]));
+        // coordinate scale for the rounding floor: the largest |coordinate|
+        // (for a captured step, the bound its particles are checked against)
+        double r;
+        memcpy(&r, &ctx->hCnt->maxAbs, sizeof(r));
+        if (ctx->capLimit > 0) r = ctx->capLimit;
         ctx->dPeriodTree = 2.0 * r;
     } else {
         ctx->dPeriodTree = 2.0 * gp->dPeriod;
@@ -275,7 +375,7 @@ extern "C" int tsph_grav_all(tsph_ctx *ctx, const tsph_grav_params *gp, tsph_gra
         rc = tsph_walk_interact(ctx, gp);
         if (rc) return rc;
     }
-    cudaEventRecord(ctx->ev[3], ctx->stream);
+    if (!cap) cudaEventRecord(ctx->ev[3], ctx->stream);
     if (n > 0) {
         bool ewald = gp->bPeriodic && gp->bEwald && gp->iEwOrder >= 1;
         if (ewald) rc = tsph_ewald(ctx, gp);
@@ -285,6 +385,10 @@ extern "C" int tsph_grav_all(tsph_ctx *ctx, const tsph_grav_params *gp, tsph_gra
     if (n > 0) {
         k_scatter_grav<<<tsph_blocks(n, 256), 256, 0, ctx->stream>>>(n, ctx->P, ctx->C);
         TSPH_LAUNCH_CK("k_scatter_grav");
+    }
+    if (cap) {
+        ctx->haveGrav = true;
+        return tsph_fold_status(ctx);
     }
     cudaEventRecord(ctx->ev[4], ctx->stream);
     rc = read_status(ctx);
@@ -445,3 +549,20 @@ extern "C" int tsph_get_timings(tsph_ctx *ctx, float *t8) {
 }
 
 extern "C" long long tsph_launch_count(tsph_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+extern "C" int tsph_set_tuning(tsph_ctx *ctx, const tsph_tuning *t) {
+    if (!ctx || !t) return TSPH_ERR_ARG;
+    if (t->taskSize < 0 || (t->taskSize > 0 && t->taskSize < 1024)) return TSPH_ERR_ARG;
+    if (t->walkBlocksPerSM < 0 || t->walkBlocksPerSM > 32) return TSPH_ERR_ARG;
+    ctx->taskSize = t->taskSize;
+    ctx->walkBlocksPerSM = t->walkBlocksPerSM;
+    return TSPH_OK;
+}
+
+extern "C" int tsph_get_tuning(tsph_ctx *ctx, tsph_tuning *t) {
+    if (!ctx || !t) return TSPH_ERR_ARG;
+    memset(t, 0, sizeof(*t));
+    t->taskSize = ctx->taskSize;
+    t->walkBlocksPerSM = ctx->walkBlocksPerSM;
+    return TSPH_OK;
+}

@@ -29,12 +29,11 @@
 
 #include "tsph_ctx.cuh"
 
-#define NB 8                    // particles per bucket handled per warp
-#define SLOTS (32 / NB)         // entry slots per particle
+// NBT (template): largest bucket one warp handles, 8, 16 or 32; lanes are
+// (bucket particle, entry slot) pairs with 32 / NBT slots per particle.
 #define WPB 4                   // warps per block
 #define STK 1536                // walk stack entries per warp (~32 x tree depth)
 #define PPF 128                 // P-P tile size
-#define PPB (PPF + 32 * NB + NB)
 #define CNF 64                  // cell tile size
 #define CNB (CNF + 32)
 
@@ -55,16 +54,16 @@ struct WalkConst {
 };
 __constant__ WalkConst cW;
 
-template <typename Real>
+template <typename Real, int NBT>
 struct WalkSmem {
     int stack[STK];
-    int pp[PPB];
+    int pp[PPF + 32 * NBT + NBT];
     int cn[CNB];
     int cs[CNB];
     // staged entry data: P-P uses x,y,z,m,h ; cells use x,y,z,m,q0..q5,h
     Real ex[PPF], ey[PPF], ez[PPF], em[PPF], eh[PPF];
     Real q[6][CNF];
-    Real px[NB], py[NB], pz[NB], pm[NB], ph[NB];
+    Real px[NBT], py[NBT], pz[NBT], pm[NBT], ph[NBT];
 };
 
 struct WalkArgs {
@@ -72,7 +71,7 @@ struct WalkArgs {
     TsphDevParts P;
     TsphDevCounters *cnt;
     int *bucketLists;      // optional, 4 ints per bucket
-    int nBuckets;
+    const int *nBuckets;   // device: the tree's leaf count
     int *workCounter;
     int iOrder;
 };
@@ -225,8 +224,8 @@ struct Acc {
 };
 
 // Stage P-P entries [0, cnt) of the warp's buffer into shared memory.
-template <typename Real>
-__device__ __forceinline__ void stage_pp(WalkSmem<Real> &S, const TsphDevParts &P, int cnt,
+template <typename Real, int NBT>
+__device__ __forceinline__ void stage_pp(WalkSmem<Real, NBT> &S, const TsphDevParts &P, int cnt,
                                          int lane, float bchx, float bchy, float bchz,
                                          float bclx, float bcly, float bclz) {
     for (int e = lane; e < cnt; e += 32) {
@@ -252,11 +251,11 @@ __device__ __forceinline__ void stage_pp(WalkSmem<Real> &S, const TsphDevParts &
 }
 
 // Evaluate staged P-P entries for this lane's particle.
-template <typename Real>
-__device__ __forceinline__ void eval_pp(WalkSmem<Real> &S, int cnt, int i, int slot, int pidx,
+template <typename Real, int NBT>
+__device__ __forceinline__ void eval_pp(WalkSmem<Real, NBT> &S, int cnt, int i, int slot, int pidx,
                                         int bucketLo, Acc<Real> &A) {
     Real xi = S.px[i], yi = S.py[i], zi = S.pz[i], hi = S.ph[i], mi = S.pm[i];
-    for (int e = slot; e < cnt; e += SLOTS) {
+    for (int e = slot; e < cnt; e += 32 / NBT) {
         int ent = S.pp[e];
         if ((ent & 31) == 31 && (ent >> 5) == bucketLo + i) continue;   // self
         Real dx = xi - S.ex[e], dy = yi - S.ey[e], dz = zi - S.ez[e];
@@ -278,8 +277,8 @@ __device__ __forceinline__ void eval_pp(WalkSmem<Real> &S, int cnt, int i, int s
 }
 
 // Stage cell entries (Newtonian when soft == 0, else softened).
-template <typename Real>
-__device__ __forceinline__ void stage_cells(WalkSmem<Real> &S, const int *buf, const TsphDevTree &T,
+template <typename Real, int NBT>
+__device__ __forceinline__ void stage_cells(WalkSmem<Real, NBT> &S, const int *buf, const TsphDevTree &T,
                                             int cnt, int lane, bool soft, float bchx, float bchy,
                                             float bchz, float bclx, float bcly, float bclz) {
     for (int e = lane; e < cnt; e += 32) {
@@ -317,11 +316,11 @@ __device__ __forceinline__ void stage_cells(WalkSmem<Real> &S, const int *buf, c
 }
 
 // Newtonian cells, QEVAL at order <= 2 (qeval.h:53-64).
-template <typename Real>
-__device__ __forceinline__ void eval_newt(WalkSmem<Real> &S, int cnt, int i, int slot, int iOrder,
+template <typename Real, int NBT>
+__device__ __forceinline__ void eval_newt(WalkSmem<Real, NBT> &S, int cnt, int i, int slot, int iOrder,
                                           Acc<Real> &A) {
     Real xi = S.px[i], yi = S.py[i], zi = S.pz[i], mi = S.pm[i];
-    for (int e = slot; e < cnt; e += SLOTS) {
+    for (int e = slot; e < cnt; e += 32 / NBT) {
         Real dx = xi - S.ex[e], dy = yi - S.ey[e], dz = zi - S.ez[e];
         Real d2 = dx * dx + dy * dy + dz * dz;
         Real g0 = rsq<Real>(d2);
@@ -361,10 +360,10 @@ __device__ __forceinline__ void eval_newt(WalkSmem<Real> &S, int cnt, int i, int
 }
 
 // Softened cells with the full quadrupole (grav.c:126-150).
-template <typename Real>
-__device__ __forceinline__ void eval_soft(WalkSmem<Real> &S, int cnt, int i, int slot, Acc<Real> &A) {
+template <typename Real, int NBT>
+__device__ __forceinline__ void eval_soft(WalkSmem<Real, NBT> &S, int cnt, int i, int slot, Acc<Real> &A) {
     Real xi = S.px[i], yi = S.py[i], zi = S.pz[i], hi = S.ph[i], mi = S.pm[i];
-    for (int e = slot; e < cnt; e += SLOTS) {
+    for (int e = slot; e < cnt; e += 32 / NBT) {
         Real dx = xi - S.ex[e], dy = yi - S.ey[e], dz = zi - S.ez[e];
         Real d2 = dx * dx + dy * dy + dz * dz;
         Real twoh = hi + S.eh[e];
@@ -398,12 +397,12 @@ __device__ __forceinline__ void flush_tile(Acc<Real> &A) {
     }
 }
 
-template <typename Real>
+template <typename Real, int NBT>
 __global__ void __launch_bounds__(WPB * 32) k_walk(WalkArgs W) {
     extern __shared__ __align__(16) unsigned char smraw[];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
-    WalkSmem<Real> &S = reinterpret_cast<WalkSmem<Real> *>(smraw)[wib];
+    WalkSmem<Real, NBT> &S = reinterpret_cast<WalkSmem<Real, NBT> *>(smraw)[wib];
     const TsphDevTree &T = W.T;
     const TsphDevParts &P = W.P;
     const unsigned FULL = 0xffffffffu;
@@ -416,12 +415,12 @@ __global__ void __launch_bounds__(WPB * 32) k_walk(WalkArgs W) {
         int b = 0;
         if (lane == 0) b = atomicAdd(W.workCounter, 1);
         b = __shfl_sync(FULL, b, 0);
-        if (b >= W.nBuckets) break;
+        if (b >= *W.nBuckets) break;
         const int node = T.leaves[b];
         const int lo = T.pLower[node];
         const int n = T.pUpper[node] - lo + 1;
-        if (n > NB) {
-            // a zero-extent leaf holding more than NB coincident particles
+        if (n > NBT) {
+            // a zero-extent leaf holding more than NBT coincident particles
             if (lane == 0) atomicOr(&W.cnt->status, 1u << TSPH_ERR_UNSUPPORTED);
             continue;
         }
@@ -442,7 +441,7 @@ __global__ void __launch_bounds__(WPB * 32) k_walk(WalkArgs W) {
             for (int k = 0; k < 3; ++k) bc64[k] = 0.0;
         }
         // bucket particles
-        if (lane < NB) {
+        if (lane < NBT) {
             int p = lo + (lane < n ? lane : 0);
             if constexpr (sizeof(Real) == 4) {
                 float4 a = P.ph[p], c = P.pl[p];
@@ -463,13 +462,14 @@ __global__ void __launch_bounds__(WPB * 32) k_walk(WalkArgs W) {
         // initial stack: the root in every replica; P-P buffer: the bucket's
         // own particles for the intra-bucket pairs (replica tag 31)
         int sp = 0, ppn = 0, cnn = 0, csn = 0, nPart = 0, nNewt = 0, nSoft = 0;
-        for (int r = lane; r < cW.nRep; r += 32) S.stack[r] = r;   // (0 << 5) | r
+        const int root = T.sysRoot[P.rid[lo]];   // the bucket's own system
+        for (int r = lane; r < cW.nRep; r += 32) S.stack[r] = (root << 5) | r;
         sp = cW.nRep;
         if (lane < n) S.pp[lane] = ((lo + lane) << 5) | 31;
         ppn = n;
         bool overflow = false;
         // accumulators: lane = (particle i, slot)
-        const int i = lane % NB, slot = lane / NB;
+        const int i = lane % NBT, slot = lane / NBT;
         Acc<Real> A;
 #pragma unroll
         for (int k = 0; k < 4; ++k) { A.s[k] = 0; A.c[k] = 0; A.t[k] = 0; }
@@ -549,7 +549,7 @@ __global__ void __launch_bounds__(WPB * 32) k_walk(WalkArgs W) {
             }
             sp += 2 * __popc(bo);
             // leaf particles
-            if (act == ACT_LEAF && cnt > NB) {
+            if (act == ACT_LEAF && cnt > NBT) {
                 atomicOr(&W.cnt->status, 1u << TSPH_ERR_UNSUPPORTED);
                 act = ACT_NONE;
             }
@@ -575,9 +575,9 @@ __global__ void __launch_bounds__(WPB * 32) k_walk(WalkArgs W) {
             __syncwarp();
             // evaluate full tiles
             while (ppn >= PPF) {
-                stage_pp<Real>(S, P, PPF, lane, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
+                stage_pp<Real, NBT>(S, P, PPF, lane, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
                 __syncwarp();
-                if (i < n) eval_pp<Real>(S, PPF, i, slot, lo + i, lo, A);
+                if (i < n) eval_pp<Real, NBT>(S, PPF, i, slot, lo + i, lo, A);
                 flush_tile(A);
                 __syncwarp();
                 for (int e = lane; e < ppn - PPF; e += 32) S.pp[e] = S.pp[PPF + e];
@@ -585,9 +585,9 @@ __global__ void __launch_bounds__(WPB * 32) k_walk(WalkArgs W) {
                 __syncwarp();
             }
             while (cnn >= CNF) {
-                stage_cells<Real>(S, S.cn, T, CNF, lane, false, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
+                stage_cells<Real, NBT>(S, S.cn, T, CNF, lane, false, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
                 __syncwarp();
-                if (i < n) eval_newt<Real>(S, CNF, i, slot, W.iOrder, A);
+                if (i < n) eval_newt<Real, NBT>(S, CNF, i, slot, W.iOrder, A);
                 flush_tile(A);
                 __syncwarp();
                 for (int e = lane; e < cnn - CNF; e += 32) S.cn[e] = S.cn[CNF + e];
@@ -595,9 +595,9 @@ __global__ void __launch_bounds__(WPB * 32) k_walk(WalkArgs W) {
                 __syncwarp();
             }
             while (csn >= CNF) {
-                stage_cells<Real>(S, S.cs, T, CNF, lane, true, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
+                stage_cells<Real, NBT>(S, S.cs, T, CNF, lane, true, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
                 __syncwarp();
-                if (i < n) eval_soft<Real>(S, CNF, i, slot, A);
+                if (i < n) eval_soft<Real, NBT>(S, CNF, i, slot, A);
                 flush_tile(A);
                 __syncwarp();
                 for (int e = lane; e < csn - CNF; e += 32) S.cs[e] = S.cs[CNF + e];
@@ -612,29 +612,29 @@ __global__ void __launch_bounds__(WPB * 32) k_walk(WalkArgs W) {
         }
         // remaining partial tiles
         if (ppn > 0) {
-            stage_pp<Real>(S, P, ppn, lane, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
+            stage_pp<Real, NBT>(S, P, ppn, lane, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
             __syncwarp();
-            if (i < n) eval_pp<Real>(S, ppn, i, slot, lo + i, lo, A);
+            if (i < n) eval_pp<Real, NBT>(S, ppn, i, slot, lo + i, lo, A);
             flush_tile(A);
             __syncwarp();
         }
         if (cnn > 0) {
-            stage_cells<Real>(S, S.cn, T, cnn, lane, false, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
+            stage_cells<Real, NBT>(S, S.cn, T, cnn, lane, false, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
             __syncwarp();
-            if (i < n) eval_newt<Real>(S, cnn, i, slot, W.iOrder, A);
+            if (i < n) eval_newt<Real, NBT>(S, cnn, i, slot, W.iOrder, A);
             flush_tile(A);
             __syncwarp();
         }
         if (csn > 0) {
-            stage_cells<Real>(S, S.cs, T, csn, lane, true, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
+            stage_cells<Real, NBT>(S, S.cs, T, csn, lane, true, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
             __syncwarp();
-            if (i < n) eval_soft<Real>(S, csn, i, slot, A);
+            if (i < n) eval_soft<Real, NBT>(S, csn, i, slot, A);
             flush_tile(A);
             __syncwarp();
         }
-        // reduce the SLOTS partial accumulators of each particle
+        // reduce the 32 / NBT partial accumulators of each particle
 #pragma unroll
-        for (int o = NB; o < 32; o <<= 1) {
+        for (int o = NBT; o < 32; o <<= 1) {
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 Real s2 = __shfl_xor_sync(FULL, A.s[k], o);
@@ -696,9 +696,9 @@ __global__ void __launch_bounds__(WPB * 32) k_walk(WalkArgs W) {
 // extent, box corners relative to the centre.  The FP64 work happens here
 // once per bucket, by one thread, instead of redundantly on every lane of
 // the walk (FP64 issues at 1/64 of the FP32 rate on this part).
-__global__ void k_bucket_prep(int nBuckets, TsphDevTree T, TsphDevParts P) {
+__global__ void k_bucket_prep(TsphDevTree T, TsphDevParts P) {
     int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= nBuckets) return;
+    if (b >= T.dcnt[1]) return;
     int node = T.leaves[b];
     int lo = T.pLower[node], hi = T.pUpper[node];
     double bc[3];
@@ -739,10 +739,21 @@ int tsph_walk_finish_f32(tsph_ctx *ctx) {
     return TSPH_OK;
 }
 
+template <typename Real, int NBT>
+static int launch_walk(tsph_ctx *ctx, const WalkArgs &A, int blocks, const char *name) {
+    size_t sm = sizeof(WalkSmem<Real, NBT>) * WPB;
+    if (!ctx->capturing)
+        TSPH_CK(cudaFuncSetAttribute(k_walk<Real, NBT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)sm));
+    k_walk<Real, NBT><<<blocks, WPB * 32, sm, ctx->stream>>>(A);
+    TSPH_LAUNCH_CK(name);
+    return TSPH_OK;
+}
+
 int tsph_walk_interact(tsph_ctx *ctx, const tsph_grav_params *gp) {
     if (gp->iOrder < 1 || gp->iOrder > 2) return TSPH_ERR_UNSUPPORTED;
     if (gp->bPeriodic && gp->nReps > 1) return TSPH_ERR_UNSUPPORTED;
-    if (gp->nBucket > NB) return TSPH_ERR_UNSUPPORTED;
+    if (gp->nBucket > 32) return TSPH_ERR_UNSUPPORTED;
     WalkConst wc;
     memset(&wc, 0, sizeof(wc));
     int nR = gp->bPeriodic ? gp->nReps : 0;
@@ -768,37 +779,44 @@ int tsph_walk_interact(tsph_ctx *ctx, const tsph_grav_params *gp) {
     // absolute coordinate (positions + offsets)
     rabs = ctx->dPeriodTree + offmax;
     wc.E0 = (float)(16.0 * 3.552713678800501e-15 * rabs) + 1e-30f;
-    TSPH_CK(cudaMemcpyToSymbolAsync(cW, &wc, sizeof(wc), 0, cudaMemcpyHostToDevice, ctx->stream));
+    // constants are uploaded outside graph capture (a captured step reuses
+    // the ones its preparation set)
+    if (!ctx->capturing)
+        TSPH_CK(cudaMemcpyToSymbolAsync(cW, &wc, sizeof(wc), 0, cudaMemcpyHostToDevice, ctx->stream));
 
     WalkArgs A;
     A.T = ctx->T;
     A.P = ctx->P;
     A.cnt = ctx->dCnt;
-    A.nBuckets = ctx->T.nLeaves;
+    A.nBuckets = ctx->T.dcnt + 1;
     A.iOrder = gp->iOrder;
     int rc = TSPH_OK;
-    if (ctx->bucketListCap < A.nBuckets) {
-        rc = tsph_grow(ctx, &ctx->dBucketLists, (size_t)4 * A.nBuckets + 64);
-        if (rc) return rc;
-        ctx->bucketListCap = A.nBuckets;
+    const int nbHost = ctx->T.nLeaves;   // exact, or an upper bound while capturing
+    A.bucketLists = nullptr;
+    if (!ctx->capturing) {
+        if (ctx->bucketListCap < nbHost) {
+            rc = tsph_grow(ctx, &ctx->dBucketLists, (size_t)4 * nbHost + 64);
+            if (rc) return rc;
+            ctx->bucketListCap = nbHost;
+        }
+        A.bucketLists = ctx->dBucketLists;
     }
-    A.bucketLists = ctx->dBucketLists;
     // work counter lives in the counters block's pad area
     A.workCounter = (int *)&ctx->dCnt->pad;
     TSPH_CK(cudaMemsetAsync(A.workCounter, 0, sizeof(int), ctx->stream));
-    k_bucket_prep<<<tsph_blocks(A.nBuckets, 128), 128, 0, ctx->stream>>>(A.nBuckets, ctx->T, ctx->P);
+    k_bucket_prep<<<tsph_blocks(nbHost, 128), 128, 0, ctx->stream>>>(ctx->T, ctx->P);
     TSPH_LAUNCH_CK("k_bucket_prep");
-    int blocks = ctx->smCount * 4;
+    int blocks = ctx->smCount * (ctx->walkBlocksPerSM > 0 ? ctx->walkBlocksPerSM : 4);
+    const int nbt = gp->nBucket <= 8 ? 8 : (gp->nBucket <= 16 ? 16 : 32);
     if (gp->precision == TSPH_FP32) {
-        size_t sm = sizeof(WalkSmem<float>) * WPB;
-        TSPH_CK(cudaFuncSetAttribute(k_walk<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        k_walk<float><<<blocks, WPB * 32, sm, ctx->stream>>>(A);
-        TSPH_LAUNCH_CK("k_walk<float>");
+        if (nbt == 8) rc = launch_walk<float, 8>(ctx, A, blocks, "k_walk<float,8>");
+        else if (nbt == 16) rc = launch_walk<float, 16>(ctx, A, blocks, "k_walk<float,16>");
+        else rc = launch_walk<float, 32>(ctx, A, blocks, "k_walk<float,32>");
     } else {
-        size_t sm = sizeof(WalkSmem<double>) * WPB;
-        TSPH_CK(cudaFuncSetAttribute(k_walk<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        k_walk<double><<<blocks, WPB * 32, sm, ctx->stream>>>(A);
-        TSPH_LAUNCH_CK("k_walk<double>");
+        if (nbt == 8) rc = launch_walk<double, 8>(ctx, A, blocks, "k_walk<double,8>");
+        else if (nbt == 16) rc = launch_walk<double, 16>(ctx, A, blocks, "k_walk<double,16>");
+        else rc = launch_walk<double, 32>(ctx, A, blocks, "k_walk<double,32>");
     }
+    if (rc) return rc;
     return TSPH_OK;
 }

@@ -147,11 +147,11 @@ __global__ void k_adam(float *W, const float *__restrict__ grad, float *m1, floa
 // Features of every gas particle of the current density pass (gas-tree
 // order): f0, f1, f2 as described at the top of this file.
 __global__ void k_hnet_features(int ng, int k, TsphDevTree T, const int *__restrict__ iord,
-                                const double *__restrict__ fb2prev,
+                                const int *__restrict__ rid, const double *__restrict__ fb2prev,
                                 const double *__restrict__ divvprev, float *feat) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= ng) return;
-    int node = 0;
+    int node = T.sysRoot[rid[i]];
     for (;;) {
         int up = T.upper[node];
         if (up < 0) break;
@@ -372,8 +372,8 @@ int tsph_hnet_features(tsph_ctx *ctx, int k) {
         if (rc) return rc;
     }
     k_hnet_features<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, k, ctx->TG, ctx->G.iord,
-                                                                  ctx->C.fb2prev, ctx->C.divvprev,
-                                                                  Hn.feat);
+                                                                  ctx->G.rid, ctx->C.fb2prev,
+                                                                  ctx->C.divvprev, Hn.feat);
     TSPH_LAUNCH_CK("k_hnet_features");
     return TSPH_OK;
 }

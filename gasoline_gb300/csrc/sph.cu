@@ -146,11 +146,11 @@ __device__ void warp_sort_idx(int *nbr, int cnt, int lane) {
 
 // Ball gather of all gas particles with d2 <= r2 around particle i.
 // Returns the count, or -1 when it exceeds SCAP or the stack overflows.
-__device__ int ball_gather(KnnSmem &W, const SphArgs &A, int lane, double xi, double yi, double zi,
-                           float xf, float yf, float zf, double r2) {
+__device__ int ball_gather(KnnSmem &W, const SphArgs &A, int lane, int root, double xi, double yi,
+                           double zi, float xf, float yf, float zf, double r2) {
     const unsigned FULL = 0xffffffffu;
     int sp = 1, nc = 0;
-    if (lane == 0) W.stack[0] = 0;
+    if (lane == 0) W.stack[0] = root;
     __syncwarp();
     float r2f = (float)r2 * 1.00001f;
     bool bad = false;
@@ -234,12 +234,13 @@ __global__ void __launch_bounds__(SW * 32) k_knn_density(SphArgs A) {
         if (i >= ng) break;
         const double xi = A.G.x[i], yi = A.G.y[i], zi = A.G.z[i];
         const float xf = (float)xi, yf = (float)yi, zf = (float)zi;
+        const int root = A.T.sysRoot[A.G.rid[i]];   // this particle's system
         // seed radius
         double r2;
         if (A.seed && A.seed[i] > 0.0) {
             r2 = A.seed[i];
         } else {
-            int node = 0;
+            int node = root;
             for (;;) {
                 int up = A.T.upper[node];
                 if (up < 0) break;
@@ -259,7 +260,7 @@ __global__ void __launch_bounds__(SW * 32) k_knn_density(SphArgs A) {
         double lo2 = 0.0, hi2 = 0.0;   // radii known too small / too large
         int nc = -1, it = 0;
         for (; it < SMAXIT; ++it) {
-            nc = ball_gather(W, A, lane, xi, yi, zi, xf, yf, zf, r2);
+            nc = ball_gather(W, A, lane, root, xi, yi, zi, xf, yf, zf, r2);
             if (nc < 0) {                       // too many candidates: shrink
                 hi2 = r2;
                 r2 = lo2 > 0.0 ? sqrt(lo2 * hi2) : 0.5 * r2;
@@ -407,12 +408,12 @@ __global__ void k_gas_pressure(int ng, TsphSphBufs S) {
 }
 
 // per gas-tree node: max fBall2 of its particles (atomicMax on the bits)
-__global__ void k_node_ball(int ng, TsphDevTree T, const double *__restrict__ fBall2,
-                            unsigned long long *nodeBall2) {
+__global__ void k_node_ball(int ng, TsphDevTree T, const int *__restrict__ rid,
+                            const double *__restrict__ fBall2, unsigned long long *nodeBall2) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     bool live = p < ng;
     unsigned long long key = live ? (unsigned long long)__double_as_longlong(fBall2[p]) : 0ULL;
-    int i = 0;
+    int i = live ? T.sysRoot[rid[p]] : 0;
     unsigned mask = __ballot_sync(0xffffffffu, live);
     while (mask) {
         if (live) {
@@ -449,7 +450,7 @@ __global__ void __launch_bounds__(SW * 32) k_pressure(SphArgs A) {
         const TsphSphBufs &S = A.S;
         double ax = 0, ay = 0, az = 0, uPdV = 0, uAV = 0, mu = 0.0, dtN = FLT_MAX;
         int sp = 1;
-        if (lane == 0) stack[0] = 0;
+        if (lane == 0) stack[0] = A.T.sysRoot[A.G.rid[i]];
         __syncwarp();
         bool bad = false;
         while (sp > 0) {
@@ -582,6 +583,13 @@ __global__ void k_gas_gather_pos(int ng, TsphDevState C, TsphDevParts G) {
     G.m[i] = C.m[o]; G.h[i] = C.h[o];
 }
 
+__global__ void k_gas_maxabs(int ng, TsphDevParts G, unsigned long long *out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double a = 0.0;
+    if (i < ng) a = fmax(fabs(G.x[i]), fmax(fabs(G.y[i]), fabs(G.z[i])));
+    warp_max_abs(a, out);
+}
+
 __global__ void k_gas_gather_vel(int ng, TsphDevState C, const int *__restrict__ iord, TsphSphBufs S) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= ng) return;
@@ -591,9 +599,9 @@ __global__ void k_gas_gather_vel(int ng, TsphDevState C, const int *__restrict__
 }
 
 // FP32 node boxes for the gas walks (stored in wcomh/wcoml of the gas tree)
-__global__ void k_gas_nodes(int nNodes, TsphDevTree T) {
+__global__ void k_gas_nodes(TsphDevTree T) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nNodes) return;
+    if (i >= T.dcnt[0]) return;
     const double *b = &T.bnd[6 * i];
     T.wcomh[i] = make_float4((float)b[0], (float)b[1], (float)b[2], 0.0f);
     T.wcoml[i] = make_float4((float)b[3], (float)b[4], (float)b[5], 0.0f);
@@ -651,11 +659,16 @@ static void set_sph_const(tsph_ctx *ctx, const tsph_sph_params *sp) {
     c.gammam1 = sp->gamma - 1;
     c.dtFacCourant = sp->dEtaCourant * 1.0 * 2 / 1.6;   // pkdDtFacCourant, a = 1
     c.limiter = sp->iViscosityLimiter;
-    // FP32 box tests: pad by a few ulps of the largest coordinate
-    double bnd[6];
-    cudaMemcpy(bnd, ctx->TG.bnd, sizeof(bnd), cudaMemcpyDeviceToHost);
-    double r = 0;
-    for (int k = 0; k < 6; ++k) r = fmax(r, fabs(bnd[k]));
+    // FP32 box tests: pad by a few ulps of the largest |coordinate| (of all
+    // systems), measured by k_gas_maxabs
+    double r = ctx->gasScale;
+    if (!ctx->capturing) {
+        unsigned long long bits = 0;
+        cudaMemcpy(&bits, ctx->dAux, sizeof(bits), cudaMemcpyDeviceToHost);
+        memcpy(&r, &bits, sizeof(r));
+        ctx->gasScale = r;
+    }
+    if (ctx->capLimit > r) r = ctx->capLimit;   // a captured step's coordinate bound
     if (sp->bPeriodic) r += sp->dPeriod;
     c.margin = (float)(8.0 * 5.960464477539063e-08 * r) + 1e-30f;
     cudaMemcpyToSymbolAsync(cS, &c, sizeof(c), 0, cudaMemcpyHostToDevice, ctx->stream);
@@ -669,6 +682,7 @@ extern "C" int tsph_set_velocities(tsph_ctx *ctx, const double *vel, int ngas, c
     const int n = ctx->n;
     ctx->ngas = ngas;
     ctx->G.n = ngas;
+    ctx->sysVersion++;
     ctx->S.haveDensity = ctx->S.havePressure = false;
     ctx->hnet.havePrev = false;
     if (n == 0) { ctx->haveVel = true; return TSPH_OK; }
@@ -681,7 +695,7 @@ extern "C" int tsph_set_velocities(tsph_ctx *ctx, const double *vel, int ngas, c
         TSPH_LAUNCH_CK("k_load_u");
         k_gas_identity<<<tsph_blocks(ngas, 256), 256, 0, ctx->stream>>>(ngas, ctx->G.iord);
         TSPH_LAUNCH_CK("k_gas_identity");
-        int rc = tsph_set_ranges(ctx, ctx->G, ctx->TG, ngas, 1, &ngas);
+        int rc = tsph_apply_gas_systems(ctx);
         if (rc) return rc;
     }
     ctx->haveVel = true;
@@ -691,19 +705,28 @@ extern "C" int tsph_set_velocities(tsph_ctx *ctx, const double *vel, int ngas, c
 static int run_density(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_out *out) {
     const int ng = ctx->ngas;
     TsphSphBufs &S = ctx->S;
-    cudaEventRecord(ctx->ev[5], ctx->stream);
+    const bool cap = ctx->capturing;
+    if (cap && sp->bLearnedH) return TSPH_ERR_UNSUPPORTED;
+    if (!cap) cudaEventRecord(ctx->ev[5], ctx->stream);
     k_gas_gather_pos<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, ctx->C, ctx->G);
     TSPH_LAUNCH_CK("k_gas_gather_pos");
+    if (!ctx->capturing) {
+        TSPH_CK(cudaMemsetAsync(ctx->dAux, 0, sizeof(unsigned long long), ctx->stream));
+        k_gas_maxabs<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, ctx->G, ctx->dAux);
+        TSPH_LAUNCH_CK("k_gas_maxabs");
+    }
     int rc = tsph_build_tree(ctx, ctx->G, ctx->TG, ng, 16);
     if (rc) return rc;
-    k_gas_nodes<<<tsph_blocks(ctx->TG.nNodes, 256), 256, 0, ctx->stream>>>(ctx->TG.nNodes, ctx->TG);
+    k_gas_nodes<<<tsph_blocks(ctx->TG.nNodes, 256), 256, 0, ctx->stream>>>(ctx->TG);
     TSPH_LAUNCH_CK("k_gas_nodes");
     k_gas_gather_vel<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, ctx->C, ctx->G.iord, S);
     TSPH_LAUNCH_CK("k_gas_gather_vel");
-    set_sph_const(ctx, sp);
+    if (!cap) set_sph_const(ctx, sp);
     const int kk = sp->nSmooth < ng ? sp->nSmooth : ng;
-    rc = tsph_hnet_features(ctx, kk);
-    if (rc) return rc;
+    if (!cap) {
+        rc = tsph_hnet_features(ctx, kk);
+        if (rc) return rc;
+    }
     if (sp->bLearnedH) {
         rc = tsph_hnet_seed(ctx);
         if (rc) return rc;
@@ -718,11 +741,23 @@ static int run_density(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_out
     A.work = (int *)&ctx->dCnt->pad;
     A.seed = (sp->bLearnedH && S.haveSeed) ? S.seed : nullptr;
     TSPH_CK(cudaMemsetAsync(ctx->dCnt, 0, sizeof(TsphDevCounters), ctx->stream));
-    cudaEventRecord(ctx->ev[6], ctx->stream);
+    if (!cap) cudaEventRecord(ctx->ev[6], ctx->stream);
     size_t sm = sizeof(KnnSmem) * SW;
-    TSPH_CK(cudaFuncSetAttribute(k_knn_density, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    if (!cap)
+        TSPH_CK(cudaFuncSetAttribute(k_knn_density, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     k_knn_density<<<ctx->smCount * 3, SW * 32, sm, ctx->stream>>>(A);
     TSPH_LAUNCH_CK("k_knn_density");
+    if (cap) {
+        rc = tsph_fold_status(ctx);
+        if (rc) return rc;
+        k_save_prev<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, ctx->G.iord, S.fBall2, S.divv,
+                                                                  ctx->C.fb2prev, ctx->C.divvprev);
+        TSPH_LAUNCH_CK("k_save_prev");
+        S.haveDensity = true;
+        S.havePressure = false;
+        S.last = *sp;
+        return TSPH_OK;
+    }
     cudaEventRecord(ctx->ev[7], ctx->stream);
     TSPH_CK(cudaMemcpyAsync(ctx->hCnt, ctx->dCnt, sizeof(TsphDevCounters), cudaMemcpyDeviceToHost,
                             ctx->stream));
@@ -755,12 +790,16 @@ static int run_density(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_out
 static int run_pressure(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_out *out) {
     const int ng = ctx->ngas;
     TsphSphBufs &S = ctx->S;
-    set_sph_const(ctx, sp);
-    cudaEventRecord(ctx->ev[8], ctx->stream);
+    const bool cap = ctx->capturing;
+    if (!cap) {
+        set_sph_const(ctx, sp);
+        cudaEventRecord(ctx->ev[8], ctx->stream);
+    }
     k_gas_pressure<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, S);
     TSPH_LAUNCH_CK("k_gas_pressure");
     TSPH_CK(cudaMemsetAsync(S.nodeBall2, 0, sizeof(unsigned long long) * ctx->TG.nNodes, ctx->stream));
-    k_node_ball<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, ctx->TG, S.fBall2, S.nodeBall2);
+    k_node_ball<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, ctx->TG, ctx->G.rid, S.fBall2,
+                                                              S.nodeBall2);
     TSPH_LAUNCH_CK("k_node_ball");
     SphArgs A;
     A.T = ctx->TG;
@@ -774,6 +813,10 @@ static int run_pressure(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_ou
     TSPH_LAUNCH_CK("k_pressure");
     k_scatter_hydro<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, ctx->G.iord, S, ctx->C);
     TSPH_LAUNCH_CK("k_scatter_hydro");
+    if (cap) {
+        S.havePressure = true;
+        return tsph_fold_status(ctx);
+    }
     cudaEventRecord(ctx->ev[9], ctx->stream);
     TSPH_CK(cudaMemcpyAsync(ctx->hCnt, ctx->dCnt, sizeof(TsphDevCounters), cudaMemcpyDeviceToHost,
                             ctx->stream));
@@ -803,6 +846,13 @@ extern "C" int tsph_smooth(tsph_ctx *ctx, int smx_type, const tsph_sph_params *s
         if (out) memset(out, 0, sizeof(*out));
         return TSPH_OK;
     }
+    if (ctx->TG.nR > 1) {
+        // several systems: isolated, and each needs nSmooth gas particles
+        if (sp->bPeriodic) return TSPH_ERR_UNSUPPORTED;
+        for (int r = 0; r < ctx->TG.nR; ++r)
+            if (ctx->TG.hHi[r] - ctx->TG.hLo[r] + 1 < sp->nSmooth) return TSPH_ERR_ARG;
+    }
+    if (!ctx->capturing) ctx->sysVersion++;   // constants change: recapture a step graph
     if (smx_type == TSPH_SMX_DENDVDX) return run_density(ctx, sp, out);
     if (!ctx->S.haveDensity) return TSPH_ERR_STATE;
     return run_pressure(ctx, sp, out);
@@ -932,7 +982,7 @@ extern "C" int tsph_kick(tsph_ctx *ctx, double dt) {
     if (ctx->n == 0) return TSPH_OK;
     k_kick<<<tsph_blocks(ctx->n, 256), 256, 0, ctx->stream>>>(ctx->n, ctx->ngas, dt, ctx->C);
     TSPH_LAUNCH_CK("k_kick");
-    TSPH_CK(cudaStreamSynchronize(ctx->stream));
+    if (!ctx->capturing) TSPH_CK(cudaStreamSynchronize(ctx->stream));
     return TSPH_OK;
 }
 
@@ -944,7 +994,7 @@ extern "C" int tsph_drift(tsph_ctx *ctx, double dt, int bPeriodic, double dPerio
     if (ctx->n == 0) return TSPH_OK;
     k_drift<<<tsph_blocks(ctx->n, 256), 256, 0, ctx->stream>>>(ctx->n, dt, bPeriodic, dPeriod, ctx->C);
     TSPH_LAUNCH_CK("k_drift");
-    TSPH_CK(cudaStreamSynchronize(ctx->stream));
+    if (!ctx->capturing) TSPH_CK(cudaStreamSynchronize(ctx->stream));
     ctx->S.haveDensity = ctx->S.havePressure = false;
     ctx->haveGrav = false;
     return TSPH_OK;

@@ -1,0 +1,141 @@
+// One kick-drift-kick step as a single stream of kernels, optionally
+// captured once as a CUDA graph and replayed.
+//
+// The step follows the reference's single-rung msrTopStepKDK
+// (master.c:8242-8465): opening kick by dt/2 (pkdKick), drift by dt
+// (pkdDrift), forces at the new positions (pkdGravAll, then for the gas
+// smSmooth(SMX_DENDVDX), pkdGasPressure, smReSmooth(SMX_SPHPRESSURETERMS)),
+// closing kick by dt/2.  In graph mode every launch of that sequence is
+// recorded once and the whole step replays as one graph launch: no host
+// round trip, no per-kernel launch cost, which is what many small systems
+// in one context need.  A captured build has no host-paced top phase
+// (every system is one subtree task) and fixed coordinate bounds; a
+// particle leaving them raises TSPH_ERR_BOUNDS and the next call recaptures.
+#include <math.h>
+#include <string.h>
+
+#include "tsph_ctx.cuh"
+
+__global__ void k_coord_maxabs(int n, TsphDevState C, unsigned long long *out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double a = 0.0;
+    if (i < n) a = fmax(fabs(C.x[i]), fmax(fabs(C.y[i]), fabs(C.z[i])));
+    warp_max_abs(a, out);
+}
+
+static int step_body(tsph_ctx *ctx, double dt, const tsph_grav_params *gp,
+                     const tsph_sph_params *sp) {
+    int rc = tsph_kick(ctx, 0.5 * dt);
+    if (!rc) rc = tsph_drift(ctx, dt, gp->bPeriodic, gp->dPeriod);
+    if (!rc) rc = tsph_grav_all(ctx, gp, nullptr);
+    if (!rc && sp && ctx->ngas > 0) {
+        rc = tsph_smooth(ctx, TSPH_SMX_DENDVDX, sp, nullptr);
+        if (!rc) rc = tsph_smooth(ctx, TSPH_SMX_SPHPRESSURETERMS, sp, nullptr);
+    }
+    if (!rc) rc = tsph_kick(ctx, 0.5 * dt);
+    return rc;
+}
+
+static void drop_graph(tsph_ctx *ctx) {
+    if (ctx->graphExec) cudaGraphExecDestroy(ctx->graphExec);
+    ctx->graphExec = nullptr;
+}
+
+static bool graph_matches(const tsph_ctx *ctx, double dt, const tsph_grav_params *gp,
+                          const tsph_sph_params *sp) {
+    if (!ctx->graphExec || ctx->graphDt != dt || ctx->graphN != ctx->n ||
+        ctx->graphNgas != ctx->ngas || ctx->graphSysVersion != ctx->sysVersion)
+        return false;
+    if (memcmp(&ctx->graphGrav, gp, sizeof(*gp)) != 0) return false;
+    if ((sp != nullptr) != (ctx->graphHasSph != 0)) return false;
+    return !sp || memcmp(&ctx->graphSph, sp, sizeof(*sp)) == 0;
+}
+
+// Record the step: forces are first evaluated once on the current state
+// (allocating everything, uploading constants; the same accelerations the
+// previous step left, as the evaluation is deterministic), then the step
+// is captured with the coordinate bound fixed at twice the current extent.
+static int capture_step(tsph_ctx *ctx, double dt, const tsph_grav_params *gp,
+                        const tsph_sph_params *sp) {
+    drop_graph(ctx);
+    const int n = ctx->n;
+    TSPH_CK(cudaMemsetAsync(ctx->dAux + 1, 0, sizeof(unsigned long long), ctx->stream));
+    k_coord_maxabs<<<tsph_blocks(n, 256), 256, 0, ctx->stream>>>(n, ctx->C, ctx->dAux + 1);
+    TSPH_LAUNCH_CK("k_coord_maxabs");
+    unsigned long long bits = 0;
+    TSPH_CK(cudaMemcpyAsync(&bits, ctx->dAux + 1, sizeof(bits), cudaMemcpyDeviceToHost, ctx->stream));
+    TSPH_CK(cudaStreamSynchronize(ctx->stream));
+    double ext;
+    memcpy(&ext, &bits, sizeof(ext));
+    ctx->capLimit = 2.0 * ext + 1e-300;
+    int rc = tsph_grav_all(ctx, gp, nullptr);
+    if (!rc && sp && ctx->ngas > 0) {
+        rc = tsph_smooth(ctx, TSPH_SMX_DENDVDX, sp, nullptr);
+        if (!rc) rc = tsph_smooth(ctx, TSPH_SMX_SPHPRESSURETERMS, sp, nullptr);
+    }
+    if (rc) { ctx->capLimit = 0; return rc; }
+    TSPH_CK(cudaStreamSynchronize(ctx->stream));
+    cudaGraph_t graph = nullptr;
+    TSPH_CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    ctx->capturing = true;
+    const long long before = ctx->launches;
+    rc = step_body(ctx, dt, gp, sp);
+    ctx->graphKernels = ctx->launches - before;
+    ctx->launches = before;
+    ctx->capturing = false;
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
+    if (!rc && e != cudaSuccess) rc = tsph_cuda_fail(ctx, e, "cudaStreamEndCapture");
+    if (!rc) {
+        e = cudaGraphInstantiate(&ctx->graphExec, graph, 0);
+        if (e != cudaSuccess) rc = tsph_cuda_fail(ctx, e, "cudaGraphInstantiate");
+    }
+    if (graph) cudaGraphDestroy(graph);
+    ctx->capLimit = 0;   // the graph keeps its own copy; direct calls measure afresh
+    if (rc) {
+        drop_graph(ctx);
+        cudaGetLastError();
+        return rc;
+    }
+    ctx->graphDt = dt;
+    ctx->graphN = n;
+    ctx->graphNgas = ctx->ngas;
+    ctx->graphSysVersion = ctx->sysVersion;
+    ctx->graphGrav = *gp;
+    ctx->graphHasSph = sp != nullptr;
+    if (sp) ctx->graphSph = *sp;
+    return TSPH_OK;
+}
+
+extern "C" int tsph_step(tsph_ctx *ctx, double dt, const tsph_grav_params *gp,
+                         const tsph_sph_params *sp, int flags) {
+    if (!ctx || !gp || !(dt >= 0)) return TSPH_ERR_ARG;
+    if (!ctx->haveParts || !ctx->haveVel) return TSPH_ERR_STATE;
+    cudaSetDevice(ctx->device);
+    if (!(flags & TSPH_STEP_GRAPH)) return step_body(ctx, dt, gp, sp);
+    if (gp->bPeriodic || (sp && sp->bLearnedH)) return TSPH_ERR_UNSUPPORTED;
+    if (ctx->T.maxRange > TSPH_STEP_GRAPH_MAX_SYSTEM || ctx->TG.maxRange > TSPH_STEP_GRAPH_MAX_SYSTEM)
+        return TSPH_ERR_UNSUPPORTED;
+    if (ctx->n == 0) return TSPH_OK;
+    if (!graph_matches(ctx, dt, gp, sp)) {
+        int rc = capture_step(ctx, dt, gp, sp);
+        if (rc) return rc;
+    }
+    TSPH_CK(cudaGraphLaunch(ctx->graphExec, ctx->stream));
+    ctx->launches += ctx->graphKernels;   // kernels the replay runs
+    return TSPH_OK;
+}
+
+extern "C" int tsph_step_status(tsph_ctx *ctx) {
+    if (!ctx) return TSPH_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    unsigned int st = 0;
+    TSPH_CK(cudaMemcpyAsync(&st, ctx->dStepStatus, sizeof(st), cudaMemcpyDeviceToHost, ctx->stream));
+    TSPH_CK(cudaMemsetAsync(ctx->dStepStatus, 0, sizeof(st), ctx->stream));
+    TSPH_CK(cudaStreamSynchronize(ctx->stream));
+    for (int k = 1; k < 32; ++k)
+        if (st & (1u << k)) {
+            if (k == TSPH_ERR_BOUNDS) drop_graph(ctx);   // recapture on the next step
+            return k;
+        }
+    return TSPH_OK;
+}

@@ -166,41 +166,73 @@ __global__ void k_seg_init(int n, int *seg, const int *__restrict__ rid, const i
     seg[p] = (rHi[r] - rLo[r] + 1 > S) ? r : -1;
 }
 
-// Segmented min/max of positions per frontier node.  Particles of one node
-// are contiguous, so runs inside a warp are reduced with shuffles and the
-// run head issues the atomics.
-__global__ void k_bounds(const double *__restrict__ x, const double *__restrict__ y,
-                         const double *__restrict__ z, const int *__restrict__ seg, double *t_bnd,
-                         int n) {
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    int lane = threadIdx.x & 31;
-    int s = (p < n) ? seg[p] : -1;
-    unsigned long long mn[3], mx[3];
-    if (s >= 0) {
-        mn[0] = mx[0] = dkey(x[p]);
-        mn[1] = mx[1] = dkey(y[p]);
-        mn[2] = mx[2] = dkey(z[p]);
-    } else {
-        mn[0] = mn[1] = mn[2] = ~0ULL;
-        mx[0] = mx[1] = mx[2] = 0ULL;
+// Top-phase bounds over fixed chunks of each frontier node's particle range:
+// a block reduces one chunk of one node and issues one set of atomics, so
+// a node of N particles costs N / TB_CHUNK atomics instead of one per warp.
+#define TB_CHUNK 4096
+#define TB_BS 256
+__global__ void k_chunk_count(int F, const int *__restrict__ f_node, const int *__restrict__ t_lo,
+                              const int *__restrict__ t_hi, int *cc) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= F) return;
+    int v = f_node[k];
+    cc[k] = (t_hi[v] - t_lo[v] + TB_CHUNK) / TB_CHUNK;
+}
+
+__device__ __forceinline__ unsigned long long umin64(unsigned long long a, unsigned long long b) {
+    return a < b ? a : b;
+}
+__device__ __forceinline__ unsigned long long umax64(unsigned long long a, unsigned long long b) {
+    return a > b ? a : b;
+}
+
+__global__ void __launch_bounds__(TB_BS) k_bounds_chunks(int F, const int *__restrict__ f_node,
+                                                         const int *__restrict__ cs,
+                                                         const int *__restrict__ t_lo,
+                                                         const int *__restrict__ t_hi,
+                                                         const double *__restrict__ x,
+                                                         const double *__restrict__ y,
+                                                         const double *__restrict__ z, double *t_bnd) {
+    __shared__ unsigned long long red[TB_BS / 32][6];
+    const int b = blockIdx.x;
+    if (b >= cs[F - 1]) return;
+    int a = 0, e = F - 1;                  // first k with cs[k] > b
+    while (a < e) {
+        int c = (a + e) >> 1;
+        if (cs[c] > b) e = c; else a = c + 1;
+    }
+    const int v = f_node[a];
+    const int j = b - (a > 0 ? cs[a - 1] : 0);
+    const int p0 = t_lo[v] + j * TB_CHUNK;
+    const int p1 = min(p0 + TB_CHUNK, t_hi[v] + 1);
+    unsigned long long mn[3] = {~0ULL, ~0ULL, ~0ULL}, mx[3] = {0ULL, 0ULL, 0ULL};
+    for (int p = p0 + threadIdx.x; p < p1; p += TB_BS) {
+        unsigned long long kx = dkey(x[p]), ky = dkey(y[p]), kz = dkey(z[p]);
+        mn[0] = umin64(mn[0], kx); mx[0] = umax64(mx[0], kx);
+        mn[1] = umin64(mn[1], ky); mx[1] = umax64(mx[1], ky);
+        mn[2] = umin64(mn[2], kz); mx[2] = umax64(mx[2], kz);
     }
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        int so = __shfl_down_sync(0xffffffffu, s, o);
-        bool same = (lane + o < 32) && (so == s);
+    for (int o = 16; o > 0; o >>= 1) {
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            unsigned long long a = __shfl_down_sync(0xffffffffu, mn[k], o);
-            unsigned long long b = __shfl_down_sync(0xffffffffu, mx[k], o);
-            if (same) {
-                mn[k] = a < mn[k] ? a : mn[k];
-                mx[k] = b > mx[k] ? b : mx[k];
-            }
+        for (int d = 0; d < 3; ++d) {
+            mn[d] = umin64(mn[d], __shfl_xor_sync(0xffffffffu, mn[d], o));
+            mx[d] = umax64(mx[d], __shfl_xor_sync(0xffffffffu, mx[d], o));
         }
     }
-    int sp = __shfl_up_sync(0xffffffffu, s, 1);
-    bool head = (lane == 0) || (sp != s);
-    if (s >= 0 && head) key_atomics(t_bnd, s, mn, mx);
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) { red[w][d] = mn[d]; red[w][3 + d] = mx[d]; }
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        const int d = threadIdx.x;
+        unsigned long long r = red[0][d];
+        for (int k = 1; k < TB_BS / 32; ++k) r = d < 3 ? umin64(r, red[k][d]) : umax64(r, red[k][d]);
+        unsigned long long *key = reinterpret_cast<unsigned long long *>(t_bnd + 6 * v);
+        if (d < 3) atomicMin(&key[d], r); else atomicMax(&key[d], r);
+    }
 }
 
 // Bounds keys -> doubles, and the split decision of a node
@@ -399,10 +431,22 @@ __device__ __forceinline__ int st_warp_offset(int wtot, int *ws, int &total) {
     return off;
 }
 
+// Particle arrays a task works on: the global arrays, or (for a task of at
+// most ST_SCAP particles) shared-memory copies of the positions plus the
+// permutation, written back once the subtree is done.  Pointers are offset
+// so that both are indexed by the global particle index.
+struct TaskView {
+    double *x, *y, *z;
+    int *seg, *scan;
+    int *lt;              // flags (global path only; the staged path re-derives them)
+    short *perm;          // staged path: original local index of each slot
+    bool staged;
+};
+
 // Bounds of every node of the current level: each warp reduces a
 // contiguous chunk of the task's particles, carrying the open run of one
 // node from step to step so a node costs about one atomic per warp.
-__device__ void st_bounds(const BuildArgs &A, int lo, int hi) {
+__device__ void st_bounds(const BuildArgs &A, const TaskView &V, int lo, int hi) {
     const unsigned FULL = 0xffffffffu;
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int m = hi - lo + 1;
@@ -413,12 +457,12 @@ __device__ void st_bounds(const BuildArgs &A, int lo, int hi) {
     unsigned long long cmn[3] = {~0ULL, ~0ULL, ~0ULL}, cmx[3] = {0ULL, 0ULL, 0ULL};
     for (int base = b0; base < b1; base += 32) {
         int p = base + lane;
-        int s = p < b1 ? A.seg[p] : -1;
+        int s = p < b1 ? V.seg[p] : -1;
         unsigned long long mn[3], mx[3];
         if (s >= 0) {
-            mn[0] = mx[0] = dkey(A.x[p]);
-            mn[1] = mx[1] = dkey(A.y[p]);
-            mn[2] = mx[2] = dkey(A.z[p]);
+            mn[0] = mx[0] = dkey(V.x[p]);
+            mn[1] = mx[1] = dkey(V.y[p]);
+            mn[2] = mx[2] = dkey(V.z[p]);
             if (lane == 0 && s == cs) {
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
@@ -466,12 +510,30 @@ __device__ void st_bounds(const BuildArgs &A, int lo, int hi) {
     if (cs >= 0 && lane == 0) key_atomics(A.t_bnd, cs, cmn, cmx);
 }
 
+__device__ __forceinline__ int st_flag(const BuildArgs &A, const TaskView &V, int p) {
+    int s = V.seg[p];
+    if (s < 0) return 0;
+    int d = A.t_dim[s];
+    if (d < 0) return 0;
+    double r = d == 0 ? V.x[p] : (d == 1 ? V.y[p] : V.z[p]);
+    return r < A.t_split[s] ? 1 : 0;
+}
+
+#define ST_SCAP 3072      // largest task staged in shared memory
+#define ST_SMEM (ST_SCAP * (3 * sizeof(double) + 2 * sizeof(int) + sizeof(short)))
+
 __global__ void __launch_bounds__(ST_BS) k_subtree(BuildArgs A) {
+    extern __shared__ __align__(16) unsigned char stsm[];
     __shared__ int ws[ST_W];
     __shared__ int lvStart[ST_MAXLEV], lvCnt[ST_MAXLEV];
     __shared__ int sTask;
     const unsigned FULL = 0xffffffffu;
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double *sx = reinterpret_cast<double *>(stsm);
+    double *sy = sx + ST_SCAP, *sz = sy + ST_SCAP;
+    int *sseg = reinterpret_cast<int *>(sz + ST_SCAP);
+    int *sscan = sseg + ST_SCAP;
+    short *sperm = reinterpret_cast<short *>(sscan + ST_SCAP);
     for (;;) {
         if (threadIdx.x == 0) {
             int t = atomicAdd(&A.ctl->taskNext, 1);
@@ -485,7 +547,22 @@ __global__ void __launch_bounds__(ST_BS) k_subtree(BuildArgs A) {
         const int slot0 = A.topCap + 2 * lo, slotEnd = slot0 + 2 * m;
         const int C = ((m + ST_BS - 1) / ST_BS) * 32;
         const int b0 = lo + w * C, b1 = min(b0 + C, hi + 1);
-        for (int p = lo + threadIdx.x; p <= hi; p += ST_BS) A.seg[p] = root;
+        TaskView V;
+        V.staged = m <= ST_SCAP;
+        if (V.staged) {
+            V.x = sx - lo; V.y = sy - lo; V.z = sz - lo;
+            V.seg = sseg - lo; V.scan = sscan - lo; V.lt = nullptr; V.perm = sperm - lo;
+            for (int p = lo + threadIdx.x; p <= hi; p += ST_BS) {
+                V.x[p] = A.x[p];
+                V.y[p] = A.y[p];
+                V.z[p] = A.z[p];
+                V.perm[p] = (short)(p - lo);
+            }
+        } else {
+            V.x = A.x; V.y = A.y; V.z = A.z;
+            V.seg = A.seg; V.scan = A.scan; V.lt = A.lt; V.perm = nullptr;
+        }
+        for (int p = lo + threadIdx.x; p <= hi; p += ST_BS) V.seg[p] = root;
         if (threadIdx.x == 0) {
             key_init(A.t_bnd, root);
             lvStart[0] = root;
@@ -497,7 +574,7 @@ __global__ void __launch_bounds__(ST_BS) k_subtree(BuildArgs A) {
         for (;;) {
             const int start = lvStart[L], cnt = lvCnt[L];
             // 1. bounds of this level's nodes
-            st_bounds(A, lo, hi);
+            st_bounds(A, V, lo, hi);
             __syncthreads();
             // 2. split decisions
             for (int k = threadIdx.x; k < cnt; k += ST_BS)
@@ -508,42 +585,42 @@ __global__ void __launch_bounds__(ST_BS) k_subtree(BuildArgs A) {
             int wtot = 0;
             for (int base = b0; base < b1; base += 32) {
                 int p = base + lane;
-                int f = 0;
-                if (p < b1) {
-                    int s = A.seg[p];
-                    if (s >= 0) {
-                        int d = A.t_dim[s];
-                        if (d >= 0) {
-                            double r = d == 0 ? A.x[p] : (d == 1 ? A.y[p] : A.z[p]);
-                            f = r < A.t_split[s] ? 1 : 0;
-                        }
-                    }
-                    A.lt[p] = f;
-                }
+                int f = p < b1 ? st_flag(A, V, p) : 0;
+                if (!V.staged && p < b1) V.lt[p] = f;
                 wtot += __popc(__ballot_sync(FULL, f));
             }
             int tot;
             int run = st_warp_offset(wtot, ws, tot);
             for (int base = b0; base < b1; base += 32) {
                 int p = base + lane;
-                int f = p < b1 ? A.lt[p] : 0;
+                int f = p < b1 ? (V.staged ? st_flag(A, V, p) : V.lt[p]) : 0;
                 unsigned bal = __ballot_sync(FULL, f);
-                if (p < b1) A.scan[p] = run + __popc(bal & (lanemask_lt_b() | (1u << lane)));
+                if (p < b1) V.scan[p] = run + __popc(bal & (lanemask_lt_b() | (1u << lane)));
                 run += __popc(bal);
             }
             __syncthreads();
             // 4. Hoare-partition swaps (scan is task-local: S(lo - 1) = 0)
             for (int p = lo + threadIdx.x; p <= hi; p += ST_BS) {
-                int s = A.seg[p];
-                if (s < 0 || A.t_dim[s] < 0 || A.lt[p]) continue;
+                int s = V.seg[p];
+                if (s < 0 || A.t_dim[s] < 0) continue;
+                const int Sp1 = p > lo ? V.scan[p - 1] : 0;
+                if (V.scan[p] - Sp1) continue;            // r < fSplit: stays
                 int vlo = A.t_lo[s], vhi = A.t_hi[s];
-                int Slo = vlo > lo ? A.scan[vlo - 1] : 0;
-                int Shi = A.scan[vhi];
+                int Slo = vlo > lo ? V.scan[vlo - 1] : 0;
+                int Shi = V.scan[vhi];
                 int mid = vlo + (Shi - Slo);
                 if (p >= mid) continue;
-                int t = (p - vlo) - ((p > lo ? A.scan[p - 1] : 0) - Slo);
-                int q = lower_bound_scan(A.scan, mid, vhi, Shi - t);
-                swap_particles(A.x, A.y, A.z, A.m, A.h, A.iord, p, q);
+                int t = (p - vlo) - (Sp1 - Slo);
+                int q = lower_bound_scan(V.scan, mid, vhi, Shi - t);
+                if (V.staged) {
+                    double t0;
+                    t0 = V.x[p]; V.x[p] = V.x[q]; V.x[q] = t0;
+                    t0 = V.y[p]; V.y[p] = V.y[q]; V.y[q] = t0;
+                    t0 = V.z[p]; V.z[p] = V.z[q]; V.z[q] = t0;
+                    short ti = V.perm[p]; V.perm[p] = V.perm[q]; V.perm[q] = ti;
+                } else {
+                    swap_particles(A.x, A.y, A.z, A.m, A.h, A.iord, p, q);
+                }
             }
             __syncthreads();
             // 5. children of the split nodes, numbered by split rank
@@ -569,8 +646,8 @@ __global__ void __launch_bounds__(ST_BS) k_subtree(BuildArgs A) {
                         atomicOr(&A.ctl->status, 1 << TSPH_ERR_ARG);
                     } else {
                         int vlo = A.t_lo[v], vhi = A.t_hi[v];
-                        int Slo = vlo > lo ? A.scan[vlo - 1] : 0;
-                        int mid = vlo + (A.scan[vhi] - Slo);
+                        int Slo = vlo > lo ? V.scan[vlo - 1] : 0;
+                        int mid = vlo + (V.scan[vhi] - Slo);
                         A.t_child[v] = c;
                         A.t_lo[c] = vlo;
                         A.t_hi[c] = mid - 1;
@@ -587,13 +664,13 @@ __global__ void __launch_bounds__(ST_BS) k_subtree(BuildArgs A) {
             __syncthreads();
             // 6. particles follow their node into a child, or finish in a leaf
             for (int p = lo + threadIdx.x; p <= hi; p += ST_BS) {
-                int s = A.seg[p];
+                int s = V.seg[p];
                 if (s < 0) continue;
                 if (A.t_dim[s] >= 0) {
                     int c = A.t_child[s];
-                    A.seg[p] = p < A.t_lo[c + 1] ? c : c + 1;
+                    V.seg[p] = p < A.t_lo[c + 1] ? c : c + 1;
                 } else {
-                    A.seg[p] = -1;
+                    V.seg[p] = -1;
                 }
             }
             if (nsplit == 0) break;
@@ -610,6 +687,31 @@ __global__ void __launch_bounds__(ST_BS) k_subtree(BuildArgs A) {
             ++L;
         }
         __syncthreads();
+        if (V.staged) {
+            // the final order back to the global arrays: positions first,
+            // then mass, softening and caller index gathered through the
+            // freed shared memory
+            for (int p = lo + threadIdx.x; p <= hi; p += ST_BS) {
+                A.x[p] = V.x[p];
+                A.y[p] = V.y[p];
+                A.z[p] = V.z[p];
+            }
+            __syncthreads();
+            double *gm = sx - lo, *gh = sy - lo;
+            int *gi = reinterpret_cast<int *>(sz) - lo;
+            for (int p = lo + threadIdx.x; p <= hi; p += ST_BS) {
+                int src = lo + V.perm[p];
+                gm[p] = A.m[src];
+                gh[p] = A.h[src];
+                gi[p] = A.iord[src];
+            }
+            __syncthreads();
+            for (int p = lo + threadIdx.x; p <= hi; p += ST_BS) {
+                A.m[p] = gm[p];
+                A.h[p] = gh[p];
+                A.iord[p] = gi[p];
+            }
+        }
         if (!failed) {
             // subtree sizes bottom-up, then depth-first offsets from the root
             for (int l = L; l >= 0; --l) {
@@ -964,6 +1066,8 @@ void tsph_free_build(TsphBuildBufs &B) {
 static int ensure_nodes(tsph_ctx *ctx, TsphDevTree &T, int nNodes) {
     TsphBuildBufs &B = ctx->B;
     int rc = 0;
+    if (ctx->capturing && (nNodes > T.cap || !T.pLower || B.nodeScratchCap < nNodes))
+        return TSPH_ERR_STATE;   // no allocation inside a capture
     if (nNodes > T.cap || !T.pLower) {
         int cap = nNodes + 64;
         rc |= tsph_grow(ctx, &T.pLower, cap);
@@ -1009,6 +1113,7 @@ static int ensure_temp(tsph_ctx *ctx, int n, int nR) {
     int topCap = nR + 2 * (n / 1024 + 1) * TSPH_MAX_LEVELS + 512;
     int tcap = topCap + 2 * n;
     if (B.ctl && topCap <= B.topCap && tcap <= B.tcap) return TSPH_OK;
+    if (ctx->capturing) return TSPH_ERR_STATE;   // no allocation inside a capture
     topCap += topCap / 8;
     tcap = topCap + 2 * (n + n / 8 + 64);
     int rc = 0;
@@ -1078,10 +1183,12 @@ int tsph_set_ranges(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, int n
 }
 
 // Task size: the largest node handed whole to one CTA.
-static int task_size(tsph_ctx *ctx, int n) {
-    int S = ctx->taskSize > 0 ? ctx->taskSize : n / (ctx->smCount * 2);
+static int task_size(tsph_ctx *ctx, const TsphDevTree &T) {
+    int S = ctx->taskSize > 0 ? ctx->taskSize : ST_SCAP;
     if (S < 1024) S = 1024;
-    if (S > 65536) S = 65536;
+    // a captured build cannot run the host-paced top phase: every tree is
+    // one task
+    if (ctx->capturing && S < T.maxRange) S = T.maxRange;
     return S;
 }
 
@@ -1110,7 +1217,7 @@ int tsph_build_tree(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, int n
     const int nodeNeed = 2 * n;
     rc = ensure_nodes(ctx, T, nodeNeed);
     if (rc) return rc;
-    const int S = task_size(ctx, n);
+    const int S = task_size(ctx, T);
     int F = 0;
     for (int r = 0; r < nR; ++r)
         if (T.hHi[r] - T.hLo[r] + 1 > S) ++F;
@@ -1129,8 +1236,14 @@ int tsph_build_tree(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, int n
     }
     while (F > 0) {
         if (level + 1 >= TSPH_MAX_LEVELS) return TSPH_ERR_TREE_DEPTH;
-        k_bounds<<<tsph_blocks(n, BS), BS, 0, ctx->stream>>>(P.x, P.y, P.z, B.seg, B.t_bnd, n);
-        TSPH_LAUNCH_CK("k_bounds");
+        k_chunk_count<<<tsph_blocks(F, BS), BS, 0, ctx->stream>>>(F, B.f_node[cur], B.t_lo, B.t_hi,
+                                                                   B.f_split);
+        TSPH_LAUNCH_CK("k_chunk_count");
+        rc = tsph_scan_inclusive(ctx, B.f_split, B.f_rank, F);
+        if (rc) return rc;
+        k_bounds_chunks<<<n / TB_CHUNK + F + 1, TB_BS, 0, ctx->stream>>>(
+            F, B.f_node[cur], B.f_rank, B.t_lo, B.t_hi, P.x, P.y, P.z, B.t_bnd);
+        TSPH_LAUNCH_CK("k_bounds_chunks");
         k_top_split<<<tsph_blocks(F, BS), BS, 0, ctx->stream>>>(
             F, B.f_node[cur], S, nBucket, B.t_lo, B.t_hi, B.t_dim, B.t_child, B.t_size, B.t_split,
             B.t_bnd, B.f_split, B.tasks, B.ctl);
@@ -1175,11 +1288,14 @@ int tsph_build_tree(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, int n
     A.tasks = B.tasks; A.ctl = B.ctl;
     A.topCap = B.topCap; A.nBucket = nBucket;
     if (ctx->subtreeBlocks == 0) {
+        if (ctx->capturing) return TSPH_ERR_STATE;
+        TSPH_CK(cudaFuncSetAttribute(k_subtree, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)ST_SMEM));
         int per = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_subtree, ST_BS, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_subtree, ST_BS, ST_SMEM);
         ctx->subtreeBlocks = (per > 0 ? per : 1) * ctx->smCount;
     }
-    k_subtree<<<ctx->subtreeBlocks, ST_BS, 0, ctx->stream>>>(A);
+    k_subtree<<<ctx->subtreeBlocks, ST_BS, ST_SMEM, ctx->stream>>>(A);
     TSPH_LAUNCH_CK("k_subtree");
     // numbering
     for (int l = topLevels - 1; l >= 0; --l) {

@@ -115,10 +115,28 @@ struct tsph_ctx {
 
     TsphHnet hnet;
 
+    unsigned long long *dAux;    // device scratch: [0] gas max |coordinate| bits
+    double gasScale;             // last measured gas max |coordinate|
+    // systems (forest): caller-order system id of every particle
+    int nSys;
+    int *hSys;
+
     // tree build tuning and mode
     int taskSize;                // largest node one CTA builds whole (0 = automatic)
     int subtreeBlocks;           // resident CTAs of the subtree kernel
+    int walkBlocksPerSM;         // resident walk blocks per SM (0 = default)
     bool capturing;              // inside a CUDA graph capture: no host reads
+    double capLimit;             // |coordinate| bound of the captured step (0 = none)
+    unsigned int *dStepStatus;   // device: status bits accumulated over a step
+    // captured kick-drift-kick step (tsph_step)
+    cudaGraphExec_t graphExec;
+    tsph_grav_params graphGrav;
+    tsph_sph_params graphSph;
+    double graphDt;
+    int graphN, graphNgas, graphHasSph;
+    long long graphKernels;      // kernel launches recorded in the graph
+    long long graphSysVersion;
+    long long sysVersion;        // bumped by every particle / system change
 
     cudaEvent_t ev[10];
     float timings[8];
@@ -158,6 +176,8 @@ int tsph_build_tree(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, int n
 int tsph_set_ranges(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, int nR, const int *counts);
 int tsph_tree_moments(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, double dTheta);
 void tsph_free_build(TsphBuildBufs &B);
+int tsph_apply_gas_systems(tsph_ctx *ctx);
+int tsph_fold_status(tsph_ctx *ctx);
 int tsph_copy_out(tsph_ctx *ctx, const double *a0, const double *a1, const double *a2, int comp,
                   double *host);
 int tsph_copy_out_n(tsph_ctx *ctx, int n, const double *a0, const double *a1, const double *a2,

@@ -32,6 +32,16 @@ __device__ __forceinline__ double dunkey(unsigned long long k) {
     return __longlong_as_double((long long)b);
 }
 
+// Largest |x|, |y|, |z| over n particles, as the bits of a non-negative
+// double (which order like the values) max-reduced into *out.
+__device__ __forceinline__ void warp_max_abs(double a, unsigned long long *out) {
+    unsigned long long key = (unsigned long long)__double_as_longlong(a);
+    unsigned hiw = (unsigned)(key >> 32), low = (unsigned)key;
+    unsigned mh = __reduce_max_sync(0xffffffffu, hiw);
+    unsigned ml = __reduce_max_sync(0xffffffffu, hiw == mh ? low : 0u);
+    if ((threadIdx.x & 31) == 0) atomicMax(out, ((unsigned long long)mh << 32) | ml);
+}
+
 // Split a double into float hi + float lo with hi + lo == x to ~2^-48.
 __host__ __device__ __forceinline__ void split2f(double x, float &hi, float &lo) {
     hi = (float)x;
@@ -112,6 +122,7 @@ struct TsphDevCounters {
     unsigned long long nEwLoop;      // Ewald real-space terms evaluated
     unsigned long long nExactTests;  // opening tests settled in FP64
     unsigned long long nTests;       // opening tests in total
+    unsigned long long maxAbs;       // bits of max |coordinate| (non-negative double)
     unsigned int status;             // TSPH_ERR_* raised on device
     unsigned int pad;
 };

@@ -146,3 +146,37 @@ def batched_systems(nsys=512, seed=5, nmin=1024, nmax=65536, gas_frac=0.2):
         systems.append(dict(pos=pos, vel=vel, mass=m, soft=np.full(n, 0.01),
                             ngas=ngas, a=1.0))
     return systems
+
+
+def pack_systems(systems, u0=0.05):
+    """Concatenate independent systems into one particle set for
+    Context.set_systems: the gas particles of all systems first (the
+    library's convention: gas = the first ngas particles), then the rest.
+    Returns (pos, vel, mass, soft, ngas, u, sys_of, index) where index[s] is
+    the array of global indices of system s's particles in its own order."""
+    gas_idx, dm_idx = [], []
+    off = 0
+    for s, d in enumerate(systems):
+        n = len(d["mass"])
+        g = d["ngas"]
+        gas_idx.append((s, np.arange(off, off + g)))
+        dm_idx.append((s, np.arange(off + g, off + n)))
+        off += n
+    order = np.concatenate([a for _, a in gas_idx] + [a for _, a in dm_idx])
+    sys_cat = np.concatenate([np.full(len(a), s, dtype=np.int32) for s, a in gas_idx] +
+                             [np.full(len(a), s, dtype=np.int32) for s, a in dm_idx])
+    pos = np.concatenate([d["pos"] for d in systems])[order]
+    vel = np.concatenate([d["vel"] for d in systems])[order]
+    mass = np.concatenate([d["mass"] for d in systems])[order]
+    soft = np.concatenate([d["soft"] for d in systems])[order]
+    ngas = int(sum(d["ngas"] for d in systems))
+    u = np.full(ngas, u0)
+    inv = np.empty(len(order), dtype=np.int64)
+    inv[order] = np.arange(len(order))
+    index = []
+    off = 0
+    for d in systems:
+        n = len(d["mass"])
+        index.append(inv[off:off + n])
+        off += n
+    return pos, vel, mass, soft, ngas, u, sys_cat, index

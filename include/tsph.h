@@ -50,7 +50,9 @@ enum tsph_status {
     TSPH_ERR_UNSUPPORTED = 7,     /* smooth type or option not implemented */
     TSPH_ERR_STATE = 8,           /* call order (e.g. no particles loaded) */
     TSPH_ERR_TREE_DEPTH = 9,      /* tree deeper than the build's level cap */
-    TSPH_ERR_NOMEM = 10           /* device allocation failed */
+    TSPH_ERR_NOMEM = 10,          /* device allocation failed */
+    TSPH_ERR_BOUNDS = 11          /* a particle left the coordinate bound a
+                                     captured step graph was built for */
 };
 
 enum tsph_precision {
@@ -150,6 +152,18 @@ int tsph_set_particles(tsph_ctx *ctx, int n, const double *pos,
 int tsph_set_velocities(tsph_ctx *ctx, const double *vel, int ngas,
                         const double *u);
 
+/* Independent systems in one context (a forest of trees).  sysOf[i] in
+ * [0, nSys) is the system of caller particle i (call after
+ * tsph_set_particles, and after tsph_set_velocities when there is gas; a
+ * later tsph_set_velocities keeps the assignment, tsph_set_particles
+ * clears it).  Every system gets its own gravity tree and, for its gas,
+ * its own gas tree: forces and SPH neighbours never cross systems, and
+ * each system's tree, lists and forces equal those of that system loaded
+ * alone.  Non-periodic only (periodic calls return TSPH_ERR_UNSUPPORTED
+ * when nSys > 1).  This is the batched form of one pkdGravAll per system;
+ * the reference runs such systems as separate jobs. */
+int tsph_set_systems(tsph_ctx *ctx, int nSys, const int *sysOf);
+
 /* --- gravity (pkdGravAll) -------------------------------------------- */
 
 /* Build the gravity tree over the loaded particles and compute every
@@ -247,6 +261,40 @@ int tsph_kick(tsph_ctx *ctx, double dt);
 int tsph_drift(tsph_ctx *ctx, double dt, int bPeriodic, double dPeriod);
 /* Copy state to the host in caller order; NULL skips a field. */
 int tsph_get_state(tsph_ctx *ctx, double *pos, double *vel, double *u);
+
+/* --- tuning --------------------------------------------------------------
+ * Launch-shape knobs of the CUDA path.  None changes a result: the tree,
+ * the interaction lists and every force are identical for any setting
+ * (no reference counterpart; the reference's equivalents are compile-time
+ * constants and nBucket).  Zero selects the default. */
+typedef struct {
+    int taskSize;         /* largest tree node one CTA builds whole (>= 1024; default 3072) */
+    int walkBlocksPerSM;  /* resident blocks per SM of the walk (default 4) */
+    int reserved[6];
+} tsph_tuning;
+int tsph_set_tuning(tsph_ctx *ctx, const tsph_tuning *t);
+int tsph_get_tuning(tsph_ctx *ctx, tsph_tuning *t);
+
+/* --- whole steps ----------------------------------------------------------
+ * One kick-drift-kick step of the single-rung msrTopStepKDK
+ * (master.c:8242-8465): kick dt/2, drift dt, gravity (+ for gas the density
+ * pass, gas pressure and the pressure pass), kick dt/2.  sp may be NULL
+ * (gravity only).  Returns when the work is queued on the context stream.
+ * With TSPH_STEP_GRAPH the step's launches are captured once into a CUDA
+ * graph (recaptured when dt, the parameters or the particle set change)
+ * and each call replays it with one launch; graph mode takes isolated
+ * (non-periodic) systems of at most TSPH_STEP_GRAPH_MAX_SYSTEM particles,
+ * no learned h.  No reference counterpart for the graph: the reference
+ * drives the same sequence from its host loop.
+ * tsph_step_status waits for the queued steps and returns the first error
+ * any of them raised (TSPH_OK if none); TSPH_ERR_BOUNDS means a particle
+ * moved beyond twice the extent the graph was captured for, and the next
+ * tsph_step recaptures. */
+#define TSPH_STEP_GRAPH 1
+#define TSPH_STEP_GRAPH_MAX_SYSTEM 65536
+int tsph_step(tsph_ctx *ctx, double dt, const tsph_grav_params *gp,
+              const tsph_sph_params *sp, int flags);
+int tsph_step_status(tsph_ctx *ctx);
 
 /* Timing of the last call's kernels on the context stream (ms), by phase:
  * t[0] tree build, t[1] moments, t[2] walk+interactions, t[3] Ewald,

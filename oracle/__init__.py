@@ -188,6 +188,17 @@ class exact_rsqrt:
         oracle().lib.orc_set_exact_rsqrt(0)
 
 
+def direct(pos, mass, soft, targets, nthreads=8):
+    """FP64 direct-sum accelerations and potentials of the particles
+    `targets` (indices) over all particles (orc_direct)."""
+    pos = _c64(pos, (-1, 3)); mass = _c64(mass); soft = _c64(soft)
+    q = np.ascontiguousarray(targets, dtype=np.int32)
+    acc = np.zeros((len(q), 3)); pot = np.zeros(len(q))
+    oracle().lib.orc_direct(len(mass), _d(pos), _d(mass), _d(soft), len(q),
+                            q.ctypes.data_as(_IP), _d(acc), _d(pot), nthreads)
+    return acc, pot
+
+
 def v_sqrt1(r2):
     r2 = _c64(r2)
     out = np.zeros_like(r2)

@@ -1717,3 +1717,38 @@ void orc_kdk(int n, int which, double dt, int bPeriodic, double dPeriod,
         }
     }
 }
+
+/* ------------------------------------------------------------------ */
+/* FP64 direct summation: the exact force the tree approximates       */
+/* ------------------------------------------------------------------ */
+/* For each target t = qidx[k]: a = -sum_j m_j b(r, h_t + h_j) (r_t - r_j),
+ * pot = -sum_j m_j a(r, h_t + h_j), j != t, with the reference's spline
+ * softening SPLINE (grav.h:74-101) as in the intra-bucket sum
+ * (grav.c:211-242).  Test infrastructure for the batched systems. */
+void orc_direct(int n, const double *pos, const double *mass, const double *soft, int nq,
+                const int *qidx, double *acc, double *pot, int nthreads) {
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 4)
+#endif
+    for (int k = 0; k < nq; ++k) {
+        int t = qidx[k];
+        double ax = 0, ay = 0, az = 0, p = 0;
+        for (int j = 0; j < n; ++j) {
+            if (j == t) continue;
+            double dx = pos[3 * t] - pos[3 * j], dy = pos[3 * t + 1] - pos[3 * j + 1],
+                   dz = pos[3 * t + 2] - pos[3 * j + 2];
+            double r2 = dx * dx + dy * dy + dz * dz;
+            double a, b;
+            spline(r2, soft[t] + soft[j], &a, &b);
+            p -= mass[j] * a;
+            ax -= mass[j] * b * dx;
+            ay -= mass[j] * b * dy;
+            az -= mass[j] * b * dz;
+        }
+        acc[3 * k] = ax;
+        acc[3 * k + 1] = ay;
+        acc[3 * k + 2] = az;
+        pot[k] = p;
+    }
+}

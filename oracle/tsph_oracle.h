@@ -83,6 +83,11 @@ void orc_set_exact_rsqrt(int on);
 /* v_sqrt1 restated (reference v_sqrt1.c:11-113). */
 void orc_v_sqrt1(int n, const double *r2, double *a);
 
+/* FP64 direct sum with the reference's SPLINE softening (grav.h:74-101)
+ * for the targets qidx[0..nq) over all n particles: acc[3 nq], pot[nq]. */
+void orc_direct(int n, const double *pos, const double *mass, const double *soft, int nq,
+                const int *qidx, double *acc, double *pot, int nthreads);
+
 #ifdef __cplusplus
 }
 #endif

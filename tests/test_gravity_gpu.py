@@ -170,6 +170,34 @@ def test_repeat_is_bit_identical(ctx):
     assert np.array_equal(a["pot"], b["pot"])
 
 
+def test_tuning_does_not_change_results():
+    """Every launch shape builds the same tree and the same forces: task
+    size 1024 (deep level-wise top phase), 3072 (shared-memory subtrees),
+    65536 (one CTA builds the whole tree from global memory), and 1 or 4
+    walk blocks per SM."""
+    pos, vel, m = g.ics.plummer(32768, seed=3)
+    soft = np.full(len(m), 0.01)
+    gp = g.grav_params(periodic=False, precision=g.FP32)
+    ref = None
+    c = g.Context(0)
+    try:
+        for task, wb in ((0, 0), (1024, 1), (65536, 4), (3072, 2)):
+            c.set_tuning(taskSize=task, walkBlocksPerSM=wb)
+            c.set_particles(pos, m, soft)
+            c.grav_all(gp)
+            r = c.get_gravity()
+            t = c.get_tree()
+            if ref is None:
+                ref = (r, t)
+                continue
+            for k in range(3):          # inode, dnode, perm
+                assert np.array_equal(t[k], ref[1][k]), (task, wb, k)
+            assert np.array_equal(r["acc"], ref[0]["acc"]), (task, wb)
+            assert np.array_equal(r["pot"], ref[0]["pot"]), (task, wb)
+    finally:
+        c.close()
+
+
 def test_second_call_on_tree_order(ctx):
     """A second grav_all on the already tree-ordered particles (the state the
     reference keeps between steps) gives the same forces."""
