@@ -95,6 +95,8 @@ extern "C" void tsph_destroy(tsph_ctx *ctx) {
     FREE(S.curl); FREE(S.dvds); FREE(S.bal); FREE(S.diff); FREE(S.pr2); FREE(S.cs); FREE(S.dtp);
     FREE(S.hax); FREE(S.hay); FREE(S.haz); FREE(S.uPdV); FREE(S.uAV); FREE(S.dtNew); FREE(S.mumax);
     FREE(S.seed); FREE(S.nnCount); FREE(S.nnHash); FREE(S.nodeBall2);
+    FREE(S.nbrList); FREE(S.rcnt); FREE(S.roff); FREE(S.rcur); FREE(S.rlist); FREE(S.listFlag);
+    FREE(S.ph); FREE(S.ih2); FREE(S.fn1); FREE(S.pr2f);
     FREE(ctx->dCnt); FREE(ctx->dBucketLists); FREE(ctx->dRoot); FREE(ctx->dEwt); FREE(ctx->dStage);
     FREE(ctx->dAux); FREE(ctx->dStepStatus);
     free(ctx->hSys);
@@ -135,6 +137,13 @@ int tsph_ensure_particles(tsph_ctx *ctx, int n) {
     rc |= tsph_grow(ctx, &S.nnCount, cap);
     rc |= tsph_grow(ctx, &S.nnHash, cap);
     rc |= tsph_grow(ctx, &S.nodeBall2, (size_t)2 * cap + 64);
+    S.nbrCap = TSPH_NBR_CAP;
+    rc |= tsph_grow(ctx, &S.nbrList, (size_t)S.nbrCap * cap);
+    rc |= tsph_grow(ctx, &S.rlist, (size_t)S.nbrCap * cap);
+    rc |= tsph_grow(ctx, &S.rcnt, cap); rc |= tsph_grow(ctx, &S.roff, cap);
+    rc |= tsph_grow(ctx, &S.rcur, cap); rc |= tsph_grow(ctx, &S.listFlag, 4);
+    rc |= tsph_grow(ctx, &S.ph, cap); rc |= tsph_grow(ctx, &S.ih2, cap);
+    rc |= tsph_grow(ctx, &S.fn1, cap); rc |= tsph_grow(ctx, &S.pr2f, cap);
     S.cap = cap;
     TsphBuildBufs &B = ctx->B;
     rc |= tsph_grow(ctx, &B.seg, cap); rc |= tsph_grow(ctx, &B.lt, cap); rc |= tsph_grow(ctx, &B.scan, cap);

@@ -185,9 +185,24 @@ __device__ int ball_gather(KnnSmem &W, const SphArgs &A, int lane, int root, dou
             double d2 = 0.0;
             int j = lk.x + k;
             if (k < cnt) {
-                double dx, dy, dz;
-                d2 = dist2_exact(xi, yi, zi, A.G.x[j], A.G.y[j], A.G.z[j], dx, dy, dz);
-                in = d2 <= r2;
+                const double xj = A.G.x[j], yj = A.G.y[j], zj = A.G.z[j];
+                // FP32 pre-reject: a lower bound of the distance (rounding
+                // margin off each axis) already beyond the radius
+                float ex = fmaxf(fabsf(xf - (float)xj) - cS.margin, 0.0f);
+                float ey = fmaxf(fabsf(yf - (float)yj) - cS.margin, 0.0f);
+                float ez = fmaxf(fabsf(zf - (float)zj) - cS.margin, 0.0f);
+                if (cS.bPeriodic) {
+                    const float Lf = (float)cS.L;
+                    ex = fminf(ex, fmaxf(Lf - ex - 2.0f * cS.margin, 0.0f));
+                    ey = fminf(ey, fmaxf(Lf - ey - 2.0f * cS.margin, 0.0f));
+                    ez = fminf(ez, fmaxf(Lf - ez - 2.0f * cS.margin, 0.0f));
+                }
+                float lb = (ex * ex + ey * ey + ez * ez) * (1.0f - 1e-6f);
+                if (lb <= r2f) {
+                    double dx, dy, dz;
+                    d2 = dist2_exact(xi, yi, zi, xj, yj, zj, dx, dy, dz);
+                    in = d2 <= r2;
+                }
             }
             unsigned bi = __ballot_sync(FULL, in);
             if (nc + __popc(bi) > SCAP) { bad = true; }
@@ -205,17 +220,37 @@ __device__ int ball_gather(KnnSmem &W, const SphArgs &A, int lane, int root, dou
     return bad ? -1 : nc;
 }
 
-// k-th smallest of the candidates' squared distances: an MSB-first search
-// on the bit patterns (non-negative doubles order like their bits).
+// k-th smallest of the candidates' squared distances, exactly: an
+// MSB-first radix select on the bit patterns (non-negative doubles order
+// like their bits), 4 bits per pass.  Each lane counts its candidates per
+// digit in 16-bit fields of four registers; the warp sums the fields.
 __device__ double select_kth(const KnnSmem &W, int nc, int k, int lane) {
     unsigned long long prefix = 0ULL;
-    for (int bit = 62; bit >= 0; --bit) {
-        unsigned long long cand = prefix | (1ULL << bit);
-        int c = 0;
-        for (int e = lane; e < nc; e += 32)
-            c += ((unsigned long long)__double_as_longlong(W.d2[e]) < cand) ? 1 : 0;
-        c = __reduce_add_sync(0xffffffffu, (unsigned)c);
-        if (c < k) prefix = cand;
+    int need = k;                       // rank still to find inside the prefix
+    for (int shift = 60; shift >= 0; shift -= 4) {
+        unsigned long long c[4] = {0ULL, 0ULL, 0ULL, 0ULL};
+        const unsigned long long hiMask = shift == 60 ? 0ULL : (~0ULL << (shift + 4));
+        for (int e = lane; e < nc; e += 32) {
+            unsigned long long key = (unsigned long long)__double_as_longlong(W.d2[e]);
+            if ((key & hiMask) != prefix) continue;
+            unsigned d = (unsigned)(key >> shift) & 15u;
+            unsigned long long inc = 1ULL << (16 * (d & 3u));
+            c[0] += (d >> 2) == 0 ? inc : 0ULL;
+            c[1] += (d >> 2) == 1 ? inc : 0ULL;
+            c[2] += (d >> 2) == 2 ? inc : 0ULL;
+            c[3] += (d >> 2) == 3 ? inc : 0ULL;
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) c[q] += __shfl_xor_sync(0xffffffffu, c[q], o);
+        int d = 0;
+        for (; d < 15; ++d) {
+            int cd = (int)((c[d >> 2] >> (16 * (d & 3))) & 0xffffULL);
+            if (need <= cd) break;
+            need -= cd;
+        }
+        prefix |= (unsigned long long)d << shift;
     }
     return __longlong_as_double((long long)prefix);
 }
@@ -256,6 +291,16 @@ __global__ void __launch_bounds__(SW * 32) k_knn_density(SphArgs A) {
                 r2 += d * d;
             }
             r2 = r2 * (1.0 + 1e-9) + 1e-300;
+            // the farthest-corner radius surely holds k particles but is loose;
+            // start instead from the node's mean density with twice the
+            // volume k particles need (a short ball grows, so the result is
+            // the same exact k-th distance either way)
+            const double vol = (b[3] - b[0]) * (b[4] - b[1]) * (b[5] - b[2]);
+            const int nNode = A.T.pUpper[node] - A.T.pLower[node] + 1;
+            if (vol > 0.0) {
+                double rd = cbrt(2.0 * 3.0 * k * vol / (4.0 * M_PI * nNode));
+                if (rd * rd < r2) r2 = rd * rd;
+            }
         }
         double lo2 = 0.0, hi2 = 0.0;   // radii known too small / too large
         int nc = -1, it = 0;
@@ -299,6 +344,12 @@ __global__ void __launch_bounds__(SW * 32) k_knn_density(SphArgs A) {
         __syncwarp();
         const bool sorted = nsel <= SNBR;
         if (sorted) warp_sort_idx(W.nbr, nsel, lane);
+        if (sorted && nsel <= A.S.nbrCap) {
+            int *dst = A.S.nbrList + (size_t)i * A.S.nbrCap;
+            for (int e = lane; e < nsel; e += 32) dst[e] = W.nbr[e];
+        } else if (lane == 0) {
+            A.S.listFlag[0] = 1;
+        }
         int nn = 0;
         unsigned long long hsh = 0ULL;
         const int nloop = sorted ? nsel : nc;
@@ -405,11 +456,64 @@ __global__ void k_gas_pressure(int ng, TsphSphBufs S) {
     double dtp = FLT_MAX;
     if (dt < dtp) dtp = dt;
     S.dtp[i] = dtp;
+    // the pair terms' per-particle factors (SphPressureTerms.h:1-40)
+    double fb = S.fBall2[i], rho = S.rho[i], d2 = rho * rho;
+    double ph = sqrt(0.25 * fb);
+    double ih2 = 4.0 / fb;
+    double fNorm = 0.5 * M_1_PI * ih2 / ph;
+    S.ph[i] = ph;
+    S.ih2[i] = ih2;
+    S.fn1[i] = fNorm * ih2;
+    S.pr2f[i] = (S.pr2[i] * d2 + 0) / d2;
+}
+
+// Reverse neighbour lists: count, fill, sort (ascending index).
+__global__ void k_rev_count(int ng, TsphSphBufs S) {
+    if (S.listFlag[0]) return;           // incomplete lists: not used
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int i = (int)(t / S.nbrCap), e = (int)(t % S.nbrCap);
+    if (i >= ng || e >= S.nnCount[i]) return;
+    atomicAdd(&S.rcnt[S.nbrList[(size_t)i * S.nbrCap + e]], 1);
+}
+
+__global__ void k_rev_fill(int ng, TsphSphBufs S) {
+    if (S.listFlag[0]) return;
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int i = (int)(t / S.nbrCap), e = (int)(t % S.nbrCap);
+    if (i >= ng || e >= S.nnCount[i]) return;
+    int j = S.nbrList[(size_t)i * S.nbrCap + e];
+    int slot = atomicAdd(&S.rcur[j], 1);
+    S.rlist[(j > 0 ? S.roff[j - 1] : 0) + slot] = i;
+}
+
+__global__ void __launch_bounds__(SW * 32) k_rev_sort(int ng, TsphSphBufs S, int *work) {
+    __shared__ int buf[SW][TSPH_RCAP];
+    const int lane = threadIdx.x & 31;
+    int *b = buf[threadIdx.x >> 5];
+    if (S.listFlag[0]) return;
+    for (;;) {
+        int j = 0;
+        if (lane == 0) j = atomicAdd(work, 1);
+        j = __shfl_sync(0xffffffffu, j, 0);
+        if (j >= ng) break;
+        const int o = j > 0 ? S.roff[j - 1] : 0, len = S.roff[j] - o;
+        if (len > TSPH_RCAP) {
+            if (lane == 0) S.listFlag[0] = 1;
+            continue;
+        }
+        for (int e = lane; e < len; e += 32) b[e] = S.rlist[o + e];
+        __syncwarp();
+        warp_sort_idx(b, len, lane);
+        for (int e = lane; e < len; e += 32) S.rlist[o + e] = b[e];
+        __syncwarp();
+    }
 }
 
 // per gas-tree node: max fBall2 of its particles (atomicMax on the bits)
 __global__ void k_node_ball(int ng, TsphDevTree T, const int *__restrict__ rid,
-                            const double *__restrict__ fBall2, unsigned long long *nodeBall2) {
+                            const double *__restrict__ fBall2, const int *listFlag,
+                            unsigned long long *nodeBall2) {
+    if (!*listFlag) return;              // only the tree-walk fallback needs node balls
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     bool live = p < ng;
     unsigned long long key = live ? (unsigned long long)__double_as_longlong(fBall2[p]) : 0ULL;
@@ -431,6 +535,101 @@ __global__ void k_node_ball(int ng, TsphDevTree T, const int *__restrict__ rid,
     }
 }
 
+// One pair of SphPressureTermsSym (smoothfcn.c:2276-2385 with
+// SphPressureTerms.h:1-152) as it acts on particle i: own = true when the
+// ball is i's (p = i, q = j), false when it is j's (p = j, q = i).  dx is
+// r_p - r_q (nearest image), fDist2 = |dx|^2.
+__device__ __forceinline__ void sph_pair(const TsphSphBufs &S, const double *__restrict__ m, int p,
+                                         int q, double dx, double dy, double dz, double fDist2,
+                                         bool own, double &ax, double &ay, double &az,
+                                         double &uPdV, double &uAV, double &mu, double &dtN) {
+    const double aFac = 1.0, vFac = 1.0, H = 0.0;
+    const double pc = S.cs[p], qc = S.cs[q];
+    const double ph = S.ph[p];
+    const double r2 = fDist2 * S.ih2[p];
+    const double rs1 = dkern_m4(r2) * S.fn1[p];
+    const double rp = rs1 * m[p], rq = rs1 * m[q];
+    const double dvx = S.vx[p] - S.vx[q], dvy = S.vy[p] - S.vy[q], dvz = S.vz[p] - S.vz[q];
+    const double dvdotdr = vFac * (dvx * dx + dvy * dy + dvz * dz) + fDist2 * H;
+    double Acc, dt;
+    if (own) {
+        uPdV += rq * S.pr2[p] * dvdotdr;
+        Acc = S.pr2f[p] + S.pr2f[q];
+    } else {
+        uPdV += rp * S.pr2[q] * dvdotdr;
+        Acc = S.pr2f[q] + S.pr2f[p];
+    }
+    if (dvdotdr >= 0.0) {
+        dt = cS.dtFacCourant * ph / (2 * (pc > qc ? pc : qc));
+    } else {
+        double absmu = -dvdotdr * aFac / sqrt(fDist2);
+        if (absmu > mu) mu = absmu;
+        double visc = (cS.alpha * (pc + qc) + cS.beta * 1.5 * absmu);
+        dt = cS.dtFacCourant * ph / (0.625 * (pc + qc) + 0.375 * visc);
+        visc = (0.5 * (S.bal[p] + S.bal[q])) * visc * absmu / (S.rho[p] + S.rho[q]);
+        if (own) uAV += rq * (0.5 * visc) * dvdotdr;
+        else uAV += rp * (0.5 * visc) * dvdotdr;
+        Acc += visc;
+    }
+    if (own) {
+        Acc *= rq * aFac;
+        ax -= Acc * dx; ay -= Acc * dy; az -= Acc * dz;
+        if (dt < dtN) dtN = dt;
+        if (4 * S.dtp[q] < dtN) dtN = 4 * S.dtp[q];
+    } else {
+        Acc *= rp * aFac;
+        ax += Acc * dx; ay += Acc * dy; az += Acc * dz;
+        if (dt < dtN) dtN = dt;
+        if (4 * S.dtp[p] < dtN) dtN = 4 * S.dtp[p];
+    }
+}
+
+// SphPressureTermsSym from the stored lists: particle i sums its own-ball
+// pairs N(i) and the pairs R(i) whose ball holds i, each list in ascending
+// index, lane-strided, then a fixed-order warp sum.  No tree walk.
+__global__ void __launch_bounds__(SW * 32) k_pressure_lists(SphArgs A) {
+    const int lane = threadIdx.x & 31;
+    const unsigned FULL = 0xffffffffu;
+    const int ng = cS.ngas;
+    const TsphSphBufs &S = A.S;
+    if (S.listFlag[0]) return;           // a list overflowed: the tree walk runs instead
+    for (;;) {
+        int i = 0;
+        if (lane == 0) i = atomicAdd(A.work, 1);
+        i = __shfl_sync(FULL, i, 0);
+        if (i >= ng) break;
+        const double xi = A.G.x[i], yi = A.G.y[i], zi = A.G.z[i];
+        double ax = 0, ay = 0, az = 0, uPdV = 0, uAV = 0, mu = 0.0, dtN = FLT_MAX;
+        const int *own = S.nbrList + (size_t)i * S.nbrCap;
+        const int nOwn = S.nnCount[i];
+        for (int e = lane; e < nOwn; e += 32) {
+            int j = own[e];
+            double dx, dy, dz;
+            double d2 = dist2_exact(xi, yi, zi, A.G.x[j], A.G.y[j], A.G.z[j], dx, dy, dz);
+            sph_pair(S, A.G.m, i, j, dx, dy, dz, d2, true, ax, ay, az, uPdV, uAV, mu, dtN);
+        }
+        const int ro = i > 0 ? S.roff[i - 1] : 0, nRev = S.roff[i] - ro;
+        for (int e = lane; e < nRev; e += 32) {
+            int j = S.rlist[ro + e];
+            double dx, dy, dz;
+            double d2 = dist2_exact(A.G.x[j], A.G.y[j], A.G.z[j], xi, yi, zi, dx, dy, dz);
+            sph_pair(S, A.G.m, j, i, dx, dy, dz, d2, false, ax, ay, az, uPdV, uAV, mu, dtN);
+        }
+        ax = wsum(ax); ay = wsum(ay); az = wsum(az); uPdV = wsum(uPdV); uAV = wsum(uAV);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            double a = __shfl_xor_sync(FULL, mu, o);
+            double b = __shfl_xor_sync(FULL, dtN, o);
+            mu = a > mu ? a : mu;
+            dtN = b < dtN ? b : dtN;
+        }
+        if (lane == 0) {
+            S.hax[i] = ax; S.hay[i] = ay; S.haz[i] = az;
+            S.uPdV[i] = uPdV; S.uAV[i] = uAV; S.mumax[i] = mu; S.dtNew[i] = dtN;
+        }
+    }
+}
+
 // SphPressureTermsSym as a gather over both roles of every pair.
 __global__ void __launch_bounds__(SW * 32) k_pressure(SphArgs A) {
     __shared__ int stackAll[SW][SSTK];
@@ -439,6 +638,7 @@ __global__ void __launch_bounds__(SW * 32) k_pressure(SphArgs A) {
     const unsigned FULL = 0xffffffffu;
     const int ng = cS.ngas;
     const double aFac = 1.0, vFac = 1.0, H = 0.0;
+    if (!A.S.listFlag[0]) return;        // the list kernel did the work
     for (;;) {
         int i = 0;
         if (lane == 0) i = atomicAdd(A.work, 1);
@@ -741,6 +941,7 @@ static int run_density(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_out
     A.work = (int *)&ctx->dCnt->pad;
     A.seed = (sp->bLearnedH && S.haveSeed) ? S.seed : nullptr;
     TSPH_CK(cudaMemsetAsync(ctx->dCnt, 0, sizeof(TsphDevCounters), ctx->stream));
+    TSPH_CK(cudaMemsetAsync(S.listFlag, 0, sizeof(int), ctx->stream));
     if (!cap) cudaEventRecord(ctx->ev[6], ctx->stream);
     size_t sm = sizeof(KnnSmem) * SW;
     if (!cap)
@@ -797,9 +998,22 @@ static int run_pressure(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_ou
     }
     k_gas_pressure<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, S);
     TSPH_LAUNCH_CK("k_gas_pressure");
+    // reverse neighbour lists (the kernels stand down when a list overflowed)
+    TSPH_CK(cudaMemsetAsync(S.rcnt, 0, sizeof(int) * ng, ctx->stream));
+    TSPH_CK(cudaMemsetAsync(S.rcur, 0, sizeof(int) * ng, ctx->stream));
+    TSPH_CK(cudaMemsetAsync(S.listFlag + 1, 0, 3 * sizeof(int), ctx->stream));
+    const long long pairSlots = (long long)ng * S.nbrCap;
+    k_rev_count<<<tsph_blocks(pairSlots, 256), 256, 0, ctx->stream>>>(ng, S);
+    TSPH_LAUNCH_CK("k_rev_count");
+    int rc = tsph_scan_inclusive(ctx, S.rcnt, S.roff, ng);
+    if (rc) return rc;
+    k_rev_fill<<<tsph_blocks(pairSlots, 256), 256, 0, ctx->stream>>>(ng, S);
+    TSPH_LAUNCH_CK("k_rev_fill");
+    k_rev_sort<<<ctx->smCount * 4, SW * 32, 0, ctx->stream>>>(ng, S, S.listFlag + 1);
+    TSPH_LAUNCH_CK("k_rev_sort");
     TSPH_CK(cudaMemsetAsync(S.nodeBall2, 0, sizeof(unsigned long long) * ctx->TG.nNodes, ctx->stream));
     k_node_ball<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, ctx->TG, ctx->G.rid, S.fBall2,
-                                                              S.nodeBall2);
+                                                              S.listFlag, S.nodeBall2);
     TSPH_LAUNCH_CK("k_node_ball");
     SphArgs A;
     A.T = ctx->TG;
@@ -809,6 +1023,10 @@ static int run_pressure(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_ou
     A.work = (int *)&ctx->dCnt->pad;
     A.seed = nullptr;
     TSPH_CK(cudaMemsetAsync(ctx->dCnt, 0, sizeof(TsphDevCounters), ctx->stream));
+    SphArgs AL = A;
+    AL.work = S.listFlag + 2;
+    k_pressure_lists<<<ctx->smCount * 4, SW * 32, 0, ctx->stream>>>(AL);
+    TSPH_LAUNCH_CK("k_pressure_lists");
     k_pressure<<<ctx->smCount * 4, SW * 32, 0, ctx->stream>>>(A);
     TSPH_LAUNCH_CK("k_pressure");
     k_scatter_hydro<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, ctx->G.iord, S, ctx->C);

@@ -52,6 +52,14 @@ struct TsphSphBufs {
     int *nnCount;
     unsigned long long *nnHash;
     unsigned long long *nodeBall2;   // per gas-tree node: max fBall2 (bits)
+    // neighbour lists of the last density pass: N(i) = {j : d2 <= fBall2_i}
+    // in ascending gas-tree index (nbrCap per particle), and the reverse
+    // lists R(i) = {j : i in N(j)}, also ascending
+    int nbrCap;
+    int *nbrList;
+    int *rcnt, *roff, *rcur, *rlist;
+    int *listFlag;               // device: [0] = a list did not fit (use the tree walk)
+    double *ph, *ih2, *fn1, *pr2f;   // per-particle kernel invariants of the pressure pass
     int nFallback;
     bool haveDensity, havePressure, haveSeed;
     tsph_sph_params last;

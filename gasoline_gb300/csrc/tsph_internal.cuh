@@ -14,6 +14,8 @@
 
 #define TSPH_WARP 32
 #define TSPH_MAX_LEVELS 128
+#define TSPH_NBR_CAP 64      // stored neighbours per gas particle (ties beyond: tree-walk pressure)
+#define TSPH_RCAP 1024       // longest reverse list sorted in shared memory
 
 // FP64 helpers that never contract into FMA: the reference's tree and walk
 // decisions are reproduced bit for bit, so every rounding step must match
