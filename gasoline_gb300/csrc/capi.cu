@@ -123,6 +123,7 @@ int tsph_ensure_particles(tsph_ctx *ctx, int n) {
     TsphDevParts &G = ctx->G;
     rc |= tsph_grow(ctx, &G.x, cap); rc |= tsph_grow(ctx, &G.y, cap); rc |= tsph_grow(ctx, &G.z, cap);
     rc |= tsph_grow(ctx, &G.m, cap); rc |= tsph_grow(ctx, &G.h, cap); rc |= tsph_grow(ctx, &G.iord, cap);
+    rc |= tsph_grow(ctx, &G.ph, cap); rc |= tsph_grow(ctx, &G.pl, cap);
     TsphDevState &C = ctx->C;
     double **cs[] = {&C.x, &C.y, &C.z, &C.vx, &C.vy, &C.vz, &C.m, &C.h, &C.u, &C.vpx, &C.vpy,
                      &C.vpz, &C.upred, &C.ax, &C.ay, &C.az, &C.pot, &C.dtGrav, &C.hax, &C.hay,

@@ -28,7 +28,7 @@
 
 #define SW 4          // warps per block
 #define SSTK 1024     // walk stack per warp
-#define SCAP 1024     // kNN candidate capacity per warp
+#define SCAP 640      // kNN candidate capacity per warp
 #define SMAXIT 48     // radius iterations before giving up
 
 struct SphConst {
@@ -38,6 +38,7 @@ struct SphConst {
     double alpha, beta, gamma, gammam1, dtFacCourant;
     int limiter;
     float margin;     // absolute slack for FP32 box-distance pruning
+    float erel, eabs; // FP32 relative-coordinate error bound: erel |dx| + eabs
 };
 __constant__ SphConst cS;
 
@@ -116,10 +117,23 @@ struct SphArgs {
 #define SNBR 256      // neighbours summed in canonical (index) order
 
 struct KnnSmem {
-    int stack[SSTK];
-    double d2[SCAP];
-    int idx[SCAP];
-    int nbr[SNBR];
+    union {
+        int stack[SSTK];          // ball-gather walk stack
+        double red[14][32];       // then: transpose of the 14 DenDVDX partial sums
+    } u;
+    float2 lh[SCAP];              // candidate squared-distance interval [lo, hi]; a
+                                  // straddling candidate's exact FP64 d2 overlays it
+    int idx[SCAP];                // candidate index (bit 31: exact value in lh)
+    int nbr[SNBR];                // N(i), then sorted
+};
+
+// Finished particles of a warp awaiting the lane-parallel DenDVDX epilogue.
+struct KnnBatch {
+    double s[14][32];
+    double fb2[32];
+    unsigned long long hsh[32];
+    int id[32];
+    int nn[32];
 };
 
 // Sort nbr[0, cnt) ascending (bitonic network over the next power of two,
@@ -144,19 +158,62 @@ __device__ void warp_sort_idx(int *nbr, int cnt, int lane) {
     }
 }
 
-// Ball gather of all gas particles with d2 <= r2 around particle i.
-// Returns the count, or -1 when it exceeds SCAP or the stack overflows.
-__device__ int ball_gather(KnnSmem &W, const SphArgs &A, int lane, int root, double xi, double yi,
-                           double zi, float xf, float yf, float zf, double r2) {
+// M4 kernel W and its derivative from one square root (KERNEL/DKERNEL,
+// smoothfcn.c:64-224): identical values to the two separate evaluations.
+__device__ __forceinline__ void kern_dkern_m4(double ar2, double &w, double &dw) {
+    const double r = sqrt(ar2);
+    double ak = 2.0 - r;
+    if (ar2 < 1.0) {
+        w = 1.0 - 0.75 * ak * ar2;
+        dw = -3 + 2.25 * r;
+    } else {
+        w = 0.25 * ak * ak * ak;
+        dw = -0.75 * (2.0 - r) * (2.0 - r) / r;
+    }
+}
+
+// Squared-distance interval of candidate j around particle i from the FP32
+// hi/lo split coordinates: |dx_true - dx32| <= erel |dx32| + eabs per axis.
+// A periodic separation close to half the box (where the FP32 and FP64
+// image choices could differ) gets the whole range.
+__device__ __forceinline__ float2 d2_interval(float4 hi_i, float4 lo_i, float4 hj, float4 lj) {
+    const float u = 5.9604645e-08f;
+    float d[3] = {(hj.x - hi_i.x) + (lj.x - lo_i.x), (hj.y - hi_i.y) + (lj.y - lo_i.y),
+                  (hj.z - hi_i.z) + (lj.z - lo_i.z)};
+    float lo = 0.0f, hi = 0.0f;
+    bool wide = false;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        float ad = fabsf(d[a]);
+        if (cS.bPeriodic) {
+            const float L = (float)cS.L;
+            if (ad > 0.5f * L) ad = L - ad;
+            if (fabsf(ad - 0.5f * L) < 1e-4f * L) wide = true;
+        }
+        const float e = cS.erel * ad + cS.eabs;
+        const float l = fmaxf(ad - e, 0.0f), h = ad + e;
+        lo += l * l;
+        hi += h * h;
+    }
+    if (wide) return make_float2(0.0f, FLT_MAX);
+    return make_float2(lo * (1.0f - 4.0f * u), hi * (1.0f + 4.0f * u));
+}
+
+// Ball gather around particle i: every gas particle whose squared-distance
+// interval may reach r2 (lo <= r2) becomes a candidate.  Returns the count
+// (-1 when it exceeds SCAP or the stack overflows) and in nSure those
+// certainly inside (hi <= r2).
+__device__ int ball_gather(KnnSmem &W, const SphArgs &A, int lane, int root, float xf, float yf,
+                           float zf, float4 hi_i, float4 lo_i, float r2, int &nSure) {
     const unsigned FULL = 0xffffffffu;
-    int sp = 1, nc = 0;
-    if (lane == 0) W.stack[0] = root;
+    int sp = 1, nc = 0, ns = 0;
+    if (lane == 0) W.u.stack[0] = root;
     __syncwarp();
-    float r2f = (float)r2 * 1.00001f;
+    const float r2box = r2 * 1.00001f;
     bool bad = false;
     while (sp > 0) {
         int take = sp < 32 ? sp : 32;
-        int node = lane < take ? W.stack[sp - take + lane] : -1;
+        int node = lane < take ? W.u.stack[sp - take + lane] : -1;
         __syncwarp();
         sp -= take;
         bool open = false, leaf = false;
@@ -164,7 +221,7 @@ __device__ int ball_gather(KnnSmem &W, const SphArgs &A, int lane, int root, dou
         if (node >= 0) {
             lk = A.T.wlink[node];
             float d2 = box_d2f(xf, yf, zf, A.T.wcomh[node], A.T.wcoml[node]);
-            if (d2 <= r2f) {
+            if (d2 <= r2box) {
                 if (lk.z >= 0) open = true;
                 else leaf = true;
             }
@@ -173,42 +230,24 @@ __device__ int ball_gather(KnnSmem &W, const SphArgs &A, int lane, int root, dou
         if (sp + 2 * __popc(bo) > SSTK) { bad = true; break; }
         if (open) {
             int pos = sp + 2 * __popc(bo & lane_lt_s());
-            W.stack[pos] = lk.z;
-            W.stack[pos + 1] = node + 1;
+            W.u.stack[pos] = lk.z;
+            W.u.stack[pos + 1] = node + 1;
         }
         sp += 2 * __popc(bo);
         // leaf particles, in a fixed order (leaf-lane major, particle minor)
         int cnt = leaf ? lk.y : 0;
         int maxc = __reduce_max_sync(FULL, (unsigned)cnt);
         for (int k = 0; k < maxc; ++k) {
-            bool in = false;
-            double d2 = 0.0;
+            float2 iv = make_float2(FLT_MAX, FLT_MAX);
             int j = lk.x + k;
-            if (k < cnt) {
-                const double xj = A.G.x[j], yj = A.G.y[j], zj = A.G.z[j];
-                // FP32 pre-reject: a lower bound of the distance (rounding
-                // margin off each axis) already beyond the radius
-                float ex = fmaxf(fabsf(xf - (float)xj) - cS.margin, 0.0f);
-                float ey = fmaxf(fabsf(yf - (float)yj) - cS.margin, 0.0f);
-                float ez = fmaxf(fabsf(zf - (float)zj) - cS.margin, 0.0f);
-                if (cS.bPeriodic) {
-                    const float Lf = (float)cS.L;
-                    ex = fminf(ex, fmaxf(Lf - ex - 2.0f * cS.margin, 0.0f));
-                    ey = fminf(ey, fmaxf(Lf - ey - 2.0f * cS.margin, 0.0f));
-                    ez = fminf(ez, fmaxf(Lf - ez - 2.0f * cS.margin, 0.0f));
-                }
-                float lb = (ex * ex + ey * ey + ez * ez) * (1.0f - 1e-6f);
-                if (lb <= r2f) {
-                    double dx, dy, dz;
-                    d2 = dist2_exact(xi, yi, zi, xj, yj, zj, dx, dy, dz);
-                    in = d2 <= r2;
-                }
-            }
+            if (k < cnt) iv = d2_interval(hi_i, lo_i, A.G.ph[j], A.G.pl[j]);
+            const bool in = iv.x <= r2;
             unsigned bi = __ballot_sync(FULL, in);
+            ns += __popc(__ballot_sync(FULL, iv.y <= r2));
             if (nc + __popc(bi) > SCAP) { bad = true; }
             else if (in) {
                 int pos = nc + __popc(bi & lane_lt_s());
-                W.d2[pos] = d2;
+                W.lh[pos] = iv;
                 W.idx[pos] = j;
             }
             nc += __popc(bi);
@@ -217,21 +256,22 @@ __device__ int ball_gather(KnnSmem &W, const SphArgs &A, int lane, int root, dou
         if (bad) break;
     }
     __syncwarp();
+    nSure = ns;
     return bad ? -1 : nc;
 }
 
-// k-th smallest of the candidates' squared distances, exactly: an
-// MSB-first radix select on the bit patterns (non-negative doubles order
-// like their bits), 4 bits per pass.  Each lane counts its candidates per
-// digit in 16-bit fields of four registers; the warp sums the fields.
-__device__ double select_kth(const KnnSmem &W, int nc, int k, int lane) {
+// Radix select (4 bits per pass, MSB first) of the need-th smallest key
+// among the candidates that `take` accepts; counts kept per lane in 16-bit
+// fields of four registers and summed over the warp.
+template <int BITS, typename KeyOf>
+__device__ unsigned long long radix_select(int nc, int need, int lane, KeyOf keyOf) {
     unsigned long long prefix = 0ULL;
-    int need = k;                       // rank still to find inside the prefix
-    for (int shift = 60; shift >= 0; shift -= 4) {
+    for (int shift = BITS - 4; shift >= 0; shift -= 4) {
         unsigned long long c[4] = {0ULL, 0ULL, 0ULL, 0ULL};
-        const unsigned long long hiMask = shift == 60 ? 0ULL : (~0ULL << (shift + 4));
+        const unsigned long long hiMask = (shift + 4 >= 64) ? 0ULL : (~0ULL << (shift + 4));
         for (int e = lane; e < nc; e += 32) {
-            unsigned long long key = (unsigned long long)__double_as_longlong(W.d2[e]);
+            unsigned long long key;
+            if (!keyOf(e, key)) continue;
             if ((key & hiMask) != prefix) continue;
             unsigned d = (unsigned)(key >> shift) & 15u;
             unsigned long long inc = 1ULL << (16 * (d & 3u));
@@ -252,28 +292,93 @@ __device__ double select_kth(const KnnSmem &W, int nc, int k, int lane) {
         }
         prefix |= (unsigned long long)d << shift;
     }
-    return __longlong_as_double((long long)prefix);
+    return prefix;
 }
 
+// The lane-parallel DenDVDX epilogue (smoothfcn.c:3390-3627) of up to 32
+// finished particles: lane l finishes batch entry l.
+__device__ void density_epilogue(const SphArgs &A, KnnBatch &Bt, int cnt, int lane) {
+    __syncwarp();
+    if (lane < cnt) {
+        const int i = Bt.id[lane];
+        const double fBall2 = Bt.fb2[lane];
+        double sm[14];
+#pragma unroll
+        for (int q = 0; q < 14; ++q) sm[q] = Bt.s[q][lane];
+        const double H = 0.0;
+        double ih2 = 4.0 / fBall2, ih = sqrt(ih2);
+        double fNorm = M_1_PI * ih2 * ih;
+        double fDensity = sm[0] * fNorm;
+        double dvxdx = sm[1], dvxdy = sm[2], dvxdz = sm[3], dvydx = sm[4], dvydy = sm[5],
+               dvydz = sm[6], dvzdx = sm[7], dvzdy = sm[8], dvzdz = sm[9];
+        double divvnorm = sm[10], grx = sm[11], gry = sm[12], grz = sm[13];
+        double trace = dvxdx + dvydy + dvzdz;
+        double fNorm1 = (divvnorm != 0 ? 3 / fabs(divvnorm) : 0);
+        double divv = fNorm1 * trace + 3 * H;
+        double cx = fNorm1 * (dvzdy - dvydz), cy = fNorm1 * (dvxdz - dvzdx),
+               cz = fNorm1 * (dvydx - dvxdy);
+        double Hcorr = (fNorm1 != 0 ? H / fNorm1 : 0);
+        double gnorm = grx * grx + gry * gry + grz * grz;
+        if (gnorm > 0) gnorm = 1 / sqrt(gnorm);
+        grx *= gnorm; gry *= gnorm; grz *= gnorm;
+        double dvdr = (((dvxdx + Hcorr) * grx + dvxdy * gry + dvxdz * grz) * grx +
+                       (dvydx * grx + (dvydy + Hcorr) * gry + dvydz * grz) * gry +
+                       (dvzdx * grx + dvzdy * gry + (dvzdz + Hcorr) * grz) * grz) * fNorm1;
+        double dvds = (divv < 0 ? 1.5 * (dvdr - (1. / 3.) * divv) : dvdr);
+        double bal;
+        if (cS.limiter == 1) {
+            bal = divv != 0.0 ? fabs(divv) / (fabs(divv) + sqrt(cx * cx + cy * cy + cz * cz)) : 0.0;
+        } else {
+            bal = 1.0;
+        }
+        double ot = (1. / 3.) * trace;
+        double sxx = dvxdx - ot, syy = dvydy - ot, szz = dvzdz - ot;
+        double sxy = 0.5 * (dvxdy + dvydx), sxz = 0.5 * (dvxdz + dvzdx), syz = 0.5 * (dvydz + dvzdy);
+        double S2 = fNorm1 * fNorm1 * (sxx * sxx + syy * syy + szz * szz +
+                                       2 * (sxy * sxy + sxz * sxz + syz * syz));
+        A.S.fBall2[i] = fBall2;
+        A.S.rho[i] = fDensity;
+        A.S.divv[i] = divv;
+        A.S.curl[3 * i] = cx;
+        A.S.curl[3 * i + 1] = cy;
+        A.S.curl[3 * i + 2] = cz;
+        A.S.dvds[i] = dvds;
+        A.S.bal[i] = bal;
+        A.S.diff[i] = 0.25 * fBall2 * sqrt(2 * S2);
+        A.S.nnCount[i] = Bt.nn[lane];
+        A.S.nnHash[i] = Bt.hsh[lane];
+    }
+    __syncwarp();
+}
+
+// kNN + DenDVDX, one warp per gas particle.  The set N(i) and fBall2 are the
+// exact FP64 ones: candidates carry FP32 distance intervals, the k-th
+// distance is bracketed from them, and only candidates whose interval
+// straddles the bracket get their FP64 distance.  The neighbour sums run
+// over N(i) in ascending index (FP64), so they depend on the set only.
 __global__ void __launch_bounds__(SW * 32) k_knn_density(SphArgs A) {
     extern __shared__ __align__(16) unsigned char smraw[];
     KnnSmem &W = reinterpret_cast<KnnSmem *>(smraw)[threadIdx.x >> 5];
+    KnnBatch &Bt = reinterpret_cast<KnnBatch *>(smraw + sizeof(KnnSmem) * SW)[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
     const unsigned FULL = 0xffffffffu;
     const int ng = cS.ngas, k = cS.k;
     unsigned long long nFall = 0, nPairs = 0, nCand = 0;
+    int nb = 0;                              // particles waiting in the batch
     for (;;) {
         int i = 0;
         if (lane == 0) i = atomicAdd(A.work, 1);
         i = __shfl_sync(FULL, i, 0);
         if (i >= ng) break;
         const double xi = A.G.x[i], yi = A.G.y[i], zi = A.G.z[i];
-        const float xf = (float)xi, yf = (float)yi, zf = (float)zi;
+        const float4 hi_i = A.G.ph[i], lo_i = A.G.pl[i];
+        const float xf = hi_i.x, yf = hi_i.y, zf = hi_i.z;
         const int root = A.T.sysRoot[A.G.rid[i]];   // this particle's system
-        // seed radius
-        double r2;
+        // seed radius (any positive value works: a short ball grows, a large
+        // one shrinks; the seed only sets the cost)
+        float r2;
         if (A.seed && A.seed[i] > 0.0) {
-            r2 = A.seed[i];
+            r2 = (float)A.seed[i];
         } else {
             int node = root;
             for (;;) {
@@ -283,85 +388,114 @@ __global__ void __launch_bounds__(SW * 32) k_knn_density(SphArgs A) {
                 if (A.T.pUpper[child] - A.T.pLower[child] + 1 < k) break;
                 node = child;
             }
-            r2 = 0.0;
-            const double *b = &A.T.bnd[6 * node];
-            double p[3] = {xi, yi, zi};
-            for (int a = 0; a < 3; ++a) {
-                double d = fmax(fabs(p[a] - b[a]), fabs(p[a] - b[3 + a]));
-                r2 += d * d;
+            // farthest box corner (surely k particles), or the radius holding
+            // twice the volume k particles need at the node's mean density
+            const float4 bl = A.T.wcomh[node], bh = A.T.wcoml[node];
+            const float p[3] = {xf, yf, zf}, a[3] = {bl.x, bl.y, bl.z}, c[3] = {bh.x, bh.y, bh.z};
+            float rc = 0.0f, vol = 1.0f;
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                float d = fmaxf(fabsf(p[q] - a[q]), fabsf(p[q] - c[q]));
+                rc += d * d;
+                vol *= c[q] - a[q];
             }
-            r2 = r2 * (1.0 + 1e-9) + 1e-300;
-            // the farthest-corner radius surely holds k particles but is loose;
-            // start instead from the node's mean density with twice the
-            // volume k particles need (a short ball grows, so the result is
-            // the same exact k-th distance either way)
-            const double vol = (b[3] - b[0]) * (b[4] - b[1]) * (b[5] - b[2]);
+            r2 = rc * 1.0001f + 1e-30f;
             const int nNode = A.T.pUpper[node] - A.T.pLower[node] + 1;
-            if (vol > 0.0) {
-                double rd = cbrt(2.0 * 3.0 * k * vol / (4.0 * M_PI * nNode));
+            if (vol > 0.0f) {
+                float rd = cbrtf(2.0f * 3.0f * k * vol / (4.0f * 3.14159265f * nNode));
                 if (rd * rd < r2) r2 = rd * rd;
             }
         }
-        double lo2 = 0.0, hi2 = 0.0;   // radii known too small / too large
-        int nc = -1, it = 0;
+        float lo2 = 0.0f, hi2 = 0.0f;   // radii known too small / too large
+        int nc = -1, nSure = 0, it = 0;
         for (; it < SMAXIT; ++it) {
-            nc = ball_gather(W, A, lane, root, xi, yi, zi, xf, yf, zf, r2);
+            nc = ball_gather(W, A, lane, root, xf, yf, zf, hi_i, lo_i, r2, nSure);
             if (nc < 0) {                       // too many candidates: shrink
                 hi2 = r2;
-                r2 = lo2 > 0.0 ? sqrt(lo2 * hi2) : 0.5 * r2;
-            } else if (nc < k) {                // too few: grow (the fallback)
+                r2 = lo2 > 0.0f ? sqrtf(lo2 * hi2) : 0.5f * r2;
+            } else if (nSure < k) {             // k not surely inside: grow
                 lo2 = r2;
-                r2 = hi2 > 0.0 ? sqrt(lo2 * hi2) : 2.25 * r2;
+                r2 = hi2 > 0.0f ? sqrtf(lo2 * hi2) : 2.25f * r2;
                 ++nFall;
             } else {
                 break;
             }
+            if (hi2 > 0.0f && lo2 > 0.0f && hi2 <= lo2 * 1.0001f) { it = SMAXIT; break; }
         }
         if (it == SMAXIT) {
             if (lane == 0) atomicOr(&A.cnt->status, 1u << TSPH_ERR_KNN_NO_CONVERGE);
             continue;
         }
         nCand += nc;
-        double fBall2 = select_kth(W, nc, k, lane);
-        // DenDVDX over N(i) = {j : d2 <= fBall2} (smoothfcn.c:3390-3627)
-        const double vxi = A.S.vx[i], vyi = A.S.vy[i], vzi = A.S.vz[i];
-        double ih2 = 4.0 / fBall2, ih = sqrt(ih2);
-        double fNorm = M_1_PI * ih2 * ih;
-        double s[14];
-#pragma unroll
-        for (int q = 0; q < 14; ++q) s[q] = 0.0;
+        // bracket the k-th distance: Tlo <= fBall2 <= Thi
+        const float Tlo = __uint_as_float((unsigned)radix_select<32>(nc, k, lane,
+            [&](int e, unsigned long long &key) { key = __float_as_uint(W.lh[e].x); return true; }));
+        const float Thi = __uint_as_float((unsigned)radix_select<32>(nc, k, lane,
+            [&](int e, unsigned long long &key) { key = __float_as_uint(W.lh[e].y); return true; }));
+        // certainly inside (hi < Tlo), straddling (exact FP64 now), outside
+        int nIn = 0;
+        for (int e = lane; e < nc; e += 32) {
+            const float2 iv = W.lh[e];
+            if (iv.y < Tlo) {
+                ++nIn;
+            } else if (iv.x <= Thi) {
+                const int j = W.idx[e];
+                double dx, dy, dz;
+                double d2 = dist2_exact(xi, yi, zi, A.G.x[j], A.G.y[j], A.G.z[j], dx, dy, dz);
+                *reinterpret_cast<double *>(&W.lh[e]) = d2;
+                W.idx[e] = j | (int)0x80000000;
+            }
+        }
+        nIn = __reduce_add_sync(FULL, (unsigned)nIn);
+        __syncwarp();
+        const double fBall2 = __longlong_as_double((long long)radix_select<64>(
+            nc, k - nIn, lane, [&](int e, unsigned long long &key) {
+                if (W.idx[e] >= 0) return false;
+                key = (unsigned long long)__double_as_longlong(*reinterpret_cast<const double *>(&W.lh[e]));
+                return true;
+            }));
         // N(i) in ascending particle order, so the sums below depend only on
         // the neighbour set, not on the order the ball gather found them
         int nsel = 0;
         for (int e0 = 0; e0 < nc; e0 += 32) {
             int e = e0 + lane;
-            bool in = e < nc && W.d2[e] <= fBall2;
+            bool in = false;
+            int j = 0;
+            if (e < nc) {
+                const int t = W.idx[e];
+                if (t < 0) {
+                    j = t & 0x7fffffff;
+                    in = *reinterpret_cast<const double *>(&W.lh[e]) <= fBall2;
+                } else {
+                    j = t;
+                    in = W.lh[e].y < Tlo;
+                }
+            }
             unsigned bi = __ballot_sync(FULL, in);
-            if (in && nsel + __popc(bi & lane_lt_s()) < SNBR)
-                W.nbr[nsel + __popc(bi & lane_lt_s())] = W.idx[e];
+            if (in && nsel + __popc(bi & lane_lt_s()) < SNBR) W.nbr[nsel + __popc(bi & lane_lt_s())] = j;
             nsel += __popc(bi);
         }
         __syncwarp();
-        const bool sorted = nsel <= SNBR;
-        if (sorted) warp_sort_idx(W.nbr, nsel, lane);
-        if (sorted && nsel <= A.S.nbrCap) {
+        if (nsel > SNBR) {                   // more than SNBR exact ties
+            if (lane == 0) atomicOr(&A.cnt->status, 1u << TSPH_ERR_LIST_OVERFLOW);
+            continue;
+        }
+        warp_sort_idx(W.nbr, nsel, lane);
+        if (nsel <= A.S.nbrCap) {
             int *dst = A.S.nbrList + (size_t)i * A.S.nbrCap;
             for (int e = lane; e < nsel; e += 32) dst[e] = W.nbr[e];
         } else if (lane == 0) {
             A.S.listFlag[0] = 1;
         }
-        int nn = 0;
+        // DenDVDX neighbour sums (smoothfcn.c:3390-3627) over N(i)
+        const double vxi = A.S.vx[i], vyi = A.S.vy[i], vzi = A.S.vz[i];
+        const double ih2 = 4.0 / fBall2;
+        double sm[14];
+#pragma unroll
+        for (int q = 0; q < 14; ++q) sm[q] = 0.0;
         unsigned long long hsh = 0ULL;
-        const int nloop = sorted ? nsel : nc;
-        for (int e = lane; e < nloop; e += 32) {
-            int j;
-            if (sorted) {
-                j = W.nbr[e];
-            } else {                             // more than SNBR ties: gather order
-                if (W.d2[e] > fBall2) continue;
-                j = W.idx[e];
-            }
-            ++nn;
+        for (int e = lane; e < nsel; e += 32) {
+            const int j = W.nbr[e];
             unsigned long long hx = (unsigned long long)(A.G.iord[j] + 1);
             hx *= 0x9E3779B97F4A7C15ULL;
             hx ^= hx >> 29;
@@ -370,76 +504,65 @@ __global__ void __launch_bounds__(SW * 32) k_knn_density(SphArgs A) {
             hsh += hx;
             double dx, dy, dz;
             const double d2 = dist2_exact(xi, yi, zi, A.G.x[j], A.G.y[j], A.G.z[j], dx, dy, dz);
-            double r2k = d2 * ih2;
-            double mj = A.G.m[j];
-            double rs = kern_m4(r2k);
-            s[0] += rs * mj;
-            double rs1 = dkern_m4(r2k) * mj;
+            double rs, rs1;
+            kern_dkern_m4(d2 * ih2, rs, rs1);
+            const double mj = A.G.m[j];
+            sm[0] += rs * mj;
+            rs1 *= mj;
             double dvx = (-vxi + A.S.vx[j]), dvy = (-vyi + A.S.vy[j]), dvz = (-vzi + A.S.vz[j]);
-            s[1] += dvx * dx * rs1; s[2] += dvx * dy * rs1; s[3] += dvx * dz * rs1;
-            s[4] += dvy * dx * rs1; s[5] += dvy * dy * rs1; s[6] += dvy * dz * rs1;
-            s[7] += dvz * dx * rs1; s[8] += dvz * dy * rs1; s[9] += dvz * dz * rs1;
-            s[10] += (dx * dx + dy * dy + dz * dz) * rs1;
-            double uj = A.S.u[j];
-            s[11] += uj * dx * rs1;
-            s[12] += uj * dy * rs1;
-            s[13] += uj * dz * rs1;
+            sm[1] += dvx * dx * rs1; sm[2] += dvx * dy * rs1; sm[3] += dvx * dz * rs1;
+            sm[4] += dvy * dx * rs1; sm[5] += dvy * dy * rs1; sm[6] += dvy * dz * rs1;
+            sm[7] += dvz * dx * rs1; sm[8] += dvz * dy * rs1; sm[9] += dvz * dz * rs1;
+            sm[10] += (dx * dx + dy * dy + dz * dz) * rs1;
+            const double uj = A.S.u[j];
+            sm[11] += uj * dx * rs1;
+            sm[12] += uj * dy * rs1;
+            sm[13] += uj * dz * rs1;
         }
+        // fixed-order sums: the 14 x 32 partials transposed through shared
+        // memory, lane q adds quantity q's 32 partials in lane order
 #pragma unroll
-        for (int q = 0; q < 14; ++q) s[q] = wsum(s[q]);
-        nn = __reduce_add_sync(FULL, (unsigned)nn);
+        for (int q = 0; q < 14; ++q) W.u.red[q][lane] = sm[q];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) hsh += __shfl_xor_sync(FULL, hsh, o);
+        __syncwarp();
+        if (lane < 14) {
+            double t = 0.0;
+            for (int l = 0; l < 32; ++l) t += W.u.red[lane][l];
+            Bt.s[lane][nb] = t;
+        }
         if (lane == 0) {
-            const double H = 0.0;
-            double fDensity = s[0] * fNorm;
-            double dvxdx = s[1], dvxdy = s[2], dvxdz = s[3], dvydx = s[4], dvydy = s[5],
-                   dvydz = s[6], dvzdx = s[7], dvzdy = s[8], dvzdz = s[9];
-            double divvnorm = s[10], grx = s[11], gry = s[12], grz = s[13];
-            double trace = dvxdx + dvydy + dvzdz;
-            double fNorm1 = (divvnorm != 0 ? 3 / fabs(divvnorm) : 0);
-            double divv = fNorm1 * trace + 3 * H;
-            double cx = fNorm1 * (dvzdy - dvydz), cy = fNorm1 * (dvxdz - dvzdx),
-                   cz = fNorm1 * (dvydx - dvxdy);
-            double Hcorr = (fNorm1 != 0 ? H / fNorm1 : 0);
-            double gnorm = grx * grx + gry * gry + grz * grz;
-            if (gnorm > 0) gnorm = 1 / sqrt(gnorm);
-            grx *= gnorm; gry *= gnorm; grz *= gnorm;
-            double dvdr = (((dvxdx + Hcorr) * grx + dvxdy * gry + dvxdz * grz) * grx +
-                           (dvydx * grx + (dvydy + Hcorr) * gry + dvydz * grz) * gry +
-                           (dvzdx * grx + dvzdy * gry + (dvzdz + Hcorr) * grz) * grz) * fNorm1;
-            double dvds = (divv < 0 ? 1.5 * (dvdr - (1. / 3.) * divv) : dvdr);
-            double bal;
-            if (cS.limiter == 1) {
-                bal = divv != 0.0 ? fabs(divv) / (fabs(divv) + sqrt(cx * cx + cy * cy + cz * cz)) : 0.0;
-            } else {
-                bal = 1.0;
-            }
-            double ot = (1. / 3.) * trace;
-            double sxx = dvxdx - ot, syy = dvydy - ot, szz = dvzdz - ot;
-            double sxy = 0.5 * (dvxdy + dvydx), sxz = 0.5 * (dvxdz + dvzdx), syz = 0.5 * (dvydz + dvzdy);
-            double S2 = fNorm1 * fNorm1 * (sxx * sxx + syy * syy + szz * szz +
-                                           2 * (sxy * sxy + sxz * sxz + syz * syz));
-            A.S.fBall2[i] = fBall2;
-            A.S.rho[i] = fDensity;
-            A.S.divv[i] = divv;
-            A.S.curl[3 * i] = cx;
-            A.S.curl[3 * i + 1] = cy;
-            A.S.curl[3 * i + 2] = cz;
-            A.S.dvds[i] = dvds;
-            A.S.bal[i] = bal;
-            A.S.diff[i] = 0.25 * fBall2 * sqrt(2 * S2);
-            A.S.nnCount[i] = nn;
-            A.S.nnHash[i] = hsh;
-            nPairs += nn;
+            Bt.fb2[nb] = fBall2;
+            Bt.hsh[nb] = hsh;
+            Bt.id[nb] = i;
+            Bt.nn[nb] = nsel;
+        }
+        nPairs += nsel;
+        ++nb;
+        if (nb == 32) {
+            density_epilogue(A, Bt, nb, lane);
+            nb = 0;
         }
         __syncwarp();
     }
+    if (nb > 0) density_epilogue(A, Bt, nb, lane);
     if (lane == 0) {
         if (nFall) atomicAdd(&A.cnt->nExactTests, nFall);
         if (nPairs) atomicAdd(&A.cnt->nPartPP, nPairs);
         if (nCand) atomicAdd(&A.cnt->nCellNewt, nCand);
     }
+}
+
+// FP32 hi/lo split of the gas positions (tree order) for the kNN intervals.
+__global__ void k_gas_split(int ng, TsphDevParts G) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ng) return;
+    float hx, lx, hy, ly, hz, lz;
+    split2f(G.x[i], hx, lx);
+    split2f(G.y[i], hy, ly);
+    split2f(G.z[i], hz, lz);
+    G.ph[i] = make_float4(hx, hy, hz, 0.0f);
+    G.pl[i] = make_float4(lx, ly, lz, 0.0f);
 }
 
 // pkdGasPressure (pkd.c:5750-5785) for the adiabatic gas model.
@@ -869,6 +992,8 @@ static void set_sph_const(tsph_ctx *ctx, const tsph_sph_params *sp) {
         ctx->gasScale = r;
     }
     if (ctx->capLimit > r) r = ctx->capLimit;   // a captured step's coordinate bound
+    c.erel = 4.0f * 5.9604645e-08f;
+    c.eabs = (float)(ldexp(1.0, -44) * r + (sp->bPeriodic ? 8.0 * 5.960464477539063e-08 * sp->dPeriod : 0.0)) + 1e-30f;
     if (sp->bPeriodic) r += sp->dPeriod;
     c.margin = (float)(8.0 * 5.960464477539063e-08 * r) + 1e-30f;
     cudaMemcpyToSymbolAsync(cS, &c, sizeof(c), 0, cudaMemcpyHostToDevice, ctx->stream);
@@ -919,6 +1044,8 @@ static int run_density(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_out
     if (rc) return rc;
     k_gas_nodes<<<tsph_blocks(ctx->TG.nNodes, 256), 256, 0, ctx->stream>>>(ctx->TG);
     TSPH_LAUNCH_CK("k_gas_nodes");
+    k_gas_split<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, ctx->G);
+    TSPH_LAUNCH_CK("k_gas_split");
     k_gas_gather_vel<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, ctx->C, ctx->G.iord, S);
     TSPH_LAUNCH_CK("k_gas_gather_vel");
     if (!cap) set_sph_const(ctx, sp);
@@ -943,7 +1070,7 @@ static int run_density(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_out
     TSPH_CK(cudaMemsetAsync(ctx->dCnt, 0, sizeof(TsphDevCounters), ctx->stream));
     TSPH_CK(cudaMemsetAsync(S.listFlag, 0, sizeof(int), ctx->stream));
     if (!cap) cudaEventRecord(ctx->ev[6], ctx->stream);
-    size_t sm = sizeof(KnnSmem) * SW;
+    size_t sm = (sizeof(KnnSmem) + sizeof(KnnBatch)) * SW;
     if (!cap)
         TSPH_CK(cudaFuncSetAttribute(k_knn_density, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     k_knn_density<<<ctx->smCount * 3, SW * 32, sm, ctx->stream>>>(A);
