@@ -111,7 +111,8 @@ def run_ours(args, rank, world, local_rank):
     import gasoline_gb300 as g
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
-    stream = torch.cuda.current_stream(dev)
+    # a dedicated stream: the library runs on it and the events bracket it
+    stream = torch.cuda.Stream(dev)
     ctx = g.Context(local_rank, stream=stream.cuda_stream)
     pos, m, soft = workload(args.ng)
     n = len(m)
@@ -141,7 +142,8 @@ def run_ours(args, rank, world, local_rank):
         launches0 = ctx.launches()
         out = None
         for _ in range(steps):
-            flush.zero_()
+            with torch.cuda.stream(stream):
+                flush.zero_()
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
@@ -276,6 +278,214 @@ def run_reference(args):
     }
 
 
+# ---------------------------------------------------------------------------
+# the other workloads (each prints its own JSON line; the default run is the
+# periodic box above)
+# ---------------------------------------------------------------------------
+def _cuda_ms(fn, stream):
+    import torch
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    fn()
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def run_plummer(args):
+    """Plummer sphere, N = 32768: one gravity evaluation plus one KDK step
+    (dt = 1e-3) in FP64 and FP32, forces against the FP64 direct sum."""
+    import torch
+    import gasoline_gb300 as g
+    import oracle
+    pos, vel, m = g.ics.plummer(32768, seed=1)
+    soft = np.full(len(m), 0.01)
+    stream = torch.cuda.Stream()
+    ctx = g.Context(0, stream=stream.cuda_stream)
+    ctx.set_particles(pos, m, soft)
+    ctx.set_velocities(vel)
+    ad, _ = oracle.direct(pos, m, soft, np.arange(len(m)), nthreads=os.cpu_count() or 1)
+    res = {}
+    for name, prec in (("fp64", g.FP64), ("fp32", g.FP32)):
+        gp = g.grav_params(periodic=False, precision=prec)
+        for _ in range(args.warmup):
+            ctx.grav_all(gp)
+        ts = [_cuda_ms(lambda: ctx.grav_all(gp), stream) for _ in range(args.steps)]
+        a = ctx.get_gravity()["acc"]
+        e = np.linalg.norm(a - ad, axis=1) / np.linalg.norm(ad, axis=1)
+        tk = [_cuda_ms(lambda: (ctx.kick(5e-4), ctx.drift(1e-3, False, 1.0), ctx.grav_all(gp),
+                                ctx.kick(5e-4)), stream)]
+        res[name] = {"grav_ms": statistics.mean(ts), "kdk_step_ms": tk[0],
+                     "err_vs_direct_rms": float(np.sqrt(np.mean(e ** 2))),
+                     "err_vs_direct_p99": float(np.percentile(e, 99))}
+        ctx.set_particles(pos, m, soft)
+        ctx.set_velocities(vel)
+    ctx.close()
+    ms = res["fp32"]["grav_ms"]
+    return {"metric": "particle force evals/s, Plummer N=32768 (gravity)", "value": 32768 / (ms * 1e-3),
+            "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "dtype": "f32", "data": "synthetic Plummer sphere, seed 1",
+            "config": {"workload": "Plummer N=32768, G=M=a=1, rmax=20a, theta=0.7, eps=0.01, "
+                                   "nBucket=8, one eval + one KDK dt=1e-3"}, "paths": res}
+
+
+def run_collapse(args):
+    """Adiabatic collapse of a 1/r gas sphere, N = 262144, self-gravity + SPH
+    over `--collapse-steps` KDK steps of `--collapse-dt` (0.002).  Run A collects the
+    h-network's samples on the first 50 steps, trains it on the GPU and then
+    seeds every kNN with its prediction; run B is the same simulation with
+    the exact kNN alone.  Neighbour sets and fBall2 are compared bit for bit
+    every step after training."""
+    import gasoline_gb300 as g
+    from gasoline_gb300.sim import Simulation
+    n = args.collapse_n
+    pos, vel, m, u = g.ics.gas_sphere(n, seed=41)
+    soft = np.full(n, 0.01)
+    kw = dict(ngas=n, u=u, nSmooth=32, precision=g.FP32)
+    A = Simulation(pos, vel, m, soft, **kw)
+    B = Simulation(pos, vel, m, soft, **kw)
+    A.ctx.hnet_init(seed=3)
+    A.ctx.hnet_mode(collect=True)
+    A.forces()
+    B.forces()
+    # fixed step: 200 x 0.002 reaches t = 0.4, before the bounce near the
+    # free-fall time (~1.1) where a fixed step would violate the Courant limit
+    dt, ntrain = args.collapse_dt, 50
+    rows = {"A": [], "B": []}
+    mismatch = 0
+    train = {}
+    for step in range(args.collapse_steps):
+        if step == ntrain:
+            t0 = time.perf_counter()
+            l0 = A.ctx.hnet_train(steps=0, batch=8192)
+            l1 = A.ctx.hnet_train(steps=600, batch=8192, lr=3e-3)
+            train = {"loss_before": l0, "loss_after": l1, "samples": A.ctx.hnet_info()[0],
+                     "train_s": time.perf_counter() - t0, "adam_steps": 600, "batch": 8192}
+            A.ctx.hnet_mode(collect=False, predict=True, margin=0.08)
+            A.learned_h = True
+        ra = A.step(dt)
+        rb = B.step(dt)
+        if step >= ntrain:
+            for key, r in (("A", ra), ("B", rb)):
+                rows[key].append((r["wall_s"], r["t_grav_ms"], r["t_knn_density_ms"],
+                                  r["t_pressure_ms"], r["density"]["dCandidates"],
+                                  r["density"]["nFallback"], r["density"]["bSeeded"]))
+            sa, sb = A.ctx.get_sph(), B.ctx.get_sph()
+            ha, hb = A.ctx.get_neighbour_hash(), B.ctx.get_neighbour_hash()
+            if not (np.array_equal(sa["fBall2"], sb["fBall2"]) and np.array_equal(ha[1], hb[1])
+                    and np.array_equal(ha[0], hb[0])):
+                mismatch += 1
+    def summ(rr):
+        a = np.array(rr, dtype=np.float64)
+        return {"step_ms": float(a[:, 0].mean() * 1e3), "grav_ms": float(a[:, 1].mean()),
+                "density_ms": float(a[:, 2].mean()), "pressure_ms": float(a[:, 3].mean()),
+                "candidates_per_particle": float(a[:, 4].mean() / n),
+                "grown_balls_per_pass": float(a[:, 5].mean()), "seeded": bool(a[:, 6].all())}
+    sa_, sb_ = summ(rows["A"]), summ(rows["B"])
+    A.ctx.close()
+    B.ctx.close()
+    return {"metric": "gas particle force evals/s (gravity + SPH density + pressure), "
+                      "adiabatic collapse N=262144, learned h", "value": n / (sa_["step_ms"] * 1e-3),
+            "unit": UNIT, "n_gpus": 1, "steps": args.collapse_steps, "warmup": ntrain,
+            "ms_per_step": sa_["step_ms"], "higher_is_better": True, "dtype": "f32 gravity, f64 SPH",
+            "data": "synthetic 1/r gas sphere, seed 41",
+            "config": {"workload": "adiabatic collapse, 262144 gas, M=R=G=1, u=0.05, gamma=5/3, "
+                                   f"nSmooth=32, alpha=1, beta=2, dt={dt}, MLP trained on steps 0-49",
+                       "timing": "host wall clock per KDK step incl. host round trips"},
+            "learned_h": sa_, "exact_knn": sb_, "training": train,
+            "density_speedup_learned_vs_exact": sb_["density_ms"] / sa_["density_ms"],
+            "neighbour_sets_bit_exact": mismatch == 0, "steps_with_mismatch": mismatch}
+
+
+def run_batched(args):
+    """512 independent Plummer/Hernquist spheres, N log-uniform in
+    [1024, 65536], every other pair with a 0.2 gas fraction: one context, a
+    forest of trees; launch shapes autotuned, then whole KDK steps replayed
+    from one CUDA graph.  FP32 gravity against the FP64 direct sum on a
+    sample of every system."""
+    import torch
+    import gasoline_gb300 as g
+    from gasoline_gb300 import autotune
+    import oracle
+    systems = g.ics.batched_systems(nsys=args.nsys, seed=5)
+    pos, vel, m, soft, ngas, u, so, index = g.ics.pack_systems(systems)
+    n = len(m)
+    stream = torch.cuda.Stream()
+    ctx = g.Context(0, stream=stream.cuda_stream)
+    ctx.set_particles(pos, m, soft)
+    ctx.set_velocities(vel, ngas, u)
+    ctx.set_systems(so)
+    sp = g.sph_params(nSmooth=32)
+    best, table = autotune.tune_gravity(ctx, g.grav_params(periodic=False, precision=g.FP32))
+    gp = g.grav_params(periodic=False, precision=g.FP32, nBucket=best["nBucket"])
+    ctx.set_tuning(taskSize=best["taskSize"], walkBlocksPerSM=best["walkBlocksPerSM"])
+    ctx.grav_all(gp)
+    acc = ctx.get_gravity()["acc"]
+    errs = []
+    for s_, d in enumerate(systems):
+        q = np.linspace(0, len(d["mass"]) - 1, 16).astype(np.int64)
+        ad, _ = oracle.direct(d["pos"], d["mass"], d["soft"], q, nthreads=os.cpu_count() or 1)
+        e = np.linalg.norm(acc[index[s_][q]] - ad, axis=1) / np.linalg.norm(ad, axis=1)
+        errs.append(float(np.sqrt(np.mean(e ** 2))))
+    res = {}
+    for graph in (False, True):
+        ctx.step(1e-4, gp, sp, graph=graph)
+        ctx.step_status()
+        l0 = ctx.launches()
+        ts = [_cuda_ms(lambda: ctx.step(1e-4, gp, sp, graph=graph), stream) for _ in range(args.steps)]
+        ctx.step_status()
+        res["graph" if graph else "direct"] = {"step_ms": statistics.mean(ts),
+                                               "kernels_per_step": (ctx.launches() - l0) / args.steps}
+    ctx.close()
+    ms = res["graph"]["step_ms"]
+    return {"metric": "particle force evals/s, 512 batched uneven systems (gravity + SPH), one CUDA graph per step",
+            "value": n / (ms * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": 1, "ms_per_step": ms, "higher_is_better": True, "dtype": "f32 gravity, f64 SPH",
+            "data": "synthetic Plummer/Hernquist spheres, seed 5",
+            "config": {"workload": f"{args.nsys} systems, N log-uniform [1024, 65536], total {n}, "
+                                   f"gas {ngas}, eps=0.01, theta=0.7, nSmooth=32",
+                       "tuned": best},
+            "autotune": table, "steps": res,
+            "per_system_err_vs_direct": {"max_rms": max(errs), "median_rms": float(np.median(errs))}}
+
+
+def run_mixed(args):
+    """Clustered periodic box, 2 x ng^3 (gas + dark matter) with 64 Plummer
+    clumps: full gravity (FP32, Ewald) + SPH step with the learned h after
+    two steps of sample collection and GPU training."""
+    import gasoline_gb300 as g
+    from gasoline_gb300.sim import Simulation
+    ng = args.mixed_ng
+    pos, vel, m, ngas, u = g.ics.mixed_box(ng, seed=6)
+    n = len(m)
+    soft = np.full(n, 1.0 / (50.0 * ng))
+    sim = Simulation(pos, vel, m, soft, ngas=ngas, u=u, periodic=True, L=1.0, nSmooth=32,
+                     precision=g.FP32)
+    sim.ctx.hnet_init(seed=3)
+    sim.ctx.hnet_mode(collect=True)
+    sim.forces()
+    for _ in range(2):
+        sim.step(1e-4)
+    loss = sim.ctx.hnet_train(steps=300, batch=8192, lr=3e-3)
+    sim.ctx.hnet_mode(collect=False, predict=True, margin=0.08)
+    sim.learned_h = True
+    recs = [sim.step(1e-4) for _ in range(max(1, args.steps // 5))]
+    r = recs[-1]
+    sim.ctx.close()
+    ms = statistics.mean(x["wall_s"] for x in recs) * 1e3
+    return {"metric": "particle force evals/s, clustered mixed box 2x%d^3 (gravity + SPH), learned h" % ng,
+            "value": n / (ms * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": len(recs), "warmup": 2,
+            "ms_per_step": ms, "higher_is_better": True, "dtype": "f32 gravity, f64 SPH",
+            "data": "synthetic two-lattice GRF box + 64 Plummer clumps, seed 6",
+            "config": {"workload": f"2x{ng}^3 periodic box, gas fraction 0.16, 20% in clumps, "
+                                   "Ewald, theta=0.7, nSmooth=32, learned h",
+                       "timing": "host wall clock per KDK step"},
+            "phases_ms": {"grav": r["t_grav_ms"], "density": r["t_knn_density_ms"],
+                          "pressure": r["t_pressure_ms"]},
+            "hnet_loss": loss, "seeded": r["density"]["bSeeded"]}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -285,7 +495,23 @@ def main():
     ap.add_argument("--ng", type=int, default=128)
     ap.add_argument("--ref-ng", type=int, default=64)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="box",
+                    choices=["box", "plummer", "collapse", "batched", "mixed"])
+    ap.add_argument("--collapse-n", type=int, default=262144)
+    ap.add_argument("--collapse-steps", type=int, default=200)
+    ap.add_argument("--collapse-dt", type=float, default=0.002)
+    ap.add_argument("--nsys", type=int, default=512)
+    ap.add_argument("--mixed-ng", type=int, default=256)
     args = ap.parse_args()
+    if args.workload != "box":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "workload": args.workload,
+                              "unavailable": "the reference arm is timed on the periodic box only"}))
+            return
+        fn = {"plummer": run_plummer, "collapse": run_collapse, "batched": run_batched,
+              "mixed": run_mixed}[args.workload]
+        print(json.dumps(fn(args)), flush=True)
+        return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))

@@ -180,3 +180,53 @@ def pack_systems(systems, u0=0.05):
         index.append(inv[off:off + n])
         off += n
     return pos, vel, mass, soft, ngas, u, sys_cat, index
+
+
+def _plummer_offsets(rng, n, a, rmax=20.0):
+    """n isotropic offsets with the Plummer radial profile of scale a."""
+    r = np.empty(n)
+    filled = 0
+    while filled < n:
+        X = rng.uniform(0.0, 1.0, 2 * (n - filled) + 16)
+        X = X[X > 0]
+        rr = 1.0 / np.sqrt(X ** (-2.0 / 3.0) - 1.0)
+        rr = rr[rr <= rmax]
+        k = min(len(rr), n - filled)
+        r[filled:filled + k] = rr[:k]
+        filled += k
+    return _iso_dirs(rng, n) * (r * a)[:, None]
+
+
+def mixed_box(ng=256, seed=6, index=-1.5, rms_frac=0.3, box=1.0, gas_frac=0.16,
+              nclump=64, clump_frac=0.2, amin=0.002, amax=0.02, u0=1e-3):
+    """Clustered periodic box of gas and dark matter: two interleaved ng^3
+    lattices (gas offset by half a spacing) displaced by one GRF with
+    P(k) ~ k^index (rms rms_frac of the spacing), then clump_frac of the
+    particles of each species moved into nclump Plummer clumps of scale
+    U[amin, amax] at random centres.  Gas holds gas_frac of the mass and
+    comes first.  Returns (pos, vel, mass, ngas, u)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    dx = box / ng
+    psi = _grf_displacement(ng, index, rms_frac * dx, seed, box)
+    g = (np.arange(ng) + 0.5) * dx - 0.5 * box
+    X, Y, Z = np.meshgrid(g, g, g, indexing="ij")
+    lat = np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1)
+    n = ng ** 3
+    gas = lat + 0.5 * dx + psi
+    dm = lat + psi
+    del lat, X, Y, Z
+    pos = np.concatenate([gas, dm])
+    del gas, dm
+    vel = np.concatenate([psi, psi])
+    centres = rng.uniform(-0.5 * box, 0.5 * box, (nclump, 3))
+    scales = rng.uniform(amin, amax, nclump)
+    for lo in (0, n):                      # each species in turn
+        sel = lo + np.nonzero(rng.uniform(0.0, 1.0, n) < clump_frac)[0]
+        cid = rng.integers(0, nclump, len(sel))
+        off = _plummer_offsets(rng, len(sel), 1.0)
+        pos[sel] = centres[cid] + off * scales[cid][:, None]
+        vel[sel] = 0.0
+    pos = (pos + 0.5 * box) % box - 0.5 * box
+    pos[pos >= 0.5 * box] -= box
+    mass = np.concatenate([np.full(n, gas_frac / n), np.full(n, (1.0 - gas_frac) / n)])
+    return pos, vel, mass, n, np.full(n, u0)
