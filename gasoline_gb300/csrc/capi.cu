@@ -96,7 +96,7 @@ extern "C" void tsph_destroy(tsph_ctx *ctx) {
     FREE(S.hax); FREE(S.hay); FREE(S.haz); FREE(S.uPdV); FREE(S.uAV); FREE(S.dtNew); FREE(S.mumax);
     FREE(S.seed); FREE(S.nnCount); FREE(S.nnHash); FREE(S.nodeBall2);
     FREE(S.nbrList); FREE(S.rcnt); FREE(S.roff); FREE(S.rcur); FREE(S.rlist); FREE(S.listFlag);
-    FREE(S.ph); FREE(S.ih2); FREE(S.fn1); FREE(S.pr2f);
+    FREE(S.ph); FREE(S.ih2); FREE(S.fn1); FREE(S.pr2f); FREE(S.pfa); FREE(S.pfb); FREE(S.pfc);
     FREE(ctx->dCnt); FREE(ctx->dBucketLists); FREE(ctx->dRoot); FREE(ctx->dEwt); FREE(ctx->dStage);
     FREE(ctx->dAux); FREE(ctx->dStepStatus);
     free(ctx->hSys);
@@ -145,6 +145,7 @@ int tsph_ensure_particles(tsph_ctx *ctx, int n) {
     rc |= tsph_grow(ctx, &S.rcur, cap); rc |= tsph_grow(ctx, &S.listFlag, 4);
     rc |= tsph_grow(ctx, &S.ph, cap); rc |= tsph_grow(ctx, &S.ih2, cap);
     rc |= tsph_grow(ctx, &S.fn1, cap); rc |= tsph_grow(ctx, &S.pr2f, cap);
+    rc |= tsph_grow(ctx, &S.pfa, cap); rc |= tsph_grow(ctx, &S.pfb, cap); rc |= tsph_grow(ctx, &S.pfc, cap);
     S.cap = cap;
     TsphBuildBufs &B = ctx->B;
     rc |= tsph_grow(ctx, &B.seg, cap); rc |= tsph_grow(ctx, &B.lt, cap); rc |= tsph_grow(ctx, &B.scan, cap);

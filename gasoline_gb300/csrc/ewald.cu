@@ -11,6 +11,7 @@
 // erf/erfc/exp/sin/cos are CUDA's own functions.
 #include <math.h>
 #include <stdlib.h>
+#include <string.h>
 
 #include "tsph_ctx.cuh"
 
@@ -25,12 +26,20 @@ struct EwMom {
     double xxzz, xyzz, xzzz, yyzz, yzzz, zzzz;
 };
 
+#define EW_MAXIMG 343   // (2*3+1)^3 images at fEwCut <= 3
+
 struct EwConst {
     EwMom mom;
     float momf[35];
     double L, alpha, alpha2, k1, ka, fEwCut2, smallR2;
     int nEwReps, nReps, nEwh, iOrder;
     double hx[EW_MAXH], hy[EW_MAXH], hz[EW_MAXH], hC[EW_MAXH], hS[EW_MAXH];
+    // FP32 copies of the k-space table for the FP32 kernel
+    float hxf[EW_MAXH], hyf[EW_MAXH], hzf[EW_MAXH], hCf[EW_MAXH], hSf[EW_MAXH];
+    // the real-space images (ix, iy, iz, hole) that can pass the cut for
+    // some particle of the box, in the reference's loop order
+    int nImg;
+    char4 img[EW_MAXIMG];
 };
 __constant__ EwConst cE;
 
@@ -225,21 +234,18 @@ __global__ void __launch_bounds__(128) k_ewald(TsphDevParts P, TsphDevCounters *
         const Real L = (Real)cE.L;
         const Real alpha2 = (Real)cE.alpha2, alpha = (Real)cE.alpha, ka = (Real)cE.ka;
         const Real fEwCut2 = (Real)cE.fEwCut2, smallR2 = (Real)cE.smallR2;
-        const int nEw = cE.nEwReps, nR = cE.nReps, iOrder = cE.iOrder;
+        const int iOrder = cE.iOrder;
         Real fPot = (Real)(cE.mom.m * cE.k1), ax = 0, ay = 0, az = 0;
         Real cpot = 0, cax = 0, cay = 0, caz = 0;   // compensations (FP32 only)
         Real dx = (Real)(P.x[p] - cE.mom.x);
         Real dy = (Real)(P.y[p] - cE.mom.y);
         Real dz = (Real)(P.z[p] - cE.mom.z);
-        for (int ix = -nEw; ix <= nEw; ++ix) {
-            bool hx = (ix >= -nR && ix <= nR);
-            Real dxo = dx + ix * L;
-            for (int iy = -nEw; iy <= nEw; ++iy) {
-                bool hxy = hx && iy >= -nR && iy <= nR;
-                Real dyo = dy + iy * L;
-                for (int iz = -nEw; iz <= nEw; ++iz) {
-                    bool hole = hxy && iz >= -nR && iz <= nR;
-                    Real dzo = dz + iz * L;
+        for (int q = 0; q < cE.nImg; ++q) {
+            {
+                {
+                    const char4 im = cE.img[q];
+                    const bool hole = im.w != 0;
+                    Real dxo = dx + im.x * L, dyo = dy + im.y * L, dzo = dz + im.z * L;
                     Real r2 = dxo * dxo + dyo * dyo + dzo * dzo;
                     if (r2 > fEwCut2 && !hole) continue;
                     Real gam[6];
@@ -313,8 +319,12 @@ __global__ void __launch_bounds__(128) k_ewald(TsphDevParts P, TsphDevCounters *
             }
         }
         for (int i = 0; i < cE.nEwh; ++i) {
-            Real hx = (Real)cE.hx[i], hy = (Real)cE.hy[i], hz = (Real)cE.hz[i];
-            Real hC = (Real)cE.hC[i], hS = (Real)cE.hS[i];
+            Real hx, hy, hz, hC, hS;
+            if constexpr (sizeof(Real) == 4) {
+                hx = cE.hxf[i]; hy = cE.hyf[i]; hz = cE.hzf[i]; hC = cE.hCf[i]; hS = cE.hSf[i];
+            } else {
+                hx = cE.hx[i]; hy = cE.hy[i]; hz = cE.hz[i]; hC = cE.hC[i]; hS = cE.hS[i];
+            }
             Real hdotx = hx * dx + hy * dy + hz * dz;
             Real s, c;
             sincos_r(hdotx, &s, &c);
@@ -466,6 +476,35 @@ int tsph_ewald(tsph_ctx *ctx, const tsph_grav_params *gp) {
             }
     E.nEwh = ih;
     ctx->nEwt = ih;
+    for (int i = 0; i < ih; ++i) {
+        E.hxf[i] = (float)E.hx[i]; E.hyf[i] = (float)E.hy[i]; E.hzf[i] = (float)E.hz[i];
+        E.hCf[i] = (float)E.hC[i]; E.hSf[i] = (float)E.hS[i];
+    }
+    // real-space images: a particle's offset from the root COM lies within
+    // max|coordinate| + |COM| per axis, so an image whose nearest point of
+    // that box is beyond fEwCut*L is never kept; the rest keep the
+    // reference's loop order
+    if (E.nEwReps > 3) return TSPH_ERR_UNSUPPORTED;
+    const double com[3] = {M.x, M.y, M.z};
+    double ext;
+    memcpy(&ext, &ctx->hCnt->maxAbs, sizeof(ext));
+    if (ext < 0.5 * L) ext = 0.5 * L;
+    int ni = 0;
+    for (int ix = -E.nEwReps; ix <= E.nEwReps; ++ix)
+        for (int iy = -E.nEwReps; iy <= E.nEwReps; ++iy)
+            for (int iz = -E.nEwReps; iz <= E.nEwReps; ++iz) {
+                const int id[3] = {ix, iy, iz};
+                double d2 = 0.0;
+                for (int k = 0; k < 3; ++k) {
+                    double s = ext + fabs(com[k]) + 1e-9 * L;
+                    double d = fabs(id[k] * L) - s;
+                    if (d > 0) d2 += d * d;
+                }
+                const bool hole = abs(ix) <= E.nReps && abs(iy) <= E.nReps && abs(iz) <= E.nReps;
+                if (d2 > E.fEwCut2 * (1.0 + 1e-9) && !hole) continue;
+                E.img[ni++] = make_char4((signed char)ix, (signed char)iy, (signed char)iz, hole ? 1 : 0);
+            }
+    E.nImg = ni;
     TSPH_CK(cudaMemcpyToSymbolAsync(cE, &E, sizeof(E), 0, cudaMemcpyHostToDevice, ctx->stream));
     const int BS = 128;
     if (gp->precision == TSPH_FP32) {

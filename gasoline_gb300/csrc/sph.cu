@@ -356,6 +356,7 @@ __device__ void density_epilogue(const SphArgs &A, KnnBatch &Bt, int cnt, int la
 // distance is bracketed from them, and only candidates whose interval
 // straddles the bracket get their FP64 distance.  The neighbour sums run
 // over N(i) in ascending index (FP64), so they depend on the set only.
+template <bool F32>
 __global__ void __launch_bounds__(SW * 32) k_knn_density(SphArgs A) {
     extern __shared__ __align__(16) unsigned char smraw[];
     KnnSmem &W = reinterpret_cast<KnnSmem *>(smraw)[threadIdx.x >> 5];
@@ -490,46 +491,105 @@ __global__ void __launch_bounds__(SW * 32) k_knn_density(SphArgs A) {
         // DenDVDX neighbour sums (smoothfcn.c:3390-3627) over N(i)
         const double vxi = A.S.vx[i], vyi = A.S.vy[i], vzi = A.S.vz[i];
         const double ih2 = 4.0 / fBall2;
-        double sm[14];
-#pragma unroll
-        for (int q = 0; q < 14; ++q) sm[q] = 0.0;
         unsigned long long hsh = 0ULL;
         for (int e = lane; e < nsel; e += 32) {
-            const int j = W.nbr[e];
-            unsigned long long hx = (unsigned long long)(A.G.iord[j] + 1);
+            unsigned long long hx = (unsigned long long)(A.G.iord[W.nbr[e]] + 1);
             hx *= 0x9E3779B97F4A7C15ULL;
             hx ^= hx >> 29;
             hx *= 0xBF58476D1CE4E5B9ULL;
             hx ^= hx >> 32;
             hsh += hx;
-            double dx, dy, dz;
-            const double d2 = dist2_exact(xi, yi, zi, A.G.x[j], A.G.y[j], A.G.z[j], dx, dy, dz);
-            double rs, rs1;
-            kern_dkern_m4(d2 * ih2, rs, rs1);
-            const double mj = A.G.m[j];
-            sm[0] += rs * mj;
-            rs1 *= mj;
-            double dvx = (-vxi + A.S.vx[j]), dvy = (-vyi + A.S.vy[j]), dvz = (-vzi + A.S.vz[j]);
-            sm[1] += dvx * dx * rs1; sm[2] += dvx * dy * rs1; sm[3] += dvx * dz * rs1;
-            sm[4] += dvy * dx * rs1; sm[5] += dvy * dy * rs1; sm[6] += dvy * dz * rs1;
-            sm[7] += dvz * dx * rs1; sm[8] += dvz * dy * rs1; sm[9] += dvz * dz * rs1;
-            sm[10] += (dx * dx + dy * dy + dz * dz) * rs1;
-            const double uj = A.S.u[j];
-            sm[11] += uj * dx * rs1;
-            sm[12] += uj * dy * rs1;
-            sm[13] += uj * dz * rs1;
         }
-        // fixed-order sums: the 14 x 32 partials transposed through shared
-        // memory, lane q adds quantity q's 32 partials in lane order
-#pragma unroll
-        for (int q = 0; q < 14; ++q) W.u.red[q][lane] = sm[q];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) hsh += __shfl_xor_sync(FULL, hsh, o);
-        __syncwarp();
-        if (lane < 14) {
-            double t = 0.0;
-            for (int l = 0; l < 32; ++l) t += W.u.red[lane][l];
-            Bt.s[lane][nb] = t;
+        if constexpr (!F32) {
+            double sm[14];
+#pragma unroll
+            for (int q = 0; q < 14; ++q) sm[q] = 0.0;
+            for (int e = lane; e < nsel; e += 32) {
+                const int j = W.nbr[e];
+                double dx, dy, dz;
+                const double d2 = dist2_exact(xi, yi, zi, A.G.x[j], A.G.y[j], A.G.z[j], dx, dy, dz);
+                double rs, rs1;
+                kern_dkern_m4(d2 * ih2, rs, rs1);
+                const double mj = A.G.m[j];
+                sm[0] += rs * mj;
+                rs1 *= mj;
+                double dvx = (-vxi + A.S.vx[j]), dvy = (-vyi + A.S.vy[j]), dvz = (-vzi + A.S.vz[j]);
+                sm[1] += dvx * dx * rs1; sm[2] += dvx * dy * rs1; sm[3] += dvx * dz * rs1;
+                sm[4] += dvy * dx * rs1; sm[5] += dvy * dy * rs1; sm[6] += dvy * dz * rs1;
+                sm[7] += dvz * dx * rs1; sm[8] += dvz * dy * rs1; sm[9] += dvz * dz * rs1;
+                sm[10] += (dx * dx + dy * dy + dz * dz) * rs1;
+                const double uj = A.S.u[j];
+                sm[11] += uj * dx * rs1;
+                sm[12] += uj * dy * rs1;
+                sm[13] += uj * dz * rs1;
+            }
+            // fixed-order sums: the 14 x 32 partials transposed through
+            // shared memory, lane q adds quantity q's 32 partials in order
+#pragma unroll
+            for (int q = 0; q < 14; ++q) W.u.red[q][lane] = sm[q];
+            __syncwarp();
+            if (lane < 14) {
+                double t = 0.0;
+                for (int l = 0; l < 32; ++l) t += W.u.red[lane][l];
+                Bt.s[lane][nb] = t;
+            }
+        } else {
+            // FP32 neighbour terms on split relative coordinates; FP64 only
+            // for the velocity differences (a bulk flow would otherwise
+            // swamp them); a fixed-order FP32 warp sum, widened for the
+            // FP64 epilogue
+            const float ih2f = (float)ih2;
+            float sm[14];
+#pragma unroll
+            for (int q = 0; q < 14; ++q) sm[q] = 0.0f;
+            for (int e = lane; e < nsel; e += 32) {
+                const int j = W.nbr[e];
+                const float4 hj = A.G.ph[j], lj = A.G.pl[j];
+                float dx = (hi_i.x - hj.x) + (lo_i.x - lj.x);
+                float dy = (hi_i.y - hj.y) + (lo_i.y - lj.y);
+                float dz = (hi_i.z - hj.z) + (lo_i.z - lj.z);
+                if (cS.bPeriodic) {
+                    const float L = (float)cS.L, h = 0.5f * L;
+                    dx = dx > h ? dx - L : (dx < -h ? dx + L : dx);
+                    dy = dy > h ? dy - L : (dy < -h ? dy + L : dy);
+                    dz = dz > h ? dz - L : (dz < -h ? dz + L : dz);
+                }
+                const float d2 = dx * dx + dy * dy + dz * dz;
+                const float ar2 = d2 * ih2f, r = sqrtf(ar2);
+                float rs, rs1;
+                if (ar2 < 1.0f) {
+                    rs = 1.0f - 0.75f * (2.0f - r) * ar2;
+                    rs1 = -3.0f + 2.25f * r;
+                } else {
+                    const float t = 2.0f - r;
+                    rs = 0.25f * t * t * t;
+                    rs1 = -0.75f * t * t / r;
+                }
+                const float mj = hj.w;
+                sm[0] += rs * mj;
+                rs1 *= mj;
+                const float dvx = (float)(A.S.vx[j] - vxi), dvy = (float)(A.S.vy[j] - vyi),
+                            dvz = (float)(A.S.vz[j] - vzi);
+                sm[1] += dvx * dx * rs1; sm[2] += dvx * dy * rs1; sm[3] += dvx * dz * rs1;
+                sm[4] += dvy * dx * rs1; sm[5] += dvy * dy * rs1; sm[6] += dvy * dz * rs1;
+                sm[7] += dvz * dx * rs1; sm[8] += dvz * dy * rs1; sm[9] += dvz * dz * rs1;
+                sm[10] += d2 * rs1;
+                const float uj = lj.w;
+                sm[11] += uj * dx * rs1;
+                sm[12] += uj * dy * rs1;
+                sm[13] += uj * dz * rs1;
+            }
+#pragma unroll
+            for (int q = 0; q < 14; ++q) {
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) sm[q] += __shfl_xor_sync(FULL, sm[q], o);
+            }
+            if (lane == 0) {
+#pragma unroll
+                for (int q = 0; q < 14; ++q) Bt.s[q][nb] = (double)sm[q];
+            }
         }
         if (lane == 0) {
             Bt.fb2[nb] = fBall2;
@@ -554,15 +614,15 @@ __global__ void __launch_bounds__(SW * 32) k_knn_density(SphArgs A) {
 }
 
 // FP32 hi/lo split of the gas positions (tree order) for the kNN intervals.
-__global__ void k_gas_split(int ng, TsphDevParts G) {
+__global__ void k_gas_split(int ng, TsphDevParts G, const double *__restrict__ u) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= ng) return;
     float hx, lx, hy, ly, hz, lz;
     split2f(G.x[i], hx, lx);
     split2f(G.y[i], hy, ly);
     split2f(G.z[i], hz, lz);
-    G.ph[i] = make_float4(hx, hy, hz, 0.0f);
-    G.pl[i] = make_float4(lx, ly, lz, 0.0f);
+    G.ph[i] = make_float4(hx, hy, hz, (float)G.m[i]);
+    G.pl[i] = make_float4(lx, ly, lz, (float)u[i]);
 }
 
 // pkdGasPressure (pkd.c:5750-5785) for the adiabatic gas model.
@@ -588,6 +648,10 @@ __global__ void k_gas_pressure(int ng, TsphSphBufs S) {
     S.ih2[i] = ih2;
     S.fn1[i] = fNorm * ih2;
     S.pr2f[i] = (S.pr2[i] * d2 + 0) / d2;
+    // FP32 copies for the FP32 pressure pass
+    S.pfa[i] = make_float4((float)ph, (float)ih2, (float)(fNorm * ih2), (float)S.pr2f[i]);
+    S.pfb[i] = make_float4((float)c, (float)rho, (float)S.bal[i], (float)dtp);
+    S.pfc[i] = make_float4((float)S.pr2[i], 0.0f, 0.0f, 0.0f);
 }
 
 // Reverse neighbour lists: count, fill, sort (ascending index).
@@ -707,9 +771,70 @@ __device__ __forceinline__ void sph_pair(const TsphSphBufs &S, const double *__r
     }
 }
 
+// sph_pair in FP32 (same terms and order); m_p, m_q come with the split
+// positions, dv is an FP64 difference rounded once.
+__device__ __forceinline__ void sph_pair_f(const TsphSphBufs &S, const TsphDevParts &G, int p, int q,
+                                           float dx, float dy, float dz, float fDist2, bool own,
+                                           float &ax, float &ay, float &az, float &uPdV,
+                                           float &uAV, float &mu, float &dtN) {
+    const float4 ap = S.pfa[p], bp = S.pfb[p], aq = S.pfa[q], bq = S.pfb[q];
+    const float pc = bp.x, qc = bq.x, ph = ap.x;
+    const float r2 = fDist2 * ap.y;
+    const float r = sqrtf(r2);
+    const float dk = r2 < 1.0f ? -3.0f + 2.25f * r : -0.75f * (2.0f - r) * (2.0f - r) / r;
+    const float rs1 = dk * ap.z;
+    const float rp = rs1 * G.ph[p].w, rq = rs1 * G.ph[q].w;
+    const float dvx = (float)(S.vx[p] - S.vx[q]), dvy = (float)(S.vy[p] - S.vy[q]),
+                dvz = (float)(S.vz[p] - S.vz[q]);
+    const float dvdotdr = dvx * dx + dvy * dy + dvz * dz;
+    float Acc, dt;
+    if (own) {
+        uPdV += rq * S.pfc[p].x * dvdotdr;
+        Acc = ap.w + aq.w;
+    } else {
+        uPdV += rp * S.pfc[q].x * dvdotdr;
+        Acc = aq.w + ap.w;
+    }
+    const float fac = (float)cS.dtFacCourant;
+    if (dvdotdr >= 0.0f) {
+        dt = fac * ph / (2 * fmaxf(pc, qc));
+    } else {
+        float absmu = -dvdotdr / sqrtf(fDist2);
+        if (absmu > mu) mu = absmu;
+        float visc = ((float)cS.alpha * (pc + qc) + (float)cS.beta * 1.5f * absmu);
+        dt = fac * ph / (0.625f * (pc + qc) + 0.375f * visc);
+        visc = (0.5f * (bp.z + bq.z)) * visc * absmu / (bp.y + bq.y);
+        uAV += (own ? rq : rp) * (0.5f * visc) * dvdotdr;
+        Acc += visc;
+    }
+    if (own) {
+        Acc *= rq;
+        ax -= Acc * dx; ay -= Acc * dy; az -= Acc * dz;
+        dtN = fminf(dtN, fminf(dt, 4 * bq.w));
+    } else {
+        Acc *= rp;
+        ax += Acc * dx; ay += Acc * dy; az += Acc * dz;
+        dtN = fminf(dtN, fminf(dt, 4 * bp.w));
+    }
+}
+
+__device__ __forceinline__ void split_dx(float4 hi, float4 lo, float4 hj, float4 lj, float &dx,
+                                         float &dy, float &dz) {
+    dx = (hi.x - hj.x) + (lo.x - lj.x);
+    dy = (hi.y - hj.y) + (lo.y - lj.y);
+    dz = (hi.z - hj.z) + (lo.z - lj.z);
+    if (cS.bPeriodic) {
+        const float L = (float)cS.L, h = 0.5f * L;
+        dx = dx > h ? dx - L : (dx < -h ? dx + L : dx);
+        dy = dy > h ? dy - L : (dy < -h ? dy + L : dy);
+        dz = dz > h ? dz - L : (dz < -h ? dz + L : dz);
+    }
+}
+
 // SphPressureTermsSym from the stored lists: particle i sums its own-ball
 // pairs N(i) and the pairs R(i) whose ball holds i, each list in ascending
 // index, lane-strided, then a fixed-order warp sum.  No tree walk.
+template <bool F32>
 __global__ void __launch_bounds__(SW * 32) k_pressure_lists(SphArgs A) {
     const int lane = threadIdx.x & 31;
     const unsigned FULL = 0xffffffffu;
@@ -721,6 +846,43 @@ __global__ void __launch_bounds__(SW * 32) k_pressure_lists(SphArgs A) {
         if (lane == 0) i = atomicAdd(A.work, 1);
         i = __shfl_sync(FULL, i, 0);
         if (i >= ng) break;
+        if constexpr (F32) {
+            const float4 hi = A.G.ph[i], lo = A.G.pl[i];
+            float ax = 0, ay = 0, az = 0, uPdV = 0, uAV = 0, mu = 0.0f, dtN = FLT_MAX;
+            const int *own = S.nbrList + (size_t)i * S.nbrCap;
+            const int nOwn = S.nnCount[i];
+            for (int e = lane; e < nOwn; e += 32) {
+                int j = own[e];
+                float dx, dy, dz;
+                split_dx(hi, lo, A.G.ph[j], A.G.pl[j], dx, dy, dz);
+                sph_pair_f(S, A.G, i, j, dx, dy, dz, dx * dx + dy * dy + dz * dz, true, ax, ay, az,
+                           uPdV, uAV, mu, dtN);
+            }
+            const int ro = i > 0 ? S.roff[i - 1] : 0, nRev = S.roff[i] - ro;
+            for (int e = lane; e < nRev; e += 32) {
+                int j = S.rlist[ro + e];
+                float dx, dy, dz;
+                split_dx(A.G.ph[j], A.G.pl[j], hi, lo, dx, dy, dz);
+                sph_pair_f(S, A.G, j, i, dx, dy, dz, dx * dx + dy * dy + dz * dz, false, ax, ay, az,
+                           uPdV, uAV, mu, dtN);
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                ax += __shfl_xor_sync(FULL, ax, o);
+                ay += __shfl_xor_sync(FULL, ay, o);
+                az += __shfl_xor_sync(FULL, az, o);
+                uPdV += __shfl_xor_sync(FULL, uPdV, o);
+                uAV += __shfl_xor_sync(FULL, uAV, o);
+                mu = fmaxf(mu, __shfl_xor_sync(FULL, mu, o));
+                dtN = fminf(dtN, __shfl_xor_sync(FULL, dtN, o));
+            }
+            if (lane == 0) {
+                S.hax[i] = ax; S.hay[i] = ay; S.haz[i] = az;
+                S.uPdV[i] = uPdV; S.uAV[i] = uAV; S.mumax[i] = mu;
+                S.dtNew[i] = dtN == FLT_MAX ? (double)FLT_MAX : (double)dtN;
+            }
+            continue;
+        }
         const double xi = A.G.x[i], yi = A.G.y[i], zi = A.G.z[i];
         double ax = 0, ay = 0, az = 0, uPdV = 0, uAV = 0, mu = 0.0, dtN = FLT_MAX;
         const int *own = S.nbrList + (size_t)i * S.nbrCap;
@@ -1044,10 +1206,10 @@ static int run_density(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_out
     if (rc) return rc;
     k_gas_nodes<<<tsph_blocks(ctx->TG.nNodes, 256), 256, 0, ctx->stream>>>(ctx->TG);
     TSPH_LAUNCH_CK("k_gas_nodes");
-    k_gas_split<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, ctx->G);
-    TSPH_LAUNCH_CK("k_gas_split");
     k_gas_gather_vel<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, ctx->C, ctx->G.iord, S);
     TSPH_LAUNCH_CK("k_gas_gather_vel");
+    k_gas_split<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, ctx->G, S.u);
+    TSPH_LAUNCH_CK("k_gas_split");
     if (!cap) set_sph_const(ctx, sp);
     const int kk = sp->nSmooth < ng ? sp->nSmooth : ng;
     if (!cap) {
@@ -1071,10 +1233,19 @@ static int run_density(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_out
     TSPH_CK(cudaMemsetAsync(S.listFlag, 0, sizeof(int), ctx->stream));
     if (!cap) cudaEventRecord(ctx->ev[6], ctx->stream);
     size_t sm = (sizeof(KnnSmem) + sizeof(KnnBatch)) * SW;
-    if (!cap)
-        TSPH_CK(cudaFuncSetAttribute(k_knn_density, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_knn_density<<<ctx->smCount * 3, SW * 32, sm, ctx->stream>>>(A);
-    TSPH_LAUNCH_CK("k_knn_density");
+    if (sp->precision == TSPH_FP32) {
+        if (!cap)
+            TSPH_CK(cudaFuncSetAttribute(k_knn_density<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)sm));
+        k_knn_density<true><<<ctx->smCount * 3, SW * 32, sm, ctx->stream>>>(A);
+        TSPH_LAUNCH_CK("k_knn_density<f32>");
+    } else {
+        if (!cap)
+            TSPH_CK(cudaFuncSetAttribute(k_knn_density<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)sm));
+        k_knn_density<false><<<ctx->smCount * 3, SW * 32, sm, ctx->stream>>>(A);
+        TSPH_LAUNCH_CK("k_knn_density<f64>");
+    }
     if (cap) {
         rc = tsph_fold_status(ctx);
         if (rc) return rc;
@@ -1152,8 +1323,13 @@ static int run_pressure(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_ou
     TSPH_CK(cudaMemsetAsync(ctx->dCnt, 0, sizeof(TsphDevCounters), ctx->stream));
     SphArgs AL = A;
     AL.work = S.listFlag + 2;
-    k_pressure_lists<<<ctx->smCount * 4, SW * 32, 0, ctx->stream>>>(AL);
-    TSPH_LAUNCH_CK("k_pressure_lists");
+    if (sp->precision == TSPH_FP32) {
+        k_pressure_lists<true><<<ctx->smCount * 4, SW * 32, 0, ctx->stream>>>(AL);
+        TSPH_LAUNCH_CK("k_pressure_lists<f32>");
+    } else {
+        k_pressure_lists<false><<<ctx->smCount * 4, SW * 32, 0, ctx->stream>>>(AL);
+        TSPH_LAUNCH_CK("k_pressure_lists<f64>");
+    }
     k_pressure<<<ctx->smCount * 4, SW * 32, 0, ctx->stream>>>(A);
     TSPH_LAUNCH_CK("k_pressure");
     k_scatter_hydro<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, ctx->G.iord, S, ctx->C);

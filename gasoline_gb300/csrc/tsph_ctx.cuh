@@ -60,6 +60,7 @@ struct TsphSphBufs {
     int *rcnt, *roff, *rcur, *rlist;
     int *listFlag;               // device: [0] = a list did not fit (use the tree walk)
     double *ph, *ih2, *fn1, *pr2f;   // per-particle kernel invariants of the pressure pass
+    float4 *pfa, *pfb, *pfc;         // FP32 copies: (ph, ih2, fn1, pr2f), (c, rho, bal, dtp), (pr2)
     int nFallback;
     bool haveDensity, havePressure, haveSeed;
     tsph_sph_params last;

@@ -99,6 +99,37 @@ def test_sph_fewer_particles_than_nsmooth(ctx, orc):
     assert np.array_equal(r["fBall2"], ref["fBall2"])
 
 
+# FP32 SPH arithmetic: neighbour sets and fBall2 stay exact, the sums and
+# pair terms carry FP32 rounding (32-64 terms per particle)
+F32_REL = 2e-5
+
+
+@pytest.mark.parametrize("periodic", [False, True])
+def test_sph_fp32_vs_fp64(ctx, periodic):
+    if periodic:
+        pos, vel, m = g.ics.lattice_box(24, seed=9)
+        u = np.full(len(m), 0.1)
+        sp64 = g.sph_params(nSmooth=32, periodic=True, L=1.0)
+    else:
+        pos, vel, m, u = g.ics.gas_sphere(20000, seed=33)
+        vel = np.random.default_rng(3).normal(0.0, 0.3, pos.shape) + 1.0   # bulk flow + dispersion
+        sp64 = g.sph_params(nSmooth=32)
+    soft = np.full(len(m), 0.01)
+    sp32 = g.SphParams.from_buffer_copy(sp64)
+    sp32.precision = g.FP32
+    r64 = run(ctx, pos, vel, m, soft, u, sp64)
+    h64 = ctx.get_neighbour_hash()
+    r32 = run(ctx, pos, vel, m, soft, u, sp32)
+    h32 = ctx.get_neighbour_hash()
+    assert np.array_equal(r32["fBall2"], r64["fBall2"])
+    assert np.array_equal(h32[0], h64[0]) and np.array_equal(h32[1], h64[1])
+    for name in ("fDensity", "divv", "ax", "ay", "az", "uDotPdV", "uDotAV", "dtNew", "mumax"):
+        a, b = r32[name], r64[name]
+        scale = np.max(np.abs(b))
+        err = np.max(np.abs(a - b)) / scale if scale > 0 else np.max(np.abs(a))
+        assert err <= F32_REL, (name, err)
+
+
 def test_sph_repeat_bit_identical(ctx):
     d = load("sph_sphere_2k")
     sp = sph_params_of(d, g)
