@@ -225,9 +225,12 @@ def run_ours(args, rank, world, local_rank):
                     "h2d_bytes_per_step": int(n * 5 * 8), "d2h_bytes_per_step": int(n * 3 * 8),
                     "ms_per_step": mse2e},
             "gpu_launches": int(launches32 // max(1, args.steps)) * args.steps,
-            "roofline": {"bound": "fp32", "kernel": "k_walk<float> (fused walk + P-P/P-C)",
+            "roofline": {"bound": "fp32", "kernel": f"k_walk<float, {NBUCKET}> (fused walk + P-P/P-C)",
                          "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                         "frac": (achieved / peak) if peak else None, "traffic": None,
+                         "frac": (achieved / peak) if peak else None,
+                         # dram__bytes_read.sum + dram__bytes_write.sum of this kernel,
+                         # one launch, ncu capture in profiles/k_walk_f32_box128.md
+                         "traffic": 1.70719488e8, "traffic_unit": "bytes per launch",
                          "flop_convention": "reference grav.c:246-247 (+,* = 1, 38 per P-P, "
                                             "76 per quadrupole cell)",
                          "walk_ms": walk_ms, "ewald_ms": ew_ms,
@@ -239,6 +242,10 @@ def run_ours(args, rank, world, local_rank):
             "precision_vs_fp64": {"rms": float(np.sqrt(np.mean(rel ** 2))),
                                   "p99": float(np.percentile(rel, 99)),
                                   "max": float(rel.max())},
+            # the theta = 0.7 tree's own error on this near-uniform box (the
+            # net force is a small residual of cancelling terms): FP64 and
+            # FP32 alike; a pairwise Ewald sum confirms theta = 0.3 as the
+            # reference (tests/test_gravity_gpu.py)
             "error_vs_fp64_theta_0.3": {
                 "fp32_theta_0.7": {"rms": float(np.sqrt(np.mean(e32 ** 2))),
                                    "p99": float(np.percentile(e32, 99))},
@@ -314,6 +321,55 @@ def _cuda_ms(fn, stream):
     e1.record(stream)
     e1.synchronize()
     return e0.elapsed_time(e1)
+
+
+def run_profile(args):
+    """The box's FP32 force evaluation alone, `steps` times after `warmup`
+    (no autotune, FP64 or error legs): the command the ncu summaries use."""
+    import torch
+    import gasoline_gb300 as g
+    stream = torch.cuda.Stream()
+    ctx = g.Context(0, stream=stream.cuda_stream)
+    pos, m, soft = workload(args.ng)
+    ctx.set_particles(pos, m, soft)
+    gp = g.grav_params(periodic=True, precision=g.FP32, nBucket=NBUCKET)
+    for _ in range(args.warmup):
+        ctx.grav_all(gp)
+    ph = []
+    for _ in range(args.steps):
+        ctx.grav_all(gp)
+        ph.append(ctx.timings())
+    ctx.close()
+    return {"profile": "box", "n_particles": len(m), "nBucket": NBUCKET,
+            "phase_ms": {k: statistics.mean(t[k] for t in ph)
+                         for k in ("build", "moments", "walk", "ewald", "total")}}
+
+
+def run_gas(args):
+    """One gravity + SPH force evaluation (density, pressure) of the 1/r gas
+    sphere, N = collapse_n, `steps` times: the SPH kernels' profiling case."""
+    import gasoline_gb300 as g
+    n = args.collapse_n
+    pos, vel, m, u = g.ics.gas_sphere(n, seed=41)
+    soft = np.full(n, 0.01)
+    ctx = g.Context(0)
+    ctx.set_particles(pos, m, soft)
+    ctx.set_velocities(vel, n, u)
+    sp = g.sph_params(nSmooth=32, precision=g.FP32 if args.sph_fp32 else g.FP64)
+    gp = g.grav_params(periodic=False, precision=g.FP32, nBucket=NBUCKET)
+    rows = []
+    for it in range(args.warmup + args.steps):
+        ctx.grav_all(gp)
+        tg = ctx.timings()
+        d = ctx.smooth(g.SMX_DENDVDX, sp)
+        ctx.smooth(g.SMX_SPHPRESSURETERMS, sp)
+        t = ctx.timings()
+        if it >= args.warmup:
+            rows.append({"grav": tg["total"], "knn_tree": t["knn"], "density": t["density"],
+                         "pressure": t["pressure"], "candidates_per_particle": d["dCandidates"] / n})
+    ctx.close()
+    return {"profile": "gas", "n_gas": n, "sph_precision": "fp32" if args.sph_fp32 else "fp64",
+            "phase_ms": {k: statistics.mean(r[k] for r in rows) for k in rows[0]}}
 
 
 def run_plummer(args):
@@ -484,7 +540,7 @@ def run_mixed(args):
     n = len(m)
     soft = np.full(n, 1.0 / (50.0 * ng))
     sim = Simulation(pos, vel, m, soft, ngas=ngas, u=u, periodic=True, L=1.0, nSmooth=32,
-                     precision=g.FP32)
+                     precision=g.FP32, sph_precision=g.FP32)
     sim.ctx.hnet_init(seed=3)
     sim.ctx.hnet_mode(collect=True)
     sim.forces()
@@ -499,7 +555,7 @@ def run_mixed(args):
     ms = statistics.mean(x["wall_s"] for x in recs) * 1e3
     return {"metric": "particle force evals/s, clustered mixed box 2x%d^3 (gravity + SPH), learned h" % ng,
             "value": n / (ms * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": len(recs), "warmup": 2,
-            "ms_per_step": ms, "higher_is_better": True, "dtype": "f32 gravity, f64 SPH",
+            "ms_per_step": ms, "higher_is_better": True, "dtype": "f32 gravity, f32 SPH",
             "data": "synthetic two-lattice GRF box + 64 Plummer clumps, seed 6",
             "config": {"workload": f"2x{ng}^3 periodic box, gas fraction 0.16, 20% in clumps, "
                                    "Ewald, theta=0.7, nSmooth=32, learned h",
@@ -519,20 +575,26 @@ def main():
     ap.add_argument("--ref-ng", type=int, default=64)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="box",
-                    choices=["box", "plummer", "collapse", "batched", "mixed"])
+                    choices=["box", "plummer", "collapse", "batched", "mixed", "gas"])
+    ap.add_argument("--profile", action="store_true",
+                    help="box FP32 evaluations only (the ncu capture command)")
+    ap.add_argument("--sph-fp32", action="store_true")
     ap.add_argument("--collapse-n", type=int, default=262144)
     ap.add_argument("--collapse-steps", type=int, default=200)
     ap.add_argument("--collapse-dt", type=float, default=0.002)
     ap.add_argument("--nsys", type=int, default=512)
     ap.add_argument("--mixed-ng", type=int, default=256)
     args = ap.parse_args()
+    if args.profile:
+        print(json.dumps(run_profile(args)), flush=True)
+        return
     if args.workload != "box":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "workload": args.workload,
                               "unavailable": "the reference arm is timed on the periodic box only"}))
             return
         fn = {"plummer": run_plummer, "collapse": run_collapse, "batched": run_batched,
-              "mixed": run_mixed}[args.workload]
+              "mixed": run_mixed, "gas": run_gas}[args.workload]
         print(json.dumps(fn(args)), flush=True)
         return
     rank = int(os.environ.get("RANK", "0"))

@@ -199,6 +199,17 @@ def direct(pos, mass, soft, targets, nthreads=8):
     return acc, pot
 
 
+def ewald_direct(pos, mass, soft, targets, L=1.0, nthreads=8):
+    """Exact periodic accelerations of `targets` by a pairwise Ewald sum
+    (orc_ewald_direct)."""
+    pos = _c64(pos, (-1, 3)); mass = _c64(mass); soft = _c64(soft)
+    q = np.ascontiguousarray(targets, dtype=np.int32)
+    acc = np.zeros((len(q), 3))
+    oracle().lib.orc_ewald_direct(len(mass), _d(pos), _d(mass), _d(soft), ctypes.c_double(L),
+                                  len(q), q.ctypes.data_as(_IP), _d(acc), nthreads)
+    return acc
+
+
 def v_sqrt1(r2):
     r2 = _c64(r2)
     out = np.zeros_like(r2)

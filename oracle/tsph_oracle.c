@@ -1752,3 +1752,68 @@ void orc_direct(int n, const double *pos, const double *mass, const double *soft
         pot[k] = p;
     }
 }
+
+/* Exact periodic accelerations by pairwise Ewald summation (not the
+ * reference's method: an independent check of the tree + Ewald result).
+ * For targets qidx[k], the force of every other particle j and all its
+ * images in a cube of side L: real space sum over images with
+ * alpha r < 6, erfc(alpha r)/r^2 + 2 alpha/sqrt(pi) e^-(alpha r)^2 / r
+ * radial profile, k space sum over k = 2 pi h / L, 0 < |h| <= hmax, with
+ * (4 pi / V) e^(-k^2 / 4 alpha^2) / k^2; the nearest image's Newtonian part
+ * is replaced by the reference's spline softening inside 2h (SPLINE,
+ * grav.h:74-101).  Test infrastructure for the periodic box. */
+void orc_ewald_direct(int n, const double *pos, const double *mass, const double *soft, double L,
+                      int nq, const int *qidx, double *acc, int nthreads) {
+    const double alpha = 2.0 / L, V = L * L * L;
+    const int nr = 4, hmax = 6;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+    for (int k = 0; k < nq; ++k) {
+        const int t = qidx[k];
+        double ax = 0, ay = 0, az = 0;
+        for (int j = 0; j < n; ++j) {
+            if (j == t) continue;
+            double d[3];
+            for (int c = 0; c < 3; ++c) {
+                double x = pos[3 * t + c] - pos[3 * j + c];
+                x -= L * floor(x / L + 0.5);          /* nearest image */
+                d[c] = x;
+            }
+            double fx = 0, fy = 0, fz = 0;
+            for (int ix = -nr; ix <= nr; ++ix)
+                for (int iy = -nr; iy <= nr; ++iy)
+                    for (int iz = -nr; iz <= nr; ++iz) {
+                        double rx = d[0] + ix * L, ry = d[1] + iy * L, rz = d[2] + iz * L;
+                        double r2 = rx * rx + ry * ry + rz * rz, r = sqrt(r2);
+                        if (alpha * r > 6.0) continue;
+                        double g = (erfc(alpha * r) + 2.0 * alpha * r / sqrt(M_PI) *
+                                    exp(-alpha * alpha * r2)) / (r2 * r);
+                        if (ix == 0 && iy == 0 && iz == 0) {
+                            double a, b;
+                            spline(r2, soft[t] + soft[j], &a, &b);
+                            g += b - 1.0 / (r2 * r);        /* softened nearest image */
+                        }
+                        fx -= g * rx; fy -= g * ry; fz -= g * rz;
+                    }
+            for (int hx = -hmax; hx <= hmax; ++hx)
+                for (int hy = -hmax; hy <= hmax; ++hy)
+                    for (int hz = -hmax; hz <= hmax; ++hz) {
+                        int h2 = hx * hx + hy * hy + hz * hz;
+                        if (h2 == 0 || h2 > hmax * hmax) continue;
+                        double kx = 2 * M_PI * hx / L, ky = 2 * M_PI * hy / L, kz = 2 * M_PI * hz / L;
+                        double k2 = kx * kx + ky * ky + kz * kz;
+                        double c = 4.0 * M_PI / V * exp(-k2 / (4.0 * alpha * alpha)) / k2 *
+                                   sin(kx * d[0] + ky * d[1] + kz * d[2]);
+                        fx -= c * kx; fy -= c * ky; fz -= c * kz;
+                    }
+            ax += mass[j] * fx;
+            ay += mass[j] * fy;
+            az += mass[j] * fz;
+        }
+        acc[3 * k] = ax;
+        acc[3 * k + 1] = ay;
+        acc[3 * k + 2] = az;
+    }
+}

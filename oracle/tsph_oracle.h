@@ -88,6 +88,11 @@ void orc_v_sqrt1(int n, const double *r2, double *a);
 void orc_direct(int n, const double *pos, const double *mass, const double *soft, int nq,
                 const int *qidx, double *acc, double *pot, int nthreads);
 
+/* Exact periodic accelerations (pairwise Ewald sum, box side L) of the
+ * targets qidx[0..nq): an independent check of tree + Ewald. */
+void orc_ewald_direct(int n, const double *pos, const double *mass, const double *soft, double L,
+                      int nq, const int *qidx, double *acc, int nthreads);
+
 #ifdef __cplusplus
 }
 #endif
