@@ -364,6 +364,11 @@ extern "C" int tsph_grav_all(tsph_ctx *ctx, const tsph_grav_params *gp, tsph_gra
     }
     int rc = cap ? TSPH_OK : read_status(ctx);
     if (rc) return rc;
+    {
+        double r;
+        memcpy(&r, &ctx->hCnt->maxAbs, sizeof(r));
+        ctx->coordScale = ctx->capLimit > 0 ? ctx->capLimit : r;
+    }
     ctx->dPeriodTree = gp->bPeriodic ? gp->dPeriod : 0.0;
     rc = tsph_build_tree(ctx, ctx->P, ctx->T, n, gp->nBucket);
     if (rc) return rc;

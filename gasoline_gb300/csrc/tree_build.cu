@@ -155,15 +155,10 @@ __global__ void k_roots(int nR, const int *__restrict__ rLo, const int *__restri
         ctl->nTop = nR;
         ctl->status = 0;
         ctl->nNodes = 0;
+        ctl->levF[0] = carry[0];
+        ctl->levStart[0] = 0;
+        ctl->levStart[1] = nR;
     }
-}
-
-__global__ void k_seg_init(int n, int *seg, const int *__restrict__ rid, const int *__restrict__ rHi,
-                           const int *__restrict__ rLo, int S) {
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n) return;
-    int r = rid[p];
-    seg[p] = (rHi[r] - rLo[r] + 1 > S) ? r : -1;
 }
 
 // Top-phase bounds over fixed chunks of each frontier node's particle range:
@@ -171,10 +166,15 @@ __global__ void k_seg_init(int n, int *seg, const int *__restrict__ rid, const i
 // a node of N particles costs N / TB_CHUNK atomics instead of one per warp.
 #define TB_CHUNK 4096
 #define TB_BS 256
-__global__ void k_chunk_count(int F, const int *__restrict__ f_node, const int *__restrict__ t_lo,
+// Top-phase kernels run over Fb >= F frontier slots (a host-side bound);
+// the frontier size F of level L lives on the device (ctl->levF[L]), so the
+// host launches levels without waiting for each one.
+__global__ void k_chunk_count(int Fb, int L, const TsphBuildCtl *__restrict__ ctl,
+                              const int *__restrict__ f_node, const int *__restrict__ t_lo,
                               const int *__restrict__ t_hi, int *cc) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= F) return;
+    if (k >= Fb) return;
+    if (k >= ctl->levF[L]) { cc[k] = 0; return; }
     int v = f_node[k];
     cc[k] = (t_hi[v] - t_lo[v] + TB_CHUNK) / TB_CHUNK;
 }
@@ -195,7 +195,7 @@ __global__ void __launch_bounds__(TB_BS) k_bounds_chunks(int F, const int *__res
                                                          const double *__restrict__ z, double *t_bnd) {
     __shared__ unsigned long long red[TB_BS / 32][6];
     const int b = blockIdx.x;
-    if (b >= cs[F - 1]) return;
+    if (b >= cs[F - 1]) return;          // F here is the slot bound; unused slots count 0
     int a = 0, e = F - 1;                  // first k with cs[k] > b
     while (a < e) {
         int c = (a + e) >> 1;
@@ -273,11 +273,13 @@ __device__ __forceinline__ bool decide_node(int v, int nBucket, int *t_lo, int *
 
 // Top-phase frontier: nodes of at most S particles become subtree tasks,
 // the others split here (or end as zero-extent leaves).
-__global__ void k_top_split(int F, const int *__restrict__ f_node, int S, int nBucket, int *t_lo,
-                            int *t_hi, int *t_dim, int *t_child, int *t_size, double *t_split,
-                            double *t_bnd, int *f_split, int *tasks, TsphBuildCtl *ctl) {
+__global__ void k_top_split(int Fb, int L, const int *__restrict__ f_node, int S, int nBucket,
+                            int *t_lo, int *t_hi, int *t_dim, int *t_child, int *t_size,
+                            double *t_split, double *t_bnd, int *f_split, int *tasks,
+                            TsphBuildCtl *ctl) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= F) return;
+    if (k >= Fb) return;
+    if (k >= ctl->levF[L]) { f_split[k] = 0; return; }
     int v = f_node[k];
     if (t_hi[v] - t_lo[v] + 1 <= S) {
         t_dim[v] = -2;                       // handed to a subtree task
@@ -289,24 +291,6 @@ __global__ void k_top_split(int F, const int *__restrict__ f_node, int S, int nB
     bool sp = decide_node(v, nBucket, t_lo, t_hi, t_dim, t_child, t_split, t_bnd);
     if (!sp) t_size[v] = 1;
     f_split[k] = sp ? 1 : 0;
-}
-
-__global__ void k_flag(const double *__restrict__ x, const double *__restrict__ y,
-                       const double *__restrict__ z, const int *__restrict__ seg,
-                       const int *__restrict__ t_dim, const double *__restrict__ t_split, int *lt,
-                       int n) {
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n) return;
-    int s = seg[p];
-    int v = 0;
-    if (s >= 0) {
-        int d = t_dim[s];
-        if (d >= 0) {
-            double r = d == 0 ? x[p] : (d == 1 ? y[p] : z[p]);
-            v = r < t_split[s] ? 1 : 0;
-        }
-    }
-    lt[p] = v;
 }
 
 // Smallest q in [a, b] with S[q] >= target (S non-decreasing).
@@ -329,41 +313,147 @@ __device__ __forceinline__ void swap_particles(double *x, double *y, double *z, 
     int ti = iord[p]; iord[p] = iord[q]; iord[q] = ti;
 }
 
-// Swap each misplaced pair of the Hoare partition: the left element of rank
-// t (t-th element >= fSplit in [lo, m)) with the right element of rank t
-// (t-th element < fSplit counted from hi downwards in [m, hi]).  S is an
-// inclusive scan of the flags that starts at particle `base`.
-__global__ void k_swap(double *x, double *y, double *z, double *m, double *h, int *iord,
-                       const int *__restrict__ seg, const int *__restrict__ t_dim,
-                       const int *__restrict__ t_lo, const int *__restrict__ t_hi,
-                       const int *__restrict__ lt, const int *__restrict__ S, int n) {
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n) return;
-    int s = seg[p];
-    if (s < 0 || t_dim[s] < 0 || lt[p]) return;
-    int lo = t_lo[s], hi = t_hi[s];
-    int Slo = lo > 0 ? S[lo - 1] : 0;
-    int mid = lo + (S[hi] - Slo);          // first index of the upper part
-    if (p >= mid) return;                  // already in place
-    int ltBefore = (p > 0 ? S[p - 1] : 0) - Slo;
-    int t = (p - lo) - ltBefore;           // rank among misplaced-left
-    int q = lower_bound_scan(S, mid, hi, S[hi] - t);
-    swap_particles(x, y, z, m, h, iord, p, q);
+// Frontier node of chunk b: the first k with cs[k] > b (cs = inclusive
+// scan of the per-node chunk counts).
+__device__ __forceinline__ int chunk_node(const int *__restrict__ cs, int Fb, int b) {
+    int a = 0, e = Fb - 1;
+    while (a < e) {
+        int c = (a + e) >> 1;
+        if (cs[c] > b) e = c; else a = c + 1;
+    }
+    return a;
 }
 
-__global__ void k_top_children(int F, const int *__restrict__ f_node, const int *__restrict__ f_split,
-                               const int *__restrict__ f_rank, const int *__restrict__ S, int nTop,
-                               int *t_lo, int *t_hi, int *t_child, double *t_bnd, int *nf_node,
-                               TsphBuildCtl *ctl) {
+// Partition flags (r[d] < fSplit) of one chunk of a split frontier node and
+// their in-chunk inclusive scan; ctot[b] = the chunk's count.  Warps take
+// contiguous runs and count with ballots; two passes over the chunk.
+__global__ void __launch_bounds__(TB_BS) k_flag_chunks(int Fb, int nChunkSlots,
+                                                       const int *__restrict__ f_node,
+                                                       const int *__restrict__ cs,
+                                                       const int *__restrict__ t_lo,
+                                                       const int *__restrict__ t_hi,
+                                                       const int *__restrict__ t_dim,
+                                                       const double *__restrict__ t_split,
+                                                       const double *__restrict__ x,
+                                                       const double *__restrict__ y,
+                                                       const double *__restrict__ z, int *scan,
+                                                       int *ctot) {
+    __shared__ int wt[TB_BS / 32];
+    const int b = blockIdx.x;
+    if (b >= nChunkSlots) return;
+    if (b >= cs[Fb - 1]) {
+        if (threadIdx.x == 0) ctot[b] = 0;
+        return;
+    }
+    const int k = chunk_node(cs, Fb, b);
+    const int v = f_node[k];
+    const int d = t_dim[v];
+    if (d < 0) {                          // a task or a leaf: nothing moves
+        if (threadIdx.x == 0) ctot[b] = 0;
+        return;
+    }
+    const int j = b - (k > 0 ? cs[k - 1] : 0);
+    const int p0 = t_lo[v] + j * TB_CHUNK, p1 = min(p0 + TB_CHUNK, t_hi[v] + 1);
+    const double fs = t_split[v];
+    const double *X = d == 0 ? x : (d == 1 ? y : z);
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int CW = TB_CHUNK / (TB_BS / 32);
+    const int w0 = p0 + w * CW, w1 = min(w0 + CW, p1);
+    int cnt = 0;
+    for (int base = w0; base < w1; base += 32) {
+        int p = base + lane;
+        cnt += __popc(__ballot_sync(0xffffffffu, p < w1 && X[p] < fs));
+    }
+    if (lane == 0) wt[w] = cnt;
+    __syncthreads();
+    int run = 0, tot = 0;
+#pragma unroll
+    for (int q = 0; q < TB_BS / 32; ++q) {
+        if (q < w) run += wt[q];
+        tot += wt[q];
+    }
+    const unsigned le = (lane == 31) ? 0xffffffffu : ((2u << lane) - 1u);
+    for (int base = w0; base < w1; base += 32) {
+        int p = base + lane;
+        unsigned bal = __ballot_sync(0xffffffffu, p < w1 && X[p] < fs);
+        if (p < w1) scan[p] = run + __popc(bal & le);
+        run += __popc(bal);
+    }
+    if (threadIdx.x == 0) ctot[b] = tot;
+}
+
+// Node-local inclusive count of flags up to particle q of node v, from the
+// in-chunk scans and the inclusive scan coff of the chunk counts.
+__device__ __forceinline__ int node_scan(const int *__restrict__ scan, const int *__restrict__ coff,
+                                         int first, int base, int lo, int q) {
+    const int c = first + (q - lo) / TB_CHUNK;
+    return scan[q] + (c > 0 ? coff[c - 1] : 0) - base;
+}
+
+// Hoare-partition swaps of one chunk: the left element of rank t (t-th
+// element >= fSplit in [lo, mid)) swaps with the right element of rank t
+// (t-th element < fSplit counted from hi downwards in [mid, hi]).
+__global__ void __launch_bounds__(TB_BS) k_swap_chunks(int Fb, const int *__restrict__ f_node,
+                                                       const int *__restrict__ cs,
+                                                       const int *__restrict__ coff,
+                                                       const int *__restrict__ t_lo,
+                                                       const int *__restrict__ t_hi,
+                                                       const int *__restrict__ t_dim,
+                                                       const int *__restrict__ scan, double *x,
+                                                       double *y, double *z, double *m, double *h,
+                                                       int *iord) {
+    const int b = blockIdx.x;
+    if (b >= cs[Fb - 1]) return;
+    const int k = chunk_node(cs, Fb, b);
+    const int v = f_node[k];
+    if (t_dim[v] < 0) return;
+    const int first = k > 0 ? cs[k - 1] : 0, last = cs[k] - 1;
+    const int base = first > 0 ? coff[first - 1] : 0;
+    const int lo = t_lo[v], hi = t_hi[v];
+    const int total = coff[last] - base;          // flags in the whole node
+    const int mid = lo + total;                    // first index of the upper part
+    const int j = b - first;
+    const int p0 = lo + j * TB_CHUNK, p1 = min(p0 + TB_CHUNK, hi + 1);
+    for (int p = p0 + threadIdx.x; p < p1 && p < mid; p += TB_BS) {
+        const int s = node_scan(scan, coff, first, base, lo, p);
+        const int sp = p == lo ? 0 : node_scan(scan, coff, first, base, lo, p - 1);
+        if (s != sp) continue;                     // r < fSplit: stays
+        const int t = (p - lo) - sp;               // rank among misplaced-left
+        const int target = total - t;
+        int a = mid, e = hi;
+        while (a < e) {
+            int c = (a + e) >> 1;
+            if (node_scan(scan, coff, first, base, lo, c) >= target) e = c; else a = c + 1;
+        }
+        swap_particles(x, y, z, m, h, iord, p, a);
+    }
+}
+
+__global__ void k_top_children(int Fb, int L, const int *__restrict__ f_node,
+                               const int *__restrict__ f_split, const int *__restrict__ f_rank,
+                               const int *__restrict__ cs, const int *__restrict__ coff,
+                               int topCap, int *t_lo, int *t_hi, int *t_child, double *t_bnd,
+                               int *nf_node, TsphBuildCtl *ctl) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k == 0) ctl->nTop = nTop + 2 * f_rank[F - 1];
-    if (k >= F || !f_split[k]) return;
+    const int nTop = ctl->levStart[L + 1];      // this level's children start here
+    if (k == 0) {
+        int nt = nTop + 2 * f_rank[Fb - 1];
+        if (nt > topCap) {
+            atomicOr(&ctl->status, 1 << TSPH_ERR_TREE_DEPTH);
+            nt = nTop;
+        }
+        ctl->levF[L + 1] = nt - nTop;
+        ctl->levStart[L + 2] = nt;
+        ctl->nTop = nt;
+    }
+    if (k >= Fb || k >= ctl->levF[L] || !f_split[k]) return;
     int v = f_node[k];
     int lo = t_lo[v], hi = t_hi[v];
-    int Slo = lo > 0 ? S[lo - 1] : 0;
-    int mid = lo + (S[hi] - Slo);
+    const int first = k > 0 ? cs[k - 1] : 0, last = cs[k] - 1;
+    const int mid = lo + coff[last] - (first > 0 ? coff[first - 1] : 0);
     int r = f_rank[k] - 1;
     int c = nTop + 2 * r;
+    if (c + 1 >= topCap) return;
     t_child[v] = c;
     t_lo[c] = lo;
     t_hi[c] = mid - 1;
@@ -373,20 +463,6 @@ __global__ void k_top_children(int F, const int *__restrict__ f_node, const int 
     key_init(t_bnd, c + 1);
     nf_node[2 * r] = c;
     nf_node[2 * r + 1] = c + 1;
-}
-
-__global__ void k_top_seg(int *seg, const int *__restrict__ t_dim, const int *__restrict__ t_child,
-                          const int *__restrict__ t_lo, int n) {
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n) return;
-    int s = seg[p];
-    if (s < 0) return;
-    if (t_dim[s] >= 0) {
-        int c = t_child[s];
-        seg[p] = p < t_lo[c + 1] ? c : c + 1;
-    } else {
-        seg[p] = -1;
-    }
 }
 
 // ---------------------------------------------------------------------------
@@ -854,6 +930,16 @@ __global__ void k_leaf_list(const TsphBuildCtl *__restrict__ ctl, const int *__r
 // ---------------------------------------------------------------------------
 // moments
 // ---------------------------------------------------------------------------
+// FP32 hi/lo copy of a node's centre of mass (w lanes are filled by k_open)
+__device__ __forceinline__ void store_com32(TsphDevTree &T, int i, double x, double y, double z) {
+    float hx, lx, hy, ly, hz, lz;
+    split2f(x, hx, lx);
+    split2f(y, hy, ly);
+    split2f(z, hz, lz);
+    T.wcomh[i] = make_float4(hx, hy, hz, 0.0f);
+    T.wcoml[i] = make_float4(lx, ly, lz, 0.0f);
+}
+
 // Mass, softening and centre of mass of an interior node from its two
 // children in the reference's order (pkd.c:2522-2547); the quadrupole by the
 // parallel-axis theorem (equal to the reference's direct sum up to
@@ -880,6 +966,7 @@ __device__ void combine_node(TsphDevTree &T, int i) {
     T.fSoft[i] = fSoft;
 #pragma unroll
     for (int j = 0; j < 3; ++j) T.r[3 * i + j] = r[j];
+    store_com32(T, i, r[0], r[1], r[2]);
     double q[6];
 #pragma unroll
     for (int k = 0; k < 6; ++k) q[k] = __ldcg(&T.Q[6 * l + k]) + __ldcg(&T.Q[6 * u + k]);
@@ -933,6 +1020,7 @@ __global__ void k_moments(TsphDevTree T, const double *__restrict__ x, const dou
     T.r[3 * i + 0] = r0;
     T.r[3 * i + 1] = r1;
     T.r[3 * i + 2] = r2;
+    store_com32(T, i, r0, r1, r2);
     double q[6] = {0, 0, 0, 0, 0, 0};
     for (int p = lo; p <= hi; ++p) {
         double fm = m[p];
@@ -962,38 +1050,75 @@ __global__ void k_zero_u64(unsigned long long *a, int n) {
     if (i < n) a[i] = 0ULL;
 }
 
-// Bmax of every node = max over its particles of |r - COM| (pkd.c:2086-2092).
-// Each particle descends from its tree's root to its leaf; max of d^2 is
-// taken on the raw bits (non-negative doubles order like their bit
-// patterns) and the square root taken once: sqrt is monotone, so this
-// equals the max of the per-particle square roots the reference takes.
-__global__ void k_bmax(int n, TsphDevTree T, const double *__restrict__ x,
-                       const double *__restrict__ y, const double *__restrict__ z,
-                       const int *__restrict__ rid, unsigned long long *maxd2) {
+// Bmax in two FP32 descents and few FP64 distances.  The squared distance
+// of particle p to the COM of node i is bracketed in FP32 from the hi/lo
+// splits ([lo, hi], per-axis error erel |d| + eabs); pass A takes each
+// node's max of lo, a lower bound of its Bmax^2; pass B computes the exact
+// FP64 distance (the reference's operations) only for particles whose hi
+// reaches that bound, the only ones that can attain the maximum.
+__device__ __forceinline__ void com_d2_interval(float4 ph, float4 pl, float4 ch, float4 cl, float eabs,
+                                                float &lo, float &hi) {
+    const float u = 5.9604645e-08f;
+    const float d[3] = {(ph.x - ch.x) + (pl.x - cl.x), (ph.y - ch.y) + (pl.y - cl.y),
+                        (ph.z - ch.z) + (pl.z - cl.z)};
+    lo = 0.0f;
+    hi = 0.0f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float ad = fabsf(d[a]), e = 4.0f * u * ad + eabs;
+        const float l = fmaxf(ad - e, 0.0f), h = ad + e;
+        lo += l * l;
+        hi += h * h;
+    }
+    lo *= 1.0f - 4.0f * u;
+    hi *= 1.0f + 4.0f * u;
+}
+
+__global__ void k_bmax_lo(int n, TsphDevTree T, const float4 *__restrict__ ph,
+                          const float4 *__restrict__ pl, const int *__restrict__ rid, float eabs,
+                          unsigned int *maxLo) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     bool live = p < n;
     int i = live ? T.sysRoot[rid[p]] : 0;
-    double px = live ? x[p] : 0.0, py = live ? y[p] : 0.0, pz = live ? z[p] : 0.0;
+    const float4 a = live ? ph[p] : make_float4(0, 0, 0, 0), b = live ? pl[p] : make_float4(0, 0, 0, 0);
     unsigned mask = __ballot_sync(0xffffffffu, live);
     while (mask) {
         if (live) {
-            double dx = xsub(px, T.r[3 * i]);
-            double dy = xsub(py, T.r[3 * i + 1]);
-            double dz = xsub(pz, T.r[3 * i + 2]);
-            double d2 = xadd(xadd(xmul(dx, dx), xmul(dy, dy)), xmul(dz, dz));
-            unsigned long long key = (unsigned long long)__double_as_longlong(d2);
+            float lo, hi;
+            com_d2_interval(a, b, T.wcomh[i], T.wcoml[i], eabs, lo, hi);
             unsigned grp = __match_any_sync(mask, i);
-            unsigned hiw = (unsigned)(key >> 32), low = (unsigned)key;
-            unsigned mh = __reduce_max_sync(grp, hiw);
-            unsigned ml = __reduce_max_sync(grp, hiw == mh ? low : 0u);
-            int leader = __ffs(grp) - 1;
-            if ((threadIdx.x & 31) == leader)
-                atomicMax(&maxd2[i], ((unsigned long long)mh << 32) | ml);
+            unsigned m = __reduce_max_sync(grp, __float_as_uint(lo));
+            if ((int)(threadIdx.x & 31) == __ffs(grp) - 1) atomicMax(&maxLo[i], m);
             int up = T.upper[i];
             if (up < 0) live = false;
             else i = (p >= T.pLower[up]) ? up : i + 1;
         }
         mask = __ballot_sync(0xffffffffu, live);
+    }
+}
+
+__global__ void k_bmax_exact(int n, TsphDevTree T, const double *__restrict__ x,
+                             const double *__restrict__ y, const double *__restrict__ z,
+                             const float4 *__restrict__ ph, const float4 *__restrict__ pl,
+                             const int *__restrict__ rid, float eabs,
+                             const unsigned int *__restrict__ maxLo, unsigned long long *maxd2) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    int i = T.sysRoot[rid[p]];
+    const float4 a = ph[p], b = pl[p];
+    for (;;) {
+        float lo, hi;
+        com_d2_interval(a, b, T.wcomh[i], T.wcoml[i], eabs, lo, hi);
+        if (hi >= __uint_as_float(maxLo[i])) {
+            double dx = xsub(x[p], T.r[3 * i]);
+            double dy = xsub(y[p], T.r[3 * i + 1]);
+            double dz = xsub(z[p], T.r[3 * i + 2]);
+            double d2 = xadd(xadd(xmul(dx, dx), xmul(dy, dy)), xmul(dz, dz));
+            atomicMax(&maxd2[i], (unsigned long long)__double_as_longlong(d2));
+        }
+        int up = T.upper[i];
+        if (up < 0) break;
+        i = (p >= T.pLower[up]) ? up : i + 1;
     }
 }
 
@@ -1055,6 +1180,7 @@ void tsph_free_tree(TsphDevTree &T) {
 
 void tsph_free_build(TsphBuildBufs &B) {
     TFREE(B.f_node[0]); TFREE(B.f_node[1]); TFREE(B.f_split); TFREE(B.f_rank); TFREE(B.tasks);
+    TFREE(B.chunkScan); TFREE(B.ctot); TFREE(B.coff);
     TFREE(B.t_lo); TFREE(B.t_hi); TFREE(B.t_dim); TFREE(B.t_child); TFREE(B.t_size);
     TFREE(B.t_pre); TFREE(B.t_root); TFREE(B.t_loc); TFREE(B.t_split); TFREE(B.t_bnd);
     TFREE(B.maxd2); TFREE(B.visit); TFREE(B.leafFlag); TFREE(B.leafScan); TFREE(B.ctl);
@@ -1122,6 +1248,9 @@ static int ensure_temp(tsph_ctx *ctx, int n, int nR) {
     rc |= tsph_grow(ctx, &B.f_split, topCap);
     rc |= tsph_grow(ctx, &B.f_rank, topCap);
     rc |= tsph_grow(ctx, &B.tasks, topCap);
+    rc |= tsph_grow(ctx, &B.chunkScan, topCap);
+    rc |= tsph_grow(ctx, &B.ctot, n / TB_CHUNK + topCap + 2);
+    rc |= tsph_grow(ctx, &B.coff, n / TB_CHUNK + topCap + 2);
     rc |= tsph_grow(ctx, &B.t_lo, tcap);
     rc |= tsph_grow(ctx, &B.t_hi, tcap);
     rc |= tsph_grow(ctx, &B.t_dim, tcap);
@@ -1225,58 +1354,73 @@ int tsph_build_tree(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, int n
                                          B.tasks, B.ctl);
     TSPH_LAUNCH_CK("k_roots");
     TSPH_CK(cudaMemsetAsync(B.t_root + B.topCap, 0xff, sizeof(int) * 2 * (size_t)n, ctx->stream));
-    // top phase
+    // top phase: levels are launched in batches; the frontier of each level
+    // is known on the device only, the host bounds it (every split node of
+    // a level holds more than S particles, so a level has at most 2n/S
+    // children) and looks at the true size every TOP_BATCH levels
+    const int TOP_BATCH = 4;
     int levelStart[TSPH_MAX_LEVELS + 2];
-    int nTop = nR, cur = 0, level = 0;
-    levelStart[0] = 0;
-    levelStart[1] = nR;
-    if (F > 0) {
-        k_seg_init<<<tsph_blocks(n, BS), BS, 0, ctx->stream>>>(n, B.seg, P.rid, T.rHi, T.rLo, S);
-        TSPH_LAUNCH_CK("k_seg_init");
-    }
-    while (F > 0) {
-        if (level + 1 >= TSPH_MAX_LEVELS) return TSPH_ERR_TREE_DEPTH;
-        k_chunk_count<<<tsph_blocks(F, BS), BS, 0, ctx->stream>>>(F, B.f_node[cur], B.t_lo, B.t_hi,
-                                                                   B.f_split);
+    int cur = 0, level = 0;
+    const int Fcap = 2 * (n / S) + 2;
+    int Fb = F;
+    while (Fb > 0) {
+        if (level + 2 >= TSPH_MAX_LEVELS) return TSPH_ERR_TREE_DEPTH;
+        const int slots = n / TB_CHUNK + Fb + 1;     // >= chunks of any frontier
+        k_chunk_count<<<tsph_blocks(Fb, BS), BS, 0, ctx->stream>>>(Fb, level, B.ctl, B.f_node[cur],
+                                                                    B.t_lo, B.t_hi, B.f_split);
         TSPH_LAUNCH_CK("k_chunk_count");
-        rc = tsph_scan_inclusive(ctx, B.f_split, B.f_rank, F);
+        rc = tsph_scan_inclusive(ctx, B.f_split, B.f_rank, Fb);
         if (rc) return rc;
-        k_bounds_chunks<<<n / TB_CHUNK + F + 1, TB_BS, 0, ctx->stream>>>(
-            F, B.f_node[cur], B.f_rank, B.t_lo, B.t_hi, P.x, P.y, P.z, B.t_bnd);
-        TSPH_LAUNCH_CK("k_bounds_chunks");
-        k_top_split<<<tsph_blocks(F, BS), BS, 0, ctx->stream>>>(
-            F, B.f_node[cur], S, nBucket, B.t_lo, B.t_hi, B.t_dim, B.t_child, B.t_size, B.t_split,
-            B.t_bnd, B.f_split, B.tasks, B.ctl);
-        TSPH_LAUNCH_CK("k_top_split");
-        k_flag<<<tsph_blocks(n, BS), BS, 0, ctx->stream>>>(P.x, P.y, P.z, B.seg, B.t_dim, B.t_split,
-                                                           B.lt, n);
-        TSPH_LAUNCH_CK("k_flag");
-        rc = tsph_scan_inclusive(ctx, B.lt, B.scan, n);
-        if (rc) return rc;
-        k_swap<<<tsph_blocks(n, BS), BS, 0, ctx->stream>>>(P.x, P.y, P.z, P.m, P.h, P.iord, B.seg,
-                                                           B.t_dim, B.t_lo, B.t_hi, B.lt, B.scan, n);
-        TSPH_LAUNCH_CK("k_swap");
-        rc = tsph_scan_inclusive(ctx, B.f_split, B.f_rank, F);
-        if (rc) return rc;
-        if (nTop + 2 * F > B.topCap) return TSPH_ERR_TREE_DEPTH;
-        k_top_children<<<tsph_blocks(F, BS), BS, 0, ctx->stream>>>(
-            F, B.f_node[cur], B.f_split, B.f_rank, B.scan, nTop, B.t_lo, B.t_hi, B.t_child, B.t_bnd,
-            B.f_node[1 - cur], B.ctl);
-        TSPH_LAUNCH_CK("k_top_children");
-        k_top_seg<<<tsph_blocks(n, BS), BS, 0, ctx->stream>>>(B.seg, B.t_dim, B.t_child, B.t_lo, n);
-        TSPH_LAUNCH_CK("k_top_seg");
-        TSPH_CK(cudaMemcpyAsync(B.hostCount, B.f_rank + (F - 1), sizeof(int), cudaMemcpyDeviceToHost,
+        TSPH_CK(cudaMemcpyAsync(B.chunkScan, B.f_rank, sizeof(int) * Fb, cudaMemcpyDeviceToDevice,
                                 ctx->stream));
-        TSPH_CK(cudaStreamSynchronize(ctx->stream));
-        int nSplit = B.hostCount[0];
-        nTop += 2 * nSplit;
-        if (nTop > B.topCap) return TSPH_ERR_TREE_DEPTH;
-        F = 2 * nSplit;
+        k_bounds_chunks<<<slots, TB_BS, 0, ctx->stream>>>(Fb, B.f_node[cur], B.chunkScan, B.t_lo,
+                                                          B.t_hi, P.x, P.y, P.z, B.t_bnd);
+        TSPH_LAUNCH_CK("k_bounds_chunks");
+        k_top_split<<<tsph_blocks(Fb, BS), BS, 0, ctx->stream>>>(
+            Fb, level, B.f_node[cur], S, nBucket, B.t_lo, B.t_hi, B.t_dim, B.t_child, B.t_size,
+            B.t_split, B.t_bnd, B.f_split, B.tasks, B.ctl);
+        TSPH_LAUNCH_CK("k_top_split");
+        k_flag_chunks<<<slots, TB_BS, 0, ctx->stream>>>(Fb, slots, B.f_node[cur], B.chunkScan,
+                                                        B.t_lo, B.t_hi, B.t_dim, B.t_split, P.x,
+                                                        P.y, P.z, B.scan, B.ctot);
+        TSPH_LAUNCH_CK("k_flag_chunks");
+        rc = tsph_scan_inclusive(ctx, B.ctot, B.coff, slots);
+        if (rc) return rc;
+        k_swap_chunks<<<slots, TB_BS, 0, ctx->stream>>>(Fb, B.f_node[cur], B.chunkScan, B.coff,
+                                                        B.t_lo, B.t_hi, B.t_dim, B.scan, P.x, P.y,
+                                                        P.z, P.m, P.h, P.iord);
+        TSPH_LAUNCH_CK("k_swap_chunks");
+        rc = tsph_scan_inclusive(ctx, B.f_split, B.f_rank, Fb);
+        if (rc) return rc;
+        k_top_children<<<tsph_blocks(Fb, BS), BS, 0, ctx->stream>>>(
+            Fb, level, B.f_node[cur], B.f_split, B.f_rank, B.chunkScan, B.coff, B.topCap, B.t_lo,
+            B.t_hi, B.t_child, B.t_bnd, B.f_node[1 - cur], B.ctl);
+        TSPH_LAUNCH_CK("k_top_children");
         cur = 1 - cur;
         ++level;
-        levelStart[level + 1] = nTop;
+        Fb = 2 * Fb < Fcap ? 2 * Fb : Fcap;
+        if (level % TOP_BATCH == 0) {
+            TSPH_CK(cudaMemcpyAsync(B.hostCount, &B.ctl->levF[level], sizeof(int),
+                                    cudaMemcpyDeviceToHost, ctx->stream));
+            TSPH_CK(cudaStreamSynchronize(ctx->stream));
+            if (B.hostCount[0] == 0) break;
+        }
     }
-    const int topLevels = level + 1;     // level 0 = the roots
+    // the true level table (levels after the last split launched empty)
+    int levF[TSPH_MAX_LEVELS + 2];
+    int topLevels = 1;
+    levelStart[0] = 0;
+    levelStart[1] = nR;
+    if (level > 0) {       // (a captured build has no top phase: level == 0)
+        TSPH_CK(cudaMemcpyAsync(levF, B.ctl->levF, sizeof(int) * (level + 1),
+                                cudaMemcpyDeviceToHost, ctx->stream));
+        TSPH_CK(cudaMemcpyAsync(levelStart, B.ctl->levStart, sizeof(int) * (level + 2),
+                                cudaMemcpyDeviceToHost, ctx->stream));
+        TSPH_CK(cudaStreamSynchronize(ctx->stream));
+        // level 0 holds the roots; level L >= 1 exists while levF[L] > 0
+        while (topLevels < level && levF[topLevels] > 0) ++topLevels;
+        if (topLevels == level && levF[level] > 0) return TSPH_ERR_TREE_DEPTH;
+    }
     B.topLevels = topLevels;
     // subtree phase
     BuildArgs A;
@@ -1350,14 +1494,21 @@ int tsph_tree_moments(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, dou
     TSPH_CK(cudaMemsetAsync(B.visit, 0, sizeof(int) * (size_t)nodeNeed, ctx->stream));
     k_moments<<<tsph_blocks(n, 128), 128, 0, ctx->stream>>>(T, P.x, P.y, P.z, P.m, P.h, B.visit);
     TSPH_LAUNCH_CK("k_moments");
+    k_parts32<<<tsph_blocks(n, BS), BS, 0, ctx->stream>>>(n, P.x, P.y, P.z, P.m, P.h, P.ph, P.pl);
+    TSPH_LAUNCH_CK("k_parts32");
     k_zero_u64<<<tsph_blocks(nodeNeed, BS), BS, 0, ctx->stream>>>(B.maxd2, nodeNeed);
     TSPH_LAUNCH_CK("k_zero_u64");
-    k_bmax<<<tsph_blocks(n, BS), BS, 0, ctx->stream>>>(n, T, P.x, P.y, P.z, P.rid, B.maxd2);
-    TSPH_LAUNCH_CK("k_bmax");
+    // the per-node arrival counters of k_moments are free again: max of lo
+    TSPH_CK(cudaMemsetAsync(B.visit, 0, sizeof(int) * (size_t)nodeNeed, ctx->stream));
+    const float eabs = (float)(ldexp(1.0, -43) * (ctx->coordScale > 0 ? ctx->coordScale : 1.0)) + 1e-30f;
+    unsigned int *maxLo = reinterpret_cast<unsigned int *>(B.visit);
+    k_bmax_lo<<<tsph_blocks(n, BS), BS, 0, ctx->stream>>>(n, T, P.ph, P.pl, P.rid, eabs, maxLo);
+    TSPH_LAUNCH_CK("k_bmax_lo");
+    k_bmax_exact<<<tsph_blocks(n, BS), BS, 0, ctx->stream>>>(n, T, P.x, P.y, P.z, P.ph, P.pl, P.rid,
+                                                             eabs, maxLo, B.maxd2);
+    TSPH_LAUNCH_CK("k_bmax_exact");
     const double twoOverSqrt3 = 2 / sqrt(3.0);
     k_open<<<tsph_blocks(nodeNeed, BS), BS, 0, ctx->stream>>>(T, B.maxd2, twoOverSqrt3, dTheta);
     TSPH_LAUNCH_CK("k_open");
-    k_parts32<<<tsph_blocks(n, BS), BS, 0, ctx->stream>>>(n, P.x, P.y, P.z, P.m, P.h, P.ph, P.pl);
-    TSPH_LAUNCH_CK("k_parts32");
     return TSPH_OK;
 }

@@ -14,6 +14,8 @@ struct TsphBuildCtl {
     int status;       // TSPH_ERR_* bits raised on the device
     int nNodes;       // nodes of the finished forest
     int pad[3];
+    int levF[TSPH_MAX_LEVELS + 2];      // top phase: frontier size of each level
+    int levStart[TSPH_MAX_LEVELS + 2];  // top phase: first temp id of each level
 };
 
 struct TsphBuildBufs {
@@ -27,6 +29,8 @@ struct TsphBuildBufs {
     int *f_node[2];   // top-phase frontier (temp ids), double-buffered
     int *f_split, *f_rank;
     int *tasks;       // subtree task roots (temp ids)
+    int *chunkScan;   // top phase: inclusive scan of the frontier nodes' chunk counts
+    int *ctot, *coff; // top phase: flags per chunk and their inclusive scan
     // temporary nodes: roots, then the top phase breadth first, then the
     // subtree slots of every task (a task over particles [lo, hi] owns
     // slots topCap + 2*lo ... topCap + 2*hi + 1)
@@ -121,6 +125,7 @@ struct tsph_ctx {
     bool haveParts, haveVel, haveTree, haveGrav;
     tsph_grav_params lastGrav;
     double dPeriodTree;
+    double coordScale;           // largest |coordinate| of the particles (or a captured bound)
 
     TsphHnet hnet;
 
