@@ -8,9 +8,10 @@
 // closing kick by dt/2.  In graph mode every launch of that sequence is
 // recorded once and the whole step replays as one graph launch: no host
 // round trip, no per-kernel launch cost, which is what many small systems
-// in one context need.  A captured build has no host-paced top phase
-// (every system is one subtree task) and fixed coordinate bounds; a
-// particle leaving them raises TSPH_ERR_BOUNDS and the next call recaptures.
+// in one context need.  A captured build runs a fixed number of top-phase
+// levels (its preparation's depth + 4; deeper nodes become subtree tasks)
+// and has fixed coordinate bounds; a particle leaving them raises
+// TSPH_ERR_BOUNDS and the next call recaptures.
 #include <math.h>
 #include <string.h>
 
@@ -113,8 +114,6 @@ extern "C" int tsph_step(tsph_ctx *ctx, double dt, const tsph_grav_params *gp,
     cudaSetDevice(ctx->device);
     if (!(flags & TSPH_STEP_GRAPH)) return step_body(ctx, dt, gp, sp);
     if (gp->bPeriodic || (sp && sp->bLearnedH)) return TSPH_ERR_UNSUPPORTED;
-    if (ctx->T.maxRange > TSPH_STEP_GRAPH_MAX_SYSTEM || ctx->TG.maxRange > TSPH_STEP_GRAPH_MAX_SYSTEM)
-        return TSPH_ERR_UNSUPPORTED;
     if (ctx->n == 0) return TSPH_OK;
     if (!graph_matches(ctx, dt, gp, sp)) {
         int rc = capture_step(ctx, dt, gp, sp);

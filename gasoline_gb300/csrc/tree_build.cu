@@ -829,6 +829,39 @@ __global__ void k_size(int a, int b, const int *__restrict__ t_child, int *t_siz
     t_size[v] = 1 + (c >= 0 ? t_size[c] + t_size[c + 1] : 0);
 }
 
+// the same over a top level whose range lives on the device (a captured
+// build does not know its levels on the host)
+__global__ void k_size_dev(int l, const TsphBuildCtl *__restrict__ ctl,
+                           const int *__restrict__ t_child, int *t_size) {
+    const int a = ctl->levStart[l], b = ctl->levStart[l + 1];
+    for (int v = a + blockIdx.x * blockDim.x + threadIdx.x; v < b; v += gridDim.x * blockDim.x) {
+        int c = t_child[v];
+        t_size[v] = 1 + (c >= 0 ? t_size[c] + t_size[c + 1] : 0);
+    }
+}
+
+__global__ void k_pre_dev(int l, const TsphBuildCtl *__restrict__ ctl, const int *__restrict__ t_child,
+                          const int *__restrict__ t_size, int *t_pre) {
+    const int a = ctl->levStart[l], b = ctl->levStart[l + 1];
+    for (int v = a + blockIdx.x * blockDim.x + threadIdx.x; v < b; v += gridDim.x * blockDim.x) {
+        int c = t_child[v];
+        if (c < 0) continue;
+        int pv = t_pre[v];
+        t_pre[c] = pv + 1;
+        t_pre[c + 1] = pv + 1 + t_size[c];
+    }
+}
+
+// Frontier nodes still unsplit when the top phase stops become subtree tasks.
+__global__ void k_frontier_to_tasks(int Fb, int L, const int *__restrict__ f_node, int *t_dim,
+                                    int *tasks, TsphBuildCtl *ctl) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= Fb || k >= ctl->levF[L]) return;
+    int v = f_node[k];
+    t_dim[v] = -2;
+    tasks[atomicAdd(&ctl->taskCount, 1)] = v;
+}
+
 // roots: trees are stored one after another in range order
 __global__ void k_root_pre(int nR, const int *__restrict__ t_size, int *t_pre, int *sysRoot,
                            int *rEnd, TsphBuildCtl *ctl) {
@@ -1315,9 +1348,6 @@ int tsph_set_ranges(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, int n
 static int task_size(tsph_ctx *ctx, const TsphDevTree &T) {
     int S = ctx->taskSize > 0 ? ctx->taskSize : ST_SCAP;
     if (S < 1024) S = 1024;
-    // a captured build cannot run the host-paced top phase: every tree is
-    // one task
-    if (ctx->capturing && S < T.maxRange) S = T.maxRange;
     return S;
 }
 
@@ -1363,8 +1393,14 @@ int tsph_build_tree(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, int n
     int cur = 0, level = 0;
     const int Fcap = 2 * (n / S) + 2;
     int Fb = F;
-    while (Fb > 0) {
-        if (level + 2 >= TSPH_MAX_LEVELS) return TSPH_ERR_TREE_DEPTH;
+    // a captured build runs a fixed number of levels (its preparation's
+    // depth + 4) with no host look; what is left becomes subtree tasks
+    const bool cap = ctx->capturing;
+    const int Lmax = cap ? (T.lastTopLevels + 4 < TSPH_MAX_LEVELS - 2 ? T.lastTopLevels + 4
+                                                                      : TSPH_MAX_LEVELS - 2)
+                         : TSPH_MAX_LEVELS - 2;
+    while (Fb > 0 && level < Lmax) {
+        if (!cap && level + 2 >= TSPH_MAX_LEVELS) return TSPH_ERR_TREE_DEPTH;
         const int slots = n / TB_CHUNK + Fb + 1;     // >= chunks of any frontier
         k_chunk_count<<<tsph_blocks(Fb, BS), BS, 0, ctx->stream>>>(Fb, level, B.ctl, B.f_node[cur],
                                                                     B.t_lo, B.t_hi, B.f_split);
@@ -1399,19 +1435,26 @@ int tsph_build_tree(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, int n
         cur = 1 - cur;
         ++level;
         Fb = 2 * Fb < Fcap ? 2 * Fb : Fcap;
-        if (level % TOP_BATCH == 0) {
+        if (!cap && level % TOP_BATCH == 0) {
             TSPH_CK(cudaMemcpyAsync(B.hostCount, &B.ctl->levF[level], sizeof(int),
                                     cudaMemcpyDeviceToHost, ctx->stream));
             TSPH_CK(cudaStreamSynchronize(ctx->stream));
             if (B.hostCount[0] == 0) break;
         }
     }
+    if (level > 0) {
+        k_frontier_to_tasks<<<tsph_blocks(Fb, BS), BS, 0, ctx->stream>>>(Fb, level, B.f_node[cur],
+                                                                         B.t_dim, B.tasks, B.ctl);
+        TSPH_LAUNCH_CK("k_frontier_to_tasks");
+    }
     // the true level table (levels after the last split launched empty)
     int levF[TSPH_MAX_LEVELS + 2];
     int topLevels = 1;
     levelStart[0] = 0;
     levelStart[1] = nR;
-    if (level > 0) {       // (a captured build has no top phase: level == 0)
+    if (cap) {
+        topLevels = level + 1;               // ranges stay on the device
+    } else if (level > 0) {
         TSPH_CK(cudaMemcpyAsync(levF, B.ctl->levF, sizeof(int) * (level + 1),
                                 cudaMemcpyDeviceToHost, ctx->stream));
         TSPH_CK(cudaMemcpyAsync(levelStart, B.ctl->levStart, sizeof(int) * (level + 2),
@@ -1421,6 +1464,7 @@ int tsph_build_tree(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, int n
         while (topLevels < level && levF[topLevels] > 0) ++topLevels;
         if (topLevels == level && levF[level] > 0) return TSPH_ERR_TREE_DEPTH;
     }
+    if (!cap) T.lastTopLevels = topLevels;
     B.topLevels = topLevels;
     // subtree phase
     BuildArgs A;
@@ -1442,16 +1486,28 @@ int tsph_build_tree(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, int n
     k_subtree<<<ctx->subtreeBlocks, ST_BS, ST_SMEM, ctx->stream>>>(A);
     TSPH_LAUNCH_CK("k_subtree");
     // numbering
+    const int levBound = nR > Fcap ? nR : Fcap;
     for (int l = topLevels - 1; l >= 0; --l) {
-        int a = levelStart[l], b = levelStart[l + 1];
-        k_size<<<tsph_blocks(b - a, BS), BS, 0, ctx->stream>>>(a, b, B.t_child, B.t_size);
+        if (cap) {
+            k_size_dev<<<tsph_blocks(levBound, BS), BS, 0, ctx->stream>>>(l, B.ctl, B.t_child,
+                                                                         B.t_size);
+        } else {
+            int a = levelStart[l], b = levelStart[l + 1];
+            k_size<<<tsph_blocks(b - a, BS), BS, 0, ctx->stream>>>(a, b, B.t_child, B.t_size);
+        }
         TSPH_LAUNCH_CK("k_size");
     }
     k_root_pre<<<1, 1024, 0, ctx->stream>>>(nR, B.t_size, B.t_pre, T.sysRoot, T.rEnd, B.ctl);
     TSPH_LAUNCH_CK("k_root_pre");
     for (int l = 0; l < topLevels; ++l) {
-        int a = levelStart[l], b = levelStart[l + 1];
-        k_pre<<<tsph_blocks(b - a, BS), BS, 0, ctx->stream>>>(a, b, B.t_child, B.t_size, B.t_pre);
+        if (cap) {
+            k_pre_dev<<<tsph_blocks(levBound, BS), BS, 0, ctx->stream>>>(l, B.ctl, B.t_child,
+                                                                        B.t_size, B.t_pre);
+        } else {
+            int a = levelStart[l], b = levelStart[l + 1];
+            k_pre<<<tsph_blocks(b - a, BS), BS, 0, ctx->stream>>>(a, b, B.t_child, B.t_size,
+                                                                  B.t_pre);
+        }
         TSPH_LAUNCH_CK("k_pre");
     }
     k_slot_pre<<<tsph_blocks(2 * (long long)n, BS), BS, 0, ctx->stream>>>(B.topCap, 2 * n, B.t_root,

@@ -82,6 +82,7 @@ struct TsphDevTree {
     int *rEnd;        // device: one past the last node of each tree
     int *dcnt;        // device: nNodes, nLeaves
     int rCap;
+    int lastTopLevels; // top-phase levels of the last host-paced build
     float4 *brec;     // per bucket: centre hi + soft max, centre lo + extent,
                       // box min - centre (+ n), box max - centre (FP32)
 };

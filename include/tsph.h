@@ -283,15 +283,13 @@ int tsph_get_tuning(tsph_ctx *ctx, tsph_tuning *t);
  * With TSPH_STEP_GRAPH the step's launches are captured once into a CUDA
  * graph (recaptured when dt, the parameters or the particle set change)
  * and each call replays it with one launch; graph mode takes isolated
- * (non-periodic) systems of at most TSPH_STEP_GRAPH_MAX_SYSTEM particles,
- * no learned h.  No reference counterpart for the graph: the reference
+ * (non-periodic) systems and no learned h.  No reference counterpart for the graph: the reference
  * drives the same sequence from its host loop.
  * tsph_step_status waits for the queued steps and returns the first error
  * any of them raised (TSPH_OK if none); TSPH_ERR_BOUNDS means a particle
  * moved beyond twice the extent the graph was captured for, and the next
  * tsph_step recaptures. */
 #define TSPH_STEP_GRAPH 1
-#define TSPH_STEP_GRAPH_MAX_SYSTEM 65536
 int tsph_step(tsph_ctx *ctx, double dt, const tsph_grav_params *gp,
               const tsph_sph_params *sp, int flags);
 int tsph_step_status(tsph_ctx *ctx);

@@ -167,6 +167,6 @@ def test_graph_step_equals_direct_steps():
     (sa, la), (sb, lb) = states
     for k in range(3):
         assert np.array_equal(sa[k], sb[k]), k
-    # a replay counts the kernels it runs: the direct step's, less the
-    # host-paced extras (scale reductions, timing) a captured step omits
-    assert 0 < lb <= la
+    # a replay counts the kernels it runs (the captured build's fixed top
+    # levels included, some of them empty)
+    assert lb > 0 and la > 0
