@@ -60,9 +60,25 @@ struct WalkSmem {
     int pp[PPF + 32 * NBT + NBT];
     int cn[CNB];
     int cs[CNB];
-    // staged entry data: P-P uses x,y,z,m,h ; cells use x,y,z,m,q0..q5,h
-    Real ex[PPF], ey[PPF], ez[PPF], em[PPF], eh[PPF];
-    Real q[6][CNF];
+    // staged entry data: P-P uses x,y,z,m,h ; cells use x,y,z,m,q0..q5,h.
+    // The FP32 walk packs them as float4 records (two or three vector
+    // loads per entry instead of five or eleven scalar ones).
+    union {
+        struct {
+            Real ex[PPF], ey[PPF], ez[PPF], em[PPF], eh[PPF];
+            Real q[6][CNF];
+        };
+        struct {
+            float4 r0[PPF];   // P-P and cells: x, y, z, m
+            union {
+                float rh[PPF];            // P-P: h
+                struct {
+                    float4 r1[CNF];       // cells: q0 q1 q2 q3
+                    float4 r2[CNF];       // cells: q4 q5 h -
+                };
+            };
+        };
+    };
     Real px[NBT], py[NBT], pz[NBT], pm[NBT], ph[NBT];
 };
 
@@ -231,14 +247,14 @@ __device__ __forceinline__ void stage_pp(WalkSmem<Real, NBT> &S, const TsphDevPa
     for (int e = lane; e < cnt; e += 32) {
         int ent = S.pp[e];
         int idx = ent >> 5, rep = ent & 31;
-        if (sizeof(Real) == 4) {
+        if constexpr (sizeof(Real) == 4) {
             float4 a = P.ph[idx], b = P.pl[idx];
             int r = rep == 31 ? cW.selfRep : rep;
-            S.ex[e] = (Real)(((a.x - bchx) + cW.offh[r][0]) + ((b.x - bclx) + cW.offl[r][0]));
-            S.ey[e] = (Real)(((a.y - bchy) + cW.offh[r][1]) + ((b.y - bcly) + cW.offl[r][1]));
-            S.ez[e] = (Real)(((a.z - bchz) + cW.offh[r][2]) + ((b.z - bclz) + cW.offl[r][2]));
-            S.em[e] = (Real)a.w;
-            S.eh[e] = (Real)b.w;
+            S.r0[e] = make_float4(((a.x - bchx) + cW.offh[r][0]) + ((b.x - bclx) + cW.offl[r][0]),
+                                  ((a.y - bchy) + cW.offh[r][1]) + ((b.y - bcly) + cW.offl[r][1]),
+                                  ((a.z - bchz) + cW.offh[r][2]) + ((b.z - bclz) + cW.offl[r][2]),
+                                  a.w);
+            S.rh[e] = b.w;
         } else {
             int r = rep == 31 ? cW.selfRep : rep;
             S.ex[e] = (Real)(P.x[idx] + cW.off[r][0]);
@@ -258,9 +274,17 @@ __device__ __forceinline__ void eval_pp(WalkSmem<Real, NBT> &S, int cnt, int i, 
     for (int e = slot; e < cnt; e += 32 / NBT) {
         int ent = S.pp[e];
         if ((ent & 31) == 31 && (ent >> 5) == bucketLo + i) continue;   // self
-        Real dx = xi - S.ex[e], dy = yi - S.ey[e], dz = zi - S.ez[e];
+        Real ex, ey, ez, me, he;
+        if constexpr (sizeof(Real) == 4) {
+            const float4 r = S.r0[e];
+            ex = r.x; ey = r.y; ez = r.z; me = r.w;
+            he = S.rh[e];
+        } else {
+            ex = S.ex[e]; ey = S.ey[e]; ez = S.ez[e]; me = S.em[e]; he = S.eh[e];
+        }
+        Real dx = xi - ex, dy = yi - ey, dz = zi - ez;
         Real d2 = dx * dx + dy * dy + dz * dz;
-        Real me = S.em[e], twoh = hi + S.eh[e];
+        Real twoh = hi + he;
         Real dir = rsq<Real>(d2);
         Real a, b;
         spline_m<Real>(dir, d2, twoh, a, b);
@@ -285,18 +309,19 @@ __device__ __forceinline__ void stage_cells(WalkSmem<Real, NBT> &S, const int *b
         int ent = buf[e];
         int c = ent >> 5, r = ent & 31;
         Real m, q[6], hc;
-        if (sizeof(Real) == 4) {
+        Real cx, cy, cz;
+        if constexpr (sizeof(Real) == 4) {
             float4 h4 = T.wcomh[c], l4 = T.wcoml[c];
             float4 m0 = T.wmom0[c], m1 = T.wmom1[c];
-            S.ex[e] = (Real)(((h4.x - bchx) + cW.offh[r][0]) + ((l4.x - bclx) + cW.offl[r][0]));
-            S.ey[e] = (Real)(((h4.y - bchy) + cW.offh[r][1]) + ((l4.y - bcly) + cW.offl[r][1]));
-            S.ez[e] = (Real)(((h4.z - bchz) + cW.offh[r][2]) + ((l4.z - bclz) + cW.offl[r][2]));
+            cx = ((h4.x - bchx) + cW.offh[r][0]) + ((l4.x - bclx) + cW.offl[r][0]);
+            cy = ((h4.y - bchy) + cW.offh[r][1]) + ((l4.y - bcly) + cW.offl[r][1]);
+            cz = ((h4.z - bchz) + cW.offh[r][2]) + ((l4.z - bclz) + cW.offl[r][2]);
             m = m0.x; q[0] = m0.y; q[1] = m0.z; q[2] = m0.w; q[3] = m1.x; q[4] = m1.y; q[5] = m1.z;
             hc = m1.w;
         } else {
-            S.ex[e] = (Real)(T.r[3 * c] + cW.off[r][0]);
-            S.ey[e] = (Real)(T.r[3 * c + 1] + cW.off[r][1]);
-            S.ez[e] = (Real)(T.r[3 * c + 2] + cW.off[r][2]);
+            cx = (Real)(T.r[3 * c] + cW.off[r][0]);
+            cy = (Real)(T.r[3 * c + 1] + cW.off[r][1]);
+            cz = (Real)(T.r[3 * c + 2] + cW.off[r][2]);
             m = (Real)T.fMass[c];
 #pragma unroll
             for (int k = 0; k < 6; ++k) q[k] = (Real)T.Q[6 * c + k];
@@ -308,10 +333,17 @@ __device__ __forceinline__ void stage_cells(WalkSmem<Real, NBT> &S, const int *b
             q[1] -= tr / Real(3.0);
             q[2] -= tr / Real(3.0);
         }
-        S.em[e] = m;
-        S.eh[e] = hc;
+        if constexpr (sizeof(Real) == 4) {
+            S.r0[e] = make_float4(cx, cy, cz, m);
+            S.r1[e] = make_float4(q[0], q[1], q[2], q[3]);
+            S.r2[e] = make_float4(q[4], q[5], hc, 0.0f);
+        } else {
+            S.ex[e] = cx; S.ey[e] = cy; S.ez[e] = cz;
+            S.em[e] = m;
+            S.eh[e] = hc;
 #pragma unroll
-        for (int k = 0; k < 6; ++k) S.q[k][e] = q[k];
+            for (int k = 0; k < 6; ++k) S.q[k][e] = q[k];
+        }
     }
 }
 
@@ -321,18 +353,25 @@ __device__ __forceinline__ void eval_newt(WalkSmem<Real, NBT> &S, int cnt, int i
                                           Acc<Real> &A) {
     Real xi = S.px[i], yi = S.py[i], zi = S.pz[i], mi = S.pm[i];
     for (int e = slot; e < cnt; e += 32 / NBT) {
-        Real dx = xi - S.ex[e], dy = yi - S.ey[e], dz = zi - S.ez[e];
+        Real cx, cy, cz, m, xx, yy, zz, xy, xz, yz;
+        if constexpr (sizeof(Real) == 4) {
+            const float4 a = S.r0[e], b = S.r1[e], c = S.r2[e];
+            cx = a.x; cy = a.y; cz = a.z; m = a.w;
+            xx = b.x; yy = b.y; zz = b.z; xy = b.w; xz = c.x; yz = c.y;
+        } else {
+            cx = S.ex[e]; cy = S.ey[e]; cz = S.ez[e]; m = S.em[e];
+            xx = S.q[0][e]; yy = S.q[1][e]; zz = S.q[2][e];
+            xy = S.q[3][e]; xz = S.q[4][e]; yz = S.q[5][e];
+        }
+        Real dx = xi - cx, dy = yi - cy, dz = zi - cz;
         Real d2 = dx * dx + dy * dy + dz * dz;
         Real g0 = rsq<Real>(d2);
         Real dir2 = g0 * g0;
         Real g1 = g0 * dir2;
         Real g2 = Real(3) * g1 * dir2;
         Real g3 = Real(5) * g2 * dir2;
-        Real m = S.em[e];
         Real Qta = 0, pot = 0, ax = 0, ay = 0, az = 0;
         if (iOrder >= 2) {
-            Real xx = S.q[0][e], yy = S.q[1][e], zz = S.q[2][e];
-            Real xy = S.q[3][e], xz = S.q[4][e], yz = S.q[5][e];
             Real Qmirx = xz * dz + xy * dy + xx * dx;
             Real Qmiry = yz * dz + xy * dx + yy * dy;
             Real Qmirz = yz * dy + xz * dx + zz * dz;
@@ -364,15 +403,22 @@ template <typename Real, int NBT>
 __device__ __forceinline__ void eval_soft(WalkSmem<Real, NBT> &S, int cnt, int i, int slot, Acc<Real> &A) {
     Real xi = S.px[i], yi = S.py[i], zi = S.pz[i], hi = S.ph[i], mi = S.pm[i];
     for (int e = slot; e < cnt; e += 32 / NBT) {
-        Real dx = xi - S.ex[e], dy = yi - S.ey[e], dz = zi - S.ez[e];
+        Real cx, cy, cz, m, xx, yy, zz, xy, xz, yz, hc;
+        if constexpr (sizeof(Real) == 4) {
+            const float4 r0 = S.r0[e], r1 = S.r1[e], r2 = S.r2[e];
+            cx = r0.x; cy = r0.y; cz = r0.z; m = r0.w;
+            xx = r1.x; yy = r1.y; zz = r1.z; xy = r1.w; xz = r2.x; yz = r2.y; hc = r2.z;
+        } else {
+            cx = S.ex[e]; cy = S.ey[e]; cz = S.ez[e]; m = S.em[e]; hc = S.eh[e];
+            xx = S.q[0][e]; yy = S.q[1][e]; zz = S.q[2][e];
+            xy = S.q[3][e]; xz = S.q[4][e]; yz = S.q[5][e];
+        }
+        Real dx = xi - cx, dy = yi - cy, dz = zi - cz;
         Real d2 = dx * dx + dy * dy + dz * dz;
-        Real twoh = hi + S.eh[e];
+        Real twoh = hi + hc;
         Real dir = rsq<Real>(d2);
         Real a, b, c, d;
         spline_q<Real>(dir, d2, twoh, a, b, c, d);
-        Real xx = S.q[0][e], yy = S.q[1][e], zz = S.q[2][e];
-        Real xy = S.q[3][e], xz = S.q[4][e], yz = S.q[5][e];
-        Real m = S.em[e];
         Real qirx = xx * dx + xy * dy + xz * dz;
         Real qiry = xy * dx + yy * dy + yz * dz;
         Real qirz = xz * dx + yz * dy + zz * dz;
