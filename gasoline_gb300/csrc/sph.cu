@@ -1356,7 +1356,8 @@ static int run_pressure(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_ou
 extern "C" int tsph_smooth(tsph_ctx *ctx, int smx_type, const tsph_sph_params *sp,
                            tsph_smooth_out *out) {
     if (!ctx || !sp) return TSPH_ERR_ARG;
-    if (smx_type != TSPH_SMX_DENDVDX && smx_type != TSPH_SMX_SPHPRESSURETERMS)
+    if (smx_type != TSPH_SMX_DENDVDX && smx_type != TSPH_SMX_SPHPRESSURETERMS &&
+        smx_type != TSPH_SMX_DENSITY)
         return TSPH_ERR_UNSUPPORTED;
     if (!ctx->haveParts || !ctx->haveVel) return TSPH_ERR_STATE;
     if (sp->nSmooth < 1 || sp->gamma <= 1.0) return TSPH_ERR_ARG;
@@ -1374,7 +1375,10 @@ extern "C" int tsph_smooth(tsph_ctx *ctx, int smx_type, const tsph_sph_params *s
             if (ctx->TG.hHi[r] - ctx->TG.hLo[r] + 1 < sp->nSmooth) return TSPH_ERR_ARG;
     }
     if (!ctx->capturing) ctx->sysVersion++;   // constants change: recapture a step graph
-    if (smx_type == TSPH_SMX_DENDVDX) return run_density(ctx, sp, out);
+    // SMX_DENSITY (Density, smoothfcn.c:239-256) is the density part of the
+    // same pass: the kNN fBall2 and fDensity = 1/pi ih^3 sum m_j W (the
+    // velocity-gradient fields come along)
+    if (smx_type == TSPH_SMX_DENDVDX || smx_type == TSPH_SMX_DENSITY) return run_density(ctx, sp, out);
     if (!ctx->S.haveDensity) return TSPH_ERR_STATE;
     return run_pressure(ctx, sp, out);
 }

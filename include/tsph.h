@@ -192,6 +192,8 @@ int tsph_get_lists(tsph_ctx *ctx, int *nBuckets, int *blist);
 /* Run one smooth pass over the gas particles:
  *   TSPH_SMX_DENDVDX: exact kNN smoothing lengths (fBall2 = nSmooth-th
  *     smallest squared distance, self included) and the DenDVDX gather;
+ *   TSPH_SMX_DENSITY: the same kNN and density (Density,
+ *     smoothfcn.c:239-256; the gradient fields come along);
  *   TSPH_SMX_SPHPRESSURETERMS: gas pressure (pkdGasPressure) and the
  *     symmetric pressure / artificial-viscosity terms over every pair with
  *     d^2 <= fBall2 of either particle.

@@ -139,6 +139,20 @@ def test_sph_repeat_bit_identical(ctx):
         assert np.array_equal(a[k], b[k]), k
 
 
+def test_smx_density_vs_reference_golden(ctx):
+    """SMX_DENSITY (the reference's Density) gives the kNN fBall2 and the
+    density of the DenDVDX pass."""
+    d = load("sph_sphere_2k")
+    sp = sph_params_of(d, g)
+    ctx.set_particles(d["pos"], d["mass"], d["soft"])
+    ctx.set_velocities(d["vel"], ngas=len(d["mass"]), u=d["u"])
+    ctx.smooth(g.SMX_DENSITY, sp)
+    r = ctx.get_sph()
+    assert np.array_equal(r["fBall2"], d["out"][:, FIELDS.index("fBall2")])
+    ref = d["out"][:, FIELDS.index("fDensity")]
+    assert np.max(np.abs(r["fDensity"] - ref)) / np.max(np.abs(ref)) <= REL
+
+
 def test_unsupported_smooth_type(ctx):
     d = load("sph_sphere_2k")
     ctx.set_particles(d["pos"], d["mass"], d["soft"])
