@@ -100,6 +100,8 @@ extern "C" void tsph_destroy(tsph_ctx *ctx) {
     FREE(ctx->dCnt); FREE(ctx->dBucketLists); FREE(ctx->dRoot); FREE(ctx->dEwt); FREE(ctx->dStage);
     FREE(ctx->dAux); FREE(ctx->dStepStatus);
     free(ctx->hSys);
+    free(ctx->hTmp);
+    free(ctx->hEw);
     if (ctx->graphExec) cudaGraphExecDestroy(ctx->graphExec);
     if (ctx->hCnt) cudaFreeHost(ctx->hCnt);
     if (ctx->B.hostCount) cudaFreeHost(ctx->B.hostCount);
@@ -244,6 +246,8 @@ extern "C" int tsph_set_particles(tsph_ctx *ctx, int n, const double *pos, const
     TSPH_LAUNCH_CK("k_load_state");
     TSPH_CK(cudaMemcpyAsync(ctx->C.m, mass, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
     TSPH_CK(cudaMemcpyAsync(ctx->C.h, soft, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    // the caller may reuse its (possibly pinned) buffers once this returns
+    TSPH_CK(cudaStreamSynchronize(ctx->stream));
     ctx->haveParts = true;
     return TSPH_OK;
 }

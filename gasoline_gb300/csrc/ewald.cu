@@ -413,7 +413,12 @@ int tsph_ewald(tsph_ctx *ctx, const tsph_grav_params *gp) {
     TSPH_CK(cudaMemcpyAsync(&node0[1], ctx->T.r, 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     TSPH_CK(cudaMemcpyAsync(&node0[4], ctx->T.Q, 6 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     TSPH_CK(cudaStreamSynchronize(ctx->stream));
-    static EwConst E;   // large; built on the host then copied
+    // the table (~32 KB) is built in a per-context host block, then copied
+    if (!ctx->hEw) {
+        ctx->hEw = malloc(sizeof(EwConst));
+        if (!ctx->hEw) return TSPH_ERR_NOMEM;
+    }
+    EwConst &E = *static_cast<EwConst *>(ctx->hEw);
     memset(&E, 0, sizeof(E));
     EwMom &M = E.mom;
     M.xxxx = h[0]; M.xyyy = h[1]; M.xxxy = h[2]; M.yyyy = h[3]; M.xxxz = h[4]; M.yyyz = h[5];
@@ -515,6 +520,6 @@ int tsph_ewald(tsph_ctx *ctx, const tsph_grav_params *gp) {
         TSPH_LAUNCH_CK("k_ewald<double>");
     }
     // (a pageable-source async copy returns once the source is staged, so
-    // the static host block may be reused by the next call)
+    // the host block may be reused by the next call)
     return TSPH_OK;
 }

@@ -1185,6 +1185,7 @@ extern "C" int tsph_set_velocities(tsph_ctx *ctx, const double *vel, int ngas, c
         int rc = tsph_apply_gas_systems(ctx);
         if (rc) return rc;
     }
+    TSPH_CK(cudaStreamSynchronize(ctx->stream));   // host buffers reusable on return
     ctx->haveVel = true;
     return TSPH_OK;
 }
@@ -1406,13 +1407,13 @@ extern "C" int tsph_get_sph(tsph_ctx *ctx, double *out16, double *dtNew, double 
                     ng, iord, src[f0 + f], strd[f0 + f], off[f0 + f], ctx->dStage, 3, f);
                 TSPH_LAUNCH_CK("k_to_caller1");
             }
-            static double *tmp = nullptr;
-            static size_t tmpN = 0;
-            if (tmpN < (size_t)3 * ng) {
-                free(tmp);
-                tmp = (double *)malloc(sizeof(double) * 3 * ng);
-                tmpN = (size_t)3 * ng;
+            if (ctx->hTmpN < (size_t)3 * ng) {
+                free(ctx->hTmp);
+                ctx->hTmp = (double *)malloc(sizeof(double) * 3 * ng);
+                ctx->hTmpN = ctx->hTmp ? (size_t)3 * ng : 0;
+                if (!ctx->hTmp) return TSPH_ERR_NOMEM;
             }
+            double *tmp = ctx->hTmp;
             TSPH_CK(cudaMemcpyAsync(tmp, ctx->dStage, sizeof(double) * 3 * ng, cudaMemcpyDeviceToHost,
                                     ctx->stream));
             TSPH_CK(cudaStreamSynchronize(ctx->stream));
@@ -1424,7 +1425,10 @@ extern "C" int tsph_get_sph(tsph_ctx *ctx, double *out16, double *dtNew, double 
     const double *srcs[2] = {S.dtNew, S.mumax};
     for (int k = 0; k < 2; ++k) {
         if (!arr[k] || ng == 0) continue;
-        if (!S.havePressure) return TSPH_ERR_STATE;
+        if (!S.havePressure) {               // set by the pressure pass; zero before it
+            memset(arr[k], 0, sizeof(double) * ng);
+            continue;
+        }
         k_to_caller1<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, iord, srcs[k], 1, 0,
                                                                     ctx->dStage, 1, 0);
         TSPH_LAUNCH_CK("k_to_caller1");

@@ -1301,6 +1301,19 @@ static int ensure_temp(tsph_ctx *ctx, int n, int nR) {
     return TSPH_OK;
 }
 
+// System (range) of every tree-order slot: the last range starting at or
+// before it.
+__global__ void k_fill_rid(int n, int nR, const int *__restrict__ rLo, int *rid) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    int a = 0, b = nR - 1;
+    while (a < b) {
+        int c = (a + b + 1) >> 1;
+        if (rLo[c] <= p) a = c; else b = c - 1;
+    }
+    rid[p] = a;
+}
+
 // The forest's trees: nR consecutive particle ranges of the given sizes
 // (each at least 1), in tree order.  A single system is one range.
 int tsph_set_ranges(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, int nR,
@@ -1322,25 +1335,28 @@ int tsph_set_ranges(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, int n
         T.rCap = nR;
     }
     if (!P.rid || ctx->B.cap < n) return TSPH_ERR_STATE;
-    int *hrid = (int *)malloc(sizeof(int) * (n > 0 ? n : 1));
-    if (!hrid) return TSPH_ERR_NOMEM;
     int lo = 0, mx = 0;
     for (int r = 0; r < nR; ++r) {
-        if (counts[r] < 1 || lo + counts[r] > n) { free(hrid); return TSPH_ERR_ARG; }
+        if (counts[r] < 1 || lo + counts[r] > n) return TSPH_ERR_ARG;
         T.hLo[r] = lo;
         T.hHi[r] = lo + counts[r] - 1;
-        for (int p = lo; p < lo + counts[r]; ++p) hrid[p] = r;
         mx = counts[r] > mx ? counts[r] : mx;
         lo += counts[r];
     }
-    if (lo != n) { free(hrid); return TSPH_ERR_ARG; }
+    if (lo != n) return TSPH_ERR_ARG;
     T.nR = nR;
     T.maxRange = mx;
-    cudaError_t e = cudaMemcpy(T.rLo, T.hLo, sizeof(int) * nR, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(T.rHi, T.hHi, sizeof(int) * nR, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && n > 0) e = cudaMemcpy(P.rid, hrid, sizeof(int) * n, cudaMemcpyHostToDevice);
-    free(hrid);
-    if (e != cudaSuccess) return tsph_cuda_fail(ctx, e, "tsph_set_ranges");
+    // the small range tables from the host, the per-slot system on the device
+    TSPH_CK(cudaMemcpyAsync(T.rLo, T.hLo, sizeof(int) * nR, cudaMemcpyHostToDevice, ctx->stream));
+    TSPH_CK(cudaMemcpyAsync(T.rHi, T.hHi, sizeof(int) * nR, cudaMemcpyHostToDevice, ctx->stream));
+    if (n > 0) {
+        if (nR == 1) {
+            TSPH_CK(cudaMemsetAsync(P.rid, 0, sizeof(int) * (size_t)n, ctx->stream));
+        } else {
+            k_fill_rid<<<tsph_blocks(n, 256), 256, 0, ctx->stream>>>(n, nR, T.rLo, P.rid);
+            TSPH_LAUNCH_CK("k_fill_rid");
+        }
+    }
     return TSPH_OK;
 }
 

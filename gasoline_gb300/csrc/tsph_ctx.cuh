@@ -130,6 +130,9 @@ struct tsph_ctx {
     TsphHnet hnet;
 
     unsigned long long *dAux;    // device scratch: [0] gas max |coordinate| bits
+    double *hTmp;                // host staging of tsph_get_sph
+    void *hEw;                   // host block of the Ewald constants
+    size_t hTmpN;
     double gasScale;             // last measured gas max |coordinate|
     // systems (forest): caller-order system id of every particle
     int nSys;

@@ -202,7 +202,9 @@ int tsph_smooth(tsph_ctx *ctx, int smx_type, const tsph_sph_params *sp,
                 tsph_smooth_out *out);
 /* SPH results in caller order for the gas particles: out[16*i] = fBall2,
  * fDensity, divv, curlv[3], dvds, BalsaraSwitch, diff, PoverRho2, c,
- * a_hydro[3], uDotPdV, uDotAV; dtNew[i]; mumax[i]. NULL skips. */
+ * a_hydro[3], uDotPdV, uDotAV; dtNew[i]; mumax[i]. NULL skips.  Fields of
+ * the pressure pass (PoverRho2 .. uDotAV, dtNew, mumax) are zero until it
+ * has run. */
 int tsph_get_sph(tsph_ctx *ctx, double *out16, double *dtNew, double *mumax);
 /* Neighbour-set fingerprint per gas particle: |N(i)| and an
  * order-independent hash of the caller indices in N(i). */

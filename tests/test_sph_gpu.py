@@ -158,7 +158,7 @@ def test_unsupported_smooth_type(ctx):
     ctx.set_particles(d["pos"], d["mass"], d["soft"])
     ctx.set_velocities(d["vel"], ngas=len(d["mass"]), u=d["u"])
     with pytest.raises(g.TsphError) as ei:
-        ctx.smooth(g.SMX_DENSITY, g.sph_params())
+        ctx.smooth(2, g.sph_params())        # a smooth type outside the path
     assert ei.value.code == 7
     with pytest.raises(g.TsphError) as ei:
         ctx.smooth(g.SMX_SPHPRESSURETERMS, g.sph_params())   # density first
