@@ -102,6 +102,22 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(x, world, device="cpu"):
+    """The largest of one float over all ranks (every rank gets it): the
+    job's time is its slowest replica's."""
+    import torch
+    t = torch.tensor([float(x)], device=device, dtype=torch.float64)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(n_per_rank, world, ms):
+    """Whole-job throughput of independent replicas: every rank's
+    particles over the slowest rank's time."""
+    return world * n_per_rank / (ms * 1e-3)
+
+
 def fma_peak_tflops(lib_ctx):
     """Measured FP32 FMA peak of this GPU (project microbenchmark)."""
     import ctypes
@@ -184,10 +200,7 @@ def run_ours(args, rank, world, local_rank):
     t64, w64, out64, _ = timed(gp64, k64, max(1, args.warmup // 3))
 
     def agg(ts):
-        ts = torch.tensor([sum(ts) / len(ts)], device=dev, dtype=torch.float64)
-        if world > 1:
-            torch.distributed.all_reduce(ts, op=torch.distributed.ReduceOp.MAX)
-        return float(ts.item())
+        return max_over_ranks(sum(ts) / len(ts), world, dev)
 
     ms32 = agg(t32)
     ms64 = agg(t64)
@@ -213,7 +226,7 @@ def run_ours(args, rank, world, local_rank):
         fgrav = out32["dFlop"] - out32["dFlopEwald"]
         peak = fma_peak_tflops(ctx)
         achieved = fgrav / (walk_ms * 1e-3) / 1e12
-        value = world * n / (ms32 * 1e-3)
+        value = replica_value(n, world, ms32)
         result = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms32,
@@ -221,7 +234,7 @@ def run_ours(args, rank, world, local_rank):
             "dtype": "f32", "data": "synthetic (seeded lattice + Gaussian random field)",
             "config": config(args.ng, nbucket=tuned["nBucket"]),
             "clocks": clk,
-            "e2e": {"value": world * n / (mse2e * 1e-3), "unit": UNIT,
+            "e2e": {"value": replica_value(n, world, mse2e), "unit": UNIT,
                     "h2d_bytes_per_step": int(n * 5 * 8), "d2h_bytes_per_step": int(n * 3 * 8),
                     "ms_per_step": mse2e},
             "gpu_launches": int(launches32 // max(1, args.steps)) * args.steps,
