@@ -28,7 +28,7 @@
 
 #define SW 4          // warps per block
 #define SSTK 1024     // walk stack per warp
-#define SCAP 640      // kNN candidate capacity per warp
+#define SCAP 384      // kNN candidate capacity per warp (more: the ball shrinks)
 #define SMAXIT 48     // radius iterations before giving up
 
 struct SphConst {
@@ -114,11 +114,13 @@ struct SphArgs {
     const double *seed;     // optional fBall2 seeds (tree order) or null
 };
 
-#define SNBR 256      // neighbours summed in canonical (index) order
+#define SNBR 192      // neighbours summed in canonical (index) order
+#define KSTK 896      // ball-gather walk stack per warp (the size of the sum transpose)
+#define KB 16         // finished particles per lane-parallel epilogue
 
 struct KnnSmem {
     union {
-        int stack[SSTK];          // ball-gather walk stack
+        int stack[KSTK];          // ball-gather walk stack
         double red[14][32];       // then: transpose of the 14 DenDVDX partial sums
     } u;
     float2 lh[SCAP];              // candidate squared-distance interval [lo, hi]; a
@@ -129,11 +131,11 @@ struct KnnSmem {
 
 // Finished particles of a warp awaiting the lane-parallel DenDVDX epilogue.
 struct KnnBatch {
-    double s[14][32];
-    double fb2[32];
-    unsigned long long hsh[32];
-    int id[32];
-    int nn[32];
+    double s[14][KB];
+    double fb2[KB];
+    unsigned long long hsh[KB];
+    int id[KB];
+    int nn[KB];
 };
 
 // Sort nbr[0, cnt) ascending (bitonic network over the next power of two,
@@ -227,7 +229,7 @@ __device__ int ball_gather(KnnSmem &W, const SphArgs &A, int lane, int root, flo
             }
         }
         unsigned bo = __ballot_sync(FULL, open);
-        if (sp + 2 * __popc(bo) > SSTK) { bad = true; break; }
+        if (sp + 2 * __popc(bo) > KSTK) { bad = true; break; }
         if (open) {
             int pos = sp + 2 * __popc(bo & lane_lt_s());
             W.u.stack[pos] = lk.z;
@@ -295,7 +297,7 @@ __device__ unsigned long long radix_select(int nc, int need, int lane, KeyOf key
     return prefix;
 }
 
-// The lane-parallel DenDVDX epilogue (smoothfcn.c:3390-3627) of up to 32
+// The lane-parallel DenDVDX epilogue (smoothfcn.c:3390-3627) of up to KB
 // finished particles: lane l finishes batch entry l.
 __device__ void density_epilogue(const SphArgs &A, KnnBatch &Bt, int cnt, int lane) {
     __syncwarp();
@@ -599,7 +601,7 @@ __global__ void __launch_bounds__(SW * 32) k_knn_density(SphArgs A) {
         }
         nPairs += nsel;
         ++nb;
-        if (nb == 32) {
+        if (nb == KB) {
             density_epilogue(A, Bt, nb, lane);
             nb = 0;
         }
@@ -1238,13 +1240,13 @@ static int run_density(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_out
         if (!cap)
             TSPH_CK(cudaFuncSetAttribute(k_knn_density<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)sm));
-        k_knn_density<true><<<ctx->smCount * 3, SW * 32, sm, ctx->stream>>>(A);
+        k_knn_density<true><<<ctx->smCount * 6, SW * 32, sm, ctx->stream>>>(A);
         TSPH_LAUNCH_CK("k_knn_density<f32>");
     } else {
         if (!cap)
             TSPH_CK(cudaFuncSetAttribute(k_knn_density<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)sm));
-        k_knn_density<false><<<ctx->smCount * 3, SW * 32, sm, ctx->stream>>>(A);
+        k_knn_density<false><<<ctx->smCount * 6, SW * 32, sm, ctx->stream>>>(A);
         TSPH_LAUNCH_CK("k_knn_density<f64>");
     }
     if (cap) {
