@@ -201,13 +201,6 @@ __global__ void k_scatter_grav(int n, TsphDevParts P, TsphDevState C) {
     C.dtGrav[o] = P.dtGrav[i];
 }
 
-__global__ void k_copy_by_order(int n, const double *__restrict__ src, const int *__restrict__ iord,
-                                double *dst) {
-    // dst[tree pos] = src[caller index]
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) dst[i] = src[iord[i]];
-}
-
 // Non-finite input, the coordinate scale of the walk's rounding bound, and
 // (for a captured step) particles beyond the bound the graph was built for.
 __global__ void k_check_finite(int n, TsphDevParts P, TsphDevCounters *cnt, double limit) {

@@ -86,12 +86,6 @@ __device__ __forceinline__ float box_d2f(float x, float y, float z, float4 lo, f
     return d2;
 }
 
-__device__ __forceinline__ double kern_m4(double ar2) {
-    double ak = 2.0 - sqrt(ar2);
-    if (ar2 < 1.0) ak = (1.0 - 0.75 * ak * ar2);
-    else ak = 0.25 * ak * ak * ak;
-    return ak;
-}
 __device__ __forceinline__ double dkern_m4(double ar2) {
     double adk = sqrt(ar2);
     if (ar2 < 1.0) adk = -3 + 2.25 * adk;

@@ -1361,8 +1361,14 @@ int tsph_set_ranges(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, int n
 }
 
 // Task size: the largest node handed whole to one CTA.
-static int task_size(tsph_ctx *ctx, const TsphDevTree &T) {
-    int S = ctx->taskSize > 0 ? ctx->taskSize : ST_SCAP;
+// By default, the shared-memory limit, lowered for small particle sets so
+// that there are tasks for every SM (about two per SM).
+static int task_size(tsph_ctx *ctx, const TsphDevTree &T, int n) {
+    int S = ctx->taskSize;
+    if (S <= 0) {
+        S = n / (2 * ctx->smCount);
+        if (S > ST_SCAP) S = ST_SCAP;
+    }
     if (S < 1024) S = 1024;
     return S;
 }
@@ -1392,7 +1398,7 @@ int tsph_build_tree(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, int n
     const int nodeNeed = 2 * n;
     rc = ensure_nodes(ctx, T, nodeNeed);
     if (rc) return rc;
-    const int S = task_size(ctx, T);
+    const int S = task_size(ctx, T, n);
     int F = 0;
     for (int r = 0; r < nR; ++r)
         if (T.hHi[r] - T.hLo[r] + 1 > S) ++F;
