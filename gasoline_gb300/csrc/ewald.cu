@@ -49,17 +49,21 @@ __constant__ EwConst cE;
 #define RM_BS 256
 #define RM_NV 25
 
+// Acc = double for the FP64 path; float for the FP32 path, whose kernel
+// uses the moments in FP32 anyway (offsets from the COM in FP64, then FP32
+// products and sums, FP64 per-block partials).
+template <typename Acc>
 __global__ void k_root_partial(int n, const double *__restrict__ x, const double *__restrict__ y,
                                const double *__restrict__ z, const double *__restrict__ m,
                                const double *__restrict__ rc, double *partial) {
-    __shared__ double sh[RM_NV][RM_BS / 32];
-    double acc[RM_NV];
+    __shared__ Acc sh[RM_NV][RM_BS / 32];
+    Acc acc[RM_NV];
 #pragma unroll
-    for (int k = 0; k < RM_NV; ++k) acc[k] = 0.0;
+    for (int k = 0; k < RM_NV; ++k) acc[k] = 0;
     double cx = rc[0], cy = rc[1], cz = rc[2];
     for (int p = blockIdx.x * RM_BS + threadIdx.x; p < n; p += gridDim.x * RM_BS) {
-        double mm = m[p], dx = x[p] - cx, dy = y[p] - cy, dz = z[p] - cz;
-        double dx2 = dx * dx, dy2 = dy * dy, dz2 = dz * dz;
+        Acc mm = (Acc)m[p], dx = (Acc)(x[p] - cx), dy = (Acc)(y[p] - cy), dz = (Acc)(z[p] - cz);
+        Acc dx2 = dx * dx, dy2 = dy * dy, dz2 = dz * dz;
         // hexadecapole (complete): xxxx xyyy xxxy yyyy xxxz yyyz xxyy xxyz xyyz xxzz xyzz xzzz yyzz yzzz zzzz
         acc[0] += mm * dx2 * dx2;
         acc[1] += mm * dx * dy2 * dy;
@@ -91,7 +95,7 @@ __global__ void k_root_partial(int n, const double *__restrict__ x, const double
     int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
     for (int k = 0; k < RM_NV; ++k) {
-        double v = acc[k];
+        Acc v = acc[k];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
         if (lane == 0) sh[k][w] = v;
@@ -99,7 +103,7 @@ __global__ void k_root_partial(int n, const double *__restrict__ x, const double
     __syncthreads();
     if (threadIdx.x < RM_NV) {
         double v = 0.0;
-        for (int j = 0; j < RM_BS / 32; ++j) v += sh[threadIdx.x][j];
+        for (int j = 0; j < RM_BS / 32; ++j) v += (double)sh[threadIdx.x][j];
         partial[blockIdx.x * RM_NV + threadIdx.x] = v;
     }
 }
@@ -401,9 +405,15 @@ int tsph_ewald(tsph_ctx *ctx, const tsph_grav_params *gp) {
     // root moments on the device
     int nb = 256;
     double *partial = ctx->dRoot + 64;
-    k_root_partial<<<nb, RM_BS, 0, ctx->stream>>>(n, ctx->P.x, ctx->P.y, ctx->P.z, ctx->P.m,
-                                                  ctx->T.r, partial);
-    TSPH_LAUNCH_CK("k_root_partial");
+    if (gp->precision == TSPH_FP32) {
+        k_root_partial<float><<<nb, RM_BS, 0, ctx->stream>>>(n, ctx->P.x, ctx->P.y, ctx->P.z,
+                                                             ctx->P.m, ctx->T.r, partial);
+        TSPH_LAUNCH_CK("k_root_partial<f32>");
+    } else {
+        k_root_partial<double><<<nb, RM_BS, 0, ctx->stream>>>(n, ctx->P.x, ctx->P.y, ctx->P.z,
+                                                              ctx->P.m, ctx->T.r, partial);
+        TSPH_LAUNCH_CK("k_root_partial<f64>");
+    }
     k_root_final<<<1, 32, 0, ctx->stream>>>(nb, partial, ctx->dRoot);
     TSPH_LAUNCH_CK("k_root_final");
     double h[25 + 11];

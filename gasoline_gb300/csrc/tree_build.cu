@@ -390,18 +390,19 @@ __device__ __forceinline__ int node_scan(const int *__restrict__ scan, const int
     return scan[q] + (c > 0 ? coff[c - 1] : 0) - base;
 }
 
-// Hoare-partition swaps of one chunk: the left element of rank t (t-th
-// element >= fSplit in [lo, mid)) swaps with the right element of rank t
-// (t-th element < fSplit counted from hi downwards in [mid, hi]).
-__global__ void __launch_bounds__(TB_BS) k_swap_chunks(int Fb, const int *__restrict__ f_node,
+// Hoare-partition swaps without searching: the left element of rank t
+// (t-th element >= fSplit in [lo, mid)) swaps with the right element of
+// rank t (t-th element < fSplit counted from hi downwards in [mid, hi]).
+// k_mark_chunks scatters both into rank-indexed lists (slot lo + t of mL
+// and mR), k_pair_chunks swaps list entry t of each.
+__global__ void __launch_bounds__(TB_BS) k_mark_chunks(int Fb, const int *__restrict__ f_node,
                                                        const int *__restrict__ cs,
                                                        const int *__restrict__ coff,
                                                        const int *__restrict__ t_lo,
                                                        const int *__restrict__ t_hi,
                                                        const int *__restrict__ t_dim,
-                                                       const int *__restrict__ scan, double *x,
-                                                       double *y, double *z, double *m, double *h,
-                                                       int *iord) {
+                                                       const int *__restrict__ scan, int *mL,
+                                                       int *mR) {
     const int b = blockIdx.x;
     if (b >= cs[Fb - 1]) return;
     const int k = chunk_node(cs, Fb, b);
@@ -414,19 +415,43 @@ __global__ void __launch_bounds__(TB_BS) k_swap_chunks(int Fb, const int *__rest
     const int mid = lo + total;                    // first index of the upper part
     const int j = b - first;
     const int p0 = lo + j * TB_CHUNK, p1 = min(p0 + TB_CHUNK, hi + 1);
-    for (int p = p0 + threadIdx.x; p < p1 && p < mid; p += TB_BS) {
-        const int s = node_scan(scan, coff, first, base, lo, p);
-        const int sp = p == lo ? 0 : node_scan(scan, coff, first, base, lo, p - 1);
-        if (s != sp) continue;                     // r < fSplit: stays
-        const int t = (p - lo) - sp;               // rank among misplaced-left
-        const int target = total - t;
-        int a = mid, e = hi;
-        while (a < e) {
-            int c = (a + e) >> 1;
-            if (node_scan(scan, coff, first, base, lo, c) >= target) e = c; else a = c + 1;
+    const int cbase = (b > 0 ? coff[b - 1] : 0) - base;   // flags before this chunk
+    for (int p = p0 + threadIdx.x; p < p1; p += TB_BS) {
+        const int s = scan[p] + cbase;             // node-local inclusive count
+        const int sp = p == p0 ? cbase : scan[p - 1] + cbase;
+        const bool flag = s != sp;                 // r < fSplit
+        if (p < mid) {
+            if (!flag) mL[lo + (p - lo) - sp] = p;          // misplaced left, rank (p-lo) - sp
+        } else if (flag) {
+            mR[lo + total - s] = p;                          // misplaced right, rank from hi
         }
-        swap_particles(x, y, z, m, h, iord, p, a);
     }
+}
+
+__global__ void __launch_bounds__(TB_BS) k_pair_chunks(int Fb, const int *__restrict__ f_node,
+                                                       const int *__restrict__ cs,
+                                                       const int *__restrict__ coff,
+                                                       const int *__restrict__ t_lo,
+                                                       const int *__restrict__ t_dim,
+                                                       const int *__restrict__ scan,
+                                                       const int *__restrict__ mL,
+                                                       const int *__restrict__ mR, double *x,
+                                                       double *y, double *z, double *m, double *h,
+                                                       int *iord) {
+    const int b = blockIdx.x;
+    if (b >= cs[Fb - 1]) return;
+    const int k = chunk_node(cs, Fb, b);
+    const int v = f_node[k];
+    if (t_dim[v] < 0) return;
+    const int first = k > 0 ? cs[k - 1] : 0, last = cs[k] - 1;
+    const int base = first > 0 ? coff[first - 1] : 0;
+    const int lo = t_lo[v];
+    const int total = coff[last] - base;
+    // misplaced pairs: the elements >= fSplit among the first `total`
+    const int nMis = total > 0 ? total - node_scan(scan, coff, first, base, lo, lo + total - 1) : 0;
+    const int j = b - first;
+    for (int t = j * TB_CHUNK + threadIdx.x; t < nMis && t < (j + 1) * TB_CHUNK; t += TB_BS)
+        swap_particles(x, y, z, m, h, iord, mL[lo + t], mR[lo + t]);
 }
 
 __global__ void k_top_children(int Fb, int L, const int *__restrict__ f_node,
@@ -1444,10 +1469,14 @@ int tsph_build_tree(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, int n
         TSPH_LAUNCH_CK("k_flag_chunks");
         rc = tsph_scan_inclusive(ctx, B.ctot, B.coff, slots);
         if (rc) return rc;
-        k_swap_chunks<<<slots, TB_BS, 0, ctx->stream>>>(Fb, B.f_node[cur], B.chunkScan, B.coff,
-                                                        B.t_lo, B.t_hi, B.t_dim, B.scan, P.x, P.y,
-                                                        P.z, P.m, P.h, P.iord);
-        TSPH_LAUNCH_CK("k_swap_chunks");
+        k_mark_chunks<<<slots, TB_BS, 0, ctx->stream>>>(Fb, B.f_node[cur], B.chunkScan, B.coff,
+                                                        B.t_lo, B.t_hi, B.t_dim, B.scan, B.lt,
+                                                        B.seg);
+        TSPH_LAUNCH_CK("k_mark_chunks");
+        k_pair_chunks<<<slots, TB_BS, 0, ctx->stream>>>(Fb, B.f_node[cur], B.chunkScan, B.coff,
+                                                        B.t_lo, B.t_dim, B.scan, B.lt, B.seg, P.x,
+                                                        P.y, P.z, P.m, P.h, P.iord);
+        TSPH_LAUNCH_CK("k_pair_chunks");
         rc = tsph_scan_inclusive(ctx, B.f_split, B.f_rank, Fb);
         if (rc) return rc;
         k_top_children<<<tsph_blocks(Fb, BS), BS, 0, ctx->stream>>>(
