@@ -454,6 +454,103 @@ __global__ void __launch_bounds__(TB_BS) k_pair_chunks(int Fb, const int *__rest
         swap_particles(x, y, z, m, h, iord, mL[lo + t], mR[lo + t]);
 }
 
+// ---- single-block forms of the per-level frontier work (one launch
+// instead of a kernel plus a multi-kernel scan when the frontier is small)
+#define LB_BS 1024
+#define LB_ITEMS 4
+#define LB_MAX (LB_BS * LB_ITEMS)
+
+// Inclusive scan of v[0, count) (count <= LB_MAX) by one 1024-thread block;
+// each thread owns LB_ITEMS consecutive items.
+__device__ void block_scan_items(int *v, int count) {
+    __shared__ int ws[LB_BS / 32];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    int a[LB_ITEMS], run = 0;
+#pragma unroll
+    for (int q = 0; q < LB_ITEMS; ++q) {
+        int i = t * LB_ITEMS + q;
+        run += i < count ? v[i] : 0;
+        a[q] = run;
+    }
+    int incl = run;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) ws[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        int x = ws[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        ws[lane] = x;
+    }
+    __syncthreads();
+    const int off = incl - run + (w > 0 ? ws[w - 1] : 0);
+#pragma unroll
+    for (int q = 0; q < LB_ITEMS; ++q) {
+        int i = t * LB_ITEMS + q;
+        if (i < count) v[i] = a[q] + off;
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(LB_BS) k_scan_small(int count, const int *__restrict__ in, int *out) {
+    for (int i = threadIdx.x; i < count; i += LB_BS) out[i] = in[i];
+    __syncthreads();
+    block_scan_items(out, count);
+}
+
+// chunk counts of the frontier nodes and their inclusive scan (Fb <= LB_MAX)
+__global__ void __launch_bounds__(LB_BS) k_level_chunks(int Fb, int L, const TsphBuildCtl *__restrict__ ctl,
+                                                        const int *__restrict__ f_node,
+                                                        const int *__restrict__ t_lo,
+                                                        const int *__restrict__ t_hi, int *cs) {
+    const int F = ctl->levF[L];
+    for (int k = threadIdx.x; k < Fb; k += LB_BS) {
+        int c = 0;
+        if (k < F) {
+            int v = f_node[k];
+            c = (t_hi[v] - t_lo[v] + TB_CHUNK) / TB_CHUNK;
+        }
+        cs[k] = c;
+    }
+    __syncthreads();
+    block_scan_items(cs, Fb);
+}
+
+// split decisions of the frontier (k_top_split) and the split ranks
+// (inclusive scan of the flags), one block (Fb <= LB_MAX)
+__global__ void __launch_bounds__(LB_BS) k_level_split(int Fb, int L, const int *__restrict__ f_node,
+                                                       int S, int nBucket, int *t_lo, int *t_hi,
+                                                       int *t_dim, int *t_child, int *t_size,
+                                                       double *t_split, double *t_bnd, int *f_split,
+                                                       int *f_rank, int *tasks, TsphBuildCtl *ctl) {
+    const int F = ctl->levF[L];
+    for (int k = threadIdx.x; k < Fb; k += LB_BS) {
+        int sp = 0;
+        if (k < F) {
+            int v = f_node[k];
+            if (t_hi[v] - t_lo[v] + 1 <= S) {
+                t_dim[v] = -2;                   // handed to a subtree task
+                key_init(t_bnd, v);
+                tasks[atomicAdd(&ctl->taskCount, 1)] = v;
+            } else {
+                sp = decide_node(v, nBucket, t_lo, t_hi, t_dim, t_child, t_split, t_bnd) ? 1 : 0;
+                if (!sp) t_size[v] = 1;
+            }
+        }
+        f_split[k] = sp;
+        f_rank[k] = sp;
+    }
+    __syncthreads();
+    block_scan_items(f_rank, Fb);
+}
+
 __global__ void k_top_children(int Fb, int L, const int *__restrict__ f_node,
                                const int *__restrict__ f_split, const int *__restrict__ f_rank,
                                const int *__restrict__ cs, const int *__restrict__ coff,
@@ -1449,26 +1546,44 @@ int tsph_build_tree(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, int n
     while (Fb > 0 && level < Lmax) {
         if (!cap && level + 2 >= TSPH_MAX_LEVELS) return TSPH_ERR_TREE_DEPTH;
         const int slots = n / TB_CHUNK + Fb + 1;     // >= chunks of any frontier
-        k_chunk_count<<<tsph_blocks(Fb, BS), BS, 0, ctx->stream>>>(Fb, level, B.ctl, B.f_node[cur],
-                                                                    B.t_lo, B.t_hi, B.f_split);
-        TSPH_LAUNCH_CK("k_chunk_count");
-        rc = tsph_scan_inclusive(ctx, B.f_split, B.f_rank, Fb);
-        if (rc) return rc;
-        TSPH_CK(cudaMemcpyAsync(B.chunkScan, B.f_rank, sizeof(int) * Fb, cudaMemcpyDeviceToDevice,
-                                ctx->stream));
+        const bool small = Fb <= LB_MAX;              // frontier work in single blocks
+        if (small) {
+            k_level_chunks<<<1, LB_BS, 0, ctx->stream>>>(Fb, level, B.ctl, B.f_node[cur], B.t_lo,
+                                                         B.t_hi, B.chunkScan);
+            TSPH_LAUNCH_CK("k_level_chunks");
+        } else {
+            k_chunk_count<<<tsph_blocks(Fb, BS), BS, 0, ctx->stream>>>(Fb, level, B.ctl,
+                                                                        B.f_node[cur], B.t_lo,
+                                                                        B.t_hi, B.f_split);
+            TSPH_LAUNCH_CK("k_chunk_count");
+            rc = tsph_scan_inclusive(ctx, B.f_split, B.chunkScan, Fb);
+            if (rc) return rc;
+        }
         k_bounds_chunks<<<slots, TB_BS, 0, ctx->stream>>>(Fb, B.f_node[cur], B.chunkScan, B.t_lo,
                                                           B.t_hi, P.x, P.y, P.z, B.t_bnd);
         TSPH_LAUNCH_CK("k_bounds_chunks");
-        k_top_split<<<tsph_blocks(Fb, BS), BS, 0, ctx->stream>>>(
-            Fb, level, B.f_node[cur], S, nBucket, B.t_lo, B.t_hi, B.t_dim, B.t_child, B.t_size,
-            B.t_split, B.t_bnd, B.f_split, B.tasks, B.ctl);
-        TSPH_LAUNCH_CK("k_top_split");
+        if (small) {
+            k_level_split<<<1, LB_BS, 0, ctx->stream>>>(
+                Fb, level, B.f_node[cur], S, nBucket, B.t_lo, B.t_hi, B.t_dim, B.t_child,
+                B.t_size, B.t_split, B.t_bnd, B.f_split, B.f_rank, B.tasks, B.ctl);
+            TSPH_LAUNCH_CK("k_level_split");
+        } else {
+            k_top_split<<<tsph_blocks(Fb, BS), BS, 0, ctx->stream>>>(
+                Fb, level, B.f_node[cur], S, nBucket, B.t_lo, B.t_hi, B.t_dim, B.t_child,
+                B.t_size, B.t_split, B.t_bnd, B.f_split, B.tasks, B.ctl);
+            TSPH_LAUNCH_CK("k_top_split");
+        }
         k_flag_chunks<<<slots, TB_BS, 0, ctx->stream>>>(Fb, slots, B.f_node[cur], B.chunkScan,
                                                         B.t_lo, B.t_hi, B.t_dim, B.t_split, P.x,
                                                         P.y, P.z, B.scan, B.ctot);
         TSPH_LAUNCH_CK("k_flag_chunks");
-        rc = tsph_scan_inclusive(ctx, B.ctot, B.coff, slots);
-        if (rc) return rc;
+        if (slots <= LB_MAX) {
+            k_scan_small<<<1, LB_BS, 0, ctx->stream>>>(slots, B.ctot, B.coff);
+            TSPH_LAUNCH_CK("k_scan_small");
+        } else {
+            rc = tsph_scan_inclusive(ctx, B.ctot, B.coff, slots);
+            if (rc) return rc;
+        }
         k_mark_chunks<<<slots, TB_BS, 0, ctx->stream>>>(Fb, B.f_node[cur], B.chunkScan, B.coff,
                                                         B.t_lo, B.t_hi, B.t_dim, B.scan, B.lt,
                                                         B.seg);
@@ -1477,8 +1592,10 @@ int tsph_build_tree(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, int n
                                                         B.t_lo, B.t_dim, B.scan, B.lt, B.seg, P.x,
                                                         P.y, P.z, P.m, P.h, P.iord);
         TSPH_LAUNCH_CK("k_pair_chunks");
-        rc = tsph_scan_inclusive(ctx, B.f_split, B.f_rank, Fb);
-        if (rc) return rc;
+        if (!small) {
+            rc = tsph_scan_inclusive(ctx, B.f_split, B.f_rank, Fb);
+            if (rc) return rc;
+        }
         k_top_children<<<tsph_blocks(Fb, BS), BS, 0, ctx->stream>>>(
             Fb, level, B.f_node[cur], B.f_split, B.f_rank, B.chunkScan, B.coff, B.topCap, B.t_lo,
             B.t_hi, B.t_child, B.t_bnd, B.f_node[1 - cur], B.ctl);
