@@ -150,7 +150,7 @@ def run_ours(args, rank, world, local_rank):
     from gasoline_gb300 import autotune
     tuned, _ = autotune.tune_gravity(ctx, g.grav_params(periodic=True, precision=g.FP32),
                                      nbuckets=(NBUCKET,), walk_blocks=(3, 4),
-                                     task_sizes=(0, 8192))
+                                     task_sizes=(0, 3072))
     gp32 = g.grav_params(periodic=True, precision=g.FP32, nBucket=tuned["nBucket"])
     gp64 = g.grav_params(periodic=True, precision=g.FP64, nBucket=tuned["nBucket"])
 

@@ -590,7 +590,7 @@ __global__ void k_top_children(int Fb, int L, const int *__restrict__ f_node,
 // ---------------------------------------------------------------------------
 // subtree phase: one CTA builds the whole subtree of a task, level by level
 // ---------------------------------------------------------------------------
-#define ST_BS 512
+#define ST_BS 256
 #define ST_W (ST_BS / 32)
 #define ST_MAXLEV 96
 
@@ -603,6 +603,7 @@ struct BuildArgs {
     const int *tasks;
     TsphBuildCtl *ctl;
     int topCap, nBucket;
+    int scap;             // tasks up to this size are staged in shared memory
 };
 
 __device__ __forceinline__ unsigned lanemask_lt_b() {
@@ -718,9 +719,10 @@ __device__ __forceinline__ int st_flag(const BuildArgs &A, const TaskView &V, in
 }
 
 #define ST_SCAP 3072      // largest task staged in shared memory
-#define ST_SMEM (ST_SCAP * (3 * sizeof(double) + 2 * sizeof(int) + sizeof(short)))
+#define ST_DEFAULT_TASK 1536   // default task size: ~52 KB of staging, 4 CTAs per SM
+#define ST_BYTES_PER (3 * sizeof(double) + 2 * sizeof(int) + sizeof(short))
 
-__global__ void __launch_bounds__(ST_BS) k_subtree(BuildArgs A) {
+__global__ void __launch_bounds__(ST_BS, 4) k_subtree(BuildArgs A) {
     extern __shared__ __align__(16) unsigned char stsm[];
     __shared__ int ws[ST_W];
     __shared__ int lvStart[ST_MAXLEV], lvCnt[ST_MAXLEV];
@@ -728,10 +730,11 @@ __global__ void __launch_bounds__(ST_BS) k_subtree(BuildArgs A) {
     const unsigned FULL = 0xffffffffu;
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     double *sx = reinterpret_cast<double *>(stsm);
-    double *sy = sx + ST_SCAP, *sz = sy + ST_SCAP;
-    int *sseg = reinterpret_cast<int *>(sz + ST_SCAP);
-    int *sscan = sseg + ST_SCAP;
-    short *sperm = reinterpret_cast<short *>(sscan + ST_SCAP);
+    const int scap = A.scap;            // staging capacity of this launch
+    double *sy = sx + scap, *sz = sy + scap;
+    int *sseg = reinterpret_cast<int *>(sz + scap);
+    int *sscan = sseg + scap;
+    short *sperm = reinterpret_cast<short *>(sscan + scap);
     for (;;) {
         if (threadIdx.x == 0) {
             int t = atomicAdd(&A.ctl->taskNext, 1);
@@ -746,7 +749,7 @@ __global__ void __launch_bounds__(ST_BS) k_subtree(BuildArgs A) {
         const int C = ((m + ST_BS - 1) / ST_BS) * 32;
         const int b0 = lo + w * C, b1 = min(b0 + C, hi + 1);
         TaskView V;
-        V.staged = m <= ST_SCAP;
+        V.staged = m <= scap;
         if (V.staged) {
             V.x = sx - lo; V.y = sy - lo; V.z = sz - lo;
             V.seg = sseg - lo; V.scan = sscan - lo; V.lt = nullptr; V.perm = sperm - lo;
@@ -1488,8 +1491,8 @@ int tsph_set_ranges(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, int n
 static int task_size(tsph_ctx *ctx, const TsphDevTree &T, int n) {
     int S = ctx->taskSize;
     if (S <= 0) {
-        S = n / (2 * ctx->smCount);
-        if (S > ST_SCAP) S = ST_SCAP;
+        S = n / (4 * ctx->smCount);
+        if (S > ST_DEFAULT_TASK) S = ST_DEFAULT_TASK;
     }
     if (S < 1024) S = 1024;
     return S;
@@ -1643,15 +1646,19 @@ int tsph_build_tree(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, int n
     A.t_split = B.t_split; A.t_bnd = B.t_bnd;
     A.tasks = B.tasks; A.ctl = B.ctl;
     A.topCap = B.topCap; A.nBucket = nBucket;
-    if (ctx->subtreeBlocks == 0) {
+    // shared memory sized to the task size (positions, flags, scan, order)
+    A.scap = S < ST_SCAP ? S : ST_SCAP;
+    const size_t smem = ((size_t)A.scap * ST_BYTES_PER + 15) & ~(size_t)15;
+    if (ctx->subtreeBlocks == 0 || ctx->subtreeSmem != smem) {
         if (ctx->capturing) return TSPH_ERR_STATE;
         TSPH_CK(cudaFuncSetAttribute(k_subtree, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)ST_SMEM));
+                                     (int)(ST_SCAP * ST_BYTES_PER)));
         int per = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_subtree, ST_BS, ST_SMEM);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_subtree, ST_BS, smem);
         ctx->subtreeBlocks = (per > 0 ? per : 1) * ctx->smCount;
+        ctx->subtreeSmem = smem;
     }
-    k_subtree<<<ctx->subtreeBlocks, ST_BS, ST_SMEM, ctx->stream>>>(A);
+    k_subtree<<<ctx->subtreeBlocks, ST_BS, smem, ctx->stream>>>(A);
     TSPH_LAUNCH_CK("k_subtree");
     // numbering
     const int levBound = nR > Fcap ? nR : Fcap;

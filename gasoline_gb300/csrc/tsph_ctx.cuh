@@ -141,6 +141,7 @@ struct tsph_ctx {
     // tree build tuning and mode
     int taskSize;                // largest node one CTA builds whole (0 = automatic)
     int subtreeBlocks;           // resident CTAs of the subtree kernel
+    size_t subtreeSmem;          // the dynamic shared memory they were sized for
     int walkBlocksPerSM;         // resident walk blocks per SM (0 = default)
     bool capturing;              // inside a CUDA graph capture: no host reads
     double capLimit;             // |coordinate| bound of the captured step (0 = none)
