@@ -40,6 +40,12 @@ struct EwConst {
     // some particle of the box, in the reference's loop order
     int nImg;
     char4 img[EW_MAXIMG];
+    // FP32 MEVAL coefficients: the moments pre-combined per monomial
+    // (c4: hexadecapole mirror over dx^3 .. dz^3, c3: octopole mirror over
+    // dx^2 .. dz^2, with MEVAL's 1/6, 1/2 and multiplicities folded in)
+    float c4[3][10], hQ[6], qtr4;
+    float c3[3][6], q3[3];
+    float q2[6], qtr2, m;
 };
 __constant__ EwConst cE;
 
@@ -207,6 +213,71 @@ __device__ __forceinline__ void meval(int iOrder, const MomR<Real> &mom, const R
     az -= dz * Qta;
 }
 
+// MEVAL (meval.h:21-81) in FP32 from the pre-combined coefficients: the
+// same terms, each multipole's mirror a dot product over the monomials of
+// (dx, dy, dz) formed once.
+__device__ __forceinline__ void meval_f32(int iOrder, const float *gam, float dx, float dy, float dz,
+                                          float &ax, float &ay, float &az, float &fPot) {
+    float Qta = 0.0f;
+    const float xx2 = dx * dx, xy2 = dx * dy, xz2 = dx * dz, yy2 = dy * dy, yz2 = dy * dz,
+                zz2 = dz * dz;
+    if (iOrder >= 4) {
+        const float m3[10] = {xx2 * dx, xx2 * dy, xx2 * dz, yy2 * dx, xy2 * dz,
+                              zz2 * dx, yy2 * dy, yy2 * dz, zz2 * dy, zz2 * dz};
+        float Qmx = 0.0f, Qmy = 0.0f, Qmz = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 10; ++k) {
+            Qmx += cE.c4[0][k] * m3[k];
+            Qmy += cE.c4[1][k] * m3[k];
+            Qmz += cE.c4[2][k] * m3[k];
+        }
+        const float Qmir = 0.25f * (Qmx * dx + Qmy * dy + Qmz * dz);
+        const float Qhx = cE.hQ[0] * dx + cE.hQ[1] * dy + cE.hQ[2] * dz;
+        const float Qhy = cE.hQ[1] * dx + cE.hQ[3] * dy + cE.hQ[4] * dz;
+        const float Qhz = cE.hQ[2] * dx + cE.hQ[4] * dy + cE.hQ[5] * dz;
+        const float Qh = 0.5f * (Qhx * dx + Qhy * dy + Qhz * dz);
+        fPot -= gam[4] * Qmir - gam[3] * Qh + gam[2] * cE.qtr4;
+        Qta += gam[5] * Qmir - gam[4] * Qh + gam[3] * cE.qtr4;
+        ax += gam[4] * Qmx - gam[3] * Qhx;
+        ay += gam[4] * Qmy - gam[3] * Qhy;
+        az += gam[4] * Qmz - gam[3] * Qhz;
+    }
+    if (iOrder >= 3) {
+        const float m2[6] = {xx2, xy2, xz2, yy2, yz2, zz2};
+        float Qmx = 0.0f, Qmy = 0.0f, Qmz = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            Qmx += cE.c3[0][k] * m2[k];
+            Qmy += cE.c3[1][k] * m2[k];
+            Qmz += cE.c3[2][k] * m2[k];
+        }
+        const float Qmir = (1.0f / 3.0f) * (Qmx * dx + Qmy * dy + Qmz * dz);
+        const float Qtr = cE.q3[0] * dx + cE.q3[1] * dy + cE.q3[2] * dz;
+        fPot -= gam[3] * Qmir - gam[2] * Qtr;
+        Qta += gam[4] * Qmir - gam[3] * Qtr;
+        ax += gam[3] * Qmx - gam[2] * cE.q3[0];
+        ay += gam[3] * Qmy - gam[2] * cE.q3[1];
+        az += gam[3] * Qmz - gam[2] * cE.q3[2];
+    }
+    if (iOrder >= 2) {
+        const float *q = cE.q2;            // xx yy zz xy xz yz
+        const float Qmx = q[4] * dz + q[3] * dy + q[0] * dx;
+        const float Qmy = q[5] * dz + q[3] * dx + q[1] * dy;
+        const float Qmz = q[5] * dy + q[4] * dx + q[2] * dz;
+        const float Qmir = 0.5f * (Qmx * dx + Qmy * dy + Qmz * dz);
+        fPot -= gam[2] * Qmir - gam[1] * cE.qtr2;
+        Qta += gam[3] * Qmir - gam[2] * cE.qtr2;
+        ax += gam[2] * Qmx;
+        ay += gam[2] * Qmy;
+        az += gam[2] * Qmz;
+    }
+    fPot -= gam[0] * cE.m;
+    Qta += gam[1] * cE.m;
+    ax -= dx * Qta;
+    ay -= dy * Qta;
+    az -= dz * Qta;
+}
+
 __device__ __forceinline__ float erf_r(float x) { return erff(x); }
 __device__ __forceinline__ double erf_r(double x) { return erf(x); }
 __device__ __forceinline__ float erfc_r(float x) { return erfcf(x); }
@@ -313,7 +384,8 @@ __global__ void __launch_bounds__(128) k_ewald(TsphDevParts P, TsphDevCounters *
                         gam[5] = 9 * gam[4] * dir2 + alphan * a;
                     }
                     Real tx = 0, ty = 0, tz = 0, tp = 0;
-                    meval<Real>(iOrder, mom, gam, dxo, dyo, dzo, tx, ty, tz, tp);
+                    if constexpr (sizeof(Real) == 4) meval_f32(iOrder, gam, dxo, dyo, dzo, tx, ty, tz, tp);
+                    else meval<Real>(iOrder, mom, gam, dxo, dyo, dzo, tx, ty, tz, tp);
                     kadd(ax, cax, tx);
                     kadd(ay, cay, ty);
                     kadd(az, caz, tz);
@@ -443,6 +515,34 @@ int tsph_ewald(tsph_ctx *ctx, const tsph_grav_params *gp) {
     M.xy = node0[7]; M.xz = node0[8]; M.yz = node0[9];
     const double *mv = &M.m;
     for (int k = 0; k < 35; ++k) E.momf[k] = (float)mv[k];
+    {   // FP32 MEVAL coefficients (monomials dx3 dx2dy dx2dz dxdy2 dxdydz dxdz2 dy3 dy2dz dydz2 dz3)
+        const double s6 = 1.0 / 6.0;
+        const double c4[3][10] = {
+            {M.xxxx, 3 * M.xxxy, 3 * M.xxxz, 3 * M.xxyy, 6 * M.xxyz, 3 * M.xxzz, M.xyyy, 3 * M.xyyz, 3 * M.xyzz, M.xzzz},
+            {M.xxxy, 3 * M.xxyy, 3 * M.xxyz, 3 * M.xyyy, 6 * M.xyyz, 3 * M.xyzz, M.yyyy, 3 * M.yyyz, 3 * M.yyzz, M.yzzz},
+            {M.xxxz, 3 * M.xxyz, 3 * M.xxzz, 3 * M.xyyz, 6 * M.xyzz, 3 * M.xzzz, M.yyyz, 3 * M.yyzz, 3 * M.yzzz, M.zzzz}};
+        for (int a = 0; a < 3; ++a)
+            for (int k = 0; k < 10; ++k) E.c4[a][k] = (float)(s6 * c4[a][k]);
+        const double Qxx = M.xxxx + M.xxyy + M.xxzz, Qxy = M.xxxy + M.xyyy + M.xyzz,
+                     Qxz = M.xxxz + M.xyyz + M.xzzz, Qyy = M.xxyy + M.yyyy + M.yyzz,
+                     Qyz = M.xxyz + M.yyyz + M.yzzz, Qzz = M.xxzz + M.yyzz + M.zzzz;
+        const double hq[6] = {Qxx, Qxy, Qxz, Qyy, Qyz, Qzz};
+        for (int k = 0; k < 6; ++k) E.hQ[k] = (float)(0.5 * hq[k]);
+        E.qtr4 = (float)(0.125 * (Qxx + Qyy + Qzz));
+        // octopole (monomials dx2 dxdy dxdz dy2 dydz dz2)
+        const double c3[3][6] = {{M.xxx, 2 * M.xxy, 2 * M.xxz, M.xyy, 2 * M.xyz, M.xzz},
+                                 {M.xxy, 2 * M.xyy, 2 * M.xyz, M.yyy, 2 * M.yyz, M.yzz},
+                                 {M.xxz, 2 * M.xyz, 2 * M.xzz, M.yyz, 2 * M.yzz, M.zzz}};
+        for (int a = 0; a < 3; ++a)
+            for (int k = 0; k < 6; ++k) E.c3[a][k] = (float)(0.5 * c3[a][k]);
+        E.q3[0] = (float)(0.5 * (M.xxx + M.xyy + M.xzz));
+        E.q3[1] = (float)(0.5 * (M.xxy + M.yyy + M.yzz));
+        E.q3[2] = (float)(0.5 * (M.xxz + M.yyz + M.zzz));
+        const double q2[6] = {M.xx, M.yy, M.zz, M.xy, M.xz, M.yz};
+        for (int k = 0; k < 6; ++k) E.q2[k] = (float)q2[k];
+        E.qtr2 = (float)(0.5 * (M.xx + M.yy + M.zz));
+        E.m = (float)M.m;
+    }
     double L = gp->dPeriod;
     E.L = L;
     E.alpha = 2.0 / L;
