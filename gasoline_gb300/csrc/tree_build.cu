@@ -1649,16 +1649,32 @@ int tsph_build_tree(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, int n
     // shared memory sized to the task size (positions, flags, scan, order)
     A.scap = S < ST_SCAP ? S : ST_SCAP;
     const size_t smem = ((size_t)A.scap * ST_BYTES_PER + 15) & ~(size_t)15;
-    if (ctx->subtreeBlocks == 0 || ctx->subtreeSmem != smem) {
+    // resident CTAs per shared-memory size (the gravity and gas trees of one
+    // step may use different task sizes; a capture finds both cached)
+    int slot = -1;
+    for (int k = 0; k < 4 && slot < 0; ++k)
+        if (ctx->subtreeBlocks[k] > 0 && ctx->subtreeSmem[k] == smem) slot = k;
+    if (slot < 0) {
         if (ctx->capturing) return TSPH_ERR_STATE;
-        TSPH_CK(cudaFuncSetAttribute(k_subtree, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)(ST_SCAP * ST_BYTES_PER)));
+        if (!ctx->subtreeAttr) {
+            TSPH_CK(cudaFuncSetAttribute(k_subtree, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(ST_SCAP * ST_BYTES_PER)));
+            ctx->subtreeAttr = true;
+        }
         int per = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_subtree, ST_BS, smem);
-        ctx->subtreeBlocks = (per > 0 ? per : 1) * ctx->smCount;
-        ctx->subtreeSmem = smem;
+        TSPH_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_subtree, ST_BS, smem));
+        for (slot = 0; slot < 4 && ctx->subtreeBlocks[slot] > 0; ++slot) {}
+        if (slot == 4) {   // full: keep the newest three
+            for (int k = 0; k < 3; ++k) {
+                ctx->subtreeBlocks[k] = ctx->subtreeBlocks[k + 1];
+                ctx->subtreeSmem[k] = ctx->subtreeSmem[k + 1];
+            }
+            slot = 3;
+        }
+        ctx->subtreeBlocks[slot] = (per > 0 ? per : 1) * ctx->smCount;
+        ctx->subtreeSmem[slot] = smem;
     }
-    k_subtree<<<ctx->subtreeBlocks, ST_BS, smem, ctx->stream>>>(A);
+    k_subtree<<<ctx->subtreeBlocks[slot], ST_BS, smem, ctx->stream>>>(A);
     TSPH_LAUNCH_CK("k_subtree");
     // numbering
     const int levBound = nR > Fcap ? nR : Fcap;

@@ -170,3 +170,34 @@ def test_graph_step_equals_direct_steps():
     # a replay counts the kernels it runs (the captured build's fixed top
     # levels included, some of them empty)
     assert lb > 0 and la > 0
+
+
+def test_graph_step_with_two_task_sizes():
+    """The gravity tree (900k particles) and the gas tree (700k) pick
+    different subtree task sizes on a 152-SM GPU; one captured step holds
+    both builds and replays bit-identically to direct steps."""
+    pg, vg, mg, u = g.ics.gas_sphere(700_000, seed=21)
+    pd, vd, md = g.ics.plummer(200_000, seed=22)
+    pos = np.concatenate([pg, pd])
+    vel = np.concatenate([vg, vd])
+    m = np.concatenate([0.2 * mg, 0.8 * md])
+    soft = np.full(len(m), 0.01)
+    gp = g.grav_params(periodic=False, precision=g.FP32)
+    sp = g.sph_params(nSmooth=32)
+    states = []
+    for graph in (False, True):
+        c = g.Context(0)
+        try:
+            c.set_particles(pos, m, soft)
+            c.set_velocities(vel, len(mg), u)
+            c.grav_all(gp)                       # the opening kick's forces
+            c.smooth(g.SMX_DENDVDX, sp)
+            c.smooth(g.SMX_SPHPRESSURETERMS, sp)
+            for _ in range(2):
+                c.step(1e-4, gp, sp, graph=graph)
+            c.step_status()
+            states.append(c.get_state())
+        finally:
+            c.close()
+    for k in range(3):
+        assert np.array_equal(states[0][k], states[1][k]), k
