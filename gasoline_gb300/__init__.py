@@ -84,6 +84,24 @@ class Tuning(ctypes.Structure):
                 ("reserved", ctypes.c_int * 6)]
 
 
+class TipsyHeader(ctypes.Structure):
+    """tsph_tipsy_header: the Tipsy file header (tipsydefs.h struct dump)."""
+    _fields_ = [("time", ctypes.c_double), ("nbodies", ctypes.c_int), ("ndim", ctypes.c_int),
+                ("nsph", ctypes.c_int), ("ndark", ctypes.c_int), ("nstar", ctypes.c_int)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+def tipsy_header(path, standard=True):
+    """The header of a Tipsy snapshot, as a dict."""
+    h = TipsyHeader()
+    rc = load().tsph_tipsy_read_header(os.fsencode(path), int(standard), ctypes.byref(h))
+    if rc:
+        raise TsphError(rc, load().tsph_error_string(rc).decode())
+    return h.as_dict()
+
+
 class TsphError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__(f"libtsph error {code}: {msg}")
@@ -114,7 +132,9 @@ def load():
                  "tsph_hnet_loss_grad", "tsph_hnet_mode", "tsph_hnet_train",
                  "tsph_hnet_info", "tsph_hnet_num_params", "tsph_set_tuning",
                  "tsph_get_tuning", "tsph_set_systems", "tsph_step",
-                 "tsph_step_status"):
+                 "tsph_step_status", "tsph_tipsy_read_header", "tsph_read_tipsy",
+                 "tsph_write_tipsy", "tsph_get_snapshot_fields",
+                 "tsph_set_snapshot_fields"):
         getattr(lib, name).restype = ctypes.c_int
     lib.tsph_destroy.restype = None
     _lib = lib
@@ -266,6 +286,60 @@ class Context:
         u = np.zeros(max(self.ngas, 1))
         self._check(self.lib.tsph_get_state(self._ctx, _d(pos), _d(vel), _d(u)))
         return pos, vel, u[:self.ngas]
+
+    # ---- Tipsy snapshots -------------------------------------------------------
+    def read_tipsy(self, path, standard=True, dvFac=1.0, dTuFac=1.0):
+        """Load a Tipsy snapshot (pkdReadTipsy pkd.c:297): replaces the
+        particles, the first nsph of them gas.  Returns the header."""
+        h = TipsyHeader()
+        self._check(self.lib.tsph_read_tipsy(self._ctx, os.fsencode(path), int(standard),
+                                             ctypes.c_double(dvFac), ctypes.c_double(dTuFac),
+                                             ctypes.byref(h)))
+        self.n = h.nbodies
+        self.ngas = h.nsph
+        self.nstar = h.nstar
+        return h.as_dict()
+
+    def write_tipsy(self, path, time, standard=True, dvFac=1.0, duTFac=1.0, nstar=None):
+        """Write the particles as a Tipsy snapshot (pkdWriteTipsy pkd.c:1628);
+        the last `nstar` particles are stars (default: as read in, else 0)."""
+        if nstar is None:
+            nstar = getattr(self, "nstar", 0)
+        self._check(self.lib.tsph_write_tipsy(self._ctx, os.fsencode(path), int(standard),
+                                              ctypes.c_double(time), int(nstar),
+                                              ctypes.c_double(dvFac), ctypes.c_double(duTFac)))
+
+    def get_snapshot_fields(self):
+        """mass, soft, pot (float64) and the snapshot's rho, metals, tform
+        (float32), in caller order."""
+        n = self.n
+        mass, soft, pot = np.zeros(n), np.zeros(n), np.zeros(n)
+        rho, met, tf = (np.zeros(n, dtype=np.float32) for _ in range(3))
+        fp = ctypes.POINTER(ctypes.c_float)
+        self._check(self.lib.tsph_get_snapshot_fields(
+            self._ctx, _d(mass), _d(soft), _d(pot), rho.ctypes.data_as(fp),
+            met.ctypes.data_as(fp), tf.ctypes.data_as(fp)))
+        return dict(mass=mass, soft=soft, pot=pot, rho=rho, metals=met, tform=tf)
+
+    def set_snapshot_fields(self, pot=None, rho=None, metals=None, tform=None):
+        """Set the potential (float64) and the snapshot's rho, metals, tform
+        (stored as float32) of the loaded particles; None keeps a field."""
+        fp = ctypes.POINTER(ctypes.c_float)
+        keep = []
+
+        def f32(a):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(a, dtype=np.float32)
+            keep.append(a)
+            return a.ctypes.data_as(fp)
+        potp = None
+        if pot is not None:
+            pot = _c64(pot)
+            keep.append(pot)
+            potp = _d(pot)
+        self._check(self.lib.tsph_set_snapshot_fields(self._ctx, potp, f32(rho), f32(metals),
+                                                      f32(tform)))
 
     # ---- learned smoothing length ---------------------------------------------
     def hnet_init(self, seed=1):

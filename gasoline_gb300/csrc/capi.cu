@@ -28,6 +28,7 @@ extern "C" const char *tsph_error_string(int s) {
     case TSPH_ERR_TREE_DEPTH: return "tree deeper than the level cap";
     case TSPH_ERR_NOMEM: return "device allocation failed";
     case TSPH_ERR_BOUNDS: return "particle outside the captured coordinate bound";
+    case TSPH_ERR_IO: return "snapshot file missing, short or inconsistent";
     default: return "unknown status";
     }
 }
@@ -99,6 +100,7 @@ extern "C" void tsph_destroy(tsph_ctx *ctx) {
     FREE(S.ph); FREE(S.ih2); FREE(S.fn1); FREE(S.pr2f); FREE(S.pfa); FREE(S.pfb); FREE(S.pfc);
     FREE(ctx->dCnt); FREE(ctx->dBucketLists); FREE(ctx->dRoot); FREE(ctx->dEwt); FREE(ctx->dStage);
     FREE(ctx->dAux); FREE(ctx->dStepStatus);
+    tsph_free_snapshot(ctx);
     free(ctx->hSys);
     free(ctx->hTmp);
     free(ctx->hEw);
@@ -215,24 +217,32 @@ __global__ void k_check_finite(int n, TsphDevParts P, TsphDevCounters *cnt, doub
     warp_max_abs(a, &cnt->maxAbs);
 }
 
-extern "C" int tsph_set_particles(tsph_ctx *ctx, int n, const double *pos, const double *mass,
-                                  const double *soft) {
-    if (!ctx || n < 0 || (n > 0 && (!pos || !mass || !soft))) return TSPH_ERR_ARG;
-    if (n >= (1 << 27)) return TSPH_ERR_ARG;   // 27-bit particle indices in the walk entries
-    cudaSetDevice(ctx->device);
+// A new particle set of n: buffers, one system, every derived state stale.
+// The caller then fills the caller-order state on the stream.
+int tsph_load_begin(tsph_ctx *ctx, int n) {
+    if (n < 0 || n >= (1 << 27)) return TSPH_ERR_ARG;   // 27-bit particle indices in the walk entries
     int rc = tsph_ensure_particles(ctx, n > 0 ? n : 1);
     if (rc) return rc;
     ctx->n = n;
     ctx->ngas = 0;
-    ctx->haveTree = ctx->haveGrav = ctx->haveVel = false;
+    ctx->haveParts = ctx->haveTree = ctx->haveGrav = ctx->haveVel = false;
     ctx->S.haveDensity = false;
+    ctx->snapValid = false;
     ctx->P.n = n;
     ctx->G.n = 0;
     ctx->sysVersion++;
-    if (n == 0) { ctx->haveParts = true; return TSPH_OK; }
-    rc = tsph_set_ranges(ctx, ctx->P, ctx->T, n, 1, &n);
-    if (rc) return rc;
     ctx->nSys = 1;
+    if (n == 0) return TSPH_OK;
+    return tsph_set_ranges(ctx, ctx->P, ctx->T, n, 1, &n);
+}
+
+extern "C" int tsph_set_particles(tsph_ctx *ctx, int n, const double *pos, const double *mass,
+                                  const double *soft) {
+    if (!ctx || n < 0 || (n > 0 && (!pos || !mass || !soft))) return TSPH_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    int rc = tsph_load_begin(ctx, n);
+    if (rc) return rc;
+    if (n == 0) { ctx->haveParts = true; return TSPH_OK; }
     TSPH_CK(cudaMemcpyAsync(ctx->dStage, pos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
     k_load_state<<<tsph_blocks(n, 256), 256, 0, ctx->stream>>>(n, ctx->dStage, ctx->C, ctx->P.iord,
                                                                ctx->G.iord);

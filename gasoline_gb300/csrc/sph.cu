@@ -1186,6 +1186,25 @@ extern "C" int tsph_set_velocities(tsph_ctx *ctx, const double *vel, int ngas, c
     return TSPH_OK;
 }
 
+// The gas of a particle set whose caller-order state (u, uPred, vPred and
+// the gas tree's identity order) is already on the device: the first ngas
+// particles become gas, as tsph_set_velocities makes them.
+int tsph_load_gas(tsph_ctx *ctx, int ngas) {
+    if (ngas < 0 || ngas > ctx->n) return TSPH_ERR_ARG;
+    ctx->ngas = ngas;
+    ctx->G.n = ngas;
+    ctx->sysVersion++;
+    ctx->S.haveDensity = ctx->S.havePressure = false;
+    ctx->hnet.havePrev = false;
+    if (ngas > 0) {
+        int rc = tsph_apply_gas_systems(ctx);
+        if (rc) return rc;
+    }
+    TSPH_CK(cudaStreamSynchronize(ctx->stream));
+    ctx->haveParts = ctx->haveVel = true;
+    return TSPH_OK;
+}
+
 static int run_density(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_out *out) {
     const int ng = ctx->ngas;
     TsphSphBufs &S = ctx->S;

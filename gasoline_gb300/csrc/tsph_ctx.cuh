@@ -116,11 +116,22 @@ struct tsph_ctx {
     int nEwt;
     int ewtCap;
 
-    // input staging (caller order) and pinned host mirror
+    // input staging (caller order)
     double *dStage;
     size_t stageBytes;
+
+    // Tipsy snapshot I/O: two chunks of pinned host and device staging, and
+    // the per-particle fields a snapshot carries that the path does not use
+    // (caller order; valid after tsph_read_tipsy until the next load)
     void *hPin;
-    size_t hPinBytes;
+    unsigned int *dSnapRaw;
+    size_t snapChunkBytes;
+    float *snapRho, *snapMetals, *snapTform;
+    int snapCap;
+    bool snapValid;
+    int snapNStar;               // star count of the last snapshot read
+    unsigned int *dSnapStatus;
+    cudaEvent_t snapEv[2];
 
     bool haveParts, haveVel, haveTree, haveGrav;
     tsph_grav_params lastGrav;
@@ -140,8 +151,9 @@ struct tsph_ctx {
 
     // tree build tuning and mode
     int taskSize;                // largest node one CTA builds whole (0 = automatic)
-    int subtreeBlocks;           // resident CTAs of the subtree kernel
-    size_t subtreeSmem;          // the dynamic shared memory they were sized for
+    int subtreeBlocks[4];        // resident CTAs of the subtree kernel ...
+    size_t subtreeSmem[4];       // ... for each dynamic shared memory size seen
+    bool subtreeAttr;            // its shared-memory limit raised
     int walkBlocksPerSM;         // resident walk blocks per SM (0 = default)
     bool capturing;              // inside a CUDA graph capture: no host reads
     double capLimit;             // |coordinate| bound of the captured step (0 = none)
@@ -195,6 +207,9 @@ int tsph_set_ranges(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, int n
 int tsph_tree_moments(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, double dTheta);
 void tsph_free_build(TsphBuildBufs &B);
 int tsph_apply_gas_systems(tsph_ctx *ctx);
+int tsph_load_begin(tsph_ctx *ctx, int n);
+int tsph_load_gas(tsph_ctx *ctx, int ngas);
+void tsph_free_snapshot(tsph_ctx *ctx);
 int tsph_fold_status(tsph_ctx *ctx);
 int tsph_copy_out(tsph_ctx *ctx, const double *a0, const double *a1, const double *a2, int comp,
                   double *host);

@@ -51,8 +51,11 @@ enum tsph_status {
     TSPH_ERR_STATE = 8,           /* call order (e.g. no particles loaded) */
     TSPH_ERR_TREE_DEPTH = 9,      /* tree deeper than the build's level cap */
     TSPH_ERR_NOMEM = 10,          /* device allocation failed */
-    TSPH_ERR_BOUNDS = 11          /* a particle left the coordinate bound a
+    TSPH_ERR_BOUNDS = 11,         /* a particle left the coordinate bound a
                                      captured step graph was built for */
+    TSPH_ERR_IO = 12              /* snapshot file: cannot be opened, is
+                                     short, or its header or masses are
+                                     inconsistent */
 };
 
 enum tsph_precision {
@@ -265,6 +268,49 @@ int tsph_kick(tsph_ctx *ctx, double dt);
 int tsph_drift(tsph_ctx *ctx, double dt, int bPeriodic, double dPeriod);
 /* Copy state to the host in caller order; NULL skips a field. */
 int tsph_get_state(tsph_ctx *ctx, double *pos, double *vel, double *u);
+
+/* --- Tipsy snapshots (pkdReadTipsy pkd.c:297, pkdWriteTipsy pkd.c:1628) --
+ * The reference's particle file (tipsydefs.h:9-45): a 32-byte header, then
+ * the gas, dark and star records, 4-byte floats; bStandard = 1 is the XDR
+ * (big-endian) form, 0 the host-order form.  Gas comes first in the file,
+ * as the library's convention wants. */
+typedef struct {
+    double time;     /* expansion factor when comoving, else time */
+    int nbodies, ndim, nsph, ndark, nstar;
+} tsph_tipsy_header;
+
+/* The header of a snapshot (msrReadTipsy's read, master.c:3612-3622). */
+int tsph_tipsy_read_header(const char *path, int bStandard, tsph_tipsy_header *h);
+/* Load a snapshot into the context, replacing its particles as
+ * tsph_set_particles + tsph_set_velocities would: v = dvFac*vel,
+ * u = uPred = dTuFac*temp for the nsph gas particles, softening = eps,
+ * potential = phi; rho, metals and tform are kept for tsph_write_tipsy.
+ * dvFac and dTuFac are the caller's unit factors (master.c:3742-3775).
+ * h (may be NULL) receives the header.  TSPH_ERR_IO for a missing, short
+ * or inconsistent file, or a mass the reference rejects (standard-form gas
+ * mass <= 0, any other mass < 0), and the context then holds no particles. */
+int tsph_read_tipsy(tsph_ctx *ctx, const char *path, int bStandard, double dvFac,
+                    double dTuFac, tsph_tipsy_header *h);
+/* Write the context's particles as a snapshot at `time`: the first ngas are
+ * gas, the last nStar stars, the rest dark; vel*dvFac and u*duTFac rounded
+ * to float (pkdWriteTipsy with the adiabatic gas model).  rho is the
+ * density of the last SPH density pass, else the value read in; metals and
+ * tform are those read in (0 for particles loaded by tsph_set_particles);
+ * phi is the potential of the last gravity evaluation, else the value read
+ * in. */
+int tsph_write_tipsy(tsph_ctx *ctx, const char *path, int bStandard, double time,
+                     int nStar, double dvFac, double duTFac);
+/* Per-particle fields of the loaded set in caller order; NULL skips one:
+ * mass, softening and potential (double; the potential read in or of the
+ * last gravity evaluation), and the snapshot's rho, metals and tform
+ * (float; zeros when the particles did not come from a snapshot). */
+int tsph_get_snapshot_fields(tsph_ctx *ctx, double *mass, double *soft, double *pot,
+                             float *rho, float *metals, float *tform);
+/* Set the fields a snapshot carries beside the particles (caller order;
+ * NULL keeps a field): the potential, and rho, metals and tform as stored
+ * in the file.  For writing particles loaded with tsph_set_particles. */
+int tsph_set_snapshot_fields(tsph_ctx *ctx, const double *pot, const float *rho,
+                             const float *metals, const float *tform);
 
 /* --- tuning --------------------------------------------------------------
  * Launch-shape knobs of the CUDA path.  None changes a result: the tree,

@@ -168,6 +168,31 @@ def reference():
     return _ref
 
 
+def reference_tipsy_write(path, standard, time, ngas, ndark, nstar, pos, vel, f,
+                          dvFac=1.0, duTFac=1.0):
+    """The reference's pkdWriteTipsy (after msrWriteTipsy's header) on these
+    particles; f is (n, 9): mass, soft, u, rho, metals, tform, phi, 0, 0."""
+    lib = reference().lib
+    pos = _c64(pos, (-1, 3)); vel = _c64(vel, (-1, 3)); f = _c64(f, (-1, 9))
+    rc = lib.ref_tipsy_write(os.fsencode(path), int(standard), ctypes.c_double(time), ngas,
+                             ndark, nstar, ctypes.c_double(dvFac), ctypes.c_double(duTFac),
+                             _d(pos), _d(vel), _d(f))
+    if rc:
+        raise OSError(f"ref_tipsy_write failed on {path}")
+
+
+def reference_tipsy_read(path, standard, ngas, ndark, nstar, dvFac=1.0, dTuFac=1.0):
+    """The reference's pkdReadTipsy: (pos, vel, f) in file order."""
+    lib = reference().lib
+    n = ngas + ndark + nstar
+    pos = np.zeros((n, 3)); vel = np.zeros((n, 3)); f = np.zeros((n, 9))
+    rc = lib.ref_tipsy_read(os.fsencode(path), int(standard), ngas, ndark, nstar,
+                            ctypes.c_double(dvFac), ctypes.c_double(dTuFac), _d(pos), _d(vel), _d(f))
+    if rc:
+        raise OSError(f"ref_tipsy_read failed on {path}")
+    return pos, vel, f
+
+
 def knn_fball2(pos, nsmooth, periodic=False, L=1.0, nthreads=1):
     pos = _c64(pos, (-1, 3))
     n = pos.shape[0]

@@ -350,3 +350,92 @@ int ref_sph(int n, const double *pos, const double *vel, const double *mass,
 /* The reference's approximate 1/sqrt (v_sqrt1.c:11), exported for tests. */
 void v_sqrt1(int, double *, double *);
 void ref_v_sqrt1(int n, double *r2, double *a) { v_sqrt1(n, r2, a); }
+
+/*
+ * Tipsy snapshot I/O through the reference's own pkdReadTipsy (pkd.c:297-686)
+ * and pkdWriteTipsy (pkd.c:1628-1798), with the stdio XDR stand-in in
+ * shim/rpc/xdr.h for the standard (big-endian) form.  The 32-byte header
+ * is written the way msrWriteTipsy does (master.c:3999-4013): xdrHeader's
+ * field order (master.c:3563-3575) for the standard form, the struct dump
+ * of tipsydefs.h as it lies in memory for the native form.
+ * Per-particle arrays are in file order (gas, dark, star):
+ *   f[9*i + ..] = mass, soft (eps), u, rho, metals, tform, phi, 0, 0
+ * pos/vel are [3n].  Returns 0, or -1 when a file cannot be opened.
+ */
+#include <rpc/types.h>
+#include <rpc/xdr.h>
+#include "tipsydefs.h"
+
+static int tipsy_type_of(int i, int nGas, int nDark)
+{
+    return i < nGas ? TYPE_GAS : (i < nGas + nDark ? TYPE_DARK : TYPE_STAR);
+}
+
+int ref_tipsy_write(const char *fname, int bStandard, double time, int nGas,
+                    int nDark, int nStar, double dvFac, double duTFac,
+                    const double *pos, const double *vel, const double *f)
+{
+    int n = nGas + nDark + nStar, i, j;
+    struct dump h;
+    FILE *fp = fopen(fname, "wb");
+    PKD pkd;
+    FLOAT fPeriod[3] = {FLOAT_MAXVAL, FLOAT_MAXVAL, FLOAT_MAXVAL};
+    if (!fp) return -1;
+    memset(&h, 0, sizeof(h));
+    h.time = time; h.nbodies = n; h.ndim = 3;
+    h.nsph = nGas; h.ndark = nDark; h.nstar = nStar;
+    if (bStandard) {
+        XDR xdrs;
+        int pad = 0;
+        xdrstdio_create(&xdrs, fp, XDR_ENCODE);
+        xdr_double(&xdrs, &h.time);
+        xdr_int(&xdrs, &h.nbodies); xdr_int(&xdrs, &h.ndim);
+        xdr_int(&xdrs, &h.nsph); xdr_int(&xdrs, &h.ndark);
+        xdr_int(&xdrs, &h.nstar); xdr_int(&xdrs, &pad);
+        xdr_destroy(&xdrs);
+    } else {
+        fwrite(&h, sizeof(struct dump), 1, fp);
+    }
+    fclose(fp);
+    memset(&g_mdl, 0, sizeof(g_mdl));
+    g_mdl.nThreads = 1;
+    pkdInitialize(&pkd, &g_mdl, 2, n > 0 ? n : 1, 0, fPeriod, 0.0, 0.0, nDark, nGas, nStar);
+    pkd->nLocal = n;
+    for (i = 0; i < n; ++i) {
+        PARTICLE *p = &pkd->pStore[i];
+        const double *q = &f[9 * i];
+        memset(p, 0, sizeof(*p));
+        p->iOrder = i;
+        p->iActive = tipsy_type_of(i, nGas, nDark);
+        for (j = 0; j < 3; ++j) { p->r[j] = pos[3 * i + j]; p->v[j] = vel[3 * i + j]; }
+        p->fMass = q[0]; p->fSoft = p->fSoft0 = q[1]; p->u = q[2];
+        p->fDensity = q[3]; p->fMetals = q[4]; p->fTimeForm = q[5]; p->fPot = q[6];
+    }
+    pkdWriteTipsy(pkd, (char *)fname, 0, bStandard, dvFac, duTFac, GASMODEL_ADIABATIC);
+    pkdFinish(pkd);
+    return 0;
+}
+
+int ref_tipsy_read(const char *fname, int bStandard, int nGas, int nDark, int nStar,
+                   double dvFac, double dTuFac, double *pos, double *vel, double *f)
+{
+    int n = nGas + nDark + nStar, i, j;
+    PKD pkd;
+    FLOAT fPeriod[3] = {FLOAT_MAXVAL, FLOAT_MAXVAL, FLOAT_MAXVAL};
+    FILE *fp = fopen(fname, "rb");
+    if (!fp) return -1;
+    fclose(fp);
+    memset(&g_mdl, 0, sizeof(g_mdl));
+    g_mdl.nThreads = 1;
+    pkdInitialize(&pkd, &g_mdl, 2, n > 0 ? n : 1, 0, fPeriod, 0.0, 0.0, nDark, nGas, nStar);
+    pkdReadTipsy(pkd, (char *)fname, 0, n, bStandard, 0, dvFac, dTuFac);
+    for (i = 0; i < n; ++i) {
+        PARTICLE *p = &pkd->pStore[i];
+        double *q = &f[9 * i];
+        for (j = 0; j < 3; ++j) { pos[3 * i + j] = p->r[j]; vel[3 * i + j] = p->v[j]; }
+        q[0] = p->fMass; q[1] = p->fSoft; q[2] = p->u; q[3] = p->fDensity;
+        q[4] = p->fMetals; q[5] = p->fTimeForm; q[6] = p->fPot; q[7] = q[8] = 0.0;
+    }
+    pkdFinish(pkd);
+    return 0;
+}

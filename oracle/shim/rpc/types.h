@@ -1,5 +1,5 @@
-/* Stand-in for SunRPC <rpc/types.h>: the reference's snapshot I/O includes it,
- * but no snapshot I/O runs in the oracle.  Test infrastructure only. */
+/* Stand-in for SunRPC <rpc/types.h>, for the reference's snapshot I/O.
+ * Test infrastructure only. */
 #ifndef TSPH_SHIM_RPC_TYPES_H
 #define TSPH_SHIM_RPC_TYPES_H
 typedef int bool_t;

@@ -24,3 +24,14 @@ def ctx():
     c = g.Context(0)
     yield c
     c.close()
+
+
+@pytest.fixture
+def scratch(request):
+    """A per-test directory under tests/.scratch for files a test writes."""
+    import shutil
+    d = os.path.join(ROOT, "tests", ".scratch", request.node.name.replace("/", "_"))
+    shutil.rmtree(d, ignore_errors=True)
+    os.makedirs(d)
+    yield d
+    shutil.rmtree(d, ignore_errors=True)

@@ -48,6 +48,45 @@ def sph_case(name, pos, vel, mass, soft, u, sp):
     print(name, len(mass))
 
 
+def tipsy_fields(ng, nd, ns, seed):
+    """Seeded particles of every Tipsy type; a few values sit on float
+    rounding edges (subnormal, -0.0, near FLT_MAX, halfway between floats)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    n = ng + nd + ns
+    pos = rng.normal(0.0, 1.0, (n, 3))
+    vel = rng.normal(0.0, 1.0, (n, 3))
+    f = np.zeros((n, 9))
+    f[:, 0] = rng.uniform(0.1, 1.0, n)
+    f[:, 1] = rng.uniform(0.01, 0.02, n)
+    f[:ng, 2] = rng.uniform(1.0, 2.0, ng)
+    f[:ng, 3] = rng.uniform(0.0, 5.0, ng)
+    f[:ng, 4] = rng.uniform(0.0, 0.02, ng)
+    f[ng + nd:, 4] = rng.uniform(0.0, 0.02, ns)
+    f[ng + nd:, 5] = rng.uniform(0.0, 1.0, ns)
+    f[:, 6] = rng.normal(-1.0, 0.1, n)
+    pos[0] = [1e-40, -0.0, 3.0e38]
+    pos[1] = [1.0 + 2.0 ** -24, 1.0 + 3 * 2.0 ** -24, -(1.0 + 2.0 ** -24)]
+    vel[2] = [1e-45, -1e-39, 0.1]
+    return pos, vel, f
+
+
+def tipsy_case(name, ng, nd, ns, seed, dvFac=1.3, duTFac=2.5, rvFac=0.7, rTuFac=0.4):
+    """A snapshot written by the reference's pkdWriteTipsy in both forms,
+    and what its pkdReadTipsy reads back (with other unit factors)."""
+    pos, vel, f = tipsy_fields(ng, nd, ns, seed)
+    out = {}
+    for std, tag in ((1, "std"), (0, "nat")):
+        path = os.path.join(HERE, f"{name}.{tag}")
+        oracle.reference_tipsy_write(path, std, 0.25, ng, nd, ns, pos, vel, f,
+                                     dvFac=dvFac, duTFac=duTFac)
+        p, v, q = oracle.reference_tipsy_read(path, std, ng, nd, ns, dvFac=rvFac, dTuFac=rTuFac)
+        out[f"pos_{tag}"], out[f"vel_{tag}"], out[f"f_{tag}"] = p, v, q
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), pos=pos, vel=vel, f=f,
+                        counts=np.array([ng, nd, ns]),
+                        factors=np.array([dvFac, duTFac, rvFac, rTuFac]), time=0.25, **out)
+    print(name, ng, nd, ns)
+
+
 def main():
     if not oracle.reference_available():
         oracle.build_reference()
@@ -65,7 +104,13 @@ def main():
     vel = rng.normal(0.0, 0.1, (len(m), 3))
     sph_case("sph_sphere_2k", pos, vel, m, np.full(len(m), 0.01), u,
              oracle.sph_params(nSmooth=32))
+    tipsy_case("tipsy_mixed", 300, 500, 200, seed=16)
 
 
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) > 1 and sys.argv[1] == "tipsy":
+        if not oracle.reference_available():
+            oracle.build_reference()
+        tipsy_case("tipsy_mixed", 300, 500, 200, seed=16)
+    else:
+        main()
