@@ -84,6 +84,25 @@ class Tuning(ctypes.Structure):
                 ("reserved", ctypes.c_int * 6)]
 
 
+class StepParams(ctypes.Structure):
+    """tsph_step_params: adaptive-timestep criteria (the reference's defaults,
+    master.c:572-623)."""
+    _fields_ = [("iMaxRung", ctypes.c_int), ("dEta", ctypes.c_double),
+                ("bGravStep", ctypes.c_int), ("bEpsAccStep", ctypes.c_int),
+                ("bSqrtPhiStep", ctypes.c_int), ("dEtauDot", ctypes.c_double),
+                ("duMinDt", ctypes.c_double)]
+
+
+def step_params(iMaxRung=4, dEta=0.1, bGravStep=0, bEpsAccStep=1, bSqrtPhiStep=0,
+                dEtauDot=0.25, duMinDt=0.0):
+    return StepParams(iMaxRung, dEta, bGravStep, bEpsAccStep, bSqrtPhiStep, dEtauDot, duMinDt)
+
+
+class StepOut(ctypes.Structure):
+    _fields_ = [("iCurrMaxRung", ctypes.c_int), ("nForcePasses", ctypes.c_int),
+                ("nActiveSum", ctypes.c_longlong), ("nEmergency", ctypes.c_int)]
+
+
 class TipsyHeader(ctypes.Structure):
     """tsph_tipsy_header: the Tipsy file header (tipsydefs.h struct dump)."""
     _fields_ = [("time", ctypes.c_double), ("nbodies", ctypes.c_int), ("ndim", ctypes.c_int),
@@ -134,7 +153,8 @@ def load():
                  "tsph_get_tuning", "tsph_set_systems", "tsph_step",
                  "tsph_step_status", "tsph_tipsy_read_header", "tsph_read_tipsy",
                  "tsph_write_tipsy", "tsph_get_snapshot_fields",
-                 "tsph_set_snapshot_fields"):
+                 "tsph_set_snapshot_fields", "tsph_kick_rung", "tsph_top_step_kdk",
+                 "tsph_set_active_rung", "tsph_set_rungs", "tsph_get_rungs"):
         getattr(lib, name).restype = ctypes.c_int
     lib.tsph_destroy.restype = None
     _lib = lib
@@ -279,6 +299,39 @@ class Context:
     def drift(self, dt, periodic=False, L=1.0):
         self._check(self.lib.tsph_drift(self._ctx, ctypes.c_double(dt),
                                         int(periodic), ctypes.c_double(L)))
+
+    def kick_rung(self, iRung, dt, close=True):
+        """pkdKick on rung iRung (all particles when iRung < 0); close=False
+        is the opening kick of a KDK step."""
+        self._check(self.lib.tsph_kick_rung(self._ctx, int(iRung), ctypes.c_double(dt),
+                                            int(close)))
+
+    # ---- adaptive timesteps ------------------------------------------------
+    def top_step_kdk(self, t, dt, gp, sp, st):
+        """One base step dt with rungs (tsph_top_step_kdk); returns its
+        counters."""
+        out = StepOut()
+        self._check(self.lib.tsph_top_step_kdk(self._ctx, ctypes.c_double(t), ctypes.c_double(dt),
+                                               ctypes.byref(gp),
+                                               ctypes.byref(sp) if sp is not None else None,
+                                               ctypes.byref(st), ctypes.byref(out)))
+        return {f: getattr(out, f) for f, _ in StepOut._fields_}
+
+    def set_active_rung(self, iRung):
+        self._check(self.lib.tsph_set_active_rung(self._ctx, int(iRung)))
+
+    def set_rungs(self, rung):
+        r = np.ascontiguousarray(rung, dtype=np.int32)
+        self._check(self.lib.tsph_set_rungs(self._ctx, r.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
+
+    def get_rungs(self):
+        """rung (int32), dt, dtNew, mumax of every particle (caller order)."""
+        n = self.n
+        r = np.zeros(n, dtype=np.int32)
+        dt, dtn, mu = np.zeros(n), np.zeros(n), np.zeros(n)
+        self._check(self.lib.tsph_get_rungs(self._ctx, r.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                            _d(dt), _d(dtn), _d(mu)))
+        return dict(rung=r, dt=dt, dtNew=dtn, mumax=mu)
 
     def get_state(self):
         pos = np.zeros((self.n, 3))

@@ -56,7 +56,7 @@ extern "C" int tsph_create(tsph_ctx **pctx, int device, void *stream) {
         cudaMallocHost((void **)&ctx->hCnt, sizeof(TsphDevCounters)) != cudaSuccess ||
         cudaMallocHost((void **)&ctx->B.hostCount, sizeof(int) * (TSPH_MAX_LEVELS + 16)) != cudaSuccess ||
         cudaMalloc((void **)&ctx->dRoot, sizeof(double) * (64 + 256 * 32)) != cudaSuccess ||
-        cudaMalloc((void **)&ctx->dAux, sizeof(unsigned long long) * 4) != cudaSuccess ||
+        cudaMalloc((void **)&ctx->dAux, sizeof(unsigned long long) * 64) != cudaSuccess ||
         cudaMalloc((void **)&ctx->dStepStatus, sizeof(unsigned int)) != cudaSuccess ||
         cudaMemset(ctx->dStepStatus, 0, sizeof(unsigned int)) != cudaSuccess) {
         tsph_destroy(ctx);
@@ -78,11 +78,13 @@ extern "C" void tsph_destroy(tsph_ctx *ctx) {
     FREE(C.u); FREE(C.vpx); FREE(C.vpy); FREE(C.vpz); FREE(C.upred); FREE(C.ax); FREE(C.ay);
     FREE(C.az); FREE(C.pot); FREE(C.dtGrav); FREE(C.hax); FREE(C.hay); FREE(C.haz); FREE(C.udot);
     FREE(C.fb2prev); FREE(C.divvprev);
+    FREE(C.rung); FREE(C.dt); FREE(C.dtNew); FREE(C.mumax); FREE(C.updv); FREE(C.cs);
     tsph_hnet_free(ctx);
     TsphDevParts *PP[2] = {&ctx->P, &ctx->G};
     for (int k = 0; k < 2; ++k) {
         TsphDevParts &P = *PP[k];
         FREE(P.x); FREE(P.y); FREE(P.z); FREE(P.m); FREE(P.h); FREE(P.iord); FREE(P.rid);
+        FREE(P.act);
         FREE(P.ph); FREE(P.pl); FREE(P.ax); FREE(P.ay); FREE(P.az); FREE(P.pot); FREE(P.dtGrav);
         FREE(P.wsum); FREE(P.wcmp); FREE(P.wdt);
     }
@@ -131,8 +133,12 @@ int tsph_ensure_particles(tsph_ctx *ctx, int n) {
     TsphDevState &C = ctx->C;
     double **cs[] = {&C.x, &C.y, &C.z, &C.vx, &C.vy, &C.vz, &C.m, &C.h, &C.u, &C.vpx, &C.vpy,
                      &C.vpz, &C.upred, &C.ax, &C.ay, &C.az, &C.pot, &C.dtGrav, &C.hax, &C.hay,
-                     &C.haz, &C.udot, &C.fb2prev, &C.divvprev};
+                     &C.haz, &C.udot, &C.fb2prev, &C.divvprev, &C.dt, &C.dtNew, &C.mumax,
+                     &C.updv, &C.cs};
     for (auto pp : cs) rc |= tsph_grow(ctx, pp, cap);
+    rc |= tsph_grow(ctx, &C.rung, cap);
+    rc |= tsph_grow(ctx, &P.act, cap);
+    rc |= tsph_grow(ctx, &G.act, cap);
     TsphSphBufs &S = ctx->S;
     double **ss[] = {&S.vx, &S.vy, &S.vz, &S.u, &S.fBall2, &S.rho, &S.divv, &S.dvds, &S.bal,
                      &S.diff, &S.pr2, &S.cs, &S.dtp, &S.hax, &S.hay, &S.haz, &S.uPdV, &S.uAV,
@@ -176,6 +182,10 @@ __global__ void k_load_state(int n, const double *__restrict__ pos3, TsphDevStat
     C.hax[i] = C.hay[i] = C.haz[i] = 0.0;
     C.ax[i] = C.ay[i] = C.az[i] = C.pot[i] = C.dtGrav[i] = 0.0;
     C.fb2prev[i] = C.divvprev[i] = 0.0;
+    // timestep state as the reference's reader leaves it (pkd.c:318-331)
+    C.rung[i] = 0;
+    C.dt[i] = C.dtNew[i] = FLT_MAX;
+    C.mumax[i] = C.updv[i] = C.cs[i] = 0.0;
     piord[i] = i;
     giord[i] = i;
 }
@@ -192,9 +202,11 @@ __global__ void k_gather_tree(int n, TsphDevState C, TsphDevParts P) {
     P.h[i] = C.h[o];
 }
 
+// gravity results of the active particles; the others keep theirs
+// (pkdInitAccel zeroes only active particles, pkd.c:5443-5456)
 __global__ void k_scatter_grav(int n, TsphDevParts P, TsphDevState C) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= n || !P.act[i]) return;
     int o = P.iord[i];
     C.ax[o] = P.ax[i];
     C.ay[o] = P.ay[i];
@@ -437,7 +449,7 @@ extern "C" int tsph_grav_all(tsph_ctx *ctx, const tsph_grav_params *gp, tsph_gra
                     (35.0 + qflop[gp->iOrder]) * (double)c.nCellNewt;
         double fe = 0.0;
         if (gp->bPeriodic && gp->bEwald && gp->iEwOrder >= 1)
-            fe = (double)c.nEwLoop * (104.0 + mflop[gp->iEwOrder]) + (double)n * ctx->nEwt * 58.0;
+            fe = (double)c.nEwLoop * (104.0 + mflop[gp->iEwOrder]) + (double)c.nActive * ctx->nEwt * 58.0;
         out->dFlop = fg + fe;
         out->dFlopEwald = fe;
         out->dExactFrac = c.nTests ? (double)c.nExactTests / (double)c.nTests : 0.0;

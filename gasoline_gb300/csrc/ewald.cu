@@ -303,7 +303,7 @@ template <typename Real>
 __global__ void __launch_bounds__(128) k_ewald(TsphDevParts P, TsphDevCounters *cnt) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned long long nLoop = 0;
-    if (p < P.n) {
+    if (p < P.n && P.act[p]) {   // active particles only (pkdBucketEwald, ewald.c:53)
         MomR<Real> mom;
         load_mom<Real>(mom);
         const Real L = (Real)cE.L;

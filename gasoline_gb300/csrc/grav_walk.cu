@@ -118,14 +118,15 @@ __device__ __forceinline__ bool intersect_exact(const double *bmin, const double
 // The reference's FP64 decisions for one (bucket, cell, replica), used only
 // when the FP32 filter cannot settle them.  Returns 0 = not opened
 // (Newtonian), 1 = opened, 2 = not opened (softened) when !openTestOnly.
-__device__ __noinline__ int exact_decision(const TsphDevTree &T, const TsphDevParts &P, int node,
+// The bucket box is the bounds of its active particles (T.bact).
+__device__ __noinline__ int exact_decision(const TsphDevTree &T, const TsphDevParts &P, int b,
                                            int lo, int n, int cell, const double *off,
                                            bool openTestOnly) {
     double bmn[3], bmx[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        bmn[k] = T.bnd[6 * node + k];
-        bmx[k] = T.bnd[6 * node + 3 + k];
+        bmn[k] = T.bact[6 * b + k];
+        bmx[k] = T.bact[6 * b + 3 + k];
     }
     double x = xadd(T.r[3 * cell], off[0]);
     double y = xadd(T.r[3 * cell + 1], off[1]);
@@ -474,13 +475,21 @@ __global__ void __launch_bounds__(WPB * 32) k_walk(WalkArgs W) {
         // for the FP32 path; the FP64 twin reads the FP64 bounds directly
         float bch[3], bcl[3], fbmn[3], fbmx[3], bext, fSoftMaxF;
         double bc64[3];
+        int nAct;
         {
             float4 r0 = T.brec[4 * b], r1 = T.brec[4 * b + 1];
             float4 r2 = T.brec[4 * b + 2], r3 = T.brec[4 * b + 3];
             bch[0] = r0.x; bch[1] = r0.y; bch[2] = r0.z; fSoftMaxF = r0.w;
             bcl[0] = r1.x; bcl[1] = r1.y; bcl[2] = r1.z; bext = r1.w;
-            fbmn[0] = r2.x; fbmn[1] = r2.y; fbmn[2] = r2.z;
+            fbmn[0] = r2.x; fbmn[1] = r2.y; fbmn[2] = r2.z; nAct = (int)r2.w;
             fbmx[0] = r3.x; fbmx[1] = r3.y; fbmx[2] = r3.z;
+        }
+        if (bext < 0.0f) {   // no active particle: not walked (pkd.c:2932)
+            if (lane == 0 && W.bucketLists) {
+                W.bucketLists[4 * b + 0] = node;
+                W.bucketLists[4 * b + 1] = W.bucketLists[4 * b + 2] = W.bucketLists[4 * b + 3] = -1;
+            }
+            continue;
         }
         if constexpr (sizeof(Real) == 8) {
 #pragma unroll
@@ -555,7 +564,7 @@ __global__ void __launch_bounds__(WPB * 32) k_walk(WalkArgs W) {
                     fo = filt(D2, M, ch.w, relF);
                     if (fo == 0) {
                         ++cExact;
-                        open = exact_decision(T, P, node, lo, n, cell, cW.off[rep], true) == 1;
+                        open = exact_decision(T, P, b, lo, n, cell, cW.off[rep], true) == 1;
                     } else {
                         open = fo < 0;
                     }
@@ -580,7 +589,7 @@ __global__ void __launch_bounds__(WPB * 32) k_walk(WalkArgs W) {
                     }
                     if (exactNeeded) {
                         ++cExact;
-                        newt = exact_decision(T, P, node, lo, n, cell, cW.off[rep], false) == 0;
+                        newt = exact_decision(T, P, b, lo, n, cell, cW.off[rep], false) == 0;
                     }
                     act = newt ? ACT_NEWT : ACT_SOFT;
                 }
@@ -705,12 +714,13 @@ __global__ void __launch_bounds__(WPB * 32) k_walk(WalkArgs W) {
             }
         }
         if (lane == 0) {
-            cAct += n;
-            cPP += (unsigned long long)n * nPart;
-            cN += (unsigned long long)n * nNewt;
-            cS += (unsigned long long)n * nSoft;
-            cBsq += (unsigned long long)n * n;
-            cIntra += (unsigned long long)n * (n - 1) / 2;
+            // pkdGravAll's sums over the active particles (pkd.c:2945-2950)
+            cAct += nAct;
+            cPP += (unsigned long long)nAct * nPart;
+            cN += (unsigned long long)nAct * nNewt;
+            cS += (unsigned long long)nAct * nSoft;
+            cBsq += (unsigned long long)nAct * n;
+            cIntra += (unsigned long long)nAct * (2 * (n - 1) - nAct + 1) / 2;
             if (W.bucketLists) {
                 W.bucketLists[4 * b + 0] = node;
                 W.bucketLists[4 * b + 1] = nPart;
@@ -742,28 +752,51 @@ __global__ void __launch_bounds__(WPB * 32) k_walk(WalkArgs W) {
 // extent, box corners relative to the centre.  The FP64 work happens here
 // once per bucket, by one thread, instead of redundantly on every lane of
 // the walk (FP64 issues at 1/64 of the FP32 rate on this part).
+//
+// As pkdGravAll does (pkd.c:2917-2944), the box a bucket walks with is the
+// bounds of its active particles; with every particle active that is the
+// node's own box.  A bucket with no active particle gets a negative extent
+// and is skipped.  The softening maximum runs over all its particles
+// (pkdBucketWalk walk.c:319-324).
 __global__ void k_bucket_prep(TsphDevTree T, TsphDevParts P) {
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= T.dcnt[1]) return;
     int node = T.leaves[b];
     int lo = T.pLower[node], hi = T.pUpper[node];
+    double amn[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, amx[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
+    double sm = 0.0;
+    int nAct = 0;
+    for (int p = lo; p <= hi; ++p) {
+        sm = fmax(sm, P.h[p]);
+        if (!P.act[p]) continue;
+        ++nAct;
+        const double r[3] = {P.x[p], P.y[p], P.z[p]};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            amn[k] = fmin(amn[k], r[k]);
+            amx[k] = fmax(amx[k], r[k]);
+        }
+    }
+    if (nAct == 0) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) amn[k] = amx[k] = T.r[3 * node + k];
+    }
     double bc[3];
     float bh[3], bl[3], mn[3], mx[3];
     float ext = 0.0f;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        double a = T.bnd[6 * node + k], c = T.bnd[6 * node + 3 + k];
-        bc[k] = 0.5 * (a + c);
+        T.bact[6 * b + k] = amn[k];
+        T.bact[6 * b + 3 + k] = amx[k];
+        bc[k] = 0.5 * (amn[k] + amx[k]);
         split2f(bc[k], bh[k], bl[k]);
-        mn[k] = (float)(a - bc[k]);
-        mx[k] = (float)(c - bc[k]);
+        mn[k] = (float)(amn[k] - bc[k]);
+        mx[k] = (float)(amx[k] - bc[k]);
         ext = fmaxf(ext, fmaxf(fabsf(mn[k]), fabsf(mx[k])));
     }
-    double sm = 0.0;
-    for (int p = lo; p <= hi; ++p) sm = fmax(sm, P.h[p]);
     T.brec[4 * b] = make_float4(bh[0], bh[1], bh[2], (float)sm);
-    T.brec[4 * b + 1] = make_float4(bl[0], bl[1], bl[2], ext);
-    T.brec[4 * b + 2] = make_float4(mn[0], mn[1], mn[2], 0.0f);
+    T.brec[4 * b + 1] = make_float4(bl[0], bl[1], bl[2], nAct > 0 ? ext : -1.0f);
+    T.brec[4 * b + 2] = make_float4(mn[0], mn[1], mn[2], (float)nAct);
     T.brec[4 * b + 3] = make_float4(mx[0], mx[1], mx[2], 0.0f);
 }
 

@@ -106,7 +106,29 @@ struct SphArgs {
     TsphDevCounters *cnt;
     int *work;
     const double *seed;     // optional fBall2 seeds (tree order) or null
+    TsphDevState C;         // caller-order state (the inactive particles' dtNew, mumax)
 };
+
+// The pressure pass acts on active particles (G.act); an inactive one
+// takes part only in pairs with an active partner, and from those only its
+// dtNew and mumax change (SphPressureTerms.h:97-110: SETDTNEW_PQ and the
+// viscous mu update both sides; initSphPressureTermsParticle resets only
+// active particles, smoothfcn.c:2204-2221; pairs of two inactive
+// particles are skipped, smoothfcn.c:2331).  Final per-particle write:
+__device__ __forceinline__ void pressure_store(const SphArgs &A, int i, bool ai, double ax,
+                                               double ay, double az, double uPdV, double uAV,
+                                               double mu, double dtN) {
+    const TsphSphBufs &S = A.S;
+    if (ai) {
+        S.hax[i] = ax; S.hay[i] = ay; S.haz[i] = az;
+        S.uPdV[i] = uPdV; S.uAV[i] = uAV; S.mumax[i] = mu; S.dtNew[i] = dtN;
+    } else {
+        const int o = A.G.iord[i];
+        const double m0 = A.C.mumax[o], d0 = A.C.dtNew[o];
+        S.mumax[i] = mu > m0 ? mu : m0;
+        S.dtNew[i] = dtN < d0 ? dtN : d0;
+    }
+}
 
 #define SNBR 192      // neighbours summed in canonical (index) order
 #define KSTK 896      // ball-gather walk stack per warp (the size of the sum transpose)
@@ -621,20 +643,30 @@ __global__ void k_gas_split(int ng, TsphDevParts G, const double *__restrict__ u
     G.pl[i] = make_float4(lx, ly, lz, (float)u[i]);
 }
 
-// pkdGasPressure (pkd.c:5750-5785) for the adiabatic gas model.
-__global__ void k_gas_pressure(int ng, TsphSphBufs S) {
+// pkdGasPressure (pkd.c:5750-5785) for the adiabatic gas model.  Every gas
+// particle's timestep p->dt (caller order, kept across passes) drops to
+// its Courant time "to scare the neighbours" (pkd.c:5779-5781).
+__global__ void k_gas_pressure(int ng, TsphSphBufs S, const int *__restrict__ iord, TsphDevState C) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= ng) return;
+    const int o = iord[i];
     double PoverRhoGas = cS.gammam1 * S.u[i];
     double cGas = sqrt(cS.gamma * PoverRhoGas);
     double PoverRho = PoverRhoGas + 0.0;
     S.pr2[i] = PoverRho / S.rho[i];
     double c = sqrt(cGas * cGas + (5. / 3.) * 0.0 + 2.0 * 0.0);
     S.cs[i] = c;
-    double dt = cS.dtFacCourant * sqrt(S.fBall2[i] * 0.25) / (2 * c);
-    double dtp = FLT_MAX;
+    double dtp = C.dt[o];
+    const double uTotDot = C.udot[o];
+    double dt;
+    if (uTotDot > 0)
+        dt = cS.dtFacCourant * sqrt(S.fBall2[i] * 0.25 / (4 * (c * c + (5. / 3.) * uTotDot * dtp)));
+    else
+        dt = cS.dtFacCourant * sqrt(S.fBall2[i] * 0.25) / (2 * c);
     if (dt < dtp) dtp = dt;
     S.dtp[i] = dtp;
+    C.dt[o] = dtp;
+    C.cs[o] = c;
     // the pair terms' per-particle factors (SphPressureTerms.h:1-40)
     double fb = S.fBall2[i], rho = S.rho[i], d2 = rho * rho;
     double ph = sqrt(0.25 * fb);
@@ -842,6 +874,7 @@ __global__ void __launch_bounds__(SW * 32) k_pressure_lists(SphArgs A) {
         if (lane == 0) i = atomicAdd(A.work, 1);
         i = __shfl_sync(FULL, i, 0);
         if (i >= ng) break;
+        const bool ai = A.G.act[i] != 0;
         if constexpr (F32) {
             const float4 hi = A.G.ph[i], lo = A.G.pl[i];
             float ax = 0, ay = 0, az = 0, uPdV = 0, uAV = 0, mu = 0.0f, dtN = FLT_MAX;
@@ -849,6 +882,7 @@ __global__ void __launch_bounds__(SW * 32) k_pressure_lists(SphArgs A) {
             const int nOwn = S.nnCount[i];
             for (int e = lane; e < nOwn; e += 32) {
                 int j = own[e];
+                if (!ai && !A.G.act[j]) continue;
                 float dx, dy, dz;
                 split_dx(hi, lo, A.G.ph[j], A.G.pl[j], dx, dy, dz);
                 sph_pair_f(S, A.G, i, j, dx, dy, dz, dx * dx + dy * dy + dz * dz, true, ax, ay, az,
@@ -857,6 +891,7 @@ __global__ void __launch_bounds__(SW * 32) k_pressure_lists(SphArgs A) {
             const int ro = i > 0 ? S.roff[i - 1] : 0, nRev = S.roff[i] - ro;
             for (int e = lane; e < nRev; e += 32) {
                 int j = S.rlist[ro + e];
+                if (!ai && !A.G.act[j]) continue;
                 float dx, dy, dz;
                 split_dx(A.G.ph[j], A.G.pl[j], hi, lo, dx, dy, dz);
                 sph_pair_f(S, A.G, j, i, dx, dy, dz, dx * dx + dy * dy + dz * dz, false, ax, ay, az,
@@ -872,11 +907,9 @@ __global__ void __launch_bounds__(SW * 32) k_pressure_lists(SphArgs A) {
                 mu = fmaxf(mu, __shfl_xor_sync(FULL, mu, o));
                 dtN = fminf(dtN, __shfl_xor_sync(FULL, dtN, o));
             }
-            if (lane == 0) {
-                S.hax[i] = ax; S.hay[i] = ay; S.haz[i] = az;
-                S.uPdV[i] = uPdV; S.uAV[i] = uAV; S.mumax[i] = mu;
-                S.dtNew[i] = dtN == FLT_MAX ? (double)FLT_MAX : (double)dtN;
-            }
+            if (lane == 0)
+                pressure_store(A, i, ai, ax, ay, az, uPdV, uAV, mu,
+                               dtN == FLT_MAX ? (double)FLT_MAX : (double)dtN);
             continue;
         }
         const double xi = A.G.x[i], yi = A.G.y[i], zi = A.G.z[i];
@@ -885,6 +918,7 @@ __global__ void __launch_bounds__(SW * 32) k_pressure_lists(SphArgs A) {
         const int nOwn = S.nnCount[i];
         for (int e = lane; e < nOwn; e += 32) {
             int j = own[e];
+            if (!ai && !A.G.act[j]) continue;
             double dx, dy, dz;
             double d2 = dist2_exact(xi, yi, zi, A.G.x[j], A.G.y[j], A.G.z[j], dx, dy, dz);
             sph_pair(S, A.G.m, i, j, dx, dy, dz, d2, true, ax, ay, az, uPdV, uAV, mu, dtN);
@@ -892,6 +926,7 @@ __global__ void __launch_bounds__(SW * 32) k_pressure_lists(SphArgs A) {
         const int ro = i > 0 ? S.roff[i - 1] : 0, nRev = S.roff[i] - ro;
         for (int e = lane; e < nRev; e += 32) {
             int j = S.rlist[ro + e];
+            if (!ai && !A.G.act[j]) continue;
             double dx, dy, dz;
             double d2 = dist2_exact(A.G.x[j], A.G.y[j], A.G.z[j], xi, yi, zi, dx, dy, dz);
             sph_pair(S, A.G.m, j, i, dx, dy, dz, d2, false, ax, ay, az, uPdV, uAV, mu, dtN);
@@ -904,10 +939,7 @@ __global__ void __launch_bounds__(SW * 32) k_pressure_lists(SphArgs A) {
             mu = a > mu ? a : mu;
             dtN = b < dtN ? b : dtN;
         }
-        if (lane == 0) {
-            S.hax[i] = ax; S.hay[i] = ay; S.haz[i] = az;
-            S.uPdV[i] = uPdV; S.uAV[i] = uAV; S.mumax[i] = mu; S.dtNew[i] = dtN;
-        }
+        if (lane == 0) pressure_store(A, i, ai, ax, ay, az, uPdV, uAV, mu, dtN);
     }
 }
 
@@ -929,6 +961,7 @@ __global__ void __launch_bounds__(SW * 32) k_pressure(SphArgs A) {
         const float xf = (float)xi, yf = (float)yi, zf = (float)zi;
         const double fbi = A.S.fBall2[i];
         const TsphSphBufs &S = A.S;
+        const bool ai = A.G.act[i] != 0;
         double ax = 0, ay = 0, az = 0, uPdV = 0, uAV = 0, mu = 0.0, dtN = FLT_MAX;
         int sp = 1;
         if (lane == 0) stack[0] = A.T.sysRoot[A.G.rid[i]];
@@ -962,6 +995,7 @@ __global__ void __launch_bounds__(SW * 32) k_pressure(SphArgs A) {
             int cnt = leaf ? lk.y : 0;
             for (int kk = 0; kk < cnt; ++kk) {
                 int j = lk.x + kk;
+                if (!ai && !A.G.act[j]) continue;
                 double xj = A.G.x[j], yj = A.G.y[j], zj = A.G.z[j];
                 double dxi, dyi, dzi, dxj, dyj, dzj;
                 double d2i = dist2_exact(xi, yi, zi, xj, yj, zj, dxi, dyi, dzi);
@@ -1040,10 +1074,7 @@ __global__ void __launch_bounds__(SW * 32) k_pressure(SphArgs A) {
             mu = a > mu ? a : mu;
             dtN = b < dtN ? b : dtN;
         }
-        if (lane == 0) {
-            S.hax[i] = ax; S.hay[i] = ay; S.haz[i] = az;
-            S.uPdV[i] = uPdV; S.uAV[i] = uAV; S.mumax[i] = mu; S.dtNew[i] = dtN;
-        }
+        if (lane == 0) pressure_store(A, i, ai, ax, ay, az, uPdV, uAV, mu, dtN);
         __syncwarp();
     }
 }
@@ -1089,12 +1120,18 @@ __global__ void k_gas_nodes(TsphDevTree T) {
     T.wlink[i] = make_int4(T.pLower[i], T.pUpper[i] - T.pLower[i] + 1, T.upper[i], 0);
 }
 
-__global__ void k_scatter_hydro(int ng, const int *__restrict__ iord, TsphSphBufs S, TsphDevState C) {
+// pressure-pass results to caller order: forces and energy rates of the
+// active particles, dtNew and mumax of every gas particle
+__global__ void k_scatter_hydro(int ng, TsphDevParts G, TsphSphBufs S, TsphDevState C) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= ng) return;
-    int o = iord[i];
+    int o = G.iord[i];
+    C.dtNew[o] = S.dtNew[i];
+    C.mumax[o] = S.mumax[i];
+    if (!G.act[i]) return;
     C.hax[o] = S.hax[i]; C.hay[o] = S.hay[i]; C.haz[o] = S.haz[i];
     C.udot[o] = S.uPdV[i] + S.uAV[i];
+    C.updv[o] = S.uPdV[i];
 }
 
 __global__ void k_to_caller1(int ng, const int *__restrict__ iord, const double *__restrict__ a,
@@ -1245,6 +1282,7 @@ static int run_density(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_out
     A.cnt = ctx->dCnt;
     A.work = (int *)&ctx->dCnt->pad;
     A.seed = (sp->bLearnedH && S.haveSeed) ? S.seed : nullptr;
+    A.C = ctx->C;
     TSPH_CK(cudaMemsetAsync(ctx->dCnt, 0, sizeof(TsphDevCounters), ctx->stream));
     TSPH_CK(cudaMemsetAsync(S.listFlag, 0, sizeof(int), ctx->stream));
     if (!cap) cudaEventRecord(ctx->ev[6], ctx->stream);
@@ -1310,7 +1348,7 @@ static int run_pressure(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_ou
         set_sph_const(ctx, sp);
         cudaEventRecord(ctx->ev[8], ctx->stream);
     }
-    k_gas_pressure<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, S);
+    k_gas_pressure<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, S, ctx->G.iord, ctx->C);
     TSPH_LAUNCH_CK("k_gas_pressure");
     // reverse neighbour lists (the kernels stand down when a list overflowed)
     TSPH_CK(cudaMemsetAsync(S.rcnt, 0, sizeof(int) * ng, ctx->stream));
@@ -1336,6 +1374,7 @@ static int run_pressure(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_ou
     A.cnt = ctx->dCnt;
     A.work = (int *)&ctx->dCnt->pad;
     A.seed = nullptr;
+    A.C = ctx->C;
     TSPH_CK(cudaMemsetAsync(ctx->dCnt, 0, sizeof(TsphDevCounters), ctx->stream));
     SphArgs AL = A;
     AL.work = S.listFlag + 2;
@@ -1348,7 +1387,7 @@ static int run_pressure(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_ou
     }
     k_pressure<<<ctx->smCount * 4, SW * 32, 0, ctx->stream>>>(A);
     TSPH_LAUNCH_CK("k_pressure");
-    k_scatter_hydro<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, ctx->G.iord, S, ctx->C);
+    k_scatter_hydro<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, ctx->G, S, ctx->C);
     TSPH_LAUNCH_CK("k_scatter_hydro");
     if (cap) {
         S.havePressure = true;
@@ -1484,51 +1523,87 @@ extern "C" int tsph_get_neighbour_hash(tsph_ctx *ctx, int *count, unsigned long 
 // ---------------------------------------------------------------------------
 // kick and drift (pkdKick pkd.c:3780-3969, pkdDrift pkd.c:3686-3778)
 // ---------------------------------------------------------------------------
-__global__ void k_kick(int n, int ngas, double dt, TsphDevState C) {
+// pkdKick (pkd.c:3780-3969) for a non-comoving canonical run with
+// NOCOOLING (dvFacOne = dvPredFacOne = 1, dvFacTwo = duDelta = dt): the
+// particles on rung iRung (every particle when iRung < 0).  The opening
+// kick of a KDK step leaves vPred = v and uPred = u from before it
+// (dvPredFacTwo = duPredDelta = 0, msrKickKDKOpen master.c:6540-6639); the
+// closing kick predicts them to its end (msrKickKDKClose master.c:6644-6741).
+// a is gravity plus, for gas, the hydrodynamic acceleration.
+__global__ void k_kick_rung(int n, int ngas, int iRung, double dt, int bClose, TsphDevState C) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    bool gas = i < ngas;
-    double ax = C.ax[i], ay = C.ay[i], az = C.az[i];
-    if (gas) { ax += C.hax[i]; ay += C.hay[i]; az += C.haz[i]; }
-    double vx = C.vx[i] + ax * dt, vy = C.vy[i] + ay * dt, vz = C.vz[i] + az * dt;
-    if (gas) {
-        C.vpx[i] = vx; C.vpy[i] = vy; C.vpz[i] = vz;
-        double up = C.u[i] + C.udot[i] * dt;
-        if (up < 0) up = 0;
-        C.upred[i] = up;
-        C.u[i] = up;
-    } else {
-        C.vpx[i] = vx; C.vpy[i] = vy; C.vpz[i] = vz;
+    if (iRung >= 0 && C.rung[i] != iRung) return;
+    const bool gas = i < ngas;
+    double a[3] = {C.ax[i], C.ay[i], C.az[i]};
+    if (gas) { a[0] = xadd(a[0], C.hax[i]); a[1] = xadd(a[1], C.hay[i]); a[2] = xadd(a[2], C.haz[i]); }
+    double *v[3] = {C.vx, C.vy, C.vz};
+    double *vp[3] = {C.vpx, C.vpy, C.vpz};
+    const double predFac = bClose ? dt : 0.0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {   // no contraction: the reference's rounding
+        const double vk = v[k][i];
+        if (gas) vp[k][i] = xadd(vk, xmul(a[k], predFac));
+        v[k][i] = xadd(vk, xmul(a[k], dt));
     }
-    C.vx[i] = vx; C.vy[i] = vy; C.vz[i] = vz;
+    if (gas) {
+        const double u = C.u[i], udot = C.udot[i];
+        C.upred[i] = xadd(u, xmul(udot, predFac));
+        C.u[i] = xadd(u, xmul(udot, dt));
+    }
 }
 
-__global__ void k_drift(int n, double dt, int bPeriodic, double L, TsphDevState C) {
+// pkdDrift (pkd.c:3686-3778) and, for gas, pkdKickVpred (pkd.c:6489-6552)
+// as msrDrift runs them (master.c:6306-6437): r += v dt with the periodic
+// wrap, then vPred += a dt and uPred += uDot dt.
+__global__ void k_drift(int n, int ngas, double dt, int bPeriodic, double L, TsphDevState C) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double *r[3] = {C.x, C.y, C.z};
     const double *v[3] = {C.vx, C.vy, C.vz};
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        double x = r[k][i] + dt * v[k][i];
+    for (int k = 0; k < 3; ++k) {   // no contraction: the reference's rounding
+        double x = xadd(r[k][i], xmul(dt, v[k][i]));
         if (bPeriodic) {
-            if (x >= 0.5 * L) x -= L;
-            if (x < -0.5 * L) x += L;
+            if (x >= 0.5 * L) x = xsub(x, L);
+            if (x < -0.5 * L) x = xadd(x, L);
         }
         r[k][i] = x;
     }
+    if (i < ngas && dt != 0.0) {
+        C.vpx[i] = xadd(C.vpx[i], xmul(xadd(C.ax[i], C.hax[i]), dt));
+        C.vpy[i] = xadd(C.vpy[i], xmul(xadd(C.ay[i], C.hay[i]), dt));
+        C.vpz[i] = xadd(C.vpz[i], xmul(xadd(C.az[i], C.haz[i]), dt));
+        C.upred[i] = xadd(C.upred[i], xmul(C.udot[i], dt));
+    }
 }
 
-extern "C" int tsph_kick(tsph_ctx *ctx, double dt) {
+int tsph_kick_launch(tsph_ctx *ctx, int iRung, double dt, int bClose) {
+    k_kick_rung<<<tsph_blocks(ctx->n, 256), 256, 0, ctx->stream>>>(ctx->n, ctx->ngas, iRung, dt,
+                                                                     bClose, ctx->C);
+    TSPH_LAUNCH_CK("k_kick_rung");
+    return TSPH_OK;
+}
+
+int tsph_drift_launch(tsph_ctx *ctx, double dt, int bPeriodic, double dPeriod) {
+    k_drift<<<tsph_blocks(ctx->n, 256), 256, 0, ctx->stream>>>(ctx->n, ctx->ngas, dt, bPeriodic,
+                                                                 dPeriod, ctx->C);
+    TSPH_LAUNCH_CK("k_drift");
+    return TSPH_OK;
+}
+
+extern "C" int tsph_kick_rung(tsph_ctx *ctx, int iRung, double dt, int bClose) {
     if (!ctx) return TSPH_ERR_ARG;
     if (!ctx->haveParts || !ctx->haveVel) return TSPH_ERR_STATE;
     cudaSetDevice(ctx->device);
     if (ctx->n == 0) return TSPH_OK;
-    k_kick<<<tsph_blocks(ctx->n, 256), 256, 0, ctx->stream>>>(ctx->n, ctx->ngas, dt, ctx->C);
-    TSPH_LAUNCH_CK("k_kick");
+    int rc = tsph_kick_launch(ctx, iRung, dt, bClose);
+    if (rc) return rc;
     if (!ctx->capturing) TSPH_CK(cudaStreamSynchronize(ctx->stream));
     return TSPH_OK;
 }
+
+extern "C" int tsph_kick(tsph_ctx *ctx, double dt) { return tsph_kick_rung(ctx, -1, dt, 1); }
 
 extern "C" int tsph_drift(tsph_ctx *ctx, double dt, int bPeriodic, double dPeriod) {
     if (!ctx) return TSPH_ERR_ARG;
@@ -1536,8 +1611,8 @@ extern "C" int tsph_drift(tsph_ctx *ctx, double dt, int bPeriodic, double dPerio
     if (bPeriodic && !(dPeriod > 0)) return TSPH_ERR_ARG;
     cudaSetDevice(ctx->device);
     if (ctx->n == 0) return TSPH_OK;
-    k_drift<<<tsph_blocks(ctx->n, 256), 256, 0, ctx->stream>>>(ctx->n, dt, bPeriodic, dPeriod, ctx->C);
-    TSPH_LAUNCH_CK("k_drift");
+    int rc = tsph_drift_launch(ctx, dt, bPeriodic, dPeriod);
+    if (rc) return rc;
     if (!ctx->capturing) TSPH_CK(cudaStreamSynchronize(ctx->stream));
     ctx->S.haveDensity = ctx->S.havePressure = false;
     ctx->haveGrav = false;

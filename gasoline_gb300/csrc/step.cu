@@ -2,10 +2,11 @@
 // captured once as a CUDA graph and replayed.
 //
 // The step follows the reference's single-rung msrTopStepKDK
-// (master.c:8242-8465): opening kick by dt/2 (pkdKick), drift by dt
-// (pkdDrift), forces at the new positions (pkdGravAll, then for the gas
-// smSmooth(SMX_DENDVDX), pkdGasPressure, smReSmooth(SMX_SPHPRESSURETERMS)),
-// closing kick by dt/2.  In graph mode every launch of that sequence is
+// (master.c:8242-8465): opening kick by dt/2 (msrKickKDKOpen), two drifts
+// by dt/2 (msrDrift: pkdDrift + pkdKickVpred), forces at the new positions
+// for every particle (pkdGravAll, then for the gas smSmooth(SMX_DENDVDX),
+// pkdGasPressure, smReSmooth(SMX_SPHPRESSURETERMS)), closing kick by dt/2
+// (msrKickKDKClose).  In graph mode every launch of that sequence is
 // recorded once and the whole step replays as one graph launch: no host
 // round trip, no per-kernel launch cost, which is what many small systems
 // in one context need.  A captured build runs a fixed number of top-phase
@@ -26,14 +27,18 @@ __global__ void k_coord_maxabs(int n, TsphDevState C, unsigned long long *out) {
 
 static int step_body(tsph_ctx *ctx, double dt, const tsph_grav_params *gp,
                      const tsph_sph_params *sp) {
-    int rc = tsph_kick(ctx, 0.5 * dt);
-    if (!rc) rc = tsph_drift(ctx, dt, gp->bPeriodic, gp->dPeriod);
+    const int actRung = ctx->actRung;
+    ctx->actRung = 0;   // one rung: every particle is active
+    int rc = tsph_kick_rung(ctx, -1, 0.5 * dt, 0);
+    if (!rc) rc = tsph_drift(ctx, 0.5 * dt, gp->bPeriodic, gp->dPeriod);
+    if (!rc) rc = tsph_drift(ctx, 0.5 * dt, gp->bPeriodic, gp->dPeriod);
     if (!rc) rc = tsph_grav_all(ctx, gp, nullptr);
     if (!rc && sp && ctx->ngas > 0) {
         rc = tsph_smooth(ctx, TSPH_SMX_DENDVDX, sp, nullptr);
         if (!rc) rc = tsph_smooth(ctx, TSPH_SMX_SPHPRESSURETERMS, sp, nullptr);
     }
-    if (!rc) rc = tsph_kick(ctx, 0.5 * dt);
+    if (!rc) rc = tsph_kick_rung(ctx, -1, 0.5 * dt, 1);
+    ctx->actRung = actRung;
     return rc;
 }
 

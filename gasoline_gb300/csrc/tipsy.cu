@@ -23,6 +23,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <float.h>
 #include <sys/stat.h>
 
 #include "tsph_ctx.cuh"
@@ -96,6 +97,9 @@ k_tipsy_decode(int i0, int i1, const unsigned int *__restrict__ raw, int swap, i
     C.hax[i] = C.hay[i] = C.haz[i] = 0.0;
     C.ax[i] = C.ay[i] = C.az[i] = C.dtGrav[i] = 0.0;
     C.fb2prev[i] = C.divvprev[i] = 0.0;
+    C.rung[i] = 0;
+    C.dt[i] = C.dtNew[i] = FLT_MAX;
+    C.mumax[i] = C.updv[i] = C.cs[i] = 0.0;
     F.rho[i] = rho; F.metals[i] = metals; F.tform[i] = tform;
     piord[i] = (int)i;
     giord[i] = (int)i;

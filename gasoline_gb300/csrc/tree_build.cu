@@ -1329,6 +1329,7 @@ void tsph_free_tree(TsphDevTree &T) {
     TFREE(T.rLo); TFREE(T.rHi); TFREE(T.sysRoot); TFREE(T.rEnd); TFREE(T.dcnt);
     if (T.brec) cudaFree(T.brec);
     T.brec = nullptr;
+    TFREE(T.bact);
     free(T.hLo);
     free(T.hHi);
     T.hLo = T.hHi = nullptr;
@@ -1375,6 +1376,7 @@ static int ensure_nodes(tsph_ctx *ctx, TsphDevTree &T, int nNodes) {
         rc |= tsph_grow(ctx, &T.wmom1, cap);
         rc |= tsph_grow(ctx, &T.leaves, cap);
         rc |= tsph_grow(ctx, &T.brec, (size_t)4 * cap);
+        rc |= tsph_grow(ctx, &T.bact, (size_t)6 * cap);
         if (rc) return TSPH_ERR_NOMEM;
         T.cap = cap;
     }
@@ -1498,7 +1500,25 @@ static int task_size(tsph_ctx *ctx, const TsphDevTree &T, int n) {
     return S;
 }
 
+// Activity of every tree slot in the final particle order: rung >= the
+// context's active rung (msrActiveRung(actRung, 1)).
+__global__ void k_tree_act(int n, const int *__restrict__ iord, const int *__restrict__ rung,
+                           int actRung, int *act) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) act[i] = rung[iord[i]] >= actRung;
+}
+
+static int build_tree_body(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, int nBucket);
+
 int tsph_build_tree(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, int nBucket) {
+    int rc = build_tree_body(ctx, P, T, n, nBucket);
+    if (rc || n == 0) return rc;
+    k_tree_act<<<tsph_blocks(n, 256), 256, 0, ctx->stream>>>(n, P.iord, ctx->C.rung, ctx->actRung, P.act);
+    TSPH_LAUNCH_CK("k_tree_act");
+    return TSPH_OK;
+}
+
+static int build_tree_body(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, int nBucket) {
     TsphBuildBufs &B = ctx->B;
     const int BS = 256;
     if (nBucket < 1) return TSPH_ERR_ARG;

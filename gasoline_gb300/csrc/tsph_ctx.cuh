@@ -130,6 +130,10 @@ struct tsph_ctx {
     int snapCap;
     bool snapValid;
     int snapNStar;               // star count of the last snapshot read
+
+    // adaptive timesteps: force passes act on particles with rung >= actRung
+    // (the reference's TYPE_ACTIVE after msrActiveRung(actRung, 1))
+    int actRung;
     unsigned int *dSnapStatus;
     cudaEvent_t snapEv[2];
 
@@ -140,7 +144,8 @@ struct tsph_ctx {
 
     TsphHnet hnet;
 
-    unsigned long long *dAux;    // device scratch: [0] gas max |coordinate| bits
+    unsigned long long *dAux;    // device scratch: [0] gas max |coordinate| bits, [1] capture
+                                 // extent, [2..] the rung statistics of the multistep driver
     double *hTmp;                // host staging of tsph_get_sph
     void *hEw;                   // host block of the Ewald constants
     size_t hTmpN;
@@ -208,6 +213,8 @@ int tsph_tree_moments(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, dou
 void tsph_free_build(TsphBuildBufs &B);
 int tsph_apply_gas_systems(tsph_ctx *ctx);
 int tsph_load_begin(tsph_ctx *ctx, int n);
+int tsph_kick_launch(tsph_ctx *ctx, int iRung, double dt, int bClose);
+int tsph_drift_launch(tsph_ctx *ctx, double dt, int bPeriodic, double dPeriod);
 int tsph_load_gas(tsph_ctx *ctx, int ngas);
 void tsph_free_snapshot(tsph_ctx *ctx);
 int tsph_fold_status(tsph_ctx *ctx);

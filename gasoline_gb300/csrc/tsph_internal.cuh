@@ -83,8 +83,11 @@ struct TsphDevTree {
     int *dcnt;        // device: nNodes, nLeaves
     int rCap;
     int lastTopLevels; // top-phase levels of the last host-paced build
-    float4 *brec;     // per bucket: centre hi + soft max, centre lo + extent,
-                      // box min - centre (+ n), box max - centre (FP32)
+    float4 *brec;     // per bucket: centre hi + soft max, centre lo + extent
+                      // (negative: no active particle), box min - centre
+                      // (+ active count), box max - centre (FP32)
+    double *bact;     // per bucket: bounds of its active particles, min xyz,
+                      // max xyz (pkdGravAll's bndActive, pkd.c:2917-2935)
 };
 
 struct TsphDevParts {
@@ -93,6 +96,7 @@ struct TsphDevParts {
     double *x, *y, *z, *m, *h;   // tree order
     int *iord;                   // caller index of each tree-order slot
     int *rid;                    // tree (range) of each tree-order slot
+    int *act;                    // 1 if the slot's particle is active (rung >= the active rung)
     float4 *ph;                  // hi xyz + mass (float)
     float4 *pl;                  // lo xyz + soft (float)
     // outputs in tree order
@@ -112,6 +116,11 @@ struct TsphDevState {
     double *ax, *ay, *az, *pot, *dtGrav; // gravity
     double *hax, *hay, *haz, *udot;      // SPH (gas only): hydro accel, uDotPdV+uDotAV
     double *fb2prev, *divvprev;          // last density pass: fBall2, divv (h-network inputs)
+    // adaptive timesteps: the reference's p->iRung, p->dt, p->dtNew, p->mumax
+    // and p->uDotPdV, kept across passes (an inactive particle keeps its own)
+    int *rung;
+    double *dt, *dtNew, *mumax, *updv;
+    double *cs;                          // gas sound speed of the last pressure pass (p->c)
 };
 
 // Counters accumulated by the walk (integers: deterministic).

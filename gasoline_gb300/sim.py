@@ -1,12 +1,13 @@
-"""Host-side step driver over libtsph, in the reference's single-rung
-kick-drift-kick order (msrTopStepKDK, master.c:8242-8465):
+"""Host-side step driver over libtsph, in the reference's kick-drift-kick
+order (msrTopStepKDK, master.c:8242-8465):
 
     forces(t=0)                              (main.c:363-387, msrInitSph)
-    repeat:  kick(dt/2); drift(dt); forces(); kick(dt/2)
+    repeat:  kick_open(dt/2); drift(dt/2); drift(dt/2); forces(); kick_close(dt/2)
 
 where forces() = gravity (pkdGravAll) and, for the gas particles, the
 density pass (SMX_DENDVDX), gas pressure and the pressure pass
-(SMX_SPHPRESSURETERMS).  Adaptive rungs are not part of this path.
+(SMX_SPHPRESSURETERMS).  `top_step` runs the same with adaptive rungs
+(tsph_top_step_kdk).
 """
 import time
 
@@ -51,10 +52,22 @@ class Simulation:
         return rec
 
     def step(self, dt):
-        self.ctx.kick(0.5 * dt)
-        self.ctx.drift(dt, self.periodic, self.L)
+        self.ctx.kick_rung(-1, 0.5 * dt, close=False)
+        self.ctx.drift(0.5 * dt, self.periodic, self.L)
+        self.ctx.drift(0.5 * dt, self.periodic, self.L)
         rec = self.forces()
-        self.ctx.kick(0.5 * dt)
+        self.ctx.kick_rung(-1, 0.5 * dt, close=True)
+        self.step_count += 1
+        rec["step"] = self.step_count
+        self.log.append(rec)
+        return rec
+
+    def top_step(self, dt, st, t=0.0):
+        """One base step dt with adaptive rungs (msrTopStepKDK with rungs)."""
+        t0 = time.perf_counter()
+        sp = self.sp if self.ngas > 0 else None
+        rec = self.ctx.top_step_kdk(t, dt, self.gp, sp, st)
+        rec["wall_s"] = time.perf_counter() - t0
         self.step_count += 1
         rec["step"] = self.step_count
         self.log.append(rec)

@@ -260,14 +260,66 @@ int tsph_hnet_loss_grad_noalloc(const float *params, int n, const float *x3,
 
 /* --- kick-drift-kick (pkdKick / pkdDrift) ------------------------------ */
 
-/* v += a*dt (a = gravity + hydro); gas: vPred = v_old + a*dt,
- * u += uDot*dt with uDot = uDotPdV + uDotAV, clamped at 0 (NOCOOLING,
- * pkd.c:3936-3939). */
+/* Every particle: v += a*dt (a = gravity + hydro); gas: vPred = v + a*dt,
+ * u += uDot*dt and uPred = u + uDot*dt with uDot = uDotPdV + uDotAV
+ * (NOCOOLING, pkd.c:3936-3939) -- the closing kick of a KDK step. */
 int tsph_kick(tsph_ctx *ctx, double dt);
-/* r += v*dt, wrapped into [-L/2, L/2) when periodic (pkd.c:3726-3756). */
+/* r += v*dt, wrapped into [-L/2, L/2) when periodic (pkdDrift
+ * pkd.c:3726-3756); for gas also vPred += a*dt and uPred += uDot*dt
+ * (pkdKickVpred pkd.c:6489-6552), as msrDrift runs them. */
 int tsph_drift(tsph_ctx *ctx, double dt, int bPeriodic, double dPeriod);
+/* pkdKick (pkd.c:3780-3969) for the particles on rung iRung (all when
+ * iRung < 0): v += a*dt and, for gas, u += uDot*dt.  bClose = 0 is the
+ * opening kick of a KDK step (vPred, uPred keep the values from before
+ * it, msrKickKDKOpen master.c:6540); bClose = 1 the closing kick (vPred,
+ * uPred predicted to its end, msrKickKDKClose master.c:6644).
+ * tsph_kick(ctx, dt) is tsph_kick_rung(ctx, -1, dt, 1). */
+int tsph_kick_rung(tsph_ctx *ctx, int iRung, double dt, int bClose);
 /* Copy state to the host in caller order; NULL skips a field. */
 int tsph_get_state(tsph_ctx *ctx, double *pos, double *vel, double *u);
+
+/* --- adaptive timesteps (rungs) -----------------------------------------
+ * Particle i steps with dDelta / 2^rung[i].  tsph_top_step_kdk advances
+ * every particle by one base step dDelta as msrTopStepKDK does
+ * (master.c:8242-8465): timestep criteria and new rungs at each level
+ * (pkdInitDt, pkdGravStep, pkdAccelStep, pkdSphStep, pkdDtToRung),
+ * emergency moves of gas whose dtNew fell below half a step
+ * (pkdEmergencyAdjust), opening and closing kicks per rung, drifts of
+ * every particle, and force passes over the particles of the kicked rungs
+ * (gravity for them on a tree of all particles with each bucket's box
+ * shrunk to its active particles, as pkdGravAll does; SPH densities of all
+ * gas and pressure forces for the active gas).  Call it after forces on
+ * every particle (tsph_grav_all and, with gas, both tsph_smooth passes),
+ * which is the reference's start-up.  Defaults are the reference's
+ * (master.c:572-623). */
+typedef struct {
+    int iMaxRung;        /* rungs 0..iMaxRung-1 (1 to 29) */
+    double dEta;         /* 0.1: acceleration criteria */
+    int bGravStep;       /* 0: dt <= dEta/sqrt(dtGrav) */
+    int bEpsAccStep;     /* 1: dt <= dEta*sqrt(eps/|a|), eps = h for gas */
+    int bSqrtPhiStep;    /* 0: dt <= 3.5*dEta*sqrt(|phi|)/|a| */
+    double dEtauDot;     /* 0.25: gas dt <= dEtauDot*u/|uDotPdV| when cooling adiabatically */
+    double duMinDt;      /* 0: floor of u in that criterion */
+} tsph_step_params;     /* the Courant factor is tsph_sph_params.dEtaCourant */
+
+typedef struct {
+    int iCurrMaxRung;       /* highest rung of any particle after the step */
+    int nForcePasses;       /* force evaluations (one per smallest substep) */
+    long long nActiveSum;   /* particles that received forces, summed over the passes */
+    int nEmergency;         /* emergency rung moves */
+} tsph_step_out;
+
+int tsph_top_step_kdk(tsph_ctx *ctx, double dTime, double dDelta,
+                      const tsph_grav_params *gp, const tsph_sph_params *sp,
+                      const tsph_step_params *st, tsph_step_out *out);
+/* Force passes (tsph_grav_all, tsph_smooth) act on the particles with
+ * rung >= iRung only (msrActiveRung(iRung, 1)); 0, the default, is all. */
+int tsph_set_active_rung(tsph_ctx *ctx, int iRung);
+int tsph_set_rungs(tsph_ctx *ctx, const int *rung);
+/* rung, the timestep dt, dtNew and mumax of every particle (caller order;
+ * NULL skips a field).  dt and dtNew start at FLT_MAX as in the reference's
+ * reader. */
+int tsph_get_rungs(tsph_ctx *ctx, int *rung, double *dt, double *dtNew, double *mumax);
 
 /* --- Tipsy snapshots (pkdReadTipsy pkd.c:297, pkdWriteTipsy pkd.c:1628) --
  * The reference's particle file (tipsydefs.h:9-45): a 32-byte header, then

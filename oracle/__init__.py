@@ -38,6 +38,26 @@ class SphParams(ctypes.Structure):
                 ("iViscosityLimiter", ctypes.c_int)]
 
 
+class StepParams(ctypes.Structure):
+    """Adaptive-timestep parameters (ref_step_params / the library's
+    tsph_step_params), the reference's defaults (master.c:572-623)."""
+    _fields_ = [("nSteps", ctypes.c_int), ("iMaxRung", ctypes.c_int),
+                ("dDelta", ctypes.c_double), ("dEta", ctypes.c_double),
+                ("bGravStep", ctypes.c_int), ("bEpsAccStep", ctypes.c_int),
+                ("bSqrtPhiStep", ctypes.c_int), ("dEtauDot", ctypes.c_double),
+                ("duMinDt", ctypes.c_double)]
+
+
+def step_params(nSteps=1, iMaxRung=4, dDelta=0.01, dEta=0.1, bGravStep=0, bEpsAccStep=1,
+                bSqrtPhiStep=0, dEtauDot=0.25, duMinDt=0.0):
+    return StepParams(nSteps, iMaxRung, dDelta, dEta, bGravStep, bEpsAccStep, bSqrtPhiStep,
+                      dEtauDot, duMinDt)
+
+
+MULTISTEP_FIELDS = ("u", "uPred", "fPot", "dtGrav", "dt", "dtNew", "mumax", "fDensity",
+                    "fBall2", "uDotPdV", "uDotAV", "rung")
+
+
 def grav_params(nBucket=8, iOrder=2, periodic=False, ewald=True, iEwOrder=4,
                 nReps=1, theta=0.7, L=1.0, fEwCut=2.6, fEwhCut=2.8):
     return GravParams(nBucket, iOrder, int(periodic), int(ewald), iEwOrder,
@@ -191,6 +211,52 @@ def reference_tipsy_read(path, standard, ngas, ndark, nstar, dvFac=1.0, dTuFac=1
     if rc:
         raise OSError(f"ref_tipsy_read failed on {path}")
     return pos, vel, f
+
+
+def reference_multistep(pos, vel, mass, soft, ngas, u, gp, sp, st):
+    """The reference's msrTopStepKDK recursion (ref_multistep in the
+    harness) for st.nSteps top steps after the initial forces."""
+    lib = reference().lib
+    pos = _c64(pos, (-1, 3)); vel = _c64(vel, (-1, 3)); mass = _c64(mass); soft = _c64(soft)
+    n = len(mass)
+    uu = _c64(u if ngas > 0 else np.zeros(1))
+    opos = np.zeros((n, 3)); ovel = np.zeros((n, 3)); ovp = np.zeros((n, 3))
+    oacc = np.zeros((n, 3)); f = np.zeros((n, 12))
+    mr = np.zeros(max(st.nSteps, 1), dtype=np.int32); cnt = np.zeros(2)
+    lib.ref_multistep(n, ngas, _d(pos), _d(vel), _d(mass), _d(soft), _d(uu), ctypes.byref(gp),
+                      ctypes.byref(sp), ctypes.byref(st), _d(opos), _d(ovel), _d(ovp), _d(oacc),
+                      _d(f), mr.ctypes.data_as(_IP), _d(cnt))
+    out = dict(pos=opos, vel=ovel, vPred=ovp, acc=oacc, maxRung=mr[:st.nSteps], counts=cnt)
+    for k, name in enumerate(MULTISTEP_FIELDS):
+        out[name] = f[:, k].copy()
+    out["rung"] = out["rung"].astype(np.int32)
+    return out
+
+
+def reference_grav_active(pos, mass, soft, rung, iRung, gp):
+    """The reference's gravity pass over the particles with rung >= iRung."""
+    lib = reference().lib
+    pos = _c64(pos, (-1, 3)); mass = _c64(mass); soft = _c64(soft)
+    r = np.ascontiguousarray(rung, dtype=np.int32)
+    n = len(mass)
+    acc = np.zeros((n, 3)); pot = np.zeros(n); dtg = np.zeros(n); cnt = np.zeros(5)
+    lib.ref_grav_active(n, _d(pos), _d(mass), _d(soft), r.ctypes.data_as(_IP), int(iRung),
+                        ctypes.byref(gp), _d(acc), _d(pot), _d(dtg), _d(cnt))
+    return dict(acc=acc, pot=pot, dtGrav=dtg, counters=cnt)
+
+
+def reference_sph_active(pos, vel, mass, soft, u, rung, iRung, sp):
+    """The reference's SPH pass (all particles gas) with rung >= iRung active."""
+    lib = reference().lib
+    pos = _c64(pos, (-1, 3)); vel = _c64(vel, (-1, 3)); mass = _c64(mass)
+    soft = _c64(soft); u = _c64(u)
+    r = np.ascontiguousarray(rung, dtype=np.int32)
+    n = len(mass)
+    acc = np.zeros((n, 3)); f = np.zeros((n, 6))
+    lib.ref_sph_active(n, _d(pos), _d(vel), _d(mass), _d(soft), _d(u), r.ctypes.data_as(_IP),
+                       int(iRung), ctypes.byref(sp), _d(acc), _d(f))
+    return dict(acc=acc, uDotPdV=f[:, 0].copy(), uDotAV=f[:, 1].copy(), dtNew=f[:, 2].copy(),
+                mumax=f[:, 3].copy(), dt=f[:, 4].copy(), fDensity=f[:, 5].copy())
 
 
 def knn_fball2(pos, nsmooth, periodic=False, L=1.0, nthreads=1):

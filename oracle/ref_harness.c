@@ -439,3 +439,321 @@ int ref_tipsy_read(const char *fname, int bStandard, int nGas, int nDark, int nS
     pkdFinish(pkd);
     return 0;
 }
+
+/*
+ * Adaptive multistepping (rungs) as msrTopStepKDK drives it
+ * (master.c:8242-8465), restated for one rank around the reference's own
+ * pkd-level functions: pkdKick / pkdDrift / pkdKickVpred (master.c:6306-6741
+ * supply their factors for a non-comoving, canonical run: dvFacOne = 1,
+ * dvFacTwo = dt), pkdInitAccel, pkdGravAll over the active rungs,
+ * the non-FastGas msrSph (master.c:9258-9362), pkdInitDt, pkdGravStep,
+ * pkdAccelStep, pkdSphStep, pkdDtToRung (msrDtToRung master.c:7980-8004,
+ * nTruncateRung 0) and pkdEmergencyAdjust (msrEmergencyAdjust
+ * master.c:6742-6763).  Initial forces as main.c:360-386 and msrInitSph
+ * (all particles active, rungs 0).  The first ngas particles are gas.
+ *
+ * Outputs by iOrder: pos, vel, vPred [3n]; a [3n] (total); f[12*i + ..] =
+ * u, uPred, fPot, dtGrav, dt, dtNew, mumax, fDensity, fBall2, uDotPdV,
+ * uDotAV, rung; per top step maxRung[s] (iCurrMaxRung after it) and
+ * counts[0] = force passes, counts[1] = sum of active particles over the
+ * gravity passes.
+ */
+typedef struct {
+    int nSteps;
+    int iMaxRung;
+    double dDelta;
+    double dEta;
+    int bGravStep;
+    int bEpsAccStep;
+    int bSqrtPhiStep;
+    double dEtauDot;
+    double duMinDt;
+} ref_step_params;
+
+typedef struct {
+    PKD pkd;
+    const ref_grav_params *gp;
+    const ref_sph_params *sp;
+    const ref_step_params *st;
+    int ngas;
+    int iCurrMaxRung;
+    double counts[2];
+} MSH;
+
+static void msh_smf(SMF *smf, const ref_sph_params *sp)
+{
+    memset(smf, 0, sizeof(*smf));
+    smf->H = 0.0;
+    smf->a = 1.0;
+    smf->alpha = sp->alpha;
+    smf->beta = sp->beta;
+    smf->gamma = sp->gamma;
+    smf->algam = smf->alpha * sqrt(smf->gamma * (smf->gamma - 1));
+    smf->iViscosityLimiter = sp->iViscosityLimiter;
+    smf->dtFacCourant = pkdDtFacCourant(sp->dEtaCourant, smf->a);
+    smf->dtFacDiffusion = 2 * 0.1;
+    smf->bCannonical = 1;
+    smf->dtMin = FLOAT_MAXVAL;
+}
+
+static UHC msh_uhc(void)
+{
+    UHC u;
+    memset(&u, 0, sizeof(u));
+    return u;
+}
+
+/* msrActiveRung + msrKickKDKOpen / msrKickKDKClose (master.c:6540-6741) */
+static void msh_kick(MSH *m, int iRung, double dDelta, int bClose)
+{
+    pkdActiveRung(m->pkd, iRung, 0);
+    pkdKick(m->pkd, 1.0, dDelta, 1.0, bClose ? dDelta : 0.0, dDelta, bClose ? dDelta : 0.0,
+            GASMODEL_ADIABATIC, 0.0, 0.0, 0.0, msh_uhc());
+}
+
+/* msrDrift (master.c:6306-6437): pkdDrift then pkdKickVpred */
+static void msh_drift(MSH *m, double dDelta)
+{
+    FLOAT fCenter[3] = {0, 0, 0};
+    pkdDrift(m->pkd, dDelta, fCenter, m->gp->bPeriodic, 0, 0, 0.0, 0.0);
+    if (dDelta != 0.0)
+        pkdKickVpred(m->pkd, 1.0, dDelta, dDelta, GASMODEL_ADIABATIC, 0.0, 0.0, 0.0, msh_uhc());
+}
+
+/* msrSph for the non-FastGas branch (master.c:9258-9362) */
+static void msh_sph(MSH *m, int iKickRung)
+{
+    PKD pkd = m->pkd;
+    KDN root;
+    SMX smx;
+    SMF smf;
+    CASTAT cs;
+    struct GasPressureContext gpc;
+    msh_smf(&smf, m->sp);
+    pkdActiveTypeRung(pkd, TYPE_GAS, TYPE_ACTIVE, iKickRung, 1);
+    pkdActiveType(pkd, TYPE_GAS, TYPE_TREEACTIVE | TYPE_SMOOTHACTIVE);
+    pkdBuildLocal(pkd, m->sp->nBucket, OPEN_JOSH, 0.7, 2, 1, 0, &root);
+    free(pkd->kdTop); free(pkd->piLeaf);
+    make_top(pkd, &root);
+    pkdActiveTypeRung(pkd, TYPE_GAS, TYPE_ACTIVE, iKickRung, 1);
+    pkdResetType(pkd, TYPE_GAS, TYPE_SMOOTHDONE | TYPE_NbrOfACTIVE);
+    pkdActiveType(pkd, TYPE_ACTIVE, TYPE_SMOOTHACTIVE | TYPE_DensACTIVE);
+    pkdActiveType(pkd, TYPE_GAS, TYPE_SMOOTHACTIVE);
+    smInitialize(&smx, pkd, &smf, m->sp->nSmooth, m->sp->bPeriodic, 1, SMX_DENDVDX, 1, 0.0);
+    smSmooth(smx, &smf);
+    smFinish(smx, &smf, &cs);
+    pkdActiveType(pkd, TYPE_NbrOfACTIVE, TYPE_SMOOTHACTIVE);
+    memset(&gpc, 0, sizeof(gpc));
+    gpc.iGasModel = GASMODEL_ADIABATIC;
+    gpc.gamma = m->sp->gamma;
+    gpc.gammam1 = m->sp->gamma - 1;
+    gpc.dResolveJeans = 0.0;
+    gpc.dCosmoFac = 1.0;
+    gpc.dtFacCourant = smf.dtFacCourant;
+    pkdGasPressure(pkd, &gpc);
+    smInitialize(&smx, pkd, &smf, m->sp->nSmooth, m->sp->bPeriodic, 1, SMX_SPHPRESSURETERMS, 0, 0.0);
+    smReSmooth(smx, &smf);
+    smFinish(smx, &smf, &cs);
+}
+
+/* the force pass of msrTopStepKDK (master.c:8397-8436) */
+static void msh_forces(MSH *m, int iKickRung)
+{
+    PKD pkd = m->pkd;
+    const ref_grav_params *gp = m->gp;
+    int nActive = 0, i;
+    double dPartSum, dCellSum, dSoftSum, dFlop;
+    double aSun[3] = {0, 0, 0};
+    CASTAT cs;
+    if (pkdActiveMaskRung(pkd, TYPE_ACTIVE, iKickRung, 1) == 0) return;
+    pkdInitAccel(pkd);
+    pkdActiveRung(pkd, iKickRung, 1);
+    pkdActiveType(pkd, TYPE_ALL, TYPE_TREEACTIVE);
+    free(pkd->kdTop); free(pkd->piLeaf);
+    build_grav_tree(pkd, gp);
+    pkdGravAll(pkd, gp->bPeriodic ? gp->nReps : 0, gp->bPeriodic, gp->iOrder, gp->bEwald,
+               gp->iEwOrder, gp->fEwCut, gp->fEwhCut, 0, 0.0, 0, 0.0, aSun, &nActive,
+               &dPartSum, &dCellSum, &dSoftSum, &cs, &dFlop);
+    m->counts[0] += 1;
+    m->counts[1] += nActive;
+    int bGasActive = 0;
+    for (i = 0; i < pkd->nLocal; ++i) {
+        PARTICLE *p = &pkd->pStore[i];
+        if (TYPETest(p, TYPE_GAS) && p->iRung >= iKickRung) bGasActive = 1;
+    }
+    if (bGasActive) msh_sph(m, iKickRung);
+}
+
+/* the Adjust block of msrTopStepKDK (master.c:8264-8317) */
+static void msh_adjust(MSH *m, int iRung, double dDelta)
+{
+    PKD pkd = m->pkd;
+    const ref_step_params *st = m->st;
+    double dtMinGas;
+    int nMaxRung, iMaxRungIdeal;
+    pkdActiveRung(pkd, iRung, 1);
+    pkdInitDt(pkd, st->dDelta);
+    if (st->bGravStep) pkdGravStep(pkd, st->dEta);
+    if (st->bEpsAccStep || st->bSqrtPhiStep)
+        pkdAccelStep(pkd, st->dEta, 1.0, 1.0, 1, st->bEpsAccStep, st->bSqrtPhiStep, 0.0);
+    pkdSphStep(pkd, 1.0, m->sp->dEtaCourant, st->dEtauDot, st->duMinDt, 0.0, 0.1, 0.0, 0,
+               &dtMinGas);
+    m->iCurrMaxRung = pkdDtToRung(pkd, iRung, dDelta, st->iMaxRung, 1, 1, &nMaxRung,
+                                  &iMaxRungIdeal);
+}
+
+static void msh_top_step(MSH *m, double dTime, double dDelta, int iRung, int iKickRung,
+                         int iAdjust)
+{
+    PKD pkd = m->pkd;
+    if (iAdjust) {
+        int nUn, iIdeal, nMax, iOut;
+        pkdActiveRung(pkd, iRung, 1);
+        pkdEmergencyAdjust(pkd, iRung, m->st->iMaxRung, dDelta, dDelta * 0.5, &nUn, &iIdeal,
+                           &nMax, &iOut);
+        if (nUn && iOut > m->iCurrMaxRung) m->iCurrMaxRung = iOut;
+    }
+    if (iAdjust && iRung < m->st->iMaxRung - 1) msh_adjust(m, iRung, dDelta);
+    msh_kick(m, iRung, 0.5 * dDelta, 0);
+    if (m->iCurrMaxRung > iRung) {
+        msh_top_step(m, dTime, 0.5 * dDelta, iRung + 1, iRung + 1, 0);
+        dTime += 0.5 * dDelta;
+        msh_top_step(m, dTime, 0.5 * dDelta, iRung + 1, iKickRung, 1);
+    } else {
+        msh_drift(m, 0.5 * dDelta);
+        dTime += 0.5 * dDelta;
+        msh_drift(m, 0.5 * dDelta);
+        dTime += 0.5 * dDelta;
+        msh_forces(m, iKickRung);
+        dTime -= 0.5 * dDelta;
+    }
+    msh_kick(m, iRung, 0.5 * dDelta, 1);
+}
+
+int ref_multistep(int n, int ngas, const double *pos, const double *vel, const double *mass,
+                  const double *soft, const double *u, const ref_grav_params *gp,
+                  const ref_sph_params *sp, const ref_step_params *st, double *opos,
+                  double *ovel, double *ovpred, double *oacc, double *f, int *maxRung,
+                  double *counts)
+{
+    MSH m;
+    PKD pkd = make_pkd(n, pos, mass, soft, gp->bPeriodic, gp->dPeriod, gp->iOrder, 0);
+    int i, j, s;
+    double dTime = 0.0;
+    pkd->nGas = ngas;
+    pkd->nDark = n - ngas;
+    for (i = 0; i < n; ++i) {
+        PARTICLE *p = &pkd->pStore[i];
+        p->iActive = TYPE_ACTIVE | TYPE_TREEACTIVE | (i < ngas ? TYPE_GAS : TYPE_DARK);
+        for (j = 0; j < 3; ++j) p->v[j] = p->vPred[j] = vel[3 * i + j];
+        if (i < ngas) p->u = p->uPred = u[i];
+        p->iRung = 0;
+        p->dt = FLT_MAX;
+        p->dtNew = FLT_MAX;
+    }
+    memset(&m, 0, sizeof(m));
+    m.pkd = pkd; m.gp = gp; m.sp = sp; m.st = st; m.ngas = ngas;
+    /* initial forces (main.c:360-386, msrInitSph master.c:9060-9100) */
+    build_grav_tree(pkd, gp);
+    pkdActiveType(pkd, TYPE_ALL, TYPE_ACTIVE);
+    msh_forces(&m, 0);
+    for (s = 0; s < st->nSteps; ++s) {
+        msh_top_step(&m, dTime, st->dDelta, 0, 0, 1);
+        dTime += st->dDelta;
+        maxRung[s] = m.iCurrMaxRung;
+    }
+    for (i = 0; i < n; ++i) {
+        PARTICLE *p = &pkd->pStore[i];
+        int k = p->iOrder;
+        double *q = &f[12 * k];
+        for (j = 0; j < 3; ++j) {
+            opos[3 * k + j] = p->r[j];
+            ovel[3 * k + j] = p->v[j];
+            ovpred[3 * k + j] = p->vPred[j];
+            oacc[3 * k + j] = p->a[j];
+        }
+        q[0] = p->u; q[1] = p->uPred; q[2] = p->fPot; q[3] = p->dtGrav; q[4] = p->dt;
+        q[5] = p->dtNew; q[6] = p->mumax; q[7] = p->fDensity; q[8] = p->fBall2;
+        q[9] = p->uDotPdV; q[10] = p->uDotAV; q[11] = p->iRung;
+    }
+    counts[0] = m.counts[0];
+    counts[1] = m.counts[1];
+    pkdFinish(pkd);
+    return 0;
+}
+
+/*
+ * Force passes over an active subset, as one step of msrTopStepKDK runs
+ * them: particles with rung >= iRung are active (msrActiveRung(iRung, 1)).
+ * Gravity: pkdInitAccel, tree of all particles, pkdGravAll.  SPH (all
+ * particles gas): the non-FastGas msrSph above.  Outputs by iOrder;
+ * inactive particles keep a = 0, fPot = 0 (gravity) or their initial
+ * dt = dtNew = FLT_MAX, mumax = 0 (SPH).
+ *   grav: acc[3n], pot[n], dtGrav[n], counters[5] as ref_grav
+ *   sph:  acc[3n] (hydro), f[6*i + ..] = uDotPdV, uDotAV, dtNew, mumax,
+ *         dt, fDensity
+ */
+int ref_grav_active(int n, const double *pos, const double *mass, const double *soft,
+                    const int *rung, int iRung, const ref_grav_params *gp, double *acc,
+                    double *pot, double *dtGrav, double *counters)
+{
+    PKD pkd = make_pkd(n, pos, mass, soft, gp->bPeriodic, gp->dPeriod, gp->iOrder, 0);
+    int nActive = 0, i, j;
+    double dPartSum, dCellSum, dSoftSum, dFlop;
+    CASTAT cs;
+    double aSun[3] = {0, 0, 0};
+    for (i = 0; i < n; ++i) pkd->pStore[i].iRung = rung[i];
+    pkdActiveRung(pkd, iRung, 1);
+    pkdInitAccel(pkd);
+    build_grav_tree(pkd, gp);
+    pkdGravAll(pkd, gp->bPeriodic ? gp->nReps : 0, gp->bPeriodic, gp->iOrder, gp->bEwald,
+               gp->iEwOrder, gp->fEwCut, gp->fEwhCut, 0, 0.0, 0, 0.0, aSun, &nActive,
+               &dPartSum, &dCellSum, &dSoftSum, &cs, &dFlop);
+    for (i = 0; i < n; ++i) {
+        PARTICLE *p = &pkd->pStore[i];
+        int k = p->iOrder;
+        for (j = 0; j < 3; ++j) acc[3 * k + j] = p->a[j];
+        pot[k] = p->fPot;
+        dtGrav[k] = p->dtGrav;
+    }
+    counters[0] = nActive; counters[1] = dPartSum; counters[2] = dCellSum;
+    counters[3] = dSoftSum; counters[4] = dFlop;
+    pkdFinish(pkd);
+    return 0;
+}
+
+int ref_sph_active(int n, const double *pos, const double *vel, const double *mass,
+                   const double *soft, const double *u, const int *rung, int iRung,
+                   const ref_sph_params *sp, double *acc, double *f)
+{
+    ref_grav_params gp;
+    MSH m;
+    PKD pkd = make_pkd(n, pos, mass, soft, sp->bPeriodic, sp->dPeriod, 2, 1);
+    int i, j;
+    memset(&gp, 0, sizeof(gp));
+    gp.bPeriodic = sp->bPeriodic;
+    gp.dPeriod = sp->dPeriod;
+    for (i = 0; i < n; ++i) {
+        PARTICLE *p = &pkd->pStore[i];
+        for (j = 0; j < 3; ++j) p->v[j] = p->vPred[j] = vel[3 * i + j];
+        p->u = p->uPred = u[i];
+        p->iRung = rung[i];
+        p->dt = FLT_MAX;
+        p->dtNew = FLT_MAX;
+        p->mumax = 0.0;
+    }
+    memset(&m, 0, sizeof(m));
+    m.pkd = pkd; m.gp = &gp; m.sp = sp; m.ngas = n;
+    pkd->kdTop = NULL; pkd->piLeaf = NULL;
+    msh_sph(&m, iRung);
+    for (i = 0; i < n; ++i) {
+        PARTICLE *p = &pkd->pStore[i];
+        int k = p->iOrder;
+        double *q = &f[6 * k];
+        for (j = 0; j < 3; ++j) acc[3 * k + j] = p->a[j];
+        q[0] = p->uDotPdV; q[1] = p->uDotAV; q[2] = p->dtNew; q[3] = p->mumax; q[4] = p->dt;
+        q[5] = p->fDensity;
+    }
+    pkdFinish(pkd);
+    return 0;
+}

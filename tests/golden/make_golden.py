@@ -87,6 +87,40 @@ def tipsy_case(name, ng, nd, ns, seed, dvFac=1.3, duTFac=2.5, rvFac=0.7, rTuFac=
     print(name, ng, nd, ns)
 
 
+def multistep_cases():
+    """Adaptive timesteps: force passes over an active subset, and a whole
+    run of msrTopStepKDK with rungs, from the reference's own code."""
+    rng = np.random.Generator(np.random.PCG64(17))
+    pos, vel, m = ics.plummer(3000, seed=18)
+    soft = np.full(len(m), 0.01)
+    rung = rng.integers(0, 3, len(m)).astype(np.int32)
+    gp = oracle.grav_params(periodic=False)
+    g = oracle.reference_grav_active(pos, m, soft, rung, 1, gp)
+    np.savez_compressed(os.path.join(HERE, "ms_active_grav.npz"), pos=pos, mass=m, soft=soft,
+                        rung=rung, iRung=1, acc=g["acc"], pot=g["pot"], dtGrav=g["dtGrav"],
+                        counters=g["counters"])
+    pos, vel, m, u = ics.gas_sphere(3000, seed=19)
+    vel = rng.normal(0.0, 0.2, pos.shape)
+    soft = np.full(len(m), 0.01)
+    rung = rng.integers(0, 3, len(m)).astype(np.int32)
+    sp = oracle.sph_params(nSmooth=32)
+    s = oracle.reference_sph_active(pos, vel, m, soft, u, rung, 1, sp)
+    np.savez_compressed(os.path.join(HERE, "ms_active_sph.npz"), pos=pos, vel=vel, mass=m,
+                        soft=soft, u=u, rung=rung, iRung=1,
+                        **{k: s[k] for k in ("acc", "uDotPdV", "uDotAV", "dtNew", "mumax", "dt",
+                                             "fDensity")})
+    pg, vg, mg, ug = ics.gas_sphere(2000, seed=20)
+    pd, vd, md = ics.plummer(1000, seed=21)
+    pos = np.concatenate([pg, pd]); vel = np.concatenate([vg, vd])
+    m = np.concatenate([0.2 * mg, 0.8 * md]); soft = np.full(len(m), 0.02)
+    st = oracle.step_params(nSteps=3, iMaxRung=5, dDelta=0.05)
+    r = oracle.reference_multistep(pos, vel, m, soft, 2000, ug, gp, sp, st)
+    np.savez_compressed(os.path.join(HERE, "ms_run.npz"), pos0=pos, vel0=vel, mass=m, soft=soft,
+                        u0=ug, ngas=2000, steps=np.array([st.nSteps, st.iMaxRung]),
+                        dDelta=st.dDelta, **{k: np.asarray(v) for k, v in r.items()})
+    print("multistep cases: run max rungs", r["maxRung"], "force passes", r["counts"])
+
+
 def main():
     if not oracle.reference_available():
         oracle.build_reference()
@@ -105,12 +139,16 @@ def main():
     sph_case("sph_sphere_2k", pos, vel, m, np.full(len(m), 0.01), u,
              oracle.sph_params(nSmooth=32))
     tipsy_case("tipsy_mixed", 300, 500, 200, seed=16)
+    multistep_cases()
 
 
 if __name__ == "__main__":
-    if len(sys.argv) > 1 and sys.argv[1] == "tipsy":
+    if len(sys.argv) > 1 and sys.argv[1] in ("tipsy", "multistep"):
         if not oracle.reference_available():
             oracle.build_reference()
-        tipsy_case("tipsy_mixed", 300, 500, 200, seed=16)
+        if sys.argv[1] == "tipsy":
+            tipsy_case("tipsy_mixed", 300, 500, 200, seed=16)
+        else:
+            multistep_cases()
     else:
         main()

@@ -1,0 +1,34 @@
+"""Adaptive timesteps on the CPU: the golden runs of the reference's
+msrTopStepKDK recursion (tests/golden/ms_*.npz) are consistent, and --
+where the reference is built here -- reproduce bit for bit."""
+import numpy as np
+import pytest
+
+import oracle
+from golden_io import load
+
+
+def test_golden_run_is_consistent():
+    d = load("ms_run")
+    nSteps, iMaxRung = (int(x) for x in d["steps"])
+    assert len(d["maxRung"]) == nSteps
+    assert d["rung"].min() >= 0 and d["rung"].max() == d["maxRung"][-1] < iMaxRung
+    # one force pass per smallest substep of each base step, plus the initial one
+    assert 1 < d["counts"][0] <= 1 + nSteps * 2 ** int(d["maxRung"].max())
+    g = load("ms_active_grav")
+    act = g["rung"] >= int(g["iRung"])
+    assert int(g["counters"][0]) == act.sum()
+    assert np.all(g["acc"][~act] == 0.0)
+
+
+@pytest.mark.skipif(not oracle.reference_available(), reason="reference not built here")
+def test_reference_run_reproduces_golden():
+    d = load("ms_run")
+    gp = oracle.grav_params(periodic=False)
+    sp = oracle.sph_params(nSmooth=32)
+    nSteps, iMaxRung = (int(x) for x in d["steps"])
+    st = oracle.step_params(nSteps=nSteps, iMaxRung=iMaxRung, dDelta=float(d["dDelta"]))
+    r = oracle.reference_multistep(d["pos0"], d["vel0"], d["mass"], d["soft"], int(d["ngas"]),
+                                   d["u0"], gp, sp, st)
+    for k in ("pos", "vel", "rung", "dt", "u", "maxRung", "counts"):
+        assert np.array_equal(r[k], d[k]), k
