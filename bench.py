@@ -490,6 +490,107 @@ def run_collapse(args):
             "neighbour_sets_bit_exact": mismatch == 0, "steps_with_mismatch": mismatch}
 
 
+def run_multistep(args):
+    """Adaptive timesteps on the 1/r gas sphere (N = collapse_n): base step
+    0.02 with up to 6 rungs (finest step 0.02/32), FP32 gravity + FP64 SPH,
+    `steps` base steps after `warmup`.  Throughput counts the particles that
+    received forces; the single-rung cost of the same time resolution is
+    one all-active step at the finest step used, times 2^maxRung."""
+    import torch
+    import gasoline_gb300 as g
+    n = args.collapse_n
+    pos, vel, m, u = g.ics.gas_sphere(n, seed=41)
+    soft = np.full(n, 0.01)
+    stream = torch.cuda.Stream()
+    ctx = g.Context(0, stream=stream.cuda_stream)
+    ctx.set_particles(pos, m, soft)
+    ctx.set_velocities(vel, ngas=n, u=u)
+    gp = g.grav_params(periodic=False, precision=g.FP32)
+    sp = g.sph_params(nSmooth=32)
+    st = g.step_params(iMaxRung=6)
+    dDelta = 0.02
+    ctx.grav_all(gp)
+    ctx.smooth(g.SMX_DENDVDX, sp)
+    ctx.smooth(g.SMX_SPHPRESSURETERMS, sp)
+    t = 0.0
+    for _ in range(args.warmup):
+        ctx.top_step_kdk(t, dDelta, gp, sp, st)
+        t += dDelta
+    outs, ts = [], []
+    for _ in range(args.steps):
+        box = {}
+        ts.append(_cuda_ms(lambda: box.update(ctx.top_step_kdk(t, dDelta, gp, sp, st)), stream))
+        outs.append(box)
+        t += dDelta
+    rungs = ctx.get_rungs()["rung"]
+    maxr = max(o["iCurrMaxRung"] for o in outs)
+    # single rung at the finest step, on the same state
+    fine = dDelta / 2 ** maxr
+    ctx.step(fine, gp, sp)
+    ctx.step_status()
+    t1 = [_cuda_ms(lambda: (ctx.step(fine, gp, sp), ctx.step_status()), stream) for _ in range(3)]
+    ctx.close()
+    ms = statistics.mean(ts)
+    act = statistics.mean(o["nActiveSum"] for o in outs)
+    single = statistics.mean(t1) * 2 ** maxr
+    return {"metric": "particle force evals/s with adaptive timesteps, gas sphere N=262144",
+            "value": act / (ms * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "dtype": "f32 gravity, f64 SPH", "data": "synthetic 1/r gas sphere, seed 41",
+            "config": {"workload": f"1/r gas sphere N={n}, base step {dDelta}, iMaxRung 6, "
+                                   "eta 0.1, eta_Courant 0.4, nSmooth 32",
+                       "timing": "CUDA events around each base step (host recursion included)"},
+            "force_passes_per_step": statistics.mean(o["nForcePasses"] for o in outs),
+            "active_per_step": act, "max_rung": maxr,
+            "rung_histogram": np.bincount(rungs, minlength=maxr + 1).tolist(),
+            "single_rung_ms_per_base_step": single,
+            "speedup_vs_single_rung_same_finest_step": single / ms}
+
+
+def run_snapshot(args):
+    """Tipsy snapshot I/O of the 128^3 box (2,097,152 dark particles, 75 MB):
+    tsph_write_tipsy and tsph_read_tipsy through the C ABI, the file in the
+    page cache, against the oracle's numpy reader on the same file."""
+    import time
+    import gasoline_gb300 as g
+    from oracle import tipsy
+    pos, m, soft = workload(args.ng)
+    n = len(m)
+    ctx = g.Context(0)
+    ctx.set_particles(pos, m, soft)
+    ctx.set_velocities(np.zeros((n, 3)))
+    os.makedirs("gpurun_out", exist_ok=True)
+    path = os.path.join("gpurun_out", "bench_snapshot.std")
+    ctx.write_tipsy(path, 0.0)
+    size = os.path.getsize(path)
+    tw, tr = [], []
+    for k in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        ctx.write_tipsy(path, 0.0)
+        t1 = time.perf_counter()
+        ctx.read_tipsy(path)
+        t2 = time.perf_counter()
+        if k >= args.warmup:
+            tw.append(t1 - t0)
+            tr.append(t2 - t1)
+    t0 = time.perf_counter()
+    tipsy.read(path)
+    tcpu = time.perf_counter() - t0
+    ctx.close()
+    os.remove(path)
+    r = statistics.mean(tr)
+    return {"metric": "Tipsy snapshot read, particles/s (file in page cache -> device state)",
+            "value": n / r, "unit": "particles/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": r * 1e3, "higher_is_better": True,
+            "dtype": "f32 file, f64 state", "data": "synthetic 128^3 box",
+            "config": {"workload": f"standard (XDR) Tipsy file, {n} dark particles, {size} bytes",
+                       "timing": "host wall clock per call"},
+            "read_GBps": size / r / 1e9, "write_ms": statistics.mean(tw) * 1e3,
+            "write_GBps": size / statistics.mean(tw) / 1e9,
+            "cpu_baseline": {"value": n / tcpu, "unit": "particles/s", "cores": 1, "kind": "port",
+                             "sample": "the oracle's numpy reader on the same file"}}
+
+
 def run_batched(args):
     """512 independent Plummer/Hernquist spheres, N log-uniform in
     [1024, 65536], every other pair with a 0.2 gas fraction: one context, a
@@ -588,7 +689,8 @@ def main():
     ap.add_argument("--ref-ng", type=int, default=64)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="box",
-                    choices=["box", "plummer", "collapse", "batched", "mixed", "gas"])
+                    choices=["box", "plummer", "collapse", "batched", "mixed", "gas", "multistep",
+                             "snapshot"])
     ap.add_argument("--profile", action="store_true",
                     help="box FP32 evaluations only (the ncu capture command)")
     ap.add_argument("--sph-fp32", action="store_true")
@@ -607,7 +709,8 @@ def main():
                               "unavailable": "the reference arm is timed on the periodic box only"}))
             return
         fn = {"plummer": run_plummer, "collapse": run_collapse, "batched": run_batched,
-              "mixed": run_mixed, "gas": run_gas}[args.workload]
+              "mixed": run_mixed, "gas": run_gas, "multistep": run_multistep,
+              "snapshot": run_snapshot}[args.workload]
         print(json.dumps(fn(args)), flush=True)
         return
     rank = int(os.environ.get("RANK", "0"))
