@@ -79,6 +79,7 @@ extern "C" void tsph_destroy(tsph_ctx *ctx) {
     FREE(C.az); FREE(C.pot); FREE(C.dtGrav); FREE(C.hax); FREE(C.hay); FREE(C.haz); FREE(C.udot);
     FREE(C.fb2prev); FREE(C.divvprev);
     FREE(C.rung); FREE(C.dt); FREE(C.dtNew); FREE(C.mumax); FREE(C.updv); FREE(C.cs);
+    FREE(C.disp);
     tsph_hnet_free(ctx);
     TsphDevParts *PP[2] = {&ctx->P, &ctx->G};
     for (int k = 0; k < 2; ++k) {
@@ -100,6 +101,7 @@ extern "C" void tsph_destroy(tsph_ctx *ctx) {
     FREE(S.seed); FREE(S.nnCount); FREE(S.nnHash); FREE(S.nodeBall2);
     FREE(S.nbrList); FREE(S.rcnt); FREE(S.roff); FREE(S.rcur); FREE(S.rlist); FREE(S.listFlag);
     FREE(S.ph); FREE(S.ih2); FREE(S.fn1); FREE(S.pr2f); FREE(S.pfa); FREE(S.pfb); FREE(S.pfc);
+    FREE(S.need); FREE(S.list); FREE(S.list2); FREE(S.listN); FREE(S.rb2);
     FREE(ctx->dCnt); FREE(ctx->dBucketLists); FREE(ctx->dRoot); FREE(ctx->dEwt); FREE(ctx->dStage);
     FREE(ctx->dAux); FREE(ctx->dStepStatus);
     tsph_free_snapshot(ctx);
@@ -134,7 +136,7 @@ int tsph_ensure_particles(tsph_ctx *ctx, int n) {
     double **cs[] = {&C.x, &C.y, &C.z, &C.vx, &C.vy, &C.vz, &C.m, &C.h, &C.u, &C.vpx, &C.vpy,
                      &C.vpz, &C.upred, &C.ax, &C.ay, &C.az, &C.pot, &C.dtGrav, &C.hax, &C.hay,
                      &C.haz, &C.udot, &C.fb2prev, &C.divvprev, &C.dt, &C.dtNew, &C.mumax,
-                     &C.updv, &C.cs};
+                     &C.updv, &C.cs, &C.disp};
     for (auto pp : cs) rc |= tsph_grow(ctx, pp, cap);
     rc |= tsph_grow(ctx, &C.rung, cap);
     rc |= tsph_grow(ctx, &P.act, cap);
@@ -156,6 +158,9 @@ int tsph_ensure_particles(tsph_ctx *ctx, int n) {
     rc |= tsph_grow(ctx, &S.ph, cap); rc |= tsph_grow(ctx, &S.ih2, cap);
     rc |= tsph_grow(ctx, &S.fn1, cap); rc |= tsph_grow(ctx, &S.pr2f, cap);
     rc |= tsph_grow(ctx, &S.pfa, cap); rc |= tsph_grow(ctx, &S.pfb, cap); rc |= tsph_grow(ctx, &S.pfc, cap);
+    rc |= tsph_grow(ctx, &S.need, cap); rc |= tsph_grow(ctx, &S.list, cap);
+    rc |= tsph_grow(ctx, &S.list2, cap); rc |= tsph_grow(ctx, &S.listN, 4);
+    rc |= tsph_grow(ctx, &S.rb2, cap);
     S.cap = cap;
     TsphBuildBufs &B = ctx->B;
     rc |= tsph_grow(ctx, &B.seg, cap); rc |= tsph_grow(ctx, &B.lt, cap); rc |= tsph_grow(ctx, &B.scan, cap);
@@ -185,7 +190,7 @@ __global__ void k_load_state(int n, const double *__restrict__ pos3, TsphDevStat
     // timestep state as the reference's reader leaves it (pkd.c:318-331)
     C.rung[i] = 0;
     C.dt[i] = C.dtNew[i] = FLT_MAX;
-    C.mumax[i] = C.updv[i] = C.cs[i] = 0.0;
+    C.mumax[i] = C.updv[i] = C.cs[i] = C.disp[i] = 0.0;
     piord[i] = i;
     giord[i] = i;
 }

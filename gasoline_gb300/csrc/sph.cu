@@ -107,6 +107,8 @@ struct SphArgs {
     int *work;
     const double *seed;     // optional fBall2 seeds (tree order) or null
     TsphDevState C;         // caller-order state (the inactive particles' dtNew, mumax)
+    const int *list;        // density pass over these gas-tree indices only (or null: all)
+    const int *nList;       // device count of list
 };
 
 // The pressure pass acts on active particles (G.act); an inactive one
@@ -388,7 +390,12 @@ __global__ void __launch_bounds__(SW * 32) k_knn_density(SphArgs A) {
         int i = 0;
         if (lane == 0) i = atomicAdd(A.work, 1);
         i = __shfl_sync(FULL, i, 0);
-        if (i >= ng) break;
+        if (A.list) {
+            if (i >= *A.nList) break;
+            i = A.list[i];
+        } else if (i >= ng) {
+            break;
+        }
         const double xi = A.G.x[i], yi = A.G.y[i], zi = A.G.z[i];
         const float4 hi_i = A.G.ph[i], lo_i = A.G.pl[i];
         const float xf = hi_i.x, yf = hi_i.y, zf = hi_i.z;
@@ -650,6 +657,22 @@ __global__ void k_gas_pressure(int ng, TsphSphBufs S, const int *__restrict__ io
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= ng) return;
     const int o = iord[i];
+    if (!S.need[i]) {
+        // not computed this pass: its sound speed and timestep from its
+        // current uPred and its last ball (what the reference's FastGas
+        // branch leaves a particle outside the active neighbourhood with)
+        const double cGas = sqrt(cS.gamma * (cS.gammam1 * S.u[i]));
+        const double c = sqrt(cGas * cGas + (5. / 3.) * 0.0 + 2.0 * 0.0);
+        const double fb = C.fb2prev[o], uTotDot = C.udot[o];
+        double dtp = C.dt[o], dt;
+        if (uTotDot > 0)
+            dt = cS.dtFacCourant * sqrt(fb * 0.25 / (4 * (c * c + (5. / 3.) * uTotDot * dtp)));
+        else
+            dt = cS.dtFacCourant * sqrt(fb * 0.25) / (2 * c);
+        if (dt < dtp) C.dt[o] = dt;
+        C.cs[o] = c;
+        return;
+    }
     double PoverRhoGas = cS.gammam1 * S.u[i];
     double cGas = sqrt(cS.gamma * PoverRhoGas);
     double PoverRho = PoverRhoGas + 0.0;
@@ -687,7 +710,7 @@ __global__ void k_rev_count(int ng, TsphSphBufs S) {
     if (S.listFlag[0]) return;           // incomplete lists: not used
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     int i = (int)(t / S.nbrCap), e = (int)(t % S.nbrCap);
-    if (i >= ng || e >= S.nnCount[i]) return;
+    if (i >= ng || !S.need[i] || e >= S.nnCount[i]) return;
     atomicAdd(&S.rcnt[S.nbrList[(size_t)i * S.nbrCap + e]], 1);
 }
 
@@ -695,7 +718,7 @@ __global__ void k_rev_fill(int ng, TsphSphBufs S) {
     if (S.listFlag[0]) return;
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     int i = (int)(t / S.nbrCap), e = (int)(t % S.nbrCap);
-    if (i >= ng || e >= S.nnCount[i]) return;
+    if (i >= ng || !S.need[i] || e >= S.nnCount[i]) return;
     int j = S.nbrList[(size_t)i * S.nbrCap + e];
     int slot = atomicAdd(&S.rcur[j], 1);
     S.rlist[(j > 0 ? S.roff[j - 1] : 0) + slot] = i;
@@ -727,11 +750,12 @@ __global__ void __launch_bounds__(SW * 32) k_rev_sort(int ng, TsphSphBufs S, int
 // per gas-tree node: max fBall2 of its particles (atomicMax on the bits)
 __global__ void k_node_ball(int ng, TsphDevTree T, const int *__restrict__ rid,
                             const double *__restrict__ fBall2, const int *listFlag,
-                            unsigned long long *nodeBall2) {
-    if (!*listFlag) return;              // only the tree-walk fallback needs node balls
+                            unsigned long long *nodeBall2, const int *__restrict__ need, int always) {
+    if (!always && !*listFlag) return;   // only the tree-walk fallback needs node balls
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     bool live = p < ng;
-    unsigned long long key = live ? (unsigned long long)__double_as_longlong(fBall2[p]) : 0ULL;
+    unsigned long long key =
+        (live && (!need || need[p])) ? (unsigned long long)__double_as_longlong(fBall2[p]) : 0ULL;
     int i = live ? T.sysRoot[rid[p]] : 0;
     unsigned mask = __ballot_sync(0xffffffffu, live);
     while (mask) {
@@ -874,6 +898,7 @@ __global__ void __launch_bounds__(SW * 32) k_pressure_lists(SphArgs A) {
         if (lane == 0) i = atomicAdd(A.work, 1);
         i = __shfl_sync(FULL, i, 0);
         if (i >= ng) break;
+        if (!S.need[i]) continue;        // not computed this pass: no pair with an active particle
         const bool ai = A.G.act[i] != 0;
         if constexpr (F32) {
             const float4 hi = A.G.ph[i], lo = A.G.pl[i];
@@ -959,6 +984,7 @@ __global__ void __launch_bounds__(SW * 32) k_pressure(SphArgs A) {
         if (i >= ng) break;
         const double xi = A.G.x[i], yi = A.G.y[i], zi = A.G.z[i];
         const float xf = (float)xi, yf = (float)yi, zf = (float)zi;
+        if (!A.S.need[i]) continue;
         const double fbi = A.S.fBall2[i];
         const TsphSphBufs &S = A.S;
         const bool ai = A.G.act[i] != 0;
@@ -995,7 +1021,7 @@ __global__ void __launch_bounds__(SW * 32) k_pressure(SphArgs A) {
             int cnt = leaf ? lk.y : 0;
             for (int kk = 0; kk < cnt; ++kk) {
                 int j = lk.x + kk;
-                if (!ai && !A.G.act[j]) continue;
+                if (!S.need[j] || (!ai && !A.G.act[j])) continue;
                 double xj = A.G.x[j], yj = A.G.y[j], zj = A.G.z[j];
                 double dxi, dyi, dzi, dxj, dyj, dzj;
                 double d2i = dist2_exact(xi, yi, zi, xj, yj, zj, dxi, dyi, dzi);
@@ -1095,6 +1121,113 @@ __global__ void k_gas_gather_pos(int ng, TsphDevState C, TsphDevParts G) {
     G.m[i] = C.m[o]; G.h[i] = C.h[o];
 }
 
+// ---------------------------------------------------------------------------
+// Density passes over active rungs.  Every particle an active one pairs
+// with must have its density, ball and lists of this pass: the active
+// particles, their gather neighbours N(i), and the particles j whose ball
+// holds an active i.  j's ball radius cannot exceed its radius at its last
+// density plus twice the largest distance any gas particle drifted since
+// the last pass over all gas (the k particles inside the old ball moved at
+// most that far, and so did j), so every j with an active particle inside
+// that bound is computed too.  The active particles' results then equal
+// those of a pass over all gas; the reference's FastGas branch
+// (master.c:9270-9298) serves the same purpose with marking passes.
+// ---------------------------------------------------------------------------
+__global__ void k_act_list(int ng, const int *__restrict__ act, int *need, int *list, int *listN) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ng) return;
+    const int a = act[i] != 0;
+    need[i] = a;
+    if (a) list[atomicAdd(&listN[0], 1)] = i;
+}
+
+__global__ void k_mark_gather(int na, const int *__restrict__ list, TsphSphBufs S) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int a = (int)(t / S.nbrCap), e = (int)(t % S.nbrCap);
+    if (a >= na) return;
+    const int i = list[a];
+    if (e >= S.nnCount[i]) return;
+    S.need[S.nbrList[(size_t)i * S.nbrCap + e]] = 1;
+}
+
+__global__ void k_disp_max(int ng, const double *__restrict__ disp, unsigned long long *out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    warp_max_abs(i < ng ? disp[i] : 0.0, out);
+}
+
+__global__ void k_rbound(int ng, const int *__restrict__ iord, const double *__restrict__ fb2prev,
+                         const unsigned long long *dmax, double *rb2) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ng) return;
+    double dm;
+    memcpy(&dm, dmax, sizeof(dm));
+    const double r = (sqrt(fb2prev[iord[i]]) + 2.0 * dm) * (1.0 + 1e-9);
+    rb2[i] = r * r * (1.0 + 1e-9);
+}
+
+__global__ void __launch_bounds__(SW * 32) k_mark_scatter(SphArgs A, const unsigned long long *nodeB) {
+    __shared__ int stackAll[SW][SSTK];
+    int *stack = stackAll[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    const unsigned FULL = 0xffffffffu;
+    const TsphSphBufs &S = A.S;
+    for (;;) {
+        int t = 0;
+        if (lane == 0) t = atomicAdd(A.work, 1);
+        t = __shfl_sync(FULL, t, 0);
+        if (t >= *A.nList) break;
+        const int i = A.list[t];
+        const double xi = A.G.x[i], yi = A.G.y[i], zi = A.G.z[i];
+        const float xf = (float)xi, yf = (float)yi, zf = (float)zi;
+        int sp = 1;
+        if (lane == 0) stack[0] = A.T.sysRoot[A.G.rid[i]];
+        __syncwarp();
+        bool bad = false;
+        while (sp > 0) {
+            int take = sp < 32 ? sp : 32;
+            int node = lane < take ? stack[sp - take + lane] : -1;
+            __syncwarp();
+            sp -= take;
+            bool open = false, leaf = false;
+            int4 lk = make_int4(0, 0, -1, 0);
+            if (node >= 0) {
+                lk = A.T.wlink[node];
+                const double nb = __longlong_as_double((long long)nodeB[node]);
+                const float d2 = box_d2f(xf, yf, zf, A.T.wcomh[node], A.T.wcoml[node]);
+                if (d2 <= (float)nb * 1.00001f) {
+                    if (lk.z >= 0) open = true;
+                    else leaf = true;
+                }
+            }
+            unsigned bo = __ballot_sync(FULL, open);
+            if (sp + 2 * __popc(bo) > SSTK) { bad = true; break; }
+            if (open) {
+                int pos = sp + 2 * __popc(bo & lane_lt_s());
+                stack[pos] = lk.z;
+                stack[pos + 1] = node + 1;
+            }
+            sp += 2 * __popc(bo);
+            const int cnt = leaf ? lk.y : 0;
+            for (int kk = 0; kk < cnt; ++kk) {
+                const int j = lk.x + kk;
+                double dx, dy, dz;
+                if (dist2_exact(xi, yi, zi, A.G.x[j], A.G.y[j], A.G.z[j], dx, dy, dz) <= S.rb2[j])
+                    S.need[j] = 1;
+            }
+            __syncwarp();
+        }
+        if (bad && lane == 0) atomicOr(&A.cnt->status, 1u << TSPH_ERR_STACK_OVERFLOW);
+        __syncwarp();
+    }
+}
+
+__global__ void k_need_list(int ng, const int *__restrict__ act, const int *__restrict__ need,
+                            int *list2, int *listN) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ng) return;
+    if (need[i] && !act[i]) list2[atomicAdd(&listN[1], 1)] = i;
+}
+
 __global__ void k_gas_maxabs(int ng, TsphDevParts G, unsigned long long *out) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     double a = 0.0;
@@ -1124,7 +1257,7 @@ __global__ void k_gas_nodes(TsphDevTree T) {
 // active particles, dtNew and mumax of every gas particle
 __global__ void k_scatter_hydro(int ng, TsphDevParts G, TsphSphBufs S, TsphDevState C) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= ng) return;
+    if (i >= ng || !S.need[i]) return;
     int o = G.iord[i];
     C.dtNew[o] = S.dtNew[i];
     C.mumax[o] = S.mumax[i];
@@ -1142,9 +1275,10 @@ __global__ void k_to_caller1(int ng, const int *__restrict__ iord, const double 
 }
 
 __global__ void k_save_prev(int ng, const int *__restrict__ iord, const double *__restrict__ fb2,
-                            const double *__restrict__ divv, double *fb2prev, double *divvprev) {
+                            const double *__restrict__ divv, double *fb2prev, double *divvprev,
+                            const int *__restrict__ need) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= ng) return;
+    if (i >= ng || !need[i]) return;
     fb2prev[iord[i]] = fb2[i];
     divvprev[iord[i]] = divv[i];
 }
@@ -1242,11 +1376,68 @@ int tsph_load_gas(tsph_ctx *ctx, int ngas) {
     return TSPH_OK;
 }
 
+static int launch_knn(tsph_ctx *ctx, const tsph_sph_params *sp, const SphArgs &A) {
+    const bool cap = ctx->capturing;
+    size_t sm = (sizeof(KnnSmem) + sizeof(KnnBatch)) * SW;
+    if (sp->precision == TSPH_FP32) {
+        if (!cap)
+            TSPH_CK(cudaFuncSetAttribute(k_knn_density<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)sm));
+        k_knn_density<true><<<ctx->smCount * 6, SW * 32, sm, ctx->stream>>>(A);
+        TSPH_LAUNCH_CK("k_knn_density<f32>");
+    } else {
+        if (!cap)
+            TSPH_CK(cudaFuncSetAttribute(k_knn_density<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)sm));
+        k_knn_density<false><<<ctx->smCount * 6, SW * 32, sm, ctx->stream>>>(A);
+        TSPH_LAUNCH_CK("k_knn_density<f64>");
+    }
+    return TSPH_OK;
+}
+
+// The density pass over only the particles the active ones need (see
+// k_act_list ... k_need_list).  Returns in *nComputed the particles done.
+static int run_density_subset(tsph_ctx *ctx, const tsph_sph_params *sp, SphArgs A, int na) {
+    const int ng = ctx->ngas;
+    TsphSphBufs &S = ctx->S;
+    int *work = A.work;
+    // the active particles
+    A.list = S.list;
+    A.nList = S.listN;
+    int rc = launch_knn(ctx, sp, A);
+    if (rc) return rc;
+    // their gather neighbours
+    k_mark_gather<<<tsph_blocks((long long)na * S.nbrCap, 256), 256, 0, ctx->stream>>>(na, S.list, S);
+    TSPH_LAUNCH_CK("k_mark_gather");
+    // particles whose ball can hold an active one
+    unsigned long long *dmax = ctx->dAux + 40;
+    TSPH_CK(cudaMemsetAsync(dmax, 0, sizeof(unsigned long long), ctx->stream));
+    k_disp_max<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, ctx->C.disp, dmax);
+    TSPH_LAUNCH_CK("k_disp_max");
+    k_rbound<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, ctx->G.iord, ctx->C.fb2prev, dmax, S.rb2);
+    TSPH_LAUNCH_CK("k_rbound");
+    TSPH_CK(cudaMemsetAsync(S.nodeBall2, 0, sizeof(unsigned long long) * ctx->TG.nNodes, ctx->stream));
+    k_node_ball<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, ctx->TG, ctx->G.rid, S.rb2, S.listFlag,
+                                                              S.nodeBall2, nullptr, 1);
+    TSPH_LAUNCH_CK("k_node_ball");
+    TSPH_CK(cudaMemsetAsync(work, 0, sizeof(int), ctx->stream));
+    k_mark_scatter<<<ctx->smCount * 4, SW * 32, 0, ctx->stream>>>(A, S.nodeBall2);
+    TSPH_LAUNCH_CK("k_mark_scatter");
+    k_need_list<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, ctx->G.act, S.need, S.list2, S.listN);
+    TSPH_LAUNCH_CK("k_need_list");
+    // and the rest of them
+    A.list = S.list2;
+    A.nList = S.listN + 1;
+    TSPH_CK(cudaMemsetAsync(work, 0, sizeof(int), ctx->stream));
+    return launch_knn(ctx, sp, A);
+}
+
 static int run_density(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_out *out) {
     const int ng = ctx->ngas;
     TsphSphBufs &S = ctx->S;
     const bool cap = ctx->capturing;
     if (cap && sp->bLearnedH) return TSPH_ERR_UNSUPPORTED;
+    if (cap && ctx->actRung > 0) return TSPH_ERR_UNSUPPORTED;
     if (!cap) cudaEventRecord(ctx->ev[5], ctx->stream);
     k_gas_gather_pos<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, ctx->C, ctx->G);
     TSPH_LAUNCH_CK("k_gas_gather_pos");
@@ -1283,28 +1474,36 @@ static int run_density(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_out
     A.work = (int *)&ctx->dCnt->pad;
     A.seed = (sp->bLearnedH && S.haveSeed) ? S.seed : nullptr;
     A.C = ctx->C;
+    A.list = nullptr;
+    A.nList = nullptr;
     TSPH_CK(cudaMemsetAsync(ctx->dCnt, 0, sizeof(TsphDevCounters), ctx->stream));
     TSPH_CK(cudaMemsetAsync(S.listFlag, 0, sizeof(int), ctx->stream));
-    if (!cap) cudaEventRecord(ctx->ev[6], ctx->stream);
-    size_t sm = (sizeof(KnnSmem) + sizeof(KnnBatch)) * SW;
-    if (sp->precision == TSPH_FP32) {
-        if (!cap)
-            TSPH_CK(cudaFuncSetAttribute(k_knn_density<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)sm));
-        k_knn_density<true><<<ctx->smCount * 6, SW * 32, sm, ctx->stream>>>(A);
-        TSPH_LAUNCH_CK("k_knn_density<f32>");
-    } else {
-        if (!cap)
-            TSPH_CK(cudaFuncSetAttribute(k_knn_density<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)sm));
-        k_knn_density<false><<<ctx->smCount * 6, SW * 32, sm, ctx->stream>>>(A);
-        TSPH_LAUNCH_CK("k_knn_density<f64>");
+    // a pass over active rungs computes only the particles the active ones
+    // need when they are a minority of the gas
+    int na = ng;
+    S.subset = false;
+    if (ctx->actRung > 0) {
+        TSPH_CK(cudaMemsetAsync(S.listN, 0, 4 * sizeof(int), ctx->stream));
+        k_act_list<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, ctx->G.act, S.need, S.list, S.listN);
+        TSPH_LAUNCH_CK("k_act_list");
+        TSPH_CK(cudaMemcpyAsync(&na, S.listN, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        TSPH_CK(cudaStreamSynchronize(ctx->stream));
+        S.subset = 2 * na < ng;
     }
+    if (!cap) cudaEventRecord(ctx->ev[6], ctx->stream);
+    if (S.subset) {
+        rc = run_density_subset(ctx, sp, A, na);
+    } else {
+        TSPH_CK(cudaMemsetAsync(S.need, 0x01, sizeof(int) * ng, ctx->stream));   // every particle
+        rc = launch_knn(ctx, sp, A);
+    }
+    if (rc) return rc;
     if (cap) {
         rc = tsph_fold_status(ctx);
         if (rc) return rc;
+        TSPH_CK(cudaMemsetAsync(ctx->C.disp, 0, sizeof(double) * ng, ctx->stream));
         k_save_prev<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, ctx->G.iord, S.fBall2, S.divv,
-                                                                  ctx->C.fb2prev, ctx->C.divvprev);
+                                                                  ctx->C.fb2prev, ctx->C.divvprev, S.need);
         TSPH_LAUNCH_CK("k_save_prev");
         S.haveDensity = true;
         S.havePressure = false;
@@ -1319,11 +1518,20 @@ static int run_density(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_out
     cudaEventElapsedTime(&ctx->timings[5], ctx->ev[6], ctx->ev[7]);
     unsigned st = ctx->hCnt->status;
     if (st) for (int k = 1; k < 32; ++k) if (st & (1u << k)) return k;
-    // h-network: samples of this pass, then this pass becomes "previous"
-    rc = tsph_hnet_append(ctx);
-    if (rc) return rc;
+    S.nComputed = ng;
+    if (S.subset) {
+        int nl[2];
+        TSPH_CK(cudaMemcpy(nl, S.listN, sizeof(nl), cudaMemcpyDeviceToHost));
+        S.nComputed = nl[0] + nl[1];
+    } else {
+        // a pass over all gas starts the drift bound afresh
+        TSPH_CK(cudaMemsetAsync(ctx->C.disp, 0, sizeof(double) * ng, ctx->stream));
+        // h-network: samples of this pass, then this pass becomes "previous"
+        rc = tsph_hnet_append(ctx);
+        if (rc) return rc;
+    }
     k_save_prev<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, ctx->G.iord, S.fBall2, S.divv,
-                                                              ctx->C.fb2prev, ctx->C.divvprev);
+                                                              ctx->C.fb2prev, ctx->C.divvprev, S.need);
     TSPH_LAUNCH_CK("k_save_prev");
     ctx->hnet.havePrev = true;
     S.nFallback = (int)ctx->hCnt->nExactTests;
@@ -1331,7 +1539,7 @@ static int run_density(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_out
     S.havePressure = false;
     S.last = *sp;
     if (out) {
-        out->nSmoothed = ng;
+        out->nSmoothed = S.nComputed;
         out->nFallback = S.nFallback;
         out->dPairs = (double)ctx->hCnt->nPartPP;
         out->dCandidates = (double)ctx->hCnt->nCellNewt;
@@ -1365,7 +1573,7 @@ static int run_pressure(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_ou
     TSPH_LAUNCH_CK("k_rev_sort");
     TSPH_CK(cudaMemsetAsync(S.nodeBall2, 0, sizeof(unsigned long long) * ctx->TG.nNodes, ctx->stream));
     k_node_ball<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, ctx->TG, ctx->G.rid, S.fBall2,
-                                                              S.listFlag, S.nodeBall2);
+                                                              S.listFlag, S.nodeBall2, S.need, 0);
     TSPH_LAUNCH_CK("k_node_ball");
     SphArgs A;
     A.T = ctx->TG;
@@ -1571,6 +1779,9 @@ __global__ void k_drift(int n, int ngas, double dt, int bPeriodic, double L, Tsp
         r[k][i] = x;
     }
     if (i < ngas && dt != 0.0) {
+        // distance bound for passes over active rungs (|r| moved by |v| dt)
+        const double vx = C.vx[i], vy = C.vy[i], vz = C.vz[i];
+        C.disp[i] += sqrt(vx * vx + vy * vy + vz * vz) * fabs(dt) * (1.0 + 1e-12);
         C.vpx[i] = xadd(C.vpx[i], xmul(xadd(C.ax[i], C.hax[i]), dt));
         C.vpy[i] = xadd(C.vpy[i], xmul(xadd(C.ay[i], C.hay[i]), dt));
         C.vpz[i] = xadd(C.vpz[i], xmul(xadd(C.az[i], C.haz[i]), dt));

@@ -99,7 +99,7 @@ k_tipsy_decode(int i0, int i1, const unsigned int *__restrict__ raw, int swap, i
     C.fb2prev[i] = C.divvprev[i] = 0.0;
     C.rung[i] = 0;
     C.dt[i] = C.dtNew[i] = FLT_MAX;
-    C.mumax[i] = C.updv[i] = C.cs[i] = 0.0;
+    C.mumax[i] = C.updv[i] = C.cs[i] = C.disp[i] = 0.0;
     F.rho[i] = rho; F.metals[i] = metals; F.tform[i] = tform;
     piord[i] = (int)i;
     giord[i] = (int)i;

@@ -68,6 +68,14 @@ struct TsphSphBufs {
     int nFallback;
     bool haveDensity, havePressure, haveSeed;
     tsph_sph_params last;
+    // passes over active rungs: which gas particles this pass computed
+    // (need, tree order), the active ones and the rest as index lists,
+    // their counts (device, [0] active, [1] rest), per-particle bound on
+    // the squared ball radius since their last density (rb2)
+    int *need, *list, *list2, *listN;
+    double *rb2;
+    bool subset;
+    int nComputed;
 };
 
 // Learned smoothing-length network (3 -> 32 -> 32 -> 1, tanh, FP32).

@@ -121,6 +121,8 @@ struct TsphDevState {
     int *rung;
     double *dt, *dtNew, *mumax, *updv;
     double *cs;                          // gas sound speed of the last pressure pass (p->c)
+    double *disp;                        // gas: bound on the distance drifted since the last
+                                         // density pass over all gas
 };
 
 // Counters accumulated by the walk (integers: deterministic).

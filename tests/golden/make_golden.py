@@ -104,11 +104,13 @@ def multistep_cases():
     soft = np.full(len(m), 0.01)
     rung = rng.integers(0, 3, len(m)).astype(np.int32)
     sp = oracle.sph_params(nSmooth=32)
-    s = oracle.reference_sph_active(pos, vel, m, soft, u, rung, 1, sp)
+    keys = ("acc", "uDotPdV", "uDotAV", "dtNew", "mumax", "dt", "fDensity")
+    out = {}
+    for iRung in (1, 2):   # two thirds and one third of the gas active
+        s = oracle.reference_sph_active(pos, vel, m, soft, u, rung, iRung, sp)
+        out.update({f"{k}_r{iRung}": s[k] for k in keys})
     np.savez_compressed(os.path.join(HERE, "ms_active_sph.npz"), pos=pos, vel=vel, mass=m,
-                        soft=soft, u=u, rung=rung, iRung=1,
-                        **{k: s[k] for k in ("acc", "uDotPdV", "uDotAV", "dtNew", "mumax", "dt",
-                                             "fDensity")})
+                        soft=soft, u=u, rung=rung, **out)
     pg, vg, mg, ug = ics.gas_sphere(2000, seed=20)
     pd, vd, md = ics.plummer(1000, seed=21)
     pos = np.concatenate([pg, pd]); vel = np.concatenate([vg, vd])
