@@ -462,7 +462,8 @@ def run_collapse(args):
             for key, r in (("A", ra), ("B", rb)):
                 rows[key].append((r["wall_s"], r["t_grav_ms"], r["t_knn_density_ms"],
                                   r["t_pressure_ms"], r["density"]["dCandidates"],
-                                  r["density"]["nFallback"], r["density"]["bSeeded"]))
+                                  r["density"]["nFallback"], r["density"]["bSeeded"],
+                                  r["t_knn_tree_ms"]))
             sa, sb = A.ctx.get_sph(), B.ctx.get_sph()
             ha, hb = A.ctx.get_neighbour_hash(), B.ctx.get_neighbour_hash()
             if not (np.array_equal(sa["fBall2"], sb["fBall2"]) and np.array_equal(ha[1], hb[1])
@@ -473,7 +474,8 @@ def run_collapse(args):
         return {"step_ms": float(a[:, 0].mean() * 1e3), "grav_ms": float(a[:, 1].mean()),
                 "density_ms": float(a[:, 2].mean()), "pressure_ms": float(a[:, 3].mean()),
                 "candidates_per_particle": float(a[:, 4].mean() / n),
-                "grown_balls_per_pass": float(a[:, 5].mean()), "seeded": bool(a[:, 6].all())}
+                "grown_balls_per_pass": float(a[:, 5].mean()), "seeded": bool(a[:, 6].all()),
+                "knn_tree_ms": float(a[:, 7].mean())}
     sa_, sb_ = summ(rows["A"]), summ(rows["B"])
     A.ctx.close()
     B.ctx.close()

@@ -13,6 +13,7 @@
 // Training runs on the GPU with these kernels: one warp per sample, lane j
 // owning hidden unit j of both layers (dot products through shuffles),
 // per-warp gradient partials summed in a fixed order (deterministic), Adam.
+// Inference (k_hnet_predict) runs one thread per particle.
 #include <math.h>
 #include <stdio.h>
 #include <string.h>
@@ -35,7 +36,10 @@ struct LaneGrad {
     float b3;   // lane 0 only
 };
 
-__device__ __forceinline__ float sample_fwd_bwd(const float *__restrict__ W, const float *x,
+// W2T is W2 transposed (W2T[k*H + j] = W2[j*H + k]): lane j reads its row
+// of W2 as a column of W2T, one bank per lane.
+__device__ __forceinline__ float sample_fwd_bwd(const float *__restrict__ W,
+                                                const float *__restrict__ W2T, const float *x,
                                                 float y, int j, LaneGrad &g, bool backward) {
     const unsigned FULL = 0xffffffffu;
     // layer 1
@@ -45,7 +49,7 @@ __device__ __forceinline__ float sample_fwd_bwd(const float *__restrict__ W, con
     // layer 2: z2_j = b2_j + sum_k W2[j,k] h1_k
     float z2 = W[OFF_B2 + j];
 #pragma unroll
-    for (int k = 0; k < H; ++k) z2 += W[OFF_W2 + H * j + k] * __shfl_sync(FULL, h1, k);
+    for (int k = 0; k < H; ++k) z2 += W2T[H * k + j] * __shfl_sync(FULL, h1, k);
     float h2 = tanhf(z2);
     // output
     float o = W[OFF_W3 + j] * h2;
@@ -80,7 +84,9 @@ __global__ void __launch_bounds__(256) k_hnet_grad(const float *__restrict__ W,
                                                    const float *__restrict__ st, float *partial,
                                                    float *lossp) {
     __shared__ float Ws[HNET_NP];
+    __shared__ float W2T[H * H];
     for (int k = threadIdx.x; k < HNET_NP; k += blockDim.x) Ws[k] = W[k];
+    for (int k = threadIdx.x; k < H * H; k += blockDim.x) W2T[(k % H) * H + k / H] = W[OFF_W2 + k];
     __syncthreads();
     const int lane = threadIdx.x & 31;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -96,7 +102,7 @@ __global__ void __launch_bounds__(256) k_hnet_grad(const float *__restrict__ W,
         x[1] = st ? (smp[1] - st[2]) / st[3] : smp[1];
         x[2] = st ? (smp[2] - st[4]) / st[5] : smp[2];
         float y = st ? (smp[3] - st[6]) / st[7] : smp[3];
-        float o = sample_fwd_bwd(Ws, x, y, lane, g, true);
+        float o = sample_fwd_bwd(Ws, W2T, x, y, lane, g, true);
         loss += 0.5f * (o - y) * (o - y);
     }
     float *P = partial + (size_t)warp * HNET_NP;
@@ -170,27 +176,38 @@ __global__ void k_hnet_features(int ng, int k, TsphDevTree T, const int *__restr
     feat[3 * i + 2] = (float)divvprev[o];
 }
 
-// seed fBall2 = exp(t_pred + 2*margin) for the kNN ball gather
-__global__ void k_hnet_predict(int ng, const float *__restrict__ W, const float *__restrict__ feat,
-                               const float *__restrict__ st, double margin, double *seed) {
+// seed fBall2 = exp(t_pred + 2*margin) for the kNN ball gather.
+// Inference runs one thread per particle: every thread reads the same
+// weight at the same time, a shared-memory broadcast (the warp-per-sample
+// form of training reads a row of W2 per lane, which conflicts).
+__global__ void __launch_bounds__(256) k_hnet_predict(int ng, const float *__restrict__ W,
+                                                      const float *__restrict__ feat,
+                                                      const float *__restrict__ st, double margin,
+                                                      double *seed) {
     __shared__ float Ws[HNET_NP];
     for (int k = threadIdx.x; k < HNET_NP; k += blockDim.x) Ws[k] = W[k];
     __syncthreads();
-    const int lane = threadIdx.x & 31;
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    LaneGrad g;
-    for (int i = warp; i < ng; i += nwarps) {
-        float x[3];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ng; i += gridDim.x * blockDim.x) {
         const float *f = feat + 3 * i;
-        x[0] = (f[0] - st[0]) / st[1];
-        x[1] = (f[1] - st[2]) / st[3];
-        x[2] = (f[2] - st[4]) / st[5];
-        float o = sample_fwd_bwd(Ws, x, 0.0f, lane, g, false);
-        if (lane == 0) {
-            double t = (double)o * st[7] + st[6];
-            seed[i] = exp(t + 2.0 * margin);
+        const float x0 = (f[0] - st[0]) / st[1];
+        const float x1 = (f[1] - st[2]) / st[3];
+        const float x2 = (f[2] - st[4]) / st[5];
+        float h1[H];
+#pragma unroll
+        for (int j = 0; j < H; ++j)
+            h1[j] = tanhf(Ws[OFF_B1 + j] + Ws[OFF_W1 + 3 * j] * x0 + Ws[OFF_W1 + 3 * j + 1] * x1 +
+                          Ws[OFF_W1 + 3 * j + 2] * x2);
+        float o = 0.0f;
+#pragma unroll 4
+        for (int j = 0; j < H; ++j) {
+            float z2 = Ws[OFF_B2 + j];
+#pragma unroll
+            for (int k = 0; k < H; ++k) z2 += Ws[OFF_W2 + H * j + k] * h1[k];
+            o += Ws[OFF_W3 + j] * tanhf(z2);
         }
+        o += Ws[OFF_B3];
+        const double t = (double)o * st[7] + st[6];
+        seed[i] = exp(t + 2.0 * margin);
     }
 }
 

@@ -46,6 +46,7 @@ class Simulation:
             rec["density"] = self.ctx.smooth(SMX_DENDVDX, self.sp)
             rec["pressure"] = self.ctx.smooth(SMX_SPHPRESSURETERMS, self.sp)
             t = self.ctx.timings()
+            rec["t_knn_tree_ms"] = t["knn"]
             rec["t_knn_density_ms"] = t["density"]
             rec["t_pressure_ms"] = t["pressure"]
         rec["wall_s"] = time.perf_counter() - t0
