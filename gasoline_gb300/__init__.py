@@ -103,6 +103,58 @@ class StepOut(ctypes.Structure):
                 ("nActiveSum", ctypes.c_longlong), ("nEmergency", ctypes.c_int)]
 
 
+class RenderParams(ctypes.Structure):
+    """tsph_render_params: a TSC frame (dfRenderParticleTSC)."""
+    _fields_ = [("nxPix", ctypes.c_int), ("nyPix", ctypes.c_int),
+                ("r", ctypes.c_double * 3), ("x", ctypes.c_double * 3),
+                ("y", ctypes.c_double * 3), ("z", ctypes.c_double * 3),
+                ("zEye", ctypes.c_double), ("zClipNear", ctypes.c_double),
+                ("zClipFar", ctypes.c_double), ("iProject", ctypes.c_int),
+                ("dGasSoftMul", ctypes.c_double), ("dDarkSoftMul", ctypes.c_double),
+                ("dStarSoftMul", ctypes.c_double), ("bGasSph", ctypes.c_int),
+                ("dMassGasMin", ctypes.c_double), ("dMassGasMax", ctypes.c_double),
+                ("dMassDarkMin", ctypes.c_double), ("dMassDarkMax", ctypes.c_double),
+                ("dMassStarMin", ctypes.c_double), ("dMassStarMax", ctypes.c_double),
+                ("bColMassWeight", ctypes.c_int), ("bColLogInterp", ctypes.c_int),
+                ("nColGas", ctypes.c_int), ("nColDark", ctypes.c_int), ("nColStar", ctypes.c_int),
+                ("dColGas", ctypes.c_float * 10), ("dColDark", ctypes.c_float * 10),
+                ("dColStar", ctypes.c_float * 10),
+                ("colGas", (ctypes.c_float * 3) * 10), ("colDark", (ctypes.c_float * 3) * 10),
+                ("colStar", (ctypes.c_float * 3) * 10)]
+
+
+def render_params(nx=320, ny=240, centre=(0.0, 0.0, 0.0), width=2.0, perspective=False,
+                  zEye=0.0, zClip=(-1e30, 1e30), gas_col=((1.0, 0.5, 0.2),), gas_levels=(),
+                  dark_col=((0.3, 0.4, 1.0),), star_col=((1.0, 1.0, 1.0),), bGasSph=1,
+                  soft_mul=(1.0, 1.0, 1.0), log_interp=0, mass_weight=0):
+    """A face-on frame of `width` length units across, looking down z."""
+    p = RenderParams()
+    p.nxPix, p.nyPix = nx, ny
+    s = nx / width
+    p.r[:] = centre
+    p.x[:] = (s, 0.0, 0.0)
+    p.y[:] = (0.0, s, 0.0)
+    p.z[:] = (0.0, 0.0, 1.0)
+    p.zEye = zEye
+    p.zClipNear, p.zClipFar = zClip
+    p.iProject = 2 if perspective else 1
+    p.dGasSoftMul, p.dDarkSoftMul, p.dStarSoftMul = soft_mul
+    p.bGasSph = bGasSph
+    big = 1e300
+    p.dMassGasMin = p.dMassDarkMin = p.dMassStarMin = 0.0
+    p.dMassGasMax = p.dMassDarkMax = p.dMassStarMax = big
+    p.bColMassWeight, p.bColLogInterp = mass_weight, log_interp
+    for cols, levels, cname, lname, nname in ((gas_col, gas_levels, "colGas", "dColGas", "nColGas"),
+                                              (dark_col, (), "colDark", "dColDark", "nColDark"),
+                                              (star_col, (), "colStar", "dColStar", "nColStar")):
+        for k, c in enumerate(cols):
+            getattr(p, cname)[k][:] = c
+        for k, v in enumerate(levels):
+            getattr(p, lname)[k] = v
+        setattr(p, nname, len(levels))
+    return p
+
+
 class TipsyHeader(ctypes.Structure):
     """tsph_tipsy_header: the Tipsy file header (tipsydefs.h struct dump)."""
     _fields_ = [("time", ctypes.c_double), ("nbodies", ctypes.c_int), ("ndim", ctypes.c_int),
@@ -154,7 +206,7 @@ def load():
                  "tsph_step_status", "tsph_tipsy_read_header", "tsph_read_tipsy",
                  "tsph_write_tipsy", "tsph_get_snapshot_fields",
                  "tsph_set_snapshot_fields", "tsph_kick_rung", "tsph_top_step_kdk",
-                 "tsph_set_active_rung", "tsph_set_rungs", "tsph_get_rungs"):
+                 "tsph_set_active_rung", "tsph_set_rungs", "tsph_get_rungs", "tsph_render_tsc"):
         getattr(lib, name).restype = ctypes.c_int
     lib.tsph_destroy.restype = None
     _lib = lib
@@ -305,6 +357,14 @@ class Context:
         is the opening kick of a KDK step."""
         self._check(self.lib.tsph_kick_rung(self._ctx, int(iRung), ctypes.c_double(dt),
                                             int(close)))
+
+    # ---- frames ---------------------------------------------------------------
+    def render_tsc(self, rp, nstar=0):
+        """A TSC frame of the loaded particles: float32 (nyPix, nxPix, 3)."""
+        img = np.zeros((rp.nyPix, rp.nxPix, 3), dtype=np.float32)
+        self._check(self.lib.tsph_render_tsc(self._ctx, ctypes.byref(rp), int(nstar),
+                                             img.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+        return img
 
     # ---- adaptive timesteps ------------------------------------------------
     def top_step_kdk(self, t, dt, gp, sp, st):

@@ -364,6 +364,35 @@ int tsph_get_snapshot_fields(tsph_ctx *ctx, double *mass, double *soft, double *
 int tsph_set_snapshot_fields(tsph_ctx *ctx, const double *pot, const float *rho,
                              const float *metals, const float *tform);
 
+/* --- rendering (dfRenderParticleTSC dumpframe.c:1125-1230) ---------------
+ * A frame of the loaded particles splatted with the reference's TSC
+ * kernel into a headless RGB float image (the reference's DFIMAGE,
+ * row-major, y = 0 the top row).  Sizes: gas from its ball (bGasSph) or
+ * softening, dark and stars from their softening, each times its
+ * multiplier; colours interpolated in the density from per-type tables
+ * (dfColInterp dumpframe.c:1096-1122; star colour by age is not
+ * supported: stars use their table).  The gas density is that of the last
+ * SPH density pass, else the snapshot's; other particles use 0.  The first
+ * ngas particles are gas and the last nStar stars.  xlim, ylim and hmul
+ * follow dfSetupFrame (dumpframe.c:259-261). */
+typedef struct {
+    int nxPix, nyPix;
+    double r[3];                 /* centre */
+    double x[3], y[3], z[3];     /* projection vectors (pixels per length unit) */
+    double zEye, zClipNear, zClipFar;
+    int iProject;                /* 1 orthographic, 2 perspective */
+    double dGasSoftMul, dDarkSoftMul, dStarSoftMul;
+    int bGasSph;
+    double dMassGasMin, dMassGasMax, dMassDarkMin, dMassDarkMax, dMassStarMin, dMassStarMax;
+    int bColMassWeight, bColLogInterp;
+    int nColGas, nColDark, nColStar;         /* table lengths, 0..10 */
+    float dColGas[10], dColDark[10], dColStar[10];
+    float colGas[10][3], colDark[10][3], colStar[10][3];
+} tsph_render_params;
+
+/* rgb receives nxPix*nyPix*3 floats (host memory). */
+int tsph_render_tsc(tsph_ctx *ctx, const tsph_render_params *rp, int nStar, float *rgb);
+
 /* --- tuning --------------------------------------------------------------
  * Launch-shape knobs of the CUDA path.  None changes a result: the tree,
  * the interaction lists and every force are identical for any setting

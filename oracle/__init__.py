@@ -259,6 +259,16 @@ def reference_sph_active(pos, vel, mass, soft, u, rung, iRung, sp):
                 mumax=f[:, 3].copy(), dt=f[:, 4].copy(), fDensity=f[:, 5].copy())
 
 
+def reference_render_tsc(pos, mass, soft, fBall2, fDensity, ngas, nstar, rp):
+    """The reference's dfRenderParticles (TSC) frame: float32 (ny, nx, 3)."""
+    lib = reference().lib
+    arrs = [_c64(pos, (-1, 3)), _c64(mass), _c64(soft), _c64(fBall2), _c64(fDensity)]
+    img = np.zeros((rp.nyPix, rp.nxPix, 3), dtype=np.float32)
+    lib.ref_render_tsc(len(arrs[1]), int(ngas), int(nstar), *[_d(a) for a in arrs], ctypes.byref(rp),
+                       img.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+    return img
+
+
 def knn_fball2(pos, nsmooth, periodic=False, L=1.0, nthreads=1):
     pos = _c64(pos, (-1, 3))
     n = pos.shape[0]

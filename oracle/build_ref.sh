@@ -10,9 +10,9 @@ OUT="$HERE/_ref"
 [ -f "$REF/pkd.c" ] || { echo "reference sources not found at $REF" >&2; exit 1; }
 mkdir -p "$OUT"
 CFLAGS="-O2 -fPIC -ffp-contract=off -fno-fast-math -w -DNOCOOLING -DGASOLINE -DM4 \
- -include stdio.h -I$HERE/shim -I$REF"
+ -include stdio.h -I$HERE/shim -I$REF -I$HERE/../include"
 OBJS=""
-for f in pkd walk grav ewald v_sqrt1 treezip smooth smoothfcn; do
+for f in pkd walk grav ewald v_sqrt1 treezip smooth smoothfcn dumpframe dffuncs; do
   gcc $CFLAGS -c "$REF/$f.c" -o "$OUT/$f.o" &
   OBJS="$OBJS $OUT/$f.o"
 done

@@ -757,3 +757,77 @@ int ref_sph_active(int n, const double *pos, const double *vel, const double *ma
     pkdFinish(pkd);
     return 0;
 }
+
+/*
+ * A TSC frame through the reference's own dfRenderParticles
+ * (dumpframe.c:1394-1470) and dfRenderParticleTSC (dumpframe.c:1125-1230),
+ * with the frame set up as dfSetupFrame does (xlim, ylim, hmul,
+ * dumpframe.c:259-261).  Particles: the first ngas gas, the last nstar
+ * stars, the rest dark; rgb receives nxPix*nyPix*3 floats.
+ */
+#include "dumpframe.h"
+#include "tsph.h"
+
+typedef struct {
+    double r[3];
+    double fMass, fSoft, fBall2;
+    unsigned int iActive;
+    double fDensity, fTimeForm;
+} RPART;
+
+int ref_render_tsc(int n, int ngas, int nstar, const double *pos, const double *mass,
+                   const double *soft, const double *fBall2, const double *fDensity,
+                   const tsph_render_params *rp, float *rgb)
+{
+    struct inDumpFrame in;
+    RPART *p = (RPART *)calloc(n > 0 ? n : 1, sizeof(RPART));
+    DFIMAGE *img = (DFIMAGE *)calloc((size_t)rp->nxPix * rp->nyPix, sizeof(DFIMAGE));
+    int i, j;
+    memset(&in, 0, sizeof(in));
+    in.nxPix = rp->nxPix; in.nyPix = rp->nyPix;
+    for (j = 0; j < 3; ++j) {
+        in.r[j] = rp->r[j]; in.x[j] = rp->x[j]; in.y[j] = rp->y[j]; in.z[j] = rp->z[j];
+    }
+    in.zEye = rp->zEye; in.zClipNear = rp->zClipNear; in.zClipFar = rp->zClipFar;
+    in.iProject = rp->iProject == 2 ? DF_PROJECT_PERSPECTIVE : DF_PROJECT_ORTHO;
+    in.dGasSoftMul = rp->dGasSoftMul; in.dDarkSoftMul = rp->dDarkSoftMul;
+    in.dStarSoftMul = rp->dStarSoftMul;
+    in.bGasSph = rp->bGasSph;
+    in.dMassGasMin = rp->dMassGasMin; in.dMassGasMax = rp->dMassGasMax;
+    in.dMassDarkMin = rp->dMassDarkMin; in.dMassDarkMax = rp->dMassDarkMax;
+    in.dMassStarMin = rp->dMassStarMin; in.dMassStarMax = rp->dMassStarMax;
+    in.bColMassWeight = rp->bColMassWeight; in.bColLogInterp = rp->bColLogInterp;
+    in.nColGas = rp->nColGas; in.nColDark = rp->nColDark; in.nColStar = rp->nColStar;
+    for (i = 0; i < 10; ++i) {
+        in.dColGas[i] = rp->dColGas[i]; in.dColDark[i] = rp->dColDark[i];
+        in.dColStar[i] = rp->dColStar[i];
+        in.ColGas[i].r = rp->colGas[i][0]; in.ColGas[i].g = rp->colGas[i][1]; in.ColGas[i].b = rp->colGas[i][2];
+        in.ColDark[i].r = rp->colDark[i][0]; in.ColDark[i].g = rp->colDark[i][1]; in.ColDark[i].b = rp->colDark[i][2];
+        in.ColStar[i].r = rp->colStar[i][0]; in.ColStar[i].g = rp->colStar[i][1]; in.ColStar[i].b = rp->colStar[i][2];
+    }
+    in.iColStarAge = DF_STAR_AGE_BASIC;
+    in.iRender = DF_RENDER_TSC;
+    in.dTime = 0.0;
+    in.dYearUnit = 1.0;
+    in.xlim = (in.nxPix - 1) * .5;
+    in.ylim = (in.nyPix - 1) * .5;
+    in.hmul = 4 * sqrt(in.x[0] * in.x[0] + in.x[1] * in.x[1] + in.x[2] * in.x[2]);
+    for (i = 0; i < n; ++i) {
+        for (j = 0; j < 3; ++j) p[i].r[j] = pos[3 * i + j];
+        p[i].fMass = mass[i];
+        p[i].fSoft = soft[i];
+        p[i].fBall2 = fBall2[i];
+        p[i].fDensity = fDensity[i];
+        p[i].iActive = i < ngas ? TYPE_GAS : (i < n - nstar ? TYPE_DARK : TYPE_STAR);
+    }
+    dfRenderParticlesInit(&in, TYPE_GAS, TYPE_DARK, TYPE_STAR, &p[0].r[0], &p[0].fMass,
+                          &p[0].fSoft, &p[0].fBall2, &p[0].iActive, &p[0].fDensity,
+                          &p[0].fTimeForm, p, sizeof(RPART));
+    dfRenderParticles(&in, img, p, n);
+    for (i = 0; i < rp->nxPix * rp->nyPix; ++i) {
+        rgb[3 * i] = img[i].r; rgb[3 * i + 1] = img[i].g; rgb[3 * i + 2] = img[i].b;
+    }
+    free(p);
+    free(img);
+    return 0;
+}

@@ -15,8 +15,10 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.abspath(os.path.join(HERE, "..", "..")))
 
+sys.path.insert(0, os.path.abspath(os.path.join(HERE, "..")))
 import oracle  # noqa: E402
 from gasoline_gb300 import ics  # noqa: E402
+from golden_io import render_frames  # noqa: E402
 
 
 def grav_case(name, pos, mass, soft, gp):
@@ -123,6 +125,24 @@ def multistep_cases():
     print("multistep cases: run max rungs", r["maxRung"], "force passes", r["counts"])
 
 
+def render_case():
+    """TSC frames of gas, dark matter and stars through the reference's
+    dfRenderParticles, gas balls and densities from the reference's SPH."""
+    pg, vg, mg, ug = ics.gas_sphere(2000, seed=22)
+    pd, vd, md = ics.plummer(1000, seed=23)
+    pos = np.concatenate([pg, pd]); n = len(pos)
+    mass = np.concatenate([0.2 * mg, 0.8 * md]); soft = np.full(n, 0.02)
+    sph = oracle.reference().sph(pg, vg, mg * 0.2, soft[:2000], ug, oracle.sph_params(nSmooth=32))
+    fb = np.concatenate([sph["fBall2"], np.zeros(n - 2000)])
+    rho = np.concatenate([sph["fDensity"], np.zeros(n - 2000)])
+    out = {}
+    for k, rp in enumerate(render_frames()):
+        out[f"img{k}"] = oracle.reference_render_tsc(pos, mass, soft, fb, rho, 2000, 100, rp)
+    np.savez_compressed(os.path.join(HERE, "render_tsc.npz"), pos=pos, mass=mass, soft=soft,
+                        u=ug, ngas=2000, nstar=100, fBall2=fb, fDensity=rho, **out)
+    print("render frames", [float(out[k].sum()) for k in sorted(out)])
+
+
 def main():
     if not oracle.reference_available():
         oracle.build_reference()
@@ -142,15 +162,18 @@ def main():
              oracle.sph_params(nSmooth=32))
     tipsy_case("tipsy_mixed", 300, 500, 200, seed=16)
     multistep_cases()
+    render_case()
 
 
 if __name__ == "__main__":
-    if len(sys.argv) > 1 and sys.argv[1] in ("tipsy", "multistep"):
+    if len(sys.argv) > 1 and sys.argv[1] in ("tipsy", "multistep", "render"):
         if not oracle.reference_available():
             oracle.build_reference()
         if sys.argv[1] == "tipsy":
             tipsy_case("tipsy_mixed", 300, 500, 200, seed=16)
-        else:
+        elif sys.argv[1] == "multistep":
             multistep_cases()
+        else:
+            render_case()
     else:
         main()

@@ -37,3 +37,16 @@ def rel_err(a, b):
         num = np.abs(a - b)
         den = np.abs(b)
     return num / np.maximum(den, 1e-300)
+
+
+def render_frames():
+    """The frame parameters of the rendering fixture (gasoline_gb300's
+    render_params): orthographic with log density colours and mass
+    weighting, and perspective."""
+    import gasoline_gb300 as g
+    return [g.render_params(nx=160, ny=120, width=3.0, gas_levels=(-1.0, 1.0),
+                            gas_col=((1.0, 0.2, 0.1), (0.2, 0.4, 1.0)), log_interp=1, mass_weight=1,
+                            soft_mul=(1.0, 2.0, 4.0)),
+            g.render_params(nx=160, ny=120, width=3.0 / 4.0, perspective=True, zEye=4.0,
+                            zClip=(0.5, 100.0), gas_levels=(0.5, 5.0),
+                            gas_col=((1.0, 0.0, 0.0), (0.0, 1.0, 0.0)))]

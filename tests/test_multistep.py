@@ -1,11 +1,11 @@
-"""Adaptive timesteps on the CPU: the golden runs of the reference's
+"""Adaptive timesteps and frames on the CPU: the golden runs of the reference's
 msrTopStepKDK recursion (tests/golden/ms_*.npz) are consistent, and --
 where the reference is built here -- reproduce bit for bit."""
 import numpy as np
 import pytest
 
 import oracle
-from golden_io import load
+from golden_io import load, render_frames
 
 
 def test_golden_run_is_consistent():
@@ -32,3 +32,12 @@ def test_reference_run_reproduces_golden():
                                    d["u0"], gp, sp, st)
     for k in ("pos", "vel", "rung", "dt", "u", "maxRung", "counts"):
         assert np.array_equal(r[k], d[k]), k
+
+
+@pytest.mark.skipif(not oracle.reference_available(), reason="reference not built here")
+def test_reference_render_reproduces_golden():
+    d = load("render_tsc")
+    for k, rp in enumerate(render_frames()):
+        img = oracle.reference_render_tsc(d["pos"], d["mass"], d["soft"], d["fBall2"],
+                                          d["fDensity"], int(d["ngas"]), int(d["nstar"]), rp)
+        assert np.array_equal(img, d[f"img{k}"]), k
