@@ -157,7 +157,7 @@ def run_ours(args, rank, world, local_rank):
     def timed(gp, steps, warmup, e2e=False):
         for _ in range(warmup):
             if e2e:
-                ctx.set_particles_ptr(n, hpos.data_ptr(), hm.data_ptr(), hs.data_ptr())
+                ctx.update_particles_ptr(n, hpos.data_ptr(), hm.data_ptr(), hs.data_ptr())
             ctx.grav_all(gp)
             if e2e:
                 ctx.get_gravity_ptr(hacc.data_ptr())
@@ -174,7 +174,7 @@ def run_ours(args, rank, world, local_rank):
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
             if e2e:
-                ctx.set_particles_ptr(n, hpos.data_ptr(), hm.data_ptr(), hs.data_ptr())
+                ctx.update_particles_ptr(n, hpos.data_ptr(), hm.data_ptr(), hs.data_ptr())
             out = ctx.grav_all(gp)
             if e2e:
                 ctx.get_gravity_ptr(hacc.data_ptr())

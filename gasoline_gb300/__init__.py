@@ -206,7 +206,8 @@ def load():
                  "tsph_step_status", "tsph_tipsy_read_header", "tsph_read_tipsy",
                  "tsph_write_tipsy", "tsph_get_snapshot_fields",
                  "tsph_set_snapshot_fields", "tsph_kick_rung", "tsph_top_step_kdk",
-                 "tsph_set_active_rung", "tsph_set_rungs", "tsph_get_rungs", "tsph_render_tsc"):
+                 "tsph_set_active_rung", "tsph_set_rungs", "tsph_get_rungs", "tsph_render_tsc",
+                 "tsph_update_particles"):
         getattr(lib, name).restype = ctypes.c_int
     lib.tsph_destroy.restype = None
     _lib = lib
@@ -268,6 +269,21 @@ class Context:
         self._check(self.lib.tsph_set_particles(
             self._ctx, n, ctypes.cast(pos_ptr, _P), ctypes.cast(mass_ptr, _P),
             ctypes.cast(soft_ptr, _P)))
+
+    def update_particles_ptr(self, n, pos_ptr, mass_ptr, soft_ptr):
+        """tsph_update_particles from raw host pointers: new values for the
+        particles already loaded, their order kept."""
+        self.n = n
+        self._check(self.lib.tsph_update_particles(
+            self._ctx, n, ctypes.cast(pos_ptr, _P), ctypes.cast(mass_ptr, _P),
+            ctypes.cast(soft_ptr, _P)))
+
+    def update_particles(self, pos, mass, soft):
+        pos = _c64(pos, (-1, 3))
+        mass = _c64(mass)
+        soft = _c64(soft)
+        self.n = len(mass)
+        self._check(self.lib.tsph_update_particles(self._ctx, self.n, _d(pos), _d(mass), _d(soft)))
 
     def set_velocities(self, vel, ngas=0, u=None):
         vel = _c64(vel, (-1, 3))

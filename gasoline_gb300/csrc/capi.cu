@@ -272,6 +272,37 @@ extern "C" int tsph_set_particles(tsph_ctx *ctx, int n, const double *pos, const
     return TSPH_OK;
 }
 
+__global__ void k_update_pos(int n, const double *__restrict__ pos3, TsphDevState C) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    C.x[i] = pos3[3 * i];
+    C.y[i] = pos3[3 * i + 1];
+    C.z[i] = pos3[3 * i + 2];
+}
+
+// New positions, masses and softenings of the particles already loaded
+// (same count, same caller indices): everything else, including the
+// particle order the last tree left, is kept, as the reference's particle
+// store keeps its order from one step to the next.
+extern "C" int tsph_update_particles(tsph_ctx *ctx, int n, const double *pos, const double *mass,
+                                     const double *soft) {
+    if (!ctx || n < 0 || (n > 0 && (!pos || !mass || !soft))) return TSPH_ERR_ARG;
+    if (!ctx->haveParts || n != ctx->n) return tsph_set_particles(ctx, n, pos, mass, soft);
+    if (ctx->capturing) return TSPH_ERR_STATE;
+    cudaSetDevice(ctx->device);
+    ctx->haveTree = ctx->haveGrav = false;
+    ctx->S.haveDensity = ctx->S.havePressure = false;
+    ctx->sysVersion++;
+    if (n == 0) return TSPH_OK;
+    TSPH_CK(cudaMemcpyAsync(ctx->dStage, pos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
+    k_update_pos<<<tsph_blocks(n, 256), 256, 0, ctx->stream>>>(n, ctx->dStage, ctx->C);
+    TSPH_LAUNCH_CK("k_update_pos");
+    TSPH_CK(cudaMemcpyAsync(ctx->C.m, mass, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    TSPH_CK(cudaMemcpyAsync(ctx->C.h, soft, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    TSPH_CK(cudaStreamSynchronize(ctx->stream));   // host buffers reusable on return
+    return TSPH_OK;
+}
+
 // Tree order grouped by system: a stable counting sort of the caller
 // indices [0, n) by sys[], the sizes of the non-empty systems in order.
 static int order_by_system(const int *sys, int n, int nSys, int *order, int *counts, int *nR) {

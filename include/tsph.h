@@ -149,6 +149,13 @@ const char *tsph_last_cuda_error(tsph_ctx *ctx);
  * set.  Device memory grows as needed and is kept between calls. */
 int tsph_set_particles(tsph_ctx *ctx, int n, const double *pos,
                        const double *mass, const double *soft);
+/* New positions, masses and softenings for the n particles already
+ * loaded (same caller indices).  Everything else stays, including the
+ * particle order the last tree build left, as the reference's particle
+ * store keeps its order between steps; the next build starts from it.
+ * With a different n it is tsph_set_particles. */
+int tsph_update_particles(tsph_ctx *ctx, int n, const double *pos,
+                          const double *mass, const double *soft);
 /* Velocities vel[3n] (all particles) and, for the first ngas particles,
  * specific thermal energy u[ngas] (the reference's u; uPred = u, vPred = v
  * at load).  ngas may be 0. */

@@ -263,3 +263,30 @@ def test_exact_fallback_is_rare(ctx):
     ctx.set_particles(pos, m, np.full(len(m), 1e-3))
     out = ctx.grav_all(g.grav_params(periodic=True, precision=g.FP32))
     assert out["dExactFrac"] < 1e-2
+
+
+def test_update_particles_keeps_order_same_forces(ctx):
+    """tsph_update_particles keeps the particle order of the last tree;
+    the tree's cells and lists are those of a fresh load and the forces
+    agree to FP64 rounding (only the order inside buckets differs)."""
+    import gasoline_gb300 as gg
+    pos, vel, m = gg.ics.plummer(20000, seed=71)
+    soft = np.full(len(m), 0.01)
+    gp = gg.grav_params(periodic=False, precision=gg.FP64)
+    ctx.set_particles(pos, m, soft)
+    ctx.grav_all(gp)
+    pos2 = pos + 1e-3 * vel
+    ctx.update_particles(pos2, m, soft)
+    a = ctx.grav_all(gp)
+    ga = ctx.get_gravity()
+    c2 = gg.Context(0)
+    try:
+        c2.set_particles(pos2, m, soft)
+        b = c2.grav_all(gp)
+        gb = c2.get_gravity()
+    finally:
+        c2.close()
+    for k in ("nActive", "nBuckets", "dPartSum", "dCellSum", "dSoftSum"):
+        assert a[k] == b[k], k
+    e = np.linalg.norm(ga["acc"] - gb["acc"], axis=1) / np.linalg.norm(gb["acc"], axis=1)
+    assert e.max() <= 1e-12
