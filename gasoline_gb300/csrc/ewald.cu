@@ -33,6 +33,8 @@ struct EwConst {
     float momf[35];
     double L, alpha, alpha2, k1, ka, fEwCut2, smallR2;
     int nEwReps, nReps, nEwh, iOrder;
+    int hMax;            // largest |component| of a k-space vector
+    int hCut2;           // floor(fEwhCut^2): the integer |h|^2 kept (ewald.c:205-211)
     double hx[EW_MAXH], hy[EW_MAXH], hz[EW_MAXH], hC[EW_MAXH], hS[EW_MAXH];
     // FP32 copies of the k-space table for the FP32 kernel
     float hxf[EW_MAXH], hyf[EW_MAXH], hzf[EW_MAXH], hCf[EW_MAXH], hSf[EW_MAXH];
@@ -394,21 +396,79 @@ __global__ void __launch_bounds__(128) k_ewald(TsphDevParts P, TsphDevCounters *
                 }
             }
         }
-        for (int i = 0; i < cE.nEwh; ++i) {
-            Real hx, hy, hz, hC, hS;
-            if constexpr (sizeof(Real) == 4) {
-                hx = cE.hxf[i]; hy = cE.hyf[i]; hz = cE.hzf[i]; hC = cE.hCf[i]; hS = cE.hSf[i];
-            } else {
-                hx = cE.hx[i]; hy = cE.hy[i]; hz = cE.hz[i]; hC = cE.hC[i]; hS = cE.hS[i];
+        if (sizeof(Real) == 4 && cE.hMax <= 3) {
+            // FP32: e^{i h.x} of every k-space vector from the three phase
+            // factors e^{i 2 pi x/L}, e^{i 2 pi y/L}, e^{i 2 pi z/L} by complex
+            // products, in the table's order (hx, hy, hz ascending) -- three
+            // sincos per particle instead of one per vector
+            const float tp = (float)(2.0 * M_PI / cE.L);
+            float c1[3], s1[3];
+            sincosf(tp * (float)dx, &s1[0], &c1[0]);
+            sincosf(tp * (float)dy, &s1[1], &c1[1]);
+            sincosf(tp * (float)dz, &s1[2], &c1[2]);
+            const int R = cE.hMax;
+            // e^{-i R theta} per axis
+            float cs0[3], sn0[3];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                float c = 1.0f, s = 0.0f;
+                for (int k = 0; k < R; ++k) {
+                    const float t = c * c1[a] + s * s1[a];   // times e^{-i theta}
+                    s = s * c1[a] - c * s1[a];
+                    c = t;
+                }
+                cs0[a] = c;
+                sn0[a] = s;
             }
-            Real hdotx = hx * dx + hy * dy + hz * dz;
-            Real s, c;
-            sincos_r(hdotx, &s, &c);
-            kadd(fPot, cpot, hC * c + hS * s);
-            Real t = hC * s - hS * c;
-            kadd(ax, cax, hx * t);
-            kadd(ay, cay, hy * t);
-            kadd(az, caz, hz * t);
+            const int cut2 = cE.hCut2;
+            int i = 0;
+            float cx = cs0[0], sx = sn0[0];
+            for (int ix = -R; ix <= R; ++ix) {
+                float cy = cs0[1], sy = sn0[1];
+                for (int iy = -R; iy <= R; ++iy) {
+                    const float cxy = cx * cy - sx * sy, sxy = cx * sy + sx * cy;
+                    float cz = cs0[2], sz = sn0[2];
+                    for (int iz = -R; iz <= R; ++iz) {
+                        const int h2 = ix * ix + iy * iy + iz * iz;
+                        if (h2 != 0 && h2 <= cut2) {
+                            const float c = cxy * cz - sxy * sz, s = cxy * sz + sxy * cz;
+                            const float hC = cE.hCf[i], hS = cE.hSf[i];
+                            kadd(fPot, cpot, (Real)(hC * c + hS * s));
+                            const float t = hC * s - hS * c;
+                            kadd(ax, cax, (Real)(cE.hxf[i] * t));
+                            kadd(ay, cay, (Real)(cE.hyf[i] * t));
+                            kadd(az, caz, (Real)(cE.hzf[i] * t));
+                            ++i;
+                        }
+                        const float t = cz * c1[2] - sz * s1[2];
+                        sz = cz * s1[2] + sz * c1[2];
+                        cz = t;
+                    }
+                    const float t = cy * c1[1] - sy * s1[1];
+                    sy = cy * s1[1] + sy * c1[1];
+                    cy = t;
+                }
+                const float t = cx * c1[0] - sx * s1[0];
+                sx = cx * s1[0] + sx * c1[0];
+                cx = t;
+            }
+        } else {
+            for (int i = 0; i < cE.nEwh; ++i) {
+                Real hx, hy, hz, hC, hS;
+                if constexpr (sizeof(Real) == 4) {
+                    hx = cE.hxf[i]; hy = cE.hyf[i]; hz = cE.hzf[i]; hC = cE.hCf[i]; hS = cE.hSf[i];
+                } else {
+                    hx = cE.hx[i]; hy = cE.hy[i]; hz = cE.hz[i]; hC = cE.hC[i]; hS = cE.hS[i];
+                }
+                Real hdotx = hx * dx + hy * dy + hz * dz;
+                Real s, c;
+                sincos_r(hdotx, &s, &c);
+                kadd(fPot, cpot, hC * c + hS * s);
+                Real t = hC * s - hS * c;
+                kadd(ax, cax, hx * t);
+                kadd(ay, cay, hy * t);
+                kadd(az, caz, hz * t);
+            }
         }
         if constexpr (sizeof(Real) == 4) {
             // walk (compensated FP32 pair) + Ewald (compensated FP32 pair), in FP64
@@ -591,6 +651,11 @@ int tsph_ewald(tsph_ctx *ctx, const tsph_grav_params *gp) {
             }
     E.nEwh = ih;
     ctx->nEwt = ih;
+    const double hc2 = gp->fEwhCut * gp->fEwhCut;
+    E.hCut2 = hc2 < 1e6 ? (int)floor(hc2) : 1000000;
+    E.hMax = 0;
+    for (int h = hReps; h >= 1; --h)
+        if (h * h <= hc2) { E.hMax = h; break; }
     for (int i = 0; i < ih; ++i) {
         E.hxf[i] = (float)E.hx[i]; E.hyf[i] = (float)E.hy[i]; E.hzf[i] = (float)E.hz[i];
         E.hCf[i] = (float)E.hC[i]; E.hSf[i] = (float)E.hS[i];
