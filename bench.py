@@ -266,7 +266,8 @@ def run_ours(args, rank, world, local_rank):
                                    "p99": float(np.percentile(e64, 99))}},
             "tuned": tuned,
             "interactions": {"dPartSum": out32["dPartSum"], "dCellSum": out32["dCellSum"],
-                             "dSoftSum": out32["dSoftSum"], "exact_fallback_frac": out32["dExactFrac"]},
+                             "dSoftSum": out32["dSoftSum"], "exact_fallback_frac": out32["dExactFrac"],
+                             "opening_tests": out32["dTests"], "walk_visits": out32["dVisits"]},
         }
         if not args.no_cpu:
             result["cpu_baseline"] = cpu_baseline(args, pos, m, soft)

@@ -46,7 +46,8 @@ class GravOut(ctypes.Structure):
     _fields_ = [("nActive", ctypes.c_int), ("nBuckets", ctypes.c_int),
                 ("dPartSum", ctypes.c_double), ("dCellSum", ctypes.c_double),
                 ("dSoftSum", ctypes.c_double), ("dFlop", ctypes.c_double),
-                ("dFlopEwald", ctypes.c_double), ("dExactFrac", ctypes.c_double)]
+                ("dFlopEwald", ctypes.c_double), ("dExactFrac", ctypes.c_double),
+                ("dTests", ctypes.c_double), ("dVisits", ctypes.c_double)]
 
 
 class SphParams(ctypes.Structure):

@@ -489,6 +489,8 @@ extern "C" int tsph_grav_all(tsph_ctx *ctx, const tsph_grav_params *gp, tsph_gra
         out->dFlop = fg + fe;
         out->dFlopEwald = fe;
         out->dExactFrac = c.nTests ? (double)c.nExactTests / (double)c.nTests : 0.0;
+        out->dTests = (double)c.nTests;
+        out->dVisits = (double)c.nVisits;
     }
     return TSPH_OK;
 }

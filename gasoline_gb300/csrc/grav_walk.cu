@@ -51,8 +51,33 @@ struct WalkConst {
     float offl[27][3];
     float offmax;      // max |offset| component
     float E0;          // absolute error floor of the hi/lo relative coordinates
+    double L;          // period (0 when not periodic)
+    float Lh, Ll;      // its hi/lo FP32 split
 };
 __constant__ WalkConst cW;
+
+// Replica offsets from the replica index r = (ix+1)*9 + (iy+1)*3 + (iz+1)
+// (at most one replica each way): i*L, and its FP32 hi/lo parts i*Lh and
+// i*Ll, exact for i in {-1, 0, 1}.  Computed instead of read from a
+// constant table, whose reads would serialise on the warp's distinct
+// replicas.
+__device__ __forceinline__ void rep_idx(int r, float &ix, float &iy, float &iz) {
+    ix = (float)(r / 9 - 1);
+    iy = (float)((r / 3) % 3 - 1);
+    iz = (float)(r % 3 - 1);
+}
+__device__ __forceinline__ void rep_off32(int r, float &hx, float &hy, float &hz, float &lx, float &ly,
+                                          float &lz) {
+    float ix, iy, iz;
+    rep_idx(r, ix, iy, iz);
+    hx = ix * cW.Lh; hy = iy * cW.Lh; hz = iz * cW.Lh;
+    lx = ix * cW.Ll; ly = iy * cW.Ll; lz = iz * cW.Ll;
+}
+__device__ __forceinline__ void rep_off64(int r, double *o) {
+    float ix, iy, iz;
+    rep_idx(r, ix, iy, iz);
+    o[0] = (double)ix * cW.L; o[1] = (double)iy * cW.L; o[2] = (double)iz * cW.L;
+}
 
 template <typename Real, int NBT>
 struct WalkSmem {
@@ -251,16 +276,19 @@ __device__ __forceinline__ void stage_pp(WalkSmem<Real, NBT> &S, const TsphDevPa
         if constexpr (sizeof(Real) == 4) {
             float4 a = P.ph[idx], b = P.pl[idx];
             int r = rep == 31 ? cW.selfRep : rep;
-            S.r0[e] = make_float4(((a.x - bchx) + cW.offh[r][0]) + ((b.x - bclx) + cW.offl[r][0]),
-                                  ((a.y - bchy) + cW.offh[r][1]) + ((b.y - bcly) + cW.offl[r][1]),
-                                  ((a.z - bchz) + cW.offh[r][2]) + ((b.z - bclz) + cW.offl[r][2]),
-                                  a.w);
+            float ohx, ohy, ohz, olx, oly, olz;
+            rep_off32(r, ohx, ohy, ohz, olx, oly, olz);
+            S.r0[e] = make_float4(((a.x - bchx) + ohx) + ((b.x - bclx) + olx),
+                                  ((a.y - bchy) + ohy) + ((b.y - bcly) + oly),
+                                  ((a.z - bchz) + ohz) + ((b.z - bclz) + olz), a.w);
             S.rh[e] = b.w;
         } else {
             int r = rep == 31 ? cW.selfRep : rep;
-            S.ex[e] = (Real)(P.x[idx] + cW.off[r][0]);
-            S.ey[e] = (Real)(P.y[idx] + cW.off[r][1]);
-            S.ez[e] = (Real)(P.z[idx] + cW.off[r][2]);
+            double o[3];
+            rep_off64(r, o);
+            S.ex[e] = (Real)(P.x[idx] + o[0]);
+            S.ey[e] = (Real)(P.y[idx] + o[1]);
+            S.ez[e] = (Real)(P.z[idx] + o[2]);
             S.em[e] = (Real)P.m[idx];
             S.eh[e] = (Real)P.h[idx];
         }
@@ -314,15 +342,19 @@ __device__ __forceinline__ void stage_cells(WalkSmem<Real, NBT> &S, const int *b
         if constexpr (sizeof(Real) == 4) {
             float4 h4 = T.wcomh[c], l4 = T.wcoml[c];
             float4 m0 = T.wmom0[c], m1 = T.wmom1[c];
-            cx = ((h4.x - bchx) + cW.offh[r][0]) + ((l4.x - bclx) + cW.offl[r][0]);
-            cy = ((h4.y - bchy) + cW.offh[r][1]) + ((l4.y - bcly) + cW.offl[r][1]);
-            cz = ((h4.z - bchz) + cW.offh[r][2]) + ((l4.z - bclz) + cW.offl[r][2]);
+            float ohx, ohy, ohz, olx, oly, olz;
+            rep_off32(r, ohx, ohy, ohz, olx, oly, olz);
+            cx = ((h4.x - bchx) + ohx) + ((l4.x - bclx) + olx);
+            cy = ((h4.y - bchy) + ohy) + ((l4.y - bcly) + oly);
+            cz = ((h4.z - bchz) + ohz) + ((l4.z - bclz) + olz);
             m = m0.x; q[0] = m0.y; q[1] = m0.z; q[2] = m0.w; q[3] = m1.x; q[4] = m1.y; q[5] = m1.z;
             hc = m1.w;
         } else {
-            cx = (Real)(T.r[3 * c] + cW.off[r][0]);
-            cy = (Real)(T.r[3 * c + 1] + cW.off[r][1]);
-            cz = (Real)(T.r[3 * c + 2] + cW.off[r][2]);
+            double o[3];
+            rep_off64(r, o);
+            cx = (Real)(T.r[3 * c] + o[0]);
+            cy = (Real)(T.r[3 * c + 1] + o[1]);
+            cz = (Real)(T.r[3 * c + 2] + o[2]);
             m = (Real)T.fMass[c];
 #pragma unroll
             for (int k = 0; k < 6; ++k) q[k] = (Real)T.Q[6 * c + k];
@@ -457,6 +489,7 @@ __global__ void __launch_bounds__(WPB * 32) k_walk(WalkArgs W) {
     const float relF = 4.0f * u32;
 
     unsigned long long cPP = 0, cN = 0, cS = 0, cExact = 0, cTests = 0, cBsq = 0, cIntra = 0, cAct = 0;
+    unsigned long long cVisit = 0;
 
     for (;;) {
         int b = 0;
@@ -538,6 +571,7 @@ __global__ void __launch_bounds__(WPB * 32) k_walk(WalkArgs W) {
             sp -= take;
             int act = ACT_NONE, cell = 0, rep = 0, up = -1, cnt = 0, plo = 0;
             if (ent >= 0) {
+                ++cVisit;
                 cell = ent >> 5;
                 rep = ent & 31;
                 int4 lk = T.wlink[cell];
@@ -545,9 +579,11 @@ __global__ void __launch_bounds__(WPB * 32) k_walk(WalkArgs W) {
                 cnt = lk.y;
                 up = lk.z;
                 float4 ch = T.wcomh[cell], cl = T.wcoml[cell];
-                float rx = ((ch.x - bch[0]) + cW.offh[rep][0]) + ((cl.x - bcl[0]) + cW.offl[rep][0]);
-                float ry = ((ch.y - bch[1]) + cW.offh[rep][1]) + ((cl.y - bcl[1]) + cW.offl[rep][1]);
-                float rz = ((ch.z - bch[2]) + cW.offh[rep][2]) + ((cl.z - bcl[2]) + cW.offl[rep][2]);
+                float ohx, ohy, ohz, olx, oly, olz;
+                rep_off32(rep, ohx, ohy, ohz, olx, oly, olz);
+                float rx = ((ch.x - bch[0]) + ohx) + ((cl.x - bcl[0]) + olx);
+                float ry = ((ch.y - bch[1]) + ohy) + ((cl.y - bcl[1]) + oly);
+                float rz = ((ch.z - bch[2]) + ohz) + ((cl.z - bcl[2]) + olz);
                 float dx = fmaxf(fmaxf(fbmn[0] - rx, rx - fbmx[0]), 0.0f);
                 float dy = fmaxf(fmaxf(fbmn[1] - ry, ry - fbmx[1]), 0.0f);
                 float dz = fmaxf(fmaxf(fbmn[2] - rz, rz - fbmx[2]), 0.0f);
@@ -564,7 +600,11 @@ __global__ void __launch_bounds__(WPB * 32) k_walk(WalkArgs W) {
                     fo = filt(D2, M, ch.w, relF);
                     if (fo == 0) {
                         ++cExact;
-                        open = exact_decision(T, P, b, lo, n, cell, cW.off[rep], true) == 1;
+                        {
+                            double o[3];
+                            rep_off64(rep, o);
+                            open = exact_decision(T, P, b, lo, n, cell, o, true) == 1;
+                        }
                     } else {
                         open = fo < 0;
                     }
@@ -589,7 +629,11 @@ __global__ void __launch_bounds__(WPB * 32) k_walk(WalkArgs W) {
                     }
                     if (exactNeeded) {
                         ++cExact;
-                        newt = exact_decision(T, P, b, lo, n, cell, cW.off[rep], false) == 0;
+                        {
+                            double o[3];
+                            rep_off64(rep, o);
+                            newt = exact_decision(T, P, b, lo, n, cell, o, false) == 0;
+                        }
                     }
                     act = newt ? ACT_NEWT : ACT_SOFT;
                 }
@@ -734,6 +778,7 @@ __global__ void __launch_bounds__(WPB * 32) k_walk(WalkArgs W) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         cTests += __shfl_xor_sync(FULL, cTests, o);
+        cVisit += __shfl_xor_sync(FULL, cVisit, o);
         cExact += __shfl_xor_sync(FULL, cExact, o);
     }
     if (lane == 0) {
@@ -744,6 +789,7 @@ __global__ void __launch_bounds__(WPB * 32) k_walk(WalkArgs W) {
         atomicAdd(&W.cnt->nBucketSq, cBsq);
         atomicAdd(&W.cnt->nIntra, cIntra);
         atomicAdd(&W.cnt->nTests, cTests);
+        atomicAdd(&W.cnt->nVisits, cVisit);
         atomicAdd(&W.cnt->nExactTests, cExact);
     }
 }
@@ -854,6 +900,9 @@ int tsph_walk_interact(tsph_ctx *ctx, const tsph_grav_params *gp) {
                 }
             }
     wc.offmax = offmax;
+    wc.L = L;
+    wc.Lh = (float)L;
+    wc.Ll = (float)(L - (double)wc.Lh);
     // absolute error floor of hi/lo coordinates: a few ulp^2 of the largest
     // absolute coordinate (positions + offsets)
     rabs = ctx->dPeriodTree + offmax;

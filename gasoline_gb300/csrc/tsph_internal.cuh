@@ -136,6 +136,7 @@ struct TsphDevCounters {
     unsigned long long nEwLoop;      // Ewald real-space terms evaluated
     unsigned long long nExactTests;  // opening tests settled in FP64
     unsigned long long nTests;       // opening tests in total
+    unsigned long long nVisits;      // (cell, replica) entries the walk examined
     unsigned long long maxAbs;       // bits of max |coordinate| (non-negative double)
     unsigned int status;             // TSPH_ERR_* raised on device
     unsigned int pad;

@@ -96,7 +96,8 @@ typedef struct {
 
 /* pkdGravAll's out-parameters (nActive, pdPartSum, pdCellSum, pdSoftSum,
  * pdFlop), same definitions (pkd.c:2946-2962, grav.c:246-247,
- * ewald.c:175-176), plus the fraction of opening tests settled in FP64. */
+ * ewald.c:175-176), plus the fraction of opening tests settled in FP64
+ * and the number of opening tests the walk made. */
 typedef struct {
     int nActive;
     int nBuckets;
@@ -106,6 +107,8 @@ typedef struct {
     double dFlop;
     double dFlopEwald;
     double dExactFrac;
+    double dTests;       /* opening tests of cells with >= 4 particles */
+    double dVisits;      /* (cell, replica) entries examined by the walk */
 } tsph_grav_out;
 
 /* SPH parameters: the SMF fields the two passes read (smoothfcn.h:22-130,
