@@ -377,7 +377,7 @@ __device__ void density_epilogue(const SphArgs &A, KnnBatch &Bt, int cnt, int la
 // straddles the bracket get their FP64 distance.  The neighbour sums run
 // over N(i) in ascending index (FP64), so they depend on the set only.
 template <bool F32>
-__global__ void __launch_bounds__(SW * 32) k_knn_density(SphArgs A) {
+__global__ void __launch_bounds__(SW * 32, 5) k_knn_density(SphArgs A) {
     extern __shared__ __align__(16) unsigned char smraw[];
     KnnSmem &W = reinterpret_cast<KnnSmem *>(smraw)[threadIdx.x >> 5];
     KnnBatch &Bt = reinterpret_cast<KnnBatch *>(smraw + sizeof(KnnSmem) * SW)[threadIdx.x >> 5];
