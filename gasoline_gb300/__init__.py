@@ -82,7 +82,7 @@ def sph_params(nSmooth=32, periodic=False, L=1.0, alpha=1.0, beta=2.0,
 class Tuning(ctypes.Structure):
     """tsph_tuning (include/tsph.h): launch-shape knobs, result-neutral."""
     _fields_ = [("taskSize", ctypes.c_int), ("walkBlocksPerSM", ctypes.c_int),
-                ("reserved", ctypes.c_int * 6)]
+                ("walkGroup", ctypes.c_int), ("reserved", ctypes.c_int * 5)]
 
 
 class StepParams(ctypes.Structure):
@@ -545,11 +545,12 @@ class Context:
         """Wait for queued steps; raise on the first error they raised."""
         self._check(self.lib.tsph_step_status(self._ctx))
 
-    def set_tuning(self, taskSize=0, walkBlocksPerSM=0):
-        t = Tuning(taskSize, walkBlocksPerSM)
+    def set_tuning(self, taskSize=0, walkBlocksPerSM=0, walkGroup=0):
+        t = Tuning(taskSize, walkBlocksPerSM, walkGroup)
         self._check(self.lib.tsph_set_tuning(self._ctx, ctypes.byref(t)))
 
     def get_tuning(self):
         t = Tuning()
         self._check(self.lib.tsph_get_tuning(self._ctx, ctypes.byref(t)))
-        return {"taskSize": t.taskSize, "walkBlocksPerSM": t.walkBlocksPerSM}
+        return {"taskSize": t.taskSize, "walkBlocksPerSM": t.walkBlocksPerSM,
+                "walkGroup": t.walkGroup}

@@ -104,6 +104,8 @@ extern "C" void tsph_destroy(tsph_ctx *ctx) {
     FREE(S.need); FREE(S.list); FREE(S.list2); FREE(S.listN); FREE(S.rb2);
     FREE(ctx->dCnt); FREE(ctx->dBucketLists); FREE(ctx->dRoot); FREE(ctx->dEwt); FREE(ctx->dStage);
     FREE(ctx->dAux); FREE(ctx->dStepStatus);
+    FREE(ctx->dGroupFlag); FREE(ctx->dGroupScan); FREE(ctx->dGroupFirst); FREE(ctx->dGroupCount);
+    FREE(ctx->dGroupScratch);
     tsph_free_snapshot(ctx);
     free(ctx->hSys);
     free(ctx->hTmp);
@@ -627,8 +629,11 @@ extern "C" int tsph_set_tuning(tsph_ctx *ctx, const tsph_tuning *t) {
     if (!ctx || !t) return TSPH_ERR_ARG;
     if (t->taskSize < 0 || (t->taskSize > 0 && t->taskSize < 1024)) return TSPH_ERR_ARG;
     if (t->walkBlocksPerSM < 0 || t->walkBlocksPerSM > 32) return TSPH_ERR_ARG;
+    if (t->walkGroup < -1 || (t->walkGroup > 0 && (t->walkGroup < 32 || t->walkGroup > 4096)))
+        return TSPH_ERR_ARG;
     ctx->taskSize = t->taskSize;
     ctx->walkBlocksPerSM = t->walkBlocksPerSM;
+    ctx->walkGroup = t->walkGroup;
     return TSPH_OK;
 }
 
@@ -637,5 +642,6 @@ extern "C" int tsph_get_tuning(tsph_ctx *ctx, tsph_tuning *t) {
     memset(t, 0, sizeof(*t));
     t->taskSize = ctx->taskSize;
     t->walkBlocksPerSM = ctx->walkBlocksPerSM;
+    t->walkGroup = ctx->walkGroup;
     return TSPH_OK;
 }

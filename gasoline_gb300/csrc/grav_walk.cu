@@ -105,6 +105,9 @@ struct WalkSmem {
         };
     };
     Real px[NBT], py[NBT], pz[NBT], pm[NBT], ph[NBT];
+    // the warp's tallies of pkdGravAll's sums (lane 0 only)
+    unsigned long long tAct, tPP, tNewt, tSoft, tBsq, tIntra;
+    int gU, gNA;   // sizes of the lists the last group walk left
 };
 
 struct WalkArgs {
@@ -115,6 +118,11 @@ struct WalkArgs {
     const int *nBuckets;   // device: the tree's leaf count
     int *workCounter;
     int iOrder;
+    // walk groups (groupFirst null: one bucket per work unit)
+    const int *groupFirst;   // first bucket of every group, then the bucket count
+    const int *nGroups;      // device: number of groups
+    int *groupScratch;       // GRP_SCRATCH ints per warp of the launch
+    int groupMax;            // particles per group at most
 };
 
 __device__ __forceinline__ unsigned lane_lt() {
@@ -295,14 +303,18 @@ __device__ __forceinline__ void stage_pp(WalkSmem<Real, NBT> &S, const TsphDevPa
     }
 }
 
-// Evaluate staged P-P entries for this lane's particle.
-template <typename Real, int NBT>
+// Evaluate staged P-P entries for this lane's particle.  SELF: the tile
+// holds the bucket's own particles (the first tile of every bucket), so
+// the particle's pair with itself is skipped.
+template <typename Real, int NBT, bool SELF>
 __device__ __forceinline__ void eval_pp(WalkSmem<Real, NBT> &S, int cnt, int i, int slot, int pidx,
                                         int bucketLo, Acc<Real> &A) {
     Real xi = S.px[i], yi = S.py[i], zi = S.pz[i], hi = S.ph[i], mi = S.pm[i];
     for (int e = slot; e < cnt; e += 32 / NBT) {
-        int ent = S.pp[e];
-        if ((ent & 31) == 31 && (ent >> 5) == bucketLo + i) continue;   // self
+        if constexpr (SELF) {
+            int ent = S.pp[e];
+            if ((ent & 31) == 31 && (ent >> 5) == bucketLo + i) continue;   // self
+        }
         Real ex, ey, ez, me, he;
         if constexpr (sizeof(Real) == 4) {
             const float4 r = S.r0[e];
@@ -380,53 +392,64 @@ __device__ __forceinline__ void stage_cells(WalkSmem<Real, NBT> &S, const int *b
     }
 }
 
-// Newtonian cells, QEVAL at order <= 2 (qeval.h:53-64).
+// One Newtonian cell, QEVAL at order <= 2 (qeval.h:53-64): the cell's
+// acceleration and potential terms for the particle at (xi, yi, zi), with
+// its mass and g1 = 1/r^3 for the timestep criterion.
+template <typename Real, int NBT>
+__device__ __forceinline__ void newt_term(const WalkSmem<Real, NBT> &S, int e, Real xi, Real yi, Real zi,
+                                          int iOrder, Real &ax, Real &ay, Real &az, Real &pot,
+                                          Real &m, Real &g1) {
+    Real cx, cy, cz, xx, yy, zz, xy, xz, yz;
+    if constexpr (sizeof(Real) == 4) {
+        const float4 a = S.r0[e], b = S.r1[e], c = S.r2[e];
+        cx = a.x; cy = a.y; cz = a.z; m = a.w;
+        xx = b.x; yy = b.y; zz = b.z; xy = b.w; xz = c.x; yz = c.y;
+    } else {
+        cx = S.ex[e]; cy = S.ey[e]; cz = S.ez[e]; m = S.em[e];
+        xx = S.q[0][e]; yy = S.q[1][e]; zz = S.q[2][e];
+        xy = S.q[3][e]; xz = S.q[4][e]; yz = S.q[5][e];
+    }
+    Real dx = xi - cx, dy = yi - cy, dz = zi - cz;
+    Real d2 = dx * dx + dy * dy + dz * dz;
+    Real g0 = rsq<Real>(d2);
+    Real dir2 = g0 * g0;
+    g1 = g0 * dir2;
+    Real g2 = Real(3) * g1 * dir2;
+    Real g3 = Real(5) * g2 * dir2;
+    Real Qta = 0;
+    pot = 0; ax = 0; ay = 0; az = 0;
+    if (iOrder >= 2) {
+        Real Qmirx = xz * dz + xy * dy + xx * dx;
+        Real Qmiry = yz * dz + xy * dx + yy * dy;
+        Real Qmirz = yz * dy + xz * dx + zz * dz;
+        Real Qmir = Real(0.5) * (Qmirx * dx + Qmiry * dy + Qmirz * dz);
+        pot -= g2 * Qmir;
+        Qta += g3 * Qmir;
+        ax += g2 * Qmirx;
+        ay += g2 * Qmiry;
+        az += g2 * Qmirz;
+    }
+    pot -= g0 * m;
+    Qta += g1 * m;
+    ax -= dx * Qta;
+    ay -= dy * Qta;
+    az -= dz * Qta;
+}
+
+// Newtonian cells.  Far cells give O(1) terms that cancel to a small net
+// force in a periodic box: compensate each term, not only each tile.
 template <typename Real, int NBT>
 __device__ __forceinline__ void eval_newt(WalkSmem<Real, NBT> &S, int cnt, int i, int slot, int iOrder,
                                           Acc<Real> &A) {
-    Real xi = S.px[i], yi = S.py[i], zi = S.pz[i], mi = S.pm[i];
+    const Real xi = S.px[i], yi = S.py[i], zi = S.pz[i], mi = S.pm[i];
     for (int e = slot; e < cnt; e += 32 / NBT) {
-        Real cx, cy, cz, m, xx, yy, zz, xy, xz, yz;
-        if constexpr (sizeof(Real) == 4) {
-            const float4 a = S.r0[e], b = S.r1[e], c = S.r2[e];
-            cx = a.x; cy = a.y; cz = a.z; m = a.w;
-            xx = b.x; yy = b.y; zz = b.z; xy = b.w; xz = c.x; yz = c.y;
-        } else {
-            cx = S.ex[e]; cy = S.ey[e]; cz = S.ez[e]; m = S.em[e];
-            xx = S.q[0][e]; yy = S.q[1][e]; zz = S.q[2][e];
-            xy = S.q[3][e]; xz = S.q[4][e]; yz = S.q[5][e];
-        }
-        Real dx = xi - cx, dy = yi - cy, dz = zi - cz;
-        Real d2 = dx * dx + dy * dy + dz * dz;
-        Real g0 = rsq<Real>(d2);
-        Real dir2 = g0 * g0;
-        Real g1 = g0 * dir2;
-        Real g2 = Real(3) * g1 * dir2;
-        Real g3 = Real(5) * g2 * dir2;
-        Real Qta = 0, pot = 0, ax = 0, ay = 0, az = 0;
-        if (iOrder >= 2) {
-            Real Qmirx = xz * dz + xy * dy + xx * dx;
-            Real Qmiry = yz * dz + xy * dx + yy * dy;
-            Real Qmirz = yz * dy + xz * dx + zz * dz;
-            Real Qmir = Real(0.5) * (Qmirx * dx + Qmiry * dy + Qmirz * dz);
-            pot -= g2 * Qmir;
-            Qta += g3 * Qmir;
-            ax += g2 * Qmirx;
-            ay += g2 * Qmiry;
-            az += g2 * Qmirz;
-        }
-        pot -= g0 * m;
-        Qta += g1 * m;
-        ax -= dx * Qta;
-        ay -= dy * Qta;
-        az -= dz * Qta;
-        // far cells give O(1) terms that cancel to a small net force in a
-        // periodic box: compensate each term, not only each tile
+        Real ax, ay, az, pot, m, g1;
+        newt_term<Real, NBT>(S, e, xi, yi, zi, iOrder, ax, ay, az, pot, m, g1);
         kahan_add(A.s[0], A.c[0], ax);
         kahan_add(A.s[1], A.c[1], ay);
         kahan_add(A.s[2], A.c[2], az);
         A.t[3] += pot;
-        Real idt2 = (mi + m) * g1;
+        const Real idt2 = (mi + m) * g1;
         A.dt = idt2 > A.dt ? idt2 : A.dt;
     }
 }
@@ -476,104 +499,125 @@ __device__ __forceinline__ void flush_tile(Acc<Real> &A) {
     }
 }
 
+// Per-lane tallies of the opening tests, summed when the warp exits.
+struct WalkTally {
+    unsigned visit, tests, exact;
+};
+
+// A group walk leaves in its warp's scratch, for the bucket walks of the
+// group, the (cell, replica) entries every bucket must still test (U, from
+// the scratch's start) and the cells every bucket accepts as Newtonian
+// (NA, from GRP_LIST on); their sizes are in the warp's shared memory.
+// U and NA together seed a bucket walk's stack, so they stay well below
+// STK (the rest of it holds at most 32 entries per tree level)
+#define GRP_LIST 640
+#define GRP_SCRATCH (2 * GRP_LIST)
+
+#define GW_NONE 0
+#define GW_PUSH 1
+#define GW_U 2
+#define GW_NA 3
+
+// One bucket's walk and interactions.  With valid group lists the walk
+// starts from the group's U entries, and the NA cells enter the list of
+// Newtonian cells untested (they sit at the bottom of the stack as
+// -2 - entry); otherwise it starts from the root in every replica.  Either
+// way the lists are the reference's.
 template <typename Real, int NBT>
-__global__ void __launch_bounds__(WPB * 32) k_walk(WalkArgs W) {
-    extern __shared__ __align__(16) unsigned char smraw[];
-    const int lane = threadIdx.x & 31;
-    const int wib = threadIdx.x >> 5;
-    WalkSmem<Real, NBT> &S = reinterpret_cast<WalkSmem<Real, NBT> *>(smraw)[wib];
+__device__ __forceinline__ void walk_bucket(const WalkArgs &W, WalkSmem<Real, NBT> &S, int b,
+                                            const int *gl, WalkTally &K, int lane) {
     const TsphDevTree &T = W.T;
     const TsphDevParts &P = W.P;
     const unsigned FULL = 0xffffffffu;
     const float u32 = 5.9604645e-08f;   // 2^-24
     const float relF = 4.0f * u32;
 
-    unsigned long long cPP = 0, cN = 0, cS = 0, cExact = 0, cTests = 0, cBsq = 0, cIntra = 0, cAct = 0;
-    unsigned long long cVisit = 0;
-
-    for (;;) {
-        int b = 0;
-        if (lane == 0) b = atomicAdd(W.workCounter, 1);
-        b = __shfl_sync(FULL, b, 0);
-        if (b >= *W.nBuckets) break;
-        const int node = T.leaves[b];
-        const int lo = T.pLower[node];
-        const int n = T.pUpper[node] - lo + 1;
-        if (n > NBT) {
-            // a zero-extent leaf holding more than NBT coincident particles
-            if (lane == 0) atomicOr(&W.cnt->status, 1u << TSPH_ERR_UNSUPPORTED);
-            continue;
+    const int node = T.leaves[b];
+    const int lo = T.pLower[node];
+    const int n = T.pUpper[node] - lo + 1;
+    if (n > NBT) {
+        // a zero-extent leaf holding more than NBT coincident particles
+        if (lane == 0) atomicOr(&W.cnt->status, 1u << TSPH_ERR_UNSUPPORTED);
+        return;
+    }
+    // bucket geometry: FP32 records prepared once per bucket (k_bucket_prep)
+    float bch[3], bcl[3], fbmn[3], fbmx[3], bext, fSoftMaxF;
+    int nAct;
+    {
+        float4 r0 = T.brec[4 * b], r1 = T.brec[4 * b + 1];
+        float4 r2 = T.brec[4 * b + 2], r3 = T.brec[4 * b + 3];
+        bch[0] = r0.x; bch[1] = r0.y; bch[2] = r0.z; fSoftMaxF = r0.w;
+        bcl[0] = r1.x; bcl[1] = r1.y; bcl[2] = r1.z; bext = r1.w;
+        fbmn[0] = r2.x; fbmn[1] = r2.y; fbmn[2] = r2.z; nAct = (int)r2.w;
+        fbmx[0] = r3.x; fbmx[1] = r3.y; fbmx[2] = r3.z;
+    }
+    if (bext < 0.0f) {   // no active particle: not walked (pkd.c:2932)
+        if (lane == 0 && W.bucketLists) {
+            W.bucketLists[4 * b + 0] = node;
+            W.bucketLists[4 * b + 1] = W.bucketLists[4 * b + 2] = W.bucketLists[4 * b + 3] = -1;
         }
-        // bucket geometry: FP32 records prepared once per bucket (k_bucket_prep)
-        // for the FP32 path; the FP64 twin reads the FP64 bounds directly
-        float bch[3], bcl[3], fbmn[3], fbmx[3], bext, fSoftMaxF;
-        double bc64[3];
-        int nAct;
-        {
-            float4 r0 = T.brec[4 * b], r1 = T.brec[4 * b + 1];
-            float4 r2 = T.brec[4 * b + 2], r3 = T.brec[4 * b + 3];
-            bch[0] = r0.x; bch[1] = r0.y; bch[2] = r0.z; fSoftMaxF = r0.w;
-            bcl[0] = r1.x; bcl[1] = r1.y; bcl[2] = r1.z; bext = r1.w;
-            fbmn[0] = r2.x; fbmn[1] = r2.y; fbmn[2] = r2.z; nAct = (int)r2.w;
-            fbmx[0] = r3.x; fbmx[1] = r3.y; fbmx[2] = r3.z;
+        return;
+    }
+    // bucket particles
+    if (lane < NBT) {
+        int p = lo + (lane < n ? lane : 0);
+        if constexpr (sizeof(Real) == 4) {
+            float4 a = P.ph[p], c = P.pl[p];
+            S.px[lane] = ((a.x - bch[0]) + (c.x - bcl[0]));
+            S.py[lane] = ((a.y - bch[1]) + (c.y - bcl[1]));
+            S.pz[lane] = ((a.z - bch[2]) + (c.z - bcl[2]));
+            S.pm[lane] = a.w;
+            S.ph[lane] = c.w;
+        } else {
+            S.px[lane] = (Real)P.x[p];
+            S.py[lane] = (Real)P.y[p];
+            S.pz[lane] = (Real)P.z[p];
+            S.pm[lane] = (Real)P.m[p];
+            S.ph[lane] = (Real)P.h[p];
         }
-        if (bext < 0.0f) {   // no active particle: not walked (pkd.c:2932)
-            if (lane == 0 && W.bucketLists) {
-                W.bucketLists[4 * b + 0] = node;
-                W.bucketLists[4 * b + 1] = W.bucketLists[4 * b + 2] = W.bucketLists[4 * b + 3] = -1;
-            }
-            continue;
-        }
-        if constexpr (sizeof(Real) == 8) {
-#pragma unroll
-            for (int k = 0; k < 3; ++k) bc64[k] = 0.0;
-        }
-        // bucket particles
-        if (lane < NBT) {
-            int p = lo + (lane < n ? lane : 0);
-            if constexpr (sizeof(Real) == 4) {
-                float4 a = P.ph[p], c = P.pl[p];
-                S.px[lane] = ((a.x - bch[0]) + (c.x - bcl[0]));
-                S.py[lane] = ((a.y - bch[1]) + (c.y - bcl[1]));
-                S.pz[lane] = ((a.z - bch[2]) + (c.z - bcl[2]));
-                S.pm[lane] = a.w;
-                S.ph[lane] = c.w;
-            } else {
-                S.px[lane] = (Real)P.x[p];
-                S.py[lane] = (Real)P.y[p];
-                S.pz[lane] = (Real)P.z[p];
-                S.pm[lane] = (Real)P.m[p];
-                S.ph[lane] = (Real)P.h[p];
-            }
-        }
-        (void)bc64;
-        // initial stack: the root in every replica; P-P buffer: the bucket's
-        // own particles for the intra-bucket pairs (replica tag 31)
-        int sp = 0, ppn = 0, cnn = 0, csn = 0, nPart = 0, nNewt = 0, nSoft = 0;
+    }
+    // initial stack: the group's NA and U entries, or the root in every
+    // replica; P-P buffer: the bucket's own particles for the intra-bucket
+    // pairs (replica tag 31)
+    int sp = 0, ppn = 0, cnn = 0, csn = 0, nPart = 0, nNewt = 0, nSoft = 0;
+    if (gl) {
+        const int nU = S.gU, nNA = S.gNA;
+        for (int k = lane; k < nNA; k += 32) S.stack[k] = -2 - gl[GRP_LIST + k];
+        for (int k = lane; k < nU; k += 32) S.stack[nNA + k] = gl[k];
+        sp = nNA + nU;
+    } else {
         const int root = T.sysRoot[P.rid[lo]];   // the bucket's own system
         for (int r = lane; r < cW.nRep; r += 32) S.stack[r] = (root << 5) | r;
         sp = cW.nRep;
-        if (lane < n) S.pp[lane] = ((lo + lane) << 5) | 31;
-        ppn = n;
-        bool overflow = false;
-        // accumulators: lane = (particle i, slot)
-        const int i = lane % NBT, slot = lane / NBT;
-        Acc<Real> A;
+    }
+    if (lane < n) S.pp[lane] = ((lo + lane) << 5) | 31;
+    ppn = n;
+    bool ppSelf = true;   // the own particles sit in the first P-P tile
+    bool overflow = false;
+    // accumulators: lane = (particle i, slot)
+    const int i = lane % NBT, slot = lane / NBT;
+    Acc<Real> A;
 #pragma unroll
-        for (int k = 0; k < 4; ++k) { A.s[k] = 0; A.c[k] = 0; A.t[k] = 0; }
-        A.dt = 0;
-        __syncwarp();
+    for (int k = 0; k < 4; ++k) { A.s[k] = 0; A.c[k] = 0; A.t[k] = 0; }
+    A.dt = 0;
+    __syncwarp();
 
-        while (sp > 0) {
-            const int take = sp < 32 ? sp : 32;
-            int ent = lane < take ? S.stack[sp - take + lane] : -1;
-            __syncwarp();
-            sp -= take;
-            int act = ACT_NONE, cell = 0, rep = 0, up = -1, cnt = 0, plo = 0;
-            if (ent >= 0) {
-                ++cVisit;
-                cell = ent >> 5;
-                rep = ent & 31;
+    while (sp > 0) {
+        const int take = sp < 32 ? sp : 32;
+        int ent = lane < take ? S.stack[sp - take + lane] : -1;
+        __syncwarp();
+        sp -= take;
+        int act = ACT_NONE, cell = 0, rep = 0, up = -1, cnt = 0, plo = 0;
+        if (ent < -1) {   // a group NA cell
+            ent = -2 - ent;
+            cell = ent >> 5;
+            rep = ent & 31;
+            act = ACT_NEWT;
+        } else if (ent >= 0) {
+            cell = ent >> 5;
+            rep = ent & 31;
+            {
+                ++K.visit;
                 int4 lk = T.wlink[cell];
                 plo = lk.x;
                 cnt = lk.y;
@@ -596,15 +640,13 @@ __global__ void __launch_bounds__(WPB * 32) k_walk(WalkArgs W) {
                 if (cnt < 4) {
                     open = true;
                 } else {
-                    ++cTests;
+                    ++K.tests;
                     fo = filt(D2, M, ch.w, relF);
                     if (fo == 0) {
-                        ++cExact;
-                        {
-                            double o[3];
-                            rep_off64(rep, o);
-                            open = exact_decision(T, P, b, lo, n, cell, o, true) == 1;
-                        }
+                        ++K.exact;
+                        double o[3];
+                        rep_off64(rep, o);
+                        open = exact_decision(T, P, b, lo, n, cell, o, true) == 1;
                     } else {
                         open = fo < 0;
                     }
@@ -628,169 +670,349 @@ __global__ void __launch_bounds__(WPB * 32) k_walk(WalkArgs W) {
                         }
                     }
                     if (exactNeeded) {
-                        ++cExact;
-                        {
-                            double o[3];
-                            rep_off64(rep, o);
-                            newt = exact_decision(T, P, b, lo, n, cell, o, false) == 0;
-                        }
+                        ++K.exact;
+                        double o[3];
+                        rep_off64(rep, o);
+                        newt = exact_decision(T, P, b, lo, n, cell, o, false) == 0;
                     }
                     act = newt ? ACT_NEWT : ACT_SOFT;
                 }
             }
-            // children (upper first so the lower child is popped first)
-            unsigned bo = __ballot_sync(FULL, act == ACT_OPEN);
-            if (sp + 2 * __popc(bo) > STK) { overflow = true; break; }
-            if (act == ACT_OPEN) {
-                int pos = sp + 2 * __popc(bo & lane_lt());
-                S.stack[pos] = (up << 5) | rep;
-                S.stack[pos + 1] = ((cell + 1) << 5) | rep;
-            }
-            sp += 2 * __popc(bo);
-            // leaf particles
-            if (act == ACT_LEAF && cnt > NBT) {
-                atomicOr(&W.cnt->status, 1u << TSPH_ERR_UNSUPPORTED);
-                act = ACT_NONE;
-            }
-            int c0 = act == ACT_LEAF ? cnt : 0;
-            int incl = c0;
+        }
+        // children (upper first so the lower child is popped first)
+        unsigned bo = __ballot_sync(FULL, act == ACT_OPEN);
+        if (sp + 2 * __popc(bo) > STK) { overflow = true; break; }
+        if (act == ACT_OPEN) {
+            int pos = sp + 2 * __popc(bo & lane_lt());
+            S.stack[pos] = (up << 5) | rep;
+            S.stack[pos + 1] = ((cell + 1) << 5) | rep;
+        }
+        sp += 2 * __popc(bo);
+        // leaf particles
+        if (act == ACT_LEAF && cnt > NBT) {
+            atomicOr(&W.cnt->status, 1u << TSPH_ERR_UNSUPPORTED);
+            act = ACT_NONE;
+        }
+        int c0 = act == ACT_LEAF ? cnt : 0;
+        int incl = c0;
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                int y = __shfl_up_sync(FULL, incl, o);
-                if (lane >= o) incl += y;
-            }
-            int tot = __shfl_sync(FULL, incl, 31);
-            for (int k = 0; k < c0; ++k) S.pp[ppn + incl - c0 + k] = ((plo + k) << 5) | rep;
-            ppn += tot;
-            nPart += tot;
-            unsigned bn = __ballot_sync(FULL, act == ACT_NEWT);
-            if (act == ACT_NEWT) S.cn[cnn + __popc(bn & lane_lt())] = (cell << 5) | rep;
-            cnn += __popc(bn);
-            nNewt += __popc(bn);
-            unsigned bs = __ballot_sync(FULL, act == ACT_SOFT);
-            if (act == ACT_SOFT) S.cs[csn + __popc(bs & lane_lt())] = (cell << 5) | rep;
-            csn += __popc(bs);
-            nSoft += __popc(bs);
-            __syncwarp();
-            // evaluate full tiles
-            while (ppn >= PPF) {
-                stage_pp<Real, NBT>(S, P, PPF, lane, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
-                __syncwarp();
-                if (i < n) eval_pp<Real, NBT>(S, PPF, i, slot, lo + i, lo, A);
-                flush_tile(A);
-                __syncwarp();
-                for (int e = lane; e < ppn - PPF; e += 32) S.pp[e] = S.pp[PPF + e];
-                ppn -= PPF;
-                __syncwarp();
-            }
-            while (cnn >= CNF) {
-                stage_cells<Real, NBT>(S, S.cn, T, CNF, lane, false, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
-                __syncwarp();
-                if (i < n) eval_newt<Real, NBT>(S, CNF, i, slot, W.iOrder, A);
-                flush_tile(A);
-                __syncwarp();
-                for (int e = lane; e < cnn - CNF; e += 32) S.cn[e] = S.cn[CNF + e];
-                cnn -= CNF;
-                __syncwarp();
-            }
-            while (csn >= CNF) {
-                stage_cells<Real, NBT>(S, S.cs, T, CNF, lane, true, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
-                __syncwarp();
-                if (i < n) eval_soft<Real, NBT>(S, CNF, i, slot, A);
-                flush_tile(A);
-                __syncwarp();
-                for (int e = lane; e < csn - CNF; e += 32) S.cs[e] = S.cs[CNF + e];
-                csn -= CNF;
-                __syncwarp();
-            }
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o) incl += y;
         }
-        if (overflow) {
-            if (lane == 0) atomicOr(&W.cnt->status, 1u << TSPH_ERR_STACK_OVERFLOW);
+        int tot = __shfl_sync(FULL, incl, 31);
+        for (int k = 0; k < c0; ++k) S.pp[ppn + incl - c0 + k] = ((plo + k) << 5) | rep;
+        ppn += tot;
+        nPart += tot;
+        unsigned bn = __ballot_sync(FULL, act == ACT_NEWT);
+        if (act == ACT_NEWT) S.cn[cnn + __popc(bn & lane_lt())] = (cell << 5) | rep;
+        cnn += __popc(bn);
+        nNewt += __popc(bn);
+        unsigned bs = __ballot_sync(FULL, act == ACT_SOFT);
+        if (act == ACT_SOFT) S.cs[csn + __popc(bs & lane_lt())] = (cell << 5) | rep;
+        csn += __popc(bs);
+        nSoft += __popc(bs);
+        __syncwarp();
+        // evaluate full tiles
+        while (ppn >= PPF) {
+            stage_pp<Real, NBT>(S, P, PPF, lane, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
             __syncwarp();
-            continue;
-        }
-        // remaining partial tiles
-        if (ppn > 0) {
-            stage_pp<Real, NBT>(S, P, ppn, lane, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
-            __syncwarp();
-            if (i < n) eval_pp<Real, NBT>(S, ppn, i, slot, lo + i, lo, A);
+            if (i < n) {
+                if (ppSelf) eval_pp<Real, NBT, true>(S, PPF, i, slot, lo + i, lo, A);
+                else eval_pp<Real, NBT, false>(S, PPF, i, slot, lo + i, lo, A);
+            }
+            ppSelf = false;
             flush_tile(A);
             __syncwarp();
-        }
-        if (cnn > 0) {
-            stage_cells<Real, NBT>(S, S.cn, T, cnn, lane, false, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
+            for (int e = lane; e < ppn - PPF; e += 32) S.pp[e] = S.pp[PPF + e];
+            ppn -= PPF;
             __syncwarp();
-            if (i < n) eval_newt<Real, NBT>(S, cnn, i, slot, W.iOrder, A);
+        }
+        while (cnn >= CNF) {
+            stage_cells<Real, NBT>(S, S.cn, T, CNF, lane, false, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
+            __syncwarp();
+            if (i < n) eval_newt<Real, NBT>(S, CNF, i, slot, W.iOrder, A);
             flush_tile(A);
             __syncwarp();
-        }
-        if (csn > 0) {
-            stage_cells<Real, NBT>(S, S.cs, T, csn, lane, true, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
+            for (int e = lane; e < cnn - CNF; e += 32) S.cn[e] = S.cn[CNF + e];
+            cnn -= CNF;
             __syncwarp();
-            if (i < n) eval_soft<Real, NBT>(S, csn, i, slot, A);
+        }
+        while (csn >= CNF) {
+            stage_cells<Real, NBT>(S, S.cs, T, CNF, lane, true, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
+            __syncwarp();
+            if (i < n) eval_soft<Real, NBT>(S, CNF, i, slot, A);
             flush_tile(A);
             __syncwarp();
+            for (int e = lane; e < csn - CNF; e += 32) S.cs[e] = S.cs[CNF + e];
+            csn -= CNF;
+            __syncwarp();
         }
-        // reduce the 32 / NBT partial accumulators of each particle
-#pragma unroll
-        for (int o = NBT; o < 32; o <<= 1) {
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                Real s2 = __shfl_xor_sync(FULL, A.s[k], o);
-                Real c2 = __shfl_xor_sync(FULL, A.c[k], o);
-                two_sum_merge(A.s[k], A.c[k], s2, c2);
-            }
-            Real d2 = __shfl_xor_sync(FULL, A.dt, o);
-            A.dt = d2 > A.dt ? d2 : A.dt;
+    }
+    if (overflow) {
+        if (lane == 0) atomicOr(&W.cnt->status, 1u << TSPH_ERR_STACK_OVERFLOW);
+        __syncwarp();
+        return;
+    }
+    // remaining partial tiles
+    if (ppn > 0) {
+        stage_pp<Real, NBT>(S, P, ppn, lane, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
+        __syncwarp();
+        if (i < n) {
+            if (ppSelf) eval_pp<Real, NBT, true>(S, ppn, i, slot, lo + i, lo, A);
+            else eval_pp<Real, NBT, false>(S, ppn, i, slot, lo + i, lo, A);
         }
-        if (lane < n) {
-            int p = lo + lane;
-            if constexpr (sizeof(Real) == 4) {
-                P.wsum[p] = make_float4(A.s[0], A.s[1], A.s[2], A.s[3]);
-                P.wcmp[p] = make_float4(A.c[0], A.c[1], A.c[2], A.c[3]);
-                P.wdt[p] = A.dt;
-            } else {
-                P.ax[p] = (double)A.s[0];
-                P.ay[p] = (double)A.s[1];
-                P.az[p] = (double)A.s[2];
-                P.pot[p] = (double)A.s[3];
-                P.dtGrav[p] = (double)A.dt;
-            }
-        }
-        if (lane == 0) {
-            // pkdGravAll's sums over the active particles (pkd.c:2945-2950)
-            cAct += nAct;
-            cPP += (unsigned long long)nAct * nPart;
-            cN += (unsigned long long)nAct * nNewt;
-            cS += (unsigned long long)nAct * nSoft;
-            cBsq += (unsigned long long)nAct * n;
-            cIntra += (unsigned long long)nAct * (2 * (n - 1) - nAct + 1) / 2;
-            if (W.bucketLists) {
-                W.bucketLists[4 * b + 0] = node;
-                W.bucketLists[4 * b + 1] = nPart;
-                W.bucketLists[4 * b + 2] = nSoft;
-                W.bucketLists[4 * b + 3] = nNewt;
-            }
-        }
+        flush_tile(A);
         __syncwarp();
     }
-    // counters: tests per lane, the rest on lane 0
+    if (cnn > 0) {
+        stage_cells<Real, NBT>(S, S.cn, T, cnn, lane, false, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
+        __syncwarp();
+        if (i < n) eval_newt<Real, NBT>(S, cnn, i, slot, W.iOrder, A);
+        flush_tile(A);
+        __syncwarp();
+    }
+    if (csn > 0) {
+        stage_cells<Real, NBT>(S, S.cs, T, csn, lane, true, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
+        __syncwarp();
+        if (i < n) eval_soft<Real, NBT>(S, csn, i, slot, A);
+        flush_tile(A);
+        __syncwarp();
+    }
+    // reduce the 32 / NBT partial accumulators of each particle
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        cTests += __shfl_xor_sync(FULL, cTests, o);
-        cVisit += __shfl_xor_sync(FULL, cVisit, o);
-        cExact += __shfl_xor_sync(FULL, cExact, o);
+    for (int o = NBT; o < 32; o <<= 1) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            Real s2 = __shfl_xor_sync(FULL, A.s[k], o);
+            Real c2 = __shfl_xor_sync(FULL, A.c[k], o);
+            two_sum_merge(A.s[k], A.c[k], s2, c2);
+        }
+        Real d2 = __shfl_xor_sync(FULL, A.dt, o);
+        A.dt = d2 > A.dt ? d2 : A.dt;
+    }
+    if (lane < n) {
+        int p = lo + lane;
+        if constexpr (sizeof(Real) == 4) {
+            P.wsum[p] = make_float4(A.s[0], A.s[1], A.s[2], A.s[3]);
+            P.wcmp[p] = make_float4(A.c[0], A.c[1], A.c[2], A.c[3]);
+            P.wdt[p] = A.dt;
+        } else {
+            P.ax[p] = (double)A.s[0];
+            P.ay[p] = (double)A.s[1];
+            P.az[p] = (double)A.s[2];
+            P.pot[p] = (double)A.s[3];
+            P.dtGrav[p] = (double)A.dt;
+        }
     }
     if (lane == 0) {
-        atomicAdd(&W.cnt->nActive, cAct);
-        atomicAdd(&W.cnt->nPartPP, cPP);
-        atomicAdd(&W.cnt->nCellNewt, cN);
-        atomicAdd(&W.cnt->nCellSoft, cS);
-        atomicAdd(&W.cnt->nBucketSq, cBsq);
-        atomicAdd(&W.cnt->nIntra, cIntra);
-        atomicAdd(&W.cnt->nTests, cTests);
-        atomicAdd(&W.cnt->nVisits, cVisit);
-        atomicAdd(&W.cnt->nExactTests, cExact);
+        // pkdGravAll's sums over the active particles (pkd.c:2945-2950)
+        S.tAct += nAct;
+        S.tPP += (unsigned long long)nAct * nPart;
+        S.tNewt += (unsigned long long)nAct * nNewt;
+        S.tSoft += (unsigned long long)nAct * nSoft;
+        S.tBsq += (unsigned long long)nAct * n;
+        S.tIntra += (unsigned long long)nAct * (2 * (n - 1) - nAct + 1) / 2;
+        if (W.bucketLists) {
+            W.bucketLists[4 * b + 0] = node;
+            W.bucketLists[4 * b + 1] = nPart;
+            W.bucketLists[4 * b + 2] = nSoft;
+            W.bucketLists[4 * b + 3] = nNewt;
+        }
+    }
+    __syncwarp();
+}
+
+// The walk of a group of buckets (the subtree node g, buckets b0..b1-1),
+// made once with the group's box, which holds every bucket's box.  A cell
+// goes to NA when it is certainly not opened and certainly Newtonian for
+// any box inside the group's (its distance from the group box exceeds
+// sqrt(fOpen2), and (cellSoft + group max softening)^2 is below fOpen2 or
+// below that distance); an interior cell is opened here when the whole
+// group box lies within sqrt(fOpen2) of it (or it holds fewer than 4
+// particles); every other cell, leaves included, goes to U.
+// The FP32 tests carry the bucket walk's rounding bound, so every such
+// verdict is the one each bucket's FP64 test would reach.  Returns false
+// when a list or the stack overflows (the buckets then walk from the root).
+template <typename Real, int NBT>
+__device__ __noinline__ bool walk_group(const WalkArgs &W, WalkSmem<Real, NBT> &S, int g, int b0,
+                                        int b1, int *gl, WalkTally &K, int lane) {
+    const TsphDevTree &T = W.T;
+    const unsigned FULL = 0xffffffffu;
+    const float u32 = 5.9604645e-08f;   // 2^-24
+    const float relF = 4.0f * u32;
+    // group box (the node's bounds) about its centre in FP32, by one lane
+    float v[13];
+    if (lane == 0) {
+        float ext = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const double mn = T.bnd[6 * g + k], mx = T.bnd[6 * g + 3 + k];
+            const double c = 0.5 * (mn + mx);
+            split2f(c, v[k], v[3 + k]);
+            v[6 + k] = (float)(mn - c);
+            v[9 + k] = (float)(mx - c);
+            ext = fmaxf(ext, fmaxf(fabsf(v[6 + k]), fabsf(v[9 + k])));
+        }
+        v[12] = ext;
+    }
+#pragma unroll
+    for (int k = 0; k < 13; ++k) v[k] = __shfl_sync(FULL, v[k], 0);
+    const float gch[3] = {v[0], v[1], v[2]}, gcl[3] = {v[3], v[4], v[5]};
+    const float gmn[3] = {v[6], v[7], v[8]}, gmx[3] = {v[9], v[10], v[11]};
+    const float gext = v[12];
+    // largest softening of the group (each bucket's FP32 maximum)
+    float gsoft = 0.0f;
+    for (int b = b0 + lane; b < b1; b += 32) gsoft = fmaxf(gsoft, T.brec[4 * b].w);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) gsoft = fmaxf(gsoft, __shfl_xor_sync(FULL, gsoft, o));
+
+    int *gu = gl, *gna = gl + GRP_LIST;
+    const int root = T.sysRoot[W.P.rid[T.pLower[g]]];
+    for (int r = lane; r < cW.nRep; r += 32) S.stack[r] = (root << 5) | r;
+    int sp = cW.nRep, nU = 0, nNA = 0;
+    bool ok = true;
+    __syncwarp();
+    while (sp > 0) {
+        const int take = sp < 32 ? sp : 32;
+        const int ent = lane < take ? S.stack[sp - take + lane] : -1;
+        __syncwarp();
+        sp -= take;
+        int cls = GW_NONE, cell = 0, rep = 0, up = -1;
+        if (ent >= 0) {
+            ++K.visit;
+            cell = ent >> 5;
+            rep = ent & 31;
+            const int4 lk = T.wlink[cell];
+            const int cnt = lk.y;
+            up = lk.z;
+            const float4 ch = T.wcomh[cell], cl = T.wcoml[cell];
+            float ohx, ohy, ohz, olx, oly, olz;
+            rep_off32(rep, ohx, ohy, ohz, olx, oly, olz);
+            const float rx = ((ch.x - gch[0]) + ohx) + ((cl.x - gcl[0]) + olx);
+            const float ry = ((ch.y - gch[1]) + ohy) + ((cl.y - gcl[1]) + oly);
+            const float rz = ((ch.z - gch[2]) + ohz) + ((cl.z - gcl[2]) + olz);
+            // nearest and farthest point of the group box
+            const float dx = fmaxf(fmaxf(gmn[0] - rx, rx - gmx[0]), 0.0f);
+            const float dy = fmaxf(fmaxf(gmn[1] - ry, ry - gmx[1]), 0.0f);
+            const float dz = fmaxf(fmaxf(gmn[2] - rz, rz - gmx[2]), 0.0f);
+            const float fx = fmaxf(rx - gmn[0], gmx[0] - rx);
+            const float fy = fmaxf(ry - gmn[1], gmx[1] - ry);
+            const float fz = fmaxf(rz - gmn[2], gmx[2] - rz);
+            const float D2 = dx * dx + dy * dy + dz * dz;
+            const float F2 = fx * fx + fy * fy + fz * fz;
+            const float Sx = fmaxf(fmaxf(fabsf(rx), fabsf(ry)), fabsf(rz)) + gext + cW.offmax;
+            const float e = 6.0f * u32 * Sx + cW.E0;
+            const float M = 2.0f * e * (dx + dy + dz + 2.0f * e) + 3.0f * e * e + 4.0f * u32 * D2;
+            const float MF = 2.0f * e * (fx + fy + fz + 2.0f * e) + 3.0f * e * e + 4.0f * u32 * F2;
+            if (cnt < 4) {
+                cls = up >= 0 ? GW_PUSH : GW_U;
+            } else {
+                ++K.tests;
+                if (filt(F2, MF, ch.w, relF) < 0) {
+                    cls = up >= 0 ? GW_PUSH : GW_U;
+                } else if (filt(D2, M, ch.w, relF) > 0) {
+                    const float a32 = cl.w + gsoft;
+                    const float t2 = a32 * a32;
+                    const bool newt = filt(t2, 8.0f * u32 * t2, ch.w, relF) < 0 ||
+                                      filt(D2, M + 8.0f * u32 * t2, t2, relF) > 0;
+                    cls = newt ? GW_NA : GW_U;
+                } else {
+                    cls = GW_U;
+                }
+            }
+        }
+        const unsigned bo = __ballot_sync(FULL, cls == GW_PUSH);
+        const unsigned bu = __ballot_sync(FULL, cls == GW_U);
+        const unsigned bn = __ballot_sync(FULL, cls == GW_NA);
+        if (sp + 2 * __popc(bo) > STK || nU + nNA + __popc(bu) + __popc(bn) > GRP_LIST) {
+            ok = false;
+            break;
+        }
+        const unsigned lt = lane_lt();
+        if (cls == GW_PUSH) {
+            const int pos = sp + 2 * __popc(bo & lt);
+            S.stack[pos] = (up << 5) | rep;
+            S.stack[pos + 1] = ((cell + 1) << 5) | rep;
+        } else if (cls == GW_U) {
+            gu[nU + __popc(bu & lt)] = ent;
+        } else if (cls == GW_NA) {
+            gna[nNA + __popc(bn & lt)] = ent;
+        }
+        sp += 2 * __popc(bo);
+        nU += __popc(bu);
+        nNA += __popc(bn);
+        __syncwarp();
+    }
+    if (lane == 0) {
+        S.gU = nU;
+        S.gNA = nNA;
+    }
+    __syncwarp();   // the lists are read back by other lanes of this warp
+    return ok;
+}
+
+template <typename Real, int NBT>
+__global__ void __launch_bounds__(WPB * 32) k_walk(WalkArgs W) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    WalkSmem<Real, NBT> &S = reinterpret_cast<WalkSmem<Real, NBT> *>(smraw)[wib];
+    const unsigned FULL = 0xffffffffu;
+    WalkTally K = {0u, 0u, 0u};
+    if (lane == 0) S.tAct = S.tPP = S.tNewt = S.tSoft = S.tBsq = S.tIntra = 0ull;
+    __syncwarp();
+
+    for (;;) {
+        int u = 0;
+        if (lane == 0) u = atomicAdd(W.workCounter, 1);
+        u = __shfl_sync(FULL, u, 0);
+        if (W.groupFirst) {
+            if (u >= *W.nGroups) break;
+            const int b0 = W.groupFirst[u], b1 = W.groupFirst[u + 1];
+            // a group walk pays off once two of its buckets walk
+            int na = 0;
+            for (int b = b0 + lane; b < b1; b += 32) na += W.T.brec[4 * b + 1].w >= 0.0f;
+            na = __reduce_add_sync(FULL, na);
+            int *gl = W.groupScratch + (size_t)(blockIdx.x * WPB + wib) * GRP_SCRATCH;
+            bool grp = false;
+            if (na >= 2) {
+                // the group's node: the highest ancestor of its first bucket
+                // holding at most groupMax particles
+                int g = W.T.leaves[b0];
+                if (lane == 0)
+                    for (;;) {
+                        const int p = W.T.parent[g];
+                        if (p < 0 || W.T.pUpper[p] - W.T.pLower[p] + 1 > W.groupMax) break;
+                        g = p;
+                    }
+                g = __shfl_sync(FULL, g, 0);
+                grp = walk_group<Real, NBT>(W, S, g, b0, b1, gl, K, lane);
+            }
+            for (int b = b0; b < b1; ++b) walk_bucket<Real, NBT>(W, S, b, grp ? gl : nullptr, K, lane);
+        } else {
+            if (u >= *W.nBuckets) break;
+            walk_bucket<Real, NBT>(W, S, u, nullptr, K, lane);
+        }
+    }
+    // counters: tests and visits per lane, the rest from the warp's tallies
+    unsigned long long tests = K.tests, visit = K.visit, exact = K.exact;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        tests += __shfl_xor_sync(FULL, tests, o);
+        visit += __shfl_xor_sync(FULL, visit, o);
+        exact += __shfl_xor_sync(FULL, exact, o);
+    }
+    if (lane == 0) {
+        atomicAdd(&W.cnt->nActive, S.tAct);
+        atomicAdd(&W.cnt->nPartPP, S.tPP);
+        atomicAdd(&W.cnt->nCellNewt, S.tNewt);
+        atomicAdd(&W.cnt->nCellSoft, S.tSoft);
+        atomicAdd(&W.cnt->nBucketSq, S.tBsq);
+        atomicAdd(&W.cnt->nIntra, S.tIntra);
+        atomicAdd(&W.cnt->nTests, tests);
+        atomicAdd(&W.cnt->nVisits, visit);
+        atomicAdd(&W.cnt->nExactTests, exact);
     }
 }
 
@@ -861,6 +1083,83 @@ __global__ void k_finish_f32(int n, TsphDevParts P) {
 int tsph_walk_finish_f32(tsph_ctx *ctx) {
     k_finish_f32<<<tsph_blocks(ctx->n, 256), 256, 0, ctx->stream>>>(ctx->n, ctx->P);
     TSPH_LAUNCH_CK("k_finish_f32");
+    return TSPH_OK;
+}
+
+// Walk groups: the largest subtrees holding at most G particles.  Bucket b
+// starts a group when the group's node begins at the bucket's first
+// particle (the buckets of a subtree are consecutive in depth-first order).
+__global__ void k_group_mark(TsphDevTree T, int G, int cap, int *flag) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= cap) return;
+    int f = 0;
+    if (b < T.dcnt[1]) {
+        const int leaf = T.leaves[b];
+        int c = leaf;
+        for (;;) {
+            const int p = T.parent[c];
+            if (p < 0 || T.pUpper[p] - T.pLower[p] + 1 > G) break;
+            c = p;
+        }
+        f = T.pLower[c] == T.pLower[leaf];
+    }
+    flag[b] = f;
+}
+
+__global__ void k_group_list(TsphDevTree T, int cap, const int *flag, const int *scan, int *first,
+                             int *count) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= cap) return;
+    const int nb = T.dcnt[1];
+    if (b < nb && flag[b]) first[scan[b] - 1] = b;
+    if (b == (nb > 0 ? nb - 1 : 0)) {
+        const int ng = nb > 0 ? scan[nb - 1] : 0;
+        *count = ng;
+        first[ng] = nb;
+    }
+}
+
+// Group arrays and the per-warp list scratch; outside a capture they grow
+// to the particle count (a bound on the buckets of any later captured
+// step).  *on stays false when groups are off or (in a capture) not sized.
+// By default groups hold up to 128 particles, and are used when there are
+// at least 256 particles per walk warp: a group is one work unit, and with
+// fewer the last units leave most warps idle.
+static int prepare_groups(tsph_ctx *ctx, WalkArgs &A, int nbHost, int warps, bool *on) {
+    *on = false;
+    const int G = ctx->walkGroup == 0 ? 128 : ctx->walkGroup;
+    if (ctx->walkGroup == 0 && (long long)ctx->n < 256LL * warps) return TSPH_OK;
+    if (G <= 0 || nbHost <= 0) return TSPH_OK;
+    if (!ctx->capturing) {
+        const int cap = nbHost > ctx->n ? nbHost : ctx->n;
+        if (ctx->groupCap < cap) {
+            int rc = tsph_grow(ctx, &ctx->dGroupFlag, (size_t)cap);
+            if (!rc) rc = tsph_grow(ctx, &ctx->dGroupScan, (size_t)cap);
+            if (!rc) rc = tsph_grow(ctx, &ctx->dGroupFirst, (size_t)cap + 2);
+            if (!rc && !ctx->dGroupCount) rc = tsph_grow(ctx, &ctx->dGroupCount, 1);
+            if (rc) { ctx->groupCap = 0; return rc; }
+            ctx->groupCap = cap;
+        }
+        if (ctx->groupScratchWarps < warps) {
+            int rc = tsph_grow(ctx, &ctx->dGroupScratch, (size_t)warps * GRP_SCRATCH);
+            if (rc) { ctx->groupScratchWarps = 0; return rc; }
+            ctx->groupScratchWarps = warps;
+        }
+    }
+    if (ctx->groupCap < nbHost || ctx->groupScratchWarps < warps) return TSPH_OK;
+    k_group_mark<<<tsph_blocks(nbHost, 256), 256, 0, ctx->stream>>>(ctx->T, G, nbHost, ctx->dGroupFlag);
+    TSPH_LAUNCH_CK("k_group_mark");
+    int rc = tsph_scan_inclusive(ctx, ctx->dGroupFlag, ctx->dGroupScan, nbHost);
+    if (rc) return rc;
+    k_group_list<<<tsph_blocks(nbHost, 256), 256, 0, ctx->stream>>>(ctx->T, nbHost, ctx->dGroupFlag,
+                                                                     ctx->dGroupScan, ctx->dGroupFirst,
+                                                                     ctx->dGroupCount);
+    TSPH_LAUNCH_CK("k_group_list");
+    A.groupFirst = ctx->dGroupFirst;
+    A.nGroups = ctx->dGroupCount;
+    A.groupScratch = ctx->dGroupScratch;
+    A.groupMax = G;
+    *on = true;
     return TSPH_OK;
 }
 
@@ -935,6 +1234,13 @@ int tsph_walk_interact(tsph_ctx *ctx, const tsph_grav_params *gp) {
     k_bucket_prep<<<tsph_blocks(nbHost, 128), 128, 0, ctx->stream>>>(ctx->T, ctx->P);
     TSPH_LAUNCH_CK("k_bucket_prep");
     int blocks = ctx->smCount * (ctx->walkBlocksPerSM > 0 ? ctx->walkBlocksPerSM : 4);
+    A.groupFirst = nullptr;
+    A.nGroups = nullptr;
+    A.groupScratch = nullptr;
+    A.groupMax = 0;
+    bool groups = false;
+    rc = prepare_groups(ctx, A, nbHost, blocks * WPB, &groups);
+    if (rc) return rc;
     const int nbt = gp->nBucket <= 8 ? 8 : (gp->nBucket <= 16 ? 16 : 32);
     if (gp->precision == TSPH_FP32) {
         if (nbt == 8) rc = launch_walk<float, 8>(ctx, A, blocks, "k_walk<float,8>");

@@ -168,6 +168,13 @@ struct tsph_ctx {
     size_t subtreeSmem[4];       // ... for each dynamic shared memory size seen
     bool subtreeAttr;            // its shared-memory limit raised
     int walkBlocksPerSM;         // resident walk blocks per SM (0 = default)
+    int walkGroup;               // particles per walk group (0 = default, -1 = off)
+    int *dGroupFlag, *dGroupScan;  // per bucket: starts a group, and the inclusive scan
+    int *dGroupFirst;            // first bucket of every group, then the bucket count
+    int *dGroupCount;            // device: number of groups
+    int groupCap;                // buckets the group arrays hold
+    int *dGroupScratch;          // per walk warp: the lists its group walk leaves
+    int groupScratchWarps;
     bool capturing;              // inside a CUDA graph capture: no host reads
     double capLimit;             // |coordinate| bound of the captured step (0 = none)
     unsigned int *dStepStatus;   // device: status bits accumulated over a step

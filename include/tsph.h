@@ -404,14 +404,22 @@ typedef struct {
 int tsph_render_tsc(tsph_ctx *ctx, const tsph_render_params *rp, int nStar, float *rgb);
 
 /* --- tuning --------------------------------------------------------------
- * Launch-shape knobs of the CUDA path.  None changes a result: the tree,
- * the interaction lists and every force are identical for any setting
- * (no reference counterpart; the reference's equivalents are compile-time
- * constants and nBucket).  Zero selects the default. */
+ * Launch-shape knobs of the CUDA path (no reference counterpart; the
+ * reference's equivalents are compile-time constants and nBucket).  None
+ * changes the tree or an interaction list.  taskSize and walkBlocksPerSM
+ * change no result at all; walkGroup changes the order in which a
+ * particle's interactions are summed, so forces move by rounding only.
+ * Zero selects the default. */
 typedef struct {
     int taskSize;         /* largest tree node one CTA builds whole (>= 1024; default 3072) */
     int walkBlocksPerSM;  /* resident blocks per SM of the walk (default 4) */
-    int reserved[6];
+    int walkGroup;        /* particles per walk group, 32..4096; -1 = no groups; default
+                             128 when there are at least 256 particles per walk warp, else
+                             none.  The buckets of a group (the largest subtree with at
+                             most this many particles) share one walk for the cells that
+                             every bucket of it opens or accepts, and each bucket walks
+                             only the rest */
+    int reserved[5];
 } tsph_tuning;
 int tsph_set_tuning(tsph_ctx *ctx, const tsph_tuning *t);
 int tsph_get_tuning(tsph_ctx *ctx, tsph_tuning *t);

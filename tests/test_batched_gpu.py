@@ -40,28 +40,37 @@ def pair():
     b.close()
 
 
+@pytest.mark.parametrize("grp", [0, 64])
 @pytest.mark.parametrize("prec", [g.FP32, g.FP64])
-def test_batch_gravity_equals_each_system_alone(pair, prec):
+def test_batch_gravity_equals_each_system_alone(pair, prec, grp):
+    """Also with walk groups of 64 particles: a group never spans two
+    systems, so each system's groups are those it has alone."""
     c, c1 = pair
     systems, (pos, vel, m, soft, ngas, u, so, index) = _batch()
-    c.set_particles(pos, m, soft)
-    c.set_velocities(vel, ngas, u)
-    c.set_systems(so)
-    gp = g.grav_params(periodic=False, precision=prec)
-    out = c.grav_all(gp)
-    r = c.get_gravity()
-    part = cell = 0.0
-    for s, d in enumerate(systems):
-        c1.set_particles(d["pos"], d["mass"], d["soft"])
-        o1 = c1.grav_all(gp)
-        r1 = c1.get_gravity()
-        for k in ("acc", "pot", "dtGrav"):
-            assert np.array_equal(r[k][index[s]], r1[k]), (s, k)
-        part += o1["dPartSum"]
-        cell += o1["dCellSum"]
-    assert out["dPartSum"] == part
-    assert out["dCellSum"] == cell
-    assert out["nActive"] == len(m)
+    c.set_tuning(walkGroup=grp)
+    c1.set_tuning(walkGroup=grp)
+    try:
+        c.set_particles(pos, m, soft)
+        c.set_velocities(vel, ngas, u)
+        c.set_systems(so)
+        gp = g.grav_params(periodic=False, precision=prec)
+        out = c.grav_all(gp)
+        r = c.get_gravity()
+        part = cell = 0.0
+        for s, d in enumerate(systems):
+            c1.set_particles(d["pos"], d["mass"], d["soft"])
+            o1 = c1.grav_all(gp)
+            r1 = c1.get_gravity()
+            for k in ("acc", "pot", "dtGrav"):
+                assert np.array_equal(r[k][index[s]], r1[k]), (s, k)
+            part += o1["dPartSum"]
+            cell += o1["dCellSum"]
+        assert out["dPartSum"] == part
+        assert out["dCellSum"] == cell
+        assert out["nActive"] == len(m)
+    finally:
+        c.set_tuning()
+        c1.set_tuning()
 
 
 def test_batch_sph_equals_each_system_alone(pair):

@@ -215,6 +215,52 @@ def test_tuning_does_not_change_results():
         c.close()
 
 
+@pytest.mark.parametrize("case", ["plummer", "box"])
+def test_walk_groups_keep_every_list(case):
+    """Walk groups (one shared walk per subtree of at most walkGroup
+    particles; each bucket walks only what the group could not settle)
+    leave every interaction list as it is: the per-bucket list lengths and
+    pkdGravAll's counters equal those of plain bucket walks for groups of
+    32, 64 and 256 particles and the default, in FP64 and FP32.  The forces
+    move by summation order only: 1e-12 of scale in FP64, 1e-5 in FP32.
+    So does the potential, but in the periodic box its FP32 rounding is
+    that of the walk's part, some 30 times the total (which the Ewald part
+    nearly cancels): 3e-4 of the total's scale."""
+    if case == "plummer":
+        pos, vel, m = g.ics.plummer(32768, seed=3)
+        soft = np.full(len(m), 0.01)
+        periodic = False
+    else:
+        pos, vel, m = g.ics.lattice_box(24, seed=5)
+        soft = np.full(len(m), 1.0 / (50 * 24))
+        periodic = True
+    c = g.Context(0)
+    try:
+        for prec, tol, tolp in ((g.FP64, 1e-12, 1e-12), (g.FP32, 1e-5, 3e-4 if periodic else 1e-5)):
+            gp = g.grav_params(periodic=periodic, precision=prec)
+            ref = None
+            for grp in (-1, 32, 64, 256, 0):
+                c.set_tuning(walkGroup=grp)
+                c.set_particles(pos, m, soft)
+                out = c.grav_all(gp)
+                lists = c.get_lists()
+                r = c.get_gravity()
+                if ref is None:
+                    ref = (out, lists, r)
+                    continue
+                for k in ("nActive", "dPartSum", "dCellSum", "dSoftSum", "dFlop"):
+                    assert out[k] == ref[0][k], (prec, grp, k)
+                assert np.array_equal(lists, ref[1]), (prec, grp)
+                for k, t in (("acc", tol), ("pot", tolp)):
+                    s = np.abs(ref[2][k]).max()
+                    assert np.abs(r[k] - ref[2][k]).max() <= t * s, (prec, grp, k)
+                # fewer opening tests than the plain walk
+                if grp > 0:
+                    assert out["dVisits"] < ref[0]["dVisits"], (prec, grp)
+    finally:
+        c.close()
+
+
 def test_second_call_on_tree_order(ctx):
     """A second grav_all on the already tree-ordered particles (the state the
     reference keeps between steps) gives the same forces."""

@@ -26,17 +26,22 @@ def _scale_err(a, b):
     return np.max(np.abs(a - b)) / s if s > 0 else np.max(np.abs(a))
 
 
+@pytest.mark.parametrize("grp", [0, 32])
 @pytest.mark.parametrize("prec,tol", [(g.FP64, 1e-9), (g.FP32, 1e-4)])
-def test_active_gravity_vs_reference(ctx, prec, tol):
+def test_active_gravity_vs_reference(ctx, prec, tol, grp):
+    """Also with walk groups of 32 particles, whose shared walk uses the
+    group's whole box while each bucket walks with its active box."""
     d = load("ms_active_grav")
     act = d["rung"] >= int(d["iRung"])
     ctx.set_particles(d["pos"], d["mass"], d["soft"])
     ctx.set_rungs(d["rung"])
     ctx.set_active_rung(int(d["iRung"]))
+    ctx.set_tuning(walkGroup=grp)
     try:
         out = ctx.grav_all(g.grav_params(periodic=False, precision=prec))
     finally:
         ctx.set_active_rung(0)
+        ctx.set_tuning()
     r = ctx.get_gravity()
     e = rel_err(r["acc"][act], d["acc"][act])
     if prec == g.FP64:
