@@ -149,8 +149,8 @@ def run_ours(args, rank, world, local_rank):
     # seconds); the FP64 path runs on the same bucket size, i.e. the same tree
     from gasoline_gb300 import autotune
     tuned, _ = autotune.tune_gravity(ctx, g.grav_params(periodic=True, precision=g.FP32),
-                                     nbuckets=(NBUCKET,), walk_blocks=(3, 4),
-                                     task_sizes=(0, 3072))
+                                     nbuckets=(NBUCKET,), walk_blocks=(4, 5),
+                                     task_sizes=(0, 3072), walk_groups=(0, -1))
     gp32 = g.grav_params(periodic=True, precision=g.FP32, nBucket=tuned["nBucket"])
     gp64 = g.grav_params(periodic=True, precision=g.FP64, nBucket=tuned["nBucket"])
 

@@ -1,16 +1,20 @@
 """Launch-shape autotuner of the gravity path.
 
 The walk's bucket size (the reference's nBucket, 8/16/32 particles handled
-by one warp), the resident walk blocks per SM and the tree builder's task
-size (the largest node one CTA builds whole) are chosen by timing real
-gravity evaluations of the caller's own particles on the device:
+by one warp), the resident walk blocks per SM, the tree builder's task
+size (the largest node one CTA builds whole) and the walk group size
+(0 = the default of 128 particles, -1 = no groups) are chosen by timing
+real gravity evaluations of the caller's own particles on the device:
 
     best, table = tune_gravity(ctx, grav_params(...))
 
-Only nBucket changes results (it is a physics parameter of the reference:
-a different bucket size is a different tree); the other two knobs are
-result-neutral, which the tests check bit for bit.  The context is left
-with the best knobs set.
+Only nBucket changes the tree and the interaction lists (it is a physics
+parameter of the reference: a different bucket size is a different tree).
+The block count and the task size are result-neutral, which the tests
+check bit for bit; the group size changes only the order in which each
+particle's terms are summed.  Groups pay off on clustered systems (fewer
+opening tests per bucket) and not on near-uniform periodic boxes, which is
+why they are tuned.  The context is left with the best knobs set.
 """
 import itertools
 
@@ -26,18 +30,20 @@ def _time_grav(ctx, gp, reps):
     return best
 
 
-def tune_gravity(ctx, gp, nbuckets=(8, 16, 32), walk_blocks=(2, 4, 6), task_sizes=(0, 65536),
-                 reps=2):
-    """Time every (nBucket, walkBlocksPerSM, taskSize) on the context's
-    current particles; returns (best, table) where best holds the winning
-    knobs and its time in ms, and table every measurement."""
+def tune_gravity(ctx, gp, nbuckets=(8, 16, 32), walk_blocks=(4, 5), task_sizes=(0, 65536),
+                 walk_groups=(0, -1), reps=2):
+    """Time every (nBucket, walkBlocksPerSM, taskSize, walkGroup) on the
+    context's current particles; returns (best, table) where best holds the
+    winning knobs and its time in ms, and table every measurement."""
     table = []
-    for nb, wb, ts in itertools.product(nbuckets, walk_blocks, task_sizes):
-        ctx.set_tuning(taskSize=ts, walkBlocksPerSM=wb)
+    for nb, wb, ts, wg in itertools.product(nbuckets, walk_blocks, task_sizes, walk_groups):
+        ctx.set_tuning(taskSize=ts, walkBlocksPerSM=wb, walkGroup=wg)
         g = GravParams.from_buffer_copy(gp)
         g.nBucket = nb
         ms = _time_grav(ctx, g, reps)
-        table.append({"nBucket": nb, "walkBlocksPerSM": wb, "taskSize": ts, "ms": ms})
+        table.append({"nBucket": nb, "walkBlocksPerSM": wb, "taskSize": ts, "walkGroup": wg,
+                      "ms": ms})
     best = min(table, key=lambda r: r["ms"])
-    ctx.set_tuning(taskSize=best["taskSize"], walkBlocksPerSM=best["walkBlocksPerSM"])
+    ctx.set_tuning(taskSize=best["taskSize"], walkBlocksPerSM=best["walkBlocksPerSM"],
+                   walkGroup=best["walkGroup"])
     return dict(best), table

@@ -32,7 +32,8 @@
 // NBT (template): largest bucket one warp handles, 8, 16 or 32; lanes are
 // (bucket particle, entry slot) pairs with 32 / NBT slots per particle.
 #define WPB 4                   // warps per block
-#define STK 1536                // walk stack entries per warp (~32 x tree depth)
+#define STK 768                 // walk stack entries per warp (a batch-of-32 descent
+                                // holds ~100 at most on clustered 4M-particle trees)
 #define PPF 128                 // P-P tile size
 #define CNF 64                  // cell tile size
 #define CNB (CNF + 32)
@@ -507,22 +508,21 @@ struct WalkTally {
 // A group walk leaves in its warp's scratch, for the bucket walks of the
 // group, the (cell, replica) entries every bucket must still test (U, from
 // the scratch's start) and the cells every bucket accepts as Newtonian
-// (NA, from GRP_LIST on); their sizes are in the warp's shared memory.
-// U and NA together seed a bucket walk's stack, so they stay well below
-// STK (the rest of it holds at most 32 entries per tree level)
-#define GRP_LIST 640
-#define GRP_SCRATCH (2 * GRP_LIST)
+// (NA, from GRP_U on); their sizes are in the warp's shared memory.  U
+// seeds a bucket walk's stack, so it stays well below STK.
+#define GRP_U 384
+#define GRP_NA 1024
+#define GRP_SCRATCH (GRP_U + GRP_NA)
 
 #define GW_NONE 0
 #define GW_PUSH 1
 #define GW_U 2
 #define GW_NA 3
 
-// One bucket's walk and interactions.  With valid group lists the walk
-// starts from the group's U entries, and the NA cells enter the list of
-// Newtonian cells untested (they sit at the bottom of the stack as
-// -2 - entry); otherwise it starts from the root in every replica.  Either
-// way the lists are the reference's.
+// One bucket's walk and interactions.  With valid group lists the group's
+// NA cells are evaluated first, as Newtonian cells, and the walk starts
+// from the group's U entries; otherwise it starts from the root in every
+// replica.  Either way the lists are the reference's.
 template <typename Real, int NBT>
 __device__ __forceinline__ void walk_bucket(const WalkArgs &W, WalkSmem<Real, NBT> &S, int b,
                                             const int *gl, WalkTally &K, int lane) {
@@ -576,15 +576,32 @@ __device__ __forceinline__ void walk_bucket(const WalkArgs &W, WalkSmem<Real, NB
             S.ph[lane] = (Real)P.h[p];
         }
     }
-    // initial stack: the group's NA and U entries, or the root in every
-    // replica; P-P buffer: the bucket's own particles for the intra-bucket
-    // pairs (replica tag 31)
+    // accumulators: lane = (particle i, slot)
+    const int i = lane % NBT, slot = lane / NBT;
+    Acc<Real> A;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) { A.s[k] = 0; A.c[k] = 0; A.t[k] = 0; }
+    A.dt = 0;
+    // initial stack: the group's U entries (after its NA cells, evaluated
+    // here tile by tile), or the root in every replica; P-P buffer: the
+    // bucket's own particles for the intra-bucket pairs (replica tag 31)
     int sp = 0, ppn = 0, cnn = 0, csn = 0, nPart = 0, nNewt = 0, nSoft = 0;
     if (gl) {
         const int nU = S.gU, nNA = S.gNA;
-        for (int k = lane; k < nNA; k += 32) S.stack[k] = -2 - gl[GRP_LIST + k];
-        for (int k = lane; k < nU; k += 32) S.stack[nNA + k] = gl[k];
-        sp = nNA + nU;
+        __syncwarp();
+        for (int k0 = 0; k0 < nNA; k0 += CNF) {
+            const int c = nNA - k0 < CNF ? nNA - k0 : CNF;
+            for (int e = lane; e < c; e += 32) S.cn[e] = gl[GRP_U + k0 + e];
+            __syncwarp();
+            stage_cells<Real, NBT>(S, S.cn, T, c, lane, false, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
+            __syncwarp();
+            if (i < n) eval_newt<Real, NBT>(S, c, i, slot, W.iOrder, A);
+            flush_tile(A);
+            __syncwarp();
+        }
+        nNewt = nNA;
+        for (int k = lane; k < nU; k += 32) S.stack[k] = gl[k];
+        sp = nU;
     } else {
         const int root = T.sysRoot[P.rid[lo]];   // the bucket's own system
         for (int r = lane; r < cW.nRep; r += 32) S.stack[r] = (root << 5) | r;
@@ -594,12 +611,6 @@ __device__ __forceinline__ void walk_bucket(const WalkArgs &W, WalkSmem<Real, NB
     ppn = n;
     bool ppSelf = true;   // the own particles sit in the first P-P tile
     bool overflow = false;
-    // accumulators: lane = (particle i, slot)
-    const int i = lane % NBT, slot = lane / NBT;
-    Acc<Real> A;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) { A.s[k] = 0; A.c[k] = 0; A.t[k] = 0; }
-    A.dt = 0;
     __syncwarp();
 
     while (sp > 0) {
@@ -608,12 +619,7 @@ __device__ __forceinline__ void walk_bucket(const WalkArgs &W, WalkSmem<Real, NB
         __syncwarp();
         sp -= take;
         int act = ACT_NONE, cell = 0, rep = 0, up = -1, cnt = 0, plo = 0;
-        if (ent < -1) {   // a group NA cell
-            ent = -2 - ent;
-            cell = ent >> 5;
-            rep = ent & 31;
-            act = ACT_NEWT;
-        } else if (ent >= 0) {
+        if (ent >= 0) {
             cell = ent >> 5;
             rep = ent & 31;
             {
@@ -867,7 +873,7 @@ __device__ __noinline__ bool walk_group(const WalkArgs &W, WalkSmem<Real, NBT> &
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) gsoft = fmaxf(gsoft, __shfl_xor_sync(FULL, gsoft, o));
 
-    int *gu = gl, *gna = gl + GRP_LIST;
+    int *gu = gl, *gna = gl + GRP_U;
     const int root = T.sysRoot[W.P.rid[T.pLower[g]]];
     for (int r = lane; r < cW.nRep; r += 32) S.stack[r] = (root << 5) | r;
     int sp = cW.nRep, nU = 0, nNA = 0;
@@ -925,7 +931,7 @@ __device__ __noinline__ bool walk_group(const WalkArgs &W, WalkSmem<Real, NBT> &
         const unsigned bo = __ballot_sync(FULL, cls == GW_PUSH);
         const unsigned bu = __ballot_sync(FULL, cls == GW_U);
         const unsigned bn = __ballot_sync(FULL, cls == GW_NA);
-        if (sp + 2 * __popc(bo) > STK || nU + nNA + __popc(bu) + __popc(bn) > GRP_LIST) {
+        if (sp + 2 * __popc(bo) > STK || nU + __popc(bu) > GRP_U || nNA + __popc(bn) > GRP_NA) {
             ok = false;
             break;
         }
@@ -952,8 +958,10 @@ __device__ __noinline__ bool walk_group(const WalkArgs &W, WalkSmem<Real, NBT> &
     return ok;
 }
 
+// FP32: five resident blocks per SM (96 registers, 44 KB of shared memory
+// per block); FP64: limited by its larger tiles.
 template <typename Real, int NBT>
-__global__ void __launch_bounds__(WPB * 32) k_walk(WalkArgs W) {
+__global__ void __launch_bounds__(WPB * 32, sizeof(Real) == 4 ? 5 : 1) k_walk(WalkArgs W) {
     extern __shared__ __align__(16) unsigned char smraw[];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
@@ -1233,7 +1241,8 @@ int tsph_walk_interact(tsph_ctx *ctx, const tsph_grav_params *gp) {
     TSPH_CK(cudaMemsetAsync(A.workCounter, 0, sizeof(int), ctx->stream));
     k_bucket_prep<<<tsph_blocks(nbHost, 128), 128, 0, ctx->stream>>>(ctx->T, ctx->P);
     TSPH_LAUNCH_CK("k_bucket_prep");
-    int blocks = ctx->smCount * (ctx->walkBlocksPerSM > 0 ? ctx->walkBlocksPerSM : 4);
+    const int wbDefault = gp->precision == TSPH_FP32 ? 5 : 4;
+    int blocks = ctx->smCount * (ctx->walkBlocksPerSM > 0 ? ctx->walkBlocksPerSM : wbDefault);
     A.groupFirst = nullptr;
     A.nGroups = nullptr;
     A.groupScratch = nullptr;

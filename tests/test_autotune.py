@@ -9,21 +9,24 @@ class FakeCtx:
         self.tuning = None
         self.last = None
 
-    def set_tuning(self, taskSize=0, walkBlocksPerSM=0):
-        self.tuning = (taskSize, walkBlocksPerSM)
+    def set_tuning(self, taskSize=0, walkBlocksPerSM=0, walkGroup=0):
+        self.tuning = (taskSize, walkBlocksPerSM, walkGroup)
 
     def grav_all(self, gp):
         self.last = gp.nBucket
 
     def timings(self):
-        ts, wb = self.tuning
-        # a made-up cost surface with its minimum at nBucket 16, 4 blocks, task 65536
-        return {"total": abs(self.last - 16) + abs(wb - 4) + (0 if ts == 65536 else 1) + 1.0}
+        ts, wb, wg = self.tuning
+        # a made-up cost surface with its minimum at nBucket 16, 4 blocks,
+        # task 65536, no walk groups
+        return {"total": abs(self.last - 16) + abs(wb - 4) + (0 if ts == 65536 else 1)
+                + (0 if wg == -1 else 0.5) + 1.0}
 
 
 def test_tune_gravity_picks_the_minimum_and_leaves_it_set():
     c = FakeCtx()
     best, table = autotune.tune_gravity(c, g.grav_params(nBucket=8), reps=1)
-    assert len(table) == 3 * 3 * 2
-    assert (best["nBucket"], best["walkBlocksPerSM"], best["taskSize"]) == (16, 4, 65536)
-    assert c.tuning == (65536, 4)
+    assert len(table) == 3 * 2 * 2 * 2
+    assert (best["nBucket"], best["walkBlocksPerSM"], best["taskSize"], best["walkGroup"]) == \
+        (16, 4, 65536, -1)
+    assert c.tuning == (65536, 4, -1)
