@@ -344,6 +344,9 @@ def run_profile(args):
     import gasoline_gb300 as g
     stream = torch.cuda.Stream()
     ctx = g.Context(0, stream=stream.cuda_stream)
+    # the knobs the timed run's autotuner picks for this box: the default
+    # five walk blocks per SM, no walk groups
+    ctx.set_tuning(walkGroup=-1)
     pos, m, soft = workload(args.ng)
     ctx.set_particles(pos, m, soft)
     gp = g.grav_params(periodic=True, precision=g.FP32, nBucket=NBUCKET)

@@ -39,8 +39,9 @@ struct EwConst {
     // FP32 copies of the k-space table for the FP32 kernel
     float hxf[EW_MAXH], hyf[EW_MAXH], hzf[EW_MAXH], hCf[EW_MAXH], hSf[EW_MAXH];
     // the real-space images (ix, iy, iz, hole) that can pass the cut for
-    // some particle of the box, in the reference's loop order
-    int nImg;
+    // some particle of the box: the nHole images of the replica "hole"
+    // first, then the others, each in the reference's loop order
+    int nImg, nHole;
     char4 img[EW_MAXIMG];
     // FP32 MEVAL coefficients: the moments pre-combined per monomial
     // (c4: hexadecapole mirror over dx^3 .. dz^3, c3: octopole mirror over
@@ -301,6 +302,81 @@ __device__ __forceinline__ void kadd(float &s, float &c, float v) {
 }
 __device__ __forceinline__ void kadd(double &s, double &c, double v) { s += v; (void)c; }
 
+// gam_0..5 of one real-space image at squared distance r2 (the g_n of
+// pkdBucketEwald, ewald.c:85-125): images of the replica "hole" carry
+// -erf(alpha r), the others erfc(alpha r).
+template <typename Real, bool HOLE>
+__device__ __forceinline__ void ewald_gam(Real r2, Real alpha, Real alpha2, Real ka, Real smallR2,
+                                          Real *gam) {
+    if (sizeof(Real) == 4 && HOLE && r2 * alpha2 < Real(4.0)) {
+        // FP32: the recurrence below cancels catastrophically for a
+        // hole image at small alpha*r.  With u = alpha^2 r^2,
+        //   gam_n = -ka (2 alpha^2)^n S_n(u),
+        //   S_n(u) = sum_j (-u)^j/(j!(2j+2n+1)) = int_0^1 t^2n e^(-u t^2) dt
+        //          = e^-u T_n(u),  T_n = sum_j (2u)^j / prod_{i<=j}(2n+2i+1),
+        // a series of positive terms; T_5 is summed directly and the
+        // stable downward recurrence T_n = (2u T_{n+1} + 1)/(2n+1)
+        // gives the rest (max rel. error ~2e-7 for u < 4).
+        // The reference's small-r branch is the first two terms of S_n.
+        Real u = r2 * alpha2, tu = 2 * u;
+        Real t = Real(1.0 / 11.0), T5 = t;
+#pragma unroll
+        for (int j = 1; j < 14; ++j) {
+            t *= tu * Real(1.0 / (11 + 2 * j));   // constant reciprocals: no divisions
+            T5 += t;
+        }
+        Real T[6];
+        T[5] = T5;
+#pragma unroll
+        for (int q = 4; q >= 0; --q) T[q] = (tu * T[q + 1] + 1) * Real(1.0 / (2 * q + 1));
+        Real pre = -ka * exp_r(-u);
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            gam[q] = pre * T[q];
+            pre *= 2 * alpha2;
+        }
+    } else if (r2 < smallR2) {
+        Real alphan = ka;
+        Real s = r2 * alpha2;
+        gam[0] = alphan * (s / 3 - 1);
+        alphan *= 2 * alpha2;
+        gam[1] = alphan * (s / 5 - Real(1.0 / 3.0));
+        alphan *= 2 * alpha2;
+        gam[2] = alphan * (s / 7 - Real(1.0 / 5.0));
+        alphan *= 2 * alpha2;
+        gam[3] = alphan * (s / 9 - Real(1.0 / 7.0));
+        alphan *= 2 * alpha2;
+        gam[4] = alphan * (s / 11 - Real(1.0 / 9.0));
+        alphan *= 2 * alpha2;
+        gam[5] = alphan * (s / 13 - Real(1.0 / 11.0));
+    } else {
+        Real r, dir;
+        if constexpr (sizeof(Real) == 4) {
+            // FP32: 1/r from the hardware reciprocal square root (a few ulp,
+            // far inside the FP32 path's error)
+            dir = rsqrtf(r2);
+            r = r2 * dir;
+        } else {
+            r = sqrt_r(r2);
+            dir = Real(1) / r;
+        }
+        Real dir2 = dir * dir;
+        Real a = exp_r(-r2 * alpha2);
+        a *= ka * dir2;
+        gam[0] = HOLE ? -erf_r(alpha * r) : erfc_r(alpha * r);
+        gam[0] *= dir;
+        gam[1] = gam[0] * dir2 + a;
+        Real alphan = 2 * alpha2;
+        gam[2] = 3 * gam[1] * dir2 + alphan * a;
+        alphan *= 2 * alpha2;
+        gam[3] = 5 * gam[2] * dir2 + alphan * a;
+        alphan *= 2 * alpha2;
+        gam[4] = 7 * gam[3] * dir2 + alphan * a;
+        alphan *= 2 * alpha2;
+        gam[5] = 9 * gam[4] * dir2 + alphan * a;
+    }
+}
+
 template <typename Real>
 __global__ void __launch_bounds__(128) k_ewald(TsphDevParts P, TsphDevCounters *cnt) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -317,84 +393,37 @@ __global__ void __launch_bounds__(128) k_ewald(TsphDevParts P, TsphDevCounters *
         Real dx = (Real)(P.x[p] - cE.mom.x);
         Real dy = (Real)(P.y[p] - cE.mom.y);
         Real dz = (Real)(P.z[p] - cE.mom.z);
-        for (int q = 0; q < cE.nImg; ++q) {
-            {
-                {
-                    const char4 im = cE.img[q];
-                    const bool hole = im.w != 0;
-                    Real dxo = dx + im.x * L, dyo = dy + im.y * L, dzo = dz + im.z * L;
-                    Real r2 = dxo * dxo + dyo * dyo + dzo * dzo;
-                    if (r2 > fEwCut2 && !hole) continue;
-                    Real gam[6];
-                    if (sizeof(Real) == 4 && hole && r2 * alpha2 < Real(4.0)) {
-                        // FP32: the recurrence below cancels catastrophically for a
-                        // hole image at small alpha*r.  With u = alpha^2 r^2,
-                        //   gam_n = -ka (2 alpha^2)^n S_n(u),
-                        //   S_n(u) = sum_j (-u)^j/(j!(2j+2n+1)) = int_0^1 t^2n e^(-u t^2) dt
-                        //          = e^-u T_n(u),  T_n = sum_j (2u)^j / prod_{i<=j}(2n+2i+1),
-                        // a series of positive terms; T_5 is summed directly and the
-                        // stable downward recurrence T_n = (2u T_{n+1} + 1)/(2n+1)
-                        // gives the rest (max rel. error ~2e-7 for u < 4).
-                        // The reference's small-r branch is the first two terms of S_n.
-                        Real u = r2 * alpha2, tu = 2 * u;
-                        Real t = Real(1.0 / 11.0), T5 = t;
-#pragma unroll
-                        for (int j = 1; j < 14; ++j) {
-                            t *= tu / Real(11 + 2 * j);
-                            T5 += t;
-                        }
-                        Real T[6];
-                        T[5] = T5;
-#pragma unroll
-                        for (int q = 4; q >= 0; --q) T[q] = (tu * T[q + 1] + 1) / Real(2 * q + 1);
-                        Real pre = -ka * exp_r(-u);
-#pragma unroll
-                        for (int q = 0; q < 6; ++q) {
-                            gam[q] = pre * T[q];
-                            pre *= 2 * alpha2;
-                        }
-                    } else if (r2 < smallR2) {
-                        Real alphan = ka;
-                        Real s = r2 * alpha2;
-                        gam[0] = alphan * (s / 3 - 1);
-                        alphan *= 2 * alpha2;
-                        gam[1] = alphan * (s / 5 - Real(1.0 / 3.0));
-                        alphan *= 2 * alpha2;
-                        gam[2] = alphan * (s / 7 - Real(1.0 / 5.0));
-                        alphan *= 2 * alpha2;
-                        gam[3] = alphan * (s / 9 - Real(1.0 / 7.0));
-                        alphan *= 2 * alpha2;
-                        gam[4] = alphan * (s / 11 - Real(1.0 / 9.0));
-                        alphan *= 2 * alpha2;
-                        gam[5] = alphan * (s / 13 - Real(1.0 / 11.0));
-                    } else {
-                        Real r = sqrt_r(r2);
-                        Real dir = Real(1) / r;
-                        Real dir2 = dir * dir;
-                        Real a = exp_r(-r2 * alpha2);
-                        a *= ka * dir2;
-                        gam[0] = hole ? -erf_r(alpha * r) : erfc_r(alpha * r);
-                        gam[0] *= dir;
-                        gam[1] = gam[0] * dir2 + a;
-                        Real alphan = 2 * alpha2;
-                        gam[2] = 3 * gam[1] * dir2 + alphan * a;
-                        alphan *= 2 * alpha2;
-                        gam[3] = 5 * gam[2] * dir2 + alphan * a;
-                        alphan *= 2 * alpha2;
-                        gam[4] = 7 * gam[3] * dir2 + alphan * a;
-                        alphan *= 2 * alpha2;
-                        gam[5] = 9 * gam[4] * dir2 + alphan * a;
-                    }
-                    Real tx = 0, ty = 0, tz = 0, tp = 0;
-                    if constexpr (sizeof(Real) == 4) meval_f32(iOrder, gam, dxo, dyo, dzo, tx, ty, tz, tp);
-                    else meval<Real>(iOrder, mom, gam, dxo, dyo, dzo, tx, ty, tz, tp);
-                    kadd(ax, cax, tx);
-                    kadd(ay, cay, ty);
-                    kadd(az, caz, tz);
-                    kadd(fPot, cpot, tp);
-                    ++nLoop;
-                }
-            }
+        // the hole images (always kept), then the others within the cut
+        for (int q = 0; q < cE.nHole; ++q) {
+            const char4 im = cE.img[q];
+            const Real dxo = dx + im.x * L, dyo = dy + im.y * L, dzo = dz + im.z * L;
+            const Real r2 = dxo * dxo + dyo * dyo + dzo * dzo;
+            Real gam[6];
+            ewald_gam<Real, true>(r2, alpha, alpha2, ka, smallR2, gam);
+            Real tx = 0, ty = 0, tz = 0, tp = 0;
+            if constexpr (sizeof(Real) == 4) meval_f32(iOrder, gam, dxo, dyo, dzo, tx, ty, tz, tp);
+            else meval<Real>(iOrder, mom, gam, dxo, dyo, dzo, tx, ty, tz, tp);
+            kadd(ax, cax, tx);
+            kadd(ay, cay, ty);
+            kadd(az, caz, tz);
+            kadd(fPot, cpot, tp);
+            ++nLoop;
+        }
+        for (int q = cE.nHole; q < cE.nImg; ++q) {
+            const char4 im = cE.img[q];
+            const Real dxo = dx + im.x * L, dyo = dy + im.y * L, dzo = dz + im.z * L;
+            const Real r2 = dxo * dxo + dyo * dyo + dzo * dzo;
+            if (r2 > fEwCut2) continue;
+            Real gam[6];
+            ewald_gam<Real, false>(r2, alpha, alpha2, ka, smallR2, gam);
+            Real tx = 0, ty = 0, tz = 0, tp = 0;
+            if constexpr (sizeof(Real) == 4) meval_f32(iOrder, gam, dxo, dyo, dzo, tx, ty, tz, tp);
+            else meval<Real>(iOrder, mom, gam, dxo, dyo, dzo, tx, ty, tz, tp);
+            kadd(ax, cax, tx);
+            kadd(ay, cay, ty);
+            kadd(az, caz, tz);
+            kadd(fPot, cpot, tp);
+            ++nLoop;
         }
         if (sizeof(Real) == 4 && cE.hMax <= 3) {
             // FP32: e^{i h.x} of every k-space vector from the three phase
@@ -670,20 +699,24 @@ int tsph_ewald(tsph_ctx *ctx, const tsph_grav_params *gp) {
     memcpy(&ext, &ctx->hCnt->maxAbs, sizeof(ext));
     if (ext < 0.5 * L) ext = 0.5 * L;
     int ni = 0;
-    for (int ix = -E.nEwReps; ix <= E.nEwReps; ++ix)
-        for (int iy = -E.nEwReps; iy <= E.nEwReps; ++iy)
-            for (int iz = -E.nEwReps; iz <= E.nEwReps; ++iz) {
-                const int id[3] = {ix, iy, iz};
-                double d2 = 0.0;
-                for (int k = 0; k < 3; ++k) {
-                    double s = ext + fabs(com[k]) + 1e-9 * L;
-                    double d = fabs(id[k] * L) - s;
-                    if (d > 0) d2 += d * d;
+    for (int pass = 0; pass < 2; ++pass) {   // hole images first
+        for (int ix = -E.nEwReps; ix <= E.nEwReps; ++ix)
+            for (int iy = -E.nEwReps; iy <= E.nEwReps; ++iy)
+                for (int iz = -E.nEwReps; iz <= E.nEwReps; ++iz) {
+                    const int id[3] = {ix, iy, iz};
+                    double d2 = 0.0;
+                    for (int k = 0; k < 3; ++k) {
+                        double s = ext + fabs(com[k]) + 1e-9 * L;
+                        double d = fabs(id[k] * L) - s;
+                        if (d > 0) d2 += d * d;
+                    }
+                    const bool hole = abs(ix) <= E.nReps && abs(iy) <= E.nReps && abs(iz) <= E.nReps;
+                    if (hole != (pass == 0)) continue;
+                    if (d2 > E.fEwCut2 * (1.0 + 1e-9) && !hole) continue;
+                    E.img[ni++] = make_char4((signed char)ix, (signed char)iy, (signed char)iz, hole ? 1 : 0);
                 }
-                const bool hole = abs(ix) <= E.nReps && abs(iy) <= E.nReps && abs(iz) <= E.nReps;
-                if (d2 > E.fEwCut2 * (1.0 + 1e-9) && !hole) continue;
-                E.img[ni++] = make_char4((signed char)ix, (signed char)iy, (signed char)iz, hole ? 1 : 0);
-            }
+        if (pass == 0) E.nHole = ni;
+    }
     E.nImg = ni;
     TSPH_CK(cudaMemcpyToSymbolAsync(cE, &E, sizeof(E), 0, cudaMemcpyHostToDevice, ctx->stream));
     const int BS = 128;
