@@ -411,8 +411,8 @@ int tsph_render_tsc(tsph_ctx *ctx, const tsph_render_params *rp, int nStar, floa
  * particle's interactions are summed, so forces move by rounding only.
  * Zero selects the default. */
 typedef struct {
-    int taskSize;         /* largest tree node one CTA builds whole (>= 1024; default 3072) */
-    int walkBlocksPerSM;  /* resident blocks per SM of the walk (default 4) */
+    int taskSize;         /* largest tree node one CTA builds whole (>= 1024; default 1536) */
+    int walkBlocksPerSM;  /* walk blocks per SM (default 5 for FP32, 4 for FP64) */
     int walkGroup;        /* particles per walk group, 32..4096; -1 = no groups; default
                              128 when there are at least 256 particles per walk warp, else
                              none.  The buckets of a group (the largest subtree with at
