@@ -63,6 +63,11 @@ extern "C" int tsph_create(tsph_ctx **pctx, int device, void *stream) {
         return TSPH_ERR_NOMEM;
     }
     for (int k = 0; k < 10; ++k) cudaEventCreate(&ctx->ev[k]);
+    if (cudaMallocHost((void **)&ctx->hRoot, sizeof(double) * 64) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->evRoot, cudaEventDisableTiming) != cudaSuccess) {
+        tsph_destroy(ctx);
+        return TSPH_ERR_NOMEM;
+    }
     *pctx = ctx;
     return TSPH_OK;
 }
@@ -114,6 +119,8 @@ extern "C" void tsph_destroy(tsph_ctx *ctx) {
     if (ctx->hCnt) cudaFreeHost(ctx->hCnt);
     if (ctx->B.hostCount) cudaFreeHost(ctx->B.hostCount);
     for (int k = 0; k < 10; ++k) if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
+    if (ctx->evRoot) cudaEventDestroy(ctx->evRoot);
+    if (ctx->hRoot) cudaFreeHost(ctx->hRoot);
     if (ctx->ownStream && ctx->stream) cudaStreamDestroy(ctx->stream);
     free(ctx);
 }
@@ -432,6 +439,11 @@ extern "C" int tsph_grav_all(tsph_ctx *ctx, const tsph_grav_params *gp, tsph_gra
     if (!cap) cudaEventRecord(ctx->ev[1], ctx->stream);
     rc = tsph_tree_moments(ctx, ctx->P, ctx->T, n, gp->dTheta);
     if (rc) return rc;
+    const bool ewald = n > 0 && gp->bPeriodic && gp->bEwald && gp->iEwOrder >= 1;
+    if (ewald) {   // the root moments now, so the host has them while the walk runs
+        rc = tsph_ewald_roots(ctx, gp);
+        if (rc) return rc;
+    }
     if (!cap) cudaEventRecord(ctx->ev[2], ctx->stream);
     ctx->haveTree = true;
     if (!gp->bPeriodic) {
@@ -450,7 +462,6 @@ extern "C" int tsph_grav_all(tsph_ctx *ctx, const tsph_grav_params *gp, tsph_gra
     }
     if (!cap) cudaEventRecord(ctx->ev[3], ctx->stream);
     if (n > 0) {
-        bool ewald = gp->bPeriodic && gp->bEwald && gp->iEwOrder >= 1;
         if (ewald) rc = tsph_ewald(ctx, gp);
         else if (gp->precision == TSPH_FP32 && ctx->T.nLeaves > 0) rc = tsph_walk_finish_f32(ctx);
         if (rc) return rc;

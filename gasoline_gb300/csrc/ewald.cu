@@ -558,12 +558,14 @@ static void qeval_h(int iOrder, const EwMom &mom, const double *gam, double dx, 
     (void)Qta; (void)ax; (void)ay; (void)az;
 }
 
-int tsph_ewald(tsph_ctx *ctx, const tsph_grav_params *gp) {
+// Root moments (pkdCalcRoot) on the device right after the cell moments,
+// read back into pinned memory; evRoot marks them ready, so the host builds
+// the Ewald constants while the walk runs.
+int tsph_ewald_roots(tsph_ctx *ctx, const tsph_grav_params *gp) {
     if (!(gp->bPeriodic && gp->bEwald) || gp->iEwOrder < 1) return TSPH_OK;
     if (gp->iEwOrder > 4) return TSPH_ERR_ARG;
     const int n = ctx->n;
     if (n == 0) return TSPH_OK;
-    // root moments on the device
     int nb = 256;
     double *partial = ctx->dRoot + 64;
     if (gp->precision == TSPH_FP32) {
@@ -577,13 +579,24 @@ int tsph_ewald(tsph_ctx *ctx, const tsph_grav_params *gp) {
     }
     k_root_final<<<1, 32, 0, ctx->stream>>>(nb, partial, ctx->dRoot);
     TSPH_LAUNCH_CK("k_root_final");
-    double h[25 + 11];
+    double *h = ctx->hRoot;   // [0, 25) octopole and hexadecapole; [32] fMass, [33, 36) r, [36, 42) Q
     TSPH_CK(cudaMemcpyAsync(h, ctx->dRoot, sizeof(double) * 25, cudaMemcpyDeviceToHost, ctx->stream));
-    double node0[11];   // fMass, r[3], Q[6]
-    TSPH_CK(cudaMemcpyAsync(&node0[0], ctx->T.fMass, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    TSPH_CK(cudaMemcpyAsync(&node0[1], ctx->T.r, 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    TSPH_CK(cudaMemcpyAsync(&node0[4], ctx->T.Q, 6 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    TSPH_CK(cudaStreamSynchronize(ctx->stream));
+    TSPH_CK(cudaMemcpyAsync(h + 32, ctx->T.fMass, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    TSPH_CK(cudaMemcpyAsync(h + 33, ctx->T.r, 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    TSPH_CK(cudaMemcpyAsync(h + 36, ctx->T.Q, 6 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    TSPH_CK(cudaEventRecord(ctx->evRoot, ctx->stream));
+    return TSPH_OK;
+}
+
+// The Ewald constants from the root moments (the host waits for evRoot
+// only) and the per-particle pass, queued behind the walk.
+int tsph_ewald(tsph_ctx *ctx, const tsph_grav_params *gp) {
+    if (!(gp->bPeriodic && gp->bEwald) || gp->iEwOrder < 1) return TSPH_OK;
+    if (gp->iEwOrder > 4) return TSPH_ERR_ARG;
+    const int n = ctx->n;
+    if (n == 0) return TSPH_OK;
+    TSPH_CK(cudaEventSynchronize(ctx->evRoot));
+    const double *h = ctx->hRoot, *node0 = ctx->hRoot + 32;
     // the table (~32 KB) is built in a per-context host block, then copied
     if (!ctx->hEw) {
         ctx->hEw = malloc(sizeof(EwConst));

@@ -120,6 +120,8 @@ struct tsph_ctx {
 
     // Ewald
     double *dRoot;               // 35 doubles: root complete moments
+    double *hRoot;               // pinned host copy of the root moments
+    cudaEvent_t evRoot;          // the root moments are on the host
     double *dEwt;                // 5 doubles per k-vector
     int nEwt;
     int ewtCap;
@@ -240,6 +242,7 @@ int tsph_copy_out_n(tsph_ctx *ctx, int n, const double *a0, const double *a1, co
 void tsph_free_tree(TsphDevTree &T);
 int tsph_walk_interact(tsph_ctx *ctx, const tsph_grav_params *gp);
 int tsph_walk_finish_f32(tsph_ctx *ctx);
+int tsph_ewald_roots(tsph_ctx *ctx, const tsph_grav_params *gp);
 int tsph_ewald(tsph_ctx *ctx, const tsph_grav_params *gp);
 int tsph_ensure_particles(tsph_ctx *ctx, int n);
 int tsph_sph_density(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_out *out);
