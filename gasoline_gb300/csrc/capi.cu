@@ -258,6 +258,7 @@ int tsph_load_begin(tsph_ctx *ctx, int n) {
     ctx->G.n = 0;
     ctx->sysVersion++;
     ctx->nSys = 1;
+    ctx->T.lastTopLevels = ctx->TG.lastTopLevels = 0;   // a new particle set: no depth known
     if (n == 0) return TSPH_OK;
     return tsph_set_ranges(ctx, ctx->P, ctx->T, n, 1, &n);
 }

@@ -1554,7 +1554,7 @@ static int build_tree_body(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n
     // top phase: levels are launched in batches; the frontier of each level
     // is known on the device only, the host bounds it (every split node of
     // a level holds more than S particles, so a level has at most 2n/S
-    // children) and looks at the true size every TOP_BATCH levels
+    // children) and looks at the true size now and then
     const int TOP_BATCH = 4;
     int levelStart[TSPH_MAX_LEVELS + 2];
     int cur = 0, level = 0;
@@ -1566,6 +1566,9 @@ static int build_tree_body(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n
     const int Lmax = cap ? (T.lastTopLevels + 4 < TSPH_MAX_LEVELS - 2 ? T.lastTopLevels + 4
                                                                       : TSPH_MAX_LEVELS - 2)
                          : TSPH_MAX_LEVELS - 2;
+    // the first look comes at the last build's depth (the same particles
+    // rebuilt give the same depth), then every TOP_BATCH levels
+    const int look0 = (!cap && T.lastTopLevels > 0) ? T.lastTopLevels : TOP_BATCH;
     while (Fb > 0 && level < Lmax) {
         if (!cap && level + 2 >= TSPH_MAX_LEVELS) return TSPH_ERR_TREE_DEPTH;
         const int slots = n / TB_CHUNK + Fb + 1;     // >= chunks of any frontier
@@ -1626,7 +1629,7 @@ static int build_tree_body(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n
         cur = 1 - cur;
         ++level;
         Fb = 2 * Fb < Fcap ? 2 * Fb : Fcap;
-        if (!cap && level % TOP_BATCH == 0) {
+        if (!cap && level >= look0 && (level - look0) % TOP_BATCH == 0) {
             TSPH_CK(cudaMemcpyAsync(B.hostCount, &B.ctl->levF[level], sizeof(int),
                                     cudaMemcpyDeviceToHost, ctx->stream));
             TSPH_CK(cudaStreamSynchronize(ctx->stream));
