@@ -204,16 +204,27 @@ __global__ void k_load_state(int n, const double *__restrict__ pos3, TsphDevStat
     giord[i] = i;
 }
 
-// tree-order copy of the state, keeping the previous tree permutation
-__global__ void k_gather_tree(int n, TsphDevState C, TsphDevParts P) {
+// The caller-order state gathered into the last tree order (the reference
+// keeps pStore in tree order between steps), checked on the way: non-finite
+// input, the coordinate scale of the walk's rounding bound, and (for a
+// captured step) particles beyond the bound the graph was built for.
+__global__ void k_gather_tree(int n, TsphDevState C, TsphDevParts P, TsphDevCounters *cnt,
+                              double limit) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int o = P.iord[i];
-    P.x[i] = C.x[o];
-    P.y[i] = C.y[o];
-    P.z[i] = C.z[o];
-    P.m[i] = C.m[o];
-    P.h[i] = C.h[o];
+    double a = 0.0;
+    if (i < n) {
+        int o = P.iord[i];
+        const double x = C.x[o], y = C.y[o], z = C.z[o], m = C.m[o], h = C.h[o];
+        P.x[i] = x;
+        P.y[i] = y;
+        P.z[i] = z;
+        P.m[i] = m;
+        P.h[i] = h;
+        if (!isfinite(x + y + z + m + h)) atomicOr(&cnt->status, 1u << TSPH_ERR_NONFINITE);
+        a = fmax(fabs(x), fmax(fabs(y), fabs(z)));
+        if (a > limit) atomicOr(&cnt->status, 1u << TSPH_ERR_BOUNDS);
+    }
+    warp_max_abs(a, &cnt->maxAbs);
 }
 
 // gravity results of the active particles; the others keep theirs
@@ -227,20 +238,6 @@ __global__ void k_scatter_grav(int n, TsphDevParts P, TsphDevState C) {
     C.az[o] = P.az[i];
     C.pot[o] = P.pot[i];
     C.dtGrav[o] = P.dtGrav[i];
-}
-
-// Non-finite input, the coordinate scale of the walk's rounding bound, and
-// (for a captured step) particles beyond the bound the graph was built for.
-__global__ void k_check_finite(int n, TsphDevParts P, TsphDevCounters *cnt, double limit) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double a = 0.0;
-    if (i < n) {
-        double v = P.x[i] + P.y[i] + P.z[i] + P.m[i] + P.h[i];
-        if (!isfinite(v)) atomicOr(&cnt->status, 1u << TSPH_ERR_NONFINITE);
-        a = fmax(fabs(P.x[i]), fmax(fabs(P.y[i]), fabs(P.z[i])));
-        if (a > limit) atomicOr(&cnt->status, 1u << TSPH_ERR_BOUNDS);
-    }
-    warp_max_abs(a, &cnt->maxAbs);
 }
 
 // A new particle set of n: buffers, one system, every derived state stale.
@@ -421,11 +418,9 @@ extern "C" int tsph_grav_all(tsph_ctx *ctx, const tsph_grav_params *gp, tsph_gra
     TSPH_CK(cudaMemsetAsync(ctx->dCnt, 0, sizeof(TsphDevCounters), ctx->stream));
     if (!cap) cudaEventRecord(ctx->ev[0], ctx->stream);
     if (n > 0) {
-        k_gather_tree<<<tsph_blocks(n, 256), 256, 0, ctx->stream>>>(n, ctx->C, ctx->P);
+        k_gather_tree<<<tsph_blocks(n, 256), 256, 0, ctx->stream>>>(
+            n, ctx->C, ctx->P, ctx->dCnt, ctx->capLimit > 0 ? ctx->capLimit : INFINITY);
         TSPH_LAUNCH_CK("k_gather_tree");
-        k_check_finite<<<tsph_blocks(n, 256), 256, 0, ctx->stream>>>(
-            n, ctx->P, ctx->dCnt, ctx->capLimit > 0 ? ctx->capLimit : INFINITY);
-        TSPH_LAUNCH_CK("k_check_finite");
     }
     int rc = cap ? TSPH_OK : read_status(ctx);
     if (rc) return rc;
