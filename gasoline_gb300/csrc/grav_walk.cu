@@ -1129,12 +1129,12 @@ __global__ void k_group_list(TsphDevTree T, int cap, const int *flag, const int 
 
 // Group arrays and the per-warp list scratch; outside a capture they grow
 // to the particle count (a bound on the buckets of any later captured
-// step).  *on stays false when groups are off or (in a capture) not sized.
+// step).  A.groupFirst stays null when groups are off or (in a capture)
+// not sized.
 // By default groups hold up to 128 particles, and are used when there are
 // at least 256 particles per walk warp: a group is one work unit, and with
 // fewer the last units leave most warps idle.
-static int prepare_groups(tsph_ctx *ctx, WalkArgs &A, int nbHost, int warps, bool *on) {
-    *on = false;
+static int prepare_groups(tsph_ctx *ctx, WalkArgs &A, int nbHost, int warps) {
     const int G = ctx->walkGroup == 0 ? 128 : ctx->walkGroup;
     if (ctx->walkGroup == 0 && (long long)ctx->n < 256LL * warps) return TSPH_OK;
     if (G <= 0 || nbHost <= 0) return TSPH_OK;
@@ -1167,7 +1167,6 @@ static int prepare_groups(tsph_ctx *ctx, WalkArgs &A, int nbHost, int warps, boo
     A.nGroups = ctx->dGroupCount;
     A.groupScratch = ctx->dGroupScratch;
     A.groupMax = G;
-    *on = true;
     return TSPH_OK;
 }
 
@@ -1247,8 +1246,7 @@ int tsph_walk_interact(tsph_ctx *ctx, const tsph_grav_params *gp) {
     A.nGroups = nullptr;
     A.groupScratch = nullptr;
     A.groupMax = 0;
-    bool groups = false;
-    rc = prepare_groups(ctx, A, nbHost, blocks * WPB, &groups);
+    rc = prepare_groups(ctx, A, nbHost, blocks * WPB);
     if (rc) return rc;
     const int nbt = gp->nBucket <= 8 ? 8 : (gp->nBucket <= 16 ? 16 : 32);
     if (gp->precision == TSPH_FP32) {
