@@ -415,6 +415,15 @@ def run_plummer(args):
         res[name] = {"grav_ms": statistics.mean(ts), "kdk_step_ms": tk[0],
                      "err_vs_direct_rms": float(np.sqrt(np.mean(e ** 2))),
                      "err_vs_direct_p99": float(np.percentile(e, 99))}
+        if prec == g.FP32:
+            # the same KDK step captured once as a CUDA graph and replayed:
+            # at this size the directly launched step is launch-bound
+            ctx.step(1e-3, gp, None, graph=True)
+            ctx.step_status()
+            tg = [_cuda_ms(lambda: ctx.step(1e-3, gp, None, graph=True), stream)
+                  for _ in range(args.steps)]
+            ctx.step_status()
+            res[name]["kdk_step_graph_ms"] = statistics.mean(tg)
         ctx.set_particles(pos, m, soft)
         ctx.set_velocities(vel)
     ctx.close()
