@@ -45,3 +45,45 @@ def test_no_cpu_fallback_without_library(tmp_path, monkeypatch):
     monkeypatch.setattr(g, "_lib", None)
     with pytest.raises(RuntimeError):
         g.load()
+
+
+STRUCTS = {   # C typedef in include/tsph.h -> ctypes class in gasoline_gb300
+    "tsph_grav_params": "GravParams",
+    "tsph_grav_out": "GravOut",
+    "tsph_sph_params": "SphParams",
+    "tsph_smooth_out": "SmoothOut",
+    "tsph_tuning": "Tuning",
+    "tsph_step_params": "StepParams",
+    "tsph_step_out": "StepOut",
+    "tsph_render_params": "RenderParams",
+    "tsph_tipsy_header": "TipsyHeader",
+}
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """Every parameter and output struct of the binding has the C layout:
+    the size and every field's offset, as gcc lays out include/tsph.h."""
+    import shutil
+    import subprocess
+    import gasoline_gb300 as g
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "tsph.h"', 'int main(void) {']
+    for cname, pyname in STRUCTS.items():
+        cls = getattr(g, pyname)
+        lines.append(f'printf("{pyname} size %zu\\n", sizeof({cname}));')
+        for field in cls._fields_:
+            f = field[0]
+            lines.append(f'printf("{pyname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.check_call([cc, "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
+    out = subprocess.check_output([str(exe)], text=True).split("\n")
+    for line in filter(None, out):
+        pyname, what, val = line.split()
+        cls = getattr(g, pyname)
+        got = ctypes.sizeof(cls) if what == "size" else getattr(cls, what).offset
+        assert got == int(val), (pyname, what, got, int(val))
