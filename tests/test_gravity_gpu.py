@@ -215,7 +215,7 @@ def test_tuning_does_not_change_results():
         c.close()
 
 
-@pytest.mark.parametrize("case", ["plummer", "box"])
+@pytest.mark.parametrize("case", ["plummer", "box", "clumps"])
 def test_walk_groups_keep_every_list(case):
     """Walk groups (one shared walk per subtree of at most walkGroup
     particles; each bucket walks only what the group could not settle)
@@ -230,9 +230,13 @@ def test_walk_groups_keep_every_list(case):
         pos, vel, m = g.ics.plummer(32768, seed=3)
         soft = np.full(len(m), 0.01)
         periodic = False
-    else:
+    elif case == "box":
         pos, vel, m = g.ics.lattice_box(24, seed=5)
         soft = np.full(len(m), 1.0 / (50 * 24))
+        periodic = True
+    else:   # periodic, two lattices with a fifth of the mass in 16 tight clumps
+        pos, vel, m, ngas, u = g.ics.mixed_box(ng=20, seed=7, nclump=16)
+        soft = np.full(len(m), 1.0 / (50 * 20))
         periodic = True
     c = g.Context(0)
     try:
