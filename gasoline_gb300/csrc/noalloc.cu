@@ -12,9 +12,10 @@
 // The scratch array (HNA_MAX_WARPS partial gradients + partial losses,
 // about 2.5 MB) is created with the library and held by every GPU that
 // loads it until the process exits.  All calls share it: each call
-// overwrites every partial it later reads, so nothing needs clearing, but
-// calls that overlap on the GPU (two streams, or two host threads) race on
-// it and must be serialised by the caller.
+// overwrites every partial it later reads (the partials of warps 0..nwarps-1,
+// whatever a larger earlier call left beyond them), so nothing needs
+// clearing, but calls that overlap on the GPU (two streams, or two host
+// threads) race on it and must be serialised by the caller.
 #include <stdio.h>
 
 #include "tsph_ctx.cuh"
@@ -23,17 +24,12 @@
 #define HNA_SAMPLES_PER_WARP 32
 #define HNA_MAX_WARPS 512
 #define HNA_MAX_SAMPLES (HNA_MAX_WARPS * HNA_SAMPLES_PER_WARP)
-#define HNA_MAX_DEVICES 64
 
 static_assert(HNA_MAX_SAMPLES == TSPH_HNET_NOALLOC_MAX_SAMPLES, "header limit");
 
 // partial gradients of up to HNA_MAX_WARPS warps, then their partial losses
 static __device__ __align__(256) float g_hna_scratch[HNA_MAX_WARPS * HNET_NP + HNA_MAX_WARPS];
 
-// Host-side cache of the scratch array's device address, per device.  The
-// symbol's name is only a host stand-in; its device address comes from
-// cudaGetSymbolAddress with that device current.
-static float *g_hna_ptr[HNA_MAX_DEVICES];
 
 // One sample, one warp: lane j owns hidden unit j of both layers.  Same
 // network and loss (0.5 (out - y)^2) as the allocating path.
@@ -124,17 +120,20 @@ __global__ void k_hna_reduce(const float *__restrict__ scratch, int nwarps, floa
     }
 }
 
-// Set-up, once per device, with that device current: the scratch array's
-// device address.  Runs on the first call made on each device.
-static int hna_setup(int device, float **ptr) {
-    if (device < 0 || device >= HNA_MAX_DEVICES) return TSPH_ERR_ARG;
-    if (!g_hna_ptr[device]) {
-        float *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress((void **)&p, g_hna_scratch);
-        if (e != cudaSuccess || !p) return TSPH_ERR_CUDA;
-        g_hna_ptr[device] = p;
-    }
-    *ptr = g_hna_ptr[device];
+// The scratch array's device address in the calling thread's current
+// context.  The symbol's name is only a host stand-in; its device address
+// comes from cudaGetSymbolAddress with the device current.  It is looked up
+// on every call rather than cached per device ordinal: the address belongs
+// to one context, and a device reset or a caller-made context on the same
+// device places the array elsewhere.  The lookup is host-side and does not
+// touch the stream; the first one on a device loads the library's device
+// code there, which is why that first call must come before any stream
+// capture.
+static int hna_scratch_address(float **ptr) {
+    float *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress((void **)&p, g_hna_scratch);
+    if (e != cudaSuccess || !p) return TSPH_ERR_CUDA;
+    *ptr = p;
     return TSPH_OK;
 }
 
@@ -143,11 +142,13 @@ extern "C" int tsph_hnet_loss_grad_noalloc(const float *params, int n, const flo
                                            void *stream) {
     if (!params || !x3 || !y || !grad || !loss || n <= 0) return TSPH_ERR_ARG;
     if (n > HNA_MAX_SAMPLES) return TSPH_ERR_ARG;   // more samples than the fixed scratch holds
-    int device = 0;
-    if (cudaGetDevice(&device) != cudaSuccess) return TSPH_ERR_CUDA;
     float *scratch = nullptr;
-    int rc = hna_setup(device, &scratch);
+    int rc = hna_scratch_address(&scratch);
     if (rc) return rc;
+    // an error left by earlier, unrelated work (not a sticky one, which
+    // would fail the launches below as well) is cleared here, so the checks
+    // after the launches report this call's own
+    (void)cudaGetLastError();
     cudaStream_t s = (cudaStream_t)stream;
     int nwarps = (n + HNA_SAMPLES_PER_WARP - 1) / HNA_SAMPLES_PER_WARP;
     int blocks = (nwarps * 32 + 255) / 256;

@@ -259,10 +259,11 @@ int tsph_hnet_info(tsph_ctx *ctx, long long *nSamples, float *stats8);
  * on `stream` (a cudaStream_t, NULL = default) of the current device and
  * returns without synchronising.  Scratch lives in one fixed device array
  * of ~2.5 MB that the library holds on every GPU that loads it until exit;
- * n above TSPH_HNET_NOALLOC_MAX_SAMPLES returns TSPH_ERR_ARG.  The first
- * call on each device looks up that array's address (make it before any
- * stream capture).  Calls share the array: calls that overlap on the GPU
- * race and must be serialised by the caller. */
+ * n above TSPH_HNET_NOALLOC_MAX_SAMPLES returns TSPH_ERR_ARG.  Every call
+ * looks up that array's address in the calling thread's current context;
+ * the first call on a device also loads the library's device code there,
+ * so make it before any stream capture.  Calls share the array: calls that
+ * overlap on the GPU race and must be serialised by the caller. */
 #define TSPH_HNET_NOALLOC_MAX_SAMPLES 16384
 int tsph_hnet_loss_grad_noalloc(const float *params, int n, const float *x3,
                                 const float *y, float *grad, float *loss,

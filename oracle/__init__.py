@@ -83,8 +83,10 @@ def reference_available():
     return os.path.exists(_REF)
 
 
-def build_reference(refdir="/root/reference"):
-    subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh"), refdir])
+def build_reference(refdir=None):
+    """Compile the reference's own sources into oracle/_ref (build_ref.sh;
+    refdir defaults to the recipe's: $GASOLINE_REFERENCE or its checkout)."""
+    subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh")] + ([refdir] if refdir else []))
 
 
 def _d(a):

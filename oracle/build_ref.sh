@@ -1,13 +1,22 @@
 #!/bin/sh
 # Builds the reference's own hot-path sources, unmodified and from where they
 # lie, into oracle/_ref/libgasref.so for pinning the oracle (test use only).
-# Usage: oracle/build_ref.sh [reference-dir]   (default /root/reference)
+# Usage: oracle/build_ref.sh [--if-present] [reference-dir]
+#   reference-dir defaults to $GASOLINE_REFERENCE, else /root/reference (the
+#   checkout this recipe was written against).  With --if-present a missing
+#   checkout is not an error: the script says so and exits 0.
 # Writes only under oracle/_ref/.  Needs gcc; no cmake, no reference Makefile.
 set -e
-REF=${1:-/root/reference}
+OPTIONAL=0
+if [ "$1" = "--if-present" ]; then OPTIONAL=1; shift; fi
+REF=${1:-${GASOLINE_REFERENCE:-/root/reference}}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
-[ -f "$REF/pkd.c" ] || { echo "reference sources not found at $REF" >&2; exit 1; }
+if [ ! -f "$REF/pkd.c" ]; then
+  echo "reference sources not found at $REF" >&2
+  [ $OPTIONAL = 1 ] && exit 0
+  exit 1
+fi
 mkdir -p "$OUT"
 CFLAGS="-O2 -fPIC -ffp-contract=off -fno-fast-math -w -DNOCOOLING -DGASOLINE -DM4 \
  -include stdio.h -I$HERE/shim -I$REF -I$HERE/../include"

@@ -8,6 +8,8 @@ rms 1e-9 (the reference's own 1/sqrt, v_sqrt1, is accurate to 2e-10 per
 term, the CUDA path uses a correctly rounded rsqrt);
 FP32 accelerations agree to p99 <= 1e-4 relative.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -122,6 +124,43 @@ def test_plummer_32k_vs_oracle(ctx, orc, prec):
         assert np.percentile(e, 99) < FP32_P99 and rms(e) < FP32_RMS
     assert r["out"]["dPartSum"] == ref["counters"][1]
     assert r["out"]["dCellSum"] == ref["counters"][2]
+
+
+@pytest.fixture(scope="module")
+def box64(orc):
+    """The 64^3 periodic box (262,144 particles, the headline construction
+    at an eighth of its size) and the oracle's evaluation of it with the
+    reference's own arithmetic (v_sqrt1), nBucket 16."""
+    pos, vel, m = g.ics.lattice_box(64, seed=2)
+    soft = np.full(len(m), 1.0 / (50 * 64))
+    ref = orc.grav(pos, m, soft, oracle.grav_params(periodic=True, nBucket=16),
+                   nthreads=os.cpu_count() or 1)
+    return pos, m, soft, ref
+
+
+@pytest.mark.parametrize("prec", [g.FP64, g.FP32])
+def test_periodic_box_64_vs_oracle(ctx, box64, prec):
+    """At 262,144 particles: pkdGravAll's counters (active particles, P-P,
+    Newtonian and softened cell interactions) equal the oracle's exactly and
+    its flop count to 1e-12; FP64 accelerations within the periodic bar
+    against the reference's arithmetic and the potential within 1e-7 of
+    max |pot|; FP32 p99 within the periodic FP32 bar."""
+    pos, m, soft, ref = box64
+    gp = g.grav_params(periodic=True, precision=prec, nBucket=16)
+    r = run(ctx, pos, m, soft, gp)
+    c, o = ref["counters"], r["out"]
+    assert o["nActive"] == int(c[0])
+    assert o["dPartSum"] == c[1]
+    assert o["dCellSum"] == c[2]
+    assert o["dSoftSum"] == c[3]
+    assert o["dFlop"] == pytest.approx(c[4], rel=1e-12)
+    e = rel_err(r["acc"], ref["acc"])
+    if prec == g.FP64:
+        assert rms(e) < PER_FP64_VS_REF_RMS, (rms(e), e.max())
+        ep = np.abs(r["pot"] - ref["pot"]) / np.abs(ref["pot"]).max()
+        assert ep.max() < PER_POT_VS_REF_SCALED, ep.max()
+    else:
+        assert np.percentile(e, 99) < PER_FP32_P99, np.percentile(e, 99)
 
 
 @pytest.mark.parametrize("prec", [g.FP64, g.FP32])
