@@ -54,6 +54,9 @@ def workload(ng=128, seed=2, with_vel=False):
 # step does, so every tree build partitions moved particles.  The box's
 # velocities equal its displacement field (rms 0.2 of the spacing), so a
 # drift of DRIFT_DT moves particles by 0.02 of the spacing rms per step.
+# The drift alternates in sign (forward, back): drifting one way only would
+# grow the displacement field step after step and turn the box into a
+# different, more clustered configuration than the one named.
 DRIFT_DT = 0.1
 
 
@@ -71,7 +74,8 @@ def config(ng, steps_flush="l2-flush", nbucket=8):
                         f"theta=0.7, eps=1/(50*{ng}), nBucket={nbucket} (autotuned)",
             "n_particles": ng ** 3, "theta": 0.7, "iOrder": 2, "iEwOrder": 4,
             "nBucket": nbucket, "precision": "fp32 bucket-relative, fp64 positions",
-            "step": f"drift (v*{DRIFT_DT}, 0.02 of the spacing rms) + one full force evaluation",
+            "step": f"drift (v*{DRIFT_DT} forward and back in turn, 0.02 of the spacing rms) "
+                    "+ one full force evaluation",
             "l2": steps_flush, "parallelism": "replicas"}
 
 
@@ -188,16 +192,17 @@ def run_ours(args, rank, world, local_rank):
     gp64 = g.grav_params(periodic=True, precision=g.FP64, nBucket=tuned["nBucket"])
 
     def timed(gp, steps, warmup, e2e=False):
-        # one step: move the particles (a device drift; end to end, the
-        # other host position set), then one full force evaluation
+        # one step: move the particles (a device drift, forward and back in
+        # turn; end to end, the other host position set), then one full
+        # force evaluation
         k = [0]
 
         def one():
+            k[0] ^= 1
             if e2e:
-                k[0] ^= 1
                 ctx.update_particles_ptr(n, hpos[k[0]].data_ptr(), hm.data_ptr(), hs.data_ptr())
             else:
-                ctx.drift(DRIFT_DT, True, 1.0)
+                ctx.drift(DRIFT_DT if k[0] else -DRIFT_DT, True, 1.0)
             o = ctx.grav_all(gp)
             if e2e:
                 ctx.get_gravity_ptr(hacc.data_ptr())
@@ -319,7 +324,10 @@ def run_ours(args, rank, world, local_rank):
         if not args.no_cpu:
             base, ref = cpu_baseline(args, pos, m, soft)
             result["cpu_baseline"] = base
-            result["parity"] = parity(o64, g64, o32, g32, ref)
+            import oracle
+            with oracle.exact_rsqrt():
+                _, ref_exact = cpu_baseline(args, pos, m, soft)
+            result["parity"] = parity(o64, g64, o32, g32, ref, ref_exact)
     ctx.close()
     return result
 
@@ -340,48 +348,67 @@ def cpu_baseline(args, pos, m, soft):
                        f"({dt:.1f} s, OpenMP over buckets, serial tree build)"}, ref)
 
 
-# parity bars at the headline size (the same ones the GPU tests state): the
-# counters exact; FP64 accelerations within the periodic bar against the
-# reference's arithmetic (its v_sqrt1 1/sqrt is accurate to 2e-10 per term,
-# amplified by the near-cancelling replica and Ewald sums); potentials
-# against max |pot| (the periodic potential crosses zero); FP32 p99
-PARITY_FP64_RMS = 3e-8
-PARITY_POT_SCALED = 1e-7
+# Parity bars at the headline size.  The reference takes 1/r from v_sqrt1,
+# accurate to 2e-10 per term; in the periodic box the replica and Ewald sums
+# cancel to a net force far smaller than the terms, which amplifies that
+# error with N (oracle with v_sqrt1 against the same oracle with an exact
+# 1/sqrt: acceleration rms 7.9e-9 at 16^3, 3.0e-8 at 64^3, 6.3e-8 at
+# 128^3).  The CUDA FP64 path takes a correctly rounded rsqrt, so it is
+# held to the oracle with an exact 1/sqrt (same tree, same lists, same
+# terms; only the order of the sums differs), and its distance from the
+# reference's own arithmetic is reported beside it.  The periodic potential
+# crosses zero and is measured against max |pot|.  FP32: p99 bar.
+PARITY_FP64_RMS = 1e-10
+PARITY_POT_SCALED = 1e-10
 PARITY_FP32_P99 = 3e-4
 
 
-def parity(o64, g64, o32, g32, ref):
+def _acc_err(a, ref):
+    return np.linalg.norm(a - ref, axis=1) / np.maximum(np.linalg.norm(ref, axis=1), 1e-300)
+
+
+def parity(o64, g64, o32, g32, ref, ref_exact):
     """The GPU's evaluations of the box (FP64 and FP32, same input) against
-    the oracle's, outside the timed region."""
+    the oracle's, outside the timed region: `ref` with the reference's own
+    arithmetic (v_sqrt1), `ref_exact` with an exact 1/sqrt."""
     c = ref["counters"]
-    oa = ref["acc"]
-    na = np.maximum(np.linalg.norm(oa, axis=1), 1e-300)
-    e64 = np.linalg.norm(g64["acc"] - oa, axis=1) / na
-    e32 = np.linalg.norm(g32["acc"] - oa, axis=1) / na
-    pscale = float(np.max(np.abs(ref["pot"])))
-    ep64 = float(np.max(np.abs(g64["pot"] - ref["pot"])) / pscale)
     counters = {}
     ok = True
     for name, o in (("fp64", o64), ("fp32", o32)):
         exact = (o["nActive"] == int(c[0]) and o["dPartSum"] == c[1] and o["dCellSum"] == c[2]
                  and o["dSoftSum"] == c[3])
-        flop = abs(o["dFlop"] - c[4]) <= 1e-12 * abs(c[4])
-        counters[name] = {"exact": bool(exact), "dFlop_rel_1e-12": bool(flop)}
-        ok = ok and exact and flop
-    rms64 = float(np.sqrt(np.mean(e64 ** 2)))
-    p99_32 = float(np.percentile(e32, 99))
-    ok = ok and rms64 <= PARITY_FP64_RMS and ep64 <= PARITY_POT_SCALED and p99_32 <= PARITY_FP32_P99
-    return {"against": "oracle (bit-exact restatement of the reference) on the same input, "
-                       "one full evaluation",
-            "counters": counters,
-            "oracle_counters": {"nActive": int(c[0]), "dPartSum": c[1], "dCellSum": c[2],
-                                "dSoftSum": c[3], "dFlop": c[4]},
-            "fp64_acc_rms": rms64, "fp64_acc_max": float(e64.max()),
-            "fp64_pot_max_over_max_pot": ep64,
-            "fp32_acc_rms": float(np.sqrt(np.mean(e32 ** 2))), "fp32_acc_p99": p99_32,
-            "bars": {"fp64_acc_rms": PARITY_FP64_RMS, "fp64_pot": PARITY_POT_SCALED,
-                     "fp32_acc_p99": PARITY_FP32_P99},
-            "pass": bool(ok)}
+        frel = abs(o["dFlop"] - c[4]) / abs(c[4])
+        counters[name] = {"nActive_PP_cells_soft_exact": bool(exact), "dFlop_rel_diff": frel}
+        ok = ok and exact
+    ok = ok and counters["fp64"]["dFlop_rel_diff"] <= 1e-12
+    pmax = float(np.max(np.abs(ref_exact["pot"])))
+    e64x = _acc_err(g64["acc"], ref_exact["acc"])
+    p64x = np.abs(g64["pot"] - ref_exact["pot"]) / pmax
+    e64r = _acc_err(g64["acc"], ref["acc"])
+    p64r = np.abs(g64["pot"] - ref["pot"]) / pmax
+    eref = _acc_err(ref["acc"], ref_exact["acc"])
+    e32 = _acc_err(g32["acc"], ref_exact["acc"])
+    rms = lambda x: float(np.sqrt(np.mean(np.square(x))))  # noqa: E731
+    res = {"against": "the oracle (a bit-exact restatement of the reference) on the same input, "
+                      "one full evaluation each",
+           "counters": counters,
+           "oracle_counters": {"nActive": int(c[0]), "dPartSum": c[1], "dCellSum": c[2],
+                               "dSoftSum": c[3], "dFlop": c[4]},
+           "fp64_vs_oracle_exact_rsqrt": {"acc_rms": rms(e64x), "acc_max": float(e64x.max()),
+                                          "pot_rms_over_max_pot": rms(p64x),
+                                          "pot_max_over_max_pot": float(p64x.max())},
+           "fp64_vs_oracle_v_sqrt1": {"acc_rms": rms(e64r), "acc_max": float(e64r.max()),
+                                      "pot_max_over_max_pot": float(p64r.max())},
+           "oracle_v_sqrt1_vs_exact_rsqrt": {"acc_rms": rms(eref), "acc_max": float(eref.max())},
+           "fp32_vs_oracle_exact_rsqrt": {"acc_rms": rms(e32), "acc_p99": float(np.percentile(e32, 99))},
+           "bars": {"fp64_acc_rms": PARITY_FP64_RMS, "fp64_pot_rms": PARITY_POT_SCALED,
+                    "fp32_acc_p99": PARITY_FP32_P99,
+                    "counters": "exact (FP64 dFlop to 1e-12; FP32 dFlop reported: its Ewald "
+                                "real-space cut is tested in FP32)"}}
+    ok = (ok and rms(e64x) <= PARITY_FP64_RMS and rms(p64x) <= PARITY_POT_SCALED
+          and float(np.percentile(e32, 99)) <= PARITY_FP32_P99)
+    res["pass"] = bool(ok)
+    return res
 
 
 def run_reference(args):

@@ -80,31 +80,39 @@ __device__ __forceinline__ void rep_off64(int r, double *o) {
     o[0] = (double)ix * cW.L; o[1] = (double)iy * cW.L; o[2] = (double)iz * cW.L;
 }
 
+// Staged tile data.  FP64: P-P uses x,y,z,m,h and cells x,y,z,m,q0..q5,h,
+// one array per field.  FP32: entries are stored in pairs (2p, 2p+1), each
+// field of a pair side by side, so one 128-bit load gives two fields of
+// both entries and every packed f32x2 instruction of the evaluation works
+// on the two entries at once:  xy = (x0, x1, y0, y1), zm = (z0, z1, m0, m1),
+// q01 = (xx0, xx1, yy0, yy1), q23 = (zz0, zz1, xy0, xy1),
+// q45 = (xz0, xz1, yz0, yz1), h = (h0, h1).
+template <typename Real>
+struct TileData {
+    Real ex[PPF], ey[PPF], ez[PPF], em[PPF], eh[PPF];
+    Real q[6][CNF];
+};
+template <>
+struct TileData<float> {
+    union {
+        struct {
+            float4 xy[PPF / 2], zm[PPF / 2];
+            float2 h[PPF / 2];
+        } pp;
+        struct {
+            float4 xy[CNF / 2], zm[CNF / 2], q01[CNF / 2], q23[CNF / 2], q45[CNF / 2];
+            float2 h[CNF / 2];
+        } cn;
+    };
+};
+
 template <typename Real, int NBT>
 struct WalkSmem {
     int stack[STK];
     int pp[PPF + 32 * NBT + NBT];
     int cn[CNB];
     int cs[CNB];
-    // staged entry data: P-P uses x,y,z,m,h ; cells use x,y,z,m,q0..q5,h.
-    // The FP32 walk packs them as float4 records (two or three vector
-    // loads per entry instead of five or eleven scalar ones).
-    union {
-        struct {
-            Real ex[PPF], ey[PPF], ez[PPF], em[PPF], eh[PPF];
-            Real q[6][CNF];
-        };
-        struct {
-            float4 r0[PPF];   // P-P and cells: x, y, z, m
-            union {
-                float rh[PPF];            // P-P: h
-                struct {
-                    float4 r1[CNF];       // cells: q0 q1 q2 q3
-                    float4 r2[CNF];       // cells: q4 q5 h -
-                };
-            };
-        };
-    };
+    TileData<Real> D;
     Real px[NBT], py[NBT], pz[NBT], pm[NBT], ph[NBT];
     // the warp's tallies of pkdGravAll's sums (lane 0 only)
     unsigned long long tAct, tPP, tNewt, tSoft, tBsq, tIntra;
@@ -270,76 +278,188 @@ __device__ __forceinline__ void spline_q(Real dir, Real r2, Real twoh, Real &a, 
 template <typename Real>
 struct Acc {
     Real s[4], c[4];     // ax, ay, az, pot (sum and compensation)
-    Real t[4];           // current tile partial
+    Real t[4];           // current tile partial (FP64 path)
     Real dt;             // max (m_i + m_j) * b
 };
+
+// ---- packed FP32 pair arithmetic (sm_100 family f32x2: one instruction,
+// two lanes' worth of FP32 work, each rounded as the scalar operation) ----
+__device__ __forceinline__ float2 p_add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 p_mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 p_fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 p_sub(float2 a, float2 b) {
+    unsigned long long r;
+    asm("sub.rn.f32x2 %0, %1, %2;"
+        : "=l"(r)
+        : "l"(*reinterpret_cast<const unsigned long long *>(&a)),
+          "l"(*reinterpret_cast<const unsigned long long *>(&b)));
+    return *reinterpret_cast<const float2 *>(&r);
+}
+__device__ __forceinline__ float2 p_rsqrt(float2 a) { return make_float2(rsqrtf(a.x), rsqrtf(a.y)); }
+__device__ __forceinline__ float2 p_splat(float a) { return make_float2(a, a); }
+
+// The partner of an odd-length tile's last entry: far away and massless,
+// so each of its terms is exactly zero (1/r^3 underflows, m = 0).
+#define FAR_ENTRY 1.0e18f
+
+// A packed tile partial folded into a compensated sum.
+__device__ __forceinline__ void kahan_add2(float &s, float &c, float2 v) {
+    kahan_add(s, c, v.x);
+    kahan_add(s, c, v.y);
+}
+
+// Relative FP32 position of an entry (particle or cell COM, hi/lo split)
+// in replica r about the bucket centre (hi/lo split).
+__device__ __forceinline__ void rel_pos(float4 h, float4 l, int r, float bchx, float bchy, float bchz,
+                                        float bclx, float bcly, float bclz, float &x, float &y,
+                                        float &z) {
+    float ohx, ohy, ohz, olx, oly, olz;
+    rep_off32(r, ohx, ohy, ohz, olx, oly, olz);
+    x = ((h.x - bchx) + ohx) + ((l.x - bclx) + olx);
+    y = ((h.y - bchy) + ohy) + ((l.y - bcly) + oly);
+    z = ((h.z - bchz) + ohz) + ((l.z - bclz) + olz);
+}
 
 // Stage P-P entries [0, cnt) of the warp's buffer into shared memory.
 template <typename Real, int NBT>
 __device__ __forceinline__ void stage_pp(WalkSmem<Real, NBT> &S, const TsphDevParts &P, int cnt,
                                          int lane, float bchx, float bchy, float bchz,
                                          float bclx, float bcly, float bclz) {
-    for (int e = lane; e < cnt; e += 32) {
-        int ent = S.pp[e];
-        int idx = ent >> 5, rep = ent & 31;
-        if constexpr (sizeof(Real) == 4) {
-            float4 a = P.ph[idx], b = P.pl[idx];
-            int r = rep == 31 ? cW.selfRep : rep;
-            float ohx, ohy, ohz, olx, oly, olz;
-            rep_off32(r, ohx, ohy, ohz, olx, oly, olz);
-            S.r0[e] = make_float4(((a.x - bchx) + ohx) + ((b.x - bclx) + olx),
-                                  ((a.y - bchy) + ohy) + ((b.y - bcly) + oly),
-                                  ((a.z - bchz) + ohz) + ((b.z - bclz) + olz), a.w);
-            S.rh[e] = b.w;
-        } else {
-            int r = rep == 31 ? cW.selfRep : rep;
+    if constexpr (sizeof(Real) == 4) {
+        const int np = (cnt + 1) >> 1;
+        for (int p = lane; p < np; p += 32) {
+            float x[2], y[2], z[2], m[2], h[2];
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                const int e = 2 * p + k;
+                if (e < cnt) {
+                    const int ent = S.pp[e];
+                    const int idx = ent >> 5, rep = ent & 31;
+                    const float4 a = P.ph[idx], b = P.pl[idx];
+                    rel_pos(a, b, rep == 31 ? cW.selfRep : rep, bchx, bchy, bchz, bclx, bcly, bclz,
+                            x[k], y[k], z[k]);
+                    m[k] = a.w;
+                    h[k] = b.w;
+                } else {
+                    x[k] = y[k] = z[k] = FAR_ENTRY;
+                    m[k] = h[k] = 0.0f;
+                }
+            }
+            S.D.pp.xy[p] = make_float4(x[0], x[1], y[0], y[1]);
+            S.D.pp.zm[p] = make_float4(z[0], z[1], m[0], m[1]);
+            S.D.pp.h[p] = make_float2(h[0], h[1]);
+        }
+    } else {
+        for (int e = lane; e < cnt; e += 32) {
+            const int ent = S.pp[e];
+            const int idx = ent >> 5, rep = ent & 31;
+            const int r = rep == 31 ? cW.selfRep : rep;
             double o[3];
             rep_off64(r, o);
-            S.ex[e] = (Real)(P.x[idx] + o[0]);
-            S.ey[e] = (Real)(P.y[idx] + o[1]);
-            S.ez[e] = (Real)(P.z[idx] + o[2]);
-            S.em[e] = (Real)P.m[idx];
-            S.eh[e] = (Real)P.h[idx];
+            S.D.ex[e] = (Real)(P.x[idx] + o[0]);
+            S.D.ey[e] = (Real)(P.y[idx] + o[1]);
+            S.D.ez[e] = (Real)(P.z[idx] + o[2]);
+            S.D.em[e] = (Real)P.m[idx];
+            S.D.eh[e] = (Real)P.h[idx];
         }
     }
 }
 
-// Evaluate staged P-P entries for this lane's particle.  SELF: the tile
-// holds the bucket's own particles (the first tile of every bucket), so
-// the particle's pair with itself is skipped.
+// Evaluate staged P-P entries for this lane's particle i.  SELF: the tile
+// holds the bucket's own particles (the first tile of every bucket, where
+// the own particles are entries 0..n-1), so the particle's pair with itself
+// is left out.
 template <typename Real, int NBT, bool SELF>
-__device__ __forceinline__ void eval_pp(WalkSmem<Real, NBT> &S, int cnt, int i, int slot, int pidx,
-                                        int bucketLo, Acc<Real> &A) {
-    Real xi = S.px[i], yi = S.py[i], zi = S.pz[i], hi = S.ph[i], mi = S.pm[i];
-    for (int e = slot; e < cnt; e += 32 / NBT) {
-        if constexpr (SELF) {
-            int ent = S.pp[e];
-            if ((ent & 31) == 31 && (ent >> 5) == bucketLo + i) continue;   // self
+__device__ __forceinline__ void eval_pp(WalkSmem<Real, NBT> &S, int cnt, int i, int slot, Acc<Real> &A) {
+    if constexpr (sizeof(Real) == 4) {
+        const float2 X = p_splat(S.px[i]), Y = p_splat(S.py[i]), Z = p_splat(S.pz[i]);
+        const float2 H = p_splat(S.ph[i]), M = p_splat(S.pm[i]);
+        float2 tx = p_splat(0.0f), ty = tx, tz = tx, tp = tx;   // tp: minus the potential
+        float dt = A.dt;
+        const int np = (cnt + 1) >> 1;
+        for (int p = slot; p < np; p += 32 / NBT) {
+            const float4 a = S.D.pp.xy[p], b = S.D.pp.zm[p];
+            const float2 he = S.D.pp.h[p];
+            float2 ex = make_float2(a.x, a.y), ey = make_float2(a.z, a.w);
+            float2 ez = make_float2(b.x, b.y), me = make_float2(b.z, b.w);
+            if constexpr (SELF) {
+                if (p == (i >> 1)) {   // entry i is the particle itself
+                    if (i & 1) { ex.y = ey.y = ez.y = FAR_ENTRY; me.y = 0.0f; }
+                    else { ex.x = ey.x = ez.x = FAR_ENTRY; me.x = 0.0f; }
+                }
+            }
+            // entry minus particle: the reference's dx with the sign flipped
+            const float2 dx = p_sub(ex, X), dy = p_sub(ey, Y), dz = p_sub(ez, Z);
+            const float2 d2 = p_fma(dz, dz, p_fma(dy, dy, p_mul(dx, dx)));
+            const float2 twoh = p_add(H, he);
+            const float2 dir = p_rsqrt(d2);
+            const float2 t2 = p_mul(twoh, twoh);
+            float2 av, bv;
+            if (d2.x < t2.x || d2.y < t2.y) {   // inside a softening length: SPLINEM
+                spline_m<float>(dir.x, d2.x, twoh.x, av.x, bv.x);
+                spline_m<float>(dir.y, d2.y, twoh.y, av.y, bv.y);
+            } else {
+                av = dir;
+                bv = p_mul(p_mul(dir, dir), dir);
+            }
+            const float2 idt2 = p_mul(p_add(M, me), bv);
+            dt = fmaxf(dt, fmaxf(idt2.x, idt2.y));
+            tp = p_fma(av, me, tp);
+            const float2 bm = p_mul(bv, me);
+            tx = p_fma(dx, bm, tx);
+            ty = p_fma(dy, bm, ty);
+            tz = p_fma(dz, bm, tz);
         }
-        Real ex, ey, ez, me, he;
-        if constexpr (sizeof(Real) == 4) {
-            const float4 r = S.r0[e];
-            ex = r.x; ey = r.y; ez = r.z; me = r.w;
-            he = S.rh[e];
-        } else {
-            ex = S.ex[e]; ey = S.ey[e]; ez = S.ez[e]; me = S.em[e]; he = S.eh[e];
+        A.dt = dt;
+        kahan_add2(A.s[0], A.c[0], tx);
+        kahan_add2(A.s[1], A.c[1], ty);
+        kahan_add2(A.s[2], A.c[2], tz);
+        kahan_add2(A.s[3], A.c[3], make_float2(-tp.x, -tp.y));
+    } else {
+        const Real xi = S.px[i], yi = S.py[i], zi = S.pz[i], hi = S.ph[i], mi = S.pm[i];
+        for (int e = slot; e < cnt; e += 32 / NBT) {
+            if constexpr (SELF) {
+                if (e == i) continue;   // self
+            }
+            const Real ex = S.D.ex[e], ey = S.D.ey[e], ez = S.D.ez[e], me = S.D.em[e], he = S.D.eh[e];
+            Real dx = xi - ex, dy = yi - ey, dz = zi - ez;
+            Real d2 = dx * dx + dy * dy + dz * dz;
+            Real twoh = hi + he;
+            Real dir = rsq<Real>(d2);
+            Real a, b;
+            spline_m<Real>(dir, d2, twoh, a, b);
+            Real idt2 = (mi + me) * b;
+            A.dt = idt2 > A.dt ? idt2 : A.dt;
+            a *= me;
+            b *= me;
+            A.t[3] -= a;
+            A.t[0] -= dx * b;
+            A.t[1] -= dy * b;
+            A.t[2] -= dz * b;
         }
-        Real dx = xi - ex, dy = yi - ey, dz = zi - ez;
-        Real d2 = dx * dx + dy * dy + dz * dz;
-        Real twoh = hi + he;
-        Real dir = rsq<Real>(d2);
-        Real a, b;
-        spline_m<Real>(dir, d2, twoh, a, b);
-        Real idt2 = (mi + me) * b;
-        A.dt = idt2 > A.dt ? idt2 : A.dt;
-        a *= me;
-        b *= me;
-        A.t[3] -= a;
-        A.t[0] -= dx * b;
-        A.t[1] -= dy * b;
-        A.t[2] -= dz * b;
     }
-    (void)pidx;
+}
+
+// One cell entry's FP32 record: relative COM, mass, quadrupole (trace
+// removed for Newtonian cells, SETILIST walk.c:41-48) and softening.
+__device__ __forceinline__ void cell_record(const TsphDevTree &T, int ent, bool soft, float bchx,
+                                            float bchy, float bchz, float bclx, float bcly, float bclz,
+                                            float *f) {
+    const int c = ent >> 5, r = ent & 31;
+    const float4 h4 = T.wcomh[c], l4 = T.wcoml[c];
+    const float4 m0 = T.wmom0[c], m1 = T.wmom1[c];
+    rel_pos(h4, l4, r, bchx, bchy, bchz, bclx, bcly, bclz, f[0], f[1], f[2]);
+    f[3] = m0.x;
+    float q[6] = {m0.y, m0.z, m0.w, m1.x, m1.y, m1.z};
+    if (!soft) {
+        const float tr = q[0] + q[1] + q[2];
+        q[0] -= tr / 3.0f;
+        q[1] -= tr / 3.0f;
+        q[2] -= tr / 3.0f;
+    }
+#pragma unroll
+    for (int k = 0; k < 6; ++k) f[4 + k] = q[k];
+    f[10] = m1.w;
 }
 
 // Stage cell entries (Newtonian when soft == 0, else softened).
@@ -347,156 +467,223 @@ template <typename Real, int NBT>
 __device__ __forceinline__ void stage_cells(WalkSmem<Real, NBT> &S, const int *buf, const TsphDevTree &T,
                                             int cnt, int lane, bool soft, float bchx, float bchy,
                                             float bchz, float bclx, float bcly, float bclz) {
-    for (int e = lane; e < cnt; e += 32) {
-        int ent = buf[e];
-        int c = ent >> 5, r = ent & 31;
-        Real m, q[6], hc;
-        Real cx, cy, cz;
-        if constexpr (sizeof(Real) == 4) {
-            float4 h4 = T.wcomh[c], l4 = T.wcoml[c];
-            float4 m0 = T.wmom0[c], m1 = T.wmom1[c];
-            float ohx, ohy, ohz, olx, oly, olz;
-            rep_off32(r, ohx, ohy, ohz, olx, oly, olz);
-            cx = ((h4.x - bchx) + ohx) + ((l4.x - bclx) + olx);
-            cy = ((h4.y - bchy) + ohy) + ((l4.y - bcly) + oly);
-            cz = ((h4.z - bchz) + ohz) + ((l4.z - bclz) + olz);
-            m = m0.x; q[0] = m0.y; q[1] = m0.z; q[2] = m0.w; q[3] = m1.x; q[4] = m1.y; q[5] = m1.z;
-            hc = m1.w;
-        } else {
+    if constexpr (sizeof(Real) == 4) {
+        const int np = (cnt + 1) >> 1;
+        for (int p = lane; p < np; p += 32) {
+            float f0[11], f1[11];
+            cell_record(T, buf[2 * p], soft, bchx, bchy, bchz, bclx, bcly, bclz, f0);
+            if (2 * p + 1 < cnt) {
+                cell_record(T, buf[2 * p + 1], soft, bchx, bchy, bchz, bclx, bcly, bclz, f1);
+            } else {
+#pragma unroll
+                for (int k = 0; k < 11; ++k) f1[k] = k < 3 ? FAR_ENTRY : 0.0f;
+            }
+            S.D.cn.xy[p] = make_float4(f0[0], f1[0], f0[1], f1[1]);
+            S.D.cn.zm[p] = make_float4(f0[2], f1[2], f0[3], f1[3]);
+            S.D.cn.q01[p] = make_float4(f0[4], f1[4], f0[5], f1[5]);
+            S.D.cn.q23[p] = make_float4(f0[6], f1[6], f0[7], f1[7]);
+            S.D.cn.q45[p] = make_float4(f0[8], f1[8], f0[9], f1[9]);
+            S.D.cn.h[p] = make_float2(f0[10], f1[10]);
+        }
+    } else {
+        for (int e = lane; e < cnt; e += 32) {
+            const int ent = buf[e];
+            const int c = ent >> 5, r = ent & 31;
             double o[3];
             rep_off64(r, o);
-            cx = (Real)(T.r[3 * c] + o[0]);
-            cy = (Real)(T.r[3 * c + 1] + o[1]);
-            cz = (Real)(T.r[3 * c + 2] + o[2]);
-            m = (Real)T.fMass[c];
+            Real q[6];
 #pragma unroll
             for (int k = 0; k < 6; ++k) q[k] = (Real)T.Q[6 * c + k];
-            hc = (Real)T.fSoft[c];
-        }
-        if (!soft) {   // reduced (trace-free) quadrupole, SETILIST walk.c:41-48
-            Real tr = q[0] + q[1] + q[2];
-            q[0] -= tr / Real(3.0);
-            q[1] -= tr / Real(3.0);
-            q[2] -= tr / Real(3.0);
-        }
-        if constexpr (sizeof(Real) == 4) {
-            S.r0[e] = make_float4(cx, cy, cz, m);
-            S.r1[e] = make_float4(q[0], q[1], q[2], q[3]);
-            S.r2[e] = make_float4(q[4], q[5], hc, 0.0f);
-        } else {
-            S.ex[e] = cx; S.ey[e] = cy; S.ez[e] = cz;
-            S.em[e] = m;
-            S.eh[e] = hc;
+            if (!soft) {   // reduced (trace-free) quadrupole, SETILIST walk.c:41-48
+                Real tr = q[0] + q[1] + q[2];
+                q[0] -= tr / Real(3.0);
+                q[1] -= tr / Real(3.0);
+                q[2] -= tr / Real(3.0);
+            }
+            S.D.ex[e] = (Real)(T.r[3 * c] + o[0]);
+            S.D.ey[e] = (Real)(T.r[3 * c + 1] + o[1]);
+            S.D.ez[e] = (Real)(T.r[3 * c + 2] + o[2]);
+            S.D.em[e] = (Real)T.fMass[c];
+            S.D.eh[e] = (Real)T.fSoft[c];
 #pragma unroll
-            for (int k = 0; k < 6; ++k) S.q[k][e] = q[k];
+            for (int k = 0; k < 6; ++k) S.D.q[k][e] = q[k];
         }
     }
 }
 
-// One Newtonian cell, QEVAL at order <= 2 (qeval.h:53-64): the cell's
-// acceleration and potential terms for the particle at (xi, yi, zi), with
-// its mass and g1 = 1/r^3 for the timestep criterion.
-template <typename Real, int NBT>
-__device__ __forceinline__ void newt_term(const WalkSmem<Real, NBT> &S, int e, Real xi, Real yi, Real zi,
-                                          int iOrder, Real &ax, Real &ay, Real &az, Real &pot,
-                                          Real &m, Real &g1) {
-    Real cx, cy, cz, xx, yy, zz, xy, xz, yz;
-    if constexpr (sizeof(Real) == 4) {
-        const float4 a = S.r0[e], b = S.r1[e], c = S.r2[e];
-        cx = a.x; cy = a.y; cz = a.z; m = a.w;
-        xx = b.x; yy = b.y; zz = b.z; xy = b.w; xz = c.x; yz = c.y;
-    } else {
-        cx = S.ex[e]; cy = S.ey[e]; cz = S.ez[e]; m = S.em[e];
-        xx = S.q[0][e]; yy = S.q[1][e]; zz = S.q[2][e];
-        xy = S.q[3][e]; xz = S.q[4][e]; yz = S.q[5][e];
-    }
-    Real dx = xi - cx, dy = yi - cy, dz = zi - cz;
-    Real d2 = dx * dx + dy * dy + dz * dz;
-    Real g0 = rsq<Real>(d2);
-    Real dir2 = g0 * g0;
-    g1 = g0 * dir2;
-    Real g2 = Real(3) * g1 * dir2;
-    Real g3 = Real(5) * g2 * dir2;
-    Real Qta = 0;
-    pot = 0; ax = 0; ay = 0; az = 0;
-    if (iOrder >= 2) {
-        Real Qmirx = xz * dz + xy * dy + xx * dx;
-        Real Qmiry = yz * dz + xy * dx + yy * dy;
-        Real Qmirz = yz * dy + xz * dx + zz * dz;
-        Real Qmir = Real(0.5) * (Qmirx * dx + Qmiry * dy + Qmirz * dz);
-        pot -= g2 * Qmir;
-        Qta += g3 * Qmir;
-        ax += g2 * Qmirx;
-        ay += g2 * Qmiry;
-        az += g2 * Qmirz;
-    }
-    pot -= g0 * m;
-    Qta += g1 * m;
-    ax -= dx * Qta;
-    ay -= dy * Qta;
-    az -= dz * Qta;
-}
-
-// Newtonian cells.  Far cells give O(1) terms that cancel to a small net
-// force in a periodic box: compensate each term, not only each tile.
+// Newtonian cells, QEVAL at order <= 2 (qeval.h:53-64), for the particle
+// i: acceleration, potential, and (m_i + m) / r^3 for the timestep.  FP32
+// evaluates two cells per packed instruction into tile partials that are
+// folded into the compensated sums once per tile.
 template <typename Real, int NBT>
 __device__ __forceinline__ void eval_newt(WalkSmem<Real, NBT> &S, int cnt, int i, int slot, int iOrder,
                                           Acc<Real> &A) {
-    const Real xi = S.px[i], yi = S.py[i], zi = S.pz[i], mi = S.pm[i];
-    for (int e = slot; e < cnt; e += 32 / NBT) {
-        Real ax, ay, az, pot, m, g1;
-        newt_term<Real, NBT>(S, e, xi, yi, zi, iOrder, ax, ay, az, pot, m, g1);
-        kahan_add(A.s[0], A.c[0], ax);
-        kahan_add(A.s[1], A.c[1], ay);
-        kahan_add(A.s[2], A.c[2], az);
-        A.t[3] += pot;
-        const Real idt2 = (mi + m) * g1;
-        A.dt = idt2 > A.dt ? idt2 : A.dt;
+    if constexpr (sizeof(Real) == 4) {
+        const float2 X = p_splat(S.px[i]), Y = p_splat(S.py[i]), Z = p_splat(S.pz[i]);
+        const float2 M = p_splat(S.pm[i]);
+        const float2 three = p_splat(3.0f), five = p_splat(5.0f), half = p_splat(0.5f);
+        const float2 mone = p_splat(-1.0f);
+        float2 tx = p_splat(0.0f), ty = tx, tz = tx, tp = tx;   // tp: minus the potential
+        float dt = A.dt;
+        const bool quad = iOrder >= 2;
+        const int np = (cnt + 1) >> 1;
+        for (int p = slot; p < np; p += 32 / NBT) {
+            const float4 a = S.D.cn.xy[p], b = S.D.cn.zm[p];
+            // entry minus particle: the reference's dx with the sign flipped
+            const float2 dx = p_sub(make_float2(a.x, a.y), X);
+            const float2 dy = p_sub(make_float2(a.z, a.w), Y);
+            const float2 dz = p_sub(make_float2(b.x, b.y), Z);
+            const float2 m = make_float2(b.z, b.w);
+            const float2 d2 = p_fma(dz, dz, p_fma(dy, dy, p_mul(dx, dx)));
+            const float2 g0 = p_rsqrt(d2);
+            const float2 dir2 = p_mul(g0, g0);
+            const float2 g1 = p_mul(g0, dir2);
+            float2 Qta = p_mul(g1, m);
+            tp = p_fma(g0, m, tp);
+            if (quad) {
+                const float4 q01 = S.D.cn.q01[p], q23 = S.D.cn.q23[p], q45 = S.D.cn.q45[p];
+                const float2 xx = make_float2(q01.x, q01.y), yy = make_float2(q01.z, q01.w);
+                const float2 zz = make_float2(q23.x, q23.y), xy = make_float2(q23.z, q23.w);
+                const float2 xz = make_float2(q45.x, q45.y), yz = make_float2(q45.z, q45.w);
+                const float2 g2 = p_mul(p_mul(three, g1), dir2);
+                const float2 g3 = p_mul(p_mul(five, g2), dir2);
+                // Q.r with the flipped dx: minus the reference's Qmir vector
+                const float2 qx = p_fma(xx, dx, p_fma(xy, dy, p_mul(xz, dz)));
+                const float2 qy = p_fma(yy, dy, p_fma(xy, dx, p_mul(yz, dz)));
+                const float2 qz = p_fma(zz, dz, p_fma(xz, dx, p_mul(yz, dy)));
+                const float2 qir = p_mul(half, p_fma(qz, dz, p_fma(qy, dy, p_mul(qx, dx))));
+                tp = p_fma(g2, qir, tp);
+                Qta = p_fma(g3, qir, Qta);
+                const float2 ng2 = p_mul(mone, g2);
+                tx = p_fma(ng2, qx, tx);
+                ty = p_fma(ng2, qy, ty);
+                tz = p_fma(ng2, qz, tz);
+            }
+            tx = p_fma(dx, Qta, tx);
+            ty = p_fma(dy, Qta, ty);
+            tz = p_fma(dz, Qta, tz);
+            const float2 idt2 = p_mul(p_add(M, m), g1);
+            dt = fmaxf(dt, fmaxf(idt2.x, idt2.y));
+        }
+        A.dt = dt;
+        kahan_add2(A.s[0], A.c[0], tx);
+        kahan_add2(A.s[1], A.c[1], ty);
+        kahan_add2(A.s[2], A.c[2], tz);
+        kahan_add2(A.s[3], A.c[3], make_float2(-tp.x, -tp.y));
+    } else {
+        const Real xi = S.px[i], yi = S.py[i], zi = S.pz[i], mi = S.pm[i];
+        for (int e = slot; e < cnt; e += 32 / NBT) {
+            const Real cx = S.D.ex[e], cy = S.D.ey[e], cz = S.D.ez[e], m = S.D.em[e];
+            const Real xx = S.D.q[0][e], yy = S.D.q[1][e], zz = S.D.q[2][e];
+            const Real xy = S.D.q[3][e], xz = S.D.q[4][e], yz = S.D.q[5][e];
+            Real dx = xi - cx, dy = yi - cy, dz = zi - cz;
+            Real d2 = dx * dx + dy * dy + dz * dz;
+            Real g0 = rsq<Real>(d2);
+            Real dir2 = g0 * g0;
+            Real g1 = g0 * dir2;
+            Real g2 = Real(3) * g1 * dir2;
+            Real g3 = Real(5) * g2 * dir2;
+            Real Qta = 0, pot = 0, ax = 0, ay = 0, az = 0;
+            if (iOrder >= 2) {
+                Real Qmirx = xz * dz + xy * dy + xx * dx;
+                Real Qmiry = yz * dz + xy * dx + yy * dy;
+                Real Qmirz = yz * dy + xz * dx + zz * dz;
+                Real Qmir = Real(0.5) * (Qmirx * dx + Qmiry * dy + Qmirz * dz);
+                pot -= g2 * Qmir;
+                Qta += g3 * Qmir;
+                ax += g2 * Qmirx;
+                ay += g2 * Qmiry;
+                az += g2 * Qmirz;
+            }
+            pot -= g0 * m;
+            Qta += g1 * m;
+            ax -= dx * Qta;
+            ay -= dy * Qta;
+            az -= dz * Qta;
+            A.s[0] += ax;
+            A.s[1] += ay;
+            A.s[2] += az;
+            A.t[3] += pot;
+            const Real idt2 = (mi + m) * g1;
+            A.dt = idt2 > A.dt ? idt2 : A.dt;
+        }
     }
 }
 
-// Softened cells with the full quadrupole (grav.c:126-150).
+// Softened cells with the full quadrupole (grav.c:126-150): one term of
+// the particle at (xi, yi, zi) from cell (c, m, q, hc).
+template <typename Real>
+__device__ __forceinline__ void soft_term(Real xi, Real yi, Real zi, Real hi, Real mi, Real cx, Real cy,
+                                          Real cz, Real m, Real xx, Real yy, Real zz, Real xy, Real xz,
+                                          Real yz, Real hc, Real &ax, Real &ay, Real &az, Real &pot,
+                                          Real &idt2) {
+    Real dx = xi - cx, dy = yi - cy, dz = zi - cz;
+    Real d2 = dx * dx + dy * dy + dz * dz;
+    Real twoh = hi + hc;
+    Real dir = rsq<Real>(d2);
+    Real a, b, c, d;
+    spline_q<Real>(dir, d2, twoh, a, b, c, d);
+    Real qirx = xx * dx + xy * dy + xz * dz;
+    Real qiry = xy * dx + yy * dy + yz * dz;
+    Real qirz = xz * dx + yz * dy + zz * dz;
+    Real qir = Real(0.5) * (qirx * dx + qiry * dy + qirz * dz);
+    Real tr = Real(0.5) * (xx + yy + zz);
+    Real qir3 = b * m + d * qir - c * tr;
+    pot = -(a * m + c * qir - b * tr);
+    ax = -(qir3 * dx - c * qirx);
+    ay = -(qir3 * dy - c * qiry);
+    az = -(qir3 * dz - c * qirz);
+    idt2 = (mi + m) * b;
+}
+
 template <typename Real, int NBT>
 __device__ __forceinline__ void eval_soft(WalkSmem<Real, NBT> &S, int cnt, int i, int slot, Acc<Real> &A) {
-    Real xi = S.px[i], yi = S.py[i], zi = S.pz[i], hi = S.ph[i], mi = S.pm[i];
-    for (int e = slot; e < cnt; e += 32 / NBT) {
-        Real cx, cy, cz, m, xx, yy, zz, xy, xz, yz, hc;
-        if constexpr (sizeof(Real) == 4) {
-            const float4 r0 = S.r0[e], r1 = S.r1[e], r2 = S.r2[e];
-            cx = r0.x; cy = r0.y; cz = r0.z; m = r0.w;
-            xx = r1.x; yy = r1.y; zz = r1.z; xy = r1.w; xz = r2.x; yz = r2.y; hc = r2.z;
-        } else {
-            cx = S.ex[e]; cy = S.ey[e]; cz = S.ez[e]; m = S.em[e]; hc = S.eh[e];
-            xx = S.q[0][e]; yy = S.q[1][e]; zz = S.q[2][e];
-            xy = S.q[3][e]; xz = S.q[4][e]; yz = S.q[5][e];
+    const Real xi = S.px[i], yi = S.py[i], zi = S.pz[i], hi = S.ph[i], mi = S.pm[i];
+    if constexpr (sizeof(Real) == 4) {
+        const int np = (cnt + 1) >> 1;
+        for (int p = slot; p < np; p += 32 / NBT) {
+            const float4 a = S.D.cn.xy[p], b = S.D.cn.zm[p];
+            const float4 q01 = S.D.cn.q01[p], q23 = S.D.cn.q23[p], q45 = S.D.cn.q45[p];
+            const float2 h = S.D.cn.h[p];
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                float ax, ay, az, pot, idt2;
+                soft_term<float>(xi, yi, zi, hi, mi, k ? a.y : a.x, k ? a.w : a.z, k ? b.y : b.x,
+                                 k ? b.w : b.z, k ? q01.y : q01.x, k ? q01.w : q01.z,
+                                 k ? q23.y : q23.x, k ? q23.w : q23.z, k ? q45.y : q45.x,
+                                 k ? q45.w : q45.z, k ? h.y : h.x, ax, ay, az, pot, idt2);
+                kahan_add(A.s[0], A.c[0], ax);
+                kahan_add(A.s[1], A.c[1], ay);
+                kahan_add(A.s[2], A.c[2], az);
+                kahan_add(A.s[3], A.c[3], pot);
+                A.dt = fmaxf(A.dt, idt2);
+            }
         }
-        Real dx = xi - cx, dy = yi - cy, dz = zi - cz;
-        Real d2 = dx * dx + dy * dy + dz * dz;
-        Real twoh = hi + hc;
-        Real dir = rsq<Real>(d2);
-        Real a, b, c, d;
-        spline_q<Real>(dir, d2, twoh, a, b, c, d);
-        Real qirx = xx * dx + xy * dy + xz * dz;
-        Real qiry = xy * dx + yy * dy + yz * dz;
-        Real qirz = xz * dx + yz * dy + zz * dz;
-        Real qir = Real(0.5) * (qirx * dx + qiry * dy + qirz * dz);
-        Real tr = Real(0.5) * (xx + yy + zz);
-        Real qir3 = b * m + d * qir - c * tr;
-        A.t[3] -= a * m + c * qir - b * tr;
-        kahan_add(A.s[0], A.c[0], -(qir3 * dx - c * qirx));
-        kahan_add(A.s[1], A.c[1], -(qir3 * dy - c * qiry));
-        kahan_add(A.s[2], A.c[2], -(qir3 * dz - c * qirz));
-        Real idt2 = (mi + m) * b;
-        A.dt = idt2 > A.dt ? idt2 : A.dt;
+    } else {
+        for (int e = slot; e < cnt; e += 32 / NBT) {
+            Real ax, ay, az, pot, idt2;
+            soft_term<Real>(xi, yi, zi, hi, mi, S.D.ex[e], S.D.ey[e], S.D.ez[e], S.D.em[e],
+                            S.D.q[0][e], S.D.q[1][e], S.D.q[2][e], S.D.q[3][e], S.D.q[4][e],
+                            S.D.q[5][e], S.D.eh[e], ax, ay, az, pot, idt2);
+            A.s[0] += ax;
+            A.s[1] += ay;
+            A.s[2] += az;
+            A.t[3] += pot;
+            A.dt = idt2 > A.dt ? idt2 : A.dt;
+        }
     }
 }
 
+// FP64: add the tile partial to the running sums.  FP32 tiles fold their
+// packed partials themselves.
 template <typename Real>
 __device__ __forceinline__ void flush_tile(Acc<Real> &A) {
+    if constexpr (sizeof(Real) == 8) {
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        kahan_add(A.s[k], A.c[k], A.t[k]);
-        A.t[k] = 0;
+        for (int k = 0; k < 4; ++k) {
+            A.s[k] += A.t[k];
+            A.t[k] = 0;
+        }
     }
 }
 
@@ -724,8 +911,8 @@ __device__ __forceinline__ void walk_bucket(const WalkArgs &W, WalkSmem<Real, NB
             stage_pp<Real, NBT>(S, P, PPF, lane, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
             __syncwarp();
             if (i < n) {
-                if (ppSelf) eval_pp<Real, NBT, true>(S, PPF, i, slot, lo + i, lo, A);
-                else eval_pp<Real, NBT, false>(S, PPF, i, slot, lo + i, lo, A);
+                if (ppSelf) eval_pp<Real, NBT, true>(S, PPF, i, slot, A);
+                else eval_pp<Real, NBT, false>(S, PPF, i, slot, A);
             }
             ppSelf = false;
             flush_tile(A);
@@ -765,8 +952,8 @@ __device__ __forceinline__ void walk_bucket(const WalkArgs &W, WalkSmem<Real, NB
         stage_pp<Real, NBT>(S, P, ppn, lane, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
         __syncwarp();
         if (i < n) {
-            if (ppSelf) eval_pp<Real, NBT, true>(S, ppn, i, slot, lo + i, lo, A);
-            else eval_pp<Real, NBT, false>(S, ppn, i, slot, lo + i, lo, A);
+            if (ppSelf) eval_pp<Real, NBT, true>(S, ppn, i, slot, A);
+            else eval_pp<Real, NBT, false>(S, ppn, i, slot, A);
         }
         flush_tile(A);
         __syncwarp();

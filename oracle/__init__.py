@@ -261,6 +261,21 @@ def reference_sph_active(pos, vel, mass, soft, u, rung, iRung, sp):
                 mumax=f[:, 3].copy(), dt=f[:, 4].copy(), fDensity=f[:, 5].copy())
 
 
+def reference_knn_sets(pos, mass, soft, sp):
+    """The reference's own smSmooth kNN sets (ref_knn_sets in the harness):
+    per particle the nnList size, the order-independent hash of its members'
+    input indices (the oracle's and the CUDA path's neighbour hash) and fBall2."""
+    lib = reference().lib
+    pos = _c64(pos, (-1, 3)); mass = _c64(mass); soft = _c64(soft)
+    n = len(mass)
+    hsh = np.zeros(n, dtype=np.uint64)
+    cnt = np.zeros(n, dtype=np.int32)
+    fb = np.zeros(n)
+    lib.ref_knn_sets(n, _d(pos), _d(mass), _d(soft), ctypes.byref(sp), hsh.ctypes.data_as(_UP),
+                     cnt.ctypes.data_as(_IP), _d(fb))
+    return dict(nbr_hash=hsh, nbr_count=cnt, fBall2=fb)
+
+
 def reference_render_tsc(pos, mass, soft, fBall2, fDensity, ngas, nstar, rp):
     """The reference's dfRenderParticles (TSC) frame: float32 (ny, nx, 3)."""
     lib = reference().lib

@@ -262,6 +262,61 @@ typedef struct {
  *                  diff, PoverRho2, c, a_hydro[3], uDotPdV, uDotAV
  *   dtNew[i], mumax[i].
  */
+/* The reference's own kNN sets: smSmooth (SMX_DENDVDX set-up, density
+ * tree as in ref_sph) with its smooth callback replaced by one that records,
+ * per particle, how many entries nnList holds and a hash of their input
+ * indices -- the same order-independent hash (sum over the set of a 64-bit
+ * mix of iOrder + 1) that the oracle and the CUDA path report -- and the
+ * fBall2 smSmooth set.  The post-pass callback is dropped too: nothing was
+ * accumulated for it to normalise. */
+static unsigned long long *g_knn_hash;
+static int *g_knn_cnt;
+
+static void knn_hash_fcn(PARTICLE *p, int nSmooth, NN *nnList, SMF *smf)
+{
+    unsigned long long h = 0;
+    int i;
+    (void)smf;
+    for (i = 0; i < nSmooth; ++i) {
+        unsigned long long x = (unsigned long long)(nnList[i].pPart->iOrder + 1);
+        x *= 0x9E3779B97F4A7C15ULL;
+        x ^= x >> 29;
+        x *= 0xBF58476D1CE4E5B9ULL;
+        x ^= x >> 32;
+        h += x;
+    }
+    g_knn_hash[p->iOrder] = h;
+    g_knn_cnt[p->iOrder] = nSmooth;
+}
+
+int ref_knn_sets(int n, const double *pos, const double *mass, const double *soft,
+                 const ref_sph_params *sp, unsigned long long *hash, int *cnt, double *fBall2)
+{
+    PKD pkd = make_pkd(n, pos, mass, soft, sp->bPeriodic, sp->dPeriod, 2, 1);
+    KDN root;
+    SMX smx;
+    SMF smf;
+    CASTAT cs;
+    int i;
+    memset(&smf, 0, sizeof(smf));
+    smf.a = 1.0;
+    smf.bCannonical = 1;
+    g_knn_hash = hash;
+    g_knn_cnt = cnt;
+    pkdBuildLocal(pkd, sp->nBucket, OPEN_JOSH, 0.7, 2, 1, 0, &root);
+    make_top(pkd, &root);
+    smInitialize(&smx, pkd, &smf, sp->nSmooth, sp->bPeriodic, 1, SMX_DENDVDX, 1, 0.0);
+    smx->fcnSmooth = knn_hash_fcn;
+    smx->fcnPost = NULL;
+    smSmooth(smx, &smf);
+    smFinish(smx, &smf, &cs);
+    for (i = 0; i < n; ++i) fBall2[pkd->pStore[i].iOrder] = pkd->pStore[i].fBall2;
+    pkdFinish(pkd);
+    g_knn_hash = NULL;
+    g_knn_cnt = NULL;
+    return 0;
+}
+
 int ref_sph(int n, const double *pos, const double *vel, const double *mass,
             const double *soft, const double *u, const ref_sph_params *sp,
             double *out, double *dtNew, double *mumax)

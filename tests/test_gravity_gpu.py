@@ -129,23 +129,38 @@ def test_plummer_32k_vs_oracle(ctx, orc, prec):
 @pytest.fixture(scope="module")
 def box64(orc):
     """The 64^3 periodic box (262,144 particles, the headline construction
-    at an eighth of its size) and the oracle's evaluation of it with the
-    reference's own arithmetic (v_sqrt1), nBucket 16."""
+    at an eighth of its size) and the oracle's evaluations of it, nBucket
+    16: with the reference's own 1/sqrt (v_sqrt1) and with an exact one."""
     pos, vel, m = g.ics.lattice_box(64, seed=2)
     soft = np.full(len(m), 1.0 / (50 * 64))
-    ref = orc.grav(pos, m, soft, oracle.grav_params(periodic=True, nBucket=16),
-                   nthreads=os.cpu_count() or 1)
-    return pos, m, soft, ref
+    gp = oracle.grav_params(periodic=True, nBucket=16)
+    nth = os.cpu_count() or 1
+    ref = orc.grav(pos, m, soft, gp, nthreads=nth)
+    with oracle.exact_rsqrt():
+        ref_exact = orc.grav(pos, m, soft, gp, nthreads=nth)
+    return pos, m, soft, ref, ref_exact
+
+
+# At 64^3 the reference's v_sqrt1 moves the oracle's periodic accelerations
+# by 3.0e-8 rms and its potential by 1.3e-7 of max |pot| from those with an
+# exact 1/sqrt (the near-cancelling replica and Ewald sums amplify its
+# 2e-10 per-term error with N).  The CUDA FP64 path computes an exact
+# 1/sqrt, so it is held to the exact-1/sqrt oracle; against the reference's
+# arithmetic the bar is that measured gap with a margin.
+BOX64_FP64_VS_EXACT = 1e-11
+BOX64_FP64_VS_REF_RMS = 5e-8
+BOX64_POT_VS_REF = 2e-7
 
 
 @pytest.mark.parametrize("prec", [g.FP64, g.FP32])
 def test_periodic_box_64_vs_oracle(ctx, box64, prec):
     """At 262,144 particles: pkdGravAll's counters (active particles, P-P,
     Newtonian and softened cell interactions) equal the oracle's exactly and
-    its flop count to 1e-12; FP64 accelerations within the periodic bar
-    against the reference's arithmetic and the potential within 1e-7 of
-    max |pot|; FP32 p99 within the periodic FP32 bar."""
-    pos, m, soft, ref = box64
+    its flop count to 1e-12 (FP64; the FP32 Ewald tests its real-space cut
+    in FP32); FP64 accelerations and potentials within 1e-11 (rms) of the
+    exact-1/sqrt oracle and within the v_sqrt1 gap of the reference's
+    arithmetic; FP32 p99 within the periodic FP32 bar."""
+    pos, m, soft, ref, ref_exact = box64
     gp = g.grav_params(periodic=True, precision=prec, nBucket=16)
     r = run(ctx, pos, m, soft, gp)
     c, o = ref["counters"], r["out"]
@@ -153,12 +168,14 @@ def test_periodic_box_64_vs_oracle(ctx, box64, prec):
     assert o["dPartSum"] == c[1]
     assert o["dCellSum"] == c[2]
     assert o["dSoftSum"] == c[3]
-    assert o["dFlop"] == pytest.approx(c[4], rel=1e-12)
-    e = rel_err(r["acc"], ref["acc"])
+    e = rel_err(r["acc"], ref_exact["acc"])
     if prec == g.FP64:
-        assert rms(e) < PER_FP64_VS_REF_RMS, (rms(e), e.max())
-        ep = np.abs(r["pot"] - ref["pot"]) / np.abs(ref["pot"]).max()
-        assert ep.max() < PER_POT_VS_REF_SCALED, ep.max()
+        assert o["dFlop"] == pytest.approx(c[4], rel=1e-12)
+        pmax = np.abs(ref_exact["pot"]).max()
+        assert rms(e) < BOX64_FP64_VS_EXACT, (rms(e), e.max())
+        assert rms((r["pot"] - ref_exact["pot"]) / pmax) < BOX64_FP64_VS_EXACT
+        assert rms(rel_err(r["acc"], ref["acc"])) < BOX64_FP64_VS_REF_RMS
+        assert np.max(np.abs(r["pot"] - ref["pot"])) / pmax < BOX64_POT_VS_REF
     else:
         assert np.percentile(e, 99) < PER_FP32_P99, np.percentile(e, 99)
 
