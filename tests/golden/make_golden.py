@@ -50,6 +50,27 @@ def sph_case(name, pos, vel, mass, soft, u, sp):
     print(name, len(mass))
 
 
+def sph_box_case():
+    """Periodic SPH: a 16^3 gas lattice in the unit box displaced by a
+    Gaussian random field (rms 0.25 of the spacing), velocities from the
+    displacements plus noise, u spread over [0.05, 0.15]; nSmooth 32, so
+    most balls reach through a face of the box.  Besides ref_sph's fields
+    the reference's own kNN sets are stored (ref_knn_sets: nnList size and
+    member hash per particle)."""
+    pos, vel, m = ics.lattice_box(16, seed=34, rms_frac=0.25)
+    n = len(m)
+    rng = np.random.default_rng(35)
+    vel = vel * 50.0 + rng.normal(0.0, 0.05, (n, 3))
+    u = rng.uniform(0.05, 0.15, n)
+    soft = np.full(n, 0.001)
+    sp = oracle.sph_params(nSmooth=32, periodic=True, L=1.0)
+    sph_case("sph_box_16", pos, vel, m, soft, u, sp)
+    k = oracle.reference_knn_sets(pos, m, soft, sp)
+    d = dict(np.load(os.path.join(HERE, "sph_box_16.npz")))
+    np.savez_compressed(os.path.join(HERE, "sph_box_16.npz"), **d, knn_hash=k["nbr_hash"],
+                        knn_count=k["nbr_count"])
+
+
 def tipsy_fields(ng, nd, ns, seed):
     """Seeded particles of every Tipsy type; a few values sit on float
     rounding edges (subnormal, -0.0, near FLT_MAX, halfway between floats)."""
@@ -160,19 +181,23 @@ def main():
     vel = rng.normal(0.0, 0.1, (len(m), 3))
     sph_case("sph_sphere_2k", pos, vel, m, np.full(len(m), 0.01), u,
              oracle.sph_params(nSmooth=32))
+    sph_box_case()
     tipsy_case("tipsy_mixed", 300, 500, 200, seed=16)
     multistep_cases()
     render_case()
 
 
 if __name__ == "__main__":
-    if len(sys.argv) > 1 and sys.argv[1] in ("tipsy", "multistep", "render"):
+    # one group of fixtures only: python make_golden.py tipsy|multistep|render|sph_box
+    if len(sys.argv) > 1 and sys.argv[1] in ("tipsy", "multistep", "render", "sph_box"):
         if not oracle.reference_available():
             oracle.build_reference()
         if sys.argv[1] == "tipsy":
             tipsy_case("tipsy_mixed", 300, 500, 200, seed=16)
         elif sys.argv[1] == "multistep":
             multistep_cases()
+        elif sys.argv[1] == "sph_box":
+            sph_box_case()
         else:
             render_case()
     else:

@@ -9,7 +9,8 @@ import numpy as np
 import pytest
 
 import oracle
-from golden_io import GRAV_CASES, grav_params_of, load, rel_err, sph_params_of
+from golden_io import (GRAV_CASES, check_periodic_sph_vs_golden, grav_params_of, load,
+                       rel_err, sph_params_of)
 
 
 @pytest.mark.parametrize("name", GRAV_CASES)
@@ -60,6 +61,19 @@ def test_oracle_sph_matches_reference(orc):
     assert np.array_equal(r["mumax"], d["mumax"])
     # the kNN neighbour count: exactly nSmooth for tie-free input
     assert (r["nbr_count"] == 32).all()
+
+
+def test_oracle_periodic_sph_matches_reference(orc):
+    """Periodic SPH (most balls reach through a face of the box): the
+    oracle's kNN sets equal the reference's own for every particle; fBall2
+    agrees to the reference's re-centring rounding, the SPH fields to 1e-12
+    of scale, dtNew and mumax apart from the reference's edge pairs (the
+    bars and their reasons are in golden_io)."""
+    d = load("sph_box_16")
+    sp = sph_params_of(d, oracle)
+    r = orc.sph(d["pos"], d["vel"], d["mass"], d["soft"], d["u"], sp)
+    assert (r["nbr_count"] == 32).all()
+    check_periodic_sph_vs_golden(r, d, oracle.SPH_FIELDS, 1e-12, r["nbr_hash"])
 
 
 def test_oracle_v_sqrt1_accuracy():

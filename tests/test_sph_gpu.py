@@ -11,7 +11,7 @@ import pytest
 
 import gasoline_gb300 as g
 import oracle
-from golden_io import load, sph_params_of
+from golden_io import PSPH_FBALL2_REL, check_periodic_sph_vs_golden, load, sph_params_of
 
 pytestmark = pytest.mark.gpu
 
@@ -66,6 +66,30 @@ def test_sph_sphere_vs_oracle(ctx, orc, n, seed):
     assert np.array_equal(cnt, np.full(n, 32))
     # N(i) from the ball gather equals the oracle's exact kNN set
     assert np.array_equal(hsh, ref["nbr_hash"])
+
+
+@pytest.mark.parametrize("prec", [g.FP64, g.FP32])
+def test_sph_periodic_vs_reference_golden(ctx, prec):
+    """Periodic SPH against the reference's own output (sph_box_16): the
+    neighbour sets equal the reference's kNN sets for every particle in FP64
+    and FP32; fBall2 within the reference's re-centring rounding (a few
+    ulps); FP64 fields within 1e-10 of scale, FP32 within 2e-5; dtNew and
+    mumax apart from the reference's edge pairs (golden_io states why)."""
+    d = load("sph_box_16")
+    sp = sph_params_of(d, g, precision=prec)
+    r = run(ctx, d["pos"], d["vel"], d["mass"], d["soft"], d["u"], sp)
+    cnt, hsh = ctx.get_neighbour_hash()
+    assert np.array_equal(cnt, np.full(len(cnt), 32))
+    if prec == g.FP64:
+        check_periodic_sph_vs_golden(r, d, FIELDS, REL, hsh)
+    else:
+        assert np.array_equal(hsh, d["knn_hash"])
+        fb = d["out"][:, 0]
+        assert np.max(np.abs(r["fBall2"] - fb) / fb) <= PSPH_FBALL2_REL
+        for k, name in enumerate(FIELDS):
+            ref = d["out"][:, k]
+            if name != "fBall2":
+                assert np.max(np.abs(r[name] - ref)) <= 2e-5 * np.max(np.abs(ref)), name
 
 
 def test_sph_periodic_box_vs_oracle(ctx, orc):
