@@ -85,6 +85,28 @@ class Tuning(ctypes.Structure):
                 ("walkGroup", ctypes.c_int), ("reserved", ctypes.c_int * 5)]
 
 
+STORE_INT_FIELDS = ("r", "fMass", "fSoft", "v", "vPred", "u", "uPred", "a", "fPot", "dtGrav",
+                    "fBall2", "fDensity", "divv", "curlv", "dvds", "BalsaraSwitch", "diff",
+                    "PoverRho2", "c", "uDotPdV", "uDotAV", "mumax", "dtNew", "iActive")
+
+
+class StoreLayout(ctypes.Structure):
+    """tsph_store_layout (include/tsph.h): stride and byte offsets of the
+    fields of a particle store laid out as the reference's PARTICLE."""
+    _fields_ = ([("stride", ctypes.c_longlong)] + [(k, ctypes.c_int) for k in STORE_INT_FIELDS] +
+                [("activeBit", ctypes.c_uint), ("reserved", ctypes.c_int * 6)])
+
+
+def store_layout(offsets):
+    """A StoreLayout from a dict of offsets (missing fields: -1)."""
+    L = StoreLayout()
+    L.stride = int(offsets["stride"])
+    for k in STORE_INT_FIELDS:
+        setattr(L, k, int(offsets.get(k, -1)))
+    L.activeBit = int(offsets.get("activeBit", 1))
+    return L
+
+
 class StepParams(ctypes.Structure):
     """tsph_step_params: adaptive-timestep criteria (the reference's defaults,
     master.c:572-623)."""
@@ -208,7 +230,8 @@ def load():
                  "tsph_write_tipsy", "tsph_get_snapshot_fields",
                  "tsph_set_snapshot_fields", "tsph_kick_rung", "tsph_top_step_kdk",
                  "tsph_set_active_rung", "tsph_set_rungs", "tsph_get_rungs", "tsph_render_tsc",
-                 "tsph_update_particles"):
+                 "tsph_update_particles", "tsph_store_register", "tsph_store_unregister",
+                 "tsph_store_load", "tsph_store_put_gravity", "tsph_store_put_sph"):
         getattr(lib, name).restype = ctypes.c_int
     lib.tsph_destroy.restype = None
     _lib = lib
@@ -544,6 +567,37 @@ class Context:
     def step_status(self):
         """Wait for queued steps; raise on the first error they raised."""
         self._check(self.lib.tsph_step_status(self._ctx))
+
+    # --- a particle store in the reference's PARTICLE layout (numpy
+    # structured arrays here) ---
+    def store_register(self, store):
+        self._check(self.lib.tsph_store_register(self._ctx, ctypes.c_void_p(store.ctypes.data),
+                                                 ctypes.c_size_t(store.nbytes)))
+
+    def store_unregister(self, store):
+        self._check(self.lib.tsph_store_unregister(self._ctx, ctypes.c_void_p(store.ctypes.data)))
+
+    @staticmethod
+    def _order(order):
+        if order is None:
+            return None, None
+        o = np.ascontiguousarray(order, dtype=np.int32)
+        return o, o.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+
+    def store_load(self, store, layout, order=None, ngas=0):
+        o, op = self._order(order)
+        self._check(self.lib.tsph_store_load(self._ctx, len(store), ctypes.c_void_p(store.ctypes.data),
+                                             ctypes.byref(layout), op, int(ngas)))
+
+    def store_put_gravity(self, store, layout, order=None):
+        o, op = self._order(order)
+        self._check(self.lib.tsph_store_put_gravity(self._ctx, ctypes.c_void_p(store.ctypes.data),
+                                                    ctypes.byref(layout), op))
+
+    def store_put_sph(self, which, store, layout, order=None):
+        o, op = self._order(order)
+        self._check(self.lib.tsph_store_put_sph(self._ctx, int(which), ctypes.c_void_p(store.ctypes.data),
+                                                ctypes.byref(layout), op))
 
     def set_tuning(self, taskSize=0, walkBlocksPerSM=0, walkGroup=0):
         t = Tuning(taskSize, walkBlocksPerSM, walkGroup)

@@ -111,6 +111,7 @@ extern "C" void tsph_destroy(tsph_ctx *ctx) {
     FREE(ctx->dAux); FREE(ctx->dStepStatus);
     FREE(ctx->dGroupFlag); FREE(ctx->dGroupScan); FREE(ctx->dGroupFirst); FREE(ctx->dGroupCount);
     FREE(ctx->dGroupScratch);
+    FREE(ctx->dStore); FREE(ctx->dStoreOrder);
     tsph_free_snapshot(ctx);
     free(ctx->hSys);
     free(ctx->hTmp);
@@ -258,6 +259,17 @@ int tsph_load_begin(tsph_ctx *ctx, int n) {
     ctx->T.lastTopLevels = ctx->TG.lastTopLevels = 0;   // a new particle set: no depth known
     if (n == 0) return TSPH_OK;
     return tsph_set_ranges(ctx, ctx->P, ctx->T, n, 1, &n);
+}
+
+// The caller-order state of a new particle set from interleaved positions
+// already in the staging buffer (k_load_state); masses, softenings and the
+// rest are the caller's to fill.
+int tsph_load_state_from_stage(tsph_ctx *ctx, int n) {
+    if (n <= 0) return TSPH_OK;
+    k_load_state<<<tsph_blocks(n, 256), 256, 0, ctx->stream>>>(n, ctx->dStage, ctx->C, ctx->P.iord,
+                                                               ctx->G.iord);
+    TSPH_LAUNCH_CK("k_load_state");
+    return TSPH_OK;
 }
 
 extern "C" int tsph_set_particles(tsph_ctx *ctx, int n, const double *pos, const double *mass,

@@ -189,6 +189,11 @@ struct tsph_ctx {
     long long graphKernels;      // kernel launches recorded in the graph
     long long graphSysVersion;
     long long sysVersion;        // bumped by every particle / system change
+    // the reference-layout particle store (store.cu)
+    unsigned long long storeKey; // store, n and order of the last tsph_store_load
+    char *dStore;                // device copy of an unregistered store
+    size_t storeCap;
+    int *dStoreOrder;            // store entry of every caller index
 
     cudaEvent_t ev[10];
     float timings[8];
@@ -233,6 +238,7 @@ int tsph_load_begin(tsph_ctx *ctx, int n);
 int tsph_kick_launch(tsph_ctx *ctx, int iRung, double dt, int bClose);
 int tsph_drift_launch(tsph_ctx *ctx, double dt, int bPeriodic, double dPeriod);
 int tsph_load_gas(tsph_ctx *ctx, int ngas);
+int tsph_load_state_from_stage(tsph_ctx *ctx, int n);
 void tsph_free_snapshot(tsph_ctx *ctx);
 int tsph_fold_status(tsph_ctx *ctx);
 int tsph_copy_out(tsph_ctx *ctx, const double *a0, const double *a1, const double *a2, int comp,

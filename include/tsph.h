@@ -177,6 +177,67 @@ int tsph_set_velocities(tsph_ctx *ctx, const double *vel, int ngas,
  * the reference runs such systems as separate jobs. */
 int tsph_set_systems(tsph_ctx *ctx, int nSys, const int *sysOf);
 
+/* --- the reference's particle store ----------------------------------------
+ * The reference keeps its particles in one array of PARTICLE structs
+ * (pkd.h:90-225, pkd->pStore) and its kernels read and write their fields
+ * in place.  These calls do the same from the store's layout: its stride
+ * and the byte offsets of the fields, as offsetof(PARTICLE, ...) gives them
+ * in code compiled against the reference's pkd.h (gasoline_gb300/pkd/
+ * tsph_pkd.c does so).  Doubles on 8-byte boundaries; an offset < 0 marks a
+ * field the store does not have.  Caller particle i is store entry order[i]
+ * (order NULL: entry i); order must name each of the entries 0..n-1 once,
+ * and the first ngas of that order are the gas.
+ * A store registered with tsph_store_register (pinned and mapped) is read
+ * and written in place by the GPU, field by field; otherwise the load
+ * copies the n entries to the device in one block and the results are
+ * written back by the host. */
+typedef struct {
+    long long stride;          /* bytes per entry: sizeof(PARTICLE) */
+    /* inputs (doubles): positions r[3], fMass, fSoft, and for gas loads
+     * v[3], vPred[3], u, uPred (a store without vPred/uPred predicts them
+     * as v/u, as tsph_set_velocities does) */
+    int r, fMass, fSoft, v, vPred, u, uPred;
+    /* gravity outputs: a[3] +=, fPot +=, dtGrav = max (pkdGravAll) */
+    int a, fPot, dtGrav;
+    /* density-pass outputs (set): fBall2, fDensity, divv, curlv[3], dvds,
+     * BalsaraSwitch, diff (DenDVDX) */
+    int fBall2, fDensity, divv, curlv, dvds, BalsaraSwitch, diff;
+    /* pressure-pass outputs: PoverRho2, c, uDotPdV, uDotAV, mumax (set),
+     * a[3] += hydro acceleration, dtNew = min (pkdGasPressure +
+     * SphPressureTermsSym) */
+    int PoverRho2, c, uDotPdV, uDotAV, mumax, dtNew;
+    /* unsigned int activity word; entries with (word & activeBit) set are
+     * active (the reference's iActive & TYPE_ACTIVE); < 0: all active */
+    int iActive;
+    unsigned int activeBit;
+    int reserved[6];
+} tsph_store_layout;
+
+/* Pin and map `bytes` of host memory holding a store (cudaHostRegister)
+ * so the GPU reads and writes it in place; once per store, before the
+ * loads.  tsph_store_unregister undoes it. */
+int tsph_store_register(tsph_ctx *ctx, void *store, size_t bytes);
+int tsph_store_unregister(tsph_ctx *ctx, void *store);
+/* Load n particles from the store: positions, masses, softenings, and when
+ * layout->v >= 0 velocities and the first ngas particles' gas fields;
+ * active particles (activity word) are the ones the force passes act on.
+ * A load of the same store with the same n and ngas as the last one is an
+ * update of the same particles (caller index i names the same particle,
+ * wherever order puts it in the store now) and keeps the particle order of
+ * the last tree, as tsph_update_particles does; any other is a new particle
+ * set, as tsph_set_particles + tsph_set_velocities make it. */
+int tsph_store_load(tsph_ctx *ctx, int n, const void *store,
+                    const tsph_store_layout *layout, const int *order, int ngas);
+/* The last tsph_grav_all's results into the store, as pkdGravAll leaves
+ * them (active particles: a[3] += acc, fPot += pot, dtGrav = max). */
+int tsph_store_put_gravity(tsph_ctx *ctx, void *store, const tsph_store_layout *layout,
+                           const int *order);
+/* The last tsph_smooth pass's results into the store's gas entries: which
+ * = TSPH_SMX_DENDVDX (or TSPH_SMX_DENSITY) writes the density-pass fields,
+ * TSPH_SMX_SPHPRESSURETERMS the pressure-pass fields of the active gas. */
+int tsph_store_put_sph(tsph_ctx *ctx, int which, void *store, const tsph_store_layout *layout,
+                       const int *order);
+
 /* --- gravity (pkdGravAll) -------------------------------------------- */
 
 /* Build the gravity tree over the loaded particles and compute every

@@ -182,6 +182,21 @@ def oracle():
     return _oracle
 
 
+_ADAPT = os.path.join(HERE, "_ref", "libgasadapt.so")
+_adapt = None
+
+
+def adapter():
+    """The reference harness with its gravity and SPH calls made through the
+    reference-side binding of libtsph (gasoline_gb300/pkd/tsph_pkd.c) and a
+    CPU stand-in of libtsph whose arithmetic is the oracle's
+    (adapter_fake_tsph.c); None where the reference was not built."""
+    global _adapt
+    if _adapt is None and os.path.exists(_ADAPT):
+        _adapt = _Impl(_ADAPT, "ref_")
+    return _adapt
+
+
 def reference():
     """The reference's own code, or None where it was not built."""
     global _ref
@@ -259,6 +274,19 @@ def reference_sph_active(pos, vel, mass, soft, u, rung, iRung, sp):
                        int(iRung), ctypes.byref(sp), _d(acc), _d(f))
     return dict(acc=acc, uDotPdV=f[:, 0].copy(), uDotAV=f[:, 1].copy(), dtNew=f[:, 2].copy(),
                 mumax=f[:, 3].copy(), dt=f[:, 4].copy(), fDensity=f[:, 5].copy())
+
+
+STORE_FIELDS = ["stride", "r", "fMass", "fSoft", "v", "vPred", "u", "uPred", "a", "fPot", "dtGrav",
+                "fBall2", "fDensity", "divv", "curlv", "dvds", "BalsaraSwitch", "diff", "PoverRho2",
+                "c", "uDotPdV", "uDotAV", "mumax", "dtNew", "iActive", "activeBit", "iOrder", "gasBit"]
+
+
+def reference_particle_layout():
+    """sizeof(PARTICLE) and the byte offsets of its fields in the reference
+    build here (ref_particle_layout), keyed by STORE_FIELDS."""
+    o = np.zeros(len(STORE_FIELDS), dtype=np.int64)
+    reference().lib.ref_particle_layout(o.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)))
+    return {k: int(v) for k, v in zip(STORE_FIELDS, o)}
 
 
 def reference_knn_sets(pos, mass, soft, sp):

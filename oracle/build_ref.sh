@@ -30,3 +30,18 @@ gcc $CFLAGS -c "$HERE/ref_harness.c" -o "$OUT/ref_harness.o" &
 wait
 gcc -shared -o "$OUT/libgasref.so" $OBJS "$OUT/mdl_null.o" "$OUT/ref_harness.o" -lm
 echo "built $OUT/libgasref.so"
+# The same harness with ref_grav/ref_sph going through the reference-side
+# binding of libtsph (gasoline_gb300/pkd/tsph_pkd.c, compiled against the
+# reference's headers as an integrator would), linked against the CPU
+# stand-in of libtsph whose arithmetic is the oracle's.
+PKDB="$HERE/../gasoline_gb300/pkd"
+gcc $CFLAGS -DTSPH_ADAPTER -I"$PKDB" -c "$HERE/ref_harness.c" -o "$OUT/ref_harness_adapter.o" &
+gcc $CFLAGS -I"$PKDB" -c "$PKDB/tsph_pkd.c" -o "$OUT/tsph_pkd.o" &
+gcc -O2 -fPIC -ffp-contract=off -fno-fast-math -w -I"$HERE" -I"$HERE/../include" \
+    -c "$HERE/adapter_fake_tsph.c" -o "$OUT/adapter_fake_tsph.o" &
+gcc -O2 -fPIC -ffp-contract=off -fno-fast-math -w -std=gnu99 \
+    -c "$HERE/tsph_oracle.c" -o "$OUT/tsph_oracle_adapter.o" &
+wait
+gcc -shared -o "$OUT/libgasadapt.so" $OBJS "$OUT/mdl_null.o" "$OUT/ref_harness_adapter.o" \
+    "$OUT/tsph_pkd.o" "$OUT/adapter_fake_tsph.o" "$OUT/tsph_oracle_adapter.o" -lm
+echo "built $OUT/libgasadapt.so"

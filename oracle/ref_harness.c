@@ -16,7 +16,15 @@
  *   msrSph (master.c:9258-9362): pkdBuildLocal, smSmooth(SMX_DENDVDX),
  *     pkdGasPressure, smReSmooth(SMX_SPHPRESSURETERMS).
  * Inputs and outputs are SoA arrays indexed by iOrder (input order).
+ *
+ * Built with -DTSPH_ADAPTER (oracle/_ref/libgasadapt.so), ref_grav and
+ * ref_sph run the same sequence through the reference-side binding of
+ * libtsph instead (gasoline_gb300/pkd/tsph_pkd.c: tsph_pkdBuildBinary,
+ * tsph_pkdGravAll, tsph_smSmooth, tsph_smReSmooth at the call sites of
+ * pstBuildTree, pstGravity, pstSmooth and pstReSmooth), linked against the
+ * CPU stand-in of libtsph in adapter_fake_tsph.c.
  */
+#include <stddef.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -29,6 +37,18 @@
 #include "smooth.h"
 #include "smoothfcn.h"
 #include "opentype.h"
+#ifdef TSPH_ADAPTER
+#include "tsph_pkd.h"
+#define BUILD_BINARY tsph_pkdBuildBinary
+#define GRAV_ALL tsph_pkdGravAll
+#define SM_SMOOTH tsph_smSmooth
+#define SM_RESMOOTH tsph_smReSmooth
+#else
+#define BUILD_BINARY pkdBuildBinary
+#define GRAV_ALL pkdGravAll
+#define SM_SMOOTH smSmooth
+#define SM_RESMOOTH smReSmooth
+#endif
 
 typedef struct {
     int nBucket;
@@ -101,8 +121,8 @@ static void build_grav_tree(PKD pkd, const ref_grav_params *gp)
     int iOrderTree = gp->iOrder;
     if (gp->bPeriodic && gp->bEwald && gp->iEwOrder > iOrderTree)
         iOrderTree = gp->iEwOrder;
-    pkdBuildBinary(pkd, gp->nBucket, OPEN_JOSH, gp->dTheta, iOrderTree,
-                   0, 1, &root);
+    BUILD_BINARY(pkd, gp->nBucket, OPEN_JOSH, gp->dTheta, iOrderTree,
+                 0, 1, &root);
     make_top(pkd, &root);
     pkdCalcRoot(pkd, &rootmom);
     pkdDistribRoot(pkd, &rootmom);
@@ -130,7 +150,7 @@ int ref_grav(int n, const double *pos, const double *mass, const double *soft,
         p->fPot = 0.0;
         p->dtGrav = 0.0;
     }
-    pkdGravAll(pkd, gp->bPeriodic ? gp->nReps : 0, gp->bPeriodic, gp->iOrder,
+    GRAV_ALL(pkd, gp->bPeriodic ? gp->nReps : 0, gp->bPeriodic, gp->iOrder,
                gp->bEwald, gp->iEwOrder, gp->fEwCut, gp->fEwhCut, 0, 0.0, 0,
                0.0, aSun, &nActive, &dPartSum, &dCellSum, &dSoftSum, &cs,
                &dFlop);
@@ -147,6 +167,9 @@ int ref_grav(int n, const double *pos, const double *mass, const double *soft,
     counters[3] = dSoftSum;
     counters[4] = dFlop;
     nNodes = pkd->nNodes;
+#ifdef TSPH_ADAPTER
+    tsph_pkd_detach(pkd);
+#endif
     pkdFinish(pkd);
     return nNodes;
 }
@@ -355,7 +378,7 @@ int ref_sph(int n, const double *pos, const double *vel, const double *mass,
     pkdBuildLocal(pkd, sp->nBucket, OPEN_JOSH, 0.7, 2, 1, 0, &root);
     make_top(pkd, &root);
     smInitialize(&smx, pkd, &smf, sp->nSmooth, sp->bPeriodic, 1, SMX_DENDVDX, 1, 0.0);
-    smSmooth(smx, &smf);
+    SM_SMOOTH(smx, &smf);
     smFinish(smx, &smf, &cs);
 
     memset(&gpc, 0, sizeof(gpc));
@@ -372,7 +395,7 @@ int ref_sph(int n, const double *pos, const double *vel, const double *mass,
         for (j = 0; j < 3; ++j) p->a[j] = 0.0;
     }
     smInitialize(&smx, pkd, &smf, sp->nSmooth, sp->bPeriodic, 1, SMX_SPHPRESSURETERMS, 0, 0.0);
-    smReSmooth(smx, &smf);
+    SM_RESMOOTH(smx, &smf);
     smFinish(smx, &smf, &cs);
 
     for (i = 0; i < n; ++i) {
@@ -398,8 +421,46 @@ int ref_sph(int n, const double *pos, const double *vel, const double *mass,
         dtNew[k] = p->dtNew;
         mumax[k] = p->mumax;
     }
+#ifdef TSPH_ADAPTER
+    tsph_pkd_detach(pkd);
+#endif
     pkdFinish(pkd);
     return 0;
+}
+
+/* The PARTICLE layout of this build (sizeof and byte offsets, in the order
+ * of tsph_store_layout's fields), for the store-layout fixture the GPU tests
+ * use where the reference's headers are absent. */
+void ref_particle_layout(long long *o)
+{
+    o[0] = (long long)sizeof(PARTICLE);
+    o[1] = offsetof(PARTICLE, r);
+    o[2] = offsetof(PARTICLE, fMass);
+    o[3] = offsetof(PARTICLE, fSoft);
+    o[4] = offsetof(PARTICLE, v);
+    o[5] = offsetof(PARTICLE, vPred);
+    o[6] = offsetof(PARTICLE, u);
+    o[7] = offsetof(PARTICLE, uPred);
+    o[8] = offsetof(PARTICLE, a);
+    o[9] = offsetof(PARTICLE, fPot);
+    o[10] = offsetof(PARTICLE, dtGrav);
+    o[11] = offsetof(PARTICLE, fBall2);
+    o[12] = offsetof(PARTICLE, fDensity);
+    o[13] = offsetof(PARTICLE, divv);
+    o[14] = offsetof(PARTICLE, curlv);
+    o[15] = offsetof(PARTICLE, dvds);
+    o[16] = offsetof(PARTICLE, BalsaraSwitch);
+    o[17] = offsetof(PARTICLE, diff);
+    o[18] = offsetof(PARTICLE, PoverRho2);
+    o[19] = offsetof(PARTICLE, c);
+    o[20] = offsetof(PARTICLE, uDotPdV);
+    o[21] = offsetof(PARTICLE, uDotAV);
+    o[22] = offsetof(PARTICLE, mumax);
+    o[23] = offsetof(PARTICLE, dtNew);
+    o[24] = offsetof(PARTICLE, iActive);
+    o[25] = TYPE_ACTIVE;
+    o[26] = offsetof(PARTICLE, iOrder);
+    o[27] = TYPE_GAS;
 }
 
 /* The reference's approximate 1/sqrt (v_sqrt1.c:11), exported for tests. */

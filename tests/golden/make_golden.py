@@ -71,6 +71,18 @@ def sph_box_case():
                         knn_count=k["nbr_count"])
 
 
+def particle_layout():
+    """The reference's PARTICLE layout (sizeof and field offsets of this
+    build, -DGASOLINE -DNOCOOLING) for the GPU tests of the store entry
+    points, which run where the reference's headers are absent."""
+    import json
+    lay = oracle.reference_particle_layout()
+    with open(os.path.join(HERE, "particle_layout.json"), "w") as f:
+        json.dump(lay, f, indent=1, sort_keys=True)
+        f.write("\n")
+    print("particle layout", lay["stride"], "bytes")
+
+
 def tipsy_fields(ng, nd, ns, seed):
     """Seeded particles of every Tipsy type; a few values sit on float
     rounding edges (subnormal, -0.0, near FLT_MAX, halfway between floats)."""
@@ -182,14 +194,15 @@ def main():
     sph_case("sph_sphere_2k", pos, vel, m, np.full(len(m), 0.01), u,
              oracle.sph_params(nSmooth=32))
     sph_box_case()
+    particle_layout()
     tipsy_case("tipsy_mixed", 300, 500, 200, seed=16)
     multistep_cases()
     render_case()
 
 
 if __name__ == "__main__":
-    # one group of fixtures only: python make_golden.py tipsy|multistep|render|sph_box
-    if len(sys.argv) > 1 and sys.argv[1] in ("tipsy", "multistep", "render", "sph_box"):
+    # one group of fixtures only: python make_golden.py tipsy|multistep|render|sph_box|layout
+    if len(sys.argv) > 1 and sys.argv[1] in ("tipsy", "multistep", "render", "sph_box", "layout"):
         if not oracle.reference_available():
             oracle.build_reference()
         if sys.argv[1] == "tipsy":
@@ -198,6 +211,8 @@ if __name__ == "__main__":
             multistep_cases()
         elif sys.argv[1] == "sph_box":
             sph_box_case()
+        elif sys.argv[1] == "layout":
+            particle_layout()
         else:
             render_case()
     else:

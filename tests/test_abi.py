@@ -57,6 +57,7 @@ STRUCTS = {   # C typedef in include/tsph.h -> ctypes class in gasoline_gb300
     "tsph_step_out": "StepOut",
     "tsph_render_params": "RenderParams",
     "tsph_tipsy_header": "TipsyHeader",
+    "tsph_store_layout": "StoreLayout",
 }
 
 
