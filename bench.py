@@ -144,12 +144,57 @@ def replica_value(n_per_rank, world, ms):
     return world * n_per_rank / (ms * 1e-3)
 
 
-def fma_peak_tflops(lib_ctx):
-    """Measured FP32 FMA peak of this GPU (project microbenchmark)."""
+def fma_peak_tflops(lib_ctx, fp32=True):
+    """Measured FP32 (or FP64) FMA peak of this GPU (project microbenchmark)."""
     import ctypes
     t = ctypes.c_double()
-    rc = lib_ctx.lib.tsph_fma_peak(lib_ctx._ctx, 1, ctypes.byref(t))
+    rc = lib_ctx.lib.tsph_fma_peak(lib_ctx._ctx, 1 if fp32 else 0, ctypes.byref(t))
     return t.value if rc == 0 else None
+
+
+# Algorithmic flops per neighbour pair of the SPH passes in the reference's
+# convention (+, -, *, /, sqrt count one each), counted from the oracle's
+# statement-by-statement restatement: DenDVDX (smoothfcn.c:3390-3627,
+# M4 KERNEL/DKERNEL) and one symmetric SphPressureTerms pair
+# (SphPressureTerms.h, both particles updated).
+FLOP_DENDVDX_PAIR = 64
+FLOP_PRESSURE_PAIR = 68
+GRAV_FLOPS = ("reference grav.c:246-247 (+,* = 1, 38 per P-P, 82 per softened cell, "
+              "76 per quadrupole cell)")
+
+
+def walk_roofline(ctx, out, walk_ms, nbt):
+    """The gravity walk (k_walk<float, nbt>): the reference's flop count of
+    the evaluation over the kernel's event-timed duration, against the FP32
+    FMA peak measured on this GPU."""
+    fl = out["dFlop"] - out["dFlopEwald"]
+    peak = fma_peak_tflops(ctx)
+    ach = fl / (walk_ms * 1e-3) / 1e12
+    return {"bound": "fp32", "kernel": f"k_walk<float, {nbt}> (fused walk + P-P/P-C)",
+            "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak if peak else None,
+            "traffic": None, "flop_convention": GRAV_FLOPS, "kernel_ms": walk_ms,
+            "peak_source": "tsph_fma_peak (FP32 FMA, measured on this GPU)"}
+
+
+def density_roofline(ctx, dens, density_ms, fp32):
+    """The kNN + DenDVDX pass (k_knn_density): DenDVDX's flops per gathered
+    pair over the kernel's event-timed duration (the kNN selection itself
+    is comparisons and integer work, not counted), against the measured FMA
+    peak of its precision."""
+    peak = fma_peak_tflops(ctx, fp32)
+    ach = dens["dPairs"] * FLOP_DENDVDX_PAIR / (density_ms * 1e-3) / 1e12
+    return {"bound": "fp32" if fp32 else "fp64",
+            "kernel": f"k_knn_density<{'f32' if fp32 else 'f64'}> (kNN + DenDVDX)",
+            "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak if peak else None,
+            "traffic": None, "flop_convention": f"{FLOP_DENDVDX_PAIR} per gathered pair (DenDVDX)",
+            "kernel_ms": density_ms, "pairs": dens["dPairs"], "candidates": dens["dCandidates"],
+            "peak_source": f"tsph_fma_peak ({'FP32' if fp32 else 'FP64'} FMA, measured on this GPU)"}
+
+
+def oracle_seconds(fn):
+    t = time.perf_counter()
+    r = fn()
+    return time.perf_counter() - t, r
 
 
 def run_ours(args, rank, world, local_rank):
@@ -531,11 +576,18 @@ def run_plummer(args):
     ctx.set_velocities(vel)
     ad, _ = oracle.direct(pos, m, soft, np.arange(len(m)), nthreads=os.cpu_count() or 1)
     res = {}
+    roof = None
     for name, prec in (("fp64", g.FP64), ("fp32", g.FP32)):
         gp = g.grav_params(periodic=False, precision=prec)
         for _ in range(args.warmup):
             ctx.grav_all(gp)
-        ts = [_cuda_ms(lambda: ctx.grav_all(gp), stream) for _ in range(args.steps)]
+        ts, walk = [], []
+        for _ in range(args.steps):
+            box = {}
+            ts.append(_cuda_ms(lambda: box.update(ctx.grav_all(gp)), stream))
+            walk.append(ctx.timings()["walk"])
+        if prec == g.FP32:
+            roof = walk_roofline(ctx, box, statistics.mean(walk), 8)
         a = ctx.get_gravity()["acc"]
         e = np.linalg.norm(a - ad, axis=1) / np.linalg.norm(ad, axis=1)
         tk = [_cuda_ms(lambda: (ctx.kick(5e-4), ctx.drift(1e-3, False, 1.0), ctx.grav_all(gp),
@@ -555,12 +607,21 @@ def run_plummer(args):
         ctx.set_particles(pos, m, soft)
         ctx.set_velocities(vel)
     ctx.close()
+    # CPU baseline: the oracle's gravity evaluation of the same sphere on
+    # every host core, and its KDK step
+    nth = os.cpu_count() or 1
+    tg, _ = oracle_seconds(lambda: oracle.oracle().grav(pos, m, soft, oracle.grav_params(periodic=False),
+                                                          nthreads=nth))
     ms = res["fp32"]["grav_ms"]
     return {"metric": "particle force evals/s, Plummer N=32768 (gravity)", "value": 32768 / (ms * 1e-3),
             "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "dtype": "f32", "data": "synthetic Plummer sphere, seed 1",
             "config": {"workload": "Plummer N=32768, G=M=a=1, rmax=20a, theta=0.7, eps=0.01, "
-                                   "nBucket=8, one eval + one KDK dt=1e-3"}, "paths": res}
+                                   "nBucket=8, one eval + one KDK dt=1e-3"}, "paths": res,
+            "roofline": roof,
+            "cpu_baseline": {"value": 32768 / tg, "unit": UNIT, "cores": nth, "kind": "port",
+                             "sample": f"one full gravity evaluation of the same sphere ({tg:.3f} s, "
+                                       "FP64, tree build serial, walk OpenMP over buckets)"}}
 
 
 def run_collapse(args):
@@ -575,7 +636,7 @@ def run_collapse(args):
     n = args.collapse_n
     pos, vel, m, u = g.ics.gas_sphere(n, seed=41)
     soft = np.full(n, 0.01)
-    kw = dict(ngas=n, u=u, nSmooth=32, precision=g.FP32)
+    kw = dict(ngas=n, u=u, nSmooth=32, precision=g.FP32, sph_precision=g.FP32)
     A = Simulation(pos, vel, m, soft, **kw)
     B = Simulation(pos, vel, m, soft, **kw)
     A.ctx.hnet_init(seed=3)
@@ -604,7 +665,7 @@ def run_collapse(args):
                 rows[key].append((r["wall_s"], r["t_grav_ms"], r["t_knn_density_ms"],
                                   r["t_pressure_ms"], r["density"]["dCandidates"],
                                   r["density"]["nFallback"], r["density"]["bSeeded"],
-                                  r["t_knn_tree_ms"]))
+                                  r["t_knn_tree_ms"], r["density"]["dPairs"]))
             sa, sb = A.ctx.get_sph(), B.ctx.get_sph()
             ha, hb = A.ctx.get_neighbour_hash(), B.ctx.get_neighbour_hash()
             if not (np.array_equal(sa["fBall2"], sb["fBall2"]) and np.array_equal(ha[1], hb[1])
@@ -616,15 +677,31 @@ def run_collapse(args):
                 "density_ms": float(a[:, 2].mean()), "pressure_ms": float(a[:, 3].mean()),
                 "candidates_per_particle": float(a[:, 4].mean() / n),
                 "grown_balls_per_pass": float(a[:, 5].mean()), "seeded": bool(a[:, 6].all()),
-                "knn_tree_ms": float(a[:, 7].mean())}
+                "knn_tree_ms": float(a[:, 7].mean()), "pairs_per_pass": float(a[:, 8].mean())}
     sa_, sb_ = summ(rows["A"]), summ(rows["B"])
+    roof = density_roofline(A.ctx, {"dPairs": sa_["pairs_per_pass"],
+                                    "dCandidates": sa_["candidates_per_particle"] * n},
+                            sa_["density_ms"], True)
     A.ctx.close()
     B.ctx.close()
+    # CPU baseline: the oracle's force evaluation of the initial sphere
+    # (gravity, then both SPH passes) on every host core
+    import oracle
+    nth = os.cpu_count() or 1
+    tg, _ = oracle_seconds(lambda: oracle.oracle().grav(pos, m, soft, oracle.grav_params(periodic=False),
+                                                          nthreads=nth))
+    tsph, _ = oracle_seconds(lambda: oracle.oracle().sph(pos, vel, m, soft, u, oracle.sph_params(nSmooth=32),
+                                                           nthreads=nth))
     return {"metric": "gas particle force evals/s (gravity + SPH density + pressure), "
                       "adiabatic collapse N=262144, learned h", "value": n / (sa_["step_ms"] * 1e-3),
             "unit": UNIT, "n_gpus": 1, "steps": args.collapse_steps, "warmup": ntrain,
-            "ms_per_step": sa_["step_ms"], "higher_is_better": True, "dtype": "f32 gravity, f64 SPH",
+            "ms_per_step": sa_["step_ms"], "higher_is_better": True, "dtype": "f32 gravity, f32 SPH",
             "data": "synthetic 1/r gas sphere, seed 41",
+            "roofline": roof,
+            "cpu_baseline": {"value": n / (tg + tsph), "unit": UNIT, "cores": nth, "kind": "port",
+                             "sample": f"one force evaluation of the initial sphere: gravity "
+                                       f"{tg:.2f} s + SPH density and pressure passes {tsph:.2f} s "
+                                       "(FP64, OpenMP)"},
             "config": {"workload": "adiabatic collapse, 262144 gas, M=R=G=1, u=0.05, gamma=5/3, "
                                    f"nSmooth=32, alpha=1, beta=2, dt={dt}, MLP trained on steps 0-49",
                        "timing": "host wall clock per KDK step incl. host round trips"},
@@ -754,11 +831,14 @@ def run_batched(args):
     ctx.set_particles(pos, m, soft)
     ctx.set_velocities(vel, ngas, u)
     ctx.set_systems(so)
-    sp = g.sph_params(nSmooth=32)
+    sp = g.sph_params(nSmooth=32, precision=g.FP32)
     best, table = autotune.tune_gravity(ctx, g.grav_params(periodic=False, precision=g.FP32))
     gp = g.grav_params(periodic=False, precision=g.FP32, nBucket=best["nBucket"])
-    ctx.set_tuning(taskSize=best["taskSize"], walkBlocksPerSM=best["walkBlocksPerSM"])
-    ctx.grav_all(gp)
+    ctx.set_tuning(taskSize=best["taskSize"], walkBlocksPerSM=best["walkBlocksPerSM"],
+                   walkGroup=best["walkGroup"])
+    gout = ctx.grav_all(gp)
+    gtim = ctx.timings()
+    roof = walk_roofline(ctx, gout, gtim["walk"], min(32, max(8, best["nBucket"])))
     acc = ctx.get_gravity()["acc"]
     errs = []
     for s_, d in enumerate(systems):
@@ -775,16 +855,43 @@ def run_batched(args):
         ctx.step_status()
         res["graph" if graph else "direct"] = {"step_ms": statistics.mean(ts),
                                                "kernels_per_step": (ctx.launches() - l0) / args.steps}
+    ctx.smooth(g.SMX_DENDVDX, sp)
+    ctx.smooth(g.SMX_SPHPRESSURETERMS, sp)
+    stim = ctx.timings()
+    phases = {"gravity": {k: gtim[k] for k in ("build", "moments", "walk", "total")},
+              "sph": {k: stim[k] for k in ("knn", "density", "pressure")}}
     ctx.close()
+    # CPU baseline: independent systems, as the reference runs them (one job
+    # each): every 16th system, gravity and (for the gas systems) both SPH
+    # passes by the oracle on every host core, one system after another
+    nth = os.cpu_count() or 1
+    t_cpu, n_cpu = 0.0, 0
+    for d in systems[::16]:
+        tg, _ = oracle_seconds(lambda: oracle.oracle().grav(d["pos"], d["mass"], d["soft"],
+                                                              oracle.grav_params(periodic=False,
+                                                                                 nBucket=best["nBucket"]),
+                                                              nthreads=nth))
+        t_cpu += tg
+        ng = d["ngas"]
+        if ng > 0:
+            ts, _ = oracle_seconds(lambda: oracle.oracle().sph(d["pos"][:ng], d["vel"][:ng], d["mass"][:ng],
+                                                                 d["soft"][:ng], np.full(ng, 0.05),
+                                                                 oracle.sph_params(nSmooth=32), nthreads=nth))
+            t_cpu += ts
+        n_cpu += len(d["mass"])
     ms = res["graph"]["step_ms"]
     return {"metric": "particle force evals/s, 512 batched uneven systems (gravity + SPH), one CUDA graph per step",
             "value": n / (ms * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
-            "warmup": 1, "ms_per_step": ms, "higher_is_better": True, "dtype": "f32 gravity, f64 SPH",
+            "warmup": 1, "ms_per_step": ms, "higher_is_better": True, "dtype": "f32 gravity, f32 SPH",
             "data": "synthetic Plummer/Hernquist spheres, seed 5",
             "config": {"workload": f"{args.nsys} systems, N log-uniform [1024, 65536], total {n}, "
                                    f"gas {ngas}, eps=0.01, theta=0.7, nSmooth=32",
                        "tuned": best},
-            "autotune": table, "steps": res,
+            "autotune": table, "steps": res, "roofline": roof, "phase_ms": phases,
+            "cpu_baseline": {"value": n_cpu / t_cpu, "unit": UNIT, "cores": nth, "kind": "port",
+                             "sample": f"{len(systems[::16])} of the {len(systems)} systems (every 16th, "
+                                       f"{n_cpu} particles): oracle gravity + SPH per system, "
+                                       f"{t_cpu:.2f} s (FP64, OpenMP within each system)"},
             "per_system_err_vs_direct": {"max_rms": max(errs), "median_rms": float(np.median(errs))}}
 
 
@@ -810,8 +917,36 @@ def run_mixed(args):
     sim.learned_h = True
     recs = [sim.step(1e-4) for _ in range(max(1, args.steps // 5))]
     r = recs[-1]
+    roof = density_roofline(sim.ctx, r["density"], r["t_knn_density_ms"], True)
+    # learned h against the exact kNN alone on the same particles: the
+    # density pass seeded by the network and unseeded, twice each
+    cmp = {}
+    for learned in (True, False, True, False):
+        sim.learned_h = learned
+        sim.sp.bLearnedH = int(learned)
+        d = sim.ctx.smooth(g.SMX_DENDVDX, sim.sp)
+        t = sim.ctx.timings()
+        cnt, hsh = sim.ctx.get_neighbour_hash()
+        key = "learned_h" if learned else "exact_knn"
+        cmp[key] = {"density_ms": t["density"], "knn_tree_ms": t["knn"],
+                    "candidates_per_particle": d["dCandidates"] / ngas, "seeded": bool(d["bSeeded"]),
+                    "grown_balls": d["nFallback"], "_hash": hsh, "_fb": sim.ctx.get_sph()["fBall2"]}
+    same = (np.array_equal(cmp["learned_h"].pop("_hash"), cmp["exact_knn"].pop("_hash")) and
+            np.array_equal(cmp["learned_h"].pop("_fb"), cmp["exact_knn"].pop("_fb")))
+    cmp["neighbour_sets_and_fBall2_identical"] = bool(same)
+    cmp["density_speedup"] = cmp["exact_knn"]["density_ms"] / cmp["learned_h"]["density_ms"]
+    sim.learned_h = True
     sim.ctx.close()
     ms = statistics.mean(x["wall_s"] for x in recs) * 1e3
+    # CPU baseline: one gravity evaluation (Ewald) of the same construction
+    # at 2 x 128^3 by the oracle on every host core (the full box's serial
+    # tree build alone takes the oracle minutes)
+    import oracle
+    nth = os.cpu_count() or 1
+    ps, _, ms_, _, _ = g.ics.mixed_box(128, seed=6)
+    ts_, _ = oracle_seconds(lambda: oracle.oracle().grav(ps, ms_, np.full(len(ms_), 1.0 / (50.0 * 128)),
+                                                         oracle.grav_params(periodic=True, ewald=True),
+                                                         nthreads=nth))
     return {"metric": "particle force evals/s, clustered mixed box 2x%d^3 (gravity + SPH), learned h" % ng,
             "value": n / (ms * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": len(recs), "warmup": 2,
             "ms_per_step": ms, "higher_is_better": True, "dtype": "f32 gravity, f32 SPH",
@@ -821,7 +956,13 @@ def run_mixed(args):
                        "timing": "host wall clock per KDK step"},
             "phases_ms": {"grav": r["t_grav_ms"], "density": r["t_knn_density_ms"],
                           "pressure": r["t_pressure_ms"]},
-            "hnet_loss": loss, "seeded": r["density"]["bSeeded"]}
+            "roofline": roof,
+            "cpu_baseline": {"value": len(ms_) / ts_, "unit": UNIT, "cores": nth, "kind": "port",
+                             "sample": f"one gravity evaluation (Ewald) of the 2x128^3 box of the same "
+                                       f"construction, {len(ms_)} particles, {ts_:.1f} s (FP64, tree build "
+                                       "serial, walk + Ewald OpenMP); the SPH passes are not in the sample"},
+            "hnet_loss": loss, "seeded": r["density"]["bSeeded"],
+            "learned_vs_exact_density_pass": cmp}
 
 
 def main():

@@ -15,6 +15,15 @@ check bit for bit; the group size changes only the order in which each
 particle's terms are summed.  Groups pay off on clustered systems (fewer
 opening tests per bucket) and not on near-uniform periodic boxes, which is
 why they are tuned.  The context is left with the best knobs set.
+
+The bucket size runs to 32 (TSPH_MAX_BUCKET): one warp walks one bucket
+with a lane per (particle, entry slot), 32/nBucket slots per particle, so
+the warp is the bucket's unit of work and "warps per bucket" is one by
+construction.  The list-tile lengths (128 particle-particle entries, 64
+cells) are compile-time constants that set the walk's shared memory and
+so its resident blocks; a 48-cell variant with six blocks per SM measured
+slower on both a periodic box and a Plummer sphere, and the walk-block
+count is the knob that trades the same resources at run time.
 """
 import itertools
 

@@ -416,6 +416,8 @@ extern "C" int tsph_grav_all(tsph_ctx *ctx, const tsph_grav_params *gp, tsph_gra
     if (!ctx || !gp) return TSPH_ERR_ARG;
     if (!ctx->haveParts) return TSPH_ERR_STATE;
     if (gp->nBucket < 1 || gp->dTheta <= 0 || gp->iOrder < 1 || gp->iOrder > 4) return TSPH_ERR_ARG;
+    // one warp walks one bucket, a lane per (particle, entry slot): at most 32 particles
+    if (gp->nBucket > TSPH_MAX_BUCKET) return TSPH_ERR_UNSUPPORTED;
     if (gp->bPeriodic && !(gp->dPeriod > 0)) return TSPH_ERR_ARG;
     if (gp->bPeriodic && ctx->T.nR > 1) return TSPH_ERR_UNSUPPORTED;   // isolated systems only
     if (gp->precision != TSPH_FP32 && gp->precision != TSPH_FP64) return TSPH_ERR_ARG;
@@ -445,7 +447,7 @@ extern "C" int tsph_grav_all(tsph_ctx *ctx, const tsph_grav_params *gp, tsph_gra
     rc = tsph_build_tree(ctx, ctx->P, ctx->T, n, gp->nBucket);
     if (rc) return rc;
     if (!cap) cudaEventRecord(ctx->ev[1], ctx->stream);
-    rc = tsph_tree_moments(ctx, ctx->P, ctx->T, n, gp->dTheta);
+    rc = tsph_tree_moments(ctx, ctx->P, ctx->T, n, gp->dTheta, gp->iOrder);
     if (rc) return rc;
     const bool ewald = n > 0 && gp->bPeriodic && gp->bEwald && gp->iEwOrder >= 1;
     if (ewald) {   // the root moments now, so the host has them while the walk runs

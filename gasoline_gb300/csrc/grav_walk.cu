@@ -87,32 +87,40 @@ __device__ __forceinline__ void rep_off64(int r, double *o) {
 // on the two entries at once:  xy = (x0, x1, y0, y1), zm = (z0, z1, m0, m1),
 // q01 = (xx0, xx1, yy0, yy1), q23 = (zz0, zz1, xy0, xy1),
 // q45 = (xz0, xz1, yz0, yz1), h = (h0, h1).
-template <typename Real>
+// HIGH (octopole and hexadecapole cells, iOrder >= 3): cell tiles of 32,
+// with the 25 reduced moments of every entry in oh[k][entry].
+template <bool HIGH>
+__host__ __device__ constexpr int cell_tile() { return HIGH ? 32 : CNF; }
+
+template <typename Real, bool HIGH>
 struct TileData {
     Real ex[PPF], ey[PPF], ez[PPF], em[PPF], eh[PPF];
-    Real q[6][CNF];
+    Real q[6][cell_tile<HIGH>()];
+    Real oh[HIGH ? 25 : 1][HIGH ? cell_tile<HIGH>() : 1];
 };
-template <>
-struct TileData<float> {
+template <bool HIGH>
+struct TileData<float, HIGH> {
+    static constexpr int C = cell_tile<HIGH>();
     union {
         struct {
             float4 xy[PPF / 2], zm[PPF / 2];
             float2 h[PPF / 2];
         } pp;
         struct {
-            float4 xy[CNF / 2], zm[CNF / 2], q01[CNF / 2], q23[CNF / 2], q45[CNF / 2];
-            float2 h[CNF / 2];
+            float4 xy[C / 2], zm[C / 2], q01[C / 2], q23[C / 2], q45[C / 2];
+            float2 h[C / 2];
+            float oh[HIGH ? 25 : 1][HIGH ? C : 1];
         } cn;
     };
 };
 
-template <typename Real, int NBT>
+template <typename Real, int NBT, bool HIGH>
 struct WalkSmem {
     int stack[STK];
     int pp[PPF + 32 * NBT + NBT];
     int cn[CNB];
     int cs[CNB];
-    TileData<Real> D;
+    TileData<Real, HIGH> D;
     Real px[NBT], py[NBT], pz[NBT], pm[NBT], ph[NBT];
     // the warp's tallies of pkdGravAll's sums (lane 0 only)
     unsigned long long tAct, tPP, tNewt, tSoft, tBsq, tIntra;
@@ -321,8 +329,8 @@ __device__ __forceinline__ void rel_pos(float4 h, float4 l, int r, float bchx, f
 }
 
 // Stage P-P entries [0, cnt) of the warp's buffer into shared memory.
-template <typename Real, int NBT>
-__device__ __forceinline__ void stage_pp(WalkSmem<Real, NBT> &S, const TsphDevParts &P, int cnt,
+template <typename Real, int NBT, bool HIGH>
+__device__ __forceinline__ void stage_pp(WalkSmem<Real, NBT, HIGH> &S, const TsphDevParts &P, int cnt,
                                          int lane, float bchx, float bchy, float bchz,
                                          float bclx, float bcly, float bclz) {
     if constexpr (sizeof(Real) == 4) {
@@ -369,8 +377,8 @@ __device__ __forceinline__ void stage_pp(WalkSmem<Real, NBT> &S, const TsphDevPa
 // holds the bucket's own particles (the first tile of every bucket, where
 // the own particles are entries 0..n-1), so the particle's pair with itself
 // is left out.
-template <typename Real, int NBT, bool SELF>
-__device__ __forceinline__ void eval_pp(WalkSmem<Real, NBT> &S, int cnt, int i, int slot, Acc<Real> &A) {
+template <typename Real, int NBT, bool HIGH, bool SELF>
+__device__ __forceinline__ void eval_pp(WalkSmem<Real, NBT, HIGH> &S, int cnt, int i, int slot, Acc<Real> &A) {
     if constexpr (sizeof(Real) == 4) {
         const float2 X = p_splat(S.px[i]), Y = p_splat(S.py[i]), Z = p_splat(S.pz[i]);
         const float2 H = p_splat(S.ph[i]), M = p_splat(S.pm[i]);
@@ -463,8 +471,8 @@ __device__ __forceinline__ void cell_record(const TsphDevTree &T, int ent, bool 
 }
 
 // Stage cell entries (Newtonian when soft == 0, else softened).
-template <typename Real, int NBT>
-__device__ __forceinline__ void stage_cells(WalkSmem<Real, NBT> &S, const int *buf, const TsphDevTree &T,
+template <typename Real, int NBT, bool HIGH>
+__device__ __forceinline__ void stage_cells(WalkSmem<Real, NBT, HIGH> &S, const int *buf, const TsphDevTree &T,
                                             int cnt, int lane, bool soft, float bchx, float bchy,
                                             float bchz, float bclx, float bcly, float bclz) {
     if constexpr (sizeof(Real) == 4) {
@@ -484,6 +492,18 @@ __device__ __forceinline__ void stage_cells(WalkSmem<Real, NBT> &S, const int *b
             S.D.cn.q23[p] = make_float4(f0[6], f1[6], f0[7], f1[7]);
             S.D.cn.q45[p] = make_float4(f0[8], f1[8], f0[9], f1[9]);
             S.D.cn.h[p] = make_float2(f0[10], f1[10]);
+            if constexpr (HIGH) {
+                if (!soft) {   // reduced octopole and hexadecapole of both entries
+                    const float *o0 = T.wOH + 25 * (size_t)(buf[2 * p] >> 5);
+                    const bool two = 2 * p + 1 < cnt;
+                    const float *o1 = T.wOH + 25 * (size_t)(two ? buf[2 * p + 1] >> 5 : 0);
+#pragma unroll
+                    for (int k = 0; k < 25; ++k) {
+                        S.D.cn.oh[k][2 * p] = o0[k];
+                        S.D.cn.oh[k][2 * p + 1] = two ? o1[k] : 0.0f;
+                    }
+                }
+            }
         }
     } else {
         for (int e = lane; e < cnt; e += 32) {
@@ -507,7 +527,127 @@ __device__ __forceinline__ void stage_cells(WalkSmem<Real, NBT> &S, const int *b
             S.D.eh[e] = (Real)T.fSoft[c];
 #pragma unroll
             for (int k = 0; k < 6; ++k) S.D.q[k][e] = q[k];
+            if constexpr (HIGH) {
+                if (!soft)
+#pragma unroll
+                    for (int k = 0; k < 25; ++k) S.D.oh[k][e] = (Real)T.OH[25 * (size_t)c + k];
+            }
         }
+    }
+}
+
+// QEVAL (qeval.h:21-64) at orders 1 to 4 for one cell: reduced moments m,
+// q (xx yy zz xy xz yz), o (pkdCalcCell's O*: xxx xyy xxy yyy xxz yyz xyz
+// xzz yzz zzz), h (H*: xxxx xyyy xxxy yyyy xxxz yyyz xxyy xxyz xyyz xxzz
+// xyzz xzzz yyzz yzzz zzzz); (dx, dy, dz) = particle - cell, gam[0..5] the
+// reference's gamma series; accumulates into a and pot like the macro.
+template <typename Real>
+__device__ __forceinline__ void qeval_cell(int iOrder, Real m, const Real *q, const Real *o, const Real *h,
+                                           const Real *gam, Real dx, Real dy, Real dz, Real &ax, Real &ay,
+                                           Real &az, Real &pot) {
+    Real Qmirx, Qmiry, Qmirz, Qmir, Qta = 0;
+    if (iOrder >= 4) {
+        Qmirx = Real(1.0 / 6.0) * (h[11] * dz * dz * dz + 3 * h[10] * dy * dz * dz + 3 * h[8] * dy * dy * dz +
+                                    h[1] * dy * dy * dy + 3 * h[9] * dx * dz * dz + 6 * h[7] * dx * dy * dz +
+                                    3 * h[6] * dx * dy * dy + 3 * h[4] * dx * dx * dz + 3 * h[2] * dx * dx * dy +
+                                    h[0] * dx * dx * dx);
+        Qmiry = Real(1.0 / 6.0) * (h[13] * dz * dz * dz + 3 * h[10] * dx * dz * dz + 3 * h[7] * dx * dx * dz +
+                                    h[2] * dx * dx * dx + 3 * h[12] * dy * dz * dz + 6 * h[8] * dx * dy * dz +
+                                    3 * h[6] * dx * dx * dy + 3 * h[5] * dy * dy * dz + 3 * h[1] * dx * dy * dy +
+                                    h[3] * dy * dy * dy);
+        Qmirz = Real(1.0 / 6.0) * (h[5] * dy * dy * dy + 3 * h[8] * dx * dy * dy + 3 * h[7] * dx * dx * dy +
+                                    h[4] * dx * dx * dx + 3 * h[12] * dy * dy * dz + 6 * h[10] * dx * dy * dz +
+                                    3 * h[9] * dx * dx * dz + 3 * h[13] * dy * dz * dz + 3 * h[11] * dx * dz * dz +
+                                    h[14] * dz * dz * dz);
+        Qmir = Real(1.0 / 4.0) * (Qmirx * dx + Qmiry * dy + Qmirz * dz);
+        pot -= gam[4] * Qmir;
+        Qta += gam[5] * Qmir;
+        ax += gam[4] * Qmirx;
+        ay += gam[4] * Qmiry;
+        az += gam[4] * Qmirz;
+    }
+    if (iOrder >= 3) {
+        Qmirx = Real(1.0 / 2.0) * (o[7] * dz * dz + 2 * o[6] * dy * dz + o[1] * dy * dy + 2 * o[4] * dx * dz +
+                                    2 * o[2] * dx * dy + o[0] * dx * dx);
+        Qmiry = Real(1.0 / 2.0) * (o[8] * dz * dz + 2 * o[6] * dx * dz + o[2] * dx * dx + 2 * o[5] * dy * dz +
+                                    2 * o[1] * dx * dy + o[3] * dy * dy);
+        Qmirz = Real(1.0 / 2.0) * (o[5] * dy * dy + 2 * o[6] * dx * dy + o[4] * dx * dx + 2 * o[8] * dy * dz +
+                                    2 * o[7] * dx * dz + o[9] * dz * dz);
+        Qmir = Real(1.0 / 3.0) * (Qmirx * dx + Qmiry * dy + Qmirz * dz);
+        pot -= gam[3] * Qmir;
+        Qta += gam[4] * Qmir;
+        ax += gam[3] * Qmirx;
+        ay += gam[3] * Qmiry;
+        az += gam[3] * Qmirz;
+    }
+    if (iOrder >= 2) {
+        Qmirx = q[4] * dz + q[3] * dy + q[0] * dx;
+        Qmiry = q[5] * dz + q[3] * dx + q[1] * dy;
+        Qmirz = q[5] * dy + q[4] * dx + q[2] * dz;
+        Qmir = Real(0.5) * (Qmirx * dx + Qmiry * dy + Qmirz * dz);
+        pot -= gam[2] * Qmir;
+        Qta += gam[3] * Qmir;
+        ax += gam[2] * Qmirx;
+        ay += gam[2] * Qmiry;
+        az += gam[2] * Qmirz;
+    }
+    pot -= gam[0] * m;
+    Qta += gam[1] * m;
+    ax -= dx * Qta;
+    ay -= dy * Qta;
+    az -= dz * Qta;
+}
+
+// Newtonian cells of a HIGH tile (iOrder >= 3), one cell per lane step, in
+// the precision of the walk; terms folded into the compensated sums.
+template <typename Real, int NBT, bool HIGH>
+__device__ __forceinline__ void eval_newt_high(WalkSmem<Real, NBT, HIGH> &S, int cnt, int i, int slot,
+                                               int iOrder, Acc<Real> &A) {
+    const Real xi = S.px[i], yi = S.py[i], zi = S.pz[i], mi = S.pm[i];
+    for (int e = slot; e < cnt; e += 32 / NBT) {
+        Real cx, cy, cz, m, q[6], o[10], h[15];
+        if constexpr (sizeof(Real) == 4) {
+            const int p = e >> 1, k = e & 1;
+            const float4 a = S.D.cn.xy[p], b = S.D.cn.zm[p];
+            const float4 q01 = S.D.cn.q01[p], q23 = S.D.cn.q23[p], q45 = S.D.cn.q45[p];
+            cx = k ? a.y : a.x; cy = k ? a.w : a.z; cz = k ? b.y : b.x; m = k ? b.w : b.z;
+            q[0] = k ? q01.y : q01.x; q[1] = k ? q01.w : q01.z; q[2] = k ? q23.y : q23.x;
+            q[3] = k ? q23.w : q23.z; q[4] = k ? q45.y : q45.x; q[5] = k ? q45.w : q45.z;
+        } else {
+            cx = S.D.ex[e]; cy = S.D.ey[e]; cz = S.D.ez[e]; m = S.D.em[e];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) q[k] = S.D.q[k][e];
+        }
+        if constexpr (sizeof(Real) == 4) {
+#pragma unroll
+            for (int k = 0; k < 10; ++k) o[k] = S.D.cn.oh[k][e];
+#pragma unroll
+            for (int k = 0; k < 15; ++k) h[k] = S.D.cn.oh[10 + k][e];
+        } else {
+#pragma unroll
+            for (int k = 0; k < 10; ++k) o[k] = S.D.oh[k][e];
+#pragma unroll
+            for (int k = 0; k < 15; ++k) h[k] = S.D.oh[10 + k][e];
+        }
+        const Real dx = xi - cx, dy = yi - cy, dz = zi - cz;
+        const Real d2 = dx * dx + dy * dy + dz * dz;
+        Real gam[6];
+        gam[0] = rsq<Real>(d2);
+        const Real dir2 = gam[0] * gam[0];
+        gam[1] = gam[0] * dir2;
+        gam[2] = Real(3) * gam[1] * dir2;
+        gam[3] = Real(5) * gam[2] * dir2;
+        gam[4] = Real(7) * gam[3] * dir2;
+        gam[5] = Real(9) * gam[4] * dir2;
+        Real ax = 0, ay = 0, az = 0, pot = 0;
+        qeval_cell<Real>(iOrder, m, q, o, h, gam, dx, dy, dz, ax, ay, az, pot);
+        kahan_add(A.s[0], A.c[0], ax);
+        kahan_add(A.s[1], A.c[1], ay);
+        kahan_add(A.s[2], A.c[2], az);
+        if constexpr (sizeof(Real) == 4) kahan_add(A.s[3], A.c[3], pot);
+        else A.t[3] += pot;
+        const Real idt2 = (mi + m) * gam[1];
+        A.dt = idt2 > A.dt ? idt2 : A.dt;
     }
 }
 
@@ -515,10 +655,12 @@ __device__ __forceinline__ void stage_cells(WalkSmem<Real, NBT> &S, const int *b
 // i: acceleration, potential, and (m_i + m) / r^3 for the timestep.  FP32
 // evaluates two cells per packed instruction into tile partials that are
 // folded into the compensated sums once per tile.
-template <typename Real, int NBT>
-__device__ __forceinline__ void eval_newt(WalkSmem<Real, NBT> &S, int cnt, int i, int slot, int iOrder,
+template <typename Real, int NBT, bool HIGH>
+__device__ __forceinline__ void eval_newt(WalkSmem<Real, NBT, HIGH> &S, int cnt, int i, int slot, int iOrder,
                                           Acc<Real> &A) {
-    if constexpr (sizeof(Real) == 4) {
+    if constexpr (HIGH) {
+        eval_newt_high<Real, NBT, HIGH>(S, cnt, i, slot, iOrder, A);
+    } else if constexpr (sizeof(Real) == 4) {
         const float2 X = p_splat(S.px[i]), Y = p_splat(S.py[i]), Z = p_splat(S.pz[i]);
         const float2 M = p_splat(S.pm[i]);
         const float2 three = p_splat(3.0f), five = p_splat(5.0f), half = p_splat(0.5f);
@@ -636,8 +778,8 @@ __device__ __forceinline__ void soft_term(Real xi, Real yi, Real zi, Real hi, Re
     idt2 = (mi + m) * b;
 }
 
-template <typename Real, int NBT>
-__device__ __forceinline__ void eval_soft(WalkSmem<Real, NBT> &S, int cnt, int i, int slot, Acc<Real> &A) {
+template <typename Real, int NBT, bool HIGH>
+__device__ __forceinline__ void eval_soft(WalkSmem<Real, NBT, HIGH> &S, int cnt, int i, int slot, Acc<Real> &A) {
     const Real xi = S.px[i], yi = S.py[i], zi = S.pz[i], hi = S.ph[i], mi = S.pm[i];
     if constexpr (sizeof(Real) == 4) {
         const int np = (cnt + 1) >> 1;
@@ -710,11 +852,12 @@ struct WalkTally {
 // NA cells are evaluated first, as Newtonian cells, and the walk starts
 // from the group's U entries; otherwise it starts from the root in every
 // replica.  Either way the lists are the reference's.
-template <typename Real, int NBT>
-__device__ __forceinline__ void walk_bucket(const WalkArgs &W, WalkSmem<Real, NBT> &S, int b,
+template <typename Real, int NBT, bool HIGH>
+__device__ __forceinline__ void walk_bucket(const WalkArgs &W, WalkSmem<Real, NBT, HIGH> &S, int b,
                                             const int *gl, WalkTally &K, int lane) {
     const TsphDevTree &T = W.T;
     const TsphDevParts &P = W.P;
+    constexpr int CT = cell_tile<HIGH>();   // cells per tile
     const unsigned FULL = 0xffffffffu;
     const float u32 = 5.9604645e-08f;   // 2^-24
     const float relF = 4.0f * u32;
@@ -776,13 +919,13 @@ __device__ __forceinline__ void walk_bucket(const WalkArgs &W, WalkSmem<Real, NB
     if (gl) {
         const int nU = S.gU, nNA = S.gNA;
         __syncwarp();
-        for (int k0 = 0; k0 < nNA; k0 += CNF) {
-            const int c = nNA - k0 < CNF ? nNA - k0 : CNF;
+        for (int k0 = 0; k0 < nNA; k0 += CT) {
+            const int c = nNA - k0 < CT ? nNA - k0 : CT;
             for (int e = lane; e < c; e += 32) S.cn[e] = gl[GRP_U + k0 + e];
             __syncwarp();
-            stage_cells<Real, NBT>(S, S.cn, T, c, lane, false, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
+            stage_cells<Real, NBT, HIGH>(S, S.cn, T, c, lane, false, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
             __syncwarp();
-            if (i < n) eval_newt<Real, NBT>(S, c, i, slot, W.iOrder, A);
+            if (i < n) eval_newt<Real, NBT, HIGH>(S, c, i, slot, W.iOrder, A);
             flush_tile(A);
             __syncwarp();
         }
@@ -908,11 +1051,11 @@ __device__ __forceinline__ void walk_bucket(const WalkArgs &W, WalkSmem<Real, NB
         __syncwarp();
         // evaluate full tiles
         while (ppn >= PPF) {
-            stage_pp<Real, NBT>(S, P, PPF, lane, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
+            stage_pp<Real, NBT, HIGH>(S, P, PPF, lane, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
             __syncwarp();
             if (i < n) {
-                if (ppSelf) eval_pp<Real, NBT, true>(S, PPF, i, slot, A);
-                else eval_pp<Real, NBT, false>(S, PPF, i, slot, A);
+                if (ppSelf) eval_pp<Real, NBT, HIGH, true>(S, PPF, i, slot, A);
+                else eval_pp<Real, NBT, HIGH, false>(S, PPF, i, slot, A);
             }
             ppSelf = false;
             flush_tile(A);
@@ -921,24 +1064,24 @@ __device__ __forceinline__ void walk_bucket(const WalkArgs &W, WalkSmem<Real, NB
             ppn -= PPF;
             __syncwarp();
         }
-        while (cnn >= CNF) {
-            stage_cells<Real, NBT>(S, S.cn, T, CNF, lane, false, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
+        while (cnn >= CT) {
+            stage_cells<Real, NBT, HIGH>(S, S.cn, T, CT, lane, false, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
             __syncwarp();
-            if (i < n) eval_newt<Real, NBT>(S, CNF, i, slot, W.iOrder, A);
+            if (i < n) eval_newt<Real, NBT, HIGH>(S, CT, i, slot, W.iOrder, A);
             flush_tile(A);
             __syncwarp();
-            for (int e = lane; e < cnn - CNF; e += 32) S.cn[e] = S.cn[CNF + e];
-            cnn -= CNF;
+            for (int e = lane; e < cnn - CT; e += 32) S.cn[e] = S.cn[CT + e];
+            cnn -= CT;
             __syncwarp();
         }
-        while (csn >= CNF) {
-            stage_cells<Real, NBT>(S, S.cs, T, CNF, lane, true, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
+        while (csn >= CT) {
+            stage_cells<Real, NBT, HIGH>(S, S.cs, T, CT, lane, true, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
             __syncwarp();
-            if (i < n) eval_soft<Real, NBT>(S, CNF, i, slot, A);
+            if (i < n) eval_soft<Real, NBT, HIGH>(S, CT, i, slot, A);
             flush_tile(A);
             __syncwarp();
-            for (int e = lane; e < csn - CNF; e += 32) S.cs[e] = S.cs[CNF + e];
-            csn -= CNF;
+            for (int e = lane; e < csn - CT; e += 32) S.cs[e] = S.cs[CT + e];
+            csn -= CT;
             __syncwarp();
         }
     }
@@ -949,26 +1092,26 @@ __device__ __forceinline__ void walk_bucket(const WalkArgs &W, WalkSmem<Real, NB
     }
     // remaining partial tiles
     if (ppn > 0) {
-        stage_pp<Real, NBT>(S, P, ppn, lane, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
+        stage_pp<Real, NBT, HIGH>(S, P, ppn, lane, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
         __syncwarp();
         if (i < n) {
-            if (ppSelf) eval_pp<Real, NBT, true>(S, ppn, i, slot, A);
-            else eval_pp<Real, NBT, false>(S, ppn, i, slot, A);
+            if (ppSelf) eval_pp<Real, NBT, HIGH, true>(S, ppn, i, slot, A);
+            else eval_pp<Real, NBT, HIGH, false>(S, ppn, i, slot, A);
         }
         flush_tile(A);
         __syncwarp();
     }
     if (cnn > 0) {
-        stage_cells<Real, NBT>(S, S.cn, T, cnn, lane, false, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
+        stage_cells<Real, NBT, HIGH>(S, S.cn, T, cnn, lane, false, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
         __syncwarp();
-        if (i < n) eval_newt<Real, NBT>(S, cnn, i, slot, W.iOrder, A);
+        if (i < n) eval_newt<Real, NBT, HIGH>(S, cnn, i, slot, W.iOrder, A);
         flush_tile(A);
         __syncwarp();
     }
     if (csn > 0) {
-        stage_cells<Real, NBT>(S, S.cs, T, csn, lane, true, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
+        stage_cells<Real, NBT, HIGH>(S, S.cs, T, csn, lane, true, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
         __syncwarp();
-        if (i < n) eval_soft<Real, NBT>(S, csn, i, slot, A);
+        if (i < n) eval_soft<Real, NBT, HIGH>(S, csn, i, slot, A);
         flush_tile(A);
         __syncwarp();
     }
@@ -1027,8 +1170,8 @@ __device__ __forceinline__ void walk_bucket(const WalkArgs &W, WalkSmem<Real, NB
 // The FP32 tests carry the bucket walk's rounding bound, so every such
 // verdict is the one each bucket's FP64 test would reach.  Returns false
 // when a list or the stack overflows (the buckets then walk from the root).
-template <typename Real, int NBT>
-__device__ __noinline__ bool walk_group(const WalkArgs &W, WalkSmem<Real, NBT> &S, int g, int b0,
+template <typename Real, int NBT, bool HIGH>
+__device__ __noinline__ bool walk_group(const WalkArgs &W, WalkSmem<Real, NBT, HIGH> &S, int g, int b0,
                                         int b1, int *gl, WalkTally &K, int lane) {
     const TsphDevTree &T = W.T;
     const unsigned FULL = 0xffffffffu;
@@ -1145,14 +1288,15 @@ __device__ __noinline__ bool walk_group(const WalkArgs &W, WalkSmem<Real, NBT> &
     return ok;
 }
 
-// FP32: five resident blocks per SM (96 registers, 44 KB of shared memory
-// per block); FP64: limited by its larger tiles.
-template <typename Real, int NBT>
-__global__ void __launch_bounds__(WPB * 32, sizeof(Real) == 4 ? 5 : 1) k_walk(WalkArgs W) {
+// FP32: five resident blocks per SM (96 registers, 40 KB of shared memory
+// per block), three with octopole/hexadecapole cells; FP64: limited by its
+// larger tiles.
+template <typename Real, int NBT, bool HIGH>
+__global__ void __launch_bounds__(WPB * 32, sizeof(Real) == 4 ? (HIGH ? 3 : 5) : 1) k_walk(WalkArgs W) {
     extern __shared__ __align__(16) unsigned char smraw[];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
-    WalkSmem<Real, NBT> &S = reinterpret_cast<WalkSmem<Real, NBT> *>(smraw)[wib];
+    WalkSmem<Real, NBT, HIGH> &S = reinterpret_cast<WalkSmem<Real, NBT, HIGH> *>(smraw)[wib];
     const unsigned FULL = 0xffffffffu;
     WalkTally K = {0u, 0u, 0u};
     if (lane == 0) S.tAct = S.tPP = S.tNewt = S.tSoft = S.tBsq = S.tIntra = 0ull;
@@ -1182,12 +1326,12 @@ __global__ void __launch_bounds__(WPB * 32, sizeof(Real) == 4 ? 5 : 1) k_walk(Wa
                         g = p;
                     }
                 g = __shfl_sync(FULL, g, 0);
-                grp = walk_group<Real, NBT>(W, S, g, b0, b1, gl, K, lane);
+                grp = walk_group<Real, NBT, HIGH>(W, S, g, b0, b1, gl, K, lane);
             }
-            for (int b = b0; b < b1; ++b) walk_bucket<Real, NBT>(W, S, b, grp ? gl : nullptr, K, lane);
+            for (int b = b0; b < b1; ++b) walk_bucket<Real, NBT, HIGH>(W, S, b, grp ? gl : nullptr, K, lane);
         } else {
             if (u >= *W.nBuckets) break;
-            walk_bucket<Real, NBT>(W, S, u, nullptr, K, lane);
+            walk_bucket<Real, NBT, HIGH>(W, S, u, nullptr, K, lane);
         }
     }
     // counters: tests and visits per lane, the rest from the warp's tallies
@@ -1357,19 +1501,19 @@ static int prepare_groups(tsph_ctx *ctx, WalkArgs &A, int nbHost, int warps) {
     return TSPH_OK;
 }
 
-template <typename Real, int NBT>
+template <typename Real, int NBT, bool HIGH>
 static int launch_walk(tsph_ctx *ctx, const WalkArgs &A, int blocks, const char *name) {
-    size_t sm = sizeof(WalkSmem<Real, NBT>) * WPB;
+    size_t sm = sizeof(WalkSmem<Real, NBT, HIGH>) * WPB;
     if (!ctx->capturing)
-        TSPH_CK(cudaFuncSetAttribute(k_walk<Real, NBT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        TSPH_CK(cudaFuncSetAttribute(k_walk<Real, NBT, HIGH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)sm));
-    k_walk<Real, NBT><<<blocks, WPB * 32, sm, ctx->stream>>>(A);
+    k_walk<Real, NBT, HIGH><<<blocks, WPB * 32, sm, ctx->stream>>>(A);
     TSPH_LAUNCH_CK(name);
     return TSPH_OK;
 }
 
 int tsph_walk_interact(tsph_ctx *ctx, const tsph_grav_params *gp) {
-    if (gp->iOrder < 1 || gp->iOrder > 2) return TSPH_ERR_UNSUPPORTED;
+    if (gp->iOrder < 1 || gp->iOrder > 4) return TSPH_ERR_ARG;
     if (gp->bPeriodic && gp->nReps > 1) return TSPH_ERR_UNSUPPORTED;
     if (gp->nBucket > 32) return TSPH_ERR_UNSUPPORTED;
     WalkConst wc;
@@ -1427,7 +1571,7 @@ int tsph_walk_interact(tsph_ctx *ctx, const tsph_grav_params *gp) {
     TSPH_CK(cudaMemsetAsync(A.workCounter, 0, sizeof(int), ctx->stream));
     k_bucket_prep<<<tsph_blocks(nbHost, 128), 128, 0, ctx->stream>>>(ctx->T, ctx->P);
     TSPH_LAUNCH_CK("k_bucket_prep");
-    const int wbDefault = gp->precision == TSPH_FP32 ? 5 : 4;
+    const int wbDefault = gp->precision == TSPH_FP32 ? (gp->iOrder >= 3 ? 3 : 5) : 4;
     int blocks = ctx->smCount * (ctx->walkBlocksPerSM > 0 ? ctx->walkBlocksPerSM : wbDefault);
     A.groupFirst = nullptr;
     A.nGroups = nullptr;
@@ -1436,14 +1580,24 @@ int tsph_walk_interact(tsph_ctx *ctx, const tsph_grav_params *gp) {
     rc = prepare_groups(ctx, A, nbHost, blocks * WPB);
     if (rc) return rc;
     const int nbt = gp->nBucket <= 8 ? 8 : (gp->nBucket <= 16 ? 16 : 32);
-    if (gp->precision == TSPH_FP32) {
-        if (nbt == 8) rc = launch_walk<float, 8>(ctx, A, blocks, "k_walk<float,8>");
-        else if (nbt == 16) rc = launch_walk<float, 16>(ctx, A, blocks, "k_walk<float,16>");
-        else rc = launch_walk<float, 32>(ctx, A, blocks, "k_walk<float,32>");
+    if (gp->iOrder >= 3) {   // octopole / hexadecapole cells
+        if (gp->precision == TSPH_FP32) {
+            if (nbt == 8) rc = launch_walk<float, 8, true>(ctx, A, blocks, "k_walk<float,8,high>");
+            else if (nbt == 16) rc = launch_walk<float, 16, true>(ctx, A, blocks, "k_walk<float,16,high>");
+            else rc = launch_walk<float, 32, true>(ctx, A, blocks, "k_walk<float,32,high>");
+        } else {
+            if (nbt == 8) rc = launch_walk<double, 8, true>(ctx, A, blocks, "k_walk<double,8,high>");
+            else if (nbt == 16) rc = launch_walk<double, 16, true>(ctx, A, blocks, "k_walk<double,16,high>");
+            else rc = launch_walk<double, 32, true>(ctx, A, blocks, "k_walk<double,32,high>");
+        }
+    } else if (gp->precision == TSPH_FP32) {
+        if (nbt == 8) rc = launch_walk<float, 8, false>(ctx, A, blocks, "k_walk<float,8>");
+        else if (nbt == 16) rc = launch_walk<float, 16, false>(ctx, A, blocks, "k_walk<float,16>");
+        else rc = launch_walk<float, 32, false>(ctx, A, blocks, "k_walk<float,32>");
     } else {
-        if (nbt == 8) rc = launch_walk<double, 8>(ctx, A, blocks, "k_walk<double,8>");
-        else if (nbt == 16) rc = launch_walk<double, 16>(ctx, A, blocks, "k_walk<double,16>");
-        else rc = launch_walk<double, 32>(ctx, A, blocks, "k_walk<double,32>");
+        if (nbt == 8) rc = launch_walk<double, 8, false>(ctx, A, blocks, "k_walk<double,8>");
+        else if (nbt == 16) rc = launch_walk<double, 16, false>(ctx, A, blocks, "k_walk<double,16>");
+        else rc = launch_walk<double, 32, false>(ctx, A, blocks, "k_walk<double,32>");
     }
     if (rc) return rc;
     return TSPH_OK;

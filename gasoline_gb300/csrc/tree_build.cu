@@ -1102,7 +1102,90 @@ __device__ __forceinline__ void store_com32(TsphDevTree &T, int i, double x, dou
 // children in the reference's order (pkd.c:2522-2547); the quadrupole by the
 // parallel-axis theorem (equal to the reference's direct sum up to
 // rounding).  Children may have been written by other SMs: read past L1.
-__device__ void combine_node(TsphDevTree &T, int i) {
+// --- octopole and hexadecapole cells (iOrder >= 3) ------------------------
+// Complete moments about each node's centre of mass, M3_abc = sum m d_a d_b
+// d_c (10) and M4_abcd (15), in the field order of the reference's reduced
+// moments (pkd.h:441-451): xxx xyy xxy yyy xxz yyz xyz xzz yzz zzz and
+// xxxx xyyy xxxy yyyy xxxz yyyz xxyy xxyz xyyz xxzz xyzz xzzz yyzz yzzz zzzz.
+// Leaves sum them over their particles; a parent adds its children's moments
+// shifted to its own centre by the binomial expansion of (d' + D)^k, as the
+// quadrupole is combined.  The reduced (trace-free) moments pkdCalcCell
+// sums per particle (pkd.c:2076-2128) follow from the complete ones by
+// linear identities (k_open).
+__host__ __device__ constexpr int q_index(int a, int b) {
+    return a == b ? a : (a + b == 1 ? 3 : (a + b == 2 ? 4 : 5));   // xx yy zz xy xz yz
+}
+__host__ __device__ constexpr int m3_index(int a, int b, int c) {
+    // sort a <= b <= c
+    int t = 0;
+    if (a > b) { t = a; a = b; b = t; }
+    if (b > c) { t = b; b = c; c = t; }
+    if (a > b) { t = a; a = b; b = t; }
+    const int code = a * 9 + b * 3 + c;
+    return code == 0 ? 0 : code == 4 ? 1 : code == 1 ? 2 : code == 13 ? 3 : code == 2 ? 4 :
+           code == 14 ? 5 : code == 5 ? 6 : code == 8 ? 7 : code == 17 ? 8 : 9;
+}
+
+__device__ __forceinline__ void leaf_high(const double *d, double m, double *m3, double *m4) {
+    const double x = d[0], y = d[1], z = d[2];
+    const double xx = xmul(x, x), yy = xmul(y, y), zz = xmul(z, z);
+    const double mx = xmul(m, x), my = xmul(m, y), mz = xmul(m, z);
+    m3[0] = xadd(m3[0], xmul(mx, xx));
+    m3[1] = xadd(m3[1], xmul(mx, yy));
+    m3[2] = xadd(m3[2], xmul(my, xx));
+    m3[3] = xadd(m3[3], xmul(my, yy));
+    m3[4] = xadd(m3[4], xmul(mz, xx));
+    m3[5] = xadd(m3[5], xmul(mz, yy));
+    m3[6] = xadd(m3[6], xmul(xmul(mx, y), z));
+    m3[7] = xadd(m3[7], xmul(mx, zz));
+    m3[8] = xadd(m3[8], xmul(my, zz));
+    m3[9] = xadd(m3[9], xmul(mz, zz));
+    m4[0] = xadd(m4[0], xmul(xmul(m, xx), xx));
+    m4[1] = xadd(m4[1], xmul(xmul(mx, yy), y));
+    m4[2] = xadd(m4[2], xmul(xmul(mx, xx), y));
+    m4[3] = xadd(m4[3], xmul(xmul(m, yy), yy));
+    m4[4] = xadd(m4[4], xmul(xmul(mx, xx), z));
+    m4[5] = xadd(m4[5], xmul(xmul(my, yy), z));
+    m4[6] = xadd(m4[6], xmul(xmul(m, xx), yy));
+    m4[7] = xadd(m4[7], xmul(xmul(m, xx), xmul(y, z)));
+    m4[8] = xadd(m4[8], xmul(xmul(mx, yy), z));
+    m4[9] = xadd(m4[9], xmul(xmul(m, xx), zz));
+    m4[10] = xadd(m4[10], xmul(xmul(mx, y), zz));
+    m4[11] = xadd(m4[11], xmul(xmul(mx, zz), z));
+    m4[12] = xadd(m4[12], xmul(xmul(m, yy), zz));
+    m4[13] = xadd(m4[13], xmul(xmul(my, zz), z));
+    m4[14] = xadd(m4[14], xmul(xmul(m, zz), zz));
+}
+
+// Child moments (mass m, complete Q, M3, M4 about its own centre) shifted
+// by d = child centre - parent centre, added into the parent's M3, M4.
+__device__ __forceinline__ void shift_high(const double *d, double m, const double *q, const double *c3,
+                                           const double *c4, double *m3, double *m4) {
+    constexpr unsigned char I3[10][3] = {{0, 0, 0}, {0, 1, 1}, {0, 0, 1}, {1, 1, 1}, {0, 0, 2},
+                                         {1, 1, 2}, {0, 1, 2}, {0, 2, 2}, {1, 2, 2}, {2, 2, 2}};
+    constexpr unsigned char I4[15][4] = {{0, 0, 0, 0}, {0, 1, 1, 1}, {0, 0, 0, 1}, {1, 1, 1, 1},
+                                         {0, 0, 0, 2}, {1, 1, 1, 2}, {0, 0, 1, 1}, {0, 0, 1, 2},
+                                         {0, 1, 1, 2}, {0, 0, 2, 2}, {0, 1, 2, 2}, {0, 2, 2, 2},
+                                         {1, 1, 2, 2}, {1, 2, 2, 2}, {2, 2, 2, 2}};
+#pragma unroll
+    for (int k = 0; k < 10; ++k) {
+        const int a = I3[k][0], b = I3[k][1], c = I3[k][2];
+        m3[k] += c3[k] + q[q_index(a, b)] * d[c] + q[q_index(a, c)] * d[b] + q[q_index(b, c)] * d[a] +
+                 m * d[a] * d[b] * d[c];
+    }
+#pragma unroll
+    for (int k = 0; k < 15; ++k) {
+        const int a = I4[k][0], b = I4[k][1], c = I4[k][2], e = I4[k][3];
+        m4[k] += c4[k] + c3[m3_index(b, c, e)] * d[a] + c3[m3_index(a, c, e)] * d[b] +
+                 c3[m3_index(a, b, e)] * d[c] + c3[m3_index(a, b, c)] * d[e] +
+                 q[q_index(c, e)] * d[a] * d[b] + q[q_index(b, e)] * d[a] * d[c] +
+                 q[q_index(b, c)] * d[a] * d[e] + q[q_index(a, e)] * d[b] * d[c] +
+                 q[q_index(a, c)] * d[b] * d[e] + q[q_index(a, b)] * d[c] * d[e] +
+                 m * d[a] * d[b] * d[c] * d[e];
+    }
+}
+
+__device__ void combine_node(TsphDevTree &T, int i, int high) {
     const int l = i + 1, u = T.upper[i];
     double fMass = 0.0, fSoft = 0.0, r[3] = {0.0, 0.0, 0.0};
     double fm = __ldcg(&T.fMass[l]);
@@ -1142,6 +1225,32 @@ __device__ void combine_node(TsphDevTree &T, int i) {
         q[4] += mc * dx * dz;
         q[5] += mc * dy * dz;
     }
+    if (high) {   // complete M3, M4 from the children's, before q is final
+        double m3[10], m4[15];
+#pragma unroll
+        for (int k = 0; k < 10; ++k) m3[k] = 0.0;
+#pragma unroll
+        for (int k = 0; k < 15; ++k) m4[k] = 0.0;
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
+            const int ch = cc[s];
+            const double mc = __ldcg(&T.fMass[ch]);
+            const double d[3] = {__ldcg(&T.r[3 * ch]) - r[0], __ldcg(&T.r[3 * ch + 1]) - r[1],
+                                 __ldcg(&T.r[3 * ch + 2]) - r[2]};
+            double qc[6], c3[10], c4[15];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) qc[k] = __ldcg(&T.Q[6 * ch + k]);
+#pragma unroll
+            for (int k = 0; k < 10; ++k) c3[k] = __ldcg(&T.M3[10 * (size_t)ch + k]);
+#pragma unroll
+            for (int k = 0; k < 15; ++k) c4[k] = __ldcg(&T.M4[15 * (size_t)ch + k]);
+            shift_high(d, mc, qc, c3, c4, m3, m4);
+        }
+#pragma unroll
+        for (int k = 0; k < 10; ++k) T.M3[10 * (size_t)i + k] = m3[k];
+#pragma unroll
+        for (int k = 0; k < 15; ++k) T.M4[15 * (size_t)i + k] = m4[k];
+    }
 #pragma unroll
     for (int k = 0; k < 6; ++k) T.Q[6 * i + k] = q[k];
 }
@@ -1153,7 +1262,7 @@ __device__ void combine_node(TsphDevTree &T, int i) {
 // node is formed once, after both children, with no per-level launches.
 __global__ void k_moments(TsphDevTree T, const double *__restrict__ x, const double *__restrict__ y,
                           const double *__restrict__ z, const double *__restrict__ m,
-                          const double *__restrict__ h, int *visit) {
+                          const double *__restrict__ h, int *visit, int high) {
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= T.dcnt[1]) return;
     int i = T.leaves[b];
@@ -1192,13 +1301,28 @@ __global__ void k_moments(TsphDevTree T, const double *__restrict__ x, const dou
     }
 #pragma unroll
     for (int k = 0; k < 6; ++k) T.Q[6 * i + k] = q[k];
+    if (high) {
+        double m3[10], m4[15];
+#pragma unroll
+        for (int k = 0; k < 10; ++k) m3[k] = 0.0;
+#pragma unroll
+        for (int k = 0; k < 15; ++k) m4[k] = 0.0;
+        for (int p = lo; p <= hi; ++p) {
+            const double d[3] = {xsub(x[p], r0), xsub(y[p], r1), xsub(z[p], r2)};
+            leaf_high(d, m[p], m3, m4);
+        }
+#pragma unroll
+        for (int k = 0; k < 10; ++k) T.M3[10 * (size_t)i + k] = m3[k];
+#pragma unroll
+        for (int k = 0; k < 15; ++k) T.M4[15 * (size_t)i + k] = m4[k];
+    }
     for (;;) {
         __threadfence();
         int par = T.parent[i];
         if (par < 0) break;
         if (atomicAdd(&visit[par], 1) == 0) break;   // the sibling is not done yet
         __threadfence();
-        combine_node(T, par);
+        combine_node(T, par, high);
         i = par;
     }
 }
@@ -1281,8 +1405,44 @@ __global__ void k_bmax_exact(int n, TsphDevTree T, const double *__restrict__ x,
 }
 
 // Opening radius, OPEN_JOSH (pkd.c:2245-2253); walk copies in FP32.
+// Reduced octopole and hexadecapole (pkdCalcCell pkd.c:2076-2128) from the
+// complete moments: sum m (d_a d_b d_c - 0.2 d^2 (...)) etc. are linear in
+// the complete moments, with sum m d^2 d_a = T_a and sum m d^2 d_a d_b =
+// S_ab, sum m d^4 = S_xx + S_yy + S_zz.
+__device__ __forceinline__ void reduce_high(const double *M, const double *H4, double *o, double *h) {
+    const double Tx = M[0] + M[1] + M[7], Ty = M[2] + M[3] + M[8], Tz = M[4] + M[5] + M[9];
+    o[0] = M[0] - 0.6 * Tx;   // xxx
+    o[1] = M[1] - 0.2 * Tx;   // xyy
+    o[2] = M[2] - 0.2 * Ty;   // xxy
+    o[3] = M[3] - 0.6 * Ty;   // yyy
+    o[4] = M[4] - 0.2 * Tz;   // xxz
+    o[5] = M[5] - 0.2 * Tz;   // yyz
+    o[6] = M[6];              // xyz
+    o[7] = M[7] - 0.2 * Tx;   // xzz
+    o[8] = M[8] - 0.2 * Ty;   // yzz
+    o[9] = M[9] - 0.6 * Tz;   // zzz
+    const double Sxx = H4[0] + H4[6] + H4[9], Syy = H4[6] + H4[3] + H4[12], Szz = H4[9] + H4[12] + H4[14];
+    const double Sxy = H4[2] + H4[1] + H4[10], Sxz = H4[4] + H4[8] + H4[11], Syz = H4[7] + H4[5] + H4[13];
+    const double S4 = Sxx + Syy + Szz;
+    h[0] = H4[0] - 6.0 / 7.0 * Sxx + 0.6 / 7.0 * S4;            // xxxx
+    h[1] = H4[1] - 3.0 / 7.0 * Sxy;                             // xyyy
+    h[2] = H4[2] - 3.0 / 7.0 * Sxy;                             // xxxy
+    h[3] = H4[3] - 6.0 / 7.0 * Syy + 0.6 / 7.0 * S4;            // yyyy
+    h[4] = H4[4] - 3.0 / 7.0 * Sxz;                             // xxxz
+    h[5] = H4[5] - 3.0 / 7.0 * Syz;                             // yyyz
+    h[6] = H4[6] - 1.0 / 7.0 * (Sxx + Syy) + 0.2 / 7.0 * S4;    // xxyy
+    h[7] = H4[7] - 1.0 / 7.0 * Syz;                             // xxyz
+    h[8] = H4[8] - 1.0 / 7.0 * Sxz;                             // xyyz
+    h[9] = H4[9] - 1.0 / 7.0 * (Sxx + Szz) + 0.2 / 7.0 * S4;    // xxzz
+    h[10] = H4[10] - 1.0 / 7.0 * Sxy;                           // xyzz
+    h[11] = H4[11] - 3.0 / 7.0 * Sxz;                           // xzzz
+    h[12] = H4[12] - 1.0 / 7.0 * (Syy + Szz) + 0.2 / 7.0 * S4;  // yyzz
+    h[13] = H4[13] - 3.0 / 7.0 * Syz;                           // yzzz
+    h[14] = H4[14] - 6.0 / 7.0 * Szz + 0.6 / 7.0 * S4;          // zzzz
+}
+
 __global__ void k_open(TsphDevTree T, const unsigned long long *__restrict__ maxd2,
-                       double twoOverSqrt3, double dCrit) {
+                       double twoOverSqrt3, double dCrit, int high) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= T.dcnt[0]) return;
     double Bmax = sqrt(__longlong_as_double((long long)maxd2[i]));
@@ -1302,6 +1462,21 @@ __global__ void k_open(TsphDevTree T, const unsigned long long *__restrict__ max
     const double *q = &T.Q[6 * i];
     T.wmom0[i] = make_float4((float)T.fMass[i], (float)q[0], (float)q[1], (float)q[2]);
     T.wmom1[i] = make_float4((float)q[3], (float)q[4], (float)q[5], (float)T.fSoft[i]);
+    if (high) {
+        double M[10], H4[15], oh[25];
+#pragma unroll
+        for (int k = 0; k < 10; ++k) M[k] = T.M3[10 * (size_t)i + k];
+#pragma unroll
+        for (int k = 0; k < 15; ++k) H4[k] = T.M4[15 * (size_t)i + k];
+        reduce_high(M, H4, oh, oh + 10);
+        if (T.pUpper[i] < T.pLower[i])
+            for (int k = 0; k < 25; ++k) oh[k] = 0.0;
+#pragma unroll
+        for (int k = 0; k < 25; ++k) {
+            T.OH[25 * (size_t)i + k] = oh[k];
+            T.wOH[25 * (size_t)i + k] = (float)oh[k];
+        }
+    }
 }
 
 __global__ void k_parts32(int n, const double *__restrict__ x, const double *__restrict__ y,
@@ -1326,6 +1501,8 @@ void tsph_free_tree(TsphDevTree &T) {
     TFREE(T.fSplit); TFREE(T.bnd); TFREE(T.fMass); TFREE(T.fSoft); TFREE(T.r);
     TFREE(T.fOpen2); TFREE(T.Bmax); TFREE(T.Q); TFREE(T.wcomh); TFREE(T.wcoml);
     TFREE(T.wlink); TFREE(T.wmom0); TFREE(T.wmom1); TFREE(T.leaves); TFREE(T.parent);
+    TFREE(T.M3); TFREE(T.M4); TFREE(T.OH); TFREE(T.wOH);
+    T.highCap = 0;
     TFREE(T.rLo); TFREE(T.rHi); TFREE(T.sysRoot); TFREE(T.rEnd); TFREE(T.dcnt);
     if (T.brec) cudaFree(T.brec);
     T.brec = nullptr;
@@ -1756,13 +1933,23 @@ static int build_tree_body(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n
     return TSPH_OK;
 }
 
-int tsph_tree_moments(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, double dTheta) {
+int tsph_tree_moments(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, double dTheta, int order) {
     TsphBuildBufs &B = ctx->B;
     const int BS = 256;
     if (n == 0) return TSPH_OK;
     const int nodeNeed = 2 * n;
+    const int high = order >= 3;
+    if (high && T.highCap < T.cap) {   // octopole/hexadecapole storage, on first use
+        if (ctx->capturing) return TSPH_ERR_STATE;
+        int rc = tsph_grow(ctx, &T.M3, (size_t)10 * T.cap);
+        rc |= tsph_grow(ctx, &T.M4, (size_t)15 * T.cap);
+        rc |= tsph_grow(ctx, &T.OH, (size_t)25 * T.cap);
+        rc |= tsph_grow(ctx, &T.wOH, (size_t)25 * T.cap);
+        if (rc) return TSPH_ERR_NOMEM;
+        T.highCap = T.cap;
+    }
     TSPH_CK(cudaMemsetAsync(B.visit, 0, sizeof(int) * (size_t)nodeNeed, ctx->stream));
-    k_moments<<<tsph_blocks(n, 128), 128, 0, ctx->stream>>>(T, P.x, P.y, P.z, P.m, P.h, B.visit);
+    k_moments<<<tsph_blocks(n, 128), 128, 0, ctx->stream>>>(T, P.x, P.y, P.z, P.m, P.h, B.visit, high);
     TSPH_LAUNCH_CK("k_moments");
     k_parts32<<<tsph_blocks(n, BS), BS, 0, ctx->stream>>>(n, P.x, P.y, P.z, P.m, P.h, P.ph, P.pl);
     TSPH_LAUNCH_CK("k_parts32");
@@ -1778,7 +1965,7 @@ int tsph_tree_moments(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, dou
                                                              eabs, maxLo, B.maxd2);
     TSPH_LAUNCH_CK("k_bmax_exact");
     const double twoOverSqrt3 = 2 / sqrt(3.0);
-    k_open<<<tsph_blocks(nodeNeed, BS), BS, 0, ctx->stream>>>(T, B.maxd2, twoOverSqrt3, dTheta);
+    k_open<<<tsph_blocks(nodeNeed, BS), BS, 0, ctx->stream>>>(T, B.maxd2, twoOverSqrt3, dTheta, high);
     TSPH_LAUNCH_CK("k_open");
     return TSPH_OK;
 }

@@ -70,6 +70,12 @@ struct TsphDevTree {
     int4 *wlink;      // pLower, count, upper (-1 leaf), 0
     float4 *wmom0;    // m, Qxx, Qyy, Qzz
     float4 *wmom1;    // Qxy, Qxz, Qyz, fSoft
+    // octopole and hexadecapole cells (iOrder >= 3; sized on first use)
+    double *M3, *M4;  // complete 3rd (10) and 4th (15) moments about the COM
+    double *OH;       // reduced octopole (10) + hexadecapole (15) per node,
+                      // pkdCalcCell's O* and H* in its field order
+    float *wOH;       // FP32 copies of OH, 25 per node
+    int highCap;      // nodes M3/M4/OH/wOH hold
     int *leaves;      // leaf node ids in depth-first order (the buckets)
     int *parent;      // parent node, -1 at a root
     // forest of independent trees over contiguous particle ranges (one

@@ -79,9 +79,13 @@ enum tsph_smx {
  * arithmetic precision.  Comoving and Sun-indirect terms (bComove,
  * bDoSun) are not part of this path.
  */
+#define TSPH_MAX_BUCKET 32   /* largest nBucket: one warp walks one bucket */
+
 typedef struct {
-    int nBucket;      /* max particles per leaf (reference default 8) */
-    int iOrder;       /* cell multipole order, 1..4 (2 = quadrupole) */
+    int nBucket;      /* max particles per leaf, 1..TSPH_MAX_BUCKET (reference
+                         default 8; larger returns TSPH_ERR_UNSUPPORTED) */
+    int iOrder;       /* cell multipole order, 1..4: 2 = quadrupole, 3 octopole,
+                         4 hexadecapole (the reference's default) */
     int bPeriodic;
     int bEwald;
     int iEwOrder;     /* Ewald multipole order, 1..4 */

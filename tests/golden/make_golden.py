@@ -50,6 +50,19 @@ def sph_case(name, pos, vel, mass, soft, u, sp):
     print(name, len(mass))
 
 
+def high_order_cases():
+    """Octopole and hexadecapole cells (iOrder 3 and 4, the reference's
+    default order): a Plummer sphere and a periodic lattice box."""
+    pos, vel, m = ics.plummer(2048, seed=24)
+    grav_case("grav_plummer_2k_o4", pos, m, np.full(len(m), 0.01),
+              oracle.grav_params(periodic=False, iOrder=4))
+    grav_case("grav_plummer_2k_o3", pos, m, np.full(len(m), 0.01),
+              oracle.grav_params(periodic=False, iOrder=3))
+    pos, vel, m = ics.lattice_box(8, seed=25)
+    grav_case("grav_box_8_o4", pos, m, np.full(len(m), 1.0 / (50 * 8)),
+              oracle.grav_params(periodic=True, ewald=True, iOrder=4))
+
+
 def sph_box_case():
     """Periodic SPH: a 16^3 gas lattice in the unit box displaced by a
     Gaussian random field (rms 0.25 of the spacing), velocities from the
@@ -188,6 +201,7 @@ def main():
     pos, vel, m = ics.uniform_cube(1500, seed=13)
     grav_case("grav_cube_soft", pos, m, np.full(len(m), 0.15),
               oracle.grav_params(periodic=False, nBucket=8, theta=0.7))
+    high_order_cases()
     pos, vel, m, u = ics.gas_sphere(2048, seed=14)
     rng = np.random.Generator(np.random.PCG64(15))
     vel = rng.normal(0.0, 0.1, (len(m), 3))
@@ -201,8 +215,10 @@ def main():
 
 
 if __name__ == "__main__":
-    # one group of fixtures only: python make_golden.py tipsy|multistep|render|sph_box|layout
-    if len(sys.argv) > 1 and sys.argv[1] in ("tipsy", "multistep", "render", "sph_box", "layout"):
+    # one group of fixtures only:
+    #   python make_golden.py tipsy|multistep|render|sph_box|layout|high_order
+    if len(sys.argv) > 1 and sys.argv[1] in ("tipsy", "multistep", "render", "sph_box", "layout",
+                                             "high_order"):
         if not oracle.reference_available():
             oracle.build_reference()
         if sys.argv[1] == "tipsy":
@@ -213,6 +229,8 @@ if __name__ == "__main__":
             sph_box_case()
         elif sys.argv[1] == "layout":
             particle_layout()
+        elif sys.argv[1] == "high_order":
+            high_order_cases()
         else:
             render_case()
     else:

@@ -4,7 +4,9 @@ import os
 import numpy as np
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-GRAV_CASES = ["grav_plummer_2k", "grav_box_8", "grav_cube_soft"]
+GRAV_CASES = ["grav_plummer_2k", "grav_box_8", "grav_cube_soft",
+              # octopole (iOrder 3) and hexadecapole (iOrder 4, the reference's default) cells
+              "grav_plummer_2k_o3", "grav_plummer_2k_o4", "grav_box_8_o4"]
 
 
 def load(name):
