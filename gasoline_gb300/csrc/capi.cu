@@ -64,7 +64,8 @@ extern "C" int tsph_create(tsph_ctx **pctx, int device, void *stream) {
     }
     for (int k = 0; k < 10; ++k) cudaEventCreate(&ctx->ev[k]);
     if (cudaMallocHost((void **)&ctx->hRoot, sizeof(double) * 64) != cudaSuccess ||
-        cudaEventCreateWithFlags(&ctx->evRoot, cudaEventDisableTiming) != cudaSuccess) {
+        cudaEventCreateWithFlags(&ctx->evRoot, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->evGather, cudaEventDisableTiming) != cudaSuccess) {
         tsph_destroy(ctx);
         return TSPH_ERR_NOMEM;
     }
@@ -121,6 +122,7 @@ extern "C" void tsph_destroy(tsph_ctx *ctx) {
     if (ctx->B.hostCount) cudaFreeHost(ctx->B.hostCount);
     for (int k = 0; k < 10; ++k) if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
     if (ctx->evRoot) cudaEventDestroy(ctx->evRoot);
+    if (ctx->evGather) cudaEventDestroy(ctx->evGather);
     if (ctx->hRoot) cudaFreeHost(ctx->hRoot);
     if (ctx->ownStream && ctx->stream) cudaStreamDestroy(ctx->stream);
     free(ctx);
@@ -436,16 +438,29 @@ extern "C" int tsph_grav_all(tsph_ctx *ctx, const tsph_grav_params *gp, tsph_gra
             n, ctx->C, ctx->P, ctx->dCnt, ctx->capLimit > 0 ? ctx->capLimit : INFINITY);
         TSPH_LAUNCH_CK("k_gather_tree");
     }
-    int rc = cap ? TSPH_OK : read_status(ctx);
+    // The gather's status and largest |coordinate| reach the host behind an
+    // event and are read once the tree build is queued: nothing in the
+    // build needs them (the moments' rounding floor and the walk's
+    // constants do), so the stream does not drain here.
+    if (!cap) {
+        TSPH_CK(cudaMemcpyAsync(ctx->hCnt, ctx->dCnt, sizeof(TsphDevCounters), cudaMemcpyDeviceToHost,
+                                ctx->stream));
+        TSPH_CK(cudaEventRecord(ctx->evGather, ctx->stream));
+    }
+    ctx->dPeriodTree = gp->bPeriodic ? gp->dPeriod : 0.0;
+    int rc = tsph_build_tree(ctx, ctx->P, ctx->T, n, gp->nBucket);
+    if (!cap) {
+        TSPH_CK(cudaEventSynchronize(ctx->evGather));
+        const unsigned st = ctx->hCnt->status;   // bad input reported before a build error
+        for (int k = 1; k < 32 && st; ++k)
+            if (st & (1u << k)) return k;
+    }
     if (rc) return rc;
     {
         double r;
         memcpy(&r, &ctx->hCnt->maxAbs, sizeof(r));
         ctx->coordScale = ctx->capLimit > 0 ? ctx->capLimit : r;
     }
-    ctx->dPeriodTree = gp->bPeriodic ? gp->dPeriod : 0.0;
-    rc = tsph_build_tree(ctx, ctx->P, ctx->T, n, gp->nBucket);
-    if (rc) return rc;
     if (!cap) cudaEventRecord(ctx->ev[1], ctx->stream);
     rc = tsph_tree_moments(ctx, ctx->P, ctx->T, n, gp->dTheta, gp->iOrder);
     if (rc) return rc;

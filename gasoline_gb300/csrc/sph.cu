@@ -254,13 +254,30 @@ __device__ int ball_gather(KnnSmem &W, const SphArgs &A, int lane, int root, flo
             W.u.stack[pos + 1] = node + 1;
         }
         sp += 2 * __popc(bo);
-        // leaf particles, in a fixed order (leaf-lane major, particle minor)
-        int cnt = leaf ? lk.y : 0;
-        int maxc = __reduce_max_sync(FULL, (unsigned)cnt);
-        for (int k = 0; k < maxc; ++k) {
+        // leaf particles, every lane one (leaf, particle) pair per step over
+        // all the leaves this round reached, in a fixed order (leaf-lane
+        // major, particle minor): the round's t-th particle belongs to the
+        // first lane whose inclusive count exceeds t
+        const int cnt = leaf ? lk.y : 0;
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o) incl += y;
+        }
+        const int tot = __shfl_sync(FULL, incl, 31);
+        const int base = lk.x - (incl - cnt);   // this lane's t-th particle: base + t
+        for (int t0 = 0; t0 < tot; t0 += 32) {
+            const int t = t0 + lane;
+            int own = 0;
+#pragma unroll
+            for (int st = 16; st > 0; st >>= 1) {
+                const int v = __shfl_sync(FULL, incl, own + st - 1);
+                if (v <= t) own += st;
+            }
+            const int j = __shfl_sync(FULL, base, own & 31) + t;
             float2 iv = make_float2(FLT_MAX, FLT_MAX);
-            int j = lk.x + k;
-            if (k < cnt) iv = d2_interval(hi_i, lo_i, A.G.ph[j], A.G.pl[j]);
+            if (t < tot) iv = d2_interval(hi_i, lo_i, A.G.ph[j], A.G.pl[j]);
             const bool in = iv.x <= r2;
             unsigned bi = __ballot_sync(FULL, in);
             ns += __popc(__ballot_sync(FULL, iv.y <= r2));
@@ -313,6 +330,41 @@ __device__ unsigned long long radix_select(int nc, int need, int lane, KeyOf key
         prefix |= (unsigned long long)d << shift;
     }
     return prefix;
+}
+
+// The k-th smallest (1-based) of up to 64 keys held two per lane (v0 for
+// element lane, v1 for element 32 + lane; pad with the type's maximum) by a
+// warp bitonic sort in registers: the same value as the radix select of the
+// same keys, in far fewer instructions for the short candidate lists of a
+// kNN ball.  T is float (the distance-interval bounds) or unsigned long long
+// (the bit patterns of non-negative FP64 squared distances, ordered as the
+// doubles are).
+template <typename T>
+__device__ __forceinline__ T warp_kth64(T v0, T v1, int k, int lane) {
+    const unsigned FULL = 0xffffffffu;
+    T v[2] = {v0, v1};
+#pragma unroll
+    for (int kk = 2; kk <= 64; kk <<= 1) {
+#pragma unroll
+        for (int j = kk >> 1; j > 0; j >>= 1) {
+            if (j == 32) {   // partner in the same lane: ascending for kk = 64
+                const T lo = v[0] < v[1] ? v[0] : v[1], hi = v[0] < v[1] ? v[1] : v[0];
+                v[0] = lo;
+                v[1] = hi;
+            } else {
+#pragma unroll
+                for (int s = 0; s < 2; ++s) {
+                    const int i = 32 * s + lane;
+                    const T p = __shfl_xor_sync(FULL, v[s], j);
+                    const bool up = (i & kk) == 0, lower = (i & j) == 0;
+                    const T mn = v[s] < p ? v[s] : p, mx = v[s] < p ? p : v[s];
+                    v[s] = (lower == up) ? mn : mx;
+                }
+            }
+        }
+    }
+    const int e = k - 1;
+    return __shfl_sync(FULL, e < 32 ? v[0] : v[1], e & 31);
 }
 
 // The lane-parallel DenDVDX epilogue (smoothfcn.c:3390-3627) of up to KB
@@ -453,11 +505,20 @@ __global__ void __launch_bounds__(SW * 32, 5) k_knn_density(SphArgs A) {
             continue;
         }
         nCand += nc;
-        // bracket the k-th distance: Tlo <= fBall2 <= Thi
-        const float Tlo = __uint_as_float((unsigned)radix_select<32>(nc, k, lane,
-            [&](int e, unsigned long long &key) { key = __float_as_uint(W.lh[e].x); return true; }));
-        const float Thi = __uint_as_float((unsigned)radix_select<32>(nc, k, lane,
-            [&](int e, unsigned long long &key) { key = __float_as_uint(W.lh[e].y); return true; }));
+        // bracket the k-th distance: Tlo <= fBall2 <= Thi (a register sort
+        // for the usual short lists, a radix select for long ones)
+        float Tlo, Thi;
+        if (nc <= 64) {
+            const float2 a = lane < nc ? W.lh[lane] : make_float2(FLT_MAX, FLT_MAX);
+            const float2 b = lane + 32 < nc ? W.lh[lane + 32] : make_float2(FLT_MAX, FLT_MAX);
+            Tlo = warp_kth64<float>(a.x, b.x, k, lane);
+            Thi = warp_kth64<float>(a.y, b.y, k, lane);
+        } else {
+            Tlo = __uint_as_float((unsigned)radix_select<32>(nc, k, lane,
+                [&](int e, unsigned long long &key) { key = __float_as_uint(W.lh[e].x); return true; }));
+            Thi = __uint_as_float((unsigned)radix_select<32>(nc, k, lane,
+                [&](int e, unsigned long long &key) { key = __float_as_uint(W.lh[e].y); return true; }));
+        }
         // certainly inside (hi < Tlo), straddling (exact FP64 now), outside
         int nIn = 0;
         for (int e = lane; e < nc; e += 32) {
@@ -474,12 +535,41 @@ __global__ void __launch_bounds__(SW * 32, 5) k_knn_density(SphArgs A) {
         }
         nIn = __reduce_add_sync(FULL, (unsigned)nIn);
         __syncwarp();
-        const double fBall2 = __longlong_as_double((long long)radix_select<64>(
-            nc, k - nIn, lane, [&](int e, unsigned long long &key) {
-                if (W.idx[e] >= 0) return false;
-                key = (unsigned long long)__double_as_longlong(*reinterpret_cast<const double *>(&W.lh[e]));
-                return true;
-            }));
+        // the (k - nIn)-th exact distance among the straddling candidates:
+        // gathered into registers (at most 64) and sorted, else radix select
+        int nStr = 0;
+        for (int e = lane; e < nc; e += 32) nStr += W.idx[e] < 0;
+        nStr = __reduce_add_sync(FULL, (unsigned)nStr);
+        double fBall2;
+        if (nStr <= 64) {
+            // compacted into the neighbour buffer, free until N(i) is chosen
+            // (192 ints hold 96 keys; 8-byte aligned within the warp's area)
+            unsigned long long *sk = reinterpret_cast<unsigned long long *>(W.nbr);
+            int got = 0;
+            for (int e0 = 0; e0 < nc; e0 += 32) {
+                const int e = e0 + lane;
+                const bool str = e < nc && W.idx[e] < 0;
+                const unsigned bs = __ballot_sync(FULL, str);
+                if (str)
+                    sk[got + __popc(bs & lane_lt_s())] =
+                        (unsigned long long)__double_as_longlong(*reinterpret_cast<const double *>(&W.lh[e]));
+                got += __popc(bs);
+            }
+            __syncwarp();
+            unsigned long long s2[2];
+            s2[0] = lane < nStr ? sk[lane] : ~0ULL;
+            s2[1] = lane + 32 < nStr ? sk[lane + 32] : ~0ULL;
+            __syncwarp();
+            fBall2 = __longlong_as_double((long long)warp_kth64<unsigned long long>(s2[0], s2[1],
+                                                                                     k - nIn, lane));
+        } else {
+            fBall2 = __longlong_as_double((long long)radix_select<64>(
+                nc, k - nIn, lane, [&](int e, unsigned long long &key) {
+                    if (W.idx[e] >= 0) return false;
+                    key = (unsigned long long)__double_as_longlong(*reinterpret_cast<const double *>(&W.lh[e]));
+                    return true;
+                }));
+        }
         // N(i) in ascending particle order, so the sums below depend only on
         // the neighbour set, not on the order the ball gather found them
         int nsel = 0;

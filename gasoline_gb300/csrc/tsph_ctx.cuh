@@ -122,6 +122,7 @@ struct tsph_ctx {
     double *dRoot;               // 35 doubles: root complete moments
     double *hRoot;               // pinned host copy of the root moments
     cudaEvent_t evRoot;          // the root moments are on the host
+    cudaEvent_t evGather;        // the gather's status and coordinate scale are on the host
     double *dEwt;                // 5 doubles per k-vector
     int nEwt;
     int ewtCap;
