@@ -232,7 +232,7 @@ def run_ours(args, rank, world, local_rank):
     from gasoline_gb300 import autotune
     tuned, _ = autotune.tune_gravity(ctx, g.grav_params(periodic=True, precision=g.FP32),
                                      nbuckets=(NBUCKET,), walk_blocks=(4, 5),
-                                     task_sizes=(0, 3072), walk_groups=(0, -1))
+                                     task_sizes=(0, 3072))
     gp32 = g.grav_params(periodic=True, precision=g.FP32, nBucket=tuned["nBucket"])
     gp64 = g.grav_params(periodic=True, precision=g.FP64, nBucket=tuned["nBucket"])
 
@@ -835,7 +835,7 @@ def run_batched(args):
     best, table = autotune.tune_gravity(ctx, g.grav_params(periodic=False, precision=g.FP32))
     gp = g.grav_params(periodic=False, precision=g.FP32, nBucket=best["nBucket"])
     ctx.set_tuning(taskSize=best["taskSize"], walkBlocksPerSM=best["walkBlocksPerSM"],
-                   walkGroup=best["walkGroup"])
+                   walkGroup=best["walkGroup"], walkLists=best["walkLists"])
     gout = ctx.grav_all(gp)
     gtim = ctx.timings()
     roof = walk_roofline(ctx, gout, gtim["walk"], min(32, max(8, best["nBucket"])))

@@ -82,7 +82,8 @@ def sph_params(nSmooth=32, periodic=False, L=1.0, alpha=1.0, beta=2.0,
 class Tuning(ctypes.Structure):
     """tsph_tuning (include/tsph.h): launch-shape knobs, result-neutral."""
     _fields_ = [("taskSize", ctypes.c_int), ("walkBlocksPerSM", ctypes.c_int),
-                ("walkGroup", ctypes.c_int), ("reserved", ctypes.c_int * 5)]
+                ("walkGroup", ctypes.c_int), ("walkLists", ctypes.c_int),
+                ("reserved", ctypes.c_int * 4)]
 
 
 STORE_INT_FIELDS = ("r", "fMass", "fSoft", "v", "vPred", "u", "uPred", "a", "fPot", "dtGrav",
@@ -599,12 +600,12 @@ class Context:
         self._check(self.lib.tsph_store_put_sph(self._ctx, int(which), ctypes.c_void_p(store.ctypes.data),
                                                 ctypes.byref(layout), op))
 
-    def set_tuning(self, taskSize=0, walkBlocksPerSM=0, walkGroup=0):
-        t = Tuning(taskSize, walkBlocksPerSM, walkGroup)
+    def set_tuning(self, taskSize=0, walkBlocksPerSM=0, walkGroup=0, walkLists=0):
+        t = Tuning(taskSize, walkBlocksPerSM, walkGroup, walkLists)
         self._check(self.lib.tsph_set_tuning(self._ctx, ctypes.byref(t)))
 
     def get_tuning(self):
         t = Tuning()
         self._check(self.lib.tsph_get_tuning(self._ctx, ctypes.byref(t)))
         return {"taskSize": t.taskSize, "walkBlocksPerSM": t.walkBlocksPerSM,
-                "walkGroup": t.walkGroup}
+                "walkGroup": t.walkGroup, "walkLists": t.walkLists}

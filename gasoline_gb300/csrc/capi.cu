@@ -63,9 +63,7 @@ extern "C" int tsph_create(tsph_ctx **pctx, int device, void *stream) {
         return TSPH_ERR_NOMEM;
     }
     for (int k = 0; k < 10; ++k) cudaEventCreate(&ctx->ev[k]);
-    if (cudaMallocHost((void **)&ctx->hRoot, sizeof(double) * 64) != cudaSuccess ||
-        cudaEventCreateWithFlags(&ctx->evRoot, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&ctx->evGather, cudaEventDisableTiming) != cudaSuccess) {
+    if (cudaEventCreateWithFlags(&ctx->evGather, cudaEventDisableTiming) != cudaSuccess) {
         tsph_destroy(ctx);
         return TSPH_ERR_NOMEM;
     }
@@ -108,22 +106,20 @@ extern "C" void tsph_destroy(tsph_ctx *ctx) {
     FREE(S.nbrList); FREE(S.rcnt); FREE(S.roff); FREE(S.rcur); FREE(S.rlist); FREE(S.listFlag);
     FREE(S.ph); FREE(S.ih2); FREE(S.fn1); FREE(S.pr2f); FREE(S.pfa); FREE(S.pfb); FREE(S.pfc);
     FREE(S.need); FREE(S.list); FREE(S.list2); FREE(S.listN); FREE(S.rb2);
-    FREE(ctx->dCnt); FREE(ctx->dBucketLists); FREE(ctx->dRoot); FREE(ctx->dEwt); FREE(ctx->dStage);
+    FREE(ctx->dCnt); FREE(ctx->dBucketLists); FREE(ctx->dRoot); FREE(ctx->dEw); FREE(ctx->dStage);
     FREE(ctx->dAux); FREE(ctx->dStepStatus);
     FREE(ctx->dGroupFlag); FREE(ctx->dGroupScan); FREE(ctx->dGroupFirst); FREE(ctx->dGroupCount);
     FREE(ctx->dGroupScratch);
     FREE(ctx->dStore); FREE(ctx->dStoreOrder);
+    FREE(ctx->dWalkLists); FREE(ctx->dWalkListCount); FREE(ctx->dKeep);
     tsph_free_snapshot(ctx);
     free(ctx->hSys);
     free(ctx->hTmp);
-    free(ctx->hEw);
     if (ctx->graphExec) cudaGraphExecDestroy(ctx->graphExec);
     if (ctx->hCnt) cudaFreeHost(ctx->hCnt);
     if (ctx->B.hostCount) cudaFreeHost(ctx->B.hostCount);
     for (int k = 0; k < 10; ++k) if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
-    if (ctx->evRoot) cudaEventDestroy(ctx->evRoot);
     if (ctx->evGather) cudaEventDestroy(ctx->evGather);
-    if (ctx->hRoot) cudaFreeHost(ctx->hRoot);
     if (ctx->ownStream && ctx->stream) cudaStreamDestroy(ctx->stream);
     free(ctx);
 }
@@ -428,7 +424,6 @@ extern "C" int tsph_grav_all(tsph_ctx *ctx, const tsph_grav_params *gp, tsph_gra
     // Inside a graph capture (tsph_step) nothing here may wait for the
     // device: no status reads, no timing events, scales fixed beforehand.
     const bool cap = ctx->capturing;
-    if (cap && gp->bPeriodic) return TSPH_ERR_UNSUPPORTED;
     // a direct call re-uploads constants a captured step relies on
     if (!cap) ctx->sysVersion++;
     TSPH_CK(cudaMemsetAsync(ctx->dCnt, 0, sizeof(TsphDevCounters), ctx->stream));
@@ -502,6 +497,8 @@ extern "C" int tsph_grav_all(tsph_ctx *ctx, const tsph_grav_params *gp, tsph_gra
     cudaEventRecord(ctx->ev[4], ctx->stream);
     rc = read_status(ctx);
     if (rc) return rc;
+    ctx->lastListFallback = ctx->hCnt->nListFallback;
+    ctx->lastListBuckets = ctx->T.nLeaves;
     cudaEventElapsedTime(&ctx->timings[0], ctx->ev[0], ctx->ev[1]);
     cudaEventElapsedTime(&ctx->timings[1], ctx->ev[1], ctx->ev[2]);
     cudaEventElapsedTime(&ctx->timings[2], ctx->ev[2], ctx->ev[3]);
@@ -667,9 +664,13 @@ extern "C" int tsph_set_tuning(tsph_ctx *ctx, const tsph_tuning *t) {
     if (t->walkBlocksPerSM < 0 || t->walkBlocksPerSM > 32) return TSPH_ERR_ARG;
     if (t->walkGroup < -1 || (t->walkGroup > 0 && (t->walkGroup < 32 || t->walkGroup > 4096)))
         return TSPH_ERR_ARG;
+    if (t->walkLists < -1 || (t->walkLists > 1 && (t->walkLists < 32 || t->walkLists > 65536)))
+        return TSPH_ERR_ARG;
     ctx->taskSize = t->taskSize;
     ctx->walkBlocksPerSM = t->walkBlocksPerSM;
     ctx->walkGroup = t->walkGroup;
+    ctx->walkLists = t->walkLists;
+    ctx->walkListSlot = t->walkLists > 1 ? t->walkLists : 0;
     return TSPH_OK;
 }
 
@@ -679,5 +680,6 @@ extern "C" int tsph_get_tuning(tsph_ctx *ctx, tsph_tuning *t) {
     t->taskSize = ctx->taskSize;
     t->walkBlocksPerSM = ctx->walkBlocksPerSM;
     t->walkGroup = ctx->walkGroup;
+    t->walkLists = ctx->walkLists;
     return TSPH_OK;
 }

@@ -6,8 +6,9 @@
 // with the small-r series below r^2 < 3e-3 L^2, then a k-space sum over the
 // table built by pkdEwaldInit (ewald.c:182-248), all with the complete root
 // multipoles of pkdCalcRoot/pkdDistribRoot (pkd.c:4395-4493) evaluated by
-// MEVAL (meval.h:21-81).  The table is built on the host in FP64 from root
-// moments reduced on the device in a fixed order (deterministic).
+// MEVAL (meval.h:21-81).  The table is built on the device in FP64 from
+// root moments reduced in a fixed order (deterministic), with no host round
+// trip, so periodic evaluations can be captured in a CUDA graph.
 // erf/erfc/exp/sin/cos are CUDA's own functions.
 #include <math.h>
 #include <stdlib.h>
@@ -521,20 +522,18 @@ __global__ void __launch_bounds__(128) k_ewald(TsphDevParts P, TsphDevCounters *
 }
 
 // --------------------------------------------------------------------------
-// host: QEVAL for the k-space table (qeval.h:21-64), same arithmetic as the
-// reference's pkdEwaldInit
+// The constants on the device: QEVAL for the k-space table (qeval.h:21-64),
+// the arithmetic of the reference's pkdEwaldInit (ewald.c:182-248)
 // --------------------------------------------------------------------------
-static void qeval_h(int iOrder, const EwMom &mom, const double *gam, double dx, double dy,
-                    double dz, double *fPot) {
-    double Qmirx, Qmiry, Qmirz, Qmir, Qta = 0.0, ax = 0, ay = 0, az = 0;
+__device__ void qeval_h(int iOrder, const EwMom &mom, const double *gam, double dx, double dy,
+                        double dz, double *fPot) {
+    double Qmirx, Qmiry, Qmirz, Qmir;
     if (iOrder >= 4) {
         Qmirx = (1.0 / 6.0) * (mom.xzzz * dz * dz * dz + 3 * mom.xyzz * dy * dz * dz + 3 * mom.xyyz * dy * dy * dz + mom.xyyy * dy * dy * dy + 3 * mom.xxzz * dx * dz * dz + 6 * mom.xxyz * dx * dy * dz + 3 * mom.xxyy * dx * dy * dy + 3 * mom.xxxz * dx * dx * dz + 3 * mom.xxxy * dx * dx * dy + mom.xxxx * dx * dx * dx);
         Qmiry = (1.0 / 6.0) * (mom.yzzz * dz * dz * dz + 3 * mom.xyzz * dx * dz * dz + 3 * mom.xxyz * dx * dx * dz + mom.xxxy * dx * dx * dx + 3 * mom.yyzz * dy * dz * dz + 6 * mom.xyyz * dx * dy * dz + 3 * mom.xxyy * dx * dx * dy + 3 * mom.yyyz * dy * dy * dz + 3 * mom.xyyy * dx * dy * dy + mom.yyyy * dy * dy * dy);
         Qmirz = (1.0 / 6.0) * (mom.yyyz * dy * dy * dy + 3 * mom.xyyz * dx * dy * dy + 3 * mom.xxyz * dx * dx * dy + mom.xxxz * dx * dx * dx + 3 * mom.yyzz * dy * dy * dz + 6 * mom.xyzz * dx * dy * dz + 3 * mom.xxzz * dx * dx * dz + 3 * mom.yzzz * dy * dz * dz + 3 * mom.xzzz * dx * dz * dz + mom.zzzz * dz * dz * dz);
         Qmir = (1.0 / 4.0) * (Qmirx * dx + Qmiry * dy + Qmirz * dz);
         *fPot -= gam[4] * Qmir;
-        Qta += gam[5] * Qmir;
-        ax += gam[4] * Qmirx; ay += gam[4] * Qmiry; az += gam[4] * Qmirz;
     }
     if (iOrder >= 3) {
         Qmirx = (1.0 / 2.0) * (mom.xzz * dz * dz + 2 * mom.xyz * dy * dz + mom.xyy * dy * dy + 2 * mom.xxz * dx * dz + 2 * mom.xxy * dx * dy + mom.xxx * dx * dx);
@@ -542,8 +541,6 @@ static void qeval_h(int iOrder, const EwMom &mom, const double *gam, double dx, 
         Qmirz = (1.0 / 2.0) * (mom.yyz * dy * dy + 2 * mom.xyz * dx * dy + mom.xxz * dx * dx + 2 * mom.yzz * dy * dz + 2 * mom.xzz * dx * dz + mom.zzz * dz * dz);
         Qmir = (1.0 / 3.0) * (Qmirx * dx + Qmiry * dy + Qmirz * dz);
         *fPot -= gam[3] * Qmir;
-        Qta += gam[4] * Qmir;
-        ax += gam[3] * Qmirx; ay += gam[3] * Qmiry; az += gam[3] * Qmirz;
     }
     if (iOrder >= 2) {
         Qmirx = (1.0 / 1.0) * (mom.xz * dz + mom.xy * dy + mom.xx * dx);
@@ -551,73 +548,76 @@ static void qeval_h(int iOrder, const EwMom &mom, const double *gam, double dx, 
         Qmirz = (1.0 / 1.0) * (mom.yz * dy + mom.xz * dx + mom.zz * dz);
         Qmir = (1.0 / 2.0) * (Qmirx * dx + Qmiry * dy + Qmirz * dz);
         *fPot -= gam[2] * Qmir;
-        Qta += gam[3] * Qmir;
-        ax += gam[2] * Qmirx; ay += gam[2] * Qmiry; az += gam[2] * Qmirz;
     }
     *fPot -= gam[0] * mom.m;
-    (void)Qta; (void)ax; (void)ay; (void)az;
 }
 
-// Root moments (pkdCalcRoot) on the device right after the cell moments,
-// read back into pinned memory; evRoot marks them ready, so the host builds
-// the Ewald constants while the walk runs.
-int tsph_ewald_roots(tsph_ctx *ctx, const tsph_grav_params *gp) {
-    if (!(gp->bPeriodic && gp->bEwald) || gp->iEwOrder < 1) return TSPH_OK;
-    if (gp->iEwOrder > 4) return TSPH_ERR_ARG;
-    const int n = ctx->n;
-    if (n == 0) return TSPH_OK;
-    int nb = 256;
-    double *partial = ctx->dRoot + 64;
-    if (gp->precision == TSPH_FP32) {
-        k_root_partial<float><<<nb, RM_BS, 0, ctx->stream>>>(n, ctx->P.x, ctx->P.y, ctx->P.z,
-                                                             ctx->P.m, ctx->T.r, partial);
-        TSPH_LAUNCH_CK("k_root_partial<f32>");
-    } else {
-        k_root_partial<double><<<nb, RM_BS, 0, ctx->stream>>>(n, ctx->P.x, ctx->P.y, ctx->P.z,
-                                                              ctx->P.m, ctx->T.r, partial);
-        TSPH_LAUNCH_CK("k_root_partial<f64>");
+// parameters of one Ewald evaluation (the caller's tsph_grav_params)
+struct EwParams {
+    double L, fEwCut, fEwhCut;
+    int nReps, nEwReps, iOrder, hReps;
+};
+
+#define EWC_BS 512
+
+// The exclusive rank of this thread's `keep` among the block's threads in
+// thread order, and the block's total; every thread of the block calls it.
+__device__ __forceinline__ int block_rank(bool keep, int *shw, int *total) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned b = __ballot_sync(0xffffffffu, keep);
+    if (lane == 0) shw[w] = __popc(b);
+    __syncthreads();
+    int off = 0, tot = 0;
+    for (int k = 0; k < EWC_BS / 32; ++k) {
+        const int v = shw[k];
+        off += k < w ? v : 0;
+        tot += v;
     }
-    k_root_final<<<1, 32, 0, ctx->stream>>>(nb, partial, ctx->dRoot);
-    TSPH_LAUNCH_CK("k_root_final");
-    double *h = ctx->hRoot;   // [0, 25) octopole and hexadecapole; [32] fMass, [33, 36) r, [36, 42) Q
-    TSPH_CK(cudaMemcpyAsync(h, ctx->dRoot, sizeof(double) * 25, cudaMemcpyDeviceToHost, ctx->stream));
-    TSPH_CK(cudaMemcpyAsync(h + 32, ctx->T.fMass, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    TSPH_CK(cudaMemcpyAsync(h + 33, ctx->T.r, 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    TSPH_CK(cudaMemcpyAsync(h + 36, ctx->T.Q, 6 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    TSPH_CK(cudaEventRecord(ctx->evRoot, ctx->stream));
-    return TSPH_OK;
+    __syncthreads();
+    *total = tot;
+    return off + __popc(b & ((1u << lane) - 1u));
 }
 
-// The Ewald constants from the root moments (the host waits for evRoot
-// only) and the per-particle pass, queued behind the walk.
-int tsph_ewald(tsph_ctx *ctx, const tsph_grav_params *gp) {
-    if (!(gp->bPeriodic && gp->bEwald) || gp->iEwOrder < 1) return TSPH_OK;
-    if (gp->iEwOrder > 4) return TSPH_ERR_ARG;
-    const int n = ctx->n;
-    if (n == 0) return TSPH_OK;
-    TSPH_CK(cudaEventSynchronize(ctx->evRoot));
-    const double *h = ctx->hRoot, *node0 = ctx->hRoot + 32;
-    // the table (~32 KB) is built in a per-context host block, then copied
-    if (!ctx->hEw) {
-        ctx->hEw = malloc(sizeof(EwConst));
-        if (!ctx->hEw) return TSPH_ERR_NOMEM;
+// One block builds every Ewald constant from the root moments left by
+// k_root_final (octopole, hexadecapole), the root cell (mass, centre of
+// mass, complete quadrupole; pkdDistribRoot, pkd.c:4472-4493) and the
+// particles' largest |coordinate| (the gather's, in cnt): the MEVAL
+// coefficients, the k-space table in the reference's loop order, and the
+// real-space images.  Nothing goes through the host, so a periodic
+// evaluation can be captured in a CUDA graph.  The host has checked that
+// the table and the image list fit (tsph_ewald_roots).
+__global__ void __launch_bounds__(EWC_BS) k_ewald_const(EwParams p, const double *__restrict__ root,
+                                                        TsphDevTree T, const TsphDevCounters *cnt,
+                                                        EwConst *out) {
+    __shared__ EwMom M;
+    __shared__ int shw[EWC_BS / 32];
+    __shared__ double ext;
+    EwConst &E = *out;
+    {   // clear the block: unused table entries read as zeros
+        unsigned *w = reinterpret_cast<unsigned *>(out);
+        for (size_t i = threadIdx.x; i < sizeof(EwConst) / sizeof(unsigned); i += EWC_BS) w[i] = 0u;
     }
-    EwConst &E = *static_cast<EwConst *>(ctx->hEw);
-    memset(&E, 0, sizeof(E));
-    EwMom &M = E.mom;
-    M.xxxx = h[0]; M.xyyy = h[1]; M.xxxy = h[2]; M.yyyy = h[3]; M.xxxz = h[4]; M.yyyz = h[5];
-    M.xxyy = h[6]; M.xxyz = h[7]; M.xyyz = h[8]; M.xxzz = h[9]; M.xyzz = h[10]; M.xzzz = h[11];
-    M.yyzz = h[12]; M.yzzz = h[13]; M.zzzz = h[14];
-    M.xxx = h[15]; M.xyy = h[16]; M.xxy = h[17]; M.yyy = h[18]; M.xxz = h[19]; M.yyz = h[20];
-    M.xyz = h[21]; M.xzz = h[22]; M.yzz = h[23]; M.zzz = h[24];
-    // pkdDistribRoot (pkd.c:4472-4493): mass, COM and complete quadrupole
-    M.m = node0[0];
-    M.x = node0[1]; M.y = node0[2]; M.z = node0[3];
-    M.xx = node0[4]; M.yy = node0[5]; M.zz = node0[6];
-    M.xy = node0[7]; M.xz = node0[8]; M.yz = node0[9];
-    const double *mv = &M.m;
-    for (int k = 0; k < 35; ++k) E.momf[k] = (float)mv[k];
-    {   // FP32 MEVAL coefficients (monomials dx3 dx2dy dx2dz dxdy2 dxdydz dxdz2 dy3 dy2dz dydz2 dz3)
+    if (threadIdx.x == 0) {
+        const double *h = root;   // xxxx xyyy xxxy yyyy xxxz yyyz xxyy xxyz xyyz xxzz xyzz xzzz yyzz yzzz zzzz, xxx ... zzz
+        M.xxxx = h[0]; M.xyyy = h[1]; M.xxxy = h[2]; M.yyyy = h[3]; M.xxxz = h[4]; M.yyyz = h[5];
+        M.xxyy = h[6]; M.xxyz = h[7]; M.xyyz = h[8]; M.xxzz = h[9]; M.xyzz = h[10]; M.xzzz = h[11];
+        M.yyzz = h[12]; M.yzzz = h[13]; M.zzzz = h[14];
+        M.xxx = h[15]; M.xyy = h[16]; M.xxy = h[17]; M.yyy = h[18]; M.xxz = h[19]; M.yyz = h[20];
+        M.xyz = h[21]; M.xzz = h[22]; M.yzz = h[23]; M.zzz = h[24];
+        M.m = T.fMass[0];
+        M.x = T.r[0]; M.y = T.r[1]; M.z = T.r[2];
+        M.xx = T.Q[0]; M.yy = T.Q[1]; M.zz = T.Q[2];
+        M.xy = T.Q[3]; M.xz = T.Q[4]; M.yz = T.Q[5];
+        double e = __longlong_as_double((long long)cnt->maxAbs);
+        ext = e < 0.5 * p.L ? 0.5 * p.L : e;
+    }
+    __syncthreads();
+    const double L = p.L;
+    if (threadIdx.x == 0) {
+        E.mom = M;
+        const double *mv = &M.m;
+        for (int k = 0; k < 35; ++k) E.momf[k] = (float)mv[k];
+        // FP32 MEVAL coefficients (monomials dx3 dx2dy dx2dz dxdy2 dxdydz dxdz2 dy3 dy2dz dydz2 dz3)
         const double s6 = 1.0 / 6.0;
         const double c4[3][10] = {
             {M.xxxx, 3 * M.xxxy, 3 * M.xxxz, 3 * M.xxyy, 6 * M.xxyz, 3 * M.xxzz, M.xyyy, 3 * M.xyyz, 3 * M.xyzz, M.xzzz},
@@ -644,94 +644,162 @@ int tsph_ewald(tsph_ctx *ctx, const tsph_grav_params *gp) {
         for (int k = 0; k < 6; ++k) E.q2[k] = (float)q2[k];
         E.qtr2 = (float)(0.5 * (M.xx + M.yy + M.zz));
         E.m = (float)M.m;
+        E.L = L;
+        E.alpha = 2.0 / L;
+        E.alpha2 = E.alpha * E.alpha;
+        E.k1 = M_PI / (E.alpha2 * L * L * L);
+        E.ka = 2.0 * E.alpha / sqrt(M_PI);
+        E.fEwCut2 = p.fEwCut * p.fEwCut * L * L;
+        E.smallR2 = 3.0e-3 * L * L;
+        E.nReps = p.nReps;
+        E.nEwReps = p.nEwReps;
+        E.iOrder = p.iOrder;
+        const double hc2 = p.fEwhCut * p.fEwhCut;
+        E.hCut2 = hc2 < 1e6 ? (int)floor(hc2) : 1000000;
+        E.hMax = 0;
+        for (int h = p.hReps; h >= 1; --h)
+            if (h * h <= hc2) { E.hMax = h; break; }
     }
-    double L = gp->dPeriod;
-    E.L = L;
-    E.alpha = 2.0 / L;
-    E.alpha2 = E.alpha * E.alpha;
-    E.k1 = M_PI / (E.alpha2 * L * L * L);
-    E.ka = 2.0 * E.alpha / sqrt(M_PI);
-    E.fEwCut2 = gp->fEwCut * gp->fEwCut * L * L;
-    E.smallR2 = 3.0e-3 * L * L;
-    int nEwReps = (int)ceil(gp->fEwCut);
-    E.nReps = gp->nReps;
-    E.nEwReps = nEwReps > gp->nReps ? nEwReps : gp->nReps;
-    E.iOrder = gp->iEwOrder;
-    // k-space table, pkdEwaldInit (ewald.c:182-248)
-    int hReps = (int)ceil(gp->fEwhCut), ih = 0;
-    double k4 = M_PI * M_PI / (E.alpha * E.alpha * L * L);
-    for (int hx = -hReps; hx <= hReps; ++hx)
-        for (int hy = -hReps; hy <= hReps; ++hy)
-            for (int hz = -hReps; hz <= hReps; ++hz) {
-                int h2 = hx * hx + hy * hy + hz * hz;
-                if (h2 == 0) continue;
-                if (h2 > gp->fEwhCut * gp->fEwhCut) continue;
-                if (ih == EW_MAXH) return TSPH_ERR_UNSUPPORTED;
-                double gam[6], mfacc = 0.0, mfacs = 0.0;
-                gam[0] = exp(-k4 * h2) / (M_PI * h2 * L);
-                gam[1] = 2 * M_PI / L * gam[0];
-                gam[2] = -2 * M_PI / L * gam[1];
-                gam[3] = 2 * M_PI / L * gam[2];
-                gam[4] = -2 * M_PI / L * gam[3];
-                gam[5] = 2 * M_PI / L * gam[4];
-                gam[1] = 0.0; gam[3] = 0.0; gam[5] = 0.0;
-                qeval_h(gp->iEwOrder, M, gam, hx, hy, hz, &mfacc);
-                gam[0] = exp(-k4 * h2) / (M_PI * h2 * L);
-                gam[1] = 2 * M_PI / L * gam[0];
-                gam[2] = -2 * M_PI / L * gam[1];
-                gam[3] = 2 * M_PI / L * gam[2];
-                gam[4] = -2 * M_PI / L * gam[3];
-                gam[5] = 2 * M_PI / L * gam[4];
-                gam[0] = 0.0; gam[2] = 0.0; gam[4] = 0.0;
-                qeval_h(gp->iEwOrder, M, gam, hx, hy, hz, &mfacs);
-                E.hx[ih] = 2 * M_PI / L * hx;
-                E.hy[ih] = 2 * M_PI / L * hy;
-                E.hz[ih] = 2 * M_PI / L * hz;
-                E.hC[ih] = mfacc;
-                E.hS[ih] = mfacs;
-                ++ih;
-            }
-    E.nEwh = ih;
-    ctx->nEwt = ih;
-    const double hc2 = gp->fEwhCut * gp->fEwhCut;
-    E.hCut2 = hc2 < 1e6 ? (int)floor(hc2) : 1000000;
-    E.hMax = 0;
-    for (int h = hReps; h >= 1; --h)
-        if (h * h <= hc2) { E.hMax = h; break; }
-    for (int i = 0; i < ih; ++i) {
-        E.hxf[i] = (float)E.hx[i]; E.hyf[i] = (float)E.hy[i]; E.hzf[i] = (float)E.hz[i];
-        E.hCf[i] = (float)E.hC[i]; E.hSf[i] = (float)E.hS[i];
+    // k-space table: (hx, hy, hz) over [-hReps, hReps]^3 in the reference's
+    // loop order (hz fastest), h = 0 and |h| > fEwhCut left out
+    const double alpha = 2.0 / L;
+    const double k4 = M_PI * M_PI / (alpha * alpha * L * L);
+    const double hc2 = p.fEwhCut * p.fEwhCut;
+    const int side = 2 * p.hReps + 1, nCand = side * side * side;
+    int base = 0;
+    for (int c0 = 0; c0 < nCand; c0 += EWC_BS) {
+        const int c = c0 + threadIdx.x;
+        const int hx = c / (side * side) - p.hReps, hy = (c / side) % side - p.hReps, hz = c % side - p.hReps;
+        const int h2 = hx * hx + hy * hy + hz * hz;
+        const bool keep = c < nCand && h2 != 0 && !(h2 > hc2);
+        int tot;
+        const int ih = base + block_rank(keep, shw, &tot);
+        if (keep && ih < EW_MAXH) {
+            double gam[6], mfacc = 0.0, mfacs = 0.0;
+            gam[0] = exp(-k4 * h2) / (M_PI * h2 * L);
+            gam[1] = 2 * M_PI / L * gam[0];
+            gam[2] = -2 * M_PI / L * gam[1];
+            gam[3] = 2 * M_PI / L * gam[2];
+            gam[4] = -2 * M_PI / L * gam[3];
+            gam[5] = 2 * M_PI / L * gam[4];
+            const double g1 = gam[1], g3 = gam[3], g5 = gam[5];
+            gam[1] = 0.0; gam[3] = 0.0; gam[5] = 0.0;
+            qeval_h(p.iOrder, M, gam, hx, hy, hz, &mfacc);
+            gam[1] = g1; gam[3] = g3; gam[5] = g5;
+            gam[0] = 0.0; gam[2] = 0.0; gam[4] = 0.0;
+            qeval_h(p.iOrder, M, gam, hx, hy, hz, &mfacs);
+            E.hx[ih] = 2 * M_PI / L * hx;
+            E.hy[ih] = 2 * M_PI / L * hy;
+            E.hz[ih] = 2 * M_PI / L * hz;
+            E.hC[ih] = mfacc;
+            E.hS[ih] = mfacs;
+            E.hxf[ih] = (float)E.hx[ih];
+            E.hyf[ih] = (float)E.hy[ih];
+            E.hzf[ih] = (float)E.hz[ih];
+            E.hCf[ih] = (float)mfacc;
+            E.hSf[ih] = (float)mfacs;
+        }
+        base += tot;
     }
+    if (threadIdx.x == 0) E.nEwh = base < EW_MAXH ? base : EW_MAXH;
     // real-space images: a particle's offset from the root COM lies within
     // max|coordinate| + |COM| per axis, so an image whose nearest point of
     // that box is beyond fEwCut*L is never kept; the rest keep the
-    // reference's loop order
-    if (E.nEwReps > 3) return TSPH_ERR_UNSUPPORTED;
+    // reference's loop order, the replica "hole" first
+    const int R = p.nEwReps, s2 = 2 * R + 1, nImg = s2 * s2 * s2;
     const double com[3] = {M.x, M.y, M.z};
-    double ext;
-    memcpy(&ext, &ctx->hCnt->maxAbs, sizeof(ext));
-    if (ext < 0.5 * L) ext = 0.5 * L;
+    const double fEwCut2 = p.fEwCut * p.fEwCut * L * L;
     int ni = 0;
-    for (int pass = 0; pass < 2; ++pass) {   // hole images first
-        for (int ix = -E.nEwReps; ix <= E.nEwReps; ++ix)
-            for (int iy = -E.nEwReps; iy <= E.nEwReps; ++iy)
-                for (int iz = -E.nEwReps; iz <= E.nEwReps; ++iz) {
-                    const int id[3] = {ix, iy, iz};
-                    double d2 = 0.0;
-                    for (int k = 0; k < 3; ++k) {
-                        double s = ext + fabs(com[k]) + 1e-9 * L;
-                        double d = fabs(id[k] * L) - s;
-                        if (d > 0) d2 += d * d;
-                    }
-                    const bool hole = abs(ix) <= E.nReps && abs(iy) <= E.nReps && abs(iz) <= E.nReps;
-                    if (hole != (pass == 0)) continue;
-                    if (d2 > E.fEwCut2 * (1.0 + 1e-9) && !hole) continue;
-                    E.img[ni++] = make_char4((signed char)ix, (signed char)iy, (signed char)iz, hole ? 1 : 0);
-                }
-        if (pass == 0) E.nHole = ni;
+    for (int pass = 0; pass < 2; ++pass) {
+        for (int c0 = 0; c0 < nImg; c0 += EWC_BS) {
+            const int c = c0 + threadIdx.x;
+            const int ix = c / (s2 * s2) - R, iy = (c / s2) % s2 - R, iz = c % s2 - R;
+            const int id[3] = {ix, iy, iz};
+            double d2 = 0.0;
+            for (int k = 0; k < 3; ++k) {
+                const double s = ext + fabs(com[k]) + 1e-9 * L;
+                const double d = fabs(id[k] * L) - s;
+                if (d > 0) d2 += d * d;
+            }
+            const bool hole = abs(ix) <= p.nReps && abs(iy) <= p.nReps && abs(iz) <= p.nReps;
+            const bool keep = c < nImg && hole == (pass == 0) && (hole || !(d2 > fEwCut2 * (1.0 + 1e-9)));
+            int tot;
+            const int k = ni + block_rank(keep, shw, &tot);
+            if (keep && k < EW_MAXIMG)
+                E.img[k] = make_char4((signed char)ix, (signed char)iy, (signed char)iz, hole ? 1 : 0);
+            ni += tot;
+        }
+        if (pass == 0 && threadIdx.x == 0) E.nHole = ni;
     }
-    E.nImg = ni;
-    TSPH_CK(cudaMemcpyToSymbolAsync(cE, &E, sizeof(E), 0, cudaMemcpyHostToDevice, ctx->stream));
+    if (threadIdx.x == 0) E.nImg = ni < EW_MAXIMG ? ni : EW_MAXIMG;
+}
+
+// The k-space vectors pkdEwaldInit keeps for fEwhCut: the count depends on
+// the cut alone, so the host checks the table's capacity without the moments.
+static int ewald_table_size(double fEwhCut) {
+    const int hReps = (int)ceil(fEwhCut);
+    int ih = 0;
+    for (int hx = -hReps; hx <= hReps; ++hx)
+        for (int hy = -hReps; hy <= hReps; ++hy)
+            for (int hz = -hReps; hz <= hReps; ++hz) {
+                const int h2 = hx * hx + hy * hy + hz * hz;
+                if (h2 != 0 && !(h2 > fEwhCut * fEwhCut)) ++ih;
+            }
+    return ih;
+}
+
+// Root moments (pkdCalcRoot) and then every Ewald constant, on the device
+// right after the cell moments; the constants land in the constant bank by
+// a device-to-device copy, so no step of the evaluation waits for the host.
+int tsph_ewald_roots(tsph_ctx *ctx, const tsph_grav_params *gp) {
+    if (!(gp->bPeriodic && gp->bEwald) || gp->iEwOrder < 1) return TSPH_OK;
+    if (gp->iEwOrder > 4) return TSPH_ERR_ARG;
+    const int n = ctx->n;
+    if (n == 0) return TSPH_OK;
+    if (!(gp->fEwhCut >= 0 && gp->fEwhCut < 32) || !(gp->fEwCut >= 0)) return TSPH_ERR_ARG;
+    EwParams p;
+    p.L = gp->dPeriod;
+    p.fEwCut = gp->fEwCut;
+    p.fEwhCut = gp->fEwhCut;
+    p.nReps = gp->nReps;
+    const int nEwReps = (int)ceil(gp->fEwCut);
+    p.nEwReps = nEwReps > gp->nReps ? nEwReps : gp->nReps;
+    p.iOrder = gp->iEwOrder;
+    p.hReps = (int)ceil(gp->fEwhCut);
+    if (p.nEwReps > 3) return TSPH_ERR_UNSUPPORTED;   // the image table holds (2*3+1)^3
+    const int nh = ewald_table_size(gp->fEwhCut);
+    if (nh > EW_MAXH) return TSPH_ERR_UNSUPPORTED;
+    ctx->nEwt = nh;
+    if (!ctx->dEw) {
+        if (ctx->capturing) return TSPH_ERR_STATE;   // no allocation inside a capture
+        if (cudaMalloc(&ctx->dEw, sizeof(EwConst)) != cudaSuccess) return TSPH_ERR_NOMEM;
+    }
+    int nb = 256;
+    double *partial = ctx->dRoot + 64;
+    if (gp->precision == TSPH_FP32) {
+        k_root_partial<float><<<nb, RM_BS, 0, ctx->stream>>>(n, ctx->P.x, ctx->P.y, ctx->P.z,
+                                                             ctx->P.m, ctx->T.r, partial);
+        TSPH_LAUNCH_CK("k_root_partial<f32>");
+    } else {
+        k_root_partial<double><<<nb, RM_BS, 0, ctx->stream>>>(n, ctx->P.x, ctx->P.y, ctx->P.z,
+                                                              ctx->P.m, ctx->T.r, partial);
+        TSPH_LAUNCH_CK("k_root_partial<f64>");
+    }
+    k_root_final<<<1, 32, 0, ctx->stream>>>(nb, partial, ctx->dRoot);
+    TSPH_LAUNCH_CK("k_root_final");
+    EwConst *dE = static_cast<EwConst *>(ctx->dEw);
+    k_ewald_const<<<1, EWC_BS, 0, ctx->stream>>>(p, ctx->dRoot, ctx->T, ctx->dCnt, dE);
+    TSPH_LAUNCH_CK("k_ewald_const");
+    TSPH_CK(cudaMemcpyToSymbolAsync(cE, dE, sizeof(EwConst), 0, cudaMemcpyDeviceToDevice, ctx->stream));
+    return TSPH_OK;
+}
+
+// The per-particle pass, queued behind the walk.
+int tsph_ewald(tsph_ctx *ctx, const tsph_grav_params *gp) {
+    if (!(gp->bPeriodic && gp->bEwald) || gp->iEwOrder < 1) return TSPH_OK;
+    if (gp->iEwOrder > 4) return TSPH_ERR_ARG;
+    const int n = ctx->n;
+    if (n == 0) return TSPH_OK;
     const int BS = 128;
     if (gp->precision == TSPH_FP32) {
         k_ewald<float><<<tsph_blocks(n, BS), BS, 0, ctx->stream>>>(ctx->P, ctx->dCnt);
@@ -740,7 +808,5 @@ int tsph_ewald(tsph_ctx *ctx, const tsph_grav_params *gp) {
         k_ewald<double><<<tsph_blocks(n, BS), BS, 0, ctx->stream>>>(ctx->P, ctx->dCnt);
         TSPH_LAUNCH_CK("k_ewald<double>");
     }
-    // (a pageable-source async copy returns once the source is staged, so
-    // the host block may be reused by the next call)
     return TSPH_OK;
 }

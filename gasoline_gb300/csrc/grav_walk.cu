@@ -140,6 +140,12 @@ struct WalkArgs {
     const int *nGroups;      // device: number of groups
     int *groupScratch;       // GRP_SCRATCH ints per warp of the launch
     int groupMax;            // particles per group at most
+    // two-pass walk (listCount null: one fused pass): the list pass stores
+    // bucket b's entries at lists + b * listCap and their number in
+    // listCount[b] (-1: left to the evaluation pass, which then walks it)
+    int *lists;
+    int *listCount;
+    int listCap;
 };
 
 __device__ __forceinline__ unsigned lane_lt() {
@@ -852,6 +858,98 @@ struct WalkTally {
 // NA cells are evaluated first, as Newtonian cells, and the walk starts
 // from the group's U entries; otherwise it starts from the root in every
 // replica.  Either way the lists are the reference's.
+// A bucket's FP32 walk geometry (k_bucket_prep): centre (hi/lo), box
+// corners about the centre, box extent (negative: no active particle),
+// largest softening and active count.
+struct BucketGeom {
+    float bch[3], bcl[3], fbmn[3], fbmx[3], bext, fSoftMaxF;
+    int nAct;
+};
+
+__device__ __forceinline__ BucketGeom bucket_geom(const TsphDevTree &T, int b) {
+    BucketGeom g;
+    const float4 r0 = T.brec[4 * b], r1 = T.brec[4 * b + 1];
+    const float4 r2 = T.brec[4 * b + 2], r3 = T.brec[4 * b + 3];
+    g.bch[0] = r0.x; g.bch[1] = r0.y; g.bch[2] = r0.z; g.fSoftMaxF = r0.w;
+    g.bcl[0] = r1.x; g.bcl[1] = r1.y; g.bcl[2] = r1.z; g.bext = r1.w;
+    g.fbmn[0] = r2.x; g.fbmn[1] = r2.y; g.fbmn[2] = r2.z; g.nAct = (int)r2.w;
+    g.fbmx[0] = r3.x; g.fbmx[1] = r3.y; g.fbmx[2] = r3.z;
+    return g;
+}
+
+// One walk entry (cell, replica) against bucket b (node `node`, particles
+// [lo, lo + n)): the reference's decisions of pkdBucketWalk (walk.c:58-178)
+// -- opened (interior: ACT_OPEN, leaf: ACT_LEAF; the bucket's own leaf in
+// the home replica is left out), or accepted as a Newtonian (ACT_NEWT) or
+// softened (ACT_SOFT) cell.  The FP32 tests carry a bound on their own
+// rounding; what they cannot settle is decided in FP64 exactly as the
+// reference does (exact_decision).  Returns the child link and the leaf's
+// particle range through up / plo / cnt.
+__device__ __forceinline__ int classify_entry(const TsphDevTree &T, const TsphDevParts &P, int b, int node,
+                                              int lo, int n, const BucketGeom &G, int cell, int rep,
+                                              int &up, int &plo, int &cnt, WalkTally &K) {
+    const float u32 = 5.9604645e-08f;   // 2^-24
+    const float relF = 4.0f * u32;
+    ++K.visit;
+    const int4 lk = T.wlink[cell];
+    plo = lk.x;
+    cnt = lk.y;
+    up = lk.z;
+    const float4 ch = T.wcomh[cell], cl = T.wcoml[cell];
+    float ohx, ohy, ohz, olx, oly, olz;
+    rep_off32(rep, ohx, ohy, ohz, olx, oly, olz);
+    const float rx = ((ch.x - G.bch[0]) + ohx) + ((cl.x - G.bcl[0]) + olx);
+    const float ry = ((ch.y - G.bch[1]) + ohy) + ((cl.y - G.bcl[1]) + oly);
+    const float rz = ((ch.z - G.bch[2]) + ohz) + ((cl.z - G.bcl[2]) + olz);
+    const float dx = fmaxf(fmaxf(G.fbmn[0] - rx, rx - G.fbmx[0]), 0.0f);
+    const float dy = fmaxf(fmaxf(G.fbmn[1] - ry, ry - G.fbmx[1]), 0.0f);
+    const float dz = fmaxf(fmaxf(G.fbmn[2] - rz, rz - G.fbmx[2]), 0.0f);
+    const float D2 = dx * dx + dy * dy + dz * dz;
+    const float Sx = fmaxf(fmaxf(fabsf(rx), fabsf(ry)), fabsf(rz)) + G.bext + cW.offmax;
+    const float e = 6.0f * u32 * Sx + cW.E0;
+    const float M = 2.0f * e * (dx + dy + dz + 2.0f * e) + 3.0f * e * e + 4.0f * u32 * D2;
+    bool open;
+    if (cnt < 4) {
+        open = true;
+    } else {
+        ++K.tests;
+        const int fo = filt(D2, M, ch.w, relF);
+        if (fo == 0) {
+            ++K.exact;
+            double o[3];
+            rep_off64(rep, o);
+            open = exact_decision(T, P, b, lo, n, cell, o, true) == 1;
+        } else {
+            open = fo < 0;
+        }
+    }
+    if (open) {
+        if (up >= 0) return ACT_OPEN;
+        return (cell == node && rep == cW.selfRep) ? ACT_NONE : ACT_LEAF;
+    }
+    // softened or Newtonian (walk.c:122-127)
+    const float a32 = cl.w + G.fSoftMaxF;
+    const float t2 = a32 * a32;
+    const int fs = filt(t2, 8.0f * u32 * t2, ch.w, relF);   // t2 vs fOpen2
+    bool newt = false;
+    bool exactNeeded = (fs == 0);
+    if (!exactNeeded) {
+        if (fs < 0) newt = true;   // twoh2 < fOpen2 (certain)
+        else {
+            const int fi = filt(D2, M + 8.0f * u32 * t2, t2, relF);
+            if (fi == 0) exactNeeded = true;
+            else newt = fi > 0;
+        }
+    }
+    if (exactNeeded) {
+        ++K.exact;
+        double o[3];
+        rep_off64(rep, o);
+        newt = exact_decision(T, P, b, lo, n, cell, o, false) == 0;
+    }
+    return newt ? ACT_NEWT : ACT_SOFT;
+}
+
 template <typename Real, int NBT, bool HIGH>
 __device__ __forceinline__ void walk_bucket(const WalkArgs &W, WalkSmem<Real, NBT, HIGH> &S, int b,
                                             const int *gl, WalkTally &K, int lane) {
@@ -859,8 +957,6 @@ __device__ __forceinline__ void walk_bucket(const WalkArgs &W, WalkSmem<Real, NB
     const TsphDevParts &P = W.P;
     constexpr int CT = cell_tile<HIGH>();   // cells per tile
     const unsigned FULL = 0xffffffffu;
-    const float u32 = 5.9604645e-08f;   // 2^-24
-    const float relF = 4.0f * u32;
 
     const int node = T.leaves[b];
     const int lo = T.pLower[node];
@@ -871,17 +967,9 @@ __device__ __forceinline__ void walk_bucket(const WalkArgs &W, WalkSmem<Real, NB
         return;
     }
     // bucket geometry: FP32 records prepared once per bucket (k_bucket_prep)
-    float bch[3], bcl[3], fbmn[3], fbmx[3], bext, fSoftMaxF;
-    int nAct;
-    {
-        float4 r0 = T.brec[4 * b], r1 = T.brec[4 * b + 1];
-        float4 r2 = T.brec[4 * b + 2], r3 = T.brec[4 * b + 3];
-        bch[0] = r0.x; bch[1] = r0.y; bch[2] = r0.z; fSoftMaxF = r0.w;
-        bcl[0] = r1.x; bcl[1] = r1.y; bcl[2] = r1.z; bext = r1.w;
-        fbmn[0] = r2.x; fbmn[1] = r2.y; fbmn[2] = r2.z; nAct = (int)r2.w;
-        fbmx[0] = r3.x; fbmx[1] = r3.y; fbmx[2] = r3.z;
-    }
-    if (bext < 0.0f) {   // no active particle: not walked (pkd.c:2932)
+    const BucketGeom G = bucket_geom(T, b);
+    const int nAct = G.nAct;
+    if (G.bext < 0.0f) {   // no active particle: not walked (pkd.c:2932)
         if (lane == 0 && W.bucketLists) {
             W.bucketLists[4 * b + 0] = node;
             W.bucketLists[4 * b + 1] = W.bucketLists[4 * b + 2] = W.bucketLists[4 * b + 3] = -1;
@@ -893,9 +981,9 @@ __device__ __forceinline__ void walk_bucket(const WalkArgs &W, WalkSmem<Real, NB
         int p = lo + (lane < n ? lane : 0);
         if constexpr (sizeof(Real) == 4) {
             float4 a = P.ph[p], c = P.pl[p];
-            S.px[lane] = ((a.x - bch[0]) + (c.x - bcl[0]));
-            S.py[lane] = ((a.y - bch[1]) + (c.y - bcl[1]));
-            S.pz[lane] = ((a.z - bch[2]) + (c.z - bcl[2]));
+            S.px[lane] = ((a.x - G.bch[0]) + (c.x - G.bcl[0]));
+            S.py[lane] = ((a.y - G.bch[1]) + (c.y - G.bcl[1]));
+            S.pz[lane] = ((a.z - G.bch[2]) + (c.z - G.bcl[2]));
             S.pm[lane] = a.w;
             S.ph[lane] = c.w;
         } else {
@@ -923,7 +1011,7 @@ __device__ __forceinline__ void walk_bucket(const WalkArgs &W, WalkSmem<Real, NB
             const int c = nNA - k0 < CT ? nNA - k0 : CT;
             for (int e = lane; e < c; e += 32) S.cn[e] = gl[GRP_U + k0 + e];
             __syncwarp();
-            stage_cells<Real, NBT, HIGH>(S, S.cn, T, c, lane, false, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
+            stage_cells<Real, NBT, HIGH>(S, S.cn, T, c, lane, false, G.bch[0], G.bch[1], G.bch[2], G.bcl[0], G.bcl[1], G.bcl[2]);
             __syncwarp();
             if (i < n) eval_newt<Real, NBT, HIGH>(S, c, i, slot, W.iOrder, A);
             flush_tile(A);
@@ -943,87 +1031,54 @@ __device__ __forceinline__ void walk_bucket(const WalkArgs &W, WalkSmem<Real, NB
     bool overflow = false;
     __syncwarp();
 
-    while (sp > 0) {
-        const int take = sp < 32 ? sp : 32;
-        int ent = lane < take ? S.stack[sp - take + lane] : -1;
-        __syncwarp();
-        sp -= take;
-        int act = ACT_NONE, cell = 0, rep = 0, up = -1, cnt = 0, plo = 0;
-        if (ent >= 0) {
-            cell = ent >> 5;
-            rep = ent & 31;
-            {
-                ++K.visit;
-                int4 lk = T.wlink[cell];
-                plo = lk.x;
-                cnt = lk.y;
-                up = lk.z;
-                float4 ch = T.wcomh[cell], cl = T.wcoml[cell];
-                float ohx, ohy, ohz, olx, oly, olz;
-                rep_off32(rep, ohx, ohy, ohz, olx, oly, olz);
-                float rx = ((ch.x - bch[0]) + ohx) + ((cl.x - bcl[0]) + olx);
-                float ry = ((ch.y - bch[1]) + ohy) + ((cl.y - bcl[1]) + oly);
-                float rz = ((ch.z - bch[2]) + ohz) + ((cl.z - bcl[2]) + olz);
-                float dx = fmaxf(fmaxf(fbmn[0] - rx, rx - fbmx[0]), 0.0f);
-                float dy = fmaxf(fmaxf(fbmn[1] - ry, ry - fbmx[1]), 0.0f);
-                float dz = fmaxf(fmaxf(fbmn[2] - rz, rz - fbmx[2]), 0.0f);
-                float D2 = dx * dx + dy * dy + dz * dz;
-                float Sx = fmaxf(fmaxf(fabsf(rx), fabsf(ry)), fabsf(rz)) + bext + cW.offmax;
-                float e = 6.0f * u32 * Sx + cW.E0;
-                float M = 2.0f * e * (dx + dy + dz + 2.0f * e) + 3.0f * e * e + 4.0f * u32 * D2;
-                bool open;
-                int fo = 0;
-                if (cnt < 4) {
-                    open = true;
-                } else {
-                    ++K.tests;
-                    fo = filt(D2, M, ch.w, relF);
-                    if (fo == 0) {
-                        ++K.exact;
-                        double o[3];
-                        rep_off64(rep, o);
-                        open = exact_decision(T, P, b, lo, n, cell, o, true) == 1;
-                    } else {
-                        open = fo < 0;
-                    }
-                }
-                if (open) {
-                    if (up >= 0) act = ACT_OPEN;
-                    else if (!(cell == node && rep == cW.selfRep)) act = ACT_LEAF;
-                } else {
-                    // softened or Newtonian (walk.c:122-127)
-                    float a32 = cl.w + fSoftMaxF;
-                    float t2 = a32 * a32;
-                    int fs = filt(t2, 8.0f * u32 * t2, ch.w, relF);   // t2 vs fOpen2
-                    bool newt;
-                    bool exactNeeded = (fs == 0);
-                    if (!exactNeeded) {
-                        if (fs < 0) newt = true;   // twoh2 < fOpen2 (certain)
-                        else {
-                            int fi = filt(D2, M + 8.0f * u32 * t2, t2, relF);
-                            if (fi == 0) exactNeeded = true;
-                            else newt = fi > 0;
-                        }
-                    }
-                    if (exactNeeded) {
-                        ++K.exact;
-                        double o[3];
-                        rep_off64(rep, o);
-                        newt = exact_decision(T, P, b, lo, n, cell, o, false) == 0;
-                    }
-                    act = newt ? ACT_NEWT : ACT_SOFT;
+    // the entries come from the tree walk below, or from the list the
+    // list pass (k_walk_lists) stored for this bucket, in the same order
+    const int lcount = W.listCount ? W.listCount[b] : -1;
+    const int *lst = lcount >= 0 ? W.lists + (size_t)b * W.listCap : nullptr;
+    int lpos = 0;
+    while (lst ? lpos < lcount : sp > 0) {
+        int act = ACT_NONE, cell = 0, rep = 0, cnt = 0, plo = 0;
+        if (lst) {
+            // one round of the list pass's walk: its entries up to the zero
+            // entry that closes it (at most 32, so the zero is at most one
+            // past the window), so the tiles below fill and are evaluated
+            // exactly as in the fused walk
+            const int avail = lcount - lpos;
+            const unsigned e = lane < avail ? (unsigned)lst[lpos + lane] : 0u;
+            const unsigned mk = __ballot_sync(FULL, lane < avail && ((e >> 5) & 3u) == 0u);
+            const int m = mk ? __ffs(mk) - 1 : 32;
+            if (lane < m) {
+                cell = (int)(e >> 7);
+                rep = (int)(e & 31u);
+                act = (int)((e >> 5) & 3u) + 1;
+                if (act == ACT_LEAF) {
+                    const int2 lk = *reinterpret_cast<const int2 *>(&T.wlink[cell]);
+                    plo = lk.x;
+                    cnt = lk.y;
                 }
             }
+            lpos += m + 1;
+        } else {
+            const int take = sp < 32 ? sp : 32;
+            const int ent = lane < take ? S.stack[sp - take + lane] : -1;
+            __syncwarp();
+            sp -= take;
+            int up = -1;
+            if (ent >= 0) {
+                cell = ent >> 5;
+                rep = ent & 31;
+                act = classify_entry(T, P, b, node, lo, n, G, cell, rep, up, plo, cnt, K);
+            }
+            // children (upper first so the lower child is popped first)
+            const unsigned bo = __ballot_sync(FULL, act == ACT_OPEN);
+            if (sp + 2 * __popc(bo) > STK) { overflow = true; break; }
+            if (act == ACT_OPEN) {
+                const int pos = sp + 2 * __popc(bo & lane_lt());
+                S.stack[pos] = (up << 5) | rep;
+                S.stack[pos + 1] = ((cell + 1) << 5) | rep;
+            }
+            sp += 2 * __popc(bo);
         }
-        // children (upper first so the lower child is popped first)
-        unsigned bo = __ballot_sync(FULL, act == ACT_OPEN);
-        if (sp + 2 * __popc(bo) > STK) { overflow = true; break; }
-        if (act == ACT_OPEN) {
-            int pos = sp + 2 * __popc(bo & lane_lt());
-            S.stack[pos] = (up << 5) | rep;
-            S.stack[pos + 1] = ((cell + 1) << 5) | rep;
-        }
-        sp += 2 * __popc(bo);
         // leaf particles
         if (act == ACT_LEAF && cnt > NBT) {
             atomicOr(&W.cnt->status, 1u << TSPH_ERR_UNSUPPORTED);
@@ -1051,7 +1106,7 @@ __device__ __forceinline__ void walk_bucket(const WalkArgs &W, WalkSmem<Real, NB
         __syncwarp();
         // evaluate full tiles
         while (ppn >= PPF) {
-            stage_pp<Real, NBT, HIGH>(S, P, PPF, lane, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
+            stage_pp<Real, NBT, HIGH>(S, P, PPF, lane, G.bch[0], G.bch[1], G.bch[2], G.bcl[0], G.bcl[1], G.bcl[2]);
             __syncwarp();
             if (i < n) {
                 if (ppSelf) eval_pp<Real, NBT, HIGH, true>(S, PPF, i, slot, A);
@@ -1065,7 +1120,7 @@ __device__ __forceinline__ void walk_bucket(const WalkArgs &W, WalkSmem<Real, NB
             __syncwarp();
         }
         while (cnn >= CT) {
-            stage_cells<Real, NBT, HIGH>(S, S.cn, T, CT, lane, false, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
+            stage_cells<Real, NBT, HIGH>(S, S.cn, T, CT, lane, false, G.bch[0], G.bch[1], G.bch[2], G.bcl[0], G.bcl[1], G.bcl[2]);
             __syncwarp();
             if (i < n) eval_newt<Real, NBT, HIGH>(S, CT, i, slot, W.iOrder, A);
             flush_tile(A);
@@ -1075,7 +1130,7 @@ __device__ __forceinline__ void walk_bucket(const WalkArgs &W, WalkSmem<Real, NB
             __syncwarp();
         }
         while (csn >= CT) {
-            stage_cells<Real, NBT, HIGH>(S, S.cs, T, CT, lane, true, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
+            stage_cells<Real, NBT, HIGH>(S, S.cs, T, CT, lane, true, G.bch[0], G.bch[1], G.bch[2], G.bcl[0], G.bcl[1], G.bcl[2]);
             __syncwarp();
             if (i < n) eval_soft<Real, NBT, HIGH>(S, CT, i, slot, A);
             flush_tile(A);
@@ -1092,7 +1147,7 @@ __device__ __forceinline__ void walk_bucket(const WalkArgs &W, WalkSmem<Real, NB
     }
     // remaining partial tiles
     if (ppn > 0) {
-        stage_pp<Real, NBT, HIGH>(S, P, ppn, lane, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
+        stage_pp<Real, NBT, HIGH>(S, P, ppn, lane, G.bch[0], G.bch[1], G.bch[2], G.bcl[0], G.bcl[1], G.bcl[2]);
         __syncwarp();
         if (i < n) {
             if (ppSelf) eval_pp<Real, NBT, HIGH, true>(S, ppn, i, slot, A);
@@ -1102,14 +1157,14 @@ __device__ __forceinline__ void walk_bucket(const WalkArgs &W, WalkSmem<Real, NB
         __syncwarp();
     }
     if (cnn > 0) {
-        stage_cells<Real, NBT, HIGH>(S, S.cn, T, cnn, lane, false, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
+        stage_cells<Real, NBT, HIGH>(S, S.cn, T, cnn, lane, false, G.bch[0], G.bch[1], G.bch[2], G.bcl[0], G.bcl[1], G.bcl[2]);
         __syncwarp();
         if (i < n) eval_newt<Real, NBT, HIGH>(S, cnn, i, slot, W.iOrder, A);
         flush_tile(A);
         __syncwarp();
     }
     if (csn > 0) {
-        stage_cells<Real, NBT, HIGH>(S, S.cs, T, csn, lane, true, bch[0], bch[1], bch[2], bcl[0], bcl[1], bcl[2]);
+        stage_cells<Real, NBT, HIGH>(S, S.cs, T, csn, lane, true, G.bch[0], G.bch[1], G.bch[2], G.bcl[0], G.bcl[1], G.bcl[2]);
         __syncwarp();
         if (i < n) eval_soft<Real, NBT, HIGH>(S, csn, i, slot, A);
         flush_tile(A);
@@ -1355,6 +1410,116 @@ __global__ void __launch_bounds__(WPB * 32, sizeof(Real) == 4 ? (HIGH ? 3 : 5) :
     }
 }
 
+// The list pass of the two-pass walk.  Each warp takes buckets from a work
+// counter and walks them exactly as walk_bucket does (classify_entry, the
+// same stack discipline), but instead of evaluating it stores the bucket's
+// accepted cells and opened leaves, in walk order, as entries
+// (cell << 7) | (type << 5) | replica with type = act - 1 (leaf, Newtonian
+// cell, softened cell), each round of the walk closed by a zero entry: the
+// evaluation pass replays the rounds, so its tiles fill, and its sums run,
+// in the fused walk's order (bit-identical results).  This mirrors the reference's own split into
+// pkdBucketWalk (walk.c:58-178), which builds the lists, and
+// pkdBucketInteract (grav.c:23-249), which evaluates them.  Without the
+// evaluation's registers and tiles a warp needs a stack only, so several
+// times more warps fit on an SM and the walk's dependent L2 loads overlap.
+// A bucket whose list would not fit its slot, or whose stack overflows, is
+// marked -1 and walked again by the evaluation pass (which raises the
+// overflow).  Buckets the evaluation pass skips (no active particle, more
+// than NBT coincident particles) are not walked here.
+#define LWPB 8   // warps per block
+#define LBPS 6   // blocks per SM: 48 warps, 40 registers a thread
+template <int NBT>
+__global__ void __launch_bounds__(LWPB * 32, LBPS) k_walk_lists(WalkArgs W) {
+    __shared__ int stk[LWPB][STK];
+    const int lane = threadIdx.x & 31;
+    int *stack = stk[threadIdx.x >> 5];
+    const unsigned FULL = 0xffffffffu;
+    const TsphDevTree &T = W.T;
+    const TsphDevParts &P = W.P;
+    WalkTally K = {0u, 0u, 0u};
+    unsigned fallback = 0;
+    int *work = reinterpret_cast<int *>(&W.cnt->listWork);
+    for (;;) {
+        int b = 0;
+        if (lane == 0) b = atomicAdd(work, 1);
+        b = __shfl_sync(FULL, b, 0);
+        if (b >= *W.nBuckets) break;
+        const int node = T.leaves[b];
+        const int lo = T.pLower[node];
+        const int n = T.pUpper[node] - lo + 1;
+        const BucketGeom G = bucket_geom(T, b);
+        if (n > NBT || G.bext < 0.0f) {
+            if (lane == 0) W.listCount[b] = 0;
+            continue;
+        }
+        int *out = W.lists + (size_t)b * W.listCap;
+        const int root = T.sysRoot[P.rid[lo]];   // the bucket's own system
+        for (int r = lane; r < cW.nRep; r += 32) stack[r] = (root << 5) | r;
+        int sp = cW.nRep, nOut = 0;
+        bool spill = false;
+        WalkTally Kb = {0u, 0u, 0u};
+        __syncwarp();
+        while (sp > 0) {
+            const int take = sp < 32 ? sp : 32;
+            const int ent = lane < take ? stack[sp - take + lane] : -1;
+            __syncwarp();
+            sp -= take;
+            int act = ACT_NONE, cell = 0, rep = 0, up = -1, plo = 0, cnt = 0;
+            if (ent >= 0) {
+                cell = ent >> 5;
+                rep = ent & 31;
+                act = classify_entry(T, P, b, node, lo, n, G, cell, rep, up, plo, cnt, Kb);
+            }
+            const unsigned bo = __ballot_sync(FULL, act == ACT_OPEN);
+            if (act == ACT_LEAF && cnt > NBT) {
+                atomicOr(&W.cnt->status, 1u << TSPH_ERR_UNSUPPORTED);
+                act = ACT_NONE;
+            }
+            // the round's entries, then a zero entry closing the round
+            const unsigned bk = __ballot_sync(FULL, act >= ACT_LEAF);
+            const int add = bk ? __popc(bk) + 1 : 0;
+            if (sp + 2 * __popc(bo) > STK || nOut + add > W.listCap) {
+                spill = true;
+                break;
+            }
+            const unsigned lt = lane_lt();
+            if (act == ACT_OPEN) {
+                const int pos = sp + 2 * __popc(bo & lt);
+                stack[pos] = (up << 5) | rep;
+                stack[pos + 1] = ((cell + 1) << 5) | rep;
+            } else if (act >= ACT_LEAF) {
+                out[nOut + __popc(bk & lt)] =
+                    (int)(((unsigned)cell << 7) | (unsigned)((act - 1) << 5) | (unsigned)rep);
+            }
+            if (bk && lane == 0) out[nOut + add - 1] = 0;
+            sp += 2 * __popc(bo);
+            nOut += add;
+            __syncwarp();
+        }
+        if (!spill) {
+            K.visit += Kb.visit;
+            K.tests += Kb.tests;
+            K.exact += Kb.exact;
+        }
+        fallback += spill;
+        if (lane == 0) W.listCount[b] = spill ? -1 : nOut;
+        __syncwarp();
+    }
+    unsigned long long tests = K.tests, visit = K.visit, exact = K.exact;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        tests += __shfl_xor_sync(FULL, tests, o);
+        visit += __shfl_xor_sync(FULL, visit, o);
+        exact += __shfl_xor_sync(FULL, exact, o);
+    }
+    if (lane == 0) {
+        atomicAdd(&W.cnt->nTests, tests);
+        atomicAdd(&W.cnt->nVisits, visit);
+        atomicAdd(&W.cnt->nExactTests, exact);
+        if (fallback) atomicAdd(&W.cnt->nListFallback, fallback);
+    }
+}
+
 // FP32 geometry of every bucket: centre (hi/lo), max softening, box
 // extent, box corners relative to the centre.  The FP64 work happens here
 // once per bucket, by one thread, instead of redundantly on every lane of
@@ -1501,6 +1666,50 @@ static int prepare_groups(tsph_ctx *ctx, WalkArgs &A, int nbHost, int warps) {
     return TSPH_OK;
 }
 
+// The two-pass walk (k_walk_lists, then k_walk reading the lists), when
+// there are no walk groups and the tuning asks for it (walkLists 1, or
+// >= 32: that many entries per bucket; 0 and -1: one fused pass).  By default a bucket's slot
+// holds 1024 entries, doubled (up to 8192) when more than 1 in 256 buckets
+// of the last evaluation did not fit; a bucket that does not fit is walked
+// by the evaluation pass.
+// Outside a capture the arrays grow to the particle count (a bound on the
+// buckets of any later captured step); a capture uses what is there.
+static int prepare_lists(tsph_ctx *ctx, WalkArgs &A, int nbHost, int nbt) {
+    A.lists = nullptr;
+    A.listCount = nullptr;
+    A.listCap = 0;
+    if (ctx->walkLists <= 0 || A.groupFirst || nbHost <= 0) return TSPH_OK;
+    if (ctx->T.nNodes >= (1 << 25)) return TSPH_OK;   // entries hold the cell index in 25 bits
+    if (!ctx->capturing) {
+        if (ctx->walkListSlot == 0) ctx->walkListSlot = 1024;
+        if (ctx->walkLists <= 1 && ctx->lastListFallback * 256LL > (long long)ctx->lastListBuckets &&
+            ctx->walkListSlot < 8192)
+            ctx->walkListSlot *= 2;
+        const long long cap = nbHost > ctx->n ? nbHost : ctx->n;
+        const size_t need = (size_t)cap * ctx->walkListSlot;
+        if (ctx->walkListBuckets < cap || ctx->walkListEntries < need) {
+            int rc = tsph_grow(ctx, &ctx->dWalkLists, need);
+            if (!rc) rc = tsph_grow(ctx, &ctx->dWalkListCount, (size_t)cap);
+            if (rc) { ctx->walkListBuckets = 0; ctx->walkListEntries = 0; return rc; }
+            ctx->walkListBuckets = cap;
+            ctx->walkListEntries = need;
+        }
+    }
+    if (ctx->walkListBuckets < nbHost || !ctx->walkListSlot ||
+        ctx->walkListEntries < (size_t)nbHost * ctx->walkListSlot)
+        return TSPH_OK;
+    A.lists = ctx->dWalkLists;
+    A.listCount = ctx->dWalkListCount;
+    A.listCap = ctx->walkListSlot;
+    TSPH_CK(cudaMemsetAsync(&ctx->dCnt->listWork, 0, sizeof(unsigned int), ctx->stream));
+    const int blocks = ctx->smCount * LBPS;
+    if (nbt == 8) k_walk_lists<8><<<blocks, LWPB * 32, 0, ctx->stream>>>(A);
+    else if (nbt == 16) k_walk_lists<16><<<blocks, LWPB * 32, 0, ctx->stream>>>(A);
+    else k_walk_lists<32><<<blocks, LWPB * 32, 0, ctx->stream>>>(A);
+    TSPH_LAUNCH_CK("k_walk_lists");
+    return TSPH_OK;
+}
+
 template <typename Real, int NBT, bool HIGH>
 static int launch_walk(tsph_ctx *ctx, const WalkArgs &A, int blocks, const char *name) {
     size_t sm = sizeof(WalkSmem<Real, NBT, HIGH>) * WPB;
@@ -1580,6 +1789,8 @@ int tsph_walk_interact(tsph_ctx *ctx, const tsph_grav_params *gp) {
     rc = prepare_groups(ctx, A, nbHost, blocks * WPB);
     if (rc) return rc;
     const int nbt = gp->nBucket <= 8 ? 8 : (gp->nBucket <= 16 ? 16 : 32);
+    rc = prepare_lists(ctx, A, nbHost, nbt);
+    if (rc) return rc;
     if (gp->iOrder >= 3) {   // octopole / hexadecapole cells
         if (gp->precision == TSPH_FP32) {
             if (nbt == 8) rc = launch_walk<float, 8, true>(ctx, A, blocks, "k_walk<float,8,high>");

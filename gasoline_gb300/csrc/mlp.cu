@@ -377,6 +377,7 @@ extern "C" int tsph_hnet_mode(tsph_ctx *ctx, int collect, int predict, double ma
     ctx->hnet.collect = collect != 0;
     ctx->hnet.predict = predict != 0;
     ctx->hnet.margin = margin;
+    ctx->sysVersion++;   // a captured step graph seeds (or not) as the mode was
     return TSPH_OK;
 }
 
@@ -384,9 +385,11 @@ int tsph_hnet_features(tsph_ctx *ctx, int k) {
     TsphHnet &Hn = ctx->hnet;
     const int ng = ctx->ngas;
     if (!(Hn.collect || Hn.predict) || !Hn.havePrev || ng == 0) return TSPH_OK;
-    if (!Hn.feat || (size_t)ng > (size_t)ctx->S.cap) {
+    if (!Hn.feat || (size_t)ng > (size_t)Hn.featCap) {
+        if (ctx->capturing) return TSPH_ERR_STATE;   // no allocation inside a capture
         int rc = tsph_grow(ctx, &Hn.feat, (size_t)3 * ctx->S.cap);
-        if (rc) return rc;
+        if (rc) { Hn.featCap = 0; return rc; }
+        Hn.featCap = ctx->S.cap;
     }
     k_hnet_features<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, k, ctx->TG, ctx->G.iord,
                                                                   ctx->G.rid, ctx->C.fb2prev,

@@ -1526,7 +1526,9 @@ static int run_density(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_out
     const int ng = ctx->ngas;
     TsphSphBufs &S = ctx->S;
     const bool cap = ctx->capturing;
-    if (cap && sp->bLearnedH) return TSPH_ERR_UNSUPPORTED;
+    // a captured pass may seed from the h-network but not collect samples
+    // (their count is host state that a replay would not advance)
+    if (cap && sp->bLearnedH && ctx->hnet.collect) return TSPH_ERR_UNSUPPORTED;
     if (cap && ctx->actRung > 0) return TSPH_ERR_UNSUPPORTED;
     if (!cap) cudaEventRecord(ctx->ev[5], ctx->stream);
     k_gas_gather_pos<<<tsph_blocks(ng, 256), 256, 0, ctx->stream>>>(ng, ctx->C, ctx->G);
@@ -1546,10 +1548,8 @@ static int run_density(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_out
     TSPH_LAUNCH_CK("k_gas_split");
     if (!cap) set_sph_const(ctx, sp);
     const int kk = sp->nSmooth < ng ? sp->nSmooth : ng;
-    if (!cap) {
-        rc = tsph_hnet_features(ctx, kk);
-        if (rc) return rc;
-    }
+    rc = tsph_hnet_features(ctx, kk);
+    if (rc) return rc;
     if (sp->bLearnedH) {
         rc = tsph_hnet_seed(ctx);
         if (rc) return rc;
@@ -1677,10 +1677,10 @@ static int run_pressure(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_ou
     SphArgs AL = A;
     AL.work = S.listFlag + 2;
     if (sp->precision == TSPH_FP32) {
-        k_pressure_lists<true><<<ctx->smCount * 4, SW * 32, 0, ctx->stream>>>(AL);
+        k_pressure_lists<true><<<ctx->smCount * 8, SW * 32, 0, ctx->stream>>>(AL);
         TSPH_LAUNCH_CK("k_pressure_lists<f32>");
     } else {
-        k_pressure_lists<false><<<ctx->smCount * 4, SW * 32, 0, ctx->stream>>>(AL);
+        k_pressure_lists<false><<<ctx->smCount * 8, SW * 32, 0, ctx->stream>>>(AL);
         TSPH_LAUNCH_CK("k_pressure_lists<f64>");
     }
     k_pressure<<<ctx->smCount * 4, SW * 32, 0, ctx->stream>>>(A);

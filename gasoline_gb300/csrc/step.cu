@@ -58,9 +58,9 @@ static bool graph_matches(const tsph_ctx *ctx, double dt, const tsph_grav_params
 }
 
 // Record the step: forces are first evaluated once on the current state
-// (allocating everything, uploading constants; the same accelerations the
-// previous step left, as the evaluation is deterministic), then the step
-// is captured with the coordinate bound fixed at twice the current extent.
+// (allocating everything, uploading constants; the accelerations the
+// previous step left are kept), then the step is captured with the
+// coordinate bound fixed at twice the current extent.
 static int capture_step(tsph_ctx *ctx, double dt, const tsph_grav_params *gp,
                         const tsph_sph_params *sp) {
     drop_graph(ctx);
@@ -74,12 +74,38 @@ static int capture_step(tsph_ctx *ctx, double dt, const tsph_grav_params *gp,
     double ext;
     memcpy(&ext, &bits, sizeof(ext));
     ctx->capLimit = 2.0 * ext + 1e-300;
+    // The preparation must leave the accelerations the step's opening kick
+    // reads as they are: the gas's pressure accelerations and uDot depend on
+    // vPred and uPred, which the last closing kick moved on, so evaluating
+    // them again here would change them.  Keep them and put them back.
+    const int ng = sp ? ctx->ngas : 0;
+    const size_t nKeep = 3 * (size_t)n + 4 * (size_t)ng;
+    if (ctx->keepCap < nKeep) {
+        int rc = tsph_grow(ctx, &ctx->dKeep, nKeep);
+        if (rc) { ctx->keepCap = 0; ctx->capLimit = 0; return rc; }
+        ctx->keepCap = nKeep;
+    }
+    double *const keep[7] = {ctx->C.ax, ctx->C.ay, ctx->C.az, ctx->C.hax, ctx->C.hay, ctx->C.haz,
+                             ctx->C.udot};
+    size_t len[7], off[7];
+    size_t o = 0;
+    for (int k = 0; k < 7; ++k) {
+        len[k] = k < 3 ? (size_t)n : (size_t)ng;
+        off[k] = o;
+        o += len[k];
+    }
+    for (int k = 0; k < 7; ++k)
+        if (len[k]) TSPH_CK(cudaMemcpyAsync(ctx->dKeep + off[k], keep[k], sizeof(double) * len[k],
+                                            cudaMemcpyDeviceToDevice, ctx->stream));
     int rc = tsph_grav_all(ctx, gp, nullptr);
     if (!rc && sp && ctx->ngas > 0) {
         rc = tsph_smooth(ctx, TSPH_SMX_DENDVDX, sp, nullptr);
         if (!rc) rc = tsph_smooth(ctx, TSPH_SMX_SPHPRESSURETERMS, sp, nullptr);
     }
     if (rc) { ctx->capLimit = 0; return rc; }
+    for (int k = 0; k < 7; ++k)
+        if (len[k]) TSPH_CK(cudaMemcpyAsync(keep[k], ctx->dKeep + off[k], sizeof(double) * len[k],
+                                            cudaMemcpyDeviceToDevice, ctx->stream));
     TSPH_CK(cudaStreamSynchronize(ctx->stream));
     cudaGraph_t graph = nullptr;
     TSPH_CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
@@ -118,7 +144,8 @@ extern "C" int tsph_step(tsph_ctx *ctx, double dt, const tsph_grav_params *gp,
     if (!ctx->haveParts || !ctx->haveVel) return TSPH_ERR_STATE;
     cudaSetDevice(ctx->device);
     if (!(flags & TSPH_STEP_GRAPH)) return step_body(ctx, dt, gp, sp);
-    if (gp->bPeriodic || (sp && sp->bLearnedH)) return TSPH_ERR_UNSUPPORTED;
+    // a captured density pass can seed from the h-network, not collect for it
+    if (sp && sp->bLearnedH && ctx->hnet.collect) return TSPH_ERR_UNSUPPORTED;
     if (ctx->n == 0) return TSPH_OK;
     if (!graph_matches(ctx, dt, gp, sp)) {
         int rc = capture_step(ctx, dt, gp, sp);

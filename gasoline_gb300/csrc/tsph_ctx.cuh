@@ -88,6 +88,7 @@ struct TsphHnet {
     float *partial;      // per-warp partial gradients
     float *loss;         // per-warp partial losses
     float *feat;         // features of the current density pass (gas-tree order), 3 per particle
+    long long featCap;   // particles feat holds
     float *samples;      // training samples: 4 floats (x0,x1,x2,target) each
     long long nSamples, capSamples;
     float stats[8];      // mean/std of the three features and the target
@@ -120,12 +121,9 @@ struct tsph_ctx {
 
     // Ewald
     double *dRoot;               // 35 doubles: root complete moments
-    double *hRoot;               // pinned host copy of the root moments
-    cudaEvent_t evRoot;          // the root moments are on the host
+    void *dEw;                   // the Ewald constants, built on the device (EwConst)
     cudaEvent_t evGather;        // the gather's status and coordinate scale are on the host
-    double *dEwt;                // 5 doubles per k-vector
-    int nEwt;
-    int ewtCap;
+    int nEwt;                    // k-space vectors kept (a function of fEwhCut only)
 
     // input staging (caller order)
     double *dStage;
@@ -158,7 +156,6 @@ struct tsph_ctx {
     unsigned long long *dAux;    // device scratch: [0] gas max |coordinate| bits, [1] capture
                                  // extent, [2..] the rung statistics of the multistep driver
     double *hTmp;                // host staging of tsph_get_sph
-    void *hEw;                   // host block of the Ewald constants
     size_t hTmpN;
     double gasScale;             // last measured gas max |coordinate|
     // systems (forest): caller-order system id of every particle
@@ -172,6 +169,16 @@ struct tsph_ctx {
     bool subtreeAttr;            // its shared-memory limit raised
     int walkBlocksPerSM;         // resident walk blocks per SM (0 = default)
     int walkGroup;               // particles per walk group (0 = default, -1 = off)
+    int walkLists;               // two-pass walk (1 or a slot size: on; 0, -1: off)
+    double *dKeep;               // accelerations kept across a step capture's preparation
+    size_t keepCap;
+    int *dWalkLists;             // the list pass's entries, walkListSlot per bucket
+    int *dWalkListCount;         // entries per bucket (-1: walked by the evaluation pass)
+    long long walkListBuckets;   // buckets the arrays hold
+    size_t walkListEntries;      // entries dWalkLists holds
+    int walkListSlot;            // entries per bucket
+    long long lastListFallback;  // buckets the list pass left over in the last evaluation
+    long long lastListBuckets;   // and the buckets of that evaluation
     int *dGroupFlag, *dGroupScan;  // per bucket: starts a group, and the inclusive scan
     int *dGroupFirst;            // first bucket of every group, then the bucket count
     int *dGroupCount;            // device: number of groups

@@ -145,5 +145,7 @@ struct TsphDevCounters {
     unsigned long long nVisits;      // (cell, replica) entries the walk examined
     unsigned long long maxAbs;       // bits of max |coordinate| (non-negative double)
     unsigned int status;             // TSPH_ERR_* raised on device
-    unsigned int pad;
+    unsigned int pad;                // work counter of the walk's evaluation pass
+    unsigned int listWork;           // work counter of the walk's list pass
+    unsigned int nListFallback;      // buckets the list pass left to the evaluation pass
 };

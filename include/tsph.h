@@ -485,7 +485,15 @@ typedef struct {
                              most this many particles) share one walk for the cells that
                              every bucket of it opens or accepts, and each bucket walks
                              only the rest */
-    int reserved[5];
+    int walkLists;        /* 1: the walk in two passes -- a list pass stores every bucket's
+                             interaction list (the tree walk alone, at high occupancy), then
+                             the evaluation pass reads them; 32..65536: the same with that
+                             many list entries per bucket (default 1024, grown when buckets
+                             overflow; a bucket that overflows is walked by the evaluation
+                             pass); -1 and the default: one fused pass.  Walk groups take
+                             precedence.  Same lists, same order: results are
+                             bit-identical either way */
+    int reserved[4];
 } tsph_tuning;
 int tsph_set_tuning(tsph_ctx *ctx, const tsph_tuning *t);
 int tsph_get_tuning(tsph_ctx *ctx, tsph_tuning *t);
@@ -497,8 +505,12 @@ int tsph_get_tuning(tsph_ctx *ctx, tsph_tuning *t);
  * (gravity only).  Returns when the work is queued on the context stream.
  * With TSPH_STEP_GRAPH the step's launches are captured once into a CUDA
  * graph (recaptured when dt, the parameters or the particle set change)
- * and each call replays it with one launch; graph mode takes isolated
- * (non-periodic) systems and no learned h.  No reference counterpart for the graph: the reference
+ * and each call replays it with one launch.  Graph mode takes isolated and
+ * periodic (Ewald) systems and a density pass seeded by the h-network; it
+ * returns TSPH_ERR_UNSUPPORTED while the h-network collects samples.  The
+ * capture evaluates the forces once outside the graph and keeps the
+ * accelerations the step's opening kick reads, so graph steps equal direct
+ * ones bit for bit.  No reference counterpart for the graph: the reference
  * drives the same sequence from its host loop.
  * tsph_step_status waits for the queued steps and returns the first error
  * any of them raised (TSPH_OK if none); TSPH_ERR_BOUNDS means a particle

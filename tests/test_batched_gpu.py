@@ -210,3 +210,85 @@ def test_graph_step_with_two_task_sizes():
             c.close()
     for k in range(3):
         assert np.array_equal(states[0][k], states[1][k]), k
+
+
+def _direct_and_graph_states(setup, dt, gp, sp, nsteps=3):
+    """Run `nsteps` KDK steps on two fresh contexts prepared by setup(c):
+    directly, then as one captured graph replayed; returns both states."""
+    states = []
+    for graph in (False, True):
+        c = g.Context(0)
+        try:
+            setup(c)
+            for _ in range(nsteps):
+                c.step(dt, gp, sp, graph=graph)
+            c.step_status()
+            states.append(c.get_state())
+        finally:
+            c.close()
+    return states
+
+
+def test_graph_step_periodic_ewald_equals_direct_steps():
+    """A periodic box with Ewald (FP32 gravity, periodic FP32 SPH): the
+    Ewald constants are rebuilt on the device from each step's root
+    moments, so the step captures; replays equal direct steps bit for bit."""
+    pos, vel, m, ngas, u = g.ics.mixed_box(ng=24, seed=31, nclump=8)
+    soft = np.full(len(m), 0.2 / 24)
+    gp = g.grav_params(periodic=True, L=1.0, precision=g.FP32)
+    sp = g.sph_params(nSmooth=32, periodic=True, L=1.0, precision=g.FP32)
+
+    def setup(c):
+        c.set_particles(pos, m, soft)
+        c.set_velocities(vel, ngas, u)
+        c.grav_all(gp)
+        c.smooth(g.SMX_DENDVDX, sp)
+        c.smooth(g.SMX_SPHPRESSURETERMS, sp)
+
+    sa, sb = _direct_and_graph_states(setup, 2e-3, gp, sp)
+    for k in range(3):
+        assert np.array_equal(sa[k], sb[k]), k
+    # the particles moved and stayed in the box
+    assert not np.array_equal(sa[0], pos)
+    assert np.all(np.abs(sa[0]) <= 0.5)
+
+
+def test_graph_step_learned_h_equals_direct_steps():
+    """A gas sphere whose kNN is seeded by a trained h-network: the seeding
+    (features, prediction) is captured with the step; replays equal direct
+    steps bit for bit, and collecting samples under capture is refused."""
+    n = 20000
+    pos, vel, m, u = g.ics.gas_sphere(n, seed=43)
+    soft = np.full(n, 0.01)
+    gp = g.grav_params(periodic=False, precision=g.FP32)
+    sp = g.sph_params(nSmooth=32, precision=g.FP32)
+    sp_l = g.sph_params(nSmooth=32, precision=g.FP32, learned_h=True)
+    dt = 0.01
+
+    def setup(c):
+        c.set_particles(pos, m, soft)
+        c.set_velocities(vel, n, u)
+        c.hnet_init(seed=5)
+        c.hnet_mode(collect=True)
+        c.grav_all(gp)
+        c.smooth(g.SMX_DENDVDX, sp)
+        c.smooth(g.SMX_SPHPRESSURETERMS, sp)
+        for _ in range(3):
+            c.step(dt, gp, sp)
+        c.hnet_train(steps=200, batch=4096, lr=3e-3)
+        c.hnet_mode(collect=False, predict=True, margin=0.08)
+
+    sa, sb = _direct_and_graph_states(setup, dt, gp, sp_l)
+    for k in range(3):
+        assert np.array_equal(sa[k], sb[k]), k
+    c = g.Context(0)
+    try:
+        c.set_particles(pos, m, soft)
+        c.set_velocities(vel, n, u)
+        c.hnet_init(seed=5)
+        c.hnet_mode(collect=True)
+        with pytest.raises(g.TsphError) as e:
+            c.step(dt, gp, sp_l, graph=True)
+        assert e.value.code == 7
+    finally:
+        c.close()
