@@ -111,7 +111,8 @@ extern "C" void tsph_destroy(tsph_ctx *ctx) {
     FREE(ctx->dGroupFlag); FREE(ctx->dGroupScan); FREE(ctx->dGroupFirst); FREE(ctx->dGroupCount);
     FREE(ctx->dGroupScratch);
     FREE(ctx->dStore); FREE(ctx->dStoreOrder);
-    FREE(ctx->dWalkLists); FREE(ctx->dWalkListCount); FREE(ctx->dKeep);
+    FREE(ctx->dWalkListPP); FREE(ctx->dWalkListCell); FREE(ctx->dWalkListSoft);
+    FREE(ctx->dWalkListInfo); FREE(ctx->dWalkListFallback); FREE(ctx->dKeep);
     tsph_free_snapshot(ctx);
     free(ctx->hSys);
     free(ctx->hTmp);
@@ -497,8 +498,7 @@ extern "C" int tsph_grav_all(tsph_ctx *ctx, const tsph_grav_params *gp, tsph_gra
     cudaEventRecord(ctx->ev[4], ctx->stream);
     rc = read_status(ctx);
     if (rc) return rc;
-    ctx->lastListFallback = ctx->hCnt->nListFallback;
-    ctx->lastListBuckets = ctx->T.nLeaves;
+    ctx->lastListNeed = ctx->hCnt->listNeed;
     cudaEventElapsedTime(&ctx->timings[0], ctx->ev[0], ctx->ev[1]);
     cudaEventElapsedTime(&ctx->timings[1], ctx->ev[1], ctx->ev[2]);
     cudaEventElapsedTime(&ctx->timings[2], ctx->ev[2], ctx->ev[3]);
@@ -669,8 +669,10 @@ extern "C" int tsph_set_tuning(tsph_ctx *ctx, const tsph_tuning *t) {
     ctx->taskSize = t->taskSize;
     ctx->walkBlocksPerSM = t->walkBlocksPerSM;
     ctx->walkGroup = t->walkGroup;
+    // a new list mode starts its slots afresh; the same mode keeps the
+    // slots it has grown to
+    if (t->walkLists != ctx->walkLists) ctx->walkListSlot = t->walkLists > 1 ? t->walkLists : 0;
     ctx->walkLists = t->walkLists;
-    ctx->walkListSlot = t->walkLists > 1 ? t->walkLists : 0;
     return TSPH_OK;
 }
 

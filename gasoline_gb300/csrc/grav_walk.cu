@@ -127,6 +127,15 @@ struct WalkSmem {
     int gU, gNA;   // sizes of the lists the last group walk left
 };
 
+// The evaluation pass's per-warp shared memory: tiles and the bucket's
+// particles only (no walk stack or list buffers).
+template <typename Real, int NBT, bool HIGH>
+struct EvalSmem {
+    TileData<Real, HIGH> D;
+    Real px[NBT], py[NBT], pz[NBT], pm[NBT], ph[NBT];
+    unsigned long long tAct, tPP, tNewt, tSoft, tBsq, tIntra;
+};
+
 struct WalkArgs {
     TsphDevTree T;
     TsphDevParts P;
@@ -140,12 +149,17 @@ struct WalkArgs {
     const int *nGroups;      // device: number of groups
     int *groupScratch;       // GRP_SCRATCH ints per warp of the launch
     int groupMax;            // particles per group at most
-    // two-pass walk (listCount null: one fused pass): the list pass stores
-    // bucket b's entries at lists + b * listCap and their number in
-    // listCount[b] (-1: left to the evaluation pass, which then walks it)
-    int *lists;
-    int *listCount;
+    // two-pass walk (listInfo null: one fused pass): the list pass stores
+    // bucket b's P-P particles at listPP + b * listCap (its own first),
+    // Newtonian cells at listCell + b * listCap and softened cells at
+    // listSoft + b * (listCap / 4), their numbers in listInfo[b] (w = -1: a
+    // list did not fit; the evaluation pass walks the bucket itself)
+    int *listPP, *listCell, *listSoft;
+    int4 *listInfo;
     int listCap;
+    // the buckets marked w = -1, walked by a fused launch after the
+    // evaluation pass (their number in cnt->nListFallback); null otherwise
+    int *fallback;
 };
 
 __device__ __forceinline__ unsigned lane_lt() {
@@ -334,10 +348,11 @@ __device__ __forceinline__ void rel_pos(float4 h, float4 l, int r, float bchx, f
     z = ((h.z - bchz) + ohz) + ((l.z - bclz) + olz);
 }
 
-// Stage P-P entries [0, cnt) of the warp's buffer into shared memory.
-template <typename Real, int NBT, bool HIGH>
-__device__ __forceinline__ void stage_pp(WalkSmem<Real, NBT, HIGH> &S, const TsphDevParts &P, int cnt,
-                                         int lane, float bchx, float bchy, float bchz,
+// Stage P-P entries [0, cnt) of buf (the warp's buffer in shared memory, or
+// a stored list) into shared memory.
+template <typename Real, int NBT, bool HIGH, class Smem>
+__device__ __forceinline__ void stage_pp(Smem &S, const TsphDevParts &P, const int *buf,
+                                         int cnt, int lane, float bchx, float bchy, float bchz,
                                          float bclx, float bcly, float bclz) {
     if constexpr (sizeof(Real) == 4) {
         const int np = (cnt + 1) >> 1;
@@ -347,7 +362,7 @@ __device__ __forceinline__ void stage_pp(WalkSmem<Real, NBT, HIGH> &S, const Tsp
             for (int k = 0; k < 2; ++k) {
                 const int e = 2 * p + k;
                 if (e < cnt) {
-                    const int ent = S.pp[e];
+                    const int ent = buf[e];
                     const int idx = ent >> 5, rep = ent & 31;
                     const float4 a = P.ph[idx], b = P.pl[idx];
                     rel_pos(a, b, rep == 31 ? cW.selfRep : rep, bchx, bchy, bchz, bclx, bcly, bclz,
@@ -365,7 +380,7 @@ __device__ __forceinline__ void stage_pp(WalkSmem<Real, NBT, HIGH> &S, const Tsp
         }
     } else {
         for (int e = lane; e < cnt; e += 32) {
-            const int ent = S.pp[e];
+            const int ent = buf[e];
             const int idx = ent >> 5, rep = ent & 31;
             const int r = rep == 31 ? cW.selfRep : rep;
             double o[3];
@@ -383,14 +398,15 @@ __device__ __forceinline__ void stage_pp(WalkSmem<Real, NBT, HIGH> &S, const Tsp
 // holds the bucket's own particles (the first tile of every bucket, where
 // the own particles are entries 0..n-1), so the particle's pair with itself
 // is left out.
-template <typename Real, int NBT, bool HIGH, bool SELF>
-__device__ __forceinline__ void eval_pp(WalkSmem<Real, NBT, HIGH> &S, int cnt, int i, int slot, Acc<Real> &A) {
+template <typename Real, int NBT, bool HIGH, bool SELF, class Smem>
+__device__ __forceinline__ void eval_pp(Smem &S, int cnt, int i, int slot, Acc<Real> &A) {
     if constexpr (sizeof(Real) == 4) {
         const float2 X = p_splat(S.px[i]), Y = p_splat(S.py[i]), Z = p_splat(S.pz[i]);
         const float2 H = p_splat(S.ph[i]), M = p_splat(S.pm[i]);
         float2 tx = p_splat(0.0f), ty = tx, tz = tx, tp = tx;   // tp: minus the potential
         float dt = A.dt;
         const int np = (cnt + 1) >> 1;
+#pragma unroll 1
         for (int p = slot; p < np; p += 32 / NBT) {
             const float4 a = S.D.pp.xy[p], b = S.D.pp.zm[p];
             const float2 he = S.D.pp.h[p];
@@ -477,8 +493,8 @@ __device__ __forceinline__ void cell_record(const TsphDevTree &T, int ent, bool 
 }
 
 // Stage cell entries (Newtonian when soft == 0, else softened).
-template <typename Real, int NBT, bool HIGH>
-__device__ __forceinline__ void stage_cells(WalkSmem<Real, NBT, HIGH> &S, const int *buf, const TsphDevTree &T,
+template <typename Real, int NBT, bool HIGH, class Smem>
+__device__ __forceinline__ void stage_cells(Smem &S, const int *buf, const TsphDevTree &T,
                                             int cnt, int lane, bool soft, float bchx, float bchy,
                                             float bchz, float bclx, float bcly, float bclz) {
     if constexpr (sizeof(Real) == 4) {
@@ -606,8 +622,8 @@ __device__ __forceinline__ void qeval_cell(int iOrder, Real m, const Real *q, co
 
 // Newtonian cells of a HIGH tile (iOrder >= 3), one cell per lane step, in
 // the precision of the walk; terms folded into the compensated sums.
-template <typename Real, int NBT, bool HIGH>
-__device__ __forceinline__ void eval_newt_high(WalkSmem<Real, NBT, HIGH> &S, int cnt, int i, int slot,
+template <typename Real, int NBT, bool HIGH, class Smem>
+__device__ __forceinline__ void eval_newt_high(Smem &S, int cnt, int i, int slot,
                                                int iOrder, Acc<Real> &A) {
     const Real xi = S.px[i], yi = S.py[i], zi = S.pz[i], mi = S.pm[i];
     for (int e = slot; e < cnt; e += 32 / NBT) {
@@ -657,67 +673,77 @@ __device__ __forceinline__ void eval_newt_high(WalkSmem<Real, NBT, HIGH> &S, int
     }
 }
 
+// FP32 Newtonian cell tile for particle i, two cells per packed
+// instruction: monopole, and with QUAD the trace-free quadrupole.  With
+// s = 1/r^5 and u = d.Q.d (d = cell - particle), QEVAL's quadrupole terms
+// (qeval.h:53-64) are pot -= 1.5 s u, a += 3 s Q.d - 7.5 s u d / r^2 (the
+// reference's g2 = 3 s, g3 = 15 s / r^2 and Qmir = u / 2 folded together).
+template <int NBT, bool QUAD, class Smem>
+__device__ __forceinline__ void newt_tile_f32(Smem &S, int cnt, int i, int slot, Acc<float> &A) {
+    const float2 X = p_splat(S.px[i]), Y = p_splat(S.py[i]), Z = p_splat(S.pz[i]);
+    const float2 M = p_splat(S.pm[i]);
+    const float2 c15 = p_splat(1.5f), c75 = p_splat(7.5f), cm3 = p_splat(-3.0f);
+    float2 tx = p_splat(0.0f), ty = tx, tz = tx, tp = tx;   // tp: minus the potential
+    float dt = A.dt;
+    const int np = (cnt + 1) >> 1;
+#pragma unroll 1
+    for (int p = slot; p < np; p += 32 / NBT) {
+        const float4 a = S.D.cn.xy[p], b = S.D.cn.zm[p];
+        // entry minus particle: the reference's dx with the sign flipped
+        const float2 dx = p_sub(make_float2(a.x, a.y), X);
+        const float2 dy = p_sub(make_float2(a.z, a.w), Y);
+        const float2 dz = p_sub(make_float2(b.x, b.y), Z);
+        const float2 m = make_float2(b.z, b.w);
+        const float2 d2 = p_fma(dz, dz, p_fma(dy, dy, p_mul(dx, dx)));
+        const float2 g0 = p_rsqrt(d2);
+        const float2 dir2 = p_mul(g0, g0);
+        const float2 g1 = p_mul(g0, dir2);
+        float2 Qta = p_mul(g1, m);
+        tp = p_fma(g0, m, tp);
+        if constexpr (QUAD) {
+            const float4 q01 = S.D.cn.q01[p], q23 = S.D.cn.q23[p], q45 = S.D.cn.q45[p];
+            const float2 xx = make_float2(q01.x, q01.y), yy = make_float2(q01.z, q01.w);
+            const float2 zz = make_float2(q23.x, q23.y), xy = make_float2(q23.z, q23.w);
+            const float2 xz = make_float2(q45.x, q45.y), yz = make_float2(q45.z, q45.w);
+            // Q.d with the flipped dx: minus the reference's Qmir vector
+            const float2 qx = p_fma(xx, dx, p_fma(xy, dy, p_mul(xz, dz)));
+            const float2 qy = p_fma(yy, dy, p_fma(xy, dx, p_mul(yz, dz)));
+            const float2 qz = p_fma(zz, dz, p_fma(xz, dx, p_mul(yz, dy)));
+            const float2 u = p_fma(qz, dz, p_fma(qy, dy, p_mul(qx, dx)));
+            const float2 s5 = p_mul(g1, dir2);
+            const float2 w = p_mul(s5, u);
+            tp = p_fma(c15, w, tp);
+            Qta = p_fma(c75, p_mul(w, dir2), Qta);
+            const float2 ns3 = p_mul(cm3, s5);
+            tx = p_fma(ns3, qx, tx);
+            ty = p_fma(ns3, qy, ty);
+            tz = p_fma(ns3, qz, tz);
+        }
+        tx = p_fma(dx, Qta, tx);
+        ty = p_fma(dy, Qta, ty);
+        tz = p_fma(dz, Qta, tz);
+        const float2 idt2 = p_mul(p_add(M, m), g1);
+        dt = fmaxf(dt, fmaxf(idt2.x, idt2.y));
+    }
+    A.dt = dt;
+    kahan_add2(A.s[0], A.c[0], tx);
+    kahan_add2(A.s[1], A.c[1], ty);
+    kahan_add2(A.s[2], A.c[2], tz);
+    kahan_add2(A.s[3], A.c[3], make_float2(-tp.x, -tp.y));
+}
+
 // Newtonian cells, QEVAL at order <= 2 (qeval.h:53-64), for the particle
 // i: acceleration, potential, and (m_i + m) / r^3 for the timestep.  FP32
 // evaluates two cells per packed instruction into tile partials that are
 // folded into the compensated sums once per tile.
-template <typename Real, int NBT, bool HIGH>
-__device__ __forceinline__ void eval_newt(WalkSmem<Real, NBT, HIGH> &S, int cnt, int i, int slot, int iOrder,
+template <typename Real, int NBT, bool HIGH, class Smem>
+__device__ __forceinline__ void eval_newt(Smem &S, int cnt, int i, int slot, int iOrder,
                                           Acc<Real> &A) {
     if constexpr (HIGH) {
         eval_newt_high<Real, NBT, HIGH>(S, cnt, i, slot, iOrder, A);
     } else if constexpr (sizeof(Real) == 4) {
-        const float2 X = p_splat(S.px[i]), Y = p_splat(S.py[i]), Z = p_splat(S.pz[i]);
-        const float2 M = p_splat(S.pm[i]);
-        const float2 three = p_splat(3.0f), five = p_splat(5.0f), half = p_splat(0.5f);
-        const float2 mone = p_splat(-1.0f);
-        float2 tx = p_splat(0.0f), ty = tx, tz = tx, tp = tx;   // tp: minus the potential
-        float dt = A.dt;
-        const bool quad = iOrder >= 2;
-        const int np = (cnt + 1) >> 1;
-        for (int p = slot; p < np; p += 32 / NBT) {
-            const float4 a = S.D.cn.xy[p], b = S.D.cn.zm[p];
-            // entry minus particle: the reference's dx with the sign flipped
-            const float2 dx = p_sub(make_float2(a.x, a.y), X);
-            const float2 dy = p_sub(make_float2(a.z, a.w), Y);
-            const float2 dz = p_sub(make_float2(b.x, b.y), Z);
-            const float2 m = make_float2(b.z, b.w);
-            const float2 d2 = p_fma(dz, dz, p_fma(dy, dy, p_mul(dx, dx)));
-            const float2 g0 = p_rsqrt(d2);
-            const float2 dir2 = p_mul(g0, g0);
-            const float2 g1 = p_mul(g0, dir2);
-            float2 Qta = p_mul(g1, m);
-            tp = p_fma(g0, m, tp);
-            if (quad) {
-                const float4 q01 = S.D.cn.q01[p], q23 = S.D.cn.q23[p], q45 = S.D.cn.q45[p];
-                const float2 xx = make_float2(q01.x, q01.y), yy = make_float2(q01.z, q01.w);
-                const float2 zz = make_float2(q23.x, q23.y), xy = make_float2(q23.z, q23.w);
-                const float2 xz = make_float2(q45.x, q45.y), yz = make_float2(q45.z, q45.w);
-                const float2 g2 = p_mul(p_mul(three, g1), dir2);
-                const float2 g3 = p_mul(p_mul(five, g2), dir2);
-                // Q.r with the flipped dx: minus the reference's Qmir vector
-                const float2 qx = p_fma(xx, dx, p_fma(xy, dy, p_mul(xz, dz)));
-                const float2 qy = p_fma(yy, dy, p_fma(xy, dx, p_mul(yz, dz)));
-                const float2 qz = p_fma(zz, dz, p_fma(xz, dx, p_mul(yz, dy)));
-                const float2 qir = p_mul(half, p_fma(qz, dz, p_fma(qy, dy, p_mul(qx, dx))));
-                tp = p_fma(g2, qir, tp);
-                Qta = p_fma(g3, qir, Qta);
-                const float2 ng2 = p_mul(mone, g2);
-                tx = p_fma(ng2, qx, tx);
-                ty = p_fma(ng2, qy, ty);
-                tz = p_fma(ng2, qz, tz);
-            }
-            tx = p_fma(dx, Qta, tx);
-            ty = p_fma(dy, Qta, ty);
-            tz = p_fma(dz, Qta, tz);
-            const float2 idt2 = p_mul(p_add(M, m), g1);
-            dt = fmaxf(dt, fmaxf(idt2.x, idt2.y));
-        }
-        A.dt = dt;
-        kahan_add2(A.s[0], A.c[0], tx);
-        kahan_add2(A.s[1], A.c[1], ty);
-        kahan_add2(A.s[2], A.c[2], tz);
-        kahan_add2(A.s[3], A.c[3], make_float2(-tp.x, -tp.y));
+        if (iOrder >= 2) newt_tile_f32<NBT, true>(S, cnt, i, slot, A);
+        else newt_tile_f32<NBT, false>(S, cnt, i, slot, A);
     } else {
         const Real xi = S.px[i], yi = S.py[i], zi = S.pz[i], mi = S.pm[i];
         for (int e = slot; e < cnt; e += 32 / NBT) {
@@ -784,8 +810,8 @@ __device__ __forceinline__ void soft_term(Real xi, Real yi, Real zi, Real hi, Re
     idt2 = (mi + m) * b;
 }
 
-template <typename Real, int NBT, bool HIGH>
-__device__ __forceinline__ void eval_soft(WalkSmem<Real, NBT, HIGH> &S, int cnt, int i, int slot, Acc<Real> &A) {
+template <typename Real, int NBT, bool HIGH, class Smem>
+__device__ __forceinline__ void eval_soft(Smem &S, int cnt, int i, int slot, Acc<Real> &A) {
     const Real xi = S.px[i], yi = S.py[i], zi = S.pz[i], hi = S.ph[i], mi = S.pm[i];
     if constexpr (sizeof(Real) == 4) {
         const int np = (cnt + 1) >> 1;
@@ -883,19 +909,15 @@ __device__ __forceinline__ BucketGeom bucket_geom(const TsphDevTree &T, int b) {
 // the home replica is left out), or accepted as a Newtonian (ACT_NEWT) or
 // softened (ACT_SOFT) cell.  The FP32 tests carry a bound on their own
 // rounding; what they cannot settle is decided in FP64 exactly as the
-// reference does (exact_decision).  Returns the child link and the leaf's
-// particle range through up / plo / cnt.
-__device__ __forceinline__ int classify_entry(const TsphDevTree &T, const TsphDevParts &P, int b, int node,
-                                              int lo, int n, const BucketGeom &G, int cell, int rep,
-                                              int &up, int &plo, int &cnt, WalkTally &K) {
+// reference does (exact_decision).  classify_loaded takes the cell's walk
+// records (particle count cnt, child link up, COM hi/lo with fOpen2 and
+// softening in .w) already loaded; classify_entry loads them and returns
+// the child link and the leaf's particle range through up / plo / cnt.
+__device__ __forceinline__ int classify_loaded(const TsphDevTree &T, const TsphDevParts &P, int b, int node,
+                                               int lo, int n, const BucketGeom &G, int cell, int rep,
+                                               int up, int cnt, float4 ch, float4 cl, WalkTally &K) {
     const float u32 = 5.9604645e-08f;   // 2^-24
     const float relF = 4.0f * u32;
-    ++K.visit;
-    const int4 lk = T.wlink[cell];
-    plo = lk.x;
-    cnt = lk.y;
-    up = lk.z;
-    const float4 ch = T.wcomh[cell], cl = T.wcoml[cell];
     float ohx, ohy, ohz, olx, oly, olz;
     rep_off32(rep, ohx, ohy, ohz, olx, oly, olz);
     const float rx = ((ch.x - G.bch[0]) + ohx) + ((cl.x - G.bcl[0]) + olx);
@@ -950,31 +972,43 @@ __device__ __forceinline__ int classify_entry(const TsphDevTree &T, const TsphDe
     return newt ? ACT_NEWT : ACT_SOFT;
 }
 
-template <typename Real, int NBT, bool HIGH>
-__device__ __forceinline__ void walk_bucket(const WalkArgs &W, WalkSmem<Real, NBT, HIGH> &S, int b,
-                                            const int *gl, WalkTally &K, int lane) {
+__device__ __forceinline__ int classify_entry(const TsphDevTree &T, const TsphDevParts &P, int b, int node,
+                                              int lo, int n, const BucketGeom &G, int cell, int rep,
+                                              int &up, int &plo, int &cnt, WalkTally &K) {
+    ++K.visit;
+    const int4 lk = T.wlink[cell];
+    plo = lk.x;
+    cnt = lk.y;
+    up = lk.z;
+    return classify_loaded(T, P, b, node, lo, n, G, cell, rep, up, cnt, T.wcomh[cell], T.wcoml[cell], K);
+}
+
+// A bucket's start, shared by the fused walk and the list evaluation: its
+// node and particles; a bucket holding more than NBT coincident particles
+// raises TSPH_ERR_UNSUPPORTED and one with no active particle is not
+// walked (pkd.c:2932) -- both return false.  Otherwise the bucket's
+// particles are in S.px.. (FP32: relative to the bucket centre).
+template <typename Real, int NBT, bool HIGH, class Smem>
+__device__ __forceinline__ bool bucket_begin(const WalkArgs &W, Smem &S, int b, int lane,
+                                             int &node, int &lo, int &n, BucketGeom &G) {
     const TsphDevTree &T = W.T;
     const TsphDevParts &P = W.P;
-    constexpr int CT = cell_tile<HIGH>();   // cells per tile
-    const unsigned FULL = 0xffffffffu;
-
-    const int node = T.leaves[b];
-    const int lo = T.pLower[node];
-    const int n = T.pUpper[node] - lo + 1;
+    node = T.leaves[b];
+    lo = T.pLower[node];
+    n = T.pUpper[node] - lo + 1;
     if (n > NBT) {
         // a zero-extent leaf holding more than NBT coincident particles
         if (lane == 0) atomicOr(&W.cnt->status, 1u << TSPH_ERR_UNSUPPORTED);
-        return;
+        return false;
     }
     // bucket geometry: FP32 records prepared once per bucket (k_bucket_prep)
-    const BucketGeom G = bucket_geom(T, b);
-    const int nAct = G.nAct;
+    G = bucket_geom(T, b);
     if (G.bext < 0.0f) {   // no active particle: not walked (pkd.c:2932)
         if (lane == 0 && W.bucketLists) {
             W.bucketLists[4 * b + 0] = node;
             W.bucketLists[4 * b + 1] = W.bucketLists[4 * b + 2] = W.bucketLists[4 * b + 3] = -1;
         }
-        return;
+        return false;
     }
     // bucket particles
     if (lane < NBT) {
@@ -994,6 +1028,71 @@ __device__ __forceinline__ void walk_bucket(const WalkArgs &W, WalkSmem<Real, NB
             S.ph[lane] = (Real)P.h[p];
         }
     }
+    return true;
+}
+
+// A bucket's end: the 32 / NBT partial accumulators of each particle
+// reduced, the results written, and pkdGravAll's sums tallied.
+template <typename Real, int NBT, bool HIGH, class Smem>
+__device__ __forceinline__ void bucket_end(const WalkArgs &W, Smem &S, int b, int node,
+                                           int lo, int n, int nAct, Acc<Real> &A, int nPart, int nNewt,
+                                           int nSoft, int lane) {
+    const TsphDevParts &P = W.P;
+    const unsigned FULL = 0xffffffffu;
+#pragma unroll
+    for (int o = NBT; o < 32; o <<= 1) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            Real s2 = __shfl_xor_sync(FULL, A.s[k], o);
+            Real c2 = __shfl_xor_sync(FULL, A.c[k], o);
+            two_sum_merge(A.s[k], A.c[k], s2, c2);
+        }
+        Real d2 = __shfl_xor_sync(FULL, A.dt, o);
+        A.dt = d2 > A.dt ? d2 : A.dt;
+    }
+    if (lane < n) {
+        int p = lo + lane;
+        if constexpr (sizeof(Real) == 4) {
+            P.wsum[p] = make_float4(A.s[0], A.s[1], A.s[2], A.s[3]);
+            P.wcmp[p] = make_float4(A.c[0], A.c[1], A.c[2], A.c[3]);
+            P.wdt[p] = A.dt;
+        } else {
+            P.ax[p] = (double)A.s[0];
+            P.ay[p] = (double)A.s[1];
+            P.az[p] = (double)A.s[2];
+            P.pot[p] = (double)A.s[3];
+            P.dtGrav[p] = (double)A.dt;
+        }
+    }
+    if (lane == 0) {
+        // pkdGravAll's sums over the active particles (pkd.c:2945-2950)
+        S.tAct += nAct;
+        S.tPP += (unsigned long long)nAct * nPart;
+        S.tNewt += (unsigned long long)nAct * nNewt;
+        S.tSoft += (unsigned long long)nAct * nSoft;
+        S.tBsq += (unsigned long long)nAct * n;
+        S.tIntra += (unsigned long long)nAct * (2 * (n - 1) - nAct + 1) / 2;
+        if (W.bucketLists) {
+            W.bucketLists[4 * b + 0] = node;
+            W.bucketLists[4 * b + 1] = nPart;
+            W.bucketLists[4 * b + 2] = nSoft;
+            W.bucketLists[4 * b + 3] = nNewt;
+        }
+    }
+    __syncwarp();
+}
+
+template <typename Real, int NBT, bool HIGH>
+__device__ __forceinline__ void walk_bucket(const WalkArgs &W, WalkSmem<Real, NBT, HIGH> &S, int b,
+                                            const int *gl, WalkTally &K, int lane) {
+    const TsphDevTree &T = W.T;
+    const TsphDevParts &P = W.P;
+    constexpr int CT = cell_tile<HIGH>();   // cells per tile
+    const unsigned FULL = 0xffffffffu;
+    int node, lo, n;
+    BucketGeom G;
+    if (!bucket_begin<Real, NBT, HIGH>(W, S, b, lane, node, lo, n, G)) return;
+    const int nAct = G.nAct;
     // accumulators: lane = (particle i, slot)
     const int i = lane % NBT, slot = lane / NBT;
     Acc<Real> A;
@@ -1031,34 +1130,9 @@ __device__ __forceinline__ void walk_bucket(const WalkArgs &W, WalkSmem<Real, NB
     bool overflow = false;
     __syncwarp();
 
-    // the entries come from the tree walk below, or from the list the
-    // list pass (k_walk_lists) stored for this bucket, in the same order
-    const int lcount = W.listCount ? W.listCount[b] : -1;
-    const int *lst = lcount >= 0 ? W.lists + (size_t)b * W.listCap : nullptr;
-    int lpos = 0;
-    while (lst ? lpos < lcount : sp > 0) {
+    while (sp > 0) {
         int act = ACT_NONE, cell = 0, rep = 0, cnt = 0, plo = 0;
-        if (lst) {
-            // one round of the list pass's walk: its entries up to the zero
-            // entry that closes it (at most 32, so the zero is at most one
-            // past the window), so the tiles below fill and are evaluated
-            // exactly as in the fused walk
-            const int avail = lcount - lpos;
-            const unsigned e = lane < avail ? (unsigned)lst[lpos + lane] : 0u;
-            const unsigned mk = __ballot_sync(FULL, lane < avail && ((e >> 5) & 3u) == 0u);
-            const int m = mk ? __ffs(mk) - 1 : 32;
-            if (lane < m) {
-                cell = (int)(e >> 7);
-                rep = (int)(e & 31u);
-                act = (int)((e >> 5) & 3u) + 1;
-                if (act == ACT_LEAF) {
-                    const int2 lk = *reinterpret_cast<const int2 *>(&T.wlink[cell]);
-                    plo = lk.x;
-                    cnt = lk.y;
-                }
-            }
-            lpos += m + 1;
-        } else {
+        {
             const int take = sp < 32 ? sp : 32;
             const int ent = lane < take ? S.stack[sp - take + lane] : -1;
             __syncwarp();
@@ -1106,7 +1180,7 @@ __device__ __forceinline__ void walk_bucket(const WalkArgs &W, WalkSmem<Real, NB
         __syncwarp();
         // evaluate full tiles
         while (ppn >= PPF) {
-            stage_pp<Real, NBT, HIGH>(S, P, PPF, lane, G.bch[0], G.bch[1], G.bch[2], G.bcl[0], G.bcl[1], G.bcl[2]);
+            stage_pp<Real, NBT, HIGH>(S, P, S.pp, PPF, lane, G.bch[0], G.bch[1], G.bch[2], G.bcl[0], G.bcl[1], G.bcl[2]);
             __syncwarp();
             if (i < n) {
                 if (ppSelf) eval_pp<Real, NBT, HIGH, true>(S, PPF, i, slot, A);
@@ -1147,7 +1221,7 @@ __device__ __forceinline__ void walk_bucket(const WalkArgs &W, WalkSmem<Real, NB
     }
     // remaining partial tiles
     if (ppn > 0) {
-        stage_pp<Real, NBT, HIGH>(S, P, ppn, lane, G.bch[0], G.bch[1], G.bch[2], G.bcl[0], G.bcl[1], G.bcl[2]);
+        stage_pp<Real, NBT, HIGH>(S, P, S.pp, ppn, lane, G.bch[0], G.bch[1], G.bch[2], G.bcl[0], G.bcl[1], G.bcl[2]);
         __syncwarp();
         if (i < n) {
             if (ppSelf) eval_pp<Real, NBT, HIGH, true>(S, ppn, i, slot, A);
@@ -1170,48 +1244,61 @@ __device__ __forceinline__ void walk_bucket(const WalkArgs &W, WalkSmem<Real, NB
         flush_tile(A);
         __syncwarp();
     }
-    // reduce the 32 / NBT partial accumulators of each particle
+    bucket_end<Real, NBT, HIGH>(W, S, b, node, lo, n, nAct, A, nPart, nNewt, nSoft, lane);
+}
+
+// The evaluation pass of the two-pass walk for bucket b: its stored lists
+// (k_walk_lists) streamed tile by tile -- P-P particles (the bucket's own
+// first: the first tile leaves out each particle's pair with itself), then
+// Newtonian cells, then softened cells.  The tiles are the fused walk's,
+// fed from memory with no walk state: the terms are the same, summed in
+// list order.
+template <typename Real, int NBT, bool HIGH, class Smem>
+__device__ __forceinline__ void eval_bucket_lists(const WalkArgs &W, Smem &S, int b,
+                                                  int4 info, int lane) {
+    const TsphDevTree &T = W.T;
+    const TsphDevParts &P = W.P;
+    constexpr int CT = cell_tile<HIGH>();   // cells per tile
+    int node, lo, n;
+    BucketGeom G;
+    if (!bucket_begin<Real, NBT, HIGH>(W, S, b, lane, node, lo, n, G)) return;
+    const int i = lane % NBT, slot = lane / NBT;
+    Acc<Real> A;
 #pragma unroll
-    for (int o = NBT; o < 32; o <<= 1) {
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            Real s2 = __shfl_xor_sync(FULL, A.s[k], o);
-            Real c2 = __shfl_xor_sync(FULL, A.c[k], o);
-            two_sum_merge(A.s[k], A.c[k], s2, c2);
-        }
-        Real d2 = __shfl_xor_sync(FULL, A.dt, o);
-        A.dt = d2 > A.dt ? d2 : A.dt;
-    }
-    if (lane < n) {
-        int p = lo + lane;
-        if constexpr (sizeof(Real) == 4) {
-            P.wsum[p] = make_float4(A.s[0], A.s[1], A.s[2], A.s[3]);
-            P.wcmp[p] = make_float4(A.c[0], A.c[1], A.c[2], A.c[3]);
-            P.wdt[p] = A.dt;
-        } else {
-            P.ax[p] = (double)A.s[0];
-            P.ay[p] = (double)A.s[1];
-            P.az[p] = (double)A.s[2];
-            P.pot[p] = (double)A.s[3];
-            P.dtGrav[p] = (double)A.dt;
-        }
-    }
-    if (lane == 0) {
-        // pkdGravAll's sums over the active particles (pkd.c:2945-2950)
-        S.tAct += nAct;
-        S.tPP += (unsigned long long)nAct * nPart;
-        S.tNewt += (unsigned long long)nAct * nNewt;
-        S.tSoft += (unsigned long long)nAct * nSoft;
-        S.tBsq += (unsigned long long)nAct * n;
-        S.tIntra += (unsigned long long)nAct * (2 * (n - 1) - nAct + 1) / 2;
-        if (W.bucketLists) {
-            W.bucketLists[4 * b + 0] = node;
-            W.bucketLists[4 * b + 1] = nPart;
-            W.bucketLists[4 * b + 2] = nSoft;
-            W.bucketLists[4 * b + 3] = nNewt;
-        }
-    }
+    for (int k = 0; k < 4; ++k) { A.s[k] = 0; A.c[k] = 0; A.t[k] = 0; }
+    A.dt = 0;
+    const size_t base = (size_t)b * W.listCap;
+    const int *lp = W.listPP + base, *lc = W.listCell + base;
+    const int *ls = W.listSoft + (size_t)b * (W.listCap / 4);
     __syncwarp();
+    for (int t0 = 0; t0 < info.x; t0 += PPF) {
+        const int c = info.x - t0 < PPF ? info.x - t0 : PPF;
+        stage_pp<Real, NBT, HIGH>(S, P, lp + t0, c, lane, G.bch[0], G.bch[1], G.bch[2], G.bcl[0], G.bcl[1], G.bcl[2]);
+        __syncwarp();
+        if (i < n) {
+            if (t0 == 0) eval_pp<Real, NBT, HIGH, true>(S, c, i, slot, A);
+            else eval_pp<Real, NBT, HIGH, false>(S, c, i, slot, A);
+        }
+        flush_tile(A);
+        __syncwarp();
+    }
+    for (int t0 = 0; t0 < info.y; t0 += CT) {
+        const int c = info.y - t0 < CT ? info.y - t0 : CT;
+        stage_cells<Real, NBT, HIGH>(S, lc + t0, T, c, lane, false, G.bch[0], G.bch[1], G.bch[2], G.bcl[0], G.bcl[1], G.bcl[2]);
+        __syncwarp();
+        if (i < n) eval_newt<Real, NBT, HIGH>(S, c, i, slot, W.iOrder, A);
+        flush_tile(A);
+        __syncwarp();
+    }
+    for (int t0 = 0; t0 < info.z; t0 += CT) {
+        const int c = info.z - t0 < CT ? info.z - t0 : CT;
+        stage_cells<Real, NBT, HIGH>(S, ls + t0, T, c, lane, true, G.bch[0], G.bch[1], G.bch[2], G.bcl[0], G.bcl[1], G.bcl[2]);
+        __syncwarp();
+        if (i < n) eval_soft<Real, NBT, HIGH>(S, c, i, slot, A);
+        flush_tile(A);
+        __syncwarp();
+    }
+    bucket_end<Real, NBT, HIGH>(W, S, b, node, lo, n, G.nAct, A, info.x - n, info.y, info.z, lane);
 }
 
 // The walk of a group of buckets (the subtree node g, buckets b0..b1-1),
@@ -1384,6 +1471,9 @@ __global__ void __launch_bounds__(WPB * 32, sizeof(Real) == 4 ? (HIGH ? 3 : 5) :
                 grp = walk_group<Real, NBT, HIGH>(W, S, g, b0, b1, gl, K, lane);
             }
             for (int b = b0; b < b1; ++b) walk_bucket<Real, NBT, HIGH>(W, S, b, grp ? gl : nullptr, K, lane);
+        } else if (W.fallback) {   // the buckets the list pass left over
+            if (u >= (int)W.cnt->nListFallback) break;
+            walk_bucket<Real, NBT, HIGH>(W, S, W.fallback[u], nullptr, K, lane);
         } else {
             if (u >= *W.nBuckets) break;
             walk_bucket<Real, NBT, HIGH>(W, S, u, nullptr, K, lane);
@@ -1412,22 +1502,24 @@ __global__ void __launch_bounds__(WPB * 32, sizeof(Real) == 4 ? (HIGH ? 3 : 5) :
 
 // The list pass of the two-pass walk.  Each warp takes buckets from a work
 // counter and walks them exactly as walk_bucket does (classify_entry, the
-// same stack discipline), but instead of evaluating it stores the bucket's
-// accepted cells and opened leaves, in walk order, as entries
-// (cell << 7) | (type << 5) | replica with type = act - 1 (leaf, Newtonian
-// cell, softened cell), each round of the walk closed by a zero entry: the
-// evaluation pass replays the rounds, so its tiles fill, and its sums run,
-// in the fused walk's order (bit-identical results).  This mirrors the reference's own split into
-// pkdBucketWalk (walk.c:58-178), which builds the lists, and
+// same stack discipline), but stores what it finds instead of evaluating:
+// the bucket's own particles and then the particles of every opened leaf
+// (P-P list), the Newtonian cells and the softened cells, each as
+// (index << 5) | replica, in walk order.  This mirrors the reference's own
+// split into pkdBucketWalk (walk.c:58-178), which builds the lists, and
 // pkdBucketInteract (grav.c:23-249), which evaluates them.  Without the
-// evaluation's registers and tiles a warp needs a stack only, so several
-// times more warps fit on an SM and the walk's dependent L2 loads overlap.
-// A bucket whose list would not fit its slot, or whose stack overflows, is
-// marked -1 and walked again by the evaluation pass (which raises the
-// overflow).  Buckets the evaluation pass skips (no active particle, more
-// than NBT coincident particles) are not walked here.
+// evaluation's registers and tiles a warp needs a stack only, so many
+// warps fit on an SM and the walk's dependent L2 loads overlap.  A bucket
+// whose lists do not fit their slots is marked (w = -1) and walked by a
+// fused launch; its walk is still counted to the end, so the longest list
+// any bucket needed sizes the slots of the next call.  Buckets the
+// evaluation pass skips (no active particle, more than NBT coincident
+// particles) are not walked here.  (Walking units of 2 or 4 neighbouring
+// buckets together, one stack entry per cell of their union walk with a
+// mask of the buckets it concerns, measured slower: the per-bucket
+// decisions and appends, not the shared loads, carry the cost.)
 #define LWPB 8   // warps per block
-#define LBPS 6   // blocks per SM: 48 warps, 40 registers a thread
+#define LBPS 5   // blocks per SM: 40 warps, 48 registers a thread
 template <int NBT>
 __global__ void __launch_bounds__(LWPB * 32, LBPS) k_walk_lists(WalkArgs W) {
     __shared__ int stk[LWPB][STK];
@@ -1437,8 +1529,8 @@ __global__ void __launch_bounds__(LWPB * 32, LBPS) k_walk_lists(WalkArgs W) {
     const TsphDevTree &T = W.T;
     const TsphDevParts &P = W.P;
     WalkTally K = {0u, 0u, 0u};
-    unsigned fallback = 0;
     int *work = reinterpret_cast<int *>(&W.cnt->listWork);
+    const int cap = W.listCap, capS = W.listCap / 4;
     for (;;) {
         int b = 0;
         if (lane == 0) b = atomicAdd(work, 1);
@@ -1449,15 +1541,17 @@ __global__ void __launch_bounds__(LWPB * 32, LBPS) k_walk_lists(WalkArgs W) {
         const int n = T.pUpper[node] - lo + 1;
         const BucketGeom G = bucket_geom(T, b);
         if (n > NBT || G.bext < 0.0f) {
-            if (lane == 0) W.listCount[b] = 0;
+            if (lane == 0) W.listInfo[b] = make_int4(0, 0, 0, 0);
             continue;
         }
-        int *out = W.lists + (size_t)b * W.listCap;
-        const int root = T.sysRoot[P.rid[lo]];   // the bucket's own system
+        int *lp = W.listPP + (size_t)b * cap;
+        int *lc = W.listCell + (size_t)b * cap;
+        int *ls = W.listSoft + (size_t)b * capS;
+        if (lane < n) lp[lane] = ((lo + lane) << 5) | 31;   // own particles, replica tag 31
+        const int root = T.sysRoot[P.rid[lo]];               // the bucket's own system
         for (int r = lane; r < cW.nRep; r += 32) stack[r] = (root << 5) | r;
-        int sp = cW.nRep, nOut = 0;
-        bool spill = false;
-        WalkTally Kb = {0u, 0u, 0u};
+        int sp = cW.nRep, nP = n, nC = 0, nS = 0;
+        bool spill = false, overflow = false;
         __syncwarp();
         while (sp > 0) {
             const int take = sp < 32 ? sp : 32;
@@ -1468,41 +1562,59 @@ __global__ void __launch_bounds__(LWPB * 32, LBPS) k_walk_lists(WalkArgs W) {
             if (ent >= 0) {
                 cell = ent >> 5;
                 rep = ent & 31;
-                act = classify_entry(T, P, b, node, lo, n, G, cell, rep, up, plo, cnt, Kb);
+                act = classify_entry(T, P, b, node, lo, n, G, cell, rep, up, plo, cnt, K);
             }
-            const unsigned bo = __ballot_sync(FULL, act == ACT_OPEN);
             if (act == ACT_LEAF && cnt > NBT) {
                 atomicOr(&W.cnt->status, 1u << TSPH_ERR_UNSUPPORTED);
                 act = ACT_NONE;
             }
-            // the round's entries, then a zero entry closing the round
-            const unsigned bk = __ballot_sync(FULL, act >= ACT_LEAF);
-            const int add = bk ? __popc(bk) + 1 : 0;
-            if (sp + 2 * __popc(bo) > STK || nOut + add > W.listCap) {
-                spill = true;
+            const unsigned bo = __ballot_sync(FULL, act == ACT_OPEN);
+            if (sp + 2 * __popc(bo) > STK) {
+                overflow = true;
                 break;
             }
+            const unsigned bl = __ballot_sync(FULL, act == ACT_LEAF);
+            const unsigned bn = __ballot_sync(FULL, act == ACT_NEWT);
+            const unsigned bs = __ballot_sync(FULL, act == ACT_SOFT);
+            const int leafParts = __reduce_add_sync(FULL, act == ACT_LEAF ? cnt : 0);
+            // past a full slot the lists are only counted
+            spill = spill || nP + leafParts > cap || nC + __popc(bn) > cap || nS + __popc(bs) > capS;
             const unsigned lt = lane_lt();
             if (act == ACT_OPEN) {
                 const int pos = sp + 2 * __popc(bo & lt);
                 stack[pos] = (up << 5) | rep;
                 stack[pos + 1] = ((cell + 1) << 5) | rep;
-            } else if (act >= ACT_LEAF) {
-                out[nOut + __popc(bk & lt)] =
-                    (int)(((unsigned)cell << 7) | (unsigned)((act - 1) << 5) | (unsigned)rep);
+            } else if (!spill && act == ACT_NEWT) {
+                lc[nC + __popc(bn & lt)] = (cell << 5) | rep;
+            } else if (!spill && act == ACT_SOFT) {
+                ls[nS + __popc(bs & lt)] = (cell << 5) | rep;
             }
-            if (bk && lane == 0) out[nOut + add - 1] = 0;
+            if (!spill) {   // opened leaves: their particles, one leaf at a time across the warp
+                int at = nP;
+                for (unsigned m = bl; m; m &= m - 1u) {
+                    const int src = __ffs(m) - 1;
+                    const int c = __shfl_sync(FULL, cnt, src);
+                    const int p0 = __shfl_sync(FULL, plo, src);
+                    const int r0 = __shfl_sync(FULL, rep, src);
+                    if (lane < c) lp[at + lane] = ((p0 + lane) << 5) | r0;
+                    at += c;
+                }
+            }
             sp += 2 * __popc(bo);
-            nOut += add;
+            nP += leafParts;
+            nC += __popc(bn);
+            nS += __popc(bs);
             __syncwarp();
         }
-        if (!spill) {
-            K.visit += Kb.visit;
-            K.tests += Kb.tests;
-            K.exact += Kb.exact;
+        if (lane == 0) {
+            const bool left = spill || overflow;
+            W.listInfo[b] = left ? make_int4(0, 0, 0, -1) : make_int4(nP, nC, nS, 0);
+            if (left) W.fallback[atomicAdd(&W.cnt->nListFallback, 1u)] = b;
+            if (spill && !overflow) {
+                const int need = nP > nC ? (nP > 4 * nS ? nP : 4 * nS) : (nC > 4 * nS ? nC : 4 * nS);
+                atomicMax(&W.cnt->listNeed, (unsigned)need);
+            }
         }
-        fallback += spill;
-        if (lane == 0) W.listCount[b] = spill ? -1 : nOut;
         __syncwarp();
     }
     unsigned long long tests = K.tests, visit = K.visit, exact = K.exact;
@@ -1516,7 +1628,37 @@ __global__ void __launch_bounds__(LWPB * 32, LBPS) k_walk_lists(WalkArgs W) {
         atomicAdd(&W.cnt->nTests, tests);
         atomicAdd(&W.cnt->nVisits, visit);
         atomicAdd(&W.cnt->nExactTests, exact);
-        if (fallback) atomicAdd(&W.cnt->nListFallback, fallback);
+    }
+}
+
+// The evaluation pass of the two-pass walk: every bucket with stored lists
+// (eval_bucket_lists), a warp per bucket from a work counter.  Its shared
+// memory holds tiles only, so registers alone set its occupancy.
+#define EVAL_BPS(Real, HIGH) (sizeof(Real) == 4 ? (HIGH ? 4 : 8) : 2)
+template <typename Real, int NBT, bool HIGH>
+__global__ void __launch_bounds__(WPB * 32, EVAL_BPS(Real, HIGH)) k_walk_eval(WalkArgs W) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    const int lane = threadIdx.x & 31;
+    EvalSmem<Real, NBT, HIGH> &S = reinterpret_cast<EvalSmem<Real, NBT, HIGH> *>(smraw)[threadIdx.x >> 5];
+    const unsigned FULL = 0xffffffffu;
+    if (lane == 0) S.tAct = S.tPP = S.tNewt = S.tSoft = S.tBsq = S.tIntra = 0ull;
+    __syncwarp();
+    int *work = reinterpret_cast<int *>(&W.cnt->evalWork);
+    for (;;) {
+        int b = 0;
+        if (lane == 0) b = atomicAdd(work, 1);
+        b = __shfl_sync(FULL, b, 0);
+        if (b >= *W.nBuckets) break;
+        const int4 info = W.listInfo[b];
+        if (info.w >= 0) eval_bucket_lists<Real, NBT, HIGH>(W, S, b, info, lane);
+    }
+    if (lane == 0) {
+        atomicAdd(&W.cnt->nActive, S.tAct);
+        atomicAdd(&W.cnt->nPartPP, S.tPP);
+        atomicAdd(&W.cnt->nCellNewt, S.tNewt);
+        atomicAdd(&W.cnt->nCellSoft, S.tSoft);
+        atomicAdd(&W.cnt->nBucketSq, S.tBsq);
+        atomicAdd(&W.cnt->nIntra, S.tIntra);
     }
 }
 
@@ -1666,30 +1808,39 @@ static int prepare_groups(tsph_ctx *ctx, WalkArgs &A, int nbHost, int warps) {
     return TSPH_OK;
 }
 
-// The two-pass walk (k_walk_lists, then k_walk reading the lists), when
-// there are no walk groups and the tuning asks for it (walkLists 1, or
-// >= 32: that many entries per bucket; 0 and -1: one fused pass).  By default a bucket's slot
-// holds 1024 entries, doubled (up to 8192) when more than 1 in 256 buckets
-// of the last evaluation did not fit; a bucket that does not fit is walked
-// by the evaluation pass.
-// Outside a capture the arrays grow to the particle count (a bound on the
-// buckets of any later captured step); a capture uses what is there.
+// The two-pass walk (k_walk_lists, then k_walk_eval over the stored
+// lists), when there are no walk groups and the tuning asks for it
+// (walkLists 1, or >= 32: that many P-P and cell entries per bucket; 0 and
+// -1: one fused pass).  By default a bucket's slots start at 512 entries
+// and grow, for the next call, to the power of two that holds the longest
+// list a bucket of the last call needed, as long as all slots stay within
+// 16 GB; a bucket that does not fit is walked by a fused launch.  Outside a
+// capture the arrays grow to twice the buckets; a capture uses what is
+// there (and walks fused when that is too little).
 static int prepare_lists(tsph_ctx *ctx, WalkArgs &A, int nbHost, int nbt) {
-    A.lists = nullptr;
-    A.listCount = nullptr;
+    A.listPP = A.listCell = A.listSoft = nullptr;
+    A.listInfo = nullptr;
     A.listCap = 0;
+    A.fallback = nullptr;
     if (ctx->walkLists <= 0 || A.groupFirst || nbHost <= 0) return TSPH_OK;
-    if (ctx->T.nNodes >= (1 << 25)) return TSPH_OK;   // entries hold the cell index in 25 bits
+    if (ctx->n >= (1 << 26) || ctx->T.nNodes >= (1 << 26)) return TSPH_OK;   // (index << 5) entries
     if (!ctx->capturing) {
-        if (ctx->walkListSlot == 0) ctx->walkListSlot = 1024;
-        if (ctx->walkLists <= 1 && ctx->lastListFallback * 256LL > (long long)ctx->lastListBuckets &&
-            ctx->walkListSlot < 8192)
-            ctx->walkListSlot *= 2;
-        const long long cap = nbHost > ctx->n ? nbHost : ctx->n;
+        // room for twice the buckets (a captured step's trees may hold more)
+        const long long cap = 2LL * nbHost > 1024 ? 2LL * nbHost : 1024;
+        if (ctx->walkListSlot == 0) ctx->walkListSlot = 512;
+        if (ctx->walkLists == 1) {
+            // P-P and cell slots, a quarter for softened cells: 9 bytes per entry
+            const long long maxSlot = (16LL << 30) / (9LL * cap);
+            while ((long long)ctx->walkListSlot < ctx->lastListNeed && 2LL * ctx->walkListSlot <= maxSlot)
+                ctx->walkListSlot *= 2;
+        }
         const size_t need = (size_t)cap * ctx->walkListSlot;
         if (ctx->walkListBuckets < cap || ctx->walkListEntries < need) {
-            int rc = tsph_grow(ctx, &ctx->dWalkLists, need);
-            if (!rc) rc = tsph_grow(ctx, &ctx->dWalkListCount, (size_t)cap);
+            int rc = tsph_grow(ctx, &ctx->dWalkListPP, need);
+            if (!rc) rc = tsph_grow(ctx, &ctx->dWalkListCell, need);
+            if (!rc) rc = tsph_grow(ctx, &ctx->dWalkListSoft, need / 4);
+            if (!rc) rc = tsph_grow(ctx, &ctx->dWalkListInfo, (size_t)cap);
+            if (!rc) rc = tsph_grow(ctx, &ctx->dWalkListFallback, (size_t)cap);
             if (rc) { ctx->walkListBuckets = 0; ctx->walkListEntries = 0; return rc; }
             ctx->walkListBuckets = cap;
             ctx->walkListEntries = need;
@@ -1698,10 +1849,14 @@ static int prepare_lists(tsph_ctx *ctx, WalkArgs &A, int nbHost, int nbt) {
     if (ctx->walkListBuckets < nbHost || !ctx->walkListSlot ||
         ctx->walkListEntries < (size_t)nbHost * ctx->walkListSlot)
         return TSPH_OK;
-    A.lists = ctx->dWalkLists;
-    A.listCount = ctx->dWalkListCount;
+    A.listPP = ctx->dWalkListPP;
+    A.listCell = ctx->dWalkListCell;
+    A.listSoft = ctx->dWalkListSoft;
+    A.listInfo = ctx->dWalkListInfo;
     A.listCap = ctx->walkListSlot;
-    TSPH_CK(cudaMemsetAsync(&ctx->dCnt->listWork, 0, sizeof(unsigned int), ctx->stream));
+    A.fallback = ctx->dWalkListFallback;
+    // list and evaluation work counters, and the left-over count
+    TSPH_CK(cudaMemsetAsync(&ctx->dCnt->listWork, 0, 3 * sizeof(unsigned int), ctx->stream));
     const int blocks = ctx->smCount * LBPS;
     if (nbt == 8) k_walk_lists<8><<<blocks, LWPB * 32, 0, ctx->stream>>>(A);
     else if (nbt == 16) k_walk_lists<16><<<blocks, LWPB * 32, 0, ctx->stream>>>(A);
@@ -1716,6 +1871,16 @@ static int launch_walk(tsph_ctx *ctx, const WalkArgs &A, int blocks, const char 
     if (!ctx->capturing)
         TSPH_CK(cudaFuncSetAttribute(k_walk<Real, NBT, HIGH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)sm));
+    if (A.listInfo) {
+        // evaluation pass over the stored lists, then the fused walk of the
+        // buckets whose lists did not fit
+        const size_t se = sizeof(EvalSmem<Real, NBT, HIGH>) * WPB;
+        if (!ctx->capturing)
+            TSPH_CK(cudaFuncSetAttribute(k_walk_eval<Real, NBT, HIGH>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)se));
+        k_walk_eval<Real, NBT, HIGH><<<ctx->smCount * EVAL_BPS(Real, HIGH), WPB * 32, se, ctx->stream>>>(A);
+        TSPH_LAUNCH_CK("k_walk_eval");
+    }
     k_walk<Real, NBT, HIGH><<<blocks, WPB * 32, sm, ctx->stream>>>(A);
     TSPH_LAUNCH_CK(name);
     return TSPH_OK;

@@ -172,13 +172,15 @@ struct tsph_ctx {
     int walkLists;               // two-pass walk (1 or a slot size: on; 0, -1: off)
     double *dKeep;               // accelerations kept across a step capture's preparation
     size_t keepCap;
-    int *dWalkLists;             // the list pass's entries, walkListSlot per bucket
-    int *dWalkListCount;         // entries per bucket (-1: walked by the evaluation pass)
+    int *dWalkListPP;            // the list pass's P-P particles, walkListSlot per bucket
+    int *dWalkListCell;          // its Newtonian cells, walkListSlot per bucket
+    int *dWalkListSoft;          // its softened cells, walkListSlot / 4 per bucket
+    int4 *dWalkListInfo;         // list lengths per bucket (w = -1: left to a fused walk)
+    int *dWalkListFallback;      // the buckets left to a fused walk
     long long walkListBuckets;   // buckets the arrays hold
-    size_t walkListEntries;      // entries dWalkLists holds
+    size_t walkListEntries;      // entries dWalkListPP and dWalkListCell hold
     int walkListSlot;            // entries per bucket
-    long long lastListFallback;  // buckets the list pass left over in the last evaluation
-    long long lastListBuckets;   // and the buckets of that evaluation
+    long long lastListNeed;      // longest list a bucket of the last evaluation did not fit
     int *dGroupFlag, *dGroupScan;  // per bucket: starts a group, and the inclusive scan
     int *dGroupFirst;            // first bucket of every group, then the bucket count
     int *dGroupCount;            // device: number of groups

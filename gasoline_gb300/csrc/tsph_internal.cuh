@@ -147,5 +147,7 @@ struct TsphDevCounters {
     unsigned int status;             // TSPH_ERR_* raised on device
     unsigned int pad;                // work counter of the walk's evaluation pass
     unsigned int listWork;           // work counter of the walk's list pass
-    unsigned int nListFallback;      // buckets the list pass left to the evaluation pass
+    unsigned int evalWork;           // work counter of its evaluation pass
+    unsigned int nListFallback;      // buckets the list pass left to a fused walk
+    unsigned int listNeed;           // longest list of such a bucket (slot entries)
 };

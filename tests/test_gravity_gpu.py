@@ -399,14 +399,19 @@ def test_update_particles_keeps_order_same_forces(ctx):
 
 
 @pytest.mark.parametrize("case", ["plummer", "box", "clumps"])
-def test_two_pass_walk_is_bit_identical(case):
-    """The two-pass walk (a list pass storing every bucket's interaction
-    list, then the evaluation pass reading it) evaluates the same lists in
-    the same order as the fused walk: accelerations, potentials, dtGrav,
-    per-bucket list lengths and pkdGravAll's counters are bit-identical, in
-    FP32 and FP64, for quadrupole and hexadecapole cells and bucket sizes
-    8, 16 and 32.  Slots of 64 entries make most buckets overflow the list
-    pass, so the evaluation pass walks those itself: still bit-identical."""
+def test_two_pass_walk_keeps_every_list(case):
+    """The two-pass walk (a list pass walking units of neighbouring buckets
+    together and storing every bucket's P-P particles, Newtonian and
+    softened cells; then the evaluation pass streaming them tile by tile)
+    builds the fused walk's lists: per-bucket list lengths and pkdGravAll's
+    counters are equal, in FP32 and FP64, for quadrupole and hexadecapole
+    cells and bucket sizes 8, 16 and 32.  The evaluation pass
+    sums all P-P tiles before the cell tiles, so the forces move by
+    summation order only (the walk-group bars), and repeat bit for bit once
+    the list slots have grown to the lists (a bucket whose lists overflow
+    its slots is walked by a fused launch, and the slots double for the
+    next call when many did).  Slots of 64 entries make most buckets
+    overflow the list pass."""
     if case == "plummer":
         pos, vel, m = g.ics.plummer(32768, seed=3)
         soft = np.full(len(m), 0.01)
@@ -421,22 +426,29 @@ def test_two_pass_walk_is_bit_identical(case):
         periodic = True
     c = g.Context(0)
     try:
-        for prec in (g.FP32, g.FP64):
+        for prec, tol, tolp in ((g.FP64, 1e-12, 1e-12), (g.FP32, 1e-5, 3e-4 if periodic else 1e-5)):
             for order, nb in ((2, 16), (4, 8), (2, 32)):
                 gp = g.grav_params(periodic=periodic, precision=prec, iOrder=order, nBucket=nb)
-                ref = None
-                for wl in (-1, 1, 64):
+                ref = prev = None
+                for wl in (-1, 1, 1, 1, 64):
                     c.set_tuning(walkGroup=-1, walkLists=wl)
                     c.set_particles(pos, m, soft)
                     out = c.grav_all(gp)
                     res = (out, c.get_lists(), c.get_gravity())
+                    key = (prec, order, nb, wl)
                     if ref is None:
                         ref = res
                         continue
-                    key = (prec, order, nb, wl)
-                    assert out == ref[0], key
+                    for k in ("nActive", "nBuckets", "dPartSum", "dCellSum", "dSoftSum", "dFlop",
+                              "dFlopEwald"):
+                        assert out[k] == ref[0][k], (key, k)
                     assert np.array_equal(res[1], ref[1]), key
-                    for k in ("acc", "pot", "dtGrav"):
-                        assert np.array_equal(res[2][k], ref[2][k]), (key, k)
+                    for k, t in (("acc", tol), ("pot", tolp)):
+                        sc = np.abs(ref[2][k]).max()
+                        assert np.abs(res[2][k] - ref[2][k]).max() <= t * sc, (key, k)
+                    if wl == 1 and prev is not None and prev[3]:   # repeats exactly
+                        for k in ("acc", "pot", "dtGrav"):
+                            assert np.array_equal(res[2][k], prev[2][k]), (key, k)
+                    prev = res + (prev is not None,) if wl == 1 else None
     finally:
         c.close()
