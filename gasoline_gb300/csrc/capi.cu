@@ -113,6 +113,7 @@ extern "C" void tsph_destroy(tsph_ctx *ctx) {
     FREE(ctx->dStore); FREE(ctx->dStoreOrder);
     FREE(ctx->dWalkListPP); FREE(ctx->dWalkListCell); FREE(ctx->dWalkListSoft);
     FREE(ctx->dWalkListInfo); FREE(ctx->dWalkListFallback); FREE(ctx->dKeep);
+    FREE(ctx->dStepDt);
     tsph_free_snapshot(ctx);
     free(ctx->hSys);
     free(ctx->hTmp);

@@ -1828,9 +1828,11 @@ extern "C" int tsph_get_neighbour_hash(tsph_ctx *ctx, int *count, unsigned long 
 // (dvPredFacTwo = duPredDelta = 0, msrKickKDKOpen master.c:6540-6639); the
 // closing kick predicts them to its end (msrKickKDKClose master.c:6644-6741).
 // a is gravity plus, for gas, the hydrodynamic acceleration.
-__global__ void k_kick_rung(int n, int ngas, int iRung, double dt, int bClose, TsphDevState C) {
+__global__ void k_kick_rung(int n, int ngas, int iRung, double dt, const double *dtp, int bClose,
+                            TsphDevState C) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    if (dtp) dt *= *dtp;   // a captured step: dt is a fraction of the step in device memory
     if (iRung >= 0 && C.rung[i] != iRung) return;
     const bool gas = i < ngas;
     double a[3] = {C.ax[i], C.ay[i], C.az[i]};
@@ -1854,9 +1856,11 @@ __global__ void k_kick_rung(int n, int ngas, int iRung, double dt, int bClose, T
 // pkdDrift (pkd.c:3686-3778) and, for gas, pkdKickVpred (pkd.c:6489-6552)
 // as msrDrift runs them (master.c:6306-6437): r += v dt with the periodic
 // wrap, then vPred += a dt and uPred += uDot dt.
-__global__ void k_drift(int n, int ngas, double dt, int bPeriodic, double L, TsphDevState C) {
+__global__ void k_drift(int n, int ngas, double dt, const double *dtp, int bPeriodic, double L,
+                        TsphDevState C) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    if (dtp) dt *= *dtp;   // a captured step: dt is a fraction of the step in device memory
     double *r[3] = {C.x, C.y, C.z};
     const double *v[3] = {C.vx, C.vy, C.vz};
 #pragma unroll
@@ -1881,14 +1885,14 @@ __global__ void k_drift(int n, int ngas, double dt, int bPeriodic, double L, Tsp
 
 int tsph_kick_launch(tsph_ctx *ctx, int iRung, double dt, int bClose) {
     k_kick_rung<<<tsph_blocks(ctx->n, 256), 256, 0, ctx->stream>>>(ctx->n, ctx->ngas, iRung, dt,
-                                                                     bClose, ctx->C);
+                                                                     ctx->stepDtDev, bClose, ctx->C);
     TSPH_LAUNCH_CK("k_kick_rung");
     return TSPH_OK;
 }
 
 int tsph_drift_launch(tsph_ctx *ctx, double dt, int bPeriodic, double dPeriod) {
-    k_drift<<<tsph_blocks(ctx->n, 256), 256, 0, ctx->stream>>>(ctx->n, ctx->ngas, dt, bPeriodic,
-                                                                 dPeriod, ctx->C);
+    k_drift<<<tsph_blocks(ctx->n, 256), 256, 0, ctx->stream>>>(ctx->n, ctx->ngas, dt, ctx->stepDtDev,
+                                                                 bPeriodic, dPeriod, ctx->C);
     TSPH_LAUNCH_CK("k_drift");
     return TSPH_OK;
 }

@@ -9,10 +9,13 @@
 // (msrKickKDKClose).  In graph mode every launch of that sequence is
 // recorded once and the whole step replays as one graph launch: no host
 // round trip, no per-kernel launch cost, which is what many small systems
-// in one context need.  A captured build runs a fixed number of top-phase
-// levels (its preparation's depth + 4; deeper nodes become subtree tasks)
-// and has fixed coordinate bounds; a particle leaving them raises
-// TSPH_ERR_BOUNDS and the next call recaptures.
+// in one context need.  The graph's kicks and drifts read dt from device
+// memory, set by a one-thread kernel before each replay, so a new dt needs
+// no recapture.  A captured build runs a fixed number of top-phase levels
+// (its preparation's depth + 4; deeper nodes become subtree tasks) and has
+// fixed coordinate bounds; a particle leaving them raises TSPH_ERR_BOUNDS
+// and the next call recaptures.  dt may be negative: the leapfrog is
+// time-reversible, so a step of -dt undoes a step of dt up to rounding.
 #include <math.h>
 #include <string.h>
 
@@ -24,6 +27,8 @@ __global__ void k_coord_maxabs(int n, TsphDevState C, unsigned long long *out) {
     if (i < n) a = fmax(fabs(C.x[i]), fmax(fabs(C.y[i]), fabs(C.z[i])));
     warp_max_abs(a, out);
 }
+
+__global__ void k_set_step_dt(double *d, double dt) { *d = dt; }
 
 static int step_body(tsph_ctx *ctx, double dt, const tsph_grav_params *gp,
                      const tsph_sph_params *sp) {
@@ -47,10 +52,10 @@ static void drop_graph(tsph_ctx *ctx) {
     ctx->graphExec = nullptr;
 }
 
-static bool graph_matches(const tsph_ctx *ctx, double dt, const tsph_grav_params *gp,
-                          const tsph_sph_params *sp) {
-    if (!ctx->graphExec || ctx->graphDt != dt || ctx->graphN != ctx->n ||
-        ctx->graphNgas != ctx->ngas || ctx->graphSysVersion != ctx->sysVersion)
+// A captured step reads dt from device memory, so one graph serves every dt.
+static bool graph_matches(const tsph_ctx *ctx, const tsph_grav_params *gp, const tsph_sph_params *sp) {
+    if (!ctx->graphExec || ctx->graphN != ctx->n || ctx->graphNgas != ctx->ngas ||
+        ctx->graphSysVersion != ctx->sysVersion)
         return false;
     if (memcmp(&ctx->graphGrav, gp, sizeof(*gp)) != 0) return false;
     if ((sp != nullptr) != (ctx->graphHasSph != 0)) return false;
@@ -61,8 +66,7 @@ static bool graph_matches(const tsph_ctx *ctx, double dt, const tsph_grav_params
 // (allocating everything, uploading constants; the accelerations the
 // previous step left are kept), then the step is captured with the
 // coordinate bound fixed at twice the current extent.
-static int capture_step(tsph_ctx *ctx, double dt, const tsph_grav_params *gp,
-                        const tsph_sph_params *sp) {
+static int capture_step(tsph_ctx *ctx, const tsph_grav_params *gp, const tsph_sph_params *sp) {
     drop_graph(ctx);
     const int n = ctx->n;
     TSPH_CK(cudaMemsetAsync(ctx->dAux + 1, 0, sizeof(unsigned long long), ctx->stream));
@@ -107,13 +111,19 @@ static int capture_step(tsph_ctx *ctx, double dt, const tsph_grav_params *gp,
         if (len[k]) TSPH_CK(cudaMemcpyAsync(keep[k], ctx->dKeep + off[k], sizeof(double) * len[k],
                                             cudaMemcpyDeviceToDevice, ctx->stream));
     TSPH_CK(cudaStreamSynchronize(ctx->stream));
+    if (!ctx->dStepDt && cudaMalloc((void **)&ctx->dStepDt, sizeof(double)) != cudaSuccess) {
+        ctx->capLimit = 0;
+        return TSPH_ERR_NOMEM;
+    }
     cudaGraph_t graph = nullptr;
     TSPH_CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     ctx->capturing = true;
+    ctx->stepDtDev = ctx->dStepDt;   // kicks and drifts scale a unit step by the dt there
     const long long before = ctx->launches;
-    rc = step_body(ctx, dt, gp, sp);
+    rc = step_body(ctx, 1.0, gp, sp);
     ctx->graphKernels = ctx->launches - before;
     ctx->launches = before;
+    ctx->stepDtDev = nullptr;
     ctx->capturing = false;
     cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
     if (!rc && e != cudaSuccess) rc = tsph_cuda_fail(ctx, e, "cudaStreamEndCapture");
@@ -128,7 +138,6 @@ static int capture_step(tsph_ctx *ctx, double dt, const tsph_grav_params *gp,
         cudaGetLastError();
         return rc;
     }
-    ctx->graphDt = dt;
     ctx->graphN = n;
     ctx->graphNgas = ctx->ngas;
     ctx->graphSysVersion = ctx->sysVersion;
@@ -140,17 +149,19 @@ static int capture_step(tsph_ctx *ctx, double dt, const tsph_grav_params *gp,
 
 extern "C" int tsph_step(tsph_ctx *ctx, double dt, const tsph_grav_params *gp,
                          const tsph_sph_params *sp, int flags) {
-    if (!ctx || !gp || !(dt >= 0)) return TSPH_ERR_ARG;
+    if (!ctx || !gp || !isfinite(dt)) return TSPH_ERR_ARG;
     if (!ctx->haveParts || !ctx->haveVel) return TSPH_ERR_STATE;
     cudaSetDevice(ctx->device);
     if (!(flags & TSPH_STEP_GRAPH)) return step_body(ctx, dt, gp, sp);
     // a captured density pass can seed from the h-network, not collect for it
     if (sp && sp->bLearnedH && ctx->hnet.collect) return TSPH_ERR_UNSUPPORTED;
     if (ctx->n == 0) return TSPH_OK;
-    if (!graph_matches(ctx, dt, gp, sp)) {
-        int rc = capture_step(ctx, dt, gp, sp);
+    if (!graph_matches(ctx, gp, sp)) {
+        int rc = capture_step(ctx, gp, sp);
         if (rc) return rc;
     }
+    k_set_step_dt<<<1, 1, 0, ctx->stream>>>(ctx->dStepDt, dt);
+    TSPH_LAUNCH_CK("k_set_step_dt");
     TSPH_CK(cudaGraphLaunch(ctx->graphExec, ctx->stream));
     ctx->launches += ctx->graphKernels;   // kernels the replay runs
     return TSPH_OK;

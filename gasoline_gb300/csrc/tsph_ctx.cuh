@@ -192,9 +192,10 @@ struct tsph_ctx {
     unsigned int *dStepStatus;   // device: status bits accumulated over a step
     // captured kick-drift-kick step (tsph_step)
     cudaGraphExec_t graphExec;
+    double *dStepDt;             // the step's dt, read by a captured step's kicks and drifts
+    const double *stepDtDev;     // dStepDt while a step is captured, else null
     tsph_grav_params graphGrav;
     tsph_sph_params graphSph;
-    double graphDt;
     int graphN, graphNgas, graphHasSph;
     long long graphKernels;      // kernel launches recorded in the graph
     long long graphSysVersion;

@@ -504,7 +504,8 @@ int tsph_get_tuning(tsph_ctx *ctx, tsph_tuning *t);
  * pass, gas pressure and the pressure pass), kick dt/2.  sp may be NULL
  * (gravity only).  Returns when the work is queued on the context stream.
  * With TSPH_STEP_GRAPH the step's launches are captured once into a CUDA
- * graph (recaptured when dt, the parameters or the particle set change)
+ * graph (recaptured when the parameters or the particle set change; the
+ * graph reads dt from device memory, so a new dt replays the same graph)
  * and each call replays it with one launch.  Graph mode takes isolated and
  * periodic (Ewald) systems and a density pass seeded by the h-network; it
  * returns TSPH_ERR_UNSUPPORTED while the h-network collects samples.  The
@@ -512,6 +513,8 @@ int tsph_get_tuning(tsph_ctx *ctx, tsph_tuning *t);
  * accelerations the step's opening kick reads, so graph steps equal direct
  * ones bit for bit.  No reference counterpart for the graph: the reference
  * drives the same sequence from its host loop.
+ * dt may be any finite value, negative included (the leapfrog is
+ * time-reversible: a step of -dt undoes one of dt up to rounding).
  * tsph_step_status waits for the queued steps and returns the first error
  * any of them raised (TSPH_OK if none); TSPH_ERR_BOUNDS means a particle
  * moved beyond twice the extent the graph was captured for, and the next
