@@ -18,6 +18,18 @@
 
 #define EW_MAXH 512
 
+// The FP32 kernel's real-space sum stops at alpha r = EW_XCUT_F32 when that
+// is nearer than fEwCut L.  An image there contributes at most
+// M alpha^2 (erfc(x)/x^2 + 2/sqrt(pi) e^(-x^2)/x) = 1.6e-9 M alpha^2 at
+// x = 4.5 (less for the higher moments), falling by 10^2 per 0.5 in x,
+// while the hole images add terms of order M alpha^2 / 4 whose FP32
+// rounding (2^-24 of each) is of the size of all the left-out terms
+// together.  The FP32 error against the FP64 path is measured on the box
+// (bench.py) and held to the FP32 bars of the tests.  The FP64 kernel
+// keeps the reference's cut, fEwCut, and both count pkdGravAll's Ewald
+// flops over the terms within it, as the reference does.
+#define EW_XCUT_F32 4.5
+
 // complete root multipoles in the reference's ILCN member order
 struct EwMom {
     double m, x, y, z;
@@ -33,6 +45,7 @@ struct EwConst {
     EwMom mom;
     float momf[35];
     double L, alpha, alpha2, k1, ka, fEwCut2, smallR2;
+    float fEwCut2f;      // the FP32 kernel's real-space cut (see EW_XCUT_F32)
     int nEwReps, nReps, nEwh, iOrder;
     int hMax;            // largest |component| of a k-space vector
     int hCut2;           // floor(fEwhCut^2): the integer |h|^2 kept (ewald.c:205-211)
@@ -388,6 +401,7 @@ __global__ void __launch_bounds__(128) k_ewald(TsphDevParts P, TsphDevCounters *
         const Real L = (Real)cE.L;
         const Real alpha2 = (Real)cE.alpha2, alpha = (Real)cE.alpha, ka = (Real)cE.ka;
         const Real fEwCut2 = (Real)cE.fEwCut2, smallR2 = (Real)cE.smallR2;
+        const Real evalCut2 = sizeof(Real) == 4 ? (Real)cE.fEwCut2f : fEwCut2;
         const int iOrder = cE.iOrder;
         Real fPot = (Real)(cE.mom.m * cE.k1), ax = 0, ay = 0, az = 0;
         Real cpot = 0, cax = 0, cay = 0, caz = 0;   // compensations (FP32 only)
@@ -415,6 +429,8 @@ __global__ void __launch_bounds__(128) k_ewald(TsphDevParts P, TsphDevCounters *
             const Real dxo = dx + im.x * L, dyo = dy + im.y * L, dzo = dz + im.z * L;
             const Real r2 = dxo * dxo + dyo * dyo + dzo * dzo;
             if (r2 > fEwCut2) continue;
+            ++nLoop;   // pkdGravAll's flop count follows the reference's cut
+            if (r2 > evalCut2) continue;
             Real gam[6];
             ewald_gam<Real, false>(r2, alpha, alpha2, ka, smallR2, gam);
             Real tx = 0, ty = 0, tz = 0, tp = 0;
@@ -424,7 +440,6 @@ __global__ void __launch_bounds__(128) k_ewald(TsphDevParts P, TsphDevCounters *
             kadd(ay, cay, ty);
             kadd(az, caz, tz);
             kadd(fPot, cpot, tp);
-            ++nLoop;
         }
         if (sizeof(Real) == 4 && cE.hMax <= 3) {
             // FP32: e^{i h.x} of every k-space vector from the three phase
@@ -650,6 +665,8 @@ __global__ void __launch_bounds__(EWC_BS) k_ewald_const(EwParams p, const double
         E.k1 = M_PI / (E.alpha2 * L * L * L);
         E.ka = 2.0 * E.alpha / sqrt(M_PI);
         E.fEwCut2 = p.fEwCut * p.fEwCut * L * L;
+        const double xc = EW_XCUT_F32 / E.alpha;
+        E.fEwCut2f = (float)(xc * xc < E.fEwCut2 ? xc * xc : E.fEwCut2);
         E.smallR2 = 3.0e-3 * L * L;
         E.nReps = p.nReps;
         E.nEwReps = p.nEwReps;

@@ -12,7 +12,7 @@
 // in one context need.  The graph's kicks and drifts read dt from device
 // memory, set by a one-thread kernel before each replay, so a new dt needs
 // no recapture.  A captured build runs a fixed number of top-phase levels
-// (its preparation's depth + 4; deeper nodes become subtree tasks) and has
+// (its preparation's depth + 2; deeper nodes become subtree tasks) and has
 // fixed coordinate bounds; a particle leaving them raises TSPH_ERR_BOUNDS
 // and the next call recaptures.  dt may be negative: the leapfrog is
 // time-reversible, so a step of -dt undoes a step of dt up to rounding.

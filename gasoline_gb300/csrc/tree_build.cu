@@ -1738,9 +1738,9 @@ static int build_tree_body(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n
     const int Fcap = 2 * (n / S) + 2;
     int Fb = F;
     // a captured build runs a fixed number of levels (its preparation's
-    // depth + 4) with no host look; what is left becomes subtree tasks
+    // depth + 2) with no host look; what is left becomes subtree tasks
     const bool cap = ctx->capturing;
-    const int Lmax = cap ? (T.lastTopLevels + 4 < TSPH_MAX_LEVELS - 2 ? T.lastTopLevels + 4
+    const int Lmax = cap ? (T.lastTopLevels + 2 < TSPH_MAX_LEVELS - 2 ? T.lastTopLevels + 2
                                                                       : TSPH_MAX_LEVELS - 2)
                          : TSPH_MAX_LEVELS - 2;
     // the first look comes at the last build's depth (the same particles
