@@ -560,28 +560,34 @@ def _cuda_ms(fn, stream):
 
 
 def run_profile(args):
-    """The box's FP32 force evaluation alone, `steps` times after `warmup`
-    (no autotune, FP64 or error legs): the command the ncu summaries use."""
+    """The box's FP32 step alone, as the timed run takes it -- a
+    kick-drift-kick step replayed from one CUDA graph, dt +-DRIFT_DT in
+    turn -- `steps` times after `warmup` (no autotune, FP64, error or CPU
+    legs): the command the ncu summaries use."""
     import torch
     import gasoline_gb300 as g
     stream = torch.cuda.Stream()
     ctx = g.Context(0, stream=stream.cuda_stream)
     # the knobs the timed run's autotuner picks for this box: the default
-    # five walk blocks per SM, no walk groups
+    # five walk blocks per SM, no walk groups, the fused walk
     ctx.set_tuning(walkGroup=-1)
-    pos, m, soft = workload(args.ng)
+    pos, vel, m, soft = workload(args.ng, with_vel=True)
     ctx.set_particles(pos, m, soft)
+    ctx.set_velocities(vel)
     gp = g.grav_params(periodic=True, precision=g.FP32, nBucket=NBUCKET)
+    ctx.grav_all(gp)
+    sgn = -1.0
     for _ in range(args.warmup):
-        ctx.grav_all(gp)
-    ph = []
+        sgn = -sgn
+        ctx.step(sgn * DRIFT_DT, gp, None, graph=True)
+    ms = []
     for _ in range(args.steps):
-        ctx.grav_all(gp)
-        ph.append(ctx.timings())
+        sgn = -sgn
+        ms.append(_cuda_ms(lambda: ctx.step(sgn * DRIFT_DT, gp, None, graph=True), stream))
+    ctx.step_status()
     ctx.close()
     return {"profile": "box", "n_particles": len(m), "nBucket": NBUCKET,
-            "phase_ms": {k: statistics.mean(t[k] for t in ph)
-                         for k in ("build", "moments", "walk", "ewald", "total")}}
+            "ms_per_step": statistics.mean(ms)}
 
 
 def run_gas(args):
