@@ -569,8 +569,9 @@ def run_profile(args):
     stream = torch.cuda.Stream()
     ctx = g.Context(0, stream=stream.cuda_stream)
     # the knobs the timed run's autotuner picks for this box: the default
-    # five walk blocks per SM, no walk groups, the fused walk
-    ctx.set_tuning(walkGroup=-1)
+    # five walk blocks per SM, no walk groups, the fused walk (or the walk
+    # mode asked for)
+    ctx.set_tuning(walkGroup=-1, walkLists=args.walk_lists)
     pos, vel, m, soft = workload(args.ng, with_vel=True)
     ctx.set_particles(pos, m, soft)
     ctx.set_velocities(vel)
@@ -1034,6 +1035,8 @@ def main():
     ap.add_argument("--profile", action="store_true",
                     help="box FP32 evaluations only (the ncu capture command)")
     ap.add_argument("--sph-fp32", action="store_true")
+    ap.add_argument("--walk-lists", type=int, default=0,
+                    help="--profile: the walk mode (tsph_tuning.walkLists; 1 = two passes)")
     ap.add_argument("--collapse-n", type=int, default=262144)
     ap.add_argument("--collapse-steps", type=int, default=200)
     ap.add_argument("--collapse-dt", type=float, default=0.002)
