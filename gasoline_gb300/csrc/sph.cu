@@ -109,6 +109,7 @@ struct SphArgs {
     TsphDevState C;         // caller-order state (the inactive particles' dtNew, mumax)
     const int *list;        // density pass over these gas-tree indices only (or null: all)
     const int *nList;       // device count of list
+    int bucketGather = 0;   // density pass over all gas: one candidate gather per gas bucket
 };
 
 // The pressure pass acts on active particles (G.act); an inactive one
@@ -135,6 +136,7 @@ __device__ __forceinline__ void pressure_store(const SphArgs &A, int i, bool ai,
 #define SNBR 192      // neighbours summed in canonical (index) order
 #define KSTK 896      // ball-gather walk stack per warp (the size of the sum transpose)
 #define KB 16         // finished particles per lane-parallel epilogue
+#define BCAP 512      // candidates of one gas bucket's union ball (more: per particle)
 
 struct KnnSmem {
     union {
@@ -145,6 +147,7 @@ struct KnnSmem {
                                   // straddling candidate's exact FP64 d2 overlays it
     int idx[SCAP];                // candidate index (bit 31: exact value in lh)
     int nbr[SNBR];                // N(i), then sorted
+    int bc[BCAP];                 // a gas bucket's gathered candidates
 };
 
 // Finished particles of a warp awaiting the lane-parallel DenDVDX epilogue.
@@ -428,6 +431,176 @@ __device__ void density_epilogue(const SphArgs &A, KnnBatch &Bt, int cnt, int la
 // distance is bracketed from them, and only candidates whose interval
 // straddles the bracket get their FP64 distance.  The neighbour sums run
 // over N(i) in ascending index (FP64), so they depend on the set only.
+// Squared distance from a box to a box in FP32, each axis the nearest
+// periodic image, less the coordinate rounding margin of both boxes: never
+// more than the true distance.
+__device__ __forceinline__ float box_box_d2f(float4 alo, float4 ahi, float4 blo, float4 bhi) {
+    const float a0[3] = {alo.x, alo.y, alo.z}, a1[3] = {ahi.x, ahi.y, ahi.z};
+    const float b0[3] = {blo.x, blo.y, blo.z}, b1[3] = {bhi.x, bhi.y, bhi.z};
+    float d2 = 0.0f;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        float d = fmaxf(fmaxf(a0[q] - b1[q], b0[q] - a1[q]), 0.0f);
+        if (cS.bPeriodic) {
+            const float L = (float)cS.L;
+            const float dp = fmaxf(fmaxf(a0[q] - (b1[q] + L), (b0[q] + L) - a1[q]), 0.0f);
+            const float dm = fmaxf(fmaxf(a0[q] - (b1[q] - L), (b0[q] - L) - a1[q]), 0.0f);
+            d = fminf(d, fminf(dp, dm));
+        }
+        d = fmaxf(d - 2.0f * cS.margin, 0.0f);
+        d2 += d * d;
+    }
+    return d2;
+}
+
+// Every gas particle whose distance from the bucket box [blo, bhi] may be
+// within sqrt(R2) (the box test of ball_gather, made against a box): a
+// superset of the candidates ball_gather finds for any particle of the
+// bucket at any radius^2 up to R2.  Stored in W.bc in walk order; returns
+// their number, or -1 when they exceed BCAP or the stack overflows.
+__device__ int bucket_gather(KnnSmem &W, const SphArgs &A, int lane, int root, float4 blo, float4 bhi,
+                             float R2) {
+    const unsigned FULL = 0xffffffffu;
+    int sp = 1, nc = 0;
+    if (lane == 0) W.u.stack[0] = root;
+    __syncwarp();
+    bool bad = false;
+    while (sp > 0) {
+        const int take = sp < 32 ? sp : 32;
+        const int node = lane < take ? W.u.stack[sp - take + lane] : -1;
+        __syncwarp();
+        sp -= take;
+        bool open = false, leaf = false;
+        int4 lk = make_int4(0, 0, -1, 0);
+        if (node >= 0) {
+            lk = A.T.wlink[node];
+            if (box_box_d2f(A.T.wcomh[node], A.T.wcoml[node], blo, bhi) <= R2) {
+                if (lk.z >= 0) open = true;
+                else leaf = true;
+            }
+        }
+        const unsigned bo = __ballot_sync(FULL, open);
+        if (sp + 2 * __popc(bo) > KSTK) { bad = true; break; }
+        if (open) {
+            const int pos = sp + 2 * __popc(bo & lane_lt_s());
+            W.u.stack[pos] = lk.z;
+            W.u.stack[pos + 1] = node + 1;
+        }
+        sp += 2 * __popc(bo);
+        // the particles of this round's leaves, a lane per particle (leaf-lane
+        // major, particle minor, as ball_gather takes them)
+        const int cnt = leaf ? lk.y : 0;
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o) incl += y;
+        }
+        const int tot = __shfl_sync(FULL, incl, 31);
+        const int base = lk.x - (incl - cnt);
+        for (int t0 = 0; t0 < tot; t0 += 32) {
+            const int t = t0 + lane;
+            int own = 0;
+#pragma unroll
+            for (int st = 16; st > 0; st >>= 1) {
+                const int v = __shfl_sync(FULL, incl, own + st - 1);
+                if (v <= t) own += st;
+            }
+            const int j = __shfl_sync(FULL, base, own & 31) + t;
+            bool in = false;
+            if (t < tot) {
+                const float4 hj = A.G.ph[j];
+                in = box_d2f(hj.x, hj.y, hj.z, blo, bhi) <= R2;
+            }
+            const unsigned bi = __ballot_sync(FULL, in);
+            if (nc + __popc(bi) > BCAP) { bad = true; break; }
+            if (in) W.bc[nc + __popc(bi & lane_lt_s())] = j;
+            nc += __popc(bi);
+        }
+        __syncwarp();
+        if (bad) break;
+    }
+    __syncwarp();
+    return bad ? -1 : nc;
+}
+
+// ball_gather's result for particle i at radius^2 r2, taken from a bucket's
+// gathered list bc[0, nbc) (which holds every candidate at any r2 up to
+// the gather's radius): the same candidates in the list's order, their
+// intervals in W.lh, and the number surely inside in nSure; -1 when they
+// exceed SCAP.
+__device__ int bucket_filter(KnnSmem &W, const int *bc, int nbc, int lane, const SphArgs &A,
+                             float4 hi_i, float4 lo_i, float r2, int &nSure) {
+    const unsigned FULL = 0xffffffffu;
+    int nc = 0, ns = 0;
+    for (int e0 = 0; e0 < nbc; e0 += 32) {
+        const int e = e0 + lane;
+        float2 iv = make_float2(FLT_MAX, FLT_MAX);
+        int j = 0;
+        if (e < nbc) {
+            j = bc[e];
+            iv = d2_interval(hi_i, lo_i, A.G.ph[j], A.G.pl[j]);
+        }
+        const bool in = iv.x <= r2;
+        const unsigned bi = __ballot_sync(FULL, in);
+        ns += __popc(__ballot_sync(FULL, iv.y <= r2));
+        if (nc + __popc(bi) > SCAP) {
+            __syncwarp();
+            return -1;
+        }
+        if (in) {
+            const int pos = nc + __popc(bi & lane_lt_s());
+            W.lh[pos] = iv;
+            W.idx[pos] = j;
+        }
+        nc += __popc(bi);
+    }
+    __syncwarp();
+    nSure = ns;
+    return nc;
+}
+
+// Particle i's starting kNN radius^2: the learned seed when there is one,
+// else from the smallest tree node around i that holds k particles (any
+// positive value works: a short ball grows, a large one shrinks; the seed
+// only sets the cost).
+__device__ __forceinline__ float seed_r2(const SphArgs &A, int i, int k) {
+    const float4 hi_i = A.G.ph[i];
+    const float xf = hi_i.x, yf = hi_i.y, zf = hi_i.z;
+    const int root = A.T.sysRoot[A.G.rid[i]];
+    float r2;
+    if (A.seed && A.seed[i] > 0.0) {
+        r2 = (float)A.seed[i];
+    } else {
+        int node = root;
+        for (;;) {
+            int up = A.T.upper[node];
+            if (up < 0) break;
+            int child = (i >= A.T.pLower[up]) ? up : node + 1;
+            if (A.T.pUpper[child] - A.T.pLower[child] + 1 < k) break;
+            node = child;
+        }
+        // farthest box corner (surely k particles), or the radius holding
+        // twice the volume k particles need at the node's mean density
+        const float4 bl = A.T.wcomh[node], bh = A.T.wcoml[node];
+        const float p[3] = {xf, yf, zf}, a[3] = {bl.x, bl.y, bl.z}, c[3] = {bh.x, bh.y, bh.z};
+        float rc = 0.0f, vol = 1.0f;
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            float d = fmaxf(fabsf(p[q] - a[q]), fabsf(p[q] - c[q]));
+            rc += d * d;
+            vol *= c[q] - a[q];
+        }
+        r2 = rc * 1.0001f + 1e-30f;
+        const int nNode = A.T.pUpper[node] - A.T.pLower[node] + 1;
+        if (vol > 0.0f) {
+            float rd = cbrtf(2.0f * 3.0f * k * vol / (4.0f * 3.14159265f * nNode));
+            if (rd * rd < r2) r2 = rd * rd;
+        }
+    }
+    return r2;
+}
+
 template <bool F32>
 __global__ void __launch_bounds__(SW * 32, 5) k_knn_density(SphArgs A) {
     extern __shared__ __align__(16) unsigned char smraw[];
@@ -438,56 +611,19 @@ __global__ void __launch_bounds__(SW * 32, 5) k_knn_density(SphArgs A) {
     const int ng = cS.ngas, k = cS.k;
     unsigned long long nFall = 0, nPairs = 0, nCand = 0;
     int nb = 0;                              // particles waiting in the batch
-    for (;;) {
-        int i = 0;
-        if (lane == 0) i = atomicAdd(A.work, 1);
-        i = __shfl_sync(FULL, i, 0);
-        if (A.list) {
-            if (i >= *A.nList) break;
-            i = A.list[i];
-        } else if (i >= ng) {
-            break;
-        }
+    // Particle i's kNN and DenDVDX sums, its search starting at radius^2 r2.
+    // With bc non-null the candidates of any ball of radius^2 <= bcR2
+    // around i come from the bucket's gathered list bc[0, nbc).
+    auto one = [&](int i, float r2, const int *bc, int nbc, float bcR2) {
         const double xi = A.G.x[i], yi = A.G.y[i], zi = A.G.z[i];
         const float4 hi_i = A.G.ph[i], lo_i = A.G.pl[i];
         const float xf = hi_i.x, yf = hi_i.y, zf = hi_i.z;
         const int root = A.T.sysRoot[A.G.rid[i]];   // this particle's system
-        // seed radius (any positive value works: a short ball grows, a large
-        // one shrinks; the seed only sets the cost)
-        float r2;
-        if (A.seed && A.seed[i] > 0.0) {
-            r2 = (float)A.seed[i];
-        } else {
-            int node = root;
-            for (;;) {
-                int up = A.T.upper[node];
-                if (up < 0) break;
-                int child = (i >= A.T.pLower[up]) ? up : node + 1;
-                if (A.T.pUpper[child] - A.T.pLower[child] + 1 < k) break;
-                node = child;
-            }
-            // farthest box corner (surely k particles), or the radius holding
-            // twice the volume k particles need at the node's mean density
-            const float4 bl = A.T.wcomh[node], bh = A.T.wcoml[node];
-            const float p[3] = {xf, yf, zf}, a[3] = {bl.x, bl.y, bl.z}, c[3] = {bh.x, bh.y, bh.z};
-            float rc = 0.0f, vol = 1.0f;
-#pragma unroll
-            for (int q = 0; q < 3; ++q) {
-                float d = fmaxf(fabsf(p[q] - a[q]), fabsf(p[q] - c[q]));
-                rc += d * d;
-                vol *= c[q] - a[q];
-            }
-            r2 = rc * 1.0001f + 1e-30f;
-            const int nNode = A.T.pUpper[node] - A.T.pLower[node] + 1;
-            if (vol > 0.0f) {
-                float rd = cbrtf(2.0f * 3.0f * k * vol / (4.0f * 3.14159265f * nNode));
-                if (rd * rd < r2) r2 = rd * rd;
-            }
-        }
         float lo2 = 0.0f, hi2 = 0.0f;   // radii known too small / too large
         int nc = -1, nSure = 0, it = 0;
         for (; it < SMAXIT; ++it) {
-            nc = ball_gather(W, A, lane, root, xf, yf, zf, hi_i, lo_i, r2, nSure);
+            nc = (bc && r2 <= bcR2) ? bucket_filter(W, bc, nbc, lane, A, hi_i, lo_i, r2, nSure)
+                                    : ball_gather(W, A, lane, root, xf, yf, zf, hi_i, lo_i, r2, nSure);
             if (nc < 0) {                       // too many candidates: shrink
                 hi2 = r2;
                 r2 = lo2 > 0.0f ? sqrtf(lo2 * hi2) : 0.5f * r2;
@@ -502,7 +638,7 @@ __global__ void __launch_bounds__(SW * 32, 5) k_knn_density(SphArgs A) {
         }
         if (it == SMAXIT) {
             if (lane == 0) atomicOr(&A.cnt->status, 1u << TSPH_ERR_KNN_NO_CONVERGE);
-            continue;
+            return;
         }
         nCand += nc;
         // bracket the k-th distance: Tlo <= fBall2 <= Thi (a register sort
@@ -594,7 +730,7 @@ __global__ void __launch_bounds__(SW * 32, 5) k_knn_density(SphArgs A) {
         __syncwarp();
         if (nsel > SNBR) {                   // more than SNBR exact ties
             if (lane == 0) atomicOr(&A.cnt->status, 1u << TSPH_ERR_LIST_OVERFLOW);
-            continue;
+            return;
         }
         warp_sort_idx(W.nbr, nsel, lane);
         if (nsel <= A.S.nbrCap) {
@@ -717,6 +853,39 @@ __global__ void __launch_bounds__(SW * 32, 5) k_knn_density(SphArgs A) {
         if (nb == KB) {
             density_epilogue(A, Bt, nb, lane);
             nb = 0;
+        }
+    };
+    for (;;) {
+        int u = 0;
+        if (lane == 0) u = atomicAdd(A.work, 1);
+        u = __shfl_sync(FULL, u, 0);
+        if (A.list) {
+            if (u >= *A.nList) break;
+            const int i = A.list[u];
+            one(i, seed_r2(A, i, k), nullptr, 0, 0.0f);
+        } else if (A.bucketGather) {
+            // a gas bucket: one tree walk gathers every candidate of its
+            // particles' balls (the largest seed around the bucket's box),
+            // then each particle takes its own from that list
+            if (u >= A.T.dcnt[1]) break;
+            const int node = A.T.leaves[u];
+            const int lo = A.T.pLower[node], n = A.T.pUpper[node] - lo + 1;
+            float r2 = lane < n ? seed_r2(A, lo + lane, k) : 0.0f;
+            float R2 = r2;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) R2 = fmaxf(R2, __shfl_xor_sync(FULL, R2, o));
+            const int root = A.T.sysRoot[A.G.rid[lo]];
+            const int nbc = bucket_gather(W, A, lane, root, A.T.wcomh[node], A.T.wcoml[node],
+                                          R2 * 1.001f);
+            for (int t = 0; t < n; ++t) {
+                const float r2t = __shfl_sync(FULL, r2, t);
+                if (nbc >= 0) one(lo + t, r2t, W.bc, nbc, R2);
+                else one(lo + t, r2t, nullptr, 0, 0.0f);
+                __syncwarp();
+            }
+        } else {
+            if (u >= ng) break;
+            one(u, seed_r2(A, u, k), nullptr, 0, 0.0f);
         }
         __syncwarp();
     }
@@ -1585,6 +1754,7 @@ static int run_density(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_out
         rc = run_density_subset(ctx, sp, A, na);
     } else {
         TSPH_CK(cudaMemsetAsync(S.need, 0x01, sizeof(int) * ng, ctx->stream));   // every particle
+        A.bucketGather = 1;
         rc = launch_knn(ctx, sp, A);
     }
     if (rc) return rc;
