@@ -105,7 +105,7 @@ extern "C" void tsph_destroy(tsph_ctx *ctx) {
     FREE(S.seed); FREE(S.nnCount); FREE(S.nnHash); FREE(S.nodeBall2);
     FREE(S.nbrList); FREE(S.rcnt); FREE(S.roff); FREE(S.rcur); FREE(S.rlist); FREE(S.listFlag);
     FREE(S.ph); FREE(S.ih2); FREE(S.fn1); FREE(S.pr2f); FREE(S.pfa); FREE(S.pfb); FREE(S.pfc);
-    FREE(S.need); FREE(S.list); FREE(S.list2); FREE(S.listN); FREE(S.rb2);
+    FREE(S.need); FREE(S.list); FREE(S.list2); FREE(S.listN); FREE(S.rb2); FREE(S.vh); FREE(S.vl);
     FREE(ctx->dCnt); FREE(ctx->dBucketLists); FREE(ctx->dRoot); FREE(ctx->dEw); FREE(ctx->dStage);
     FREE(ctx->dAux); FREE(ctx->dStepStatus);
     FREE(ctx->dGroupFlag); FREE(ctx->dGroupScan); FREE(ctx->dGroupFirst); FREE(ctx->dGroupCount);
@@ -168,6 +168,7 @@ int tsph_ensure_particles(tsph_ctx *ctx, int n) {
     rc |= tsph_grow(ctx, &S.ph, cap); rc |= tsph_grow(ctx, &S.ih2, cap);
     rc |= tsph_grow(ctx, &S.fn1, cap); rc |= tsph_grow(ctx, &S.pr2f, cap);
     rc |= tsph_grow(ctx, &S.pfa, cap); rc |= tsph_grow(ctx, &S.pfb, cap); rc |= tsph_grow(ctx, &S.pfc, cap);
+    rc |= tsph_grow(ctx, &S.vh, cap); rc |= tsph_grow(ctx, &S.vl, cap);
     rc |= tsph_grow(ctx, &S.need, cap); rc |= tsph_grow(ctx, &S.list, cap);
     rc |= tsph_grow(ctx, &S.list2, cap); rc |= tsph_grow(ctx, &S.listN, 4);
     rc |= tsph_grow(ctx, &S.rb2, cap);

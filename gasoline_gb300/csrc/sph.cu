@@ -109,7 +109,7 @@ struct SphArgs {
     TsphDevState C;         // caller-order state (the inactive particles' dtNew, mumax)
     const int *list;        // density pass over these gas-tree indices only (or null: all)
     const int *nList;       // device count of list
-    int bucketGather = 0;   // density pass over all gas: one candidate gather per gas bucket
+    int bucketGather = 0;   // seeded pass over all gas: one candidate gather per gas bucket
 };
 
 // The pressure pass acts on active particles (G.act); an inactive one
@@ -147,7 +147,6 @@ struct KnnSmem {
                                   // straddling candidate's exact FP64 d2 overlays it
     int idx[SCAP];                // candidate index (bit 31: exact value in lh)
     int nbr[SNBR];                // N(i), then sorted
-    int bc[BCAP];                 // a gas bucket's gathered candidates
 };
 
 // Finished particles of a warp awaiting the lane-parallel DenDVDX epilogue.
@@ -199,6 +198,15 @@ __device__ __forceinline__ void kern_dkern_m4(double ar2, double &w, double &dw)
 // hi/lo split coordinates: |dx_true - dx32| <= erel |dx32| + eabs per axis.
 // A periodic separation close to half the box (where the FP32 and FP64
 // image choices could differ) gets the whole range.
+// Velocity difference p - q from the FP32 hi/lo parts (no FP64 arithmetic).
+__device__ __forceinline__ void split_dv(const TsphSphBufs &S, int p, int q, float &dvx, float &dvy,
+                                         float &dvz) {
+    const float4 hp = S.vh[p], lp = S.vl[p], hq = S.vh[q], lq = S.vl[q];
+    dvx = (hp.x - hq.x) + (lp.x - lq.x);
+    dvy = (hp.y - hq.y) + (lp.y - lq.y);
+    dvz = (hp.z - hq.z) + (lp.z - lq.z);
+}
+
 __device__ __forceinline__ float2 d2_interval(float4 hi_i, float4 lo_i, float4 hj, float4 lj) {
     const float u = 5.9604645e-08f;
     float d[3] = {(hj.x - hi_i.x) + (lj.x - lo_i.x), (hj.y - hi_i.y) + (lj.y - lo_i.y),
@@ -456,10 +464,10 @@ __device__ __forceinline__ float box_box_d2f(float4 alo, float4 ahi, float4 blo,
 // Every gas particle whose distance from the bucket box [blo, bhi] may be
 // within sqrt(R2) (the box test of ball_gather, made against a box): a
 // superset of the candidates ball_gather finds for any particle of the
-// bucket at any radius^2 up to R2.  Stored in W.bc in walk order; returns
+// bucket at any radius^2 up to R2.  Stored in bc in walk order; returns
 // their number, or -1 when they exceed BCAP or the stack overflows.
-__device__ int bucket_gather(KnnSmem &W, const SphArgs &A, int lane, int root, float4 blo, float4 bhi,
-                             float R2) {
+__device__ int bucket_gather(KnnSmem &W, int *bc, const SphArgs &A, int lane, int root, float4 blo,
+                             float4 bhi, float R2) {
     const unsigned FULL = 0xffffffffu;
     int sp = 1, nc = 0;
     if (lane == 0) W.u.stack[0] = root;
@@ -514,7 +522,7 @@ __device__ int bucket_gather(KnnSmem &W, const SphArgs &A, int lane, int root, f
             }
             const unsigned bi = __ballot_sync(FULL, in);
             if (nc + __popc(bi) > BCAP) { bad = true; break; }
-            if (in) W.bc[nc + __popc(bi & lane_lt_s())] = j;
+            if (in) bc[nc + __popc(bi & lane_lt_s())] = j;
             nc += __popc(bi);
         }
         __syncwarp();
@@ -606,6 +614,10 @@ __global__ void __launch_bounds__(SW * 32, 5) k_knn_density(SphArgs A) {
     extern __shared__ __align__(16) unsigned char smraw[];
     KnnSmem &W = reinterpret_cast<KnnSmem *>(smraw)[threadIdx.x >> 5];
     KnnBatch &Bt = reinterpret_cast<KnnBatch *>(smraw + sizeof(KnnSmem) * SW)[threadIdx.x >> 5];
+    // a bucket launch's candidate lists follow the batches (the other
+    // launches do not allocate them: their occupancy stays a block higher)
+    int *bcw = reinterpret_cast<int *>(smraw + (sizeof(KnnSmem) + sizeof(KnnBatch)) * SW) +
+               (threadIdx.x >> 5) * BCAP;
     const int lane = threadIdx.x & 31;
     const unsigned FULL = 0xffffffffu;
     const int ng = cS.ngas, k = cS.k;
@@ -787,9 +799,9 @@ __global__ void __launch_bounds__(SW * 32, 5) k_knn_density(SphArgs A) {
                 Bt.s[lane][nb] = t;
             }
         } else {
-            // FP32 neighbour terms on split relative coordinates; FP64 only
-            // for the velocity differences (a bulk flow would otherwise
-            // swamp them); a fixed-order FP32 warp sum, widened for the
+            // FP32 neighbour terms on split relative coordinates and split
+            // velocities (the hi/lo differences keep a bulk flow from
+            // swamping them); a fixed-order FP32 warp sum, widened for the
             // FP64 epilogue
             const float ih2f = (float)ih2;
             float sm[14];
@@ -821,8 +833,8 @@ __global__ void __launch_bounds__(SW * 32, 5) k_knn_density(SphArgs A) {
                 const float mj = hj.w;
                 sm[0] += rs * mj;
                 rs1 *= mj;
-                const float dvx = (float)(A.S.vx[j] - vxi), dvy = (float)(A.S.vy[j] - vyi),
-                            dvz = (float)(A.S.vz[j] - vzi);
+                float dvx, dvy, dvz;
+                split_dv(A.S, j, i, dvx, dvy, dvz);
                 sm[1] += dvx * dx * rs1; sm[2] += dvx * dy * rs1; sm[3] += dvx * dz * rs1;
                 sm[4] += dvy * dx * rs1; sm[5] += dvy * dy * rs1; sm[6] += dvy * dz * rs1;
                 sm[7] += dvz * dx * rs1; sm[8] += dvz * dy * rs1; sm[9] += dvz * dz * rs1;
@@ -855,38 +867,47 @@ __global__ void __launch_bounds__(SW * 32, 5) k_knn_density(SphArgs A) {
             nb = 0;
         }
     };
+    // the work: particles from the list, or (a pass over all gas) gas
+    // buckets, each gathered once when that pays, or single particles; one
+    // call site for the per-particle work keeps the kernel's code compact
+    int curLo = 0, curN = 0, curT = 0, nbc = -1;
+    float r2l = 0.0f, R2 = 0.0f;
     for (;;) {
-        int u = 0;
-        if (lane == 0) u = atomicAdd(A.work, 1);
-        u = __shfl_sync(FULL, u, 0);
-        if (A.list) {
-            if (u >= *A.nList) break;
-            const int i = A.list[u];
-            one(i, seed_r2(A, i, k), nullptr, 0, 0.0f);
-        } else if (A.bucketGather) {
-            // a gas bucket: one tree walk gathers every candidate of its
-            // particles' balls (the largest seed around the bucket's box),
-            // then each particle takes its own from that list
-            if (u >= A.T.dcnt[1]) break;
-            const int node = A.T.leaves[u];
-            const int lo = A.T.pLower[node], n = A.T.pUpper[node] - lo + 1;
-            float r2 = lane < n ? seed_r2(A, lo + lane, k) : 0.0f;
-            float R2 = r2;
+        if (curT >= curN) {
+            int u = 0;
+            if (lane == 0) u = atomicAdd(A.work, 1);
+            u = __shfl_sync(FULL, u, 0);
+            curT = 0;
+            nbc = -1;
+            if (A.list) {
+                if (u >= *A.nList) break;
+                curLo = A.list[u];
+                curN = 1;
+                r2l = seed_r2(A, curLo, k);
+            } else if (A.bucketGather) {
+                // a gas bucket: one tree walk gathers every candidate of its
+                // particles' balls (the largest seed around the bucket's
+                // box), then each particle takes its own from that list
+                if (u >= A.T.dcnt[1]) break;
+                const int node = A.T.leaves[u];
+                curLo = A.T.pLower[node];
+                curN = A.T.pUpper[node] - curLo + 1;
+                r2l = lane < curN ? seed_r2(A, curLo + lane, k) : 0.0f;
+                R2 = r2l;
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) R2 = fmaxf(R2, __shfl_xor_sync(FULL, R2, o));
-            const int root = A.T.sysRoot[A.G.rid[lo]];
-            const int nbc = bucket_gather(W, A, lane, root, A.T.wcomh[node], A.T.wcoml[node],
-                                          R2 * 1.001f);
-            for (int t = 0; t < n; ++t) {
-                const float r2t = __shfl_sync(FULL, r2, t);
-                if (nbc >= 0) one(lo + t, r2t, W.bc, nbc, R2);
-                else one(lo + t, r2t, nullptr, 0, 0.0f);
-                __syncwarp();
+                for (int o = 16; o > 0; o >>= 1) R2 = fmaxf(R2, __shfl_xor_sync(FULL, R2, o));
+                nbc = bucket_gather(W, bcw, A, lane, A.T.sysRoot[A.G.rid[curLo]], A.T.wcomh[node],
+                                    A.T.wcoml[node], R2 * 1.001f);
+            } else {
+                if (u >= ng) break;
+                curLo = u;
+                curN = 1;
+                r2l = seed_r2(A, u, k);
             }
-        } else {
-            if (u >= ng) break;
-            one(u, seed_r2(A, u, k), nullptr, 0, 0.0f);
         }
+        const int t = curT++;
+        const float r2t = A.bucketGather && !A.list ? __shfl_sync(FULL, r2l, t) : r2l;
+        one(curLo + t, r2t, nbc >= 0 ? bcw : nullptr, nbc, R2);
         __syncwarp();
     }
     if (nb > 0) density_epilogue(A, Bt, nb, lane);
@@ -1095,8 +1116,8 @@ __device__ __forceinline__ void sph_pair_f(const TsphSphBufs &S, const TsphDevPa
     const float dk = r2 < 1.0f ? -3.0f + 2.25f * r : -0.75f * (2.0f - r) * (2.0f - r) / r;
     const float rs1 = dk * ap.z;
     const float rp = rs1 * G.ph[p].w, rq = rs1 * G.ph[q].w;
-    const float dvx = (float)(S.vx[p] - S.vx[q]), dvy = (float)(S.vy[p] - S.vy[q]),
-                dvz = (float)(S.vz[p] - S.vz[q]);
+    float dvx, dvy, dvz;
+    split_dv(S, p, q, dvx, dvy, dvz);
     const float dvdotdr = dvx * dx + dvy * dy + dvz * dz;
     float Acc, dt;
     if (own) {
@@ -1498,9 +1519,19 @@ __global__ void k_gas_gather_vel(int ng, TsphDevState C, const int *__restrict__
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= ng) return;
     int o = iord[i];
-    S.vx[i] = C.vpx[o]; S.vy[i] = C.vpy[o]; S.vz[i] = C.vpz[o];
+    const double vx = C.vpx[o], vy = C.vpy[o], vz = C.vpz[o];
+    S.vx[i] = vx; S.vy[i] = vy; S.vz[i] = vz;
     S.u[i] = C.upred[o];
+    // FP32 hi/lo parts: (hj - hi) + (lj - li) is the velocity difference to
+    // FP32 rounding however large a bulk flow both share
+    float hx, lx, hy, ly, hz, lz;
+    split2f(vx, hx, lx);
+    split2f(vy, hy, ly);
+    split2f(vz, hz, lz);
+    S.vh[i] = make_float4(hx, hy, hz, 0.0f);
+    S.vl[i] = make_float4(lx, ly, lz, 0.0f);
 }
+
 
 // FP32 node boxes for the gas walks (stored in wcomh/wcoml of the gas tree)
 __global__ void k_gas_nodes(TsphDevTree T) {
@@ -1637,17 +1668,20 @@ int tsph_load_gas(tsph_ctx *ctx, int ngas) {
 
 static int launch_knn(tsph_ctx *ctx, const tsph_sph_params *sp, const SphArgs &A) {
     const bool cap = ctx->capturing;
-    size_t sm = (sizeof(KnnSmem) + sizeof(KnnBatch)) * SW;
+    // the buckets' candidate lists only in a bucket launch; the attribute
+    // allows the larger size for every launch (a capture sets none)
+    const size_t smMax = (sizeof(KnnSmem) + sizeof(KnnBatch) + sizeof(int) * BCAP) * SW;
+    const size_t sm = A.bucketGather ? smMax : (sizeof(KnnSmem) + sizeof(KnnBatch)) * SW;
     if (sp->precision == TSPH_FP32) {
         if (!cap)
             TSPH_CK(cudaFuncSetAttribute(k_knn_density<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)sm));
+                                         (int)smMax));
         k_knn_density<true><<<ctx->smCount * 6, SW * 32, sm, ctx->stream>>>(A);
         TSPH_LAUNCH_CK("k_knn_density<f32>");
     } else {
         if (!cap)
             TSPH_CK(cudaFuncSetAttribute(k_knn_density<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)sm));
+                                         (int)smMax));
         k_knn_density<false><<<ctx->smCount * 6, SW * 32, sm, ctx->stream>>>(A);
         TSPH_LAUNCH_CK("k_knn_density<f64>");
     }
@@ -1754,7 +1788,11 @@ static int run_density(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_out
         rc = run_density_subset(ctx, sp, A, na);
     } else {
         TSPH_CK(cudaMemsetAsync(S.need, 0x01, sizeof(int) * ng, ctx->stream));   // every particle
-        A.bucketGather = 1;
+        // one gather per gas bucket pays with the h-network's tight seeds;
+        // with the tree's coarse ones the buckets' union balls grow too large
+        // (measured: 1/r collapse 2.01 -> 1.77 ms with learned seeds; 128
+        // Plummer/Hernquist systems 3.70 -> 5.36 ms with tree seeds)
+        A.bucketGather = A.seed != nullptr;
         rc = launch_knn(ctx, sp, A);
     }
     if (rc) return rc;

@@ -50,6 +50,7 @@ struct TsphBuildBufs {
 struct TsphSphBufs {
     int cap;
     double *vx, *vy, *vz, *u;    // vPred, uPred gathered from the state
+    float4 *vh, *vl;             // vPred split into FP32 hi and lo parts (FP32 passes)
     double *fBall2, *rho, *divv, *curl, *dvds, *bal, *diff, *pr2, *cs, *dtp;
     double *hax, *hay, *haz, *uPdV, *uAV, *dtNew, *mumax;
     double *seed;                // optional fBall2 seed per particle (learned h)
