@@ -39,6 +39,7 @@ struct SphConst {
     int limiter;
     float margin;     // absolute slack for FP32 box-distance pruning
     float erel, eabs; // FP32 relative-coordinate error bound: erel |dx| + eabs
+    float Lf, alphaf, betaf, dtFacCourantf;   // FP32 copies for the FP32 kernels
 };
 __constant__ SphConst cS;
 
@@ -75,7 +76,7 @@ __device__ __forceinline__ float box_d2f(float x, float y, float z, float4 lo, f
     for (int k = 0; k < 3; ++k) {
         float d = fmaxf(fmaxf(a[k] - p[k], p[k] - b[k]), 0.0f);
         if (cS.bPeriodic) {
-            float L = (float)cS.L;
+            float L = cS.Lf;
             float d1 = fmaxf(fmaxf(a[k] - (p[k] + L), (p[k] + L) - b[k]), 0.0f);
             float d2b = fmaxf(fmaxf(a[k] - (p[k] - L), (p[k] - L) - b[k]), 0.0f);
             d = fminf(d, fminf(d1, d2b));
@@ -217,7 +218,7 @@ __device__ __forceinline__ float2 d2_interval(float4 hi_i, float4 lo_i, float4 h
     for (int a = 0; a < 3; ++a) {
         float ad = fabsf(d[a]);
         if (cS.bPeriodic) {
-            const float L = (float)cS.L;
+            const float L = cS.Lf;
             if (ad > 0.5f * L) ad = L - ad;
             if (fabsf(ad - 0.5f * L) < 1e-4f * L) wide = true;
         }
@@ -450,7 +451,7 @@ __device__ __forceinline__ float box_box_d2f(float4 alo, float4 ahi, float4 blo,
     for (int q = 0; q < 3; ++q) {
         float d = fmaxf(fmaxf(a0[q] - b1[q], b0[q] - a1[q]), 0.0f);
         if (cS.bPeriodic) {
-            const float L = (float)cS.L;
+            const float L = cS.Lf;
             const float dp = fmaxf(fmaxf(a0[q] - (b1[q] + L), (b0[q] + L) - a1[q]), 0.0f);
             const float dm = fmaxf(fmaxf(a0[q] - (b1[q] - L), (b0[q] - L) - a1[q]), 0.0f);
             d = fminf(d, fminf(dp, dm));
@@ -814,7 +815,7 @@ __global__ void __launch_bounds__(SW * 32, 5) k_knn_density(SphArgs A) {
                 float dy = (hi_i.y - hj.y) + (lo_i.y - lj.y);
                 float dz = (hi_i.z - hj.z) + (lo_i.z - lj.z);
                 if (cS.bPeriodic) {
-                    const float L = (float)cS.L, h = 0.5f * L;
+                    const float L = cS.Lf, h = 0.5f * L;
                     dx = dx > h ? dx - L : (dx < -h ? dx + L : dx);
                     dy = dy > h ? dy - L : (dy < -h ? dy + L : dy);
                     dz = dz > h ? dz - L : (dz < -h ? dz + L : dz);
@@ -1127,13 +1128,13 @@ __device__ __forceinline__ void sph_pair_f(const TsphSphBufs &S, const TsphDevPa
         uPdV += rp * S.pfc[q].x * dvdotdr;
         Acc = aq.w + ap.w;
     }
-    const float fac = (float)cS.dtFacCourant;
+    const float fac = cS.dtFacCourantf;
     if (dvdotdr >= 0.0f) {
         dt = fac * ph / (2 * fmaxf(pc, qc));
     } else {
         float absmu = -dvdotdr / sqrtf(fDist2);
         if (absmu > mu) mu = absmu;
-        float visc = ((float)cS.alpha * (pc + qc) + (float)cS.beta * 1.5f * absmu);
+        float visc = (cS.alphaf * (pc + qc) + cS.betaf * 1.5f * absmu);
         dt = fac * ph / (0.625f * (pc + qc) + 0.375f * visc);
         visc = (0.5f * (bp.z + bq.z)) * visc * absmu / (bp.y + bq.y);
         uAV += (own ? rq : rp) * (0.5f * visc) * dvdotdr;
@@ -1156,7 +1157,7 @@ __device__ __forceinline__ void split_dx(float4 hi, float4 lo, float4 hj, float4
     dy = (hi.y - hj.y) + (lo.y - lj.y);
     dz = (hi.z - hj.z) + (lo.z - lj.z);
     if (cS.bPeriodic) {
-        const float L = (float)cS.L, h = 0.5f * L;
+        const float L = cS.Lf, h = 0.5f * L;
         dx = dx > h ? dx - L : (dx < -h ? dx + L : dx);
         dy = dy > h ? dy - L : (dy < -h ? dy + L : dy);
         dz = dz > h ? dz - L : (dz < -h ? dz + L : dz);
@@ -1600,6 +1601,10 @@ static void set_sph_const(tsph_ctx *ctx, const tsph_sph_params *sp) {
     c.gamma = sp->gamma;
     c.gammam1 = sp->gamma - 1;
     c.dtFacCourant = sp->dEtaCourant * 1.0 * 2 / 1.6;   // pkdDtFacCourant, a = 1
+    c.Lf = (float)c.L;
+    c.alphaf = (float)c.alpha;
+    c.betaf = (float)c.beta;
+    c.dtFacCourantf = (float)c.dtFacCourant;
     c.limiter = sp->iViscosityLimiter;
     // FP32 box tests: pad by a few ulps of the largest |coordinate| (of all
     // systems), measured by k_gas_maxabs
