@@ -668,6 +668,10 @@ extern "C" int tsph_set_tuning(tsph_ctx *ctx, const tsph_tuning *t) {
         return TSPH_ERR_ARG;
     if (t->walkLists < -1 || (t->walkLists > 1 && (t->walkLists < 32 || t->walkLists > 65536)))
         return TSPH_ERR_ARG;
+    // a captured step keeps the knobs it was captured with: a change recaptures
+    if (t->taskSize != ctx->taskSize || t->walkBlocksPerSM != ctx->walkBlocksPerSM ||
+        t->walkGroup != ctx->walkGroup || t->walkLists != ctx->walkLists)
+        ctx->sysVersion++;
     ctx->taskSize = t->taskSize;
     ctx->walkBlocksPerSM = t->walkBlocksPerSM;
     ctx->walkGroup = t->walkGroup;
