@@ -169,14 +169,33 @@ __global__ void k_roots(int nR, const int *__restrict__ rLo, const int *__restri
 // Top-phase kernels run over Fb >= F frontier slots (a host-side bound);
 // the frontier size F of level L lives on the device (ctl->levF[L]), so the
 // host launches levels without waiting for each one.
-__global__ void k_chunk_count(int Fb, int L, const TsphBuildCtl *__restrict__ ctl,
+// Chunks of frontier node v: none for a node of at most S particles (it
+// becomes a subtree task, which finds its own bounds).
+__device__ __forceinline__ int node_chunks(int size, int S) {
+    return size > S ? (size + TB_CHUNK - 1) / TB_CHUNK : 0;
+}
+
+__global__ void k_chunk_count(int Fb, int L, int S, const TsphBuildCtl *__restrict__ ctl,
                               const int *__restrict__ f_node, const int *__restrict__ t_lo,
                               const int *__restrict__ t_hi, int *cc) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= Fb) return;
     if (k >= ctl->levF[L]) { cc[k] = 0; return; }
     int v = f_node[k];
-    cc[k] = (t_hi[v] - t_lo[v] + TB_CHUNK) / TB_CHUNK;
+    cc[k] = node_chunks(t_hi[v] - t_lo[v] + 1, S);
+}
+
+// The frontier index of every chunk (cs = inclusive scan of the chunk
+// counts), so that a chunk's block finds its node with one load.
+__global__ void k_chunk_map(int Fb, const int *__restrict__ cs, int *chunkNode) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= cs[Fb - 1]) return;
+    int a = 0, e = Fb - 1;   // first k with cs[k] > c
+    while (a < e) {
+        int m = (a + e) >> 1;
+        if (cs[m] > c) e = m; else a = m + 1;
+    }
+    chunkNode[c] = a;
 }
 
 __device__ __forceinline__ unsigned long long umin64(unsigned long long a, unsigned long long b) {
@@ -188,6 +207,7 @@ __device__ __forceinline__ unsigned long long umax64(unsigned long long a, unsig
 
 __global__ void __launch_bounds__(TB_BS) k_bounds_chunks(int F, const int *__restrict__ f_node,
                                                          const int *__restrict__ cs,
+                                                         const int *__restrict__ chunkNode,
                                                          const int *__restrict__ t_lo,
                                                          const int *__restrict__ t_hi,
                                                          const double *__restrict__ x,
@@ -196,11 +216,7 @@ __global__ void __launch_bounds__(TB_BS) k_bounds_chunks(int F, const int *__res
     __shared__ unsigned long long red[TB_BS / 32][6];
     const int b = blockIdx.x;
     if (b >= cs[F - 1]) return;          // F here is the slot bound; unused slots count 0
-    int a = 0, e = F - 1;                  // first k with cs[k] > b
-    while (a < e) {
-        int c = (a + e) >> 1;
-        if (cs[c] > b) e = c; else a = c + 1;
-    }
+    const int a = chunkNode[b];
     const int v = f_node[a];
     const int j = b - (a > 0 ? cs[a - 1] : 0);
     const int p0 = t_lo[v] + j * TB_CHUNK;
@@ -313,23 +329,13 @@ __device__ __forceinline__ void swap_particles(double *x, double *y, double *z, 
     int ti = iord[p]; iord[p] = iord[q]; iord[q] = ti;
 }
 
-// Frontier node of chunk b: the first k with cs[k] > b (cs = inclusive
-// scan of the per-node chunk counts).
-__device__ __forceinline__ int chunk_node(const int *__restrict__ cs, int Fb, int b) {
-    int a = 0, e = Fb - 1;
-    while (a < e) {
-        int c = (a + e) >> 1;
-        if (cs[c] > b) e = c; else a = c + 1;
-    }
-    return a;
-}
-
 // Partition flags (r[d] < fSplit) of one chunk of a split frontier node and
 // their in-chunk inclusive scan; ctot[b] = the chunk's count.  Warps take
 // contiguous runs and count with ballots; two passes over the chunk.
 __global__ void __launch_bounds__(TB_BS) k_flag_chunks(int Fb, int nChunkSlots,
                                                        const int *__restrict__ f_node,
                                                        const int *__restrict__ cs,
+                                                       const int *__restrict__ chunkNode,
                                                        const int *__restrict__ t_lo,
                                                        const int *__restrict__ t_hi,
                                                        const int *__restrict__ t_dim,
@@ -345,7 +351,7 @@ __global__ void __launch_bounds__(TB_BS) k_flag_chunks(int Fb, int nChunkSlots,
         if (threadIdx.x == 0) ctot[b] = 0;
         return;
     }
-    const int k = chunk_node(cs, Fb, b);
+    const int k = chunkNode[b];
     const int v = f_node[k];
     const int d = t_dim[v];
     if (d < 0) {                          // a task or a leaf: nothing moves
@@ -397,6 +403,7 @@ __device__ __forceinline__ int node_scan(const int *__restrict__ scan, const int
 // and mR), k_pair_chunks swaps list entry t of each.
 __global__ void __launch_bounds__(TB_BS) k_mark_chunks(int Fb, const int *__restrict__ f_node,
                                                        const int *__restrict__ cs,
+                                                       const int *__restrict__ chunkNode,
                                                        const int *__restrict__ coff,
                                                        const int *__restrict__ t_lo,
                                                        const int *__restrict__ t_hi,
@@ -405,7 +412,7 @@ __global__ void __launch_bounds__(TB_BS) k_mark_chunks(int Fb, const int *__rest
                                                        int *mR) {
     const int b = blockIdx.x;
     if (b >= cs[Fb - 1]) return;
-    const int k = chunk_node(cs, Fb, b);
+    const int k = chunkNode[b];
     const int v = f_node[k];
     if (t_dim[v] < 0) return;
     const int first = k > 0 ? cs[k - 1] : 0, last = cs[k] - 1;
@@ -430,6 +437,7 @@ __global__ void __launch_bounds__(TB_BS) k_mark_chunks(int Fb, const int *__rest
 
 __global__ void __launch_bounds__(TB_BS) k_pair_chunks(int Fb, const int *__restrict__ f_node,
                                                        const int *__restrict__ cs,
+                                                       const int *__restrict__ chunkNode,
                                                        const int *__restrict__ coff,
                                                        const int *__restrict__ t_lo,
                                                        const int *__restrict__ t_dim,
@@ -440,7 +448,7 @@ __global__ void __launch_bounds__(TB_BS) k_pair_chunks(int Fb, const int *__rest
                                                        int *iord) {
     const int b = blockIdx.x;
     if (b >= cs[Fb - 1]) return;
-    const int k = chunk_node(cs, Fb, b);
+    const int k = chunkNode[b];
     const int v = f_node[k];
     if (t_dim[v] < 0) return;
     const int first = k > 0 ? cs[k - 1] : 0, last = cs[k] - 1;
@@ -505,22 +513,36 @@ __global__ void __launch_bounds__(LB_BS) k_scan_small(int count, const int *__re
     block_scan_items(out, count);
 }
 
-// chunk counts of the frontier nodes and their inclusive scan (Fb <= LB_MAX)
-__global__ void __launch_bounds__(LB_BS) k_level_chunks(int Fb, int L, const TsphBuildCtl *__restrict__ ctl,
+// chunk counts of the frontier nodes, their inclusive scan and the
+// frontier index of every chunk (Fb <= LB_MAX)
+__global__ void __launch_bounds__(LB_BS) k_level_chunks(int Fb, int L, int S,
+                                                        const TsphBuildCtl *__restrict__ ctl,
                                                         const int *__restrict__ f_node,
                                                         const int *__restrict__ t_lo,
-                                                        const int *__restrict__ t_hi, int *cs) {
+                                                        const int *__restrict__ t_hi, int *cs,
+                                                        int *chunkNode) {
+    __shared__ int scs[LB_MAX];
     const int F = ctl->levF[L];
     for (int k = threadIdx.x; k < Fb; k += LB_BS) {
         int c = 0;
         if (k < F) {
             int v = f_node[k];
-            c = (t_hi[v] - t_lo[v] + TB_CHUNK) / TB_CHUNK;
+            c = node_chunks(t_hi[v] - t_lo[v] + 1, S);
         }
-        cs[k] = c;
+        scs[k] = c;
     }
     __syncthreads();
-    block_scan_items(cs, Fb);
+    block_scan_items(scs, Fb);
+    for (int k = threadIdx.x; k < Fb; k += LB_BS) cs[k] = scs[k];
+    const int total = Fb > 0 ? scs[Fb - 1] : 0;
+    for (int c = threadIdx.x; c < total; c += LB_BS) {
+        int a = 0, e = Fb - 1;   // first k with scs[k] > c
+        while (a < e) {
+            int m = (a + e) >> 1;
+            if (scs[m] > c) e = m; else a = m + 1;
+        }
+        chunkNode[c] = a;
+    }
 }
 
 // split decisions of the frontier (k_top_split) and the split ranks
@@ -1516,7 +1538,7 @@ void tsph_free_tree(TsphDevTree &T) {
 
 void tsph_free_build(TsphBuildBufs &B) {
     TFREE(B.f_node[0]); TFREE(B.f_node[1]); TFREE(B.f_split); TFREE(B.f_rank); TFREE(B.tasks);
-    TFREE(B.chunkScan); TFREE(B.ctot); TFREE(B.coff);
+    TFREE(B.chunkScan); TFREE(B.ctot); TFREE(B.coff); TFREE(B.chunkNode);
     TFREE(B.t_lo); TFREE(B.t_hi); TFREE(B.t_dim); TFREE(B.t_child); TFREE(B.t_size);
     TFREE(B.t_pre); TFREE(B.t_root); TFREE(B.t_loc); TFREE(B.t_split); TFREE(B.t_bnd);
     TFREE(B.maxd2); TFREE(B.visit); TFREE(B.leafFlag); TFREE(B.leafScan); TFREE(B.ctl);
@@ -1588,6 +1610,7 @@ static int ensure_temp(tsph_ctx *ctx, int n, int nR) {
     rc |= tsph_grow(ctx, &B.chunkScan, topCap);
     rc |= tsph_grow(ctx, &B.ctot, n / TB_CHUNK + topCap + 2);
     rc |= tsph_grow(ctx, &B.coff, n / TB_CHUNK + topCap + 2);
+    rc |= tsph_grow(ctx, &B.chunkNode, n / TB_CHUNK + topCap + 2);
     rc |= tsph_grow(ctx, &B.t_lo, tcap);
     rc |= tsph_grow(ctx, &B.t_hi, tcap);
     rc |= tsph_grow(ctx, &B.t_dim, tcap);
@@ -1751,19 +1774,21 @@ static int build_tree_body(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n
         const int slots = n / TB_CHUNK + Fb + 1;     // >= chunks of any frontier
         const bool small = Fb <= LB_MAX;              // frontier work in single blocks
         if (small) {
-            k_level_chunks<<<1, LB_BS, 0, ctx->stream>>>(Fb, level, B.ctl, B.f_node[cur], B.t_lo,
-                                                         B.t_hi, B.chunkScan);
+            k_level_chunks<<<1, LB_BS, 0, ctx->stream>>>(Fb, level, S, B.ctl, B.f_node[cur], B.t_lo,
+                                                         B.t_hi, B.chunkScan, B.chunkNode);
             TSPH_LAUNCH_CK("k_level_chunks");
         } else {
-            k_chunk_count<<<tsph_blocks(Fb, BS), BS, 0, ctx->stream>>>(Fb, level, B.ctl,
+            k_chunk_count<<<tsph_blocks(Fb, BS), BS, 0, ctx->stream>>>(Fb, level, S, B.ctl,
                                                                         B.f_node[cur], B.t_lo,
                                                                         B.t_hi, B.f_split);
             TSPH_LAUNCH_CK("k_chunk_count");
             rc = tsph_scan_inclusive(ctx, B.f_split, B.chunkScan, Fb);
             if (rc) return rc;
+            k_chunk_map<<<tsph_blocks(slots, BS), BS, 0, ctx->stream>>>(Fb, B.chunkScan, B.chunkNode);
+            TSPH_LAUNCH_CK("k_chunk_map");
         }
-        k_bounds_chunks<<<slots, TB_BS, 0, ctx->stream>>>(Fb, B.f_node[cur], B.chunkScan, B.t_lo,
-                                                          B.t_hi, P.x, P.y, P.z, B.t_bnd);
+        k_bounds_chunks<<<slots, TB_BS, 0, ctx->stream>>>(Fb, B.f_node[cur], B.chunkScan, B.chunkNode,
+                                                          B.t_lo, B.t_hi, P.x, P.y, P.z, B.t_bnd);
         TSPH_LAUNCH_CK("k_bounds_chunks");
         if (small) {
             k_level_split<<<1, LB_BS, 0, ctx->stream>>>(
@@ -1777,7 +1802,7 @@ static int build_tree_body(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n
             TSPH_LAUNCH_CK("k_top_split");
         }
         k_flag_chunks<<<slots, TB_BS, 0, ctx->stream>>>(Fb, slots, B.f_node[cur], B.chunkScan,
-                                                        B.t_lo, B.t_hi, B.t_dim, B.t_split, P.x,
+                                                        B.chunkNode, B.t_lo, B.t_hi, B.t_dim, B.t_split, P.x,
                                                         P.y, P.z, B.scan, B.ctot);
         TSPH_LAUNCH_CK("k_flag_chunks");
         if (slots <= LB_MAX) {
@@ -1787,11 +1812,11 @@ static int build_tree_body(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n
             rc = tsph_scan_inclusive(ctx, B.ctot, B.coff, slots);
             if (rc) return rc;
         }
-        k_mark_chunks<<<slots, TB_BS, 0, ctx->stream>>>(Fb, B.f_node[cur], B.chunkScan, B.coff,
+        k_mark_chunks<<<slots, TB_BS, 0, ctx->stream>>>(Fb, B.f_node[cur], B.chunkScan, B.chunkNode, B.coff,
                                                         B.t_lo, B.t_hi, B.t_dim, B.scan, B.lt,
                                                         B.seg);
         TSPH_LAUNCH_CK("k_mark_chunks");
-        k_pair_chunks<<<slots, TB_BS, 0, ctx->stream>>>(Fb, B.f_node[cur], B.chunkScan, B.coff,
+        k_pair_chunks<<<slots, TB_BS, 0, ctx->stream>>>(Fb, B.f_node[cur], B.chunkScan, B.chunkNode, B.coff,
                                                         B.t_lo, B.t_dim, B.scan, B.lt, B.seg, P.x,
                                                         P.y, P.z, P.m, P.h, P.iord);
         TSPH_LAUNCH_CK("k_pair_chunks");

@@ -31,6 +31,7 @@ struct TsphBuildBufs {
     int *tasks;       // subtree task roots (temp ids)
     int *chunkScan;   // top phase: inclusive scan of the frontier nodes' chunk counts
     int *ctot, *coff; // top phase: flags per chunk and their inclusive scan
+    int *chunkNode;   // top phase: frontier index of each chunk
     // temporary nodes: roots, then the top phase breadth first, then the
     // subtree slots of every task (a task over particles [lo, hi] owns
     // slots topCap + 2*lo ... topCap + 2*hi + 1)
