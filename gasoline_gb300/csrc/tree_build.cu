@@ -331,8 +331,11 @@ __device__ __forceinline__ void swap_particles(double *x, double *y, double *z, 
 
 // Partition flags (r[d] < fSplit) of one chunk of a split frontier node and
 // their in-chunk inclusive scan; ctot[b] = the chunk's count.  Warps take
-// contiguous runs and count with ballots; two passes over the chunk.
-__global__ void __launch_bounds__(TB_BS) k_flag_chunks(int Fb, int nChunkSlots,
+// contiguous runs and count with ballots; two passes over the chunk.  The
+// first also gathers the bounds of the node's two children (their keys were
+// initialised when the node was split), so the next level needs no pass of
+// its own for them.
+__global__ void __launch_bounds__(TB_BS) k_flag_chunks(int Fb, int L, int nChunkSlots,
                                                        const int *__restrict__ f_node,
                                                        const int *__restrict__ cs,
                                                        const int *__restrict__ chunkNode,
@@ -343,8 +346,11 @@ __global__ void __launch_bounds__(TB_BS) k_flag_chunks(int Fb, int nChunkSlots,
                                                        const double *__restrict__ x,
                                                        const double *__restrict__ y,
                                                        const double *__restrict__ z, int *scan,
-                                                       int *ctot) {
+                                                       int *ctot, const TsphBuildCtl *__restrict__ ctl,
+                                                       const int *__restrict__ f_rank, int topCap,
+                                                       double *t_bnd) {
     __shared__ int wt[TB_BS / 32];
+    __shared__ unsigned long long kred[TB_BS / 32][12];
     const int b = blockIdx.x;
     if (b >= nChunkSlots) return;
     if (b >= cs[Fb - 1]) {
@@ -365,13 +371,70 @@ __global__ void __launch_bounds__(TB_BS) k_flag_chunks(int Fb, int nChunkSlots,
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int CW = TB_CHUNK / (TB_BS / 32);
     const int w0 = p0 + w * CW, w1 = min(w0 + CW, p1);
+    // first pass: the flags' count, and the bounds keys of the two
+    // children (flagged: the lower child, the others: the upper one), which
+    // the partition only moves about
+    unsigned long long mn[2][3], mx[2][3];
+#pragma unroll
+    for (int c = 0; c < 2; ++c)
+#pragma unroll
+        for (int e = 0; e < 3; ++e) { mn[c][e] = ~0ULL; mx[c][e] = 0ULL; }
     int cnt = 0;
-    for (int base = w0; base < w1; base += 32) {
-        int p = base + lane;
-        cnt += __popc(__ballot_sync(0xffffffffu, p < w1 && X[p] < fs));
+    for (int base = w0; base < w1; base += 4 * 32) {   // four rows' loads in flight at once
+        double r[4][3];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int p = base + 32 * u + lane;
+            r[u][0] = p < w1 ? x[p] : 0.0;
+            r[u][1] = p < w1 ? y[p] : 0.0;
+            r[u][2] = p < w1 ? z[p] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int p = base + 32 * u + lane;
+            bool f = false;
+            if (p < w1) {
+                f = (d == 0 ? r[u][0] : (d == 1 ? r[u][1] : r[u][2])) < fs;
+#pragma unroll
+                for (int e = 0; e < 3; ++e) {
+                    const unsigned long long kk = dkey(r[u][e]);
+                    if (f) { mn[0][e] = umin64(mn[0][e], kk); mx[0][e] = umax64(mx[0][e], kk); }
+                    else { mn[1][e] = umin64(mn[1][e], kk); mx[1][e] = umax64(mx[1][e], kk); }
+                }
+            }
+            cnt += __popc(__ballot_sync(0xffffffffu, f));
+        }
     }
-    if (lane == 0) wt[w] = cnt;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int c = 0; c < 2; ++c)
+#pragma unroll
+            for (int e = 0; e < 3; ++e) {
+                mn[c][e] = umin64(mn[c][e], __shfl_xor_sync(0xffffffffu, mn[c][e], o));
+                mx[c][e] = umax64(mx[c][e], __shfl_xor_sync(0xffffffffu, mx[c][e], o));
+            }
+    }
+    if (lane == 0) {
+        wt[w] = cnt;
+#pragma unroll
+        for (int c = 0; c < 2; ++c)
+#pragma unroll
+            for (int e = 0; e < 3; ++e) { kred[w][6 * c + e] = mn[c][e]; kred[w][6 * c + 3 + e] = mx[c][e]; }
+    }
     __syncthreads();
+    if (threadIdx.x < 12) {
+        // the children are numbered by the node's split rank (k_top_children)
+        const int q = threadIdx.x % 6, c0 = ctl->levStart[L + 1] + 2 * (f_rank[k] - 1);
+        const int c = c0 + threadIdx.x / 6;
+        unsigned long long r = kred[0][threadIdx.x];
+        for (int u = 1; u < TB_BS / 32; ++u)
+            r = q < 3 ? umin64(r, kred[u][threadIdx.x]) : umax64(r, kred[u][threadIdx.x]);
+        unsigned long long *key = reinterpret_cast<unsigned long long *>(t_bnd + 6 * (size_t)c) + q;
+        if (c0 + 1 < topCap && (q < 3 ? r != ~0ULL : r != 0ULL)) {   // else k_top_children fails
+            if (q < 3) atomicMin(key, r); else atomicMax(key, r);
+        }
+    }
     int run = 0, tot = 0;
 #pragma unroll
     for (int q = 0; q < TB_BS / 32; ++q) {
@@ -379,11 +442,20 @@ __global__ void __launch_bounds__(TB_BS) k_flag_chunks(int Fb, int nChunkSlots,
         tot += wt[q];
     }
     const unsigned le = (lane == 31) ? 0xffffffffu : ((2u << lane) - 1u);
-    for (int base = w0; base < w1; base += 32) {
-        int p = base + lane;
-        unsigned bal = __ballot_sync(0xffffffffu, p < w1 && X[p] < fs);
-        if (p < w1) scan[p] = run + __popc(bal & le);
-        run += __popc(bal);
+    for (int base = w0; base < w1; base += 4 * 32) {
+        double xv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int p = base + 32 * u + lane;
+            xv[u] = p < w1 ? X[p] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int p = base + 32 * u + lane;
+            unsigned bal = __ballot_sync(0xffffffffu, p < w1 && xv[u] < fs);
+            if (p < w1) scan[p] = run + __popc(bal & le);
+            run += __popc(bal);
+        }
     }
     if (threadIdx.x == 0) ctot[b] = tot;
 }
@@ -423,14 +495,27 @@ __global__ void __launch_bounds__(TB_BS) k_mark_chunks(int Fb, const int *__rest
     const int j = b - first;
     const int p0 = lo + j * TB_CHUNK, p1 = min(p0 + TB_CHUNK, hi + 1);
     const int cbase = (b > 0 ? coff[b - 1] : 0) - base;   // flags before this chunk
-    for (int p = p0 + threadIdx.x; p < p1; p += TB_BS) {
-        const int s = scan[p] + cbase;             // node-local inclusive count
-        const int sp = p == p0 ? cbase : scan[p - 1] + cbase;
-        const bool flag = s != sp;                 // r < fSplit
-        if (p < mid) {
-            if (!flag) mL[lo + (p - lo) - sp] = p;          // misplaced left, rank (p-lo) - sp
-        } else if (flag) {
-            mR[lo + total - s] = p;                          // misplaced right, rank from hi
+    // four strides' loads in flight at once
+    for (int q = p0 + threadIdx.x; q < p1; q += 4 * TB_BS) {
+        int sv[4], pv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int p = q + u * TB_BS;
+            sv[u] = p < p1 ? scan[p] : 0;
+            pv[u] = p < p1 && p > p0 ? scan[p - 1] : 0;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int p = q + u * TB_BS;
+            if (p >= p1) break;
+            const int s = sv[u] + cbase;               // node-local inclusive count
+            const int sp = p == p0 ? cbase : pv[u] + cbase;
+            const bool flag = s != sp;                 // r < fSplit
+            if (p < mid) {
+                if (!flag) mL[lo + (p - lo) - sp] = p;          // misplaced left, rank (p-lo) - sp
+            } else if (flag) {
+                mR[lo + total - s] = p;                          // misplaced right, rank from hi
+            }
         }
     }
 }
@@ -457,8 +542,9 @@ __global__ void __launch_bounds__(TB_BS) k_pair_chunks(int Fb, const int *__rest
     const int total = coff[last] - base;
     // misplaced pairs: the elements >= fSplit among the first `total`
     const int nMis = total > 0 ? total - node_scan(scan, coff, first, base, lo, lo + total - 1) : 0;
-    const int j = b - first;
-    for (int t = j * TB_CHUNK + threadIdx.x; t < nMis && t < (j + 1) * TB_CHUNK; t += TB_BS)
+    // the node's swaps are dealt out over all of its chunk blocks
+    const int j = b - first, nc = last - first + 1;
+    for (int t = j * TB_BS + threadIdx.x; t < nMis; t += nc * TB_BS)
         swap_particles(x, y, z, m, h, iord, mL[lo + t], mR[lo + t]);
 }
 
@@ -545,32 +631,74 @@ __global__ void __launch_bounds__(LB_BS) k_level_chunks(int Fb, int L, int S,
     }
 }
 
-// split decisions of the frontier (k_top_split) and the split ranks
-// (inclusive scan of the flags), one block (Fb <= LB_MAX)
-__global__ void __launch_bounds__(LB_BS) k_level_split(int Fb, int L, const int *__restrict__ f_node,
-                                                       int S, int nBucket, int *t_lo, int *t_hi,
-                                                       int *t_dim, int *t_child, int *t_size,
-                                                       double *t_split, double *t_bnd, int *f_split,
-                                                       int *f_rank, int *tasks, TsphBuildCtl *ctl) {
+// One level's frontier work in one block (Fb <= LB_MAX): the split
+// decisions (as k_top_split, from the bounds the parent's flag pass
+// gathered), the split ranks, the chunks of the nodes above the task size
+// with their scan and node map (k_level_chunks), and the bounds keys of
+// the children, which this level's flag pass accumulates.
+__global__ void __launch_bounds__(LB_BS) k_level_prep(int Fb, int L, const int *__restrict__ f_node,
+                                                      int S, int nBucket, int *t_lo, int *t_hi,
+                                                      int *t_dim, int *t_child, int *t_size,
+                                                      double *t_split, double *t_bnd, int *f_split,
+                                                      int *f_rank, int *tasks, TsphBuildCtl *ctl,
+                                                      int *cs, int *chunkNode, int topCap) {
+    __shared__ int scs[LB_MAX];
     const int F = ctl->levF[L];
     for (int k = threadIdx.x; k < Fb; k += LB_BS) {
-        int sp = 0;
+        int sp = 0, nc = 0;
         if (k < F) {
             int v = f_node[k];
-            if (t_hi[v] - t_lo[v] + 1 <= S) {
+            const int size = t_hi[v] - t_lo[v] + 1;
+            if (size <= S) {
                 t_dim[v] = -2;                   // handed to a subtree task
                 key_init(t_bnd, v);
                 tasks[atomicAdd(&ctl->taskCount, 1)] = v;
             } else {
                 sp = decide_node(v, nBucket, t_lo, t_hi, t_dim, t_child, t_split, t_bnd) ? 1 : 0;
                 if (!sp) t_size[v] = 1;
+                nc = node_chunks(size, S);
             }
         }
         f_split[k] = sp;
         f_rank[k] = sp;
+        scs[k] = nc;
     }
     __syncthreads();
     block_scan_items(f_rank, Fb);
+    block_scan_items(scs, Fb);
+    const int nTop = ctl->levStart[L + 1];
+    for (int k = threadIdx.x; k < Fb; k += LB_BS) {
+        cs[k] = scs[k];
+        if (f_split[k]) {
+            const int c = nTop + 2 * (f_rank[k] - 1);
+            if (c + 1 < topCap) {
+                key_init(t_bnd, c);
+                key_init(t_bnd, c + 1);
+            }
+        }
+    }
+    const int total = Fb > 0 ? scs[Fb - 1] : 0;
+    for (int c = threadIdx.x; c < total; c += LB_BS) {
+        int a = 0, e = Fb - 1;   // first k with scs[k] > c
+        while (a < e) {
+            int m = (a + e) >> 1;
+            if (scs[m] > c) e = m; else a = m + 1;
+        }
+        chunkNode[c] = a;
+    }
+}
+
+// The children's bounds keys when the frontier is too large for one block.
+__global__ void k_child_keys(int Fb, int L, const int *__restrict__ f_split,
+                             const int *__restrict__ f_rank, const TsphBuildCtl *__restrict__ ctl,
+                             int topCap, double *t_bnd) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= Fb || k >= ctl->levF[L] || !f_split[k]) return;
+    const int c = ctl->levStart[L + 1] + 2 * (f_rank[k] - 1);
+    if (c + 1 < topCap) {
+        key_init(t_bnd, c);
+        key_init(t_bnd, c + 1);
+    }
 }
 
 __global__ void k_top_children(int Fb, int L, const int *__restrict__ f_node,
@@ -603,8 +731,6 @@ __global__ void k_top_children(int Fb, int L, const int *__restrict__ f_node,
     t_hi[c] = mid - 1;
     t_lo[c + 1] = mid;
     t_hi[c + 1] = hi;
-    key_init(t_bnd, c);
-    key_init(t_bnd, c + 1);
     nf_node[2 * r] = c;
     nf_node[2 * r + 1] = c + 1;
 }
@@ -1769,41 +1895,60 @@ static int build_tree_body(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n
     // the first look comes at the last build's depth (the same particles
     // rebuilt give the same depth), then every TOP_BATCH levels
     const int look0 = (!cap && T.lastTopLevels > 0) ? T.lastTopLevels : TOP_BATCH;
+    // level 0: the bounds of the roots; every later frontier node gets its
+    // bounds from its parent's flag pass
+    if (Fb > 0) {
+        const int slots = n / TB_CHUNK + Fb + 1;
+        if (Fb <= LB_MAX) {
+            k_level_chunks<<<1, LB_BS, 0, ctx->stream>>>(Fb, 0, S, B.ctl, B.f_node[0], B.t_lo,
+                                                         B.t_hi, B.chunkScan, B.chunkNode);
+            TSPH_LAUNCH_CK("k_level_chunks");
+        } else {
+            k_chunk_count<<<tsph_blocks(Fb, BS), BS, 0, ctx->stream>>>(Fb, 0, S, B.ctl, B.f_node[0],
+                                                                        B.t_lo, B.t_hi, B.ctot);
+            TSPH_LAUNCH_CK("k_chunk_count");
+            rc = tsph_scan_inclusive(ctx, B.ctot, B.chunkScan, Fb);
+            if (rc) return rc;
+            k_chunk_map<<<tsph_blocks(slots, BS), BS, 0, ctx->stream>>>(Fb, B.chunkScan, B.chunkNode);
+            TSPH_LAUNCH_CK("k_chunk_map");
+        }
+        k_bounds_chunks<<<slots, TB_BS, 0, ctx->stream>>>(Fb, B.f_node[0], B.chunkScan, B.chunkNode,
+                                                          B.t_lo, B.t_hi, P.x, P.y, P.z, B.t_bnd);
+        TSPH_LAUNCH_CK("k_bounds_chunks");
+    }
     while (Fb > 0 && level < Lmax) {
         if (!cap && level + 2 >= TSPH_MAX_LEVELS) return TSPH_ERR_TREE_DEPTH;
         const int slots = n / TB_CHUNK + Fb + 1;     // >= chunks of any frontier
         const bool small = Fb <= LB_MAX;              // frontier work in single blocks
         if (small) {
-            k_level_chunks<<<1, LB_BS, 0, ctx->stream>>>(Fb, level, S, B.ctl, B.f_node[cur], B.t_lo,
-                                                         B.t_hi, B.chunkScan, B.chunkNode);
-            TSPH_LAUNCH_CK("k_level_chunks");
-        } else {
-            k_chunk_count<<<tsph_blocks(Fb, BS), BS, 0, ctx->stream>>>(Fb, level, S, B.ctl,
-                                                                        B.f_node[cur], B.t_lo,
-                                                                        B.t_hi, B.f_split);
-            TSPH_LAUNCH_CK("k_chunk_count");
-            rc = tsph_scan_inclusive(ctx, B.f_split, B.chunkScan, Fb);
-            if (rc) return rc;
-            k_chunk_map<<<tsph_blocks(slots, BS), BS, 0, ctx->stream>>>(Fb, B.chunkScan, B.chunkNode);
-            TSPH_LAUNCH_CK("k_chunk_map");
-        }
-        k_bounds_chunks<<<slots, TB_BS, 0, ctx->stream>>>(Fb, B.f_node[cur], B.chunkScan, B.chunkNode,
-                                                          B.t_lo, B.t_hi, P.x, P.y, P.z, B.t_bnd);
-        TSPH_LAUNCH_CK("k_bounds_chunks");
-        if (small) {
-            k_level_split<<<1, LB_BS, 0, ctx->stream>>>(
-                Fb, level, B.f_node[cur], S, nBucket, B.t_lo, B.t_hi, B.t_dim, B.t_child,
-                B.t_size, B.t_split, B.t_bnd, B.f_split, B.f_rank, B.tasks, B.ctl);
-            TSPH_LAUNCH_CK("k_level_split");
+            k_level_prep<<<1, LB_BS, 0, ctx->stream>>>(
+                Fb, level, B.f_node[cur], S, nBucket, B.t_lo, B.t_hi, B.t_dim, B.t_child, B.t_size,
+                B.t_split, B.t_bnd, B.f_split, B.f_rank, B.tasks, B.ctl, B.chunkScan, B.chunkNode,
+                B.topCap);
+            TSPH_LAUNCH_CK("k_level_prep");
         } else {
             k_top_split<<<tsph_blocks(Fb, BS), BS, 0, ctx->stream>>>(
                 Fb, level, B.f_node[cur], S, nBucket, B.t_lo, B.t_hi, B.t_dim, B.t_child,
                 B.t_size, B.t_split, B.t_bnd, B.f_split, B.tasks, B.ctl);
             TSPH_LAUNCH_CK("k_top_split");
+            rc = tsph_scan_inclusive(ctx, B.f_split, B.f_rank, Fb);
+            if (rc) return rc;
+            k_child_keys<<<tsph_blocks(Fb, BS), BS, 0, ctx->stream>>>(Fb, level, B.f_split, B.f_rank,
+                                                                       B.ctl, B.topCap, B.t_bnd);
+            TSPH_LAUNCH_CK("k_child_keys");
+            k_chunk_count<<<tsph_blocks(Fb, BS), BS, 0, ctx->stream>>>(Fb, level, S, B.ctl,
+                                                                        B.f_node[cur], B.t_lo,
+                                                                        B.t_hi, B.ctot);
+            TSPH_LAUNCH_CK("k_chunk_count");
+            rc = tsph_scan_inclusive(ctx, B.ctot, B.chunkScan, Fb);
+            if (rc) return rc;
+            k_chunk_map<<<tsph_blocks(slots, BS), BS, 0, ctx->stream>>>(Fb, B.chunkScan, B.chunkNode);
+            TSPH_LAUNCH_CK("k_chunk_map");
         }
-        k_flag_chunks<<<slots, TB_BS, 0, ctx->stream>>>(Fb, slots, B.f_node[cur], B.chunkScan,
+        k_flag_chunks<<<slots, TB_BS, 0, ctx->stream>>>(Fb, level, slots, B.f_node[cur], B.chunkScan,
                                                         B.chunkNode, B.t_lo, B.t_hi, B.t_dim, B.t_split, P.x,
-                                                        P.y, P.z, B.scan, B.ctot);
+                                                        P.y, P.z, B.scan, B.ctot, B.ctl, B.f_rank,
+                                                        B.topCap, B.t_bnd);
         TSPH_LAUNCH_CK("k_flag_chunks");
         if (slots <= LB_MAX) {
             k_scan_small<<<1, LB_BS, 0, ctx->stream>>>(slots, B.ctot, B.coff);
@@ -1820,10 +1965,6 @@ static int build_tree_body(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n
                                                         B.t_lo, B.t_dim, B.scan, B.lt, B.seg, P.x,
                                                         P.y, P.z, P.m, P.h, P.iord);
         TSPH_LAUNCH_CK("k_pair_chunks");
-        if (!small) {
-            rc = tsph_scan_inclusive(ctx, B.f_split, B.f_rank, Fb);
-            if (rc) return rc;
-        }
         k_top_children<<<tsph_blocks(Fb, BS), BS, 0, ctx->stream>>>(
             Fb, level, B.f_node[cur], B.f_split, B.f_rank, B.chunkScan, B.coff, B.topCap, B.t_lo,
             B.t_hi, B.t_child, B.t_bnd, B.f_node[1 - cur], B.ctl);
