@@ -331,11 +331,11 @@ __device__ __forceinline__ void swap_particles(double *x, double *y, double *z, 
 
 // Partition flags (r[d] < fSplit) of one chunk of a split frontier node and
 // their in-chunk inclusive scan; ctot[b] = the chunk's count.  Warps take
-// contiguous runs and count with ballots; two passes over the chunk.  The
-// first also gathers the bounds of the node's two children (their keys were
+// contiguous runs and count with ballots, kept in registers for the scan.
+// The pass also gathers the bounds of the node's two children (their keys were
 // initialised when the node was split), so the next level needs no pass of
 // its own for them.
-__global__ void __launch_bounds__(TB_BS) k_flag_chunks(int Fb, int L, int nChunkSlots,
+__global__ void __launch_bounds__(TB_BS, 3) k_flag_chunks(int Fb, int L, int nChunkSlots,
                                                        const int *__restrict__ f_node,
                                                        const int *__restrict__ cs,
                                                        const int *__restrict__ chunkNode,
@@ -366,8 +366,7 @@ __global__ void __launch_bounds__(TB_BS) k_flag_chunks(int Fb, int L, int nChunk
     }
     const int j = b - (k > 0 ? cs[k - 1] : 0);
     const int p0 = t_lo[v] + j * TB_CHUNK, p1 = min(p0 + TB_CHUNK, t_hi[v] + 1);
-    const double fs = t_split[v];
-    const double *X = d == 0 ? x : (d == 1 ? y : z);
+    const unsigned long long kfs = dlt_key(t_split[v]);
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int CW = TB_CHUNK / (TB_BS / 32);
     const int w0 = p0 + w * CW, w1 = min(w0 + CW, p1);
@@ -379,22 +378,27 @@ __global__ void __launch_bounds__(TB_BS) k_flag_chunks(int Fb, int L, int nChunk
     for (int c = 0; c < 2; ++c)
 #pragma unroll
         for (int e = 0; e < 3; ++e) { mn[c][e] = ~0ULL; mx[c][e] = 0ULL; }
+    // the warp's rows of 32 (CW / 32 of them): their flag ballots stay in
+    // registers for the second pass
+    constexpr int NR = CW / 32;
+    unsigned bal[NR];
     int cnt = 0;
-    for (int base = w0; base < w1; base += 4 * 32) {   // four rows' loads in flight at once
+#pragma unroll
+    for (int r0 = 0; r0 < NR; r0 += 4) {   // four rows' loads in flight at once
         double r[4][3];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-            const int p = base + 32 * u + lane;
+            const int p = w0 + 32 * (r0 + u) + lane;
             r[u][0] = p < w1 ? x[p] : 0.0;
             r[u][1] = p < w1 ? y[p] : 0.0;
             r[u][2] = p < w1 ? z[p] : 0.0;
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-            const int p = base + 32 * u + lane;
+            const int p = w0 + 32 * (r0 + u) + lane;
             bool f = false;
             if (p < w1) {
-                f = (d == 0 ? r[u][0] : (d == 1 ? r[u][1] : r[u][2])) < fs;
+                f = dlt_key(d == 0 ? r[u][0] : (d == 1 ? r[u][1] : r[u][2])) < kfs;
 #pragma unroll
                 for (int e = 0; e < 3; ++e) {
                     const unsigned long long kk = dkey(r[u][e]);
@@ -402,7 +406,8 @@ __global__ void __launch_bounds__(TB_BS) k_flag_chunks(int Fb, int L, int nChunk
                     else { mn[1][e] = umin64(mn[1][e], kk); mx[1][e] = umax64(mx[1][e], kk); }
                 }
             }
-            cnt += __popc(__ballot_sync(0xffffffffu, f));
+            bal[r0 + u] = __ballot_sync(0xffffffffu, f);
+            cnt += __popc(bal[r0 + u]);
         }
     }
 #pragma unroll
@@ -442,20 +447,11 @@ __global__ void __launch_bounds__(TB_BS) k_flag_chunks(int Fb, int L, int nChunk
         tot += wt[q];
     }
     const unsigned le = (lane == 31) ? 0xffffffffu : ((2u << lane) - 1u);
-    for (int base = w0; base < w1; base += 4 * 32) {
-        double xv[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const int p = base + 32 * u + lane;
-            xv[u] = p < w1 ? X[p] : 0.0;
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const int p = base + 32 * u + lane;
-            unsigned bal = __ballot_sync(0xffffffffu, p < w1 && xv[u] < fs);
-            if (p < w1) scan[p] = run + __popc(bal & le);
-            run += __popc(bal);
-        }
+    for (int q = 0; q < NR; ++q) {
+        const int p = w0 + 32 * q + lane;
+        if (p < w1) scan[p] = run + __popc(bal[q] & le);
+        run += __popc(bal[q]);
     }
     if (threadIdx.x == 0) ctot[b] = tot;
 }

@@ -29,6 +29,14 @@ __device__ __forceinline__ unsigned long long dkey(double x) {
     unsigned long long b = (unsigned long long)__double_as_longlong(x);
     return (b & 0x8000000000000000ULL) ? ~b : (b | 0x8000000000000000ULL);
 }
+// A key that orders finite doubles as < does, -0 equal to +0: a partition
+// test r < fSplit in integer instructions (GB300 issues FP64 compares at
+// the FP64 rate, 1/64 of FP32).
+__device__ __forceinline__ unsigned long long dlt_key(double x) {
+    unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    if (b == 0x8000000000000000ULL) b = 0ULL;
+    return (b & 0x8000000000000000ULL) ? ~b : (b | 0x8000000000000000ULL);
+}
 __device__ __forceinline__ double dunkey(unsigned long long k) {
     unsigned long long b = (k & 0x8000000000000000ULL) ? (k & 0x7FFFFFFFFFFFFFFFULL) : ~k;
     return __longlong_as_double((long long)b);
