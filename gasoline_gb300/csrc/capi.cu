@@ -216,13 +216,11 @@ __global__ void k_gather_tree(int n, TsphDevState C, TsphDevParts P, TsphDevCoun
     double a = 0.0;
     if (i < n) {
         int o = P.iord[i];
-        const double x = C.x[o], y = C.y[o], z = C.z[o], m = C.m[o], h = C.h[o];
+        const double x = C.x[o], y = C.y[o], z = C.z[o];   // masses and softenings after the build
         P.x[i] = x;
         P.y[i] = y;
         P.z[i] = z;
-        P.m[i] = m;
-        P.h[i] = h;
-        if (!isfinite(x + y + z + m + h)) atomicOr(&cnt->status, 1u << TSPH_ERR_NONFINITE);
+        if (!isfinite(x + y + z)) atomicOr(&cnt->status, 1u << TSPH_ERR_NONFINITE);
         a = fmax(fabs(x), fmax(fabs(y), fabs(z)));
         if (a > limit) atomicOr(&cnt->status, 1u << TSPH_ERR_BOUNDS);
     }

@@ -1398,8 +1398,7 @@ __global__ void k_gas_gather_pos(int ng, TsphDevState C, TsphDevParts G) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= ng) return;
     int o = G.iord[i];
-    G.x[i] = C.x[o]; G.y[i] = C.y[o]; G.z[i] = C.z[o];
-    G.m[i] = C.m[o]; G.h[i] = C.h[o];
+    G.x[i] = C.x[o]; G.y[i] = C.y[o]; G.z[i] = C.z[o];   // masses and softenings after the build
 }
 
 // ---------------------------------------------------------------------------

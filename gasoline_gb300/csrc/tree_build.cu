@@ -318,14 +318,13 @@ __device__ __forceinline__ int lower_bound_scan(const int *__restrict__ S, int a
     return a;
 }
 
-__device__ __forceinline__ void swap_particles(double *x, double *y, double *z, double *m, double *h,
-                                               int *iord, int p, int q) {
+// The build moves positions and caller indices only; masses and
+// softenings follow by one gather at its end (k_gather_mass).
+__device__ __forceinline__ void swap_particles(double *x, double *y, double *z, int *iord, int p, int q) {
     double t0;
     t0 = x[p]; x[p] = x[q]; x[q] = t0;
     t0 = y[p]; y[p] = y[q]; y[q] = t0;
     t0 = z[p]; z[p] = z[q]; z[q] = t0;
-    t0 = m[p]; m[p] = m[q]; m[q] = t0;
-    t0 = h[p]; h[p] = h[q]; h[q] = t0;
     int ti = iord[p]; iord[p] = iord[q]; iord[q] = ti;
 }
 
@@ -525,8 +524,7 @@ __global__ void __launch_bounds__(TB_BS) k_pair_chunks(int Fb, const int *__rest
                                                        const int *__restrict__ scan,
                                                        const int *__restrict__ mL,
                                                        const int *__restrict__ mR, double *x,
-                                                       double *y, double *z, double *m, double *h,
-                                                       int *iord) {
+                                                       double *y, double *z, int *iord) {
     const int b = blockIdx.x;
     if (b >= cs[Fb - 1]) return;
     const int k = chunkNode[b];
@@ -541,7 +539,7 @@ __global__ void __launch_bounds__(TB_BS) k_pair_chunks(int Fb, const int *__rest
     // the node's swaps are dealt out over all of its chunk blocks
     const int j = b - first, nc = last - first + 1;
     for (int t = j * TB_BS + threadIdx.x; t < nMis; t += nc * TB_BS)
-        swap_particles(x, y, z, m, h, iord, mL[lo + t], mR[lo + t]);
+        swap_particles(x, y, z, iord, mL[lo + t], mR[lo + t]);
 }
 
 // ---- single-block forms of the per-level frontier work (one launch
@@ -964,7 +962,7 @@ __global__ void __launch_bounds__(ST_BS, 4) k_subtree(BuildArgs A) {
                     t0 = V.z[p]; V.z[p] = V.z[q]; V.z[q] = t0;
                     short ti = V.perm[p]; V.perm[p] = V.perm[q]; V.perm[q] = ti;
                 } else {
-                    swap_particles(A.x, A.y, A.z, A.m, A.h, A.iord, p, q);
+                    swap_particles(A.x, A.y, A.z, A.iord, p, q);
                 }
             }
             __syncthreads();
@@ -1034,28 +1032,17 @@ __global__ void __launch_bounds__(ST_BS, 4) k_subtree(BuildArgs A) {
         __syncthreads();
         if (V.staged) {
             // the final order back to the global arrays: positions first,
-            // then mass, softening and caller index gathered through the
-            // freed shared memory
+            // then the caller index gathered through the freed shared memory
             for (int p = lo + threadIdx.x; p <= hi; p += ST_BS) {
                 A.x[p] = V.x[p];
                 A.y[p] = V.y[p];
                 A.z[p] = V.z[p];
             }
             __syncthreads();
-            double *gm = sx - lo, *gh = sy - lo;
-            int *gi = reinterpret_cast<int *>(sz) - lo;
-            for (int p = lo + threadIdx.x; p <= hi; p += ST_BS) {
-                int src = lo + V.perm[p];
-                gm[p] = A.m[src];
-                gh[p] = A.h[src];
-                gi[p] = A.iord[src];
-            }
+            int *gi = reinterpret_cast<int *>(sx) - lo;
+            for (int p = lo + threadIdx.x; p <= hi; p += ST_BS) gi[p] = A.iord[lo + V.perm[p]];
             __syncthreads();
-            for (int p = lo + threadIdx.x; p <= hi; p += ST_BS) {
-                A.m[p] = gm[p];
-                A.h[p] = gh[p];
-                A.iord[p] = gi[p];
-            }
+            for (int p = lo + threadIdx.x; p <= hi; p += ST_BS) A.iord[p] = gi[p];
         }
         if (!failed) {
             // subtree sizes bottom-up, then depth-first offsets from the root
@@ -1832,6 +1819,19 @@ __global__ void k_tree_act(int n, const int *__restrict__ iord, const int *__res
 
 static int build_tree_body(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, int nBucket);
 
+// Masses and softenings of the particles in the order a build left them,
+// from the caller-order state.
+__global__ void k_gather_mass(int n, const double *__restrict__ cm, const double *__restrict__ ch,
+                              TsphDevParts P, unsigned int *status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int o = P.iord[i];
+    const double m = cm[o], h = ch[o];
+    P.m[i] = m;
+    P.h[i] = h;
+    if (status && !isfinite(m + h)) atomicOr(status, 1u << TSPH_ERR_NONFINITE);
+}
+
 int tsph_build_tree(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, int nBucket) {
     int rc = build_tree_body(ctx, P, T, n, nBucket);
     if (rc || n == 0) return rc;
@@ -1883,9 +1883,10 @@ static int build_tree_body(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n
     const int Fcap = 2 * (n / S) + 2;
     int Fb = F;
     // a captured build runs a fixed number of levels (its preparation's
-    // depth + 2) with no host look; what is left becomes subtree tasks
+    // depth + 1: one spare level) with no host look; what is left becomes
+    // subtree tasks
     const bool cap = ctx->capturing;
-    const int Lmax = cap ? (T.lastTopLevels + 2 < TSPH_MAX_LEVELS - 2 ? T.lastTopLevels + 2
+    const int Lmax = cap ? (T.lastTopLevels + 1 < TSPH_MAX_LEVELS - 2 ? T.lastTopLevels + 1
                                                                       : TSPH_MAX_LEVELS - 2)
                          : TSPH_MAX_LEVELS - 2;
     // the first look comes at the last build's depth (the same particles
@@ -1959,7 +1960,7 @@ static int build_tree_body(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n
         TSPH_LAUNCH_CK("k_mark_chunks");
         k_pair_chunks<<<slots, TB_BS, 0, ctx->stream>>>(Fb, B.f_node[cur], B.chunkScan, B.chunkNode, B.coff,
                                                         B.t_lo, B.t_dim, B.scan, B.lt, B.seg, P.x,
-                                                        P.y, P.z, P.m, P.h, P.iord);
+                                                        P.y, P.z, P.iord);
         TSPH_LAUNCH_CK("k_pair_chunks");
         k_top_children<<<tsph_blocks(Fb, BS), BS, 0, ctx->stream>>>(
             Fb, level, B.f_node[cur], B.f_split, B.f_rank, B.chunkScan, B.coff, B.topCap, B.t_lo,
@@ -2038,6 +2039,11 @@ static int build_tree_body(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n
     }
     k_subtree<<<ctx->subtreeBlocks[slot], ST_BS, smem, ctx->stream>>>(A);
     TSPH_LAUNCH_CK("k_subtree");
+    // masses and softenings in the final order (the build moved only the
+    // positions and caller indices); a non-finite one is bad input
+    k_gather_mass<<<tsph_blocks(n, BS), BS, 0, ctx->stream>>>(
+        n, ctx->C.m, ctx->C.h, P, &P == &ctx->P ? &ctx->dCnt->status : nullptr);
+    TSPH_LAUNCH_CK("k_gather_mass");
     // numbering
     const int levBound = nR > Fcap ? nR : Fcap;
     for (int l = topLevels - 1; l >= 0; --l) {
