@@ -220,9 +220,18 @@ __global__ void k_gather_tree(int n, TsphDevState C, TsphDevParts P, TsphDevCoun
         P.x[i] = x;
         P.y[i] = y;
         P.z[i] = z;
-        if (!isfinite(x + y + z)) atomicOr(&cnt->status, 1u << TSPH_ERR_NONFINITE);
-        a = fmax(fabs(x), fmax(fabs(y), fabs(z)));
-        if (a > limit) atomicOr(&cnt->status, 1u << TSPH_ERR_BOUNDS);
+        // the checks on the bits of |x|, |y|, |z| (they order like the
+        // values): integer instructions, not the FP64 pipe
+        const unsigned long long M = 0x7FFFFFFFFFFFFFFFULL;
+        unsigned long long b = (unsigned long long)__double_as_longlong(x) & M;
+        const unsigned long long by = (unsigned long long)__double_as_longlong(y) & M;
+        const unsigned long long bz = (unsigned long long)__double_as_longlong(z) & M;
+        b = b > by ? b : by;
+        b = b > bz ? b : bz;
+        if (b >= 0x7FF0000000000000ULL) atomicOr(&cnt->status, 1u << TSPH_ERR_NONFINITE);
+        else if (b > (unsigned long long)__double_as_longlong(limit))
+            atomicOr(&cnt->status, 1u << TSPH_ERR_BOUNDS);
+        a = __longlong_as_double((long long)b);
     }
     warp_max_abs(a, &cnt->maxAbs);
 }

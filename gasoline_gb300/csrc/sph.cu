@@ -2075,12 +2075,15 @@ __global__ void k_drift(int n, int ngas, double dt, const double *dtp, int bPeri
     if (dtp) dt *= *dtp;   // a captured step: dt is a fraction of the step in device memory
     double *r[3] = {C.x, C.y, C.z};
     const double *v[3] = {C.vx, C.vy, C.vz};
+    // the wrap tests x >= L/2 and x < -L/2 on integer order keys (the FP64
+    // pipe is left the arithmetic)
+    const unsigned long long kHi = dlt_key(0.5 * L), kLo = dlt_key(-0.5 * L);
 #pragma unroll
     for (int k = 0; k < 3; ++k) {   // no contraction: the reference's rounding
         double x = xadd(r[k][i], xmul(dt, v[k][i]));
         if (bPeriodic) {
-            if (x >= 0.5 * L) x = xsub(x, L);
-            if (x < -0.5 * L) x = xadd(x, L);
+            if (!(dlt_key(x) < kHi)) x = xsub(x, L);
+            if (dlt_key(x) < kLo) x = xadd(x, L);
         }
         r[k][i] = x;
     }
