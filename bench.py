@@ -221,11 +221,14 @@ def run_ours(args, rank, world, local_rank):
     hacc = torch.empty(3 * n, dtype=torch.float64).pin_memory()
 
     # the first evaluation of a new particle set builds its tree from the
-    # caller's order (later ones start from the last tree's order)
+    # caller's order (later ones start from the last tree's order); the
+    # context's first call (kernel loading, allocations) is made beforehand
+    gp_first = g.grav_params(periodic=True, precision=g.FP32, nBucket=NBUCKET)
+    ctx.set_particles(pos, m, soft)
+    ctx.grav_all(gp_first)
     ctx.set_particles(pos, m, soft)
     ctx.set_velocities(vel)
-    first_ms = _cuda_ms(lambda: ctx.grav_all(g.grav_params(periodic=True, precision=g.FP32,
-                                                            nBucket=NBUCKET)), stream)
+    first_ms = _cuda_ms(lambda: ctx.grav_all(gp_first), stream)
     first_build_ms = ctx.timings()["build"]
     ctx.set_particles(pos, m, soft)
     ctx.set_velocities(vel)
