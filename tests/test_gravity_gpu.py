@@ -271,6 +271,36 @@ def test_tuning_does_not_change_results():
         c.close()
 
 
+def test_large_frontier_builds_the_same_tree():
+    """The top phase's multi-block frontier path (more than 4096 frontier
+    nodes in a level: split decisions, children's bounds keys, chunk counts
+    and chunk map in separate kernels) builds the same tree and forces as
+    the single-block path: a 2.2M-particle Plummer sphere with task size
+    1024 (frontier bound 4298 from level 13 on, the dense core still
+    splitting there) against task size 65536 (at most 69 frontier nodes)."""
+    pos, vel, m = g.ics.plummer(2_200_000, seed=7)
+    soft = np.full(len(m), 1e-3)
+    gp = g.grav_params(periodic=False, precision=g.FP32)
+    ref = None
+    c = g.Context(0)
+    try:
+        for task in (65536, 1024):
+            c.set_tuning(taskSize=task)
+            c.set_particles(pos, m, soft)
+            c.grav_all(gp)
+            r = c.get_gravity()
+            t = c.get_tree()
+            if ref is None:
+                ref = (r, t)
+                continue
+            for k in range(3):          # inode, dnode, perm
+                assert np.array_equal(t[k], ref[1][k]), k
+            assert np.array_equal(r["acc"], ref[0]["acc"])
+            assert np.array_equal(r["pot"], ref[0]["pot"])
+    finally:
+        c.close()
+
+
 @pytest.mark.parametrize("case", ["plummer", "box", "clumps"])
 def test_walk_groups_keep_every_list(case):
     """Walk groups (one shared walk per subtree of at most walkGroup
