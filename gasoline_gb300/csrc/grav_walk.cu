@@ -1310,7 +1310,7 @@ __device__ __forceinline__ void eval_bucket_lists(const WalkArgs &W, Smem &S, in
 // group box lies within sqrt(fOpen2) of it (or it holds fewer than 4
 // particles); every other cell, leaves included, goes to U.
 // The FP32 tests carry the bucket walk's rounding bound, so every such
-// verdict is the one each bucket's FP64 test would reach.  Returns false
+// decision is the one each bucket's FP64 test would reach.  Returns false
 // when a list or the stack overflows (the buckets then walk from the root).
 template <typename Real, int NBT, bool HIGH>
 __device__ __noinline__ bool walk_group(const WalkArgs &W, WalkSmem<Real, NBT, HIGH> &S, int g, int b0,
