@@ -229,6 +229,41 @@ def _direct_and_graph_states(setup, dt, gp, sp, nsteps=3):
     return states
 
 
+def test_graph_step_recaptures_on_a_tuning_change():
+    """A launch shape changed between graph steps is captured anew (the
+    knobs are part of the graph): the step after the change runs the
+    preparation and the capture besides the replay, the next one replays
+    only, and the states equal direct steps with the same change."""
+    pos, vel, m = g.ics.plummer(20000, seed=9)
+    soft = np.full(len(m), 0.01)
+    gp = g.grav_params(periodic=False, precision=g.FP32)
+
+    def run(graph):
+        c = g.Context(0)
+        try:
+            c.set_particles(pos, m, soft)
+            c.set_velocities(vel)
+            c.grav_all(gp)
+            for _ in range(2):
+                c.step(1e-3, gp, None, graph=graph)
+            c.set_tuning(walkBlocksPerSM=2)
+            l0 = c.launches()
+            c.step(1e-3, gp, None, graph=graph)
+            l1 = c.launches()
+            c.step(1e-3, gp, None, graph=graph)
+            l2 = c.launches()
+            c.step_status()
+            return c.get_state(), l1 - l0, l2 - l1
+        finally:
+            c.close()
+
+    sa, _, _ = run(False)
+    sb, first, replay = run(True)
+    for k in range(3):
+        assert np.array_equal(sa[k], sb[k]), k
+    assert first > replay > 0
+
+
 def test_graph_step_periodic_ewald_equals_direct_steps():
     """A periodic box with Ewald (FP32 gravity, periodic FP32 SPH): the
     Ewald constants are rebuilt on the device from each step's root
