@@ -63,7 +63,10 @@ extern "C" int tsph_create(tsph_ctx **pctx, int device, void *stream) {
         return TSPH_ERR_NOMEM;
     }
     for (int k = 0; k < 10; ++k) cudaEventCreate(&ctx->ev[k]);
-    if (cudaEventCreateWithFlags(&ctx->evGather, cudaEventDisableTiming) != cudaSuccess) {
+    if (cudaEventCreateWithFlags(&ctx->evGather, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->evMoments, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->evEwald, cudaEventDisableTiming) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking) != cudaSuccess) {
         tsph_destroy(ctx);
         return TSPH_ERR_NOMEM;
     }
@@ -77,6 +80,7 @@ extern "C" void tsph_destroy(tsph_ctx *ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->side) cudaStreamSynchronize(ctx->side);
     TsphDevState &C = ctx->C;
     FREE(C.x); FREE(C.y); FREE(C.z); FREE(C.vx); FREE(C.vy); FREE(C.vz); FREE(C.m); FREE(C.h);
     FREE(C.u); FREE(C.vpx); FREE(C.vpy); FREE(C.vpz); FREE(C.upred); FREE(C.ax); FREE(C.ay);
@@ -122,6 +126,9 @@ extern "C" void tsph_destroy(tsph_ctx *ctx) {
     if (ctx->B.hostCount) cudaFreeHost(ctx->B.hostCount);
     for (int k = 0; k < 10; ++k) if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
     if (ctx->evGather) cudaEventDestroy(ctx->evGather);
+    if (ctx->evMoments) cudaEventDestroy(ctx->evMoments);
+    if (ctx->evEwald) cudaEventDestroy(ctx->evEwald);
+    if (ctx->side) cudaStreamDestroy(ctx->side);
     if (ctx->ownStream && ctx->stream) cudaStreamDestroy(ctx->stream);
     free(ctx);
 }
@@ -470,9 +477,17 @@ extern "C" int tsph_grav_all(tsph_ctx *ctx, const tsph_grav_params *gp, tsph_gra
     rc = tsph_tree_moments(ctx, ctx->P, ctx->T, n, gp->dTheta, gp->iOrder);
     if (rc) return rc;
     const bool ewald = n > 0 && gp->bPeriodic && gp->bEwald && gp->iEwOrder >= 1;
-    if (ewald) {   // the root moments now, so the host has them while the walk runs
-        rc = tsph_ewald_roots(ctx, gp);
-        if (rc) return rc;
+    if (ewald) {
+        // the root multipoles and the Ewald constants need only the root
+        // cell: a second stream builds them beside the Bmax and opening
+        // passes, from the moments' completion to the Ewald pass
+        TSPH_CK(cudaStreamWaitEvent(ctx->side, ctx->evMoments, 0));
+        rc = tsph_ewald_roots(ctx, gp, ctx->side);
+        TSPH_CK(cudaEventRecord(ctx->evEwald, ctx->side));   // the merge, error or not
+        if (rc) {
+            TSPH_CK(cudaStreamWaitEvent(ctx->stream, ctx->evEwald, 0));
+            return rc;
+        }
     }
     if (!cap) cudaEventRecord(ctx->ev[2], ctx->stream);
     ctx->haveTree = true;
@@ -491,6 +506,7 @@ extern "C" int tsph_grav_all(tsph_ctx *ctx, const tsph_grav_params *gp, tsph_gra
         if (rc) return rc;
     }
     if (!cap) cudaEventRecord(ctx->ev[3], ctx->stream);
+    if (ewald) TSPH_CK(cudaStreamWaitEvent(ctx->stream, ctx->evEwald, 0));
     if (n > 0) {
         if (ewald) rc = tsph_ewald(ctx, gp);
         else if (gp->precision == TSPH_FP32 && ctx->T.nLeaves > 0) rc = tsph_walk_finish_f32(ctx);

@@ -768,7 +768,7 @@ static int ewald_table_size(double fEwhCut) {
 // Root moments (pkdCalcRoot) and then every Ewald constant, on the device
 // right after the cell moments; the constants land in the constant bank by
 // a device-to-device copy, so no step of the evaluation waits for the host.
-int tsph_ewald_roots(tsph_ctx *ctx, const tsph_grav_params *gp) {
+int tsph_ewald_roots(tsph_ctx *ctx, const tsph_grav_params *gp, cudaStream_t s) {
     if (!(gp->bPeriodic && gp->bEwald) || gp->iEwOrder < 1) return TSPH_OK;
     if (gp->iEwOrder > 4) return TSPH_ERR_ARG;
     const int n = ctx->n;
@@ -794,20 +794,20 @@ int tsph_ewald_roots(tsph_ctx *ctx, const tsph_grav_params *gp) {
     int nb = 256;
     double *partial = ctx->dRoot + 64;
     if (gp->precision == TSPH_FP32) {
-        k_root_partial<float><<<nb, RM_BS, 0, ctx->stream>>>(n, ctx->P.x, ctx->P.y, ctx->P.z,
+        k_root_partial<float><<<nb, RM_BS, 0, s>>>(n, ctx->P.x, ctx->P.y, ctx->P.z,
                                                              ctx->P.m, ctx->T.r, partial);
         TSPH_LAUNCH_CK("k_root_partial<f32>");
     } else {
-        k_root_partial<double><<<nb, RM_BS, 0, ctx->stream>>>(n, ctx->P.x, ctx->P.y, ctx->P.z,
+        k_root_partial<double><<<nb, RM_BS, 0, s>>>(n, ctx->P.x, ctx->P.y, ctx->P.z,
                                                               ctx->P.m, ctx->T.r, partial);
         TSPH_LAUNCH_CK("k_root_partial<f64>");
     }
-    k_root_final<<<1, 32, 0, ctx->stream>>>(nb, partial, ctx->dRoot);
+    k_root_final<<<1, 32, 0, s>>>(nb, partial, ctx->dRoot);
     TSPH_LAUNCH_CK("k_root_final");
     EwConst *dE = static_cast<EwConst *>(ctx->dEw);
-    k_ewald_const<<<1, EWC_BS, 0, ctx->stream>>>(p, ctx->dRoot, ctx->T, ctx->dCnt, dE);
+    k_ewald_const<<<1, EWC_BS, 0, s>>>(p, ctx->dRoot, ctx->T, ctx->dCnt, dE);
     TSPH_LAUNCH_CK("k_ewald_const");
-    TSPH_CK(cudaMemcpyToSymbolAsync(cE, dE, sizeof(EwConst), 0, cudaMemcpyDeviceToDevice, ctx->stream));
+    TSPH_CK(cudaMemcpyToSymbolAsync(cE, dE, sizeof(EwConst), 0, cudaMemcpyDeviceToDevice, s));
     return TSPH_OK;
 }
 

@@ -2119,6 +2119,7 @@ int tsph_tree_moments(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, dou
     TSPH_CK(cudaMemsetAsync(B.visit, 0, sizeof(int) * (size_t)nodeNeed, ctx->stream));
     k_moments<<<tsph_blocks(n, 128), 128, 0, ctx->stream>>>(T, P.x, P.y, P.z, P.m, P.h, B.visit, high);
     TSPH_LAUNCH_CK("k_moments");
+    TSPH_CK(cudaEventRecord(ctx->evMoments, ctx->stream));   // the root cell is final
     k_parts32<<<tsph_blocks(n, BS), BS, 0, ctx->stream>>>(n, P.x, P.y, P.z, P.m, P.h, P.ph, P.pl);
     TSPH_LAUNCH_CK("k_parts32");
     k_zero_u64<<<tsph_blocks(nodeNeed, BS), BS, 0, ctx->stream>>>(B.maxd2, nodeNeed);

@@ -125,6 +125,8 @@ struct tsph_ctx {
     double *dRoot;               // 35 doubles: root complete moments
     void *dEw;                   // the Ewald constants, built on the device (EwConst)
     cudaEvent_t evGather;        // the gather's status and coordinate scale are on the host
+    cudaStream_t side;           // the Ewald constants beside the Bmax pass
+    cudaEvent_t evMoments, evEwald;   // their branch (moments done) and merge
     int nEwt;                    // k-space vectors kept (a function of fEwhCut only)
 
     // input staging (caller order)
@@ -262,7 +264,7 @@ int tsph_copy_out_n(tsph_ctx *ctx, int n, const double *a0, const double *a1, co
 void tsph_free_tree(TsphDevTree &T);
 int tsph_walk_interact(tsph_ctx *ctx, const tsph_grav_params *gp);
 int tsph_walk_finish_f32(tsph_ctx *ctx);
-int tsph_ewald_roots(tsph_ctx *ctx, const tsph_grav_params *gp);
+int tsph_ewald_roots(tsph_ctx *ctx, const tsph_grav_params *gp, cudaStream_t s);
 int tsph_ewald(tsph_ctx *ctx, const tsph_grav_params *gp);
 int tsph_ensure_particles(tsph_ctx *ctx, int n);
 int tsph_sph_density(tsph_ctx *ctx, const tsph_sph_params *sp, tsph_smooth_out *out);
