@@ -64,7 +64,10 @@ extern "C" int tsph_create(tsph_ctx **pctx, int device, void *stream) {
     }
     for (int k = 0; k < 10; ++k) cudaEventCreate(&ctx->ev[k]);
     if (cudaEventCreateWithFlags(&ctx->evGather, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->evBuilt, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->evParts, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->evMoments, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->evPrep, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->evEwald, cudaEventDisableTiming) != cudaSuccess ||
         cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking) != cudaSuccess) {
         tsph_destroy(ctx);
@@ -126,8 +129,8 @@ extern "C" void tsph_destroy(tsph_ctx *ctx) {
     if (ctx->B.hostCount) cudaFreeHost(ctx->B.hostCount);
     for (int k = 0; k < 10; ++k) if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
     if (ctx->evGather) cudaEventDestroy(ctx->evGather);
-    if (ctx->evMoments) cudaEventDestroy(ctx->evMoments);
-    if (ctx->evEwald) cudaEventDestroy(ctx->evEwald);
+    cudaEvent_t *evs[5] = {&ctx->evBuilt, &ctx->evParts, &ctx->evMoments, &ctx->evPrep, &ctx->evEwald};
+    for (cudaEvent_t *e : evs) if (*e) cudaEventDestroy(*e);
     if (ctx->side) cudaStreamDestroy(ctx->side);
     if (ctx->ownStream && ctx->stream) cudaStreamDestroy(ctx->stream);
     free(ctx);
@@ -477,15 +480,28 @@ extern "C" int tsph_grav_all(tsph_ctx *ctx, const tsph_grav_params *gp, tsph_gra
     rc = tsph_tree_moments(ctx, ctx->P, ctx->T, n, gp->dTheta, gp->iOrder);
     if (rc) return rc;
     const bool ewald = n > 0 && gp->bPeriodic && gp->bEwald && gp->iEwOrder >= 1;
+    // from the moments' completion a second stream prepares the walk's
+    // bucket geometry and (periodic) the root multipoles and Ewald
+    // constants, beside the Bmax and opening passes; the walk and the
+    // Ewald pass wait for them
+    if (n > 0 && ctx->T.nLeaves > 0) {
+        TSPH_CK(cudaStreamWaitEvent(ctx->side, ctx->evMoments, 0));
+        rc = tsph_bucket_prep(ctx, ctx->side);
+        TSPH_CK(cudaEventRecord(ctx->evPrep, ctx->side));
+        if (rc) {
+            TSPH_CK(cudaStreamWaitEvent(ctx->stream, ctx->evPrep, 0));
+            return rc;
+        }
+        ctx->bucketPrepQueued = true;
+    }
     if (ewald) {
-        // the root multipoles and the Ewald constants need only the root
-        // cell: a second stream builds them beside the Bmax and opening
-        // passes, from the moments' completion to the Ewald pass
         TSPH_CK(cudaStreamWaitEvent(ctx->side, ctx->evMoments, 0));
         rc = tsph_ewald_roots(ctx, gp, ctx->side);
         TSPH_CK(cudaEventRecord(ctx->evEwald, ctx->side));   // the merge, error or not
         if (rc) {
             TSPH_CK(cudaStreamWaitEvent(ctx->stream, ctx->evEwald, 0));
+            if (ctx->bucketPrepQueued) TSPH_CK(cudaStreamWaitEvent(ctx->stream, ctx->evPrep, 0));
+            ctx->bucketPrepQueued = false;
             return rc;
         }
     }
@@ -503,6 +519,7 @@ extern "C" int tsph_grav_all(tsph_ctx *ctx, const tsph_grav_params *gp, tsph_gra
     }
     if (n > 0 && ctx->T.nLeaves > 0) {
         rc = tsph_walk_interact(ctx, gp);
+        ctx->bucketPrepQueued = false;
         if (rc) return rc;
     }
     if (!cap) cudaEventRecord(ctx->ev[3], ctx->stream);

@@ -1886,6 +1886,13 @@ static int launch_walk(tsph_ctx *ctx, const WalkArgs &A, int blocks, const char 
     return TSPH_OK;
 }
 
+// The walk's per-bucket geometry (k_bucket_prep) on stream s.
+int tsph_bucket_prep(tsph_ctx *ctx, cudaStream_t s) {
+    k_bucket_prep<<<tsph_blocks(ctx->T.nLeaves, 128), 128, 0, s>>>(ctx->T, ctx->P);
+    TSPH_LAUNCH_CK("k_bucket_prep");
+    return TSPH_OK;
+}
+
 int tsph_walk_interact(tsph_ctx *ctx, const tsph_grav_params *gp) {
     if (gp->iOrder < 1 || gp->iOrder > 4) return TSPH_ERR_ARG;
     if (gp->bPeriodic && gp->nReps > 1) return TSPH_ERR_UNSUPPORTED;
@@ -1943,8 +1950,12 @@ int tsph_walk_interact(tsph_ctx *ctx, const tsph_grav_params *gp) {
     // work counter lives in the counters block's pad area
     A.workCounter = (int *)&ctx->dCnt->pad;
     TSPH_CK(cudaMemsetAsync(A.workCounter, 0, sizeof(int), ctx->stream));
-    k_bucket_prep<<<tsph_blocks(nbHost, 128), 128, 0, ctx->stream>>>(ctx->T, ctx->P);
-    TSPH_LAUNCH_CK("k_bucket_prep");
+    if (ctx->bucketPrepQueued) {   // prepared on the side stream beside the moments
+        TSPH_CK(cudaStreamWaitEvent(ctx->stream, ctx->evPrep, 0));
+    } else {
+        rc = tsph_bucket_prep(ctx, ctx->stream);
+        if (rc) return rc;
+    }
     const int wbDefault = gp->precision == TSPH_FP32 ? (gp->iOrder >= 3 ? 3 : 5) : 4;
     int blocks = ctx->smCount * (ctx->walkBlocksPerSM > 0 ? ctx->walkBlocksPerSM : wbDefault);
     A.groupFirst = nullptr;

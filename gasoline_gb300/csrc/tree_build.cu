@@ -2116,12 +2116,18 @@ int tsph_tree_moments(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, dou
         if (rc) return TSPH_ERR_NOMEM;
         T.highCap = T.cap;
     }
+    // the FP32 particle records on the side stream beside k_moments (FP64
+    // bound at low issue); the Bmax passes wait for them
+    TSPH_CK(cudaEventRecord(ctx->evBuilt, ctx->stream));
+    TSPH_CK(cudaStreamWaitEvent(ctx->side, ctx->evBuilt, 0));
+    k_parts32<<<tsph_blocks(n, BS), BS, 0, ctx->side>>>(n, P.x, P.y, P.z, P.m, P.h, P.ph, P.pl);
+    TSPH_LAUNCH_CK("k_parts32");
+    TSPH_CK(cudaEventRecord(ctx->evParts, ctx->side));
     TSPH_CK(cudaMemsetAsync(B.visit, 0, sizeof(int) * (size_t)nodeNeed, ctx->stream));
     k_moments<<<tsph_blocks(n, 128), 128, 0, ctx->stream>>>(T, P.x, P.y, P.z, P.m, P.h, B.visit, high);
     TSPH_LAUNCH_CK("k_moments");
     TSPH_CK(cudaEventRecord(ctx->evMoments, ctx->stream));   // the root cell is final
-    k_parts32<<<tsph_blocks(n, BS), BS, 0, ctx->stream>>>(n, P.x, P.y, P.z, P.m, P.h, P.ph, P.pl);
-    TSPH_LAUNCH_CK("k_parts32");
+    TSPH_CK(cudaStreamWaitEvent(ctx->stream, ctx->evParts, 0));
     k_zero_u64<<<tsph_blocks(nodeNeed, BS), BS, 0, ctx->stream>>>(B.maxd2, nodeNeed);
     TSPH_LAUNCH_CK("k_zero_u64");
     // the per-node arrival counters of k_moments are free again: max of lo

@@ -125,8 +125,10 @@ struct tsph_ctx {
     double *dRoot;               // 35 doubles: root complete moments
     void *dEw;                   // the Ewald constants, built on the device (EwConst)
     cudaEvent_t evGather;        // the gather's status and coordinate scale are on the host
-    cudaStream_t side;           // the Ewald constants beside the Bmax pass
-    cudaEvent_t evMoments, evEwald;   // their branch (moments done) and merge
+    cudaStream_t side;           // work beside the moments: FP32 particle records, bucket
+                                 // geometry, Ewald constants
+    cudaEvent_t evBuilt, evParts, evMoments, evPrep, evEwald;   // its branches and merges
+    bool bucketPrepQueued;       // the walk's bucket geometry is queued on the side stream
     int nEwt;                    // k-space vectors kept (a function of fEwhCut only)
 
     // input staging (caller order)
@@ -263,6 +265,7 @@ int tsph_copy_out_n(tsph_ctx *ctx, int n, const double *a0, const double *a1, co
                     int comp, double *host);
 void tsph_free_tree(TsphDevTree &T);
 int tsph_walk_interact(tsph_ctx *ctx, const tsph_grav_params *gp);
+int tsph_bucket_prep(tsph_ctx *ctx, cudaStream_t s);
 int tsph_walk_finish_f32(tsph_ctx *ctx);
 int tsph_ewald_roots(tsph_ctx *ctx, const tsph_grav_params *gp, cudaStream_t s);
 int tsph_ewald(tsph_ctx *ctx, const tsph_grav_params *gp);
