@@ -1194,6 +1194,7 @@ __global__ void k_scatter_nodes(int topCap, int tcap, const TsphBuildCtl *__rest
 #pragma unroll
     for (int k = 0; k < 6; ++k) T.bnd[6 * i + k] = t_bnd[6 * v + k];
     T.upper[i] = c >= 0 ? t_pre[c + 1] : -1;
+    T.dlink[i] = c >= 0 ? make_int2(t_pre[c + 1], t_lo[c + 1]) : make_int2(-1, 0);
     int nx = i + t_size[v];
     T.skip[i] = nx < T.rEnd[rid[t_lo[v]]] ? nx : -1;
     leafFlag[i] = c < 0 ? 1 : 0;
@@ -1508,9 +1509,9 @@ __global__ void k_bmax_lo(int n, TsphDevTree T, const float4 *__restrict__ ph,
             unsigned grp = __match_any_sync(mask, i);
             unsigned m = __reduce_max_sync(grp, __float_as_uint(lo));
             if ((int)(threadIdx.x & 31) == __ffs(grp) - 1) atomicMax(&maxLo[i], m);
-            int up = T.upper[i];
-            if (up < 0) live = false;
-            else i = (p >= T.pLower[up]) ? up : i + 1;
+            const int2 dl = T.dlink[i];
+            if (dl.x < 0) live = false;
+            else i = (p >= dl.y) ? dl.x : i + 1;
         }
         mask = __ballot_sync(0xffffffffu, live);
     }
@@ -1535,9 +1536,9 @@ __global__ void k_bmax_exact(int n, TsphDevTree T, const double *__restrict__ x,
             double d2 = xadd(xadd(xmul(dx, dx), xmul(dy, dy)), xmul(dz, dz));
             atomicMax(&maxd2[i], (unsigned long long)__double_as_longlong(d2));
         }
-        int up = T.upper[i];
-        if (up < 0) break;
-        i = (p >= T.pLower[up]) ? up : i + 1;
+        const int2 dl = T.dlink[i];
+        if (dl.x < 0) break;
+        i = (p >= dl.y) ? dl.x : i + 1;
     }
 }
 
@@ -1634,7 +1635,7 @@ __global__ void k_parts32(int n, const double *__restrict__ x, const double *__r
 // ---------------------------------------------------------------------------
 #define TFREE(p) do { if (p) cudaFree(p); (p) = nullptr; } while (0)
 void tsph_free_tree(TsphDevTree &T) {
-    TFREE(T.pLower); TFREE(T.pUpper); TFREE(T.iDim); TFREE(T.upper); TFREE(T.skip);
+    TFREE(T.pLower); TFREE(T.pUpper); TFREE(T.iDim); TFREE(T.upper); TFREE(T.dlink); TFREE(T.skip);
     TFREE(T.fSplit); TFREE(T.bnd); TFREE(T.fMass); TFREE(T.fSoft); TFREE(T.r);
     TFREE(T.fOpen2); TFREE(T.Bmax); TFREE(T.Q); TFREE(T.wcomh); TFREE(T.wcoml);
     TFREE(T.wlink); TFREE(T.wmom0); TFREE(T.wmom1); TFREE(T.leaves); TFREE(T.parent);
@@ -1673,6 +1674,7 @@ static int ensure_nodes(tsph_ctx *ctx, TsphDevTree &T, int nNodes) {
         rc |= tsph_grow(ctx, &T.pUpper, cap);
         rc |= tsph_grow(ctx, &T.iDim, cap);
         rc |= tsph_grow(ctx, &T.upper, cap);
+        rc |= tsph_grow(ctx, &T.dlink, cap);
         rc |= tsph_grow(ctx, &T.skip, cap);
         rc |= tsph_grow(ctx, &T.parent, cap);
         rc |= tsph_grow(ctx, &T.fSplit, cap);

@@ -65,6 +65,7 @@ struct TsphDevTree {
     // node arrays, depth-first (reference) order
     int *pLower, *pUpper, *iDim;
     int *upper;       // upper child index, -1 for a leaf
+    int2 *dlink;      // (upper child, its first particle): one load a level of a descent
     int *skip;        // node after this subtree, -1 at the end (threaded "next")
     double *fSplit;
     double *bnd;      // 6 per node: min xyz, max xyz
