@@ -394,6 +394,42 @@ def test_nonfinite_input_reports_error_and_context_survives(ctx):
     assert rms(rel_err(r["acc"], d["acc"])) < FP64_RMS
 
 
+@pytest.mark.parametrize("field", ["mass", "soft"])
+def test_nonfinite_mass_or_softening_reports_error(ctx, field):
+    """A non-finite mass or softening (checked when they are gathered in
+    tree order after the build) is bad input: the call returns
+    TSPH_ERR_NONFINITE and the context still evaluates the next set."""
+    rng = np.random.default_rng(1)
+    pos = rng.uniform(-1, 1, (500, 3))
+    m = np.full(500, 0.002)
+    soft = np.full(500, 0.01)
+    (m if field == "mass" else soft)[123] = np.inf
+    ctx.set_particles(pos, m, soft)
+    with pytest.raises(g.TsphError) as ei:
+        ctx.grav_all(g.grav_params(periodic=False))
+    assert ei.value.code == 6
+    d = load("grav_plummer_2k")
+    r = run(ctx, d["pos"], d["mass"], d["soft"], grav_params_of(d, g))
+    assert rms(rel_err(r["acc"], d["acc"])) < FP64_RMS
+
+
+def test_coincident_particles_beyond_a_warp_are_refused(ctx):
+    """More than 32 particles at one point make a zero-extent leaf larger
+    than one walk warp's lanes: the walk refuses it with
+    TSPH_ERR_UNSUPPORTED instead of reading past its bucket, and the
+    context still evaluates the next set."""
+    rng = np.random.default_rng(2)
+    pos = rng.uniform(-1, 1, (400, 3))
+    pos[:40] = 0.25                     # 40 coincident particles
+    ctx.set_particles(pos, np.full(400, 0.0025), np.full(400, 0.01))
+    with pytest.raises(g.TsphError) as ei:
+        ctx.grav_all(g.grav_params(periodic=False, nBucket=16))
+    assert ei.value.code == 7           # TSPH_ERR_UNSUPPORTED
+    d = load("grav_plummer_2k")
+    r = run(ctx, d["pos"], d["mass"], d["soft"], grav_params_of(d, g))
+    assert rms(rel_err(r["acc"], d["acc"])) < FP64_RMS
+
+
 def test_exact_fallback_is_rare(ctx):
     pos, vel, m = g.ics.lattice_box(16, seed=3)
     ctx.set_particles(pos, m, np.full(len(m), 1e-3))
