@@ -1258,35 +1258,41 @@ __host__ __device__ constexpr int m3_index(int a, int b, int c) {
            code == 14 ? 5 : code == 5 ? 6 : code == 8 ? 7 : code == 17 ? 8 : 9;
 }
 
+// A particle's complete third and fourth moments about the leaf's centre
+// of mass, added to m3 (xxx xyy xxy yyy xxz yyz xyz xzz yzz zzz) and m4
+// (xxxx xyyy xxxy yyyy xxxz yyyz xxyy xxyz xyyz xxzz xyzz xzzz yyzz yzzz
+// zzzz): fused multiply-adds on shared products, 37 FP64 operations (they
+// are checked to rounding, as the parents' binomial shifts are).
 __device__ __forceinline__ void leaf_high(const double *d, double m, double *m3, double *m4) {
     const double x = d[0], y = d[1], z = d[2];
-    const double xx = xmul(x, x), yy = xmul(y, y), zz = xmul(z, z);
-    const double mx = xmul(m, x), my = xmul(m, y), mz = xmul(m, z);
-    m3[0] = xadd(m3[0], xmul(mx, xx));
-    m3[1] = xadd(m3[1], xmul(mx, yy));
-    m3[2] = xadd(m3[2], xmul(my, xx));
-    m3[3] = xadd(m3[3], xmul(my, yy));
-    m3[4] = xadd(m3[4], xmul(mz, xx));
-    m3[5] = xadd(m3[5], xmul(mz, yy));
-    m3[6] = xadd(m3[6], xmul(xmul(mx, y), z));
-    m3[7] = xadd(m3[7], xmul(mx, zz));
-    m3[8] = xadd(m3[8], xmul(my, zz));
-    m3[9] = xadd(m3[9], xmul(mz, zz));
-    m4[0] = xadd(m4[0], xmul(xmul(m, xx), xx));
-    m4[1] = xadd(m4[1], xmul(xmul(mx, yy), y));
-    m4[2] = xadd(m4[2], xmul(xmul(mx, xx), y));
-    m4[3] = xadd(m4[3], xmul(xmul(m, yy), yy));
-    m4[4] = xadd(m4[4], xmul(xmul(mx, xx), z));
-    m4[5] = xadd(m4[5], xmul(xmul(my, yy), z));
-    m4[6] = xadd(m4[6], xmul(xmul(m, xx), yy));
-    m4[7] = xadd(m4[7], xmul(xmul(m, xx), xmul(y, z)));
-    m4[8] = xadd(m4[8], xmul(xmul(mx, yy), z));
-    m4[9] = xadd(m4[9], xmul(xmul(m, xx), zz));
-    m4[10] = xadd(m4[10], xmul(xmul(mx, y), zz));
-    m4[11] = xadd(m4[11], xmul(xmul(mx, zz), z));
-    m4[12] = xadd(m4[12], xmul(xmul(m, yy), zz));
-    m4[13] = xadd(m4[13], xmul(xmul(my, zz), z));
-    m4[14] = xadd(m4[14], xmul(xmul(m, zz), zz));
+    const double xx = x * x, yy = y * y, zz = z * z, xy = x * y, xz = x * z, yz = y * z;
+    const double mx = m * x, my = m * y, mz = m * z;
+    m3[0] = fma(mx, xx, m3[0]);
+    m3[1] = fma(mx, yy, m3[1]);
+    m3[2] = fma(my, xx, m3[2]);
+    m3[3] = fma(my, yy, m3[3]);
+    m3[4] = fma(mz, xx, m3[4]);
+    m3[5] = fma(mz, yy, m3[5]);
+    m3[6] = fma(mx, yz, m3[6]);
+    m3[7] = fma(mx, zz, m3[7]);
+    m3[8] = fma(my, zz, m3[8]);
+    m3[9] = fma(mz, zz, m3[9]);
+    const double mxx = m * xx, myy = m * yy, mzz = m * zz;
+    m4[0] = fma(mxx, xx, m4[0]);
+    m4[1] = fma(myy, xy, m4[1]);
+    m4[2] = fma(mxx, xy, m4[2]);
+    m4[3] = fma(myy, yy, m4[3]);
+    m4[4] = fma(mxx, xz, m4[4]);
+    m4[5] = fma(myy, yz, m4[5]);
+    m4[6] = fma(mxx, yy, m4[6]);
+    m4[7] = fma(mxx, yz, m4[7]);
+    m4[8] = fma(myy, xz, m4[8]);
+    m4[9] = fma(mxx, zz, m4[9]);
+    m4[10] = fma(mzz, xy, m4[10]);
+    m4[11] = fma(mzz, xz, m4[11]);
+    m4[12] = fma(myy, zz, m4[12]);
+    m4[13] = fma(mzz, yz, m4[13]);
+    m4[14] = fma(mzz, zz, m4[14]);
 }
 
 // Child moments (mass m, complete Q, M3, M4 about its own centre) shifted
