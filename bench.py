@@ -589,7 +589,7 @@ def run_profile(args):
     pos, vel, m, soft = workload(args.ng, with_vel=True)
     ctx.set_particles(pos, m, soft)
     ctx.set_velocities(vel)
-    gp = g.grav_params(periodic=True, precision=g.FP32, nBucket=NBUCKET)
+    gp = g.grav_params(periodic=True, precision=g.FP32, nBucket=NBUCKET, iOrder=args.iorder)
     ctx.grav_all(gp)
     sgn = -1.0
     for _ in range(args.warmup):
@@ -601,7 +601,7 @@ def run_profile(args):
         ms.append(_cuda_ms(lambda: ctx.step(sgn * DRIFT_DT, gp, None, graph=True), stream))
     ctx.step_status()
     ctx.close()
-    return {"profile": "box", "n_particles": len(m), "nBucket": NBUCKET,
+    return {"profile": "box", "n_particles": len(m), "nBucket": NBUCKET, "iOrder": args.iorder,
             "ms_per_step": statistics.mean(ms)}
 
 
@@ -1062,6 +1062,8 @@ def main():
     ap.add_argument("--profile", action="store_true",
                     help="box FP32 evaluations only (the ncu capture command)")
     ap.add_argument("--sph-fp32", action="store_true")
+    ap.add_argument("--iorder", type=int, default=2,
+                    help="cell multipole order of the profile leg (4: the reference's default)")
     ap.add_argument("--walk-lists", type=int, default=0,
                     help="--profile: the walk mode (tsph_tuning.walkLists; 1 = two passes)")
     ap.add_argument("--collapse-n", type=int, default=262144)
