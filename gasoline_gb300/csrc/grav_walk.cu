@@ -88,7 +88,9 @@ __device__ __forceinline__ void rep_off64(int r, double *o) {
 // q01 = (xx0, xx1, yy0, yy1), q23 = (zz0, zz1, xy0, xy1),
 // q45 = (xz0, xz1, yz0, yz1), h = (h0, h1).
 // HIGH (octopole and hexadecapole cells, iOrder >= 3): cell tiles of 32,
-// with the 25 reduced moments of every entry in oh[k][entry].
+// with the 25 reduced moments of every entry in oh[k][entry] (FP32: the
+// octopole scaled by -15/2 and the hexadecapole by 35/2, the factors of
+// the packed evaluation).
 template <bool HIGH>
 __host__ __device__ constexpr int cell_tile() { return HIGH ? 32 : CNF; }
 
@@ -515,14 +517,15 @@ __device__ __forceinline__ void stage_cells(Smem &S, const int *buf, const TsphD
             S.D.cn.q45[p] = make_float4(f0[8], f1[8], f0[9], f1[9]);
             S.D.cn.h[p] = make_float2(f0[10], f1[10]);
             if constexpr (HIGH) {
-                if (!soft) {   // reduced octopole and hexadecapole of both entries
+                if (!soft) {   // reduced octopole (x -15/2) and hexadecapole (x 35/2) of both entries
                     const float *o0 = T.wOH + 25 * (size_t)(buf[2 * p] >> 5);
                     const bool two = 2 * p + 1 < cnt;
                     const float *o1 = T.wOH + 25 * (size_t)(two ? buf[2 * p + 1] >> 5 : 0);
 #pragma unroll
                     for (int k = 0; k < 25; ++k) {
-                        S.D.cn.oh[k][2 * p] = o0[k];
-                        S.D.cn.oh[k][2 * p + 1] = two ? o1[k] : 0.0f;
+                        const float sc = k < 10 ? -7.5f : 17.5f;
+                        S.D.cn.oh[k][2 * p] = sc * o0[k];
+                        S.D.cn.oh[k][2 * p + 1] = two ? sc * o1[k] : 0.0f;
                     }
                 }
             }
@@ -620,37 +623,21 @@ __device__ __forceinline__ void qeval_cell(int iOrder, Real m, const Real *q, co
     az -= dz * Qta;
 }
 
-// Newtonian cells of a HIGH tile (iOrder >= 3), one cell per lane step, in
-// the precision of the walk; terms folded into the compensated sums.
+// FP64 Newtonian cells of a HIGH tile (iOrder >= 3), one cell per lane
+// step, by QEVAL in the reference's form.
 template <typename Real, int NBT, bool HIGH, class Smem>
 __device__ __forceinline__ void eval_newt_high(Smem &S, int cnt, int i, int slot,
                                                int iOrder, Acc<Real> &A) {
     const Real xi = S.px[i], yi = S.py[i], zi = S.pz[i], mi = S.pm[i];
     for (int e = slot; e < cnt; e += 32 / NBT) {
-        Real cx, cy, cz, m, q[6], o[10], h[15];
-        if constexpr (sizeof(Real) == 4) {
-            const int p = e >> 1, k = e & 1;
-            const float4 a = S.D.cn.xy[p], b = S.D.cn.zm[p];
-            const float4 q01 = S.D.cn.q01[p], q23 = S.D.cn.q23[p], q45 = S.D.cn.q45[p];
-            cx = k ? a.y : a.x; cy = k ? a.w : a.z; cz = k ? b.y : b.x; m = k ? b.w : b.z;
-            q[0] = k ? q01.y : q01.x; q[1] = k ? q01.w : q01.z; q[2] = k ? q23.y : q23.x;
-            q[3] = k ? q23.w : q23.z; q[4] = k ? q45.y : q45.x; q[5] = k ? q45.w : q45.z;
-        } else {
-            cx = S.D.ex[e]; cy = S.D.ey[e]; cz = S.D.ez[e]; m = S.D.em[e];
+        Real q[6], o[10], h[15];
+        const Real cx = S.D.ex[e], cy = S.D.ey[e], cz = S.D.ez[e], m = S.D.em[e];
 #pragma unroll
-            for (int k = 0; k < 6; ++k) q[k] = S.D.q[k][e];
-        }
-        if constexpr (sizeof(Real) == 4) {
+        for (int k = 0; k < 6; ++k) q[k] = S.D.q[k][e];
 #pragma unroll
-            for (int k = 0; k < 10; ++k) o[k] = S.D.cn.oh[k][e];
+        for (int k = 0; k < 10; ++k) o[k] = S.D.oh[k][e];
 #pragma unroll
-            for (int k = 0; k < 15; ++k) h[k] = S.D.cn.oh[10 + k][e];
-        } else {
-#pragma unroll
-            for (int k = 0; k < 10; ++k) o[k] = S.D.oh[k][e];
-#pragma unroll
-            for (int k = 0; k < 15; ++k) h[k] = S.D.oh[10 + k][e];
-        }
+        for (int k = 0; k < 15; ++k) h[k] = S.D.oh[10 + k][e];
         const Real dx = xi - cx, dy = yi - cy, dz = zi - cz;
         const Real d2 = dx * dx + dy * dy + dz * dz;
         Real gam[6];
@@ -666,11 +653,125 @@ __device__ __forceinline__ void eval_newt_high(Smem &S, int cnt, int i, int slot
         kahan_add(A.s[0], A.c[0], ax);
         kahan_add(A.s[1], A.c[1], ay);
         kahan_add(A.s[2], A.c[2], az);
-        if constexpr (sizeof(Real) == 4) kahan_add(A.s[3], A.c[3], pot);
-        else A.t[3] += pot;
+        A.t[3] += pot;
         const Real idt2 = (mi + m) * gam[1];
         A.dt = idt2 > A.dt ? idt2 : A.dt;
     }
+}
+
+// FP32 Newtonian cells of a HIGH tile for particle i, two cells per packed
+// instruction: QEVAL (qeval.h:21-64) at order 3, or with HEX at order 4,
+// restated on the unit vector n = d / r (d = cell - particle, the
+// reference's dx with the sign flipped; ir = 1/r), so that no power of r
+// is formed unscaled:
+//   W2 = 3 Q.n,  W3 = -15/2 O:nn,  W4 = 35/2 H:nnn,  p_k = W_k . n,
+//   E  = (W2 - 5/2 p2 n) + ir ((W3 - 7/3 p3 n) + ir (W4 - 9/4 p4 n)),
+//   a += m ir^2 n - ir^4 E,
+//   -pot = m ir + ir^3 (p2 / 2 + ir (p3 / 3 + ir p4 / 4)),
+// which is the reference's gamma series (g_k = (2k-1)!! / r^(2k+1)) with
+// its Qmir vectors and scalars regrouped by powers of 1/r.  The factors
+// -15/2 and 35/2 are applied to O and H when the tile is staged; the
+// monomials carry the multiplicities of the symmetric contractions (2 for
+// xy, 3 for xxy, 6 for xyz).  The odd tile's massless partner (FAR_ENTRY,
+// zero moments) adds exactly zero: its n is finite and ir^3 underflows.
+template <int NBT, bool HEX, class Smem>
+__device__ __forceinline__ void newt_tile_f32_high(Smem &S, int cnt, int i, int slot, Acc<float> &A) {
+    const float2 X = p_splat(S.px[i]), Y = p_splat(S.py[i]), Z = p_splat(S.pz[i]);
+    const float2 M = p_splat(S.pm[i]);
+    const float2 c3 = p_splat(3.0f), cm52 = p_splat(-2.5f), cm73 = p_splat(-7.0f / 3.0f);
+    const float2 cm94 = p_splat(-2.25f), ch = p_splat(0.5f), c13 = p_splat(1.0f / 3.0f);
+    const float2 c14 = p_splat(0.25f);
+    float2 tx = p_splat(0.0f), ty = tx, tz = tx;   // monopole: m ir^2 n
+    float2 ux = tx, uy = tx, uz = tx;              // ir^4 E
+    float2 tp = tx;                                // minus the potential
+    float dt = A.dt;
+    constexpr int RS = cell_tile<true>() / 2;      // float2 pairs per moment row
+    const float2 *oh = reinterpret_cast<const float2 *>(&S.D.cn.oh[0][0]);
+    const int np = (cnt + 1) >> 1;
+#pragma unroll 1
+    for (int p = slot; p < np; p += 32 / NBT) {
+        const float4 a = S.D.cn.xy[p], b = S.D.cn.zm[p];
+        const float2 dx = p_sub(make_float2(a.x, a.y), X);
+        const float2 dy = p_sub(make_float2(a.z, a.w), Y);
+        const float2 dz = p_sub(make_float2(b.x, b.y), Z);
+        const float2 m = make_float2(b.z, b.w);
+        const float2 d2 = p_fma(dz, dz, p_fma(dy, dy, p_mul(dx, dx)));
+        const float2 ir = p_rsqrt(d2);
+        const float2 ir2 = p_mul(ir, ir);
+        const float2 nx = p_mul(dx, ir), ny = p_mul(dy, ir), nz = p_mul(dz, ir);
+        const float2 n3x = p_mul(c3, nx), n3y = p_mul(c3, ny), n3z = p_mul(c3, nz);
+        // W2 = 3 Q.n (Q: xx yy zz xy xz yz)
+        const float4 q01 = S.D.cn.q01[p], q23 = S.D.cn.q23[p], q45 = S.D.cn.q45[p];
+        const float2 qxx = make_float2(q01.x, q01.y), qyy = make_float2(q01.z, q01.w);
+        const float2 qzz = make_float2(q23.x, q23.y), qxy = make_float2(q23.z, q23.w);
+        const float2 qxz = make_float2(q45.x, q45.y), qyz = make_float2(q45.z, q45.w);
+        const float2 w2x = p_fma(qxx, n3x, p_fma(qxy, n3y, p_mul(qxz, n3z)));
+        const float2 w2y = p_fma(qyy, n3y, p_fma(qxy, n3x, p_mul(qyz, n3z)));
+        const float2 w2z = p_fma(qzz, n3z, p_fma(qxz, n3x, p_mul(qyz, n3y)));
+        const float2 p2 = p_fma(w2z, nz, p_fma(w2y, ny, p_mul(w2x, nx)));
+        // W3 = -15/2 O:nn (O: xxx xyy xxy yyy xxz yyz xyz xzz yzz zzz)
+        const float2 xx = p_mul(nx, nx), yy = p_mul(ny, ny), zz = p_mul(nz, nz);
+        const float2 n2x = p_add(nx, nx), n2y = p_add(ny, ny);
+        const float2 xy2 = p_mul(n2x, ny), xz2 = p_mul(n2x, nz), yz2 = p_mul(n2y, nz);
+#define OHR(k) oh[(k) * RS + p]
+        const float2 w3x = p_fma(OHR(0), xx, p_fma(OHR(2), xy2, p_fma(OHR(4), xz2,
+                           p_fma(OHR(1), yy, p_fma(OHR(6), yz2, p_mul(OHR(7), zz))))));
+        const float2 w3y = p_fma(OHR(2), xx, p_fma(OHR(1), xy2, p_fma(OHR(6), xz2,
+                           p_fma(OHR(3), yy, p_fma(OHR(5), yz2, p_mul(OHR(8), zz))))));
+        const float2 w3z = p_fma(OHR(4), xx, p_fma(OHR(6), xy2, p_fma(OHR(7), xz2,
+                           p_fma(OHR(5), yy, p_fma(OHR(8), yz2, p_mul(OHR(9), zz))))));
+        const float2 p3 = p_fma(w3z, nz, p_fma(w3y, ny, p_mul(w3x, nx)));
+        const float2 c3p = p_mul(cm73, p3);
+        float2 fx = p_fma(c3p, nx, w3x), fy = p_fma(c3p, ny, w3y), fz = p_fma(c3p, nz, w3z);
+        float2 pin = p_mul(c13, p3);
+        if constexpr (HEX) {
+            // W4 = 35/2 H:nnn (H: xxxx xyyy xxxy yyyy xxxz yyyz xxyy xxyz xyyz
+            // xxzz xyzz xzzz yyzz yzzz zzzz, rows 10..24)
+            const float2 mxxx = p_mul(xx, nx), myyy = p_mul(yy, ny), mzzz = p_mul(zz, nz);
+            const float2 mxxy = p_mul(xx, n3y), mxxz = p_mul(xx, n3z), mxyy = p_mul(yy, n3x);
+            const float2 myyz = p_mul(yy, n3z), mxzz = p_mul(zz, n3x), myzz = p_mul(zz, n3y);
+            const float2 mxyz = p_mul(xy2, n3z);
+#define HR(k) OHR(10 + (k))
+            const float2 w4x = p_fma(HR(0), mxxx, p_fma(HR(2), mxxy, p_fma(HR(4), mxxz, p_fma(HR(6), mxyy,
+                               p_fma(HR(7), mxyz, p_fma(HR(9), mxzz, p_fma(HR(1), myyy, p_fma(HR(8), myyz,
+                               p_fma(HR(10), myzz, p_mul(HR(11), mzzz))))))))));
+            const float2 w4y = p_fma(HR(2), mxxx, p_fma(HR(6), mxxy, p_fma(HR(7), mxxz, p_fma(HR(1), mxyy,
+                               p_fma(HR(8), mxyz, p_fma(HR(10), mxzz, p_fma(HR(3), myyy, p_fma(HR(5), myyz,
+                               p_fma(HR(12), myzz, p_mul(HR(13), mzzz))))))))));
+            const float2 w4z = p_fma(HR(4), mxxx, p_fma(HR(7), mxxy, p_fma(HR(9), mxxz, p_fma(HR(8), mxyy,
+                               p_fma(HR(10), mxyz, p_fma(HR(11), mxzz, p_fma(HR(5), myyy, p_fma(HR(12), myyz,
+                               p_fma(HR(13), myzz, p_mul(HR(14), mzzz))))))))));
+#undef HR
+            const float2 p4 = p_fma(w4z, nz, p_fma(w4y, ny, p_mul(w4x, nx)));
+            const float2 c4p = p_mul(cm94, p4);
+            fx = p_fma(ir, p_fma(c4p, nx, w4x), fx);
+            fy = p_fma(ir, p_fma(c4p, ny, w4y), fy);
+            fz = p_fma(ir, p_fma(c4p, nz, w4z), fz);
+            pin = p_fma(p_mul(c14, ir), p4, pin);
+        }
+#undef OHR
+        const float2 c2p = p_mul(cm52, p2);
+        const float2 ex = p_fma(ir, fx, p_fma(c2p, nx, w2x));
+        const float2 ey = p_fma(ir, fy, p_fma(c2p, ny, w2y));
+        const float2 ez = p_fma(ir, fz, p_fma(c2p, nz, w2z));
+        const float2 ir4 = p_mul(ir2, ir2);
+        ux = p_fma(ir4, ex, ux);
+        uy = p_fma(ir4, ey, uy);
+        uz = p_fma(ir4, ez, uz);
+        const float2 mir2 = p_mul(m, ir2);
+        tx = p_fma(mir2, nx, tx);
+        ty = p_fma(mir2, ny, ty);
+        tz = p_fma(mir2, nz, tz);
+        const float2 ir3 = p_mul(ir2, ir);
+        tp = p_fma(ir3, p_fma(ir, pin, p_mul(ch, p2)), p_fma(m, ir, tp));
+        const float2 idt2 = p_mul(p_add(M, m), ir3);
+        dt = fmaxf(dt, fmaxf(idt2.x, idt2.y));
+    }
+    A.dt = dt;
+    kahan_add2(A.s[0], A.c[0], p_sub(tx, ux));
+    kahan_add2(A.s[1], A.c[1], p_sub(ty, uy));
+    kahan_add2(A.s[2], A.c[2], p_sub(tz, uz));
+    kahan_add2(A.s[3], A.c[3], make_float2(-tp.x, -tp.y));
 }
 
 // FP32 Newtonian cell tile for particle i, two cells per packed
@@ -732,14 +833,17 @@ __device__ __forceinline__ void newt_tile_f32(Smem &S, int cnt, int i, int slot,
     kahan_add2(A.s[3], A.c[3], make_float2(-tp.x, -tp.y));
 }
 
-// Newtonian cells, QEVAL at order <= 2 (qeval.h:53-64), for the particle
-// i: acceleration, potential, and (m_i + m) / r^3 for the timestep.  FP32
+// Newtonian cells, QEVAL (qeval.h:21-64), for the particle i:
+// acceleration, potential, and (m_i + m) / r^3 for the timestep.  FP32
 // evaluates two cells per packed instruction into tile partials that are
-// folded into the compensated sums once per tile.
+// folded into the compensated sums once per tile, at every order.
 template <typename Real, int NBT, bool HIGH, class Smem>
 __device__ __forceinline__ void eval_newt(Smem &S, int cnt, int i, int slot, int iOrder,
                                           Acc<Real> &A) {
-    if constexpr (HIGH) {
+    if constexpr (HIGH && sizeof(Real) == 4) {
+        if (iOrder >= 4) newt_tile_f32_high<NBT, true>(S, cnt, i, slot, A);
+        else newt_tile_f32_high<NBT, false>(S, cnt, i, slot, A);
+    } else if constexpr (HIGH) {
         eval_newt_high<Real, NBT, HIGH>(S, cnt, i, slot, iOrder, A);
     } else if constexpr (sizeof(Real) == 4) {
         if (iOrder >= 2) newt_tile_f32<NBT, true>(S, cnt, i, slot, A);
