@@ -442,20 +442,33 @@ __global__ void __launch_bounds__(128) k_ewald(TsphDevParts P, TsphDevCounters *
             kadd(fPot, cpot, tp);
         }
         if (sizeof(Real) == 4 && cE.hMax <= 3) {
-            // FP32: e^{i h.x} of every k-space vector from the three phase
-            // factors e^{i 2 pi x/L}, e^{i 2 pi y/L}, e^{i 2 pi z/L} by complex
-            // products, in the table's order (hx, hy, hz ascending) -- three
-            // sincos per particle instead of one per vector
+            // FP32: e^{i h.x} of every kept k-space vector from the three
+            // phase factors e^{i 2 pi x/L}, e^{i 2 pi y/L}, e^{i 2 pi z/L} by
+            // complex products, in the table's order (hx, hy, hz ascending) --
+            // three sincos per particle instead of one per vector.  The z
+            // factors e^{i k 2 pi z/L}, |k| <= 3, are tabulated; a row (hx, hy)
+            // outside the cut is skipped and a row inside it visits only its
+            // kept hz.
             const float tp = (float)(2.0 * M_PI / cE.L);
             float c1[3], s1[3];
             sincosf(tp * (float)dx, &s1[0], &c1[0]);
             sincosf(tp * (float)dy, &s1[1], &c1[1]);
             sincosf(tp * (float)dz, &s1[2], &c1[2]);
             const int R = cE.hMax;
-            // e^{-i R theta} per axis
-            float cs0[3], sn0[3];
+            float czt[7], szt[7];   // e^{i k theta_z} at index k + 3
+            czt[3] = 1.0f;
+            szt[3] = 0.0f;
 #pragma unroll
-            for (int a = 0; a < 3; ++a) {
+            for (int k = 1; k <= 3; ++k) {
+                czt[3 + k] = czt[2 + k] * c1[2] - szt[2 + k] * s1[2];
+                szt[3 + k] = czt[2 + k] * s1[2] + szt[2 + k] * c1[2];
+                czt[3 - k] = czt[3 + k];
+                szt[3 - k] = -szt[3 + k];
+            }
+            // e^{-i R theta} for x and y
+            float cs0[2], sn0[2];
+#pragma unroll
+            for (int a = 0; a < 2; ++a) {
                 float c = 1.0f, s = 0.0f;
                 for (int k = 0; k < R; ++k) {
                     const float t = c * c1[a] + s * s1[a];   // times e^{-i theta}
@@ -471,23 +484,23 @@ __global__ void __launch_bounds__(128) k_ewald(TsphDevParts P, TsphDevCounters *
             for (int ix = -R; ix <= R; ++ix) {
                 float cy = cs0[1], sy = sn0[1];
                 for (int iy = -R; iy <= R; ++iy) {
-                    const float cxy = cx * cy - sx * sy, sxy = cx * sy + sx * cy;
-                    float cz = cs0[2], sz = sn0[2];
-                    for (int iz = -R; iz <= R; ++iz) {
-                        const int h2 = ix * ix + iy * iy + iz * iz;
-                        if (h2 != 0 && h2 <= cut2) {
-                            const float c = cxy * cz - sxy * sz, s = cxy * sz + sxy * cz;
-                            const float hC = cE.hCf[i], hS = cE.hSf[i];
-                            kadd(fPot, cpot, (Real)(hC * c + hS * s));
-                            const float t = hC * s - hS * c;
-                            kadd(ax, cax, (Real)(cE.hxf[i] * t));
-                            kadd(ay, cay, (Real)(cE.hyf[i] * t));
-                            kadd(az, caz, (Real)(cE.hzf[i] * t));
-                            ++i;
+                    const int rem = cut2 - ix * ix - iy * iy;
+                    if (rem >= 0) {
+                        const float cxy = cx * cy - sx * sy, sxy = cx * sy + sx * cy;
+#pragma unroll
+                        for (int iz = -3; iz <= 3; ++iz) {
+                            if (iz >= -R && iz <= R && iz * iz <= rem && (ix | iy | iz) != 0) {
+                                const float c = cxy * czt[3 + iz] - sxy * szt[3 + iz];
+                                const float s = cxy * szt[3 + iz] + sxy * czt[3 + iz];
+                                const float hC = cE.hCf[i], hS = cE.hSf[i];
+                                kadd(fPot, cpot, (Real)(hC * c + hS * s));
+                                const float t = hC * s - hS * c;
+                                kadd(ax, cax, (Real)(cE.hxf[i] * t));
+                                kadd(ay, cay, (Real)(cE.hyf[i] * t));
+                                kadd(az, caz, (Real)(cE.hzf[i] * t));
+                                ++i;
+                            }
                         }
-                        const float t = cz * c1[2] - sz * s1[2];
-                        sz = cz * s1[2] + sz * c1[2];
-                        cz = t;
                     }
                     const float t = cy * c1[1] - sy * s1[1];
                     sy = cy * s1[1] + sy * c1[1];
