@@ -46,6 +46,10 @@ struct EwConst {
     float momf[35];
     double L, alpha, alpha2, k1, ka, fEwCut2, smallR2;
     float fEwCut2f;      // the FP32 kernel's real-space cut (see EW_XCUT_F32)
+    // FP32 copies of L, alpha, alpha^2, ka, fEwCut2, smallR2, 2 pi / L and
+    // the potential's constant term m k1, converted once here rather than
+    // by every thread of the FP32 kernel
+    float fL, fAlpha, fAlpha2, fKa, fCut2, fSmallR2, fTwoPiL, fPot0;
     int nEwReps, nReps, nEwh, iOrder;
     int hMax;            // largest |component| of a k-space vector
     int hCut2;           // floor(fEwhCut^2): the integer |h|^2 kept (ewald.c:205-211)
@@ -398,12 +402,16 @@ __global__ void __launch_bounds__(128) k_ewald(TsphDevParts P, TsphDevCounters *
     if (p < P.n && P.act[p]) {   // active particles only (pkdBucketEwald, ewald.c:53)
         MomR<Real> mom;
         load_mom<Real>(mom);
-        const Real L = (Real)cE.L;
-        const Real alpha2 = (Real)cE.alpha2, alpha = (Real)cE.alpha, ka = (Real)cE.ka;
-        const Real fEwCut2 = (Real)cE.fEwCut2, smallR2 = (Real)cE.smallR2;
-        const Real evalCut2 = sizeof(Real) == 4 ? (Real)cE.fEwCut2f : fEwCut2;
+        constexpr bool F32 = sizeof(Real) == 4;
+        const Real L = F32 ? (Real)cE.fL : (Real)cE.L;
+        const Real alpha2 = F32 ? (Real)cE.fAlpha2 : (Real)cE.alpha2;
+        const Real alpha = F32 ? (Real)cE.fAlpha : (Real)cE.alpha;
+        const Real ka = F32 ? (Real)cE.fKa : (Real)cE.ka;
+        const Real fEwCut2 = F32 ? (Real)cE.fCut2 : (Real)cE.fEwCut2;
+        const Real smallR2 = F32 ? (Real)cE.fSmallR2 : (Real)cE.smallR2;
+        const Real evalCut2 = F32 ? (Real)cE.fEwCut2f : fEwCut2;
         const int iOrder = cE.iOrder;
-        Real fPot = (Real)(cE.mom.m * cE.k1), ax = 0, ay = 0, az = 0;
+        Real fPot = F32 ? (Real)cE.fPot0 : (Real)(cE.mom.m * cE.k1), ax = 0, ay = 0, az = 0;
         Real cpot = 0, cax = 0, cay = 0, caz = 0;   // compensations (FP32 only)
         Real dx = (Real)(P.x[p] - cE.mom.x);
         Real dy = (Real)(P.y[p] - cE.mom.y);
@@ -449,7 +457,7 @@ __global__ void __launch_bounds__(128) k_ewald(TsphDevParts P, TsphDevCounters *
             // factors e^{i k 2 pi z/L}, |k| <= 3, are tabulated; a row (hx, hy)
             // outside the cut is skipped and a row inside it visits only its
             // kept hz.
-            const float tp = (float)(2.0 * M_PI / cE.L);
+            const float tp = cE.fTwoPiL;
             float c1[3], s1[3];
             sincosf(tp * (float)dx, &s1[0], &c1[0]);
             sincosf(tp * (float)dy, &s1[1], &c1[1]);
@@ -681,6 +689,14 @@ __global__ void __launch_bounds__(EWC_BS) k_ewald_const(EwParams p, const double
         const double xc = EW_XCUT_F32 / E.alpha;
         E.fEwCut2f = (float)(xc * xc < E.fEwCut2 ? xc * xc : E.fEwCut2);
         E.smallR2 = 3.0e-3 * L * L;
+        E.fL = (float)E.L;
+        E.fAlpha = (float)E.alpha;
+        E.fAlpha2 = (float)E.alpha2;
+        E.fKa = (float)E.ka;
+        E.fCut2 = (float)E.fEwCut2;
+        E.fSmallR2 = (float)E.smallR2;
+        E.fTwoPiL = (float)(2.0 * M_PI / E.L);
+        E.fPot0 = (float)(M.m * E.k1);
         E.nReps = p.nReps;
         E.nEwReps = p.nEwReps;
         E.iOrder = p.iOrder;
