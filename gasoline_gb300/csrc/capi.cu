@@ -477,7 +477,7 @@ extern "C" int tsph_grav_all(tsph_ctx *ctx, const tsph_grav_params *gp, tsph_gra
         ctx->coordScale = ctx->capLimit > 0 ? ctx->capLimit : r;
     }
     if (!cap) cudaEventRecord(ctx->ev[1], ctx->stream);
-    rc = tsph_tree_moments(ctx, ctx->P, ctx->T, n, gp->dTheta, gp->iOrder);
+    rc = tsph_tree_moments(ctx, ctx->P, ctx->T, n, gp->dTheta, gp->iOrder, gp->precision == TSPH_FP32);
     if (rc) return rc;
     const bool ewald = n > 0 && gp->bPeriodic && gp->bEwald && gp->iEwOrder >= 1;
     // from the moments' completion a second stream prepares the walk's

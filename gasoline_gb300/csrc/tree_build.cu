@@ -1263,10 +1263,11 @@ __host__ __device__ constexpr int m3_index(int a, int b, int c) {
 // (xxxx xyyy xxxy yyyy xxxz yyyz xxyy xxyz xyyz xxzz xyzz xzzz yyzz yzzz
 // zzzz): fused multiply-adds on shared products, 37 FP64 operations (they
 // are checked to rounding, as the parents' binomial shifts are).
-__device__ __forceinline__ void leaf_high(const double *d, double m, double *m3, double *m4) {
-    const double x = d[0], y = d[1], z = d[2];
-    const double xx = x * x, yy = y * y, zz = z * z, xy = x * y, xz = x * z, yz = y * z;
-    const double mx = m * x, my = m * y, mz = m * z;
+template <typename R>
+__device__ __forceinline__ void leaf_high(const R *d, R m, R *m3, R *m4) {
+    const R x = d[0], y = d[1], z = d[2];
+    const R xx = x * x, yy = y * y, zz = z * z, xy = x * y, xz = x * z, yz = y * z;
+    const R mx = m * x, my = m * y, mz = m * z;
     m3[0] = fma(mx, xx, m3[0]);
     m3[1] = fma(mx, yy, m3[1]);
     m3[2] = fma(my, xx, m3[2]);
@@ -1277,7 +1278,7 @@ __device__ __forceinline__ void leaf_high(const double *d, double m, double *m3,
     m3[7] = fma(mx, zz, m3[7]);
     m3[8] = fma(my, zz, m3[8]);
     m3[9] = fma(mz, zz, m3[9]);
-    const double mxx = m * xx, myy = m * yy, mzz = m * zz;
+    const R mxx = m * xx, myy = m * yy, mzz = m * zz;
     m4[0] = fma(mxx, xx, m4[0]);
     m4[1] = fma(myy, xy, m4[1]);
     m4[2] = fma(mxx, xy, m4[2]);
@@ -1297,8 +1298,9 @@ __device__ __forceinline__ void leaf_high(const double *d, double m, double *m3,
 
 // Child moments (mass m, complete Q, M3, M4 about its own centre) shifted
 // by d = child centre - parent centre, added into the parent's M3, M4.
-__device__ __forceinline__ void shift_high(const double *d, double m, const double *q, const double *c3,
-                                           const double *c4, double *m3, double *m4) {
+template <typename R>
+__device__ __forceinline__ void shift_high(const R *d, R m, const R *q, const R *c3, const R *c4, R *m3,
+                                           R *m4) {
     constexpr unsigned char I3[10][3] = {{0, 0, 0}, {0, 1, 1}, {0, 0, 1}, {1, 1, 1}, {0, 0, 2},
                                          {1, 1, 2}, {0, 1, 2}, {0, 2, 2}, {1, 2, 2}, {2, 2, 2}};
     constexpr unsigned char I4[15][4] = {{0, 0, 0, 0}, {0, 1, 1, 1}, {0, 0, 0, 1}, {1, 1, 1, 1},
@@ -1321,6 +1323,62 @@ __device__ __forceinline__ void shift_high(const double *d, double m, const doub
                  q[q_index(a, c)] * d[b] * d[e] + q[q_index(a, b)] * d[c] * d[e] +
                  m * d[a] * d[b] * d[c] * d[e];
     }
+}
+
+// A parent's complete M3, M4 from its children's (cc), shifted to its
+// centre r, in R: FP64 (M3, M4 as allocated) for the FP64 walk, FP32 for
+// the FP32 walk, whose cells only use FP32 copies of the reduced moments
+// (the arrays then hold FP32 moments in their first half).  The child
+// offsets are FP64 differences of the FP64 centres.
+template <typename R>
+__device__ __forceinline__ void combine_high(const TsphDevTree &T, int i, const double *r, const int *cc,
+                                             R *M3, R *M4) {
+    R m3[10], m4[15];
+#pragma unroll
+    for (int k = 0; k < 10; ++k) m3[k] = R(0);
+#pragma unroll
+    for (int k = 0; k < 15; ++k) m4[k] = R(0);
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+        const int ch = cc[s];
+        const R mc = (R)__ldcg(&T.fMass[ch]);
+        const R d[3] = {(R)(__ldcg(&T.r[3 * ch]) - r[0]), (R)(__ldcg(&T.r[3 * ch + 1]) - r[1]),
+                        (R)(__ldcg(&T.r[3 * ch + 2]) - r[2])};
+        R qc[6], c3[10], c4[15];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) qc[k] = (R)__ldcg(&T.Q[6 * ch + k]);
+#pragma unroll
+        for (int k = 0; k < 10; ++k) c3[k] = __ldcg(&M3[10 * (size_t)ch + k]);
+#pragma unroll
+        for (int k = 0; k < 15; ++k) c4[k] = __ldcg(&M4[15 * (size_t)ch + k]);
+        shift_high<R>(d, mc, qc, c3, c4, m3, m4);
+    }
+#pragma unroll
+    for (int k = 0; k < 10; ++k) M3[10 * (size_t)i + k] = m3[k];
+#pragma unroll
+    for (int k = 0; k < 15; ++k) M4[15 * (size_t)i + k] = m4[k];
+}
+
+// A leaf's complete M3, M4 about its centre (r0, r1, r2) from its
+// particles [lo, hi], in R as combine_high.
+template <typename R>
+__device__ __forceinline__ void leaf_moments_high(int i, int lo, int hi, const double *__restrict__ x,
+                                                  const double *__restrict__ y, const double *__restrict__ z,
+                                                  const double *__restrict__ m, double r0, double r1,
+                                                  double r2, R *M3, R *M4) {
+    R m3[10], m4[15];
+#pragma unroll
+    for (int k = 0; k < 10; ++k) m3[k] = R(0);
+#pragma unroll
+    for (int k = 0; k < 15; ++k) m4[k] = R(0);
+    for (int p = lo; p <= hi; ++p) {
+        const R d[3] = {(R)xsub(x[p], r0), (R)xsub(y[p], r1), (R)xsub(z[p], r2)};
+        leaf_high<R>(d, (R)m[p], m3, m4);
+    }
+#pragma unroll
+    for (int k = 0; k < 10; ++k) M3[10 * (size_t)i + k] = m3[k];
+#pragma unroll
+    for (int k = 0; k < 15; ++k) M4[15 * (size_t)i + k] = m4[k];
 }
 
 __device__ void combine_node(TsphDevTree &T, int i, int high) {
@@ -1363,32 +1421,10 @@ __device__ void combine_node(TsphDevTree &T, int i, int high) {
         q[4] += mc * dx * dz;
         q[5] += mc * dy * dz;
     }
-    if (high) {   // complete M3, M4 from the children's, before q is final
-        double m3[10], m4[15];
-#pragma unroll
-        for (int k = 0; k < 10; ++k) m3[k] = 0.0;
-#pragma unroll
-        for (int k = 0; k < 15; ++k) m4[k] = 0.0;
-#pragma unroll
-        for (int s = 0; s < 2; ++s) {
-            const int ch = cc[s];
-            const double mc = __ldcg(&T.fMass[ch]);
-            const double d[3] = {__ldcg(&T.r[3 * ch]) - r[0], __ldcg(&T.r[3 * ch + 1]) - r[1],
-                                 __ldcg(&T.r[3 * ch + 2]) - r[2]};
-            double qc[6], c3[10], c4[15];
-#pragma unroll
-            for (int k = 0; k < 6; ++k) qc[k] = __ldcg(&T.Q[6 * ch + k]);
-#pragma unroll
-            for (int k = 0; k < 10; ++k) c3[k] = __ldcg(&T.M3[10 * (size_t)ch + k]);
-#pragma unroll
-            for (int k = 0; k < 15; ++k) c4[k] = __ldcg(&T.M4[15 * (size_t)ch + k]);
-            shift_high(d, mc, qc, c3, c4, m3, m4);
-        }
-#pragma unroll
-        for (int k = 0; k < 10; ++k) T.M3[10 * (size_t)i + k] = m3[k];
-#pragma unroll
-        for (int k = 0; k < 15; ++k) T.M4[15 * (size_t)i + k] = m4[k];
-    }
+    // complete M3, M4 from the children's, before q is final
+    if (high == 1) combine_high<double>(T, i, r, cc, T.M3, T.M4);
+    else if (high == 2) combine_high<float>(T, i, r, cc, reinterpret_cast<float *>(T.M3),
+                                            reinterpret_cast<float *>(T.M4));
 #pragma unroll
     for (int k = 0; k < 6; ++k) T.Q[6 * i + k] = q[k];
 }
@@ -1445,21 +1481,11 @@ __global__ void k_moments(TsphDevTree T, const double *__restrict__ x, const dou
     }
 #pragma unroll
     for (int k = 0; k < 6; ++k) T.Q[6 * i + k] = q[k];
-    if (high) {
-        double m3[10], m4[15];
-#pragma unroll
-        for (int k = 0; k < 10; ++k) m3[k] = 0.0;
-#pragma unroll
-        for (int k = 0; k < 15; ++k) m4[k] = 0.0;
-        for (int p = lo; p <= hi; ++p) {
-            const double d[3] = {xsub(x[p], r0), xsub(y[p], r1), xsub(z[p], r2)};
-            leaf_high(d, m[p], m3, m4);
-        }
-#pragma unroll
-        for (int k = 0; k < 10; ++k) T.M3[10 * (size_t)i + k] = m3[k];
-#pragma unroll
-        for (int k = 0; k < 15; ++k) T.M4[15 * (size_t)i + k] = m4[k];
-    }
+    if (high == 1)
+        leaf_moments_high<double>(i, lo, hi, x, y, z, m, r0, r1, r2, T.M3, T.M4);
+    else if (high == 2)
+        leaf_moments_high<float>(i, lo, hi, x, y, z, m, r0, r1, r2, reinterpret_cast<float *>(T.M3),
+                                 reinterpret_cast<float *>(T.M4));
     for (;;) {
         __threadfence();
         int par = T.parent[i];
@@ -1553,36 +1579,37 @@ __global__ void k_bmax_exact(int n, TsphDevTree T, const double *__restrict__ x,
 // complete moments: sum m (d_a d_b d_c - 0.2 d^2 (...)) etc. are linear in
 // the complete moments, with sum m d^2 d_a = T_a and sum m d^2 d_a d_b =
 // S_ab, sum m d^4 = S_xx + S_yy + S_zz.
-__device__ __forceinline__ void reduce_high(const double *M, const double *H4, double *o, double *h) {
-    const double Tx = M[0] + M[1] + M[7], Ty = M[2] + M[3] + M[8], Tz = M[4] + M[5] + M[9];
-    o[0] = M[0] - 0.6 * Tx;   // xxx
-    o[1] = M[1] - 0.2 * Tx;   // xyy
-    o[2] = M[2] - 0.2 * Ty;   // xxy
-    o[3] = M[3] - 0.6 * Ty;   // yyy
-    o[4] = M[4] - 0.2 * Tz;   // xxz
-    o[5] = M[5] - 0.2 * Tz;   // yyz
+template <typename R>
+__device__ __forceinline__ void reduce_high(const R *M, const R *H4, R *o, R *h) {
+    const R Tx = M[0] + M[1] + M[7], Ty = M[2] + M[3] + M[8], Tz = M[4] + M[5] + M[9];
+    o[0] = M[0] - R(0.6) * Tx;   // xxx
+    o[1] = M[1] - R(0.2) * Tx;   // xyy
+    o[2] = M[2] - R(0.2) * Ty;   // xxy
+    o[3] = M[3] - R(0.6) * Ty;   // yyy
+    o[4] = M[4] - R(0.2) * Tz;   // xxz
+    o[5] = M[5] - R(0.2) * Tz;   // yyz
     o[6] = M[6];              // xyz
-    o[7] = M[7] - 0.2 * Tx;   // xzz
-    o[8] = M[8] - 0.2 * Ty;   // yzz
-    o[9] = M[9] - 0.6 * Tz;   // zzz
-    const double Sxx = H4[0] + H4[6] + H4[9], Syy = H4[6] + H4[3] + H4[12], Szz = H4[9] + H4[12] + H4[14];
-    const double Sxy = H4[2] + H4[1] + H4[10], Sxz = H4[4] + H4[8] + H4[11], Syz = H4[7] + H4[5] + H4[13];
-    const double S4 = Sxx + Syy + Szz;
-    h[0] = H4[0] - 6.0 / 7.0 * Sxx + 0.6 / 7.0 * S4;            // xxxx
-    h[1] = H4[1] - 3.0 / 7.0 * Sxy;                             // xyyy
-    h[2] = H4[2] - 3.0 / 7.0 * Sxy;                             // xxxy
-    h[3] = H4[3] - 6.0 / 7.0 * Syy + 0.6 / 7.0 * S4;            // yyyy
-    h[4] = H4[4] - 3.0 / 7.0 * Sxz;                             // xxxz
-    h[5] = H4[5] - 3.0 / 7.0 * Syz;                             // yyyz
-    h[6] = H4[6] - 1.0 / 7.0 * (Sxx + Syy) + 0.2 / 7.0 * S4;    // xxyy
-    h[7] = H4[7] - 1.0 / 7.0 * Syz;                             // xxyz
-    h[8] = H4[8] - 1.0 / 7.0 * Sxz;                             // xyyz
-    h[9] = H4[9] - 1.0 / 7.0 * (Sxx + Szz) + 0.2 / 7.0 * S4;    // xxzz
-    h[10] = H4[10] - 1.0 / 7.0 * Sxy;                           // xyzz
-    h[11] = H4[11] - 3.0 / 7.0 * Sxz;                           // xzzz
-    h[12] = H4[12] - 1.0 / 7.0 * (Syy + Szz) + 0.2 / 7.0 * S4;  // yyzz
-    h[13] = H4[13] - 3.0 / 7.0 * Syz;                           // yzzz
-    h[14] = H4[14] - 6.0 / 7.0 * Szz + 0.6 / 7.0 * S4;          // zzzz
+    o[7] = M[7] - R(0.2) * Tx;   // xzz
+    o[8] = M[8] - R(0.2) * Ty;   // yzz
+    o[9] = M[9] - R(0.6) * Tz;   // zzz
+    const R Sxx = H4[0] + H4[6] + H4[9], Syy = H4[6] + H4[3] + H4[12], Szz = H4[9] + H4[12] + H4[14];
+    const R Sxy = H4[2] + H4[1] + H4[10], Sxz = H4[4] + H4[8] + H4[11], Syz = H4[7] + H4[5] + H4[13];
+    const R S4 = Sxx + Syy + Szz;
+    h[0] = H4[0] - R(6.0 / 7.0) * Sxx + R(0.6 / 7.0) * S4;            // xxxx
+    h[1] = H4[1] - R(3.0 / 7.0) * Sxy;                             // xyyy
+    h[2] = H4[2] - R(3.0 / 7.0) * Sxy;                             // xxxy
+    h[3] = H4[3] - R(6.0 / 7.0) * Syy + R(0.6 / 7.0) * S4;            // yyyy
+    h[4] = H4[4] - R(3.0 / 7.0) * Sxz;                             // xxxz
+    h[5] = H4[5] - R(3.0 / 7.0) * Syz;                             // yyyz
+    h[6] = H4[6] - R(1.0 / 7.0) * (Sxx + Syy) + R(0.2 / 7.0) * S4;    // xxyy
+    h[7] = H4[7] - R(1.0 / 7.0) * Syz;                             // xxyz
+    h[8] = H4[8] - R(1.0 / 7.0) * Sxz;                             // xyyz
+    h[9] = H4[9] - R(1.0 / 7.0) * (Sxx + Szz) + R(0.2 / 7.0) * S4;    // xxzz
+    h[10] = H4[10] - R(1.0 / 7.0) * Sxy;                           // xyzz
+    h[11] = H4[11] - R(3.0 / 7.0) * Sxz;                           // xzzz
+    h[12] = H4[12] - R(1.0 / 7.0) * (Syy + Szz) + R(0.2 / 7.0) * S4;  // yyzz
+    h[13] = H4[13] - R(3.0 / 7.0) * Syz;                           // yzzz
+    h[14] = H4[14] - R(6.0 / 7.0) * Szz + R(0.6 / 7.0) * S4;          // zzzz
 }
 
 __global__ void k_open(TsphDevTree T, const unsigned long long *__restrict__ maxd2,
@@ -1606,13 +1633,25 @@ __global__ void k_open(TsphDevTree T, const unsigned long long *__restrict__ max
     const double *q = &T.Q[6 * i];
     T.wmom0[i] = make_float4((float)T.fMass[i], (float)q[0], (float)q[1], (float)q[2]);
     T.wmom1[i] = make_float4((float)q[3], (float)q[4], (float)q[5], (float)T.fSoft[i]);
-    if (high) {
+    if (high == 2) {   // FP32 moments: the FP32 copies only
+        const float *M3f = reinterpret_cast<const float *>(T.M3);
+        const float *M4f = reinterpret_cast<const float *>(T.M4);
+        float M[10], H4[15], oh[25];
+#pragma unroll
+        for (int k = 0; k < 10; ++k) M[k] = M3f[10 * (size_t)i + k];
+#pragma unroll
+        for (int k = 0; k < 15; ++k) H4[k] = M4f[15 * (size_t)i + k];
+        reduce_high<float>(M, H4, oh, oh + 10);
+        const bool empty = T.pUpper[i] < T.pLower[i];
+#pragma unroll
+        for (int k = 0; k < 25; ++k) T.wOH[25 * (size_t)i + k] = empty ? 0.0f : oh[k];
+    } else if (high) {
         double M[10], H4[15], oh[25];
 #pragma unroll
         for (int k = 0; k < 10; ++k) M[k] = T.M3[10 * (size_t)i + k];
 #pragma unroll
         for (int k = 0; k < 15; ++k) H4[k] = T.M4[15 * (size_t)i + k];
-        reduce_high(M, H4, oh, oh + 10);
+        reduce_high<double>(M, H4, oh, oh + 10);
         if (T.pUpper[i] < T.pLower[i])
             for (int k = 0; k < 25; ++k) oh[k] = 0.0;
 #pragma unroll
@@ -2115,12 +2154,15 @@ static int build_tree_body(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n
     return TSPH_OK;
 }
 
-int tsph_tree_moments(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, double dTheta, int order) {
+int tsph_tree_moments(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, double dTheta, int order,
+                      int fp32) {
     TsphBuildBufs &B = ctx->B;
     const int BS = 256;
     if (n == 0) return TSPH_OK;
     const int nodeNeed = 2 * n;
-    const int high = order >= 3;
+    // octopole/hexadecapole moments: FP64 for the FP64 walk (1), FP32 for
+    // the FP32 walk (2), whose cells read FP32 copies of them only
+    const int high = order >= 3 ? (fp32 ? 2 : 1) : 0;
     if (high && T.highCap < T.cap) {   // octopole/hexadecapole storage, on first use
         if (ctx->capturing) return TSPH_ERR_STATE;
         int rc = tsph_grow(ctx, &T.M3, (size_t)10 * T.cap);

@@ -249,7 +249,7 @@ int tsph_scan_inclusive(tsph_ctx *ctx, const int *in, int *out, int n);
 int tsph_build_tree(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, int nBucket);
 int tsph_set_ranges(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, int nR, const int *counts);
 int tsph_tree_moments(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, double dTheta,
-                      int order);
+                      int order, int fp32);
 void tsph_free_build(TsphBuildBufs &B);
 int tsph_apply_gas_systems(tsph_ctx *ctx);
 int tsph_load_begin(tsph_ctx *ctx, int n);
