@@ -1431,15 +1431,13 @@ __device__ void combine_node(TsphDevTree &T, int i, int high) {
 
 // Leaf mass, softening and centre of mass summed in tree order exactly as
 // BuildBinary (pkd.c:2559-2574); quadrupole summed as pkdCalcCell
-// (pkd.c:2094-2130).  Then the thread climbs: at each parent the second
+// (pkd.c:2094-2130).  k_moments then climbs: at each parent the second
 // child to finish (counted by an atomic) combines it, so every interior
 // node is formed once, after both children, with no per-level launches.
-__global__ void k_moments(TsphDevTree T, const double *__restrict__ x, const double *__restrict__ y,
-                          const double *__restrict__ z, const double *__restrict__ m,
-                          const double *__restrict__ h, int *visit, int high) {
-    int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= T.dcnt[1]) return;
-    int i = T.leaves[b];
+__device__ __forceinline__ void leaf_node(TsphDevTree &T, int i, const double *__restrict__ x,
+                                          const double *__restrict__ y, const double *__restrict__ z,
+                                          const double *__restrict__ m, const double *__restrict__ h,
+                                          int high) {
     int lo = T.pLower[i], hi = T.pUpper[i];
     double fMass = 0.0, fSoft = 0.0, r0 = 0.0, r1 = 0.0, r2 = 0.0;
     for (int p = lo; p <= hi; ++p) {
@@ -1486,14 +1484,60 @@ __global__ void k_moments(TsphDevTree T, const double *__restrict__ x, const dou
     else if (high == 2)
         leaf_moments_high<float>(i, lo, hi, x, y, z, m, r0, r1, r2, reinterpret_cast<float *>(T.M3),
                                  reinterpret_cast<float *>(T.M4));
+}
+
+// The arrival at i's parent once i is complete: the parent if i was its
+// second child to finish (its combination is then due), else -1.
+__device__ __forceinline__ int arrive(const TsphDevTree &T, int *visit, int i) {
+    __threadfence();
+    const int par = T.parent[i];
+    if (par < 0) return -1;
+    if (atomicAdd(&visit[par], 1) == 0) return -1;   // the sibling is not done yet
+    __threadfence();
+    return par;
+}
+
+#define MOM_BS 128
+
+__global__ void __launch_bounds__(MOM_BS) k_moments(TsphDevTree T, const double *__restrict__ x,
+                                                    const double *__restrict__ y, const double *__restrict__ z,
+                                                    const double *__restrict__ m, const double *__restrict__ h,
+                                                    int *visit, int high) {
+    __shared__ int queue[MOM_BS];
+    __shared__ int wcount[MOM_BS / 32];
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int next = -1;
+    if (b < T.dcnt[1]) {
+        const int i = T.leaves[b];
+        leaf_node(T, i, x, y, z, m, h, high);
+        next = arrive(T, visit, i);
+    }
+    // The climb: the parents that this block's threads completed are packed
+    // into the first threads of the block and combined there, level after
+    // level, so a warp's FP64 instructions serve up to 32 nodes however
+    // few of the block's threads are still climbing.
     for (;;) {
-        __threadfence();
-        int par = T.parent[i];
-        if (par < 0) break;
-        if (atomicAdd(&visit[par], 1) == 0) break;   // the sibling is not done yet
-        __threadfence();
-        combine_node(T, par, high);
-        i = par;
+        const unsigned bal = __ballot_sync(0xffffffffu, next >= 0);
+        if (lane == 0) wcount[w] = __popc(bal);
+        __syncthreads();
+        int off = 0, tot = 0;
+#pragma unroll
+        for (int k = 0; k < MOM_BS / 32; ++k) {
+            const int c = wcount[k];
+            off += k < w ? c : 0;
+            tot += c;
+        }
+        if (next >= 0) queue[off + __popc(bal & ((1u << lane) - 1u))] = next;
+        __syncthreads();
+        if (tot == 0) break;
+        next = -1;
+        if ((int)threadIdx.x < tot) {
+            const int node = queue[threadIdx.x];
+            __threadfence();
+            combine_node(T, node, high);
+            next = arrive(T, visit, node);
+        }
     }
 }
 
@@ -2180,7 +2224,7 @@ int tsph_tree_moments(tsph_ctx *ctx, TsphDevParts &P, TsphDevTree &T, int n, dou
     TSPH_LAUNCH_CK("k_parts32");
     TSPH_CK(cudaEventRecord(ctx->evParts, ctx->side));
     TSPH_CK(cudaMemsetAsync(B.visit, 0, sizeof(int) * (size_t)nodeNeed, ctx->stream));
-    k_moments<<<tsph_blocks(n, 128), 128, 0, ctx->stream>>>(T, P.x, P.y, P.z, P.m, P.h, B.visit, high);
+    k_moments<<<tsph_blocks(n, MOM_BS), MOM_BS, 0, ctx->stream>>>(T, P.x, P.y, P.z, P.m, P.h, B.visit, high);
     TSPH_LAUNCH_CK("k_moments");
     TSPH_CK(cudaEventRecord(ctx->evMoments, ctx->stream));   // the root cell is final
     TSPH_CK(cudaStreamWaitEvent(ctx->stream, ctx->evParts, 0));
